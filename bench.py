@@ -1,0 +1,290 @@
+"""Benchmark of the residual-and-timestep path on GB300.
+
+Workload (the plain large configuration): steady 2D Euler flow past a cylinder
+on a 512 (radial) x 1024 (circumferential) O-grid, radius 0.5 to 20 with
+geometric radial stretching 1.01, freestream Mach 0.3; Roe flux, MUSCL with
+the van Albada limiter, least-squares gradients, ssp34 with local timestepping
+at CFL 0.5, FP64.  One step = one full RK step (4 stages) over all cells;
+the metric is cell-updates/s (cells x steps / s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) every rank advances its own replica of the workload
+(the path does not shard; replicas only) and value is the whole-job total.
+--impl reference times the reference algorithm's CPU implementation (the
+OpenMP oracle port built with the reference's flags) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s (MUSCL+Roe+RK)"
+UNIT = "cell-updates/s"
+NR, NTH, MACH = 512, 1024, 0.3
+FLUX, LIMITER, RKT, DTMODE, CFL = "roe", "vanalbada", "ssp34", "local", 0.5
+NSTAGES = 4
+# algorithmic bytes per cell per RK stage: read q_stage, read q0, write q_next
+# (3 x 4 values) + 2 geometry values, in FP64
+ALG_BYTES_PER_CELL_STAGE = (3 * 4 + 2) * 8
+L2_BYTES = 129 * 2 ** 20
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "stage_kernel_fp64_ogrid.md")
+
+
+def workload_config():
+    return {"workload": f"cylinder O-grid {NR}x{NTH}, r 0.5..20, stretch 1.01, M{MACH}",
+            "cells": NR * NTH, "flux": FLUX, "limiter": LIMITER, "gradients": "lsq", "rk": RKT,
+            "dt": DTMODE, "cfl": CFL, "precision": "fp64", "step": "one RK step (4 stages) over all cells"}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic_per_cell():
+    """dram bytes per cell per stage launch from the committed ncu summary, if any."""
+    if not os.path.exists(PROFILE_TRAFFIC):
+        return None
+    for line in open(PROFILE_TRAFFIC):
+        if line.startswith("traffic_bytes_per_cell_stage:"):
+            return float(line.split(":", 1)[1].split()[0])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"hc_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_baseline(steps_budget_s: float = 12.0, threads: int | None = None):
+    """The reference algorithm on the host cores: OpenMP oracle port built with the
+    reference's flags (-O3 -ffast-math -fopenmp), on a bounded number of steps of
+    the same workload."""
+    from hyperboliconvergence_gb300 import cases
+    from oracle import oracle_py
+    threads = threads or os.cpu_count() or 1
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    lib = oracle_py.load(fast=True)
+    lib.hco_set_threads(int(threads))
+    mesh, bc, ref, q, species = cases.cylinder(NR, NTH, mach=MACH)
+    o = oracle_py.OracleSolver(mesh.ni, mesh.nj, mesh.nodes.ravel(), bc, flux=FLUX, limiter=LIMITER, rk=RKT,
+                               dt=DTMODE, cfl=CFL, species=species, ghost_ref=ref, fast=True)
+    o.set_state(q)
+    o.step(1)  # warm-up (first touch of the arrays)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.step(1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= steps_budget_s or n >= 200:
+            break
+    v = NR * NTH * n / el
+    return {"value": v, "unit": UNIT, "cores": int(lib.hco_get_threads()), "kind": "port",
+            "sample": f"{n} RK steps of the {NR}x{NTH} O-grid workload ({el:.1f} s), OpenMP oracle port, "
+                      f"-O3 -ffast-math -fopenmp"}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    steps = max(1, args.steps)
+    cb = cpu_baseline(steps_budget_s=min(20.0, 4.0 + 2.0 * steps))
+    v = cb["value"]
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+            "warmup": args.warmup, "ms_per_step": NR * NTH / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(), "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    from hyperboliconvergence_gb300 import cases
+    from hyperboliconvergence_gb300.solver import Solver
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+    stream = torch.cuda.current_stream()
+    mesh, bc, ref, q, species = cases.cylinder(NR, NTH, mach=MACH)
+    s = Solver(mesh, bc, ref, flux=FLUX, limiter=LIMITER, rk=RKT, precision="fp64", dt=DTMODE, cfl=CFL,
+               species=species, stream=stream.cuda_stream)
+    s.set_state(q)
+    ncell = NR * NTH
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up
+    s.step_async(max(3, args.warmup))
+    s.sync()
+    barrier()
+    launches0 = s.sync().kernel_launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(stream)
+        s.step_async(args.steps)
+        ev1.record(stream)
+        barrier()
+    st = s.sync()
+    launches = st.kernel_launches - launches0
+    ms = ev0.elapsed_time(ev1)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if pg is not None:
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * ncell * args.steps / (ms / 1e3)
+
+    # roofline of the dominant kernel (the fused stage kernel; the timed region
+    # holds only stage kernels and two 8-byte memsets per step)
+    stage_ms = ms / (args.steps * NSTAGES)
+    alg_bytes = ALG_BYTES_PER_CELL_STAGE * ncell
+    achieved = alg_bytes / (stage_ms / 1e3) / 1e9
+    peak, peak_src = measured_peaks()
+    tpc = profiled_traffic_per_cell()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None if tpc is None else tpc * ncell, "peak_source": peak_src,
+            "kernel": "stage_kernel<8,32,double,ROE>", "alg_bytes_per_launch": alg_bytes,
+            "avg_launch_ms": stage_ms}
+
+    # end to end through the C ABI with host buffers: upload the state from
+    # pinned host memory, one RK step, download the state, every step
+    host_in = torch.from_numpy(np.ascontiguousarray(s.get_state())).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    in_np, out_np = host_in.numpy(), host_out.numpy()
+    ke = max(3, min(args.steps, 20))
+    for _ in range(2):
+        s.set_state(in_np)
+        s.step(1)
+        out_np[...] = s.get_state()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        s.set_state(in_np)
+        s.step(1)
+        out_np[...] = s.get_state()
+    barrier()
+    el = time.perf_counter() - t0
+    tt = torch.tensor([el], dtype=torch.float64, device="cuda")
+    if pg is not None:
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+    e2e = {"value": world * ncell * ke / float(tt.item()), "unit": UNIT,
+           "h2d_bytes_per_step": int(host_in.numel() * 8), "d2h_bytes_per_step": int(host_out.numel() * 8),
+           "steps": ke}
+
+    if rank == 0:
+        cfg = workload_config()
+        cfg["l2"] = (f"no flush: per-step working set {(3 * 4 + 3 * 5) * 8 * ncell / 2**20 + 2 * 14 * 8 * ncell / 2**20:.0f}"
+                     f" MiB > {L2_BYTES / 2**20:.0f} MiB L2")
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": cfg, "roofline": roof, "e2e": e2e, "gpu_launches": int(launches),
+                "clocks": clk.summary()}
+        if world == 1 and not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(line), flush=True)
+    s.close()
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,103 @@
+"""ctypes binding of the C ABI declared in include/hc.h (libhcgb300.so).
+
+The library is the only compute path: if it is missing, loading raises; there
+is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libhcgb300.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "hc.h")
+
+HC_OK, HC_ERR_ARG, HC_ERR_CUDA, HC_ERR_NONPHYSICAL, HC_ERR_TIMEOUT, HC_ERR_UNSUPPORTED = range(6)
+STATUS_NAMES = {0: "HC_OK", 1: "HC_ERR_ARG", 2: "HC_ERR_CUDA", 3: "HC_ERR_NONPHYSICAL",
+                4: "HC_ERR_TIMEOUT", 5: "HC_ERR_UNSUPPORTED"}
+
+FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5}
+LIMITER = {"nolimit1": 0, "nolimit2": 1, "nolimit3": 2, "vanalbada": 3, "minmod": 4,
+           "superbee": 5, "mc": 6, "vanleer": 7, "vanleer_ref": 8, "cada3": 9}
+RK = {"ssp11": 0, "ssp22": 1, "ssp33": 2, "ssp34": 3}
+PRECISION = {"fp64": 0, "fp32": 1}
+DTMODE = {"global": 0, "local": 1}
+BC = {"periodic": 0, "fixed": 1, "riemann": 2, "entropy": 3, "wall": 4}
+
+
+class HCError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [("flux", C.c_int), ("limiter", C.c_int), ("rk", C.c_int), ("precision", C.c_int),
+                ("dt_mode", C.c_int), ("cfl", C.c_double)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("dt", C.c_double), ("t", C.c_double), ("resnorm", C.c_double), ("status", C.c_int),
+                ("bad_cell", C.c_int), ("kernel_launches", C.c_longlong)]
+
+
+_lib = None
+
+
+def _declare(lib):
+    p, i, d, v = C.c_void_p, C.c_int, C.c_double, C.c_void_p
+    dp = C.POINTER(C.c_double)
+    sig = {
+        "hc_context_create": [C.POINTER(Config), C.POINTER(p)],
+        "hc_context_destroy": [p],
+        "hc_set_stream": [p, v],
+        "hc_mesh_upload": [p, i, i, dp],
+        "hc_set_species": [p, d, d, d],
+        "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],
+        "hc_state_upload": [p, dp],
+        "hc_state_download": [p, dp],
+        "hc_state_upload_device": [p, v],
+        "hc_state_download_device": [p, v],
+        "hc_residual": [p, dp],
+        "hc_step": [p, i, C.POINTER(StepStats)],
+        "hc_step_async": [p, i],
+        "hc_sync": [p, C.POINTER(StepStats)],
+        "hc_mesh_cylinder_nodes": [i, i, d, d, d, dp],
+        "hc_mesh_linspace_nodes": [i, i, d, d, d, d, dp],
+    }
+    for name, args in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    lib.hc_last_error_string.restype = C.c_char_p
+    lib.hc_last_error_string.argtypes = []
+    lib.hc_version.restype = C.c_char_p
+    lib.hc_version.argtypes = []
+
+
+def load(build_if_missing: bool = True):
+    """Load libhcgb300.so (building it with nvcc when absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise OSError(f"{LIB_PATH} not built")
+        from . import build as _build
+        _build.build()
+    lib = C.CDLL(LIB_PATH)
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+def check(code: int) -> None:
+    if code != HC_OK:
+        raise HCError(code, load().hc_last_error_string().decode())
+
+
+def header_symbols() -> list[str]:
+    """Function names declared in include/hc.h."""
+    import re
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(hc_[a-z0-9_]+)\s*\(", txt)))

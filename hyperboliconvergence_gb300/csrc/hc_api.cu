@@ -1,0 +1,525 @@
+// hc_api.cu -- the C ABI of include/hc.h: contexts, mesh/state transfer and
+// the explicit RK time loop over the fused stage kernels.
+#include "../../include/hc.h"
+#include "hc_launch.h"
+#include "hc_geometry.cuh"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace hc;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define HC_CUDA(call)                                                                              \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(HC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// RK tables ssp11..ssp34 (ode.h:107-197)
+struct RKTab {
+  int nst;
+  double alpha[4][4];
+  double beta[4];
+};
+RKTab rk_table(int kind) {
+  RKTab t{};
+  if (kind == HC_RK_SSP11) { t.nst = 1; t.beta[0] = 1.0; t.alpha[0][0] = 1.0; }
+  else if (kind == HC_RK_SSP22) {
+    t.nst = 2; t.beta[0] = 1.0; t.beta[1] = 1.0;
+    t.alpha[0][0] = 1.0; t.alpha[1][0] = 0.5; t.alpha[1][1] = 0.5;
+  } else if (kind == HC_RK_SSP33) {
+    t.nst = 3; t.beta[0] = 1.0; t.beta[1] = 0.5; t.beta[2] = 1.0;
+    t.alpha[0][0] = 1.; t.alpha[1][0] = 0.5; t.alpha[1][1] = 0.5;
+    t.alpha[2][0] = 1. / 6.; t.alpha[2][1] = 1. / 6.; t.alpha[2][2] = 2. / 3.;
+  } else {
+    t.nst = 4; t.beta[0] = 0.5; t.beta[1] = 1.0; t.beta[2] = 0.5; t.beta[3] = 1.0;
+    t.alpha[0][0] = 1.0; t.alpha[1][0] = 0.5; t.alpha[1][1] = 0.5;
+    t.alpha[2][0] = 1. / 3.; t.alpha[2][1] = 1. / 3.; t.alpha[2][2] = 1. / 3.;
+    t.alpha[3][0] = 1. / 6.; t.alpha[3][1] = 1. / 6.; t.alpha[3][2] = 1. / 6.; t.alpha[3][3] = 1. / 2.;
+  }
+  return t;
+}
+
+template <class R> using StageFn = cudaError_t (*)(const StageArgs<R>&, int, cudaStream_t);
+
+template <class R> StageFn<R> stage_fn(int flux) {
+  switch (flux) {
+    case FLUX_ROE: return launch_stage<R, FLUX_ROE>;
+    case FLUX_SLAU: return launch_stage<R, FLUX_SLAU>;
+    case FLUX_SLAU_REF: return launch_stage<R, FLUX_SLAU_REF>;
+    case FLUX_AUSMPUP: return launch_stage<R, FLUX_AUSMPUP>;
+    case FLUX_RUSANOV: return launch_stage<R, FLUX_RUSANOV>;
+    default: return launch_stage<R, FLUX_CENTRAL>;
+  }
+}
+template <class R> cudaError_t prepare(int flux) {
+  switch (flux) {
+    case FLUX_ROE: return prepare_stage<R, FLUX_ROE>();
+    case FLUX_SLAU: return prepare_stage<R, FLUX_SLAU>();
+    case FLUX_SLAU_REF: return prepare_stage<R, FLUX_SLAU_REF>();
+    case FLUX_AUSMPUP: return prepare_stage<R, FLUX_AUSMPUP>();
+    case FLUX_RUSANOV: return prepare_stage<R, FLUX_RUSANOV>();
+    default: return prepare_stage<R, FLUX_CENTRAL>();
+  }
+}
+
+}  // namespace
+
+struct hc_ctx {
+  hc_config cfg{};
+  bool fp32 = false;
+  size_t rsz = 8;
+  int ni = 0, nj = 0;
+  int bc[4] = {-1, -1, -1, -1};
+  bool have_mesh = false, have_bcs = false, have_state = false, geom_dirty = true;
+  double gamma = 1.4, Rgas = 287.058, minf = 1e-4;
+  cudaStream_t own = nullptr, stream = nullptr;
+  int tile = TILE_8x32;
+  // device buffers
+  double* nodes = nullptr;
+  double* cx = nullptr;
+  double* cy = nullptr;
+  double* xm = nullptr;
+  double* fi64 = nullptr;
+  double* fj64 = nullptr;
+  double* vol64 = nullptr;
+  void* fi = nullptr;   // face records in R (aliases fi64 for FP64)
+  void* fj = nullptr;
+  void* vol = nullptr;
+  void* q[3] = {nullptr, nullptr, nullptr};
+  void* res[4] = {nullptr, nullptr, nullptr, nullptr};
+  void* gref[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* staging = nullptr;  // FP64 staging for FP32 transfers (4 planes)
+  StepInfo* info = nullptr;
+  std::vector<double> href[4];
+  long long launches = 0;
+
+  size_t ncell() const { return size_t(ni) * nj; }
+  int nface(int side) const { return side < 2 ? nj : ni; }
+};
+
+namespace {
+
+void free_buffers(hc_ctx* c) {
+  void* ptrs[] = {c->nodes, c->cx, c->cy, c->xm, c->fi64, c->fj64, c->vol64, c->q[0], c->q[1], c->q[2],
+                  c->res[0], c->res[1], c->res[2], c->res[3], c->gref[0], c->gref[1], c->gref[2], c->gref[3],
+                  c->staging, c->info};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (c->fp32) {
+    if (c->fi) cudaFree(c->fi);
+    if (c->fj) cudaFree(c->fj);
+    if (c->vol) cudaFree(c->vol);
+  }
+  c->nodes = c->cx = c->cy = c->xm = c->fi64 = c->fj64 = c->vol64 = c->staging = nullptr;
+  c->fi = c->fj = c->vol = nullptr;
+  for (int k = 0; k < 3; ++k) c->q[k] = nullptr;
+  for (int k = 0; k < 4; ++k) c->res[k] = c->gref[k] = nullptr;
+  c->info = nullptr;
+}
+
+int check_ctx(hc_ctx* c) {
+  if (!c) return fail(HC_ERR_ARG, "null context");
+  return HC_OK;
+}
+
+// Derive cells, faces and least-squares weights on the device (runs once per mesh/bc set).
+int build_geometry(hc_ctx* c) {
+  if (!c->have_mesh || !c->have_bcs) return fail(HC_ERR_ARG, "mesh and boundary conditions must be set first");
+  const int ni = c->ni, nj = c->nj;
+  const size_t n = c->ncell();
+  const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
+  const int B = 256;
+  geom_cells_kernel<<<unsigned((n + B - 1) / B), B, 0, c->stream>>>(c->nodes, ni, nj, c->vol64, c->cx, c->cy);
+  GeomArgs g{};
+  g.nodes = c->nodes; g.ni = ni; g.nj = nj;
+  for (int k = 0; k < 4; ++k) g.bc[k] = c->bc[k];
+  g.cx = c->cx; g.cy = c->cy; g.fi = c->fi64; g.fj = c->fj64; g.xm = c->xm;
+  geom_faces1_kernel<<<(nfi + B - 1) / B, B, 0, c->stream>>>(g, 0);
+  geom_faces1_kernel<<<(nfj + B - 1) / B, B, 0, c->stream>>>(g, 1);
+  geom_xm_kernel<<<unsigned((n + B - 1) / B), B, 0, c->stream>>>(g);
+  geom_faces2_kernel<<<(nfi + B - 1) / B, B, 0, c->stream>>>(g, 0);
+  geom_faces2_kernel<<<(nfj + B - 1) / B, B, 0, c->stream>>>(g, 1);
+  c->launches += 6;
+  if (c->fp32) {
+    convert_kernel<float><<<1024, 256, 0, c->stream>>>(c->fi64, (float*)c->fi, size_t(FREC) * nfi);
+    convert_kernel<float><<<1024, 256, 0, c->stream>>>(c->fj64, (float*)c->fj, size_t(FREC) * nfj);
+    convert_kernel<float><<<1024, 256, 0, c->stream>>>(c->vol64, (float*)c->vol, n);
+    c->launches += 3;
+  }
+  HC_CUDA(cudaGetLastError());
+  // ghost reference planes in the context precision
+  for (int s = 0; s < 4; ++s) {
+    if (c->bc[s] == HC_BC_PERIODIC || c->bc[s] == HC_BC_WALL || c->href[s].empty()) continue;
+    const size_t m = size_t(4) * c->nface(s);
+    if (c->fp32) {
+      std::vector<float> tmp(m);
+      for (size_t k = 0; k < m; ++k) tmp[k] = float(c->href[s][k]);
+      HC_CUDA(cudaMemcpyAsync(c->gref[s], tmp.data(), m * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+      HC_CUDA(cudaStreamSynchronize(c->stream));
+    } else {
+      HC_CUDA(cudaMemcpyAsync(c->gref[s], c->href[s].data(), m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    }
+  }
+  c->geom_dirty = false;
+  return HC_OK;
+}
+
+int ensure_ready(hc_ctx* c) {
+  if (c->geom_dirty) {
+    const int st = build_geometry(c);
+    if (st != HC_OK) return st;
+  }
+  if (!c->have_state) return fail(HC_ERR_ARG, "state not uploaded");
+  return HC_OK;
+}
+
+template <class R> StageArgs<R> base_args(hc_ctx* c) {
+  StageArgs<R> a{};
+  a.ni = c->ni; a.nj = c->nj;
+  for (int k = 0; k < 4; ++k) a.bc[k] = c->bc[k];
+  a.gas.gamma = R(c->gamma);
+  a.gas.gm1 = R(c->gamma - 1.);
+  a.gas.gamma1 = R(1. / (c->gamma - 1.));
+  a.gas.Rgas = R(c->Rgas);
+  a.gas.minf = R(c->minf);
+  a.limiter = c->cfg.limiter;
+  a.fi = (const R*)c->fi; a.fj = (const R*)c->fj; a.vol = (const R*)c->vol;
+  for (int k = 0; k < 4; ++k) a.gref[k] = (const R*)c->gref[k];
+  a.q0 = (const R*)c->q[0];
+  a.info = c->info;
+  a.cfl = R(c->cfg.cfl);
+  return a;
+}
+
+template <class R> int run_residual(hc_ctx* c) {
+  StageArgs<R> a = base_args<R>(c);
+  a.q = (const R*)c->q[0];
+  a.res_out = (R*)c->res[0];
+  a.mode = MODE_RESIDUAL;
+  HC_CUDA(stage_fn<R>(c->cfg.flux)(a, c->tile, c->stream));
+  c->launches += 1;
+  return HC_OK;
+}
+
+// One RK step: the stage loop of integrate() (timestepping/rungeKutta.h:97-164).
+template <class R> int run_step(hc_ctx* c) {
+  const RKTab tab = rk_table(c->cfg.rk);
+  const int nst = tab.nst;
+  const bool global = c->cfg.dt_mode == HC_DT_GLOBAL;
+  const StageFn<R> fn = stage_fn<R>(c->cfg.flux);
+  HC_CUDA(cudaMemsetAsync(&c->info->maxrate, 0, sizeof(unsigned long long), c->stream));
+  HC_CUDA(cudaMemsetAsync(&c->info->resnorm2, 0, sizeof(double), c->stream));
+  auto out_of = [&](int s) -> R* { return (R*)((s == nst - 1) ? c->q[0] : c->q[1 + (s % 2)]); };
+  for (int s = 0; s < nst; ++s) {
+    StageArgs<R> a = base_args<R>(c);
+    a.q = (s == 0) ? (const R*)c->q[0] : out_of(s - 1);
+    a.stage = s;
+    a.beta = R(tab.beta[s]);
+    for (int k = 0; k <= s; ++k) a.alpha[k] = R(tab.alpha[s][k]);
+    for (int k = 0; k < s; ++k) a.res_prev[k] = (const R*)c->res[k];
+    a.res_out = (s < nst - 1) ? (R*)c->res[s] : nullptr;
+    a.norm_stage0 = (s == 0);
+    if (global && s == 0) {
+      a.mode = MODE_RES_MAXRATE;
+      a.res_out = (R*)c->res[0];
+      HC_CUDA(fn(a, c->tile, c->stream));
+      const size_t n = c->ncell();
+      const int B = 256;
+      const unsigned grid = unsigned(std::min<size_t>((n + B - 1) / B, 152 * 16));
+      update0_kernel<R><<<grid, B, 0, c->stream>>>(c->ni, c->nj, a.gas, (const R*)c->q[0], (const R*)c->res[0],
+                                                   (const R*)c->vol, R(tab.alpha[0][0]), R(tab.beta[0]),
+                                                   c->cfg.cfl, c->info, out_of(0), 1);
+      HC_CUDA(cudaGetLastError());
+      c->launches += 2;
+    } else {
+      a.mode = global ? MODE_FUSED_GLOBAL : MODE_FUSED_LOCAL;
+      a.q_out = out_of(s);
+      HC_CUDA(fn(a, c->tile, c->stream));
+      c->launches += 1;
+    }
+  }
+  return HC_OK;
+}
+
+int read_stats(hc_ctx* c, hc_step_stats* st) {
+  StepInfo info{};
+  HC_CUDA(cudaMemcpyAsync(&info, c->info, sizeof(StepInfo), cudaMemcpyDeviceToHost, c->stream));
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  if (st) {
+    st->dt = info.dt;
+    st->t = info.t;
+    st->resnorm = std::sqrt(info.resnorm2);
+    st->status = info.status == ST_OK ? HC_OK : HC_ERR_NONPHYSICAL;
+    st->bad_cell = info.bad_cell;
+    st->kernel_launches = c->launches;
+  }
+  if (info.status != ST_OK)
+    return fail(HC_ERR_NONPHYSICAL, "non-physical state at cell " + std::to_string(info.bad_cell));
+  return HC_OK;
+}
+
+template <class R> __global__ void d2r_kernel(const double* a, R* b, size_t n) {
+  for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < n; k += size_t(gridDim.x) * blockDim.x)
+    b[k] = R(a[k]);
+}
+template <class R> __global__ void r2d_kernel(const R* a, double* b, size_t n) {
+  for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < n; k += size_t(gridDim.x) * blockDim.x)
+    b[k] = double(a[k]);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* hc_last_error_string(void) { return g_last_error.c_str(); }
+const char* hc_version(void) { return "hyperboliconvergence_gb300 0.1 sm_103a"; }
+
+int hc_context_create(const hc_config* cfg, hc_ctx** out) {
+  if (!cfg || !out) return fail(HC_ERR_ARG, "null argument");
+  if (cfg->flux < 0 || cfg->flux >= FLUX_COUNT) return fail(HC_ERR_ARG, "unknown flux");
+  if (cfg->limiter < 0 || cfg->limiter >= LIM_COUNT) return fail(HC_ERR_ARG, "unknown limiter");
+  if (cfg->rk < HC_RK_SSP11 || cfg->rk > HC_RK_SSP34) return fail(HC_ERR_ARG, "unknown RK table");
+  if (cfg->precision != HC_FP64 && cfg->precision != HC_FP32) return fail(HC_ERR_ARG, "unknown precision");
+  if (cfg->dt_mode != HC_DT_GLOBAL && cfg->dt_mode != HC_DT_LOCAL) return fail(HC_ERR_ARG, "unknown dt mode");
+  if (!(cfg->cfl > 0)) return fail(HC_ERR_ARG, "cfl must be positive");
+  hc_ctx* c = new hc_ctx();
+  c->cfg = *cfg;
+  c->fp32 = cfg->precision == HC_FP32;
+  c->rsz = c->fp32 ? sizeof(float) : sizeof(double);
+  cudaError_t e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = c->fp32 ? prepare<float>(cfg->flux) : prepare<double>(cfg->flux);
+  if (e == cudaSuccess) e = cudaMalloc(&c->info, sizeof(StepInfo));
+  if (e == cudaSuccess) e = cudaMemset(c->info, 0, sizeof(StepInfo));
+  if (e != cudaSuccess) {
+    if (c->own) cudaStreamDestroy(c->own);
+    if (c->info) cudaFree(c->info);
+    delete c;
+    return fail(HC_ERR_CUDA, std::string("context creation: ") + cudaGetErrorString(e));
+  }
+  c->stream = c->own;
+  *out = c;
+  return HC_OK;
+}
+
+int hc_context_destroy(hc_ctx* c) {
+  if (!c) return HC_OK;
+  cudaStreamSynchronize(c->stream);
+  free_buffers(c);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+  return HC_OK;
+}
+
+int hc_set_stream(hc_ctx* c, void* stream) {
+  if (int st = check_ctx(c)) return st;
+  c->stream = stream ? (cudaStream_t)stream : c->own;
+  return HC_OK;
+}
+
+int hc_mesh_upload(hc_ctx* c, int ni, int nj, const double* nodes_xy) {
+  if (int st = check_ctx(c)) return st;
+  if (!nodes_xy) return fail(HC_ERR_ARG, "null nodes");
+  if (ni < 3 || nj < 3) return fail(HC_ERR_ARG, "mesh needs at least 3 cells in each direction");
+  if (size_t(ni + 1) * size_t(nj + 1) > (size_t(1) << 28)) return fail(HC_ERR_ARG, "mesh too large");
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  free_buffers(c);
+  c->ni = ni; c->nj = nj;
+  const size_t n = c->ncell();
+  const size_t nfi = size_t(ni + 1) * nj, nfj = size_t(ni) * (nj + 1);
+  const size_t nn = size_t(ni + 1) * (nj + 1) * 2;
+  HC_CUDA(cudaMalloc(&c->info, sizeof(StepInfo)));
+  HC_CUDA(cudaMemsetAsync(c->info, 0, sizeof(StepInfo), c->stream));
+  HC_CUDA(cudaMalloc(&c->nodes, nn * sizeof(double)));
+  HC_CUDA(cudaMalloc(&c->cx, n * sizeof(double)));
+  HC_CUDA(cudaMalloc(&c->cy, n * sizeof(double)));
+  HC_CUDA(cudaMalloc(&c->xm, 3 * n * sizeof(double)));
+  HC_CUDA(cudaMalloc(&c->vol64, n * sizeof(double)));
+  HC_CUDA(cudaMalloc(&c->fi64, FREC * nfi * sizeof(double)));
+  HC_CUDA(cudaMalloc(&c->fj64, FREC * nfj * sizeof(double)));
+  if (c->fp32) {
+    HC_CUDA(cudaMalloc(&c->fi, FREC * nfi * sizeof(float)));
+    HC_CUDA(cudaMalloc(&c->fj, FREC * nfj * sizeof(float)));
+    HC_CUDA(cudaMalloc(&c->vol, n * sizeof(float)));
+    HC_CUDA(cudaMalloc(&c->staging, 5 * n * sizeof(double)));
+  } else {
+    c->fi = c->fi64; c->fj = c->fj64; c->vol = c->vol64;
+  }
+  for (int k = 0; k < 3; ++k) HC_CUDA(cudaMalloc(&c->q[k], 4 * n * c->rsz));
+  for (int k = 0; k < 4; ++k) HC_CUDA(cudaMalloc(&c->res[k], 5 * n * c->rsz));
+  for (int s = 0; s < 4; ++s) HC_CUDA(cudaMalloc(&c->gref[s], 4 * size_t(c->nface(s)) * c->rsz));
+  HC_CUDA(cudaMemcpyAsync(c->nodes, nodes_xy, nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_mesh = true;
+  c->have_state = false;
+  c->geom_dirty = true;
+  for (int s = 0; s < 4; ++s)
+    if (!c->href[s].empty() && c->href[s].size() != size_t(4) * c->nface(s)) c->href[s].clear();
+  return HC_OK;
+}
+
+int hc_set_species(hc_ctx* c, double gamma, double gas_constant, double minf) {
+  if (int st = check_ctx(c)) return st;
+  if (!(gamma > 1.0) || !(gas_constant > 0.0) || !(minf > 0.0)) return fail(HC_ERR_ARG, "invalid species");
+  c->gamma = gamma; c->Rgas = gas_constant; c->minf = minf;
+  return HC_OK;
+}
+
+int hc_set_bcs(hc_ctx* c, const int bc_type[4], const double* const ref[4]) {
+  if (int st = check_ctx(c)) return st;
+  if (!c->have_mesh) return fail(HC_ERR_ARG, "upload the mesh before the boundary conditions");
+  if (!bc_type) return fail(HC_ERR_ARG, "null bc types");
+  for (int s = 0; s < 4; ++s)
+    if (bc_type[s] < HC_BC_PERIODIC || bc_type[s] > HC_BC_WALL) return fail(HC_ERR_ARG, "unknown bc type");
+  if ((bc_type[0] == HC_BC_PERIODIC) != (bc_type[1] == HC_BC_PERIODIC) ||
+      (bc_type[2] == HC_BC_PERIODIC) != (bc_type[3] == HC_BC_PERIODIC))
+    return fail(HC_ERR_ARG, "periodic sides must come in pairs (0,1) and (2,3)");
+  for (int s = 0; s < 4; ++s) {
+    c->bc[s] = bc_type[s];
+    c->href[s].clear();
+    const bool needs = bc_type[s] != HC_BC_PERIODIC && bc_type[s] != HC_BC_WALL;
+    if (needs) {
+      if (!ref || !ref[s]) return fail(HC_ERR_ARG, "side " + std::to_string(s) + " needs reference values");
+      c->href[s].assign(ref[s], ref[s] + size_t(4) * c->nface(s));
+    }
+  }
+  c->have_bcs = true;
+  c->geom_dirty = true;
+  return HC_OK;
+}
+
+int hc_state_upload(hc_ctx* c, const double* prim) {
+  if (int st = check_ctx(c)) return st;
+  if (!c->have_mesh) return fail(HC_ERR_ARG, "upload the mesh first");
+  if (!prim) return fail(HC_ERR_ARG, "null state");
+  const size_t m = 4 * c->ncell();
+  if (c->fp32) {
+    HC_CUDA(cudaMemcpyAsync(c->staging, prim, m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    d2r_kernel<float><<<1024, 256, 0, c->stream>>>(c->staging, (float*)c->q[0], m);
+    HC_CUDA(cudaGetLastError());
+    c->launches += 1;
+  } else {
+    HC_CUDA(cudaMemcpyAsync(c->q[0], prim, m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  }
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  c->have_state = true;
+  return HC_OK;
+}
+
+int hc_state_download(hc_ctx* c, double* prim) {
+  if (int st = check_ctx(c)) return st;
+  if (!c->have_state) return fail(HC_ERR_ARG, "no state");
+  if (!prim) return fail(HC_ERR_ARG, "null output");
+  const size_t m = 4 * c->ncell();
+  if (c->fp32) {
+    r2d_kernel<float><<<1024, 256, 0, c->stream>>>((const float*)c->q[0], c->staging, m);
+    HC_CUDA(cudaGetLastError());
+    c->launches += 1;
+    HC_CUDA(cudaMemcpyAsync(prim, c->staging, m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    HC_CUDA(cudaMemcpyAsync(prim, c->q[0], m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  }
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  return HC_OK;
+}
+
+int hc_state_upload_device(hc_ctx* c, const void* prim) {
+  if (int st = check_ctx(c)) return st;
+  if (!c->have_mesh || !prim) return fail(HC_ERR_ARG, "mesh and a state pointer are required");
+  HC_CUDA(cudaMemcpyAsync(c->q[0], prim, 4 * c->ncell() * c->rsz, cudaMemcpyDeviceToDevice, c->stream));
+  c->have_state = true;
+  return HC_OK;
+}
+
+int hc_state_download_device(hc_ctx* c, void* prim) {
+  if (int st = check_ctx(c)) return st;
+  if (!c->have_state || !prim) return fail(HC_ERR_ARG, "no state or null output");
+  HC_CUDA(cudaMemcpyAsync(prim, c->q[0], 4 * c->ncell() * c->rsz, cudaMemcpyDeviceToDevice, c->stream));
+  return HC_OK;
+}
+
+int hc_residual(hc_ctx* c, double* out5) {
+  if (int st = check_ctx(c)) return st;
+  if (int st = ensure_ready(c)) return st;
+  if (!out5) return fail(HC_ERR_ARG, "null output");
+  const int st = c->fp32 ? run_residual<float>(c) : run_residual<double>(c);
+  if (st != HC_OK) return st;
+  const size_t m = 5 * c->ncell();
+  if (c->fp32) {
+    r2d_kernel<float><<<1024, 256, 0, c->stream>>>((const float*)c->res[0], c->staging, m);
+    HC_CUDA(cudaGetLastError());
+    c->launches += 1;
+    HC_CUDA(cudaMemcpyAsync(out5, c->staging, m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    HC_CUDA(cudaMemcpyAsync(out5, c->res[0], m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  }
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  return HC_OK;
+}
+
+int hc_step_async(hc_ctx* c, int nsteps) {
+  if (int st = check_ctx(c)) return st;
+  if (nsteps < 0) return fail(HC_ERR_ARG, "negative step count");
+  if (int st = ensure_ready(c)) return st;
+  // clear the device status of earlier calls (status and bad_cell are adjacent ints)
+  HC_CUDA(cudaMemsetAsync(&c->info->status, 0, 2 * sizeof(int), c->stream));
+  for (int k = 0; k < nsteps; ++k) {
+    const int st = c->fp32 ? run_step<float>(c) : run_step<double>(c);
+    if (st != HC_OK) return st;
+  }
+  return HC_OK;
+}
+
+int hc_sync(hc_ctx* c, hc_step_stats* stats) {
+  if (int st = check_ctx(c)) return st;
+  return read_stats(c, stats);
+}
+
+int hc_step(hc_ctx* c, int nsteps, hc_step_stats* stats) {
+  const int st = hc_step_async(c, nsteps);
+  if (st != HC_OK) return st;
+  return hc_sync(c, stats);
+}
+
+// make_cylinder_mesh (mesh/generate/twoD.h:223-263) with geometric radial stretching
+int hc_mesh_cylinder_nodes(int nr, int nth, double rc, double rb, double stretch, double* nodes) {
+  if (nr < 1 || nth < 1 || !nodes || !(rb > rc) || !(stretch > 0)) return fail(HC_ERR_ARG, "invalid cylinder mesh");
+  const double dr = (rb - rc) / nr;
+  const double dth = (2. * M_PI) / nth;
+  const double dr0 = (stretch == 1.0) ? dr : (rb - rc) * (stretch - 1.) / (std::pow(stretch, nr) - 1.);
+  for (int i = 0; i <= nr; ++i) {
+    const double r = (stretch == 1.0) ? rc + i * dr : rc + dr0 * (std::pow(stretch, i) - 1.) / (stretch - 1.);
+    for (int j = 0; j <= nth; ++j) {
+      const double th = j * dth;
+      nodes[(size_t(i) * (nth + 1) + j) * 2 + 0] = r * cos(th);
+      nodes[(size_t(i) * (nth + 1) + j) * 2 + 1] = r * sin(th);
+    }
+  }
+  return HC_OK;
+}
+
+// make_linspace_mesh (mesh/generate/twoD.h:99-124)
+int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, double hiy, double* nodes) {
+  if (nx < 1 || ny < 1 || !nodes) return fail(HC_ERR_ARG, "invalid linspace mesh");
+  const double dx = (hix - lox) / nx, dy = (hiy - loy) / ny;
+  for (int i = 0; i <= nx; ++i)
+    for (int j = 0; j <= ny; ++j) {
+      nodes[(size_t(i) * (ny + 1) + j) * 2 + 0] = lox + i * dx;
+      nodes[(size_t(i) * (ny + 1) + j) * 2 + 1] = loy + j * dy;
+    }
+  return HC_OK;
+}
+
+}  // extern "C"

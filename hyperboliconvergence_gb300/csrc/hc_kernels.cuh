@@ -1,0 +1,393 @@
+// hc_kernels.cuh -- CUDA kernels of the residual-and-timestep path.
+//
+//  * geometry kernels (once per mesh, always FP64): cell volumes/centres,
+//    face normals/areas, least-squares metrics folded into per-face weights;
+//  * stage kernel: one RK stage fused -- qmetric (LSQ) of every cell of a
+//    halo tile, MUSCL reconstruction with the limiter, the face flux, face to
+//    cell accumulation, and either the spectral-radius reduction (global dt,
+//    stage 0) or the alpha/beta RK update (spatial/eulerForwardUpdate.h:38-168);
+//  * update kernel: the stage-0 update once the global dt is known.
+//
+// Layouts in HBM (all SoA, cell (i,j) at i*nj+j, j fastest):
+//   state      4 planes of ni*nj primitive values {u, v, rho, p}
+//   residual   5 planes: 4 conserved flux sums + spectral-radius sum
+//   i-faces    FREC planes of (ni+1)*nj records, face (i,j) between cells (i-1,j),(i,j)
+//   j-faces    FREC planes of ni*(nj+1) records, face (i,j) between cells (i,j-1),(i,j)
+#pragma once
+
+#include "hc_physics.cuh"
+
+#include <cstdint>
+
+namespace hc {
+
+// face record fields
+enum FaceField { F_NX = 0, F_NY, F_A, F_DL, F_DR, F_IDLR, F_WLX, F_WLY, F_SL, F_WRX, F_WRY, F_SR, F_DXX, F_DXY,
+                 FREC };
+
+// Per-step scalars shared by the kernels of one RK step (device memory).
+struct StepInfo {
+  unsigned long long maxrate;  // max over cells of lambda/V as the bit pattern of a positive double
+  double dt;                   // global timestep of the current step
+  double t;                    // accumulated time
+  int status;                  // 0 ok, 1 non-physical state produced
+  int bad_cell;                // first cell found non-physical
+  double resnorm2;             // sum over cells of the stage-0 density residual squared
+};
+
+// Status codes of the device-side checks
+enum { ST_OK = 0, ST_NONPHYSICAL = 1 };
+
+template <class R> struct StageArgs {
+  int ni, nj;
+  int bc[4];
+  Gas<R> gas;
+  int limiter;
+  const R* q;         // input stage state
+  const R* q0;        // state at the start of the step
+  const R* fi;        // i-face records
+  const R* fj;        // j-face records
+  const R* vol;       // cell volumes
+  const R* gref[4];   // per side: far-field/fixed primitive values, 4 planes of nface
+  R* res_out;         // residual of this stage (5 planes) or null
+  const R* res_prev[4];  // residuals of earlier stages (flux planes)
+  R alpha[4];         // alpha[s][0..s]
+  int stage;
+  int mode;           // MODE_*
+  R beta, cfl;
+  StepInfo* info;
+  R* q_out;           // next stage state (fused modes)
+  int norm_stage0;    // accumulate the density-residual norm
+};
+
+enum { MODE_RESIDUAL = 0, MODE_RES_MAXRATE = 1, MODE_FUSED_GLOBAL = 2, MODE_FUSED_LOCAL = 3 };
+
+template <class R> __global__ void convert_kernel(const double* __restrict__ a, R* __restrict__ b, size_t n) {
+  for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < n; k += size_t(gridDim.x) * blockDim.x)
+    b[k] = R(a[k]);
+}
+
+// ---------------------------------------------------------------- stage kernel
+template <int TI, int TJ, class R> struct StageSmem {
+  static constexpr int QI = TI + 4, QJ = TJ + 4;   // state tile with a 2-cell halo
+  static constexpr int MI = TI + 2, MJ = TJ + 2;   // qmetric tile with a 1-cell halo
+  static constexpr size_t q_elems = size_t(4) * QI * QJ;
+  static constexpr size_t m_elems = size_t(8) * MI * MJ;
+  static constexpr size_t fi_elems = size_t(5) * (TI + 1) * TJ;
+  static constexpr size_t fj_elems = size_t(5) * TI * (TJ + 1);
+  static constexpr size_t bytes = (q_elems + m_elems + fi_elems + fj_elems) * sizeof(R);
+};
+
+__device__ __forceinline__ int wrapi(int a, int n) {
+  a %= n;
+  return a < 0 ? a + n : a;
+}
+
+template <class R> __device__ __forceinline__ void atomic_max_rate(StepInfo* info, R v);
+template <> __device__ __forceinline__ void atomic_max_rate<double>(StepInfo* info, double v) {
+  if (v > 0.0) atomicMax(&info->maxrate, (unsigned long long)__double_as_longlong(v));
+}
+template <> __device__ __forceinline__ void atomic_max_rate<float>(StepInfo* info, float v) {
+  const double d = double(v);
+  if (d > 0.0) atomicMax(&info->maxrate, (unsigned long long)__double_as_longlong(d));
+}
+
+template <class R> __device__ __forceinline__ void flag_nonphysical(StepInfo* info, const R* q, int cell) {
+  const bool bad = !(q[2] > R(0)) || !(q[3] > R(0)) || !isfinite(q[0]) || !isfinite(q[1]);
+  if (bad) {
+    if (atomicCAS(&info->status, ST_OK, ST_NONPHYSICAL) == ST_OK) info->bad_cell = cell;
+  }
+}
+
+// cons(q0) + tot*fac -> primitive (spatial/eulerForwardUpdate.h:76-85)
+template <class R> __device__ __forceinline__ void forward_update(const Gas<R>& g, const R* q0, const R* tot, R fac,
+                                                                  R* qn) {
+  const St<R> s0 = prim_state(g, q0[0], q0[1], q0[2], q0[3]);
+  R qc[4];
+  state_cons(s0, qc);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) qc[v] = qc[v] + tot[v] * fac;
+  const St<R> s1 = cons_state(g, qc);
+  qn[0] = s1.u; qn[1] = s1.v; qn[2] = s1.r; qn[3] = s1.p;
+}
+
+template <int TI, int TJ, class R, int FK>
+__global__ void __launch_bounds__(TI * TJ) stage_kernel(const StageArgs<R> a) {
+  using SM = StageSmem<TI, TJ, R>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* sq = reinterpret_cast<R*>(smem_raw);
+  R* sm = sq + SM::q_elems;
+  R* sfi = sm + SM::m_elems;
+  R* sfj = sfi + SM::fi_elems;
+  constexpr int QI = SM::QI, QJ = SM::QJ, MI = SM::MI, MJ = SM::MJ;
+  constexpr int NT = TI * TJ;
+  const int ni = a.ni, nj = a.nj;
+  const size_t ncell = size_t(ni) * nj;
+  const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
+  const int tid = threadIdx.x;
+  const bool per_i = a.bc[0] == BC_PERIODIC, per_j = a.bc[2] == BC_PERIODIC;
+  const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
+
+  // ---- phase 1: state tile with a 2-cell halo (periodic sides wrap)
+  for (int k = tid; k < QI * QJ; k += NT) {
+    const int la = k / QJ, lb = k % QJ;
+    int gi = i0 - 2 + la, gj = j0 - 2 + lb;
+    bool ok = true;
+    if (gi < 0 || gi >= ni) { if (per_i) gi = wrapi(gi, ni); else ok = false; }
+    if (gj < 0 || gj >= nj) { if (per_j) gj = wrapi(gj, nj); else ok = false; }
+    const size_t c = size_t(gi) * nj + gj;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) sq[(v * QI + la) * QJ + lb] = ok ? a.q[v * ncell + c] : R(0);
+  }
+  __syncthreads();
+
+  auto Q = [&](int v, int la, int lb) -> R { return sq[(v * QI + la + 2) * QJ + lb + 2]; };  // tile coords
+  auto M = [&](int k, int la, int lb) -> R& { return sm[(k * MI + la + 1) * MJ + lb + 1]; };
+
+  // ---- phase 2: qmetric of the tile cells and of the 1-cell halo strips
+  // (lsq/qmetric.ipp via spatial/lsqMetrics.h:269-301; D2 periodic wrap)
+  for (int k = tid; k < MI * MJ; k += NT) {
+    const int la = k / MJ - 1, lb = k % MJ - 1;
+    const bool corner = (la < 0 || la >= TI) && (lb < 0 || lb >= TJ);
+    int gi = i0 + la, gj = j0 + lb;
+    bool ok = !corner;
+    if (gi < 0 || gi >= ni) { if (per_i) gi = wrapi(gi, ni); else ok = false; }
+    if (gj < 0 || gj >= nj) { if (per_j) gj = wrapi(gj, nj); else ok = false; }
+    R m[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) m[q] = R(0);
+    if (ok) {
+      // the cell's four faces: (face index, neighbour offset, is pair face)
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        const bool idir = f < 2;
+        const int hi = f & 1;
+        int fidx;
+        bool pair;
+        if (idir) {
+          const int fi = gi + hi;
+          pair = (fi > 0 && fi < ni) || per_i;
+          fidx = fi * nj + gj;
+        } else {
+          const int fj = gj + hi;
+          pair = (fj > 0 && fj < nj) || per_j;
+          fidx = gi * (nj + 1) + fj;
+        }
+        if (!pair) continue;
+        const R* rec = idir ? a.fi : a.fj;
+        const int nf = idir ? nfi : nfj;
+        const R dx = rec[size_t(F_DXX) * nf + fidx], dy = rec[size_t(F_DXY) * nf + fidx];
+        const int na = la + (idir ? (hi ? 1 : -1) : 0), nb = lb + (idir ? 0 : (hi ? 1 : -1));
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          // (q_right - q_left) of the face
+          const R dq = hi ? (Q(v, na, nb) - Q(v, la, lb)) : (Q(v, la, lb) - Q(v, na, nb));
+          m[2 * v] += dq * dx;
+          m[2 * v + 1] += dq * dy;
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) M(q, la, lb) = m[q];
+  }
+  __syncthreads();
+
+  // ---- phase 3: face fluxes (i-faces then j-faces of the tile, each once)
+  const Gas<R> g = a.gas;
+  const int lim = a.limiter;
+  constexpr int NFI = (TI + 1) * TJ, NFJ = TI * (TJ + 1);
+  for (int k = tid; k < NFI + NFJ; k += NT) {
+    const bool idir = k < NFI;
+    int la, lb;  // local coordinates of the face's right cell
+    if (idir) { la = k / TJ; lb = k % TJ; } else { const int kk = k - NFI; la = kk / (TJ + 1); lb = kk % (TJ + 1); }
+    const int gi = i0 + la, gj = j0 + lb;
+    bool valid = idir ? (gi <= ni && gj < nj) : (gi < ni && gj <= nj);
+    Flux5<R> F;
+    F.f[0] = F.f[1] = F.f[2] = F.f[3] = F.lam = R(0);
+    if (valid) {
+      const R* rec = idir ? a.fi : a.fj;
+      const int nf = idir ? nfi : nfj;
+      const int fidx = idir ? gi * nj + gj : gi * (nj + 1) + gj;
+      auto rd = [&](int fld) -> R { return rec[size_t(fld) * nf + fidx]; };
+      const R nx = rd(F_NX), ny = rd(F_NY), A = rd(F_A);
+      const int lo = idir ? gi : gj, nalong = idir ? ni : nj;
+      const int side = idir ? (lo == 0 ? 0 : 1) : (lo == 0 ? 2 : 3);
+      const bool bnd = (lo == 0 || lo == nalong) && a.bc[side] != BC_PERIODIC;
+      const int la_l = idir ? la - 1 : la, lb_l = idir ? lb : lb - 1;  // left cell
+      if (!bnd) {
+        R ql[4], qr[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) { ql[v] = Q(v, la_l, lb_l); qr[v] = Q(v, la, lb); }
+        if (lim != LIM_NOLIMIT1) {
+          const R dl = rd(F_DL), dr = rd(F_DR), idlr = rd(F_IDLR);
+          const R wlx = rd(F_WLX), wly = rd(F_WLY), sl = rd(F_SL);
+          const R wrx = rd(F_WRX), wry = rd(F_WRY), sr = rd(F_SR);
+          R qL[4], qR[4];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            const R dq = qr[v] - ql[v];
+            const R gc = dq * idlr;
+            const R gl = (M(2 * v, la_l, lb_l) * wlx + M(2 * v + 1, la_l, lb_l) * wly) - dq * sl;
+            const R gr = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
+            qL[v] = ql[v] + dl * limit<R>(lim, gc, gl);
+            qR[v] = qr[v] - dr * limit<R>(lim, gc, gr);
+          }
+          F = face_flux<R, FK>(g, nx, ny, A, prim_state(g, qL[0], qL[1], qL[2], qL[3]),
+                               prim_state(g, qR[0], qR[1], qR[2], qR[3]));
+        } else {
+          F = face_flux<R, FK>(g, nx, ny, A, prim_state(g, ql[0], ql[1], ql[2], ql[3]),
+                               prim_state(g, qr[0], qr[1], qr[2], qr[3]));
+        }
+      } else {
+        // boundary face: interior cell is the right cell on sides 0/2, the left on 1/3
+        const bool int_right = lo == 0;
+        const int ia = int_right ? la : la_l, ib = int_right ? lb : lb_l;
+        R qi[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) qi[v] = Q(v, ia, ib);
+        const int kf = idir ? gj : gi;  // face index along the side
+        const int bct = a.bc[side];
+        if (bct == BC_WALL) {
+          const R wx = int_right ? rd(F_WLX) : rd(F_WRX), wy = int_right ? rd(F_WLY) : rd(F_WRY);
+          R qw[4];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) qw[v] = qi[v] - (M(2 * v, ia, ib) * wx + M(2 * v + 1, ia, ib) * wy);
+          F = wall_flux(g, nx, ny, A, qw);
+        } else {
+          const int nfs = idir ? nj : ni;
+          R qref[4], qg[4];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) qref[v] = a.gref[side][size_t(v) * nfs + kf];
+          const R sgn = int_right ? R(1) : R(-1);  // normal into the domain
+          if (bct == BC_RIEMANN) farfield_update<R, BC_RIEMANN>(g, sgn * nx, sgn * ny, qi, qref, qg);
+          else if (bct == BC_ENTROPY) farfield_update<R, BC_ENTROPY>(g, sgn * nx, sgn * ny, qi, qref, qg);
+          else {
+#pragma unroll
+            for (int v = 0; v < 4; ++v) qg[v] = qref[v];
+          }
+          R qL[4], qR[4];
+          if (lim != LIM_NOLIMIT1) {
+            const R d = rd(F_DL), idlr = rd(F_IDLR);
+            const R wx = int_right ? rd(F_WRX) : rd(F_WLX), wy = int_right ? rd(F_WRY) : rd(F_WLY);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+              const R dq = int_right ? (qi[v] - qg[v]) : (qg[v] - qi[v]);
+              const R gb = M(2 * v, ia, ib) * wx + M(2 * v + 1, ia, ib) * wy;
+              const R s = limit<R>(lim, dq * idlr, gb);
+              if (int_right) { qL[v] = qg[v]; qR[v] = qi[v] - d * s; }
+              else { qL[v] = qi[v] + d * s; qR[v] = qg[v]; }
+            }
+          } else {
+#pragma unroll
+            for (int v = 0; v < 4; ++v) { qL[v] = int_right ? qg[v] : qi[v]; qR[v] = int_right ? qi[v] : qg[v]; }
+          }
+          F = face_flux<R, FK>(g, nx, ny, A, prim_state(g, qL[0], qL[1], qL[2], qL[3]),
+                               prim_state(g, qR[0], qR[1], qR[2], qR[3]));
+        }
+      }
+    }
+    R* dst = idir ? sfi : sfj;
+    const int slot = idir ? (la * TJ + lb) : (la * (TJ + 1) + lb);
+    const int pl = idir ? NFI : NFJ;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) dst[v * pl + slot] = F.f[v];
+    dst[4 * pl + slot] = F.lam;
+  }
+  __syncthreads();
+
+  // ---- phase 4: accumulate to cells (residualCalc.h:199-253 signs) and update
+  const int la = tid / TJ, lb = tid % TJ;
+  const int gi = i0 + la, gj = j0 + lb;
+  const bool own = gi < ni && gj < nj;
+  R res[4], lam = R(0);
+  if (own) {
+    const int s0 = la * TJ + lb, s1 = (la + 1) * TJ + lb;
+    const int t0 = la * (TJ + 1) + lb, t1 = t0 + 1;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) res[v] = ((sfi[v * NFI + s0] - sfi[v * NFI + s1]) + sfj[v * NFJ + t0]) - sfj[v * NFJ + t1];
+    lam = ((sfi[4 * NFI + s0] + sfi[4 * NFI + s1]) + sfj[4 * NFJ + t0]) + sfj[4 * NFJ + t1];
+  }
+  const size_t c = size_t(gi) * nj + gj;
+  if (own && a.res_out) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) a.res_out[v * ncell + c] = res[v];
+    a.res_out[4 * ncell + c] = lam;
+  }
+  if (a.mode == MODE_RES_MAXRATE) {
+    // spectralRadius: max over cells of lambda/V (spatial/spectralRadius.h:19-48)
+    R rate = own ? lam / a.vol[c] : R(0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+    if ((tid & 31) == 0) atomic_max_rate<R>(a.info, rate);
+    if (a.norm_stage0) {
+      R r2 = own ? res[2] * res[2] : R(0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+      if ((tid & 31) == 0) atomicAdd(&a.info->resnorm2, double(r2));
+    }
+    return;
+  }
+  if (a.mode == MODE_RESIDUAL) return;
+  if (a.norm_stage0 && a.stage == 0) {
+    R r2 = own ? res[2] * res[2] : R(0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
+    if ((tid & 31) == 0) atomicAdd(&a.info->resnorm2, double(r2));
+  }
+  if (!own) return;
+  // rungeKuttaAccumulation (timestepping/rungeKutta.h:172-197)
+  R tot[4] = {R(0), R(0), R(0), R(0)};
+  for (int k = 0; k < a.stage; ++k)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) tot[v] += a.alpha[k] * a.res_prev[k][v * ncell + c];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) tot[v] += a.alpha[a.stage] * res[v];
+  R fac;
+  if (a.mode == MODE_FUSED_GLOBAL) {
+    const R dts = a.beta * R(a.info->dt);
+    fac = dts / a.vol[c];
+  } else {
+    // local timestep from the stage-0 spectral radius sum (eulerForwardUpdate.h:155-161)
+    const R l0 = (a.stage == 0) ? lam : a.res_prev[0][4 * ncell + c];
+    const R cs = a.beta * a.cfl;
+    fac = cs / l0;
+  }
+  R q0[4], qn[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) q0[v] = a.q0[v * ncell + c];
+  forward_update(g, q0, tot, fac, qn);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) a.q_out[v * ncell + c] = qn[v];
+  flag_nonphysical(a.info, qn, int(c));
+}
+
+// Stage-0 update with the global timestep dt = cfl / max(lambda/V)
+// (timestepping/rungeKutta.h:131-154).
+template <class R>
+__global__ void update0_kernel(int ni, int nj, Gas<R> g, const R* __restrict__ q0, const R* __restrict__ res0,
+                               const R* __restrict__ vol, R alpha00, R beta0, double cfl, StepInfo* info,
+                               R* __restrict__ q_out, int advance_time) {
+  const size_t ncell = size_t(ni) * nj;
+  const double rate = fmax(DBL_MIN, __longlong_as_double((long long)info->maxrate));
+  const R dt = R(cfl / rate);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    info->dt = double(dt);
+    if (advance_time) info->t += double(dt);
+  }
+  for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < ncell; c += size_t(gridDim.x) * blockDim.x) {
+    R tot[4], q[4], qn[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      tot[v] = R(0) + alpha00 * res0[v * ncell + c];
+      q[v] = q0[v * ncell + c];
+    }
+    const R dts = beta0 * dt;
+    const R fac = dts / vol[c];
+    forward_update(g, q, tot, fac, qn);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) q_out[v * ncell + c] = qn[v];
+    flag_nonphysical(info, qn, int(c));
+  }
+}
+
+}  // namespace hc

@@ -1,0 +1,60 @@
+// hc_launch.h -- host-side launchers of the per-flux stage kernels.  Each
+// flux is compiled in its own translation unit (hc_stage_<flux>.cu) so the
+// build runs them in parallel.
+#pragma once
+
+#include "hc_kernels.cuh"
+
+namespace hc {
+
+// Tile shapes the stage kernel is built for (cells along i x cells along j).
+enum TileShape { TILE_8x32 = 0, TILE_4x32 = 1, TILE_16x16 = 2, TILE_COUNT = 3 };
+
+template <class R, int FK> cudaError_t launch_stage(const StageArgs<R>& a, int tile, cudaStream_t s);
+template <class R, int FK> cudaError_t prepare_stage();
+
+inline void tile_dims(int tile, int* ti, int* tj) {
+  switch (tile) {
+    case TILE_4x32: *ti = 4; *tj = 32; break;
+    case TILE_16x16: *ti = 16; *tj = 16; break;
+    default: *ti = 8; *tj = 32; break;
+  }
+}
+
+}  // namespace hc
+
+#define HC_STAGE_INSTANTIATE(FK)                                                                         \
+  namespace hc {                                                                                         \
+  template <class R, int TI, int TJ> static cudaError_t prep_one() {                                     \
+    return cudaFuncSetAttribute(stage_kernel<TI, TJ, R, FK>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                int(StageSmem<TI, TJ, R>::bytes));                                       \
+  }                                                                                                      \
+  template <class R, int TI, int TJ> static void go(const StageArgs<R>& a, cudaStream_t s) {             \
+    const dim3 grid((a.nj + TJ - 1) / TJ, (a.ni + TI - 1) / TI);                                         \
+    stage_kernel<TI, TJ, R, FK><<<grid, TI * TJ, StageSmem<TI, TJ, R>::bytes, s>>>(a);                   \
+  }                                                                                                      \
+  template <> cudaError_t prepare_stage<double, FK>() {                                                  \
+    cudaError_t e = prep_one<double, 8, 32>();                                                           \
+    if (e == cudaSuccess) e = prep_one<double, 4, 32>();                                                 \
+    if (e == cudaSuccess) e = prep_one<double, 16, 16>();                                                \
+    return e;                                                                                            \
+  }                                                                                                      \
+  template <> cudaError_t prepare_stage<float, FK>() {                                                   \
+    cudaError_t e = prep_one<float, 8, 32>();                                                            \
+    if (e == cudaSuccess) e = prep_one<float, 4, 32>();                                                  \
+    if (e == cudaSuccess) e = prep_one<float, 16, 16>();                                                 \
+    return e;                                                                                            \
+  }                                                                                                      \
+  template <class R> static cudaError_t dispatch(const StageArgs<R>& a, int tile, cudaStream_t s) {     \
+    if (tile == TILE_4x32) go<R, 4, 32>(a, s);                                                           \
+    else if (tile == TILE_16x16) go<R, 16, 16>(a, s);                                                    \
+    else go<R, 8, 32>(a, s);                                                                             \
+    return cudaGetLastError();                                                                           \
+  }                                                                                                      \
+  template <> cudaError_t launch_stage<double, FK>(const StageArgs<double>& a, int tile, cudaStream_t s) { \
+    return dispatch<double>(a, tile, s);                                                                 \
+  }                                                                                                      \
+  template <> cudaError_t launch_stage<float, FK>(const StageArgs<float>& a, int tile, cudaStream_t s) {   \
+    return dispatch<float>(a, tile, s);                                                                  \
+  }                                                                                                      \
+  }

@@ -1,0 +1,429 @@
+// hc_physics.cuh -- device pointwise physics for the 2D Euler residual path.
+//
+// Every function is templated on the arithmetic type R (double or float) and
+// keeps all constants in R, so the FP32 path never touches the FP64 pipe.
+// Formulas follow the reference solver (lacrymose/hyperboliConvergence,
+// cpp/inc); each function names the file:line it follows.  Variable order:
+// primitive {u, v, rho, p}, conserved {rho u, rho v, rho, rho E}
+// (conservationLaws/euler/euler.h:19-25).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cfloat>
+
+namespace hc {
+
+enum FluxKind { FLUX_ROE = 0, FLUX_SLAU = 1, FLUX_SLAU_REF = 2, FLUX_AUSMPUP = 3,
+                FLUX_RUSANOV = 4, FLUX_CENTRAL = 5, FLUX_COUNT = 6 };
+enum LimiterKind { LIM_NOLIMIT1 = 0, LIM_NOLIMIT2 = 1, LIM_NOLIMIT3 = 2, LIM_VANALBADA = 3,
+                   LIM_MINMOD = 4, LIM_SUPERBEE = 5, LIM_MC = 6, LIM_VANLEER = 7,
+                   LIM_VANLEER_REF = 8, LIM_CADA3 = 9, LIM_COUNT = 10 };
+enum BcKind { BC_PERIODIC = 0, BC_FIXED = 1, BC_RIEMANN = 2, BC_ENTROPY = 3, BC_WALL = 4 };
+
+template <class R> struct Lim;
+template <> struct Lim<double> {
+  __host__ __device__ static constexpr double tiny() { return DBL_MIN; }
+  __host__ __device__ static constexpr double huge() { return DBL_MAX; }
+};
+template <> struct Lim<float> {
+  __host__ __device__ static constexpr float tiny() { return FLT_MIN; }
+  __host__ __device__ static constexpr float huge() { return FLT_MAX; }
+};
+
+// Species<Euler> subset used on the path (conservationLaws/euler/euler.h:48-60)
+template <class R> struct Gas {
+  R gamma;   // ratio of specific heats
+  R gm1;     // gamma - 1
+  R gamma1;  // 1/(gamma-1)
+  R Rgas;    // gas constant
+  R minf;    // cut-off Mach number (AUSM+up)
+};
+
+// State<Euler,2> without the unused temperature (conservationLaws/euler/euler.h:62-83)
+template <class R> struct St { R p, r, h, u2, a2, u, v; };
+
+template <class R> struct Flux5 { R f[4]; R lam; };
+
+// set2State(primitive) (conservationLaws/euler/transforms/primitive.ipp:101-137)
+template <class R> __device__ __forceinline__ St<R> prim_state(const Gas<R>& g, R u, R v, R r, R p) {
+  St<R> s;
+  s.u = u; s.v = v;
+  s.u2 = u * u;
+  s.u2 += v * v;
+  const R k = R(0.5) * s.u2;
+  const R t = p / (r * g.Rgas);
+  s.a2 = g.gamma * g.Rgas * t;
+  s.h = s.a2 * g.gamma1 + k;
+  s.p = p; s.r = r;
+  return s;
+}
+
+// set2State(conserved) (conservationLaws/euler/transforms/conserved.ipp:31-76)
+template <class R> __device__ __forceinline__ St<R> cons_state(const Gas<R>& g, const R* qc) {
+  St<R> s;
+  const R r = qc[2], re = qc[3];
+  const R r1 = R(1) / r;
+  s.u = qc[0] * r1; s.v = qc[1] * r1;
+  s.u2 = s.u * s.u;
+  s.u2 += s.v * s.v;
+  const R k = R(0.5) * s.u2;
+  const R p = g.gm1 * (re - r * k);
+  const R t = p / (g.Rgas * r);
+  s.a2 = g.gamma * g.Rgas * t;
+  s.h = s.a2 * g.gamma1 + k;
+  s.p = p; s.r = r;
+  return s;
+}
+
+// state2Set<conserved> (conservationLaws/euler/transforms/conserved.ipp:2-29)
+template <class R> __device__ __forceinline__ void state_cons(const St<R>& s, R* qc) {
+  qc[0] = s.r * s.u; qc[1] = s.r * s.v; qc[2] = s.r; qc[3] = s.r * s.h - s.p;
+}
+
+// projectedVelocity (conservationLaws/base/base.h:148-158)
+template <class R> __device__ __forceinline__ R proj(R nx, R ny, const St<R>& s) { return nx * s.u + ny * s.v; }
+
+// exactFlux (conservationLaws/euler/fluxes/exactFlux.ipp:231-263)
+template <class R> __device__ __forceinline__ Flux5<R> exact_flux(R nx, R ny, const St<R>& s) {
+  Flux5<R> o;
+  const R a = sqrt(s.a2);
+  const R un = proj(nx, ny, s);
+  const R mn = s.r * un;
+  o.f[0] = mn * s.u + s.p * nx;
+  o.f[1] = mn * s.v + s.p * ny;
+  o.f[2] = mn;
+  o.f[3] = mn * s.h;
+  o.lam = fabs(un) + a;
+  return o;
+}
+
+// CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:25-37)
+template <class R> __device__ __forceinline__ Flux5<R> central_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
+  const Flux5<R> fl = exact_flux(nx, ny, l), fr = exact_flux(nx, ny, r);
+  Flux5<R> o;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) o.f[i] = (R(0.5) * (fl.f[i] + fr.f[i])) * A;
+  o.lam = fmax(fl.lam, fr.lam) * A;
+  return o;
+}
+
+// Roe flux = central + matrix dissipation (conservationLaws/base/fluxes/roeFlux.ipp:39-95),
+// with roeAverage and Harten's entropy fix (conservationLaws/euler/fluxes/roe.ipp:150-226)
+// and the characteristic transforms (conservationLaws/euler/transforms/primitive.ipp:142-313).
+// The Roe-averaged state keeps its velocity in the global frame while the jump
+// is rotated to the face frame, exactly as the reference composes them.
+template <class R> __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g, R nx, R ny, R A,
+                                                               const St<R>& l, const St<R>& r) {
+  const Flux5<R> c = central_flux(nx, ny, A, l, r);
+  // roe average
+  const R cr = sqrt(r.r / l.r);
+  const R wl = R(1) / (R(1) + cr);
+  const R wr = R(1) - wl;
+  const R ra = cr * l.r;
+  const R ua = wl * l.u + wr * r.u;
+  const R va = wl * l.v + wr * r.v;
+  R ka = ua * ua;
+  ka += va * va;
+  ka *= R(0.5);
+  const R ha = wl * l.h + wr * r.h;
+  const R a2a = g.gm1 * (ha - ka);
+  const R aa = sqrt(a2a);
+  // wave speeds and entropy fix
+  const R una = nx * ua + ny * va;
+  const R unl = proj(nx, ny, l), unr = proj(nx, ny, r);
+  const R al = sqrt(l.a2), ar = sqrt(r.a2);
+  R lam[4];
+  const R la0 = fabs(una);
+  lam[0] = la0; lam[3] = la0;
+  {
+    const R la1 = una - aa, ll1 = unl - al, lr1 = unr - ar;
+    const R le = R(0.05) * fmax(R(0), fmax(la1 - ll1, lr1 - la1));
+    const R laa = fabs(la1);
+    lam[1] = (laa > le) ? laa : R(0.5) * (le + laa * laa / le);
+  }
+  {
+    const R la2 = una + aa, ll2 = unl + al, lr2 = unr + ar;
+    const R le = R(0.05) * fmax(R(0), fmax(la2 - ll2, lr2 - la2));
+    const R laa = fabs(la2);
+    lam[2] = (laa > le) ? laa : R(0.5) * (le + laa * laa / le);
+  }
+  // face-aligned jump of conserved variables
+  const R tx = -ny, ty = nx;
+  const R d0 = r.r * r.u - l.r * l.u;
+  const R d1 = r.r * r.v - l.r * l.v;
+  const R d2 = r.r - l.r;
+  const R d3 = (r.r * r.h - r.p) - (l.r * l.h - l.p);
+  const R c0 = nx * d0 + ny * d1;
+  const R c1 = tx * d0 + ty * d1;
+  // conserved -> primitive about the average state
+  const R rho1 = R(1) / ra;
+  R cc = ka * d2 + d3;
+  const R du0 = (c0 - ua * d2) * rho1;
+  cc -= ua * c0;
+  const R du1 = (c1 - va * d2) * rho1;
+  cc -= va * c1;
+  const R dp = cc * g.gm1;
+  // primitive -> characteristic, scaled by the wave speeds
+  const R a1 = R(1) / aa;
+  const R w0 = lam[0] * ((g.gamma * (dp * a1 * a1 - d2)) * rho1);
+  const R w1 = lam[1] * (du0 - dp * rho1 * a1);
+  const R w2 = lam[2] * (du0 + dp * rho1 * a1);
+  const R w3 = lam[3] * du1;
+  // characteristic -> primitive -> conserved
+  const R dpp = R(0.5) * ra * aa * (w2 - w1);
+  const R drr = dpp / (aa * aa) - ra * w0 / g.gamma;
+  const R du = R(0.5) * (w1 + w2);
+  const R dv = w3;
+  const R e0 = ra * du + ua * drr;
+  const R e1 = ra * dv + va * drr;
+  R dk = ua * du;
+  dk += va * dv;
+  const R e3 = dpp * g.gamma1 + ra * dk + ka * drr;
+  // rotate back
+  const R f0 = nx * e0 + tx * e1;
+  const R f1 = ny * e0 + ty * e1;
+  const R s = R(-0.5) * A;
+  Flux5<R> o;
+  o.f[0] = c.f[0] + s * f0;
+  o.f[1] = c.f[1] + s * f1;
+  o.f[2] = c.f[2] + s * drr;
+  o.f[3] = c.f[3] + s * e3;
+  o.lam = fmax(c.lam, (fabs(una) + aa) * A);
+  return o;
+}
+
+// RusanovFlux (conservationLaws/base/fluxes/rusanovFlux.ipp:99-147)
+template <class R> __device__ __forceinline__ Flux5<R> rusanov_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
+  Flux5<R> o = central_flux(nx, ny, A, l, r);
+  const R lambda = fmax(fabs(proj(nx, ny, l)) + sqrt(l.a2), fabs(proj(nx, ny, r)) + sqrt(r.a2));
+  const R s = R(-0.5) * (lambda * A);
+  o.f[0] += s * (r.r * r.u - l.r * l.u);
+  o.f[1] += s * (r.r * r.v - l.r * l.v);
+  o.f[2] += s * (r.r - l.r);
+  o.f[3] += s * ((r.r * r.h - r.p) - (l.r * l.h - l.p));
+  return o;
+}
+
+// Mach splittings (conservationLaws/euler/fluxes/machSplittings.ipp:163-204)
+template <class R> __device__ __forceinline__ R ms_m1(R s, R M) { return R(0.5) * (M + s * fabs(M)); }
+template <class R> __device__ __forceinline__ R ms_m2(R s, R M) { return s * R(0.25) * (M + s) * (M + s); }
+template <class R> __device__ __forceinline__ R ms_m4(R s, R M, R beta) {
+  return ms_m2(s, M) * (R(1) - s * R(16) * beta * ms_m2(-s, M));
+}
+// (M1 + eps)/(|M| + eps) with eps the largest finite value
+template <class R> __device__ __forceinline__ R ms_p1(R s, R M) {
+  const R eps = Lim<R>::huge();
+  return (ms_m1(s, M) + eps) / (fabs(M) + eps);
+}
+template <class R> __device__ __forceinline__ R ms_p3(R s, R M) { return ms_m2(s, M) * (s * R(2) - M); }
+template <class R> __device__ __forceinline__ R ms_p5(R s, R M, R alpha) {
+  return ms_p3(s, M) - s * R(16) * alpha * M * ms_m2(s, M) * ms_m2(-s, M);
+}
+
+// SLAU2 with (Convective, Acoustic) tags (conservationLaws/euler/fluxes/slau.ipp:4-161).
+// by_mdot=false: literal reference upwinding by the sign of ua (slau.ipp:124-125);
+// by_mdot=true: upwinding by the sign of the interface mass flux.
+template <class R, bool by_mdot>
+__device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
+  const R ua = sqrt(R(0.5) * (l.u2 + r.u2));
+  const R al = sqrt(l.a2), ar = sqrt(r.a2);
+  const R aa = R(0.5) * (al + ar);
+  const R aa1 = R(1) / aa;
+  const R ma = ua * aa1;
+  const R ma_hat = fmin(R(1), ma);
+  const R unl = proj(nx, ny, l), unr = proj(nx, ny, r);
+  const R ml = unl * aa1, mr = unr * aa1;
+  const R una = (l.r * fabs(unl) + r.r * fabs(unr)) / (l.r + r.r);
+  const R chi = (R(1) - ma_hat) * (R(1) - ma_hat);
+  const R gs = -fmax(fmin(ml, R(0)), R(-1)) * fmin(fmax(mr, R(0)), R(1));
+  const R dr = r.r - l.r, dp = r.p - l.p;
+  const R mdot_c = l.r * unl + r.r * unr;
+  const R mdot = R(0.5) * ((mdot_c - una * dr) * (R(1) - gs) - chi * dp * aa1) * A;
+  const R betal = (fabs(ml) > R(1)) ? ms_p1(R(1), ml) : ms_p3(R(1), ml);
+  const R betar = (fabs(mr) > R(1)) ? ms_p1(R(-1), mr) : ms_p3(R(-1), mr);
+  const R p_c = l.p + r.p;
+  const R p_dp = (betal - betar) * dp;
+  const R p_du = -ma * (betal + betar - R(1)) * (p_c);
+  const R pa = R(0.5) * (p_c - p_dp - p_du) * A;
+  const bool left = by_mdot ? (mdot > R(0)) : (ua > R(0));
+  const St<R>& w = left ? l : r;
+  Flux5<R> o;
+  o.f[0] = mdot * w.u + pa * nx;
+  o.f[1] = mdot * w.v + pa * ny;
+  o.f[2] = mdot;
+  o.f[3] = mdot * w.h;
+  o.lam = (sqrt(fmax(l.a2, r.a2)) + fmax(fabs(unl), fabs(unr))) * A;
+  return o;
+}
+
+// AUSM+up with (Convective, Convective) tags (conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171)
+template <class R> __device__ __forceinline__ Flux5<R> ausmpup_flux(const Gas<R>& g, R nx, R ny, R A,
+                                                                   const St<R>& l, const St<R>& r) {
+  const R alpha0 = R(0.1875), beta = R(0.125), Ku = R(0.75 * 2.), Kp = R(0.25), sigma = R(1.0);
+  const R ascoeff = R(2) * g.gm1 / (g.gamma + R(1));
+  const R unl = proj(nx, ny, l), unr = proj(nx, ny, r);
+  const R als2 = ascoeff * l.h, ars2 = ascoeff * r.h;
+  const R als = als2 / fmax(unl, sqrt(als2));
+  const R ars = ars2 / fmax(-unr, sqrt(ars2));
+  const R ra = R(0.5) * (l.r + r.r);
+  const R as = fmin(ars, als);
+  const R ml = unl / as, mr = unr / as;
+  const R m0 = sqrt(R(0.5) * (ml * ml + mr * mr));
+  const R m0c = (m0 < g.minf) ? g.minf : ((R(1) < m0) ? R(1) : m0);
+  const R fa = m0c * (R(2) - m0c);
+  const bool lsup = fabs(ml) > R(1), rsup = fabs(mr) > R(1);
+  const R mlp = lsup ? ms_m1(R(1), ml) : ms_m4(R(1), ml, beta);
+  const R mrm = rsup ? ms_m1(R(-1), mr) : ms_m4(R(-1), mr, beta);
+  const R delp = r.p - l.p;
+  const R mp = Kp * fmax(R(1) - sigma * m0 * m0, R(0)) * delp / (fa * ra * as * as);
+  const R uaf = as * (mlp + mrm - mp) * A;
+  const R alpha = alpha0 * (R(5) * fa * fa - R(4));
+  const R plp = lsup ? ms_p1(R(1), ml) : ms_p5(R(1), ml, alpha);
+  const R prm = rsup ? ms_p1(R(-1), mr) : ms_p5(R(-1), mr, alpha);
+  const R pu = Ku * plp * prm * ra * (fa * as) * (unr - unl);
+  const R pa = (plp * l.p + prm * r.p - pu) * A;
+  const St<R>& w = (uaf > R(0)) ? l : r;
+  const R mdot = uaf * w.r;
+  Flux5<R> o;
+  o.f[0] = mdot * w.u + pa * nx;
+  o.f[1] = mdot * w.v + pa * ny;
+  o.f[2] = mdot;
+  o.f[3] = mdot * w.h;
+  const R lmd = R(0.5) * (m0c + R(1)) / fa;
+  const R amax = sqrt(fmax(as * as, fmax(l.a2, r.a2)));
+  o.lam = (lmd * amax + fmax(fabs(uaf), fmax(fabs(unl), fabs(unr)))) * A;
+  return o;
+}
+
+template <class R, int FK>
+__device__ __forceinline__ Flux5<R> face_flux(const Gas<R>& g, R nx, R ny, R A, const St<R>& l, const St<R>& r) {
+  if constexpr (FK == FLUX_ROE) return roe_flux(g, nx, ny, A, l, r);
+  else if constexpr (FK == FLUX_SLAU) return slau_flux<R, true>(nx, ny, A, l, r);
+  else if constexpr (FK == FLUX_SLAU_REF) return slau_flux<R, false>(nx, ny, A, l, r);
+  else if constexpr (FK == FLUX_AUSMPUP) return ausmpup_flux(g, nx, ny, A, l, r);
+  else if constexpr (FK == FLUX_RUSANOV) return rusanov_flux(nx, ny, A, l, r);
+  else return central_flux(nx, ny, A, l, r);
+}
+
+// Slope limiters (limiters/limiter.ipp:141-297), called as limit(central, biased).
+// LIM_VANLEER is the harmonic-mean slope (a|b|+|a|b)/(|a|+|b|+eps);
+// LIM_VANLEER_REF the literal reference expression (limiter.ipp:216-224).
+template <class R> __device__ __forceinline__ R limit(int kind, R a, R b) {
+  const R tiny = Lim<R>::tiny();
+  switch (kind) {
+    case LIM_NOLIMIT1: return R(0);
+    case LIM_NOLIMIT2: return R(0.5) * (a + b);
+    case LIM_NOLIMIT3: return R(0.33333333333333333) * (R(2) * a + b);
+    case LIM_VANALBADA: return (a * b < R(0)) ? R(0) : (b * (a * a) + a * (b * b)) / (a * a + b * b + tiny);
+    case LIM_MINMOD: return (a > R(0)) ? fmin(a, fmax(b, R(0))) : fmax(a, fmin(b, R(0)));
+    case LIM_SUPERBEE:
+      return (a > R(0)) ? fmax(R(0), fmax(fmin(R(2) * a, b), fmin(R(2) * b, a)))
+                        : fmin(R(0), fmin(fmax(R(2) * a, b), fmax(R(2) * b, a)));
+    case LIM_MC:
+      return (a > R(0)) ? fmax(R(0), fmin(R(0.5) * (a + b), fmin(R(2) * b, R(2) * a)))
+                        : fmin(R(0), fmax(R(0.5) * (a + b), fmax(R(2) * b, R(2) * a)));
+    case LIM_VANLEER: return (a * fabs(b) + fabs(a) * b) / (fabs(a) + fabs(b) + tiny);
+    case LIM_VANLEER_REF: return (b + fabs(b)) / (a + fabs(b) + tiny);
+    case LIM_CADA3: {
+      const R gam = R(1.5), c1 = R(-2. / 7.), c2 = R(0.4), c3 = R(3) * gam - R(2);
+      const R u = (a > R(0)) ? a : -a;
+      const R v = (a > R(0)) ? b : -b;
+      R w;
+      if (fabs(a) + fabs(b) > R(0)) {
+        if (v < R(-2) * u) w = R(0);
+        else if (v < c1 * u) w = (v + R(2) * u) / R(3);
+        else if (v < R(0)) w = R(-2) * v;
+        else if (v < c2 * u) w = R(2) * v;
+        else if (v < c3 * u) w = (v + R(2) * u) / R(3);
+        else w = gam * u;
+      } else {
+        w = (v + R(2) * u) / R(3);
+      }
+      return (a <= R(0)) ? -w : w;
+    }
+    default: return R(0);
+  }
+}
+
+// Roe average of two primitive states in the face frame, used by the far-field
+// boundary updates (conservationLaws/euler/fluxes/roe.ipp:150-196).
+template <class R> __device__ __forceinline__ void roe_avg_vel(const St<R>& l, const St<R>& r, R* uav, R* u2,
+                                                              R* a2, const Gas<R>& g) {
+  const R cr = sqrt(r.r / l.r);
+  const R wl = R(1) / (R(1) + cr);
+  const R wr = R(1) - wl;
+  const R ua = wl * l.u + wr * r.u;
+  const R va = wl * l.v + wr * r.v;
+  R ka = ua * ua;
+  ka += va * va;
+  ka *= R(0.5);
+  const R ha = wl * l.h + wr * r.h;
+  *a2 = g.gm1 * (ha - ka);
+  uav[0] = ua; uav[1] = va;
+  *u2 = R(2) * ka;
+}
+
+// Riemann-invariant far field (conservationLaws/euler/boundary/riemann.ipp:18-113)
+// and entropy/pressure far field (entropy.ipp:18-88).  (nx,ny) points into the
+// domain; qi, qf, qb are primitive.
+template <class R, int BK>
+__device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, R ny, const R* qi, const R* qf, R* qb) {
+  const R tx = -ny, ty = nx;
+  const R ri[4] = {nx * qi[0] + ny * qi[1], tx * qi[0] + ty * qi[1], qi[2], qi[3]};
+  const R rf[4] = {nx * qf[0] + ny * qf[1], tx * qf[0] + ty * qf[1], qf[2], qf[3]};
+  const St<R> sI = prim_state(g, ri[0], ri[1], ri[2], ri[3]);
+  const St<R> sF = prim_state(g, rf[0], rf[1], rf[2], rf[3]);
+  R uav[2], u2a, a2a;
+  roe_avg_vel(sI, sF, uav, &u2a, &a2a, g);
+  const R thr = (BK == BC_RIEMANN) ? R(0.001) : R(0.0001);
+  if ((uav[0] / sqrt(u2a)) < thr) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) qb[k] = qi[k];
+    return;
+  }
+  const R ma = uav[0] / sqrt(a2a);
+  const bool inflow = ma > R(0);
+  const R* quw = inflow ? qf : qi;
+  if (fabs(ma) > R(1)) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) qb[k] = quw[k];
+    return;
+  }
+  const St<R>& sU = inflow ? sF : sI;
+  R b[4];
+  if constexpr (BK == BC_RIEMANN) {
+    const R ai = sqrt(sI.a2), af = sqrt(sF.a2);
+    const R rim = sI.u - R(2) * ai * g.gamma1;
+    const R rip = sF.u + R(2) * af * g.gamma1;
+    const R ub = R(0.5) * (rim + rip);
+    const R ab = R(0.25) * g.gm1 * (rip - rim);
+    const R sb = sU.a2 / (g.gamma * pow(sU.r, g.gm1));
+    const R rb = pow(ab * ab / (g.gamma * sb), g.gamma1);
+    const R pb = rb * ab * ab / g.gamma;
+    b[0] = ub; b[1] = sU.v; b[2] = rb; b[3] = pb;
+  } else {
+    const St<R>& sD = inflow ? sI : sF;
+    const R pb = sD.p;
+    const R sb = sU.a2 / (g.gamma * pow(sU.r, g.gm1));
+    const R rb = pow(pb / sb, R(1) / g.gamma);
+    b[0] = sU.u; b[1] = sU.v; b[2] = rb; b[3] = pb;
+  }
+  qb[0] = nx * b[0] + tx * b[1];
+  qb[1] = ny * b[0] + ty * b[1];
+  qb[2] = b[2]; qb[3] = b[3];
+}
+
+// Inviscid wall (conservationLaws/euler/boundary/inviscidWall.ipp:33-72): pressure
+// flux only, from the interior state moved to the face (qw primitive).
+template <class R> __device__ __forceinline__ Flux5<R> wall_flux(const Gas<R>& g, R nx, R ny, R A, const R* qw) {
+  const St<R> s = prim_state(g, qw[0], qw[1], qw[2], qw[3]);
+  Flux5<R> o;
+  o.f[0] = A * s.p * nx;
+  o.f[1] = A * s.p * ny;
+  o.f[2] = R(0);
+  o.f[3] = R(0);
+  o.lam = A * (fabs(proj(nx, ny, s)) + sqrt(s.a2));
+  return o;
+}
+
+}  // namespace hc

@@ -1,0 +1,144 @@
+"""Host-side mirror of the reference's integrate() interface over the C ABI.
+
+The reference drives one run as (timestepping/rungeKutta.h:37-51)
+
+    integrate(policy, UnsteadyTimeControls{nTimesteps, cfl}, rungeKutta,
+              make_muscl_flux(Limiter{}, Flux{}), boundaryConditions, species,
+              mesh, solutionField)
+
+``Solver`` takes the same ingredients -- flux and limiter names, RK table,
+CFL, species, mesh nodes, boundary-condition types with their reference
+states, and the primitive solution field -- and runs them on the GPU through
+libhcgb300.so.  Errors raise ``HCError`` (the C ABI returns status codes).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import BC, DTMODE, FLUX, LIMITER, PRECISION, RK, Config, HCError, StepStats, check
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Mesh:
+    """Structured 2D mesh: (ni+1) x (nj+1) nodes, node (i,j) at nodes[i, j] = (x, y)."""
+
+    def __init__(self, nodes: np.ndarray):
+        nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        if nodes.ndim != 3 or nodes.shape[2] != 2:
+            raise ValueError("nodes must have shape (ni+1, nj+1, 2)")
+        self.nodes = nodes
+        self.ni, self.nj = nodes.shape[0] - 1, nodes.shape[1] - 1
+
+    @classmethod
+    def cylinder(cls, nr: int, nth: int, rc: float, rb: float, stretch: float = 1.0) -> "Mesh":
+        """O-grid around a cylinder (make_cylinder_mesh, mesh/generate/twoD.h:223-263)."""
+        out = np.empty((nr + 1, nth + 1, 2))
+        check(_capi.load().hc_mesh_cylinder_nodes(nr, nth, rc, rb, stretch, _dptr(out)))
+        return cls(out)
+
+    @classmethod
+    def linspace(cls, nx: int, ny: int, lox: float, hix: float, loy: float, hiy: float) -> "Mesh":
+        """Uniform Cartesian mesh (make_linspace_mesh, mesh/generate/twoD.h:99-124)."""
+        out = np.empty((nx + 1, ny + 1, 2))
+        check(_capi.load().hc_mesh_linspace_nodes(nx, ny, lox, hix, loy, hiy, _dptr(out)))
+        return cls(out)
+
+    def centres(self) -> np.ndarray:
+        """Vertex centroids of the cells, shape (2, ni, nj)."""
+        p = self.nodes
+        c = 0.25 * p[:-1, :-1] + 0.25 * p[1:, :-1] + 0.25 * p[:-1, 1:] + 0.25 * p[1:, 1:]
+        return np.moveaxis(c, 2, 0).copy()
+
+    def nface(self, side: int) -> int:
+        return self.nj if side < 2 else self.ni
+
+
+class Solver:
+    """One mesh, its boundary conditions and state, advanced by explicit RK on the GPU."""
+
+    def __init__(self, mesh: Mesh, bc, ref=None, flux="roe", limiter="vanleer", rk="ssp34",
+                 precision="fp64", dt="global", cfl=0.5, species=(1.4, 287.058, 1e-4), stream=None):
+        self.lib = _capi.load()
+        self.mesh = mesh
+        self.precision = precision
+        cfg = Config(FLUX[flux] if isinstance(flux, str) else int(flux),
+                     LIMITER[limiter] if isinstance(limiter, str) else int(limiter),
+                     RK[rk] if isinstance(rk, str) else int(rk),
+                     PRECISION[precision], DTMODE[dt], float(cfl))
+        h = C.c_void_p()
+        check(self.lib.hc_context_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        if stream is not None:
+            check(self.lib.hc_set_stream(self.h, C.c_void_p(int(stream))))
+        check(self.lib.hc_mesh_upload(self.h, mesh.ni, mesh.nj, _dptr(mesh.nodes)))
+        check(self.lib.hc_set_species(self.h, *[float(s) for s in species]))
+        bct = (C.c_int * 4)(*[BC[b] if isinstance(b, str) else int(b) for b in bc])
+        self._refs = []
+        ptrs = (C.POINTER(C.c_double) * 4)()
+        for s in range(4):
+            r = None if ref is None else ref[s]
+            if r is None:
+                ptrs[s] = C.POINTER(C.c_double)()
+            else:
+                arr = np.ascontiguousarray(np.broadcast_to(
+                    np.asarray(r, dtype=np.float64).reshape(4, -1), (4, mesh.nface(s))))
+                self._refs.append(arr)
+                ptrs[s] = _dptr(arr)
+        check(self.lib.hc_set_bcs(self.h, bct, ptrs))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.hc_context_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def set_stream(self, stream) -> None:
+        check(self.lib.hc_set_stream(self.h, C.c_void_p(int(stream) if stream else 0)))
+
+    # -- solution field ------------------------------------------------------
+    def set_state(self, prim: np.ndarray) -> None:
+        a = np.ascontiguousarray(prim, dtype=np.float64)
+        if a.shape != (4, self.mesh.ni, self.mesh.nj):
+            raise ValueError(f"state must have shape (4, {self.mesh.ni}, {self.mesh.nj})")
+        check(self.lib.hc_state_upload(self.h, _dptr(a)))
+
+    def get_state(self) -> np.ndarray:
+        out = np.empty((4, self.mesh.ni, self.mesh.nj))
+        check(self.lib.hc_state_download(self.h, _dptr(out)))
+        return out
+
+    def set_state_device(self, ptr: int) -> None:
+        check(self.lib.hc_state_upload_device(self.h, C.c_void_p(ptr)))
+
+    def get_state_device(self, ptr: int) -> None:
+        check(self.lib.hc_state_download_device(self.h, C.c_void_p(ptr)))
+
+    # -- path ----------------------------------------------------------------
+    def residual(self) -> np.ndarray:
+        """Flux sums (4 conserved planes) and spectral-radius sum of the current state."""
+        out = np.empty((5, self.mesh.ni, self.mesh.nj))
+        check(self.lib.hc_residual(self.h, _dptr(out)))
+        return out
+
+    def step(self, n: int = 1) -> StepStats:
+        st = StepStats()
+        check(self.lib.hc_step(self.h, int(n), C.byref(st)))
+        return st
+
+    def step_async(self, n: int = 1) -> None:
+        check(self.lib.hc_step_async(self.h, int(n)))
+
+    def sync(self) -> StepStats:
+        st = StepStats()
+        check(self.lib.hc_sync(self.h, C.byref(st)))
+        return st
+
+
+__all__ = ["Mesh", "Solver", "HCError"]

@@ -1,0 +1,137 @@
+/* hc.h -- C ABI of the GB300 residual-and-timestep path.
+ *
+ * One context owns one 2D structured mesh, its boundary conditions, a solution
+ * state and the device buffers of an explicit Runge-Kutta integrator.  All
+ * calls are synchronous unless named *_async; none throws; every function
+ * returns an hc_status and hc_last_error_string() describes the last failure
+ * of the calling thread.  A context is not thread-safe; distinct contexts are
+ * independent.  Arrays are plain host pointers unless the name ends in _device.
+ *
+ * The reference (lacrymose/hyperboliConvergence, header-only C++20) has no ABI;
+ * each entry point below replaces the C++ interface named beside it.
+ *
+ * Array layouts: cell (i,j) of an ni x nj mesh is element i*nj + j; state
+ * arrays are 4 planes of ni*nj values; node arrays hold (ni+1)*(nj+1) points
+ * as x,y pairs, node (i,j) at 2*(i*(nj+1)+j).
+ */
+#ifndef HC_H
+#define HC_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct hc_ctx hc_ctx;
+
+typedef enum {
+  HC_OK = 0,
+  HC_ERR_ARG = 1,         /* invalid argument or call order */
+  HC_ERR_CUDA = 2,        /* CUDA runtime failure */
+  HC_ERR_NONPHYSICAL = 3, /* a step produced rho<=0, p<=0 or a non-finite value */
+  HC_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
+  HC_ERR_UNSUPPORTED = 5  /* combination not built */
+} hc_status;
+
+/* Interface flux (FluxFunctor, conservationLaws/base/concepts.h:97-107) */
+typedef enum {
+  HC_FLUX_ROE = 0,      /* RoeFlux<Euler>, conservationLaws/base/fluxes/roeFlux.ipp:39-95 */
+  HC_FLUX_SLAU = 1,     /* SLAU2 upwinded by the sign of the mass flux */
+  HC_FLUX_SLAU_REF = 2, /* Slau<Convective,Acoustic> as written, conservationLaws/euler/fluxes/slau.ipp:4-161 */
+  HC_FLUX_AUSMPUP = 3,  /* AusmPlusUP<Convective,Convective>, conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171 */
+  HC_FLUX_RUSANOV = 4,  /* RusanovFlux<Euler>, conservationLaws/base/fluxes/rusanovFlux.ipp:99-147 */
+  HC_FLUX_CENTRAL = 5   /* CentralFlux<Euler>, conservationLaws/base/fluxes/centralFlux.ipp:25-37 */
+} hc_flux;
+
+/* Slope limiter (VariableLimiterInterface, limiters/limiter.h:14-28) */
+typedef enum {
+  HC_LIM_NOLIMIT1 = 0, HC_LIM_NOLIMIT2 = 1, HC_LIM_NOLIMIT3 = 2, HC_LIM_VANALBADA = 3,
+  HC_LIM_MINMOD = 4, HC_LIM_SUPERBEE = 5, HC_LIM_MC = 6,
+  HC_LIM_VANLEER = 7,     /* harmonic-mean van Leer slope */
+  HC_LIM_VANLEER_REF = 8, /* Limiters::VanLeer2 as written, limiters/limiter.ipp:216-224 */
+  HC_LIM_CADA3 = 9
+} hc_limiter;
+
+/* Runge-Kutta table (ODE::Explicit, ode.h:107-197) */
+typedef enum { HC_RK_SSP11 = 0, HC_RK_SSP22 = 1, HC_RK_SSP33 = 2, HC_RK_SSP34 = 3 } hc_rk;
+
+typedef enum { HC_FP64 = 0, HC_FP32 = 1 } hc_precision;
+
+/* global: dt = cfl / max(lambda/V) at stage 0 (timestepping/rungeKutta.h:131-133);
+ * local: per-cell cfl/lambda (spatial/eulerForwardUpdate.h:117-168) */
+typedef enum { HC_DT_GLOBAL = 0, HC_DT_LOCAL = 1 } hc_dtmode;
+
+/* Boundary condition of a mesh side (EulerBCs, conservationLaws/euler/euler.h:34-41).
+ * Sides: 0 = i low, 1 = i high, 2 = j low, 3 = j high; periodic pairs (0,1), (2,3). */
+typedef enum { HC_BC_PERIODIC = 0, HC_BC_FIXED = 1, HC_BC_RIEMANN = 2, HC_BC_ENTROPY = 3, HC_BC_WALL = 4 } hc_bc;
+
+typedef struct {
+  int flux;      /* hc_flux */
+  int limiter;   /* hc_limiter */
+  int rk;        /* hc_rk */
+  int precision; /* hc_precision */
+  int dt_mode;   /* hc_dtmode */
+  double cfl;    /* UnsteadyTimeControls::cfl (controls.h:11-19) */
+} hc_config;
+
+typedef struct {
+  double dt;        /* last global dt (global mode) or the smallest local dt */
+  double t;         /* accumulated time (global mode) */
+  double resnorm;   /* L2 norm of the stage-0 density residual of the last step */
+  int status;       /* hc_status of the device checks */
+  int bad_cell;     /* first non-physical cell when status == HC_ERR_NONPHYSICAL */
+  long long kernel_launches; /* kernels this context has launched so far */
+} hc_step_stats;
+
+/* Context lifetime.  Replaces the integrate() set-up of timestepping/rungeKutta.h:44-79. */
+int hc_context_create(const hc_config* cfg, hc_ctx** out);
+int hc_context_destroy(hc_ctx* ctx);
+/* Run the context's kernels on this CUDA stream (a cudaStream_t; 0 = the context's own). */
+int hc_set_stream(hc_ctx* ctx, void* stream);
+
+/* Mesh<2,Real> nodes (mesh/mesh.h:283-321); cells and face metrics are derived on the
+ * device: geom::volume/surface, dual, xmetrics (geometry/volume.ipp:55-96,
+ * geometry/surface.ipp:12-29, mesh/dual.ipp:42-83, spatial/lsqMetrics.h:119-251). */
+int hc_mesh_upload(hc_ctx* ctx, int ni, int nj, const double* nodes_xy);
+
+/* Species<Euler> (conservationLaws/euler/euler.h:48-60): gamma, R, minf. */
+int hc_set_species(hc_ctx* ctx, double gamma, double gas_constant, double minf);
+
+/* SolutionField::bcTypes and the reference layer of SolutionField::boundary
+ * (solutionField/solutionField.h:56-91).  ref[side] holds 4 planes of primitive
+ * values, one per boundary face (nj faces on sides 0/1, ni on 2/3); NULL for
+ * periodic or wall sides. */
+int hc_set_bcs(hc_ctx* ctx, const int bc_type[4], const double* const ref[4]);
+
+/* SolutionField::interior in the primitive basis {u, v, rho, p}. */
+int hc_state_upload(hc_ctx* ctx, const double* prim_soa);
+int hc_state_download(hc_ctx* ctx, double* prim_soa);
+/* Same through device pointers of the context's precision (no host copy). */
+int hc_state_upload_device(hc_ctx* ctx, const void* prim_soa_device);
+int hc_state_download_device(hc_ctx* ctx, void* prim_soa_device);
+
+/* One residual evaluation of the current state: residualCalc (spatial/residualCalc.h:45-69)
+ * including the boundary update (spatial/boundary/boundaryUpdate.h:137-266).
+ * out: 5 planes -- 4 conserved flux sums and the spectral-radius sum. */
+int hc_residual(hc_ctx* ctx, double* out5);
+
+/* nsteps explicit RK steps: the time loop of integrate() (timestepping/rungeKutta.h:96-164). */
+int hc_step(hc_ctx* ctx, int nsteps, hc_step_stats* stats);
+/* Enqueue nsteps without waiting; hc_sync waits and reports. */
+int hc_step_async(hc_ctx* ctx, int nsteps);
+int hc_sync(hc_ctx* ctx, hc_step_stats* stats);
+
+/* Mesh generators: make_cylinder_mesh (mesh/generate/twoD.h:223-263), radial
+ * spacing stretched geometrically when stretch != 1; make_linspace_mesh
+ * (mesh/generate/twoD.h:99-124). */
+int hc_mesh_cylinder_nodes(int nr, int nth, double rc, double rb, double stretch, double* nodes_xy);
+int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, double hiy, double* nodes_xy);
+
+const char* hc_last_error_string(void);
+const char* hc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HC_H */

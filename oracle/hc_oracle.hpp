@@ -1,0 +1,640 @@
+// hc_oracle.hpp -- CPU oracle for the residual-and-timestep path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker that the CUDA path is
+// compared against; it is never linked into the product library.  Only the
+// tests, the smoke check and the CPU-baseline leg of the benchmark load it.
+//
+// It restates, in plain scalar C++, the algorithm of the reference solver
+// (lacrymose/hyperboliConvergence, cpp/inc) for 2D structured meshes:
+// pointwise Euler physics, limiters, least-squares gradients, MUSCL faces,
+// residual accumulation, boundary conditions, spectral radius and the
+// alpha/beta Runge-Kutta integrator.  Operation order follows the reference
+// expression by expression so that, built without contraction or fast-math,
+// the pointwise functions reproduce the reference bit for bit (pinned by the
+// golden vectors generated from the reference's own headers).
+//
+// Variable order everywhere (reference conservationLaws/euler/euler.h:19-25):
+//   primitive  = { u, v, rho, p }
+//   conserved  = { rho*u, rho*v, rho, rho*E }
+// Storage order of 2D arrays: cell (i,j) at i*nj + j (j fastest), as
+// par::Array (parallalg/array.h:46-59).
+#pragma once
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+namespace hco {
+
+// ---------------------------------------------------------------- enums
+enum Flux { FLUX_ROE = 0, FLUX_SLAU = 1, FLUX_SLAU_REF = 2, FLUX_AUSMPUP = 3,
+            FLUX_RUSANOV = 4, FLUX_CENTRAL = 5 };
+enum Limiter { LIM_NOLIMIT1 = 0, LIM_NOLIMIT2 = 1, LIM_NOLIMIT3 = 2, LIM_VANALBADA = 3,
+               LIM_MINMOD = 4, LIM_SUPERBEE = 5, LIM_MC = 6, LIM_VANLEER = 7,
+               LIM_VANLEER_REF = 8, LIM_CADA3 = 9 };
+enum BC { BC_PERIODIC = 0, BC_FIXED = 1, BC_RIEMANN = 2, BC_ENTROPY = 3, BC_WALL = 4 };
+enum RK { RK_SSP11 = 0, RK_SSP22 = 1, RK_SSP33 = 2, RK_SSP34 = 3 };
+enum DtMode { DT_GLOBAL = 0, DT_LOCAL = 1 };
+
+// ---------------------------------------------------------------- types
+// Species<Euler> (conservationLaws/euler/euler.h:48-60)
+template <class R> struct Species {
+  R gamma, minf, lref, nu, pr, dt, Rgas, gamma1;
+};
+
+// get_air_species (conservationLaws/euler/species.ipp:363-379)
+template <class R> Species<R> air_species() {
+  Species<R> s;
+  s.gamma = 1.4; s.minf = 0.0001; s.lref = 1.; s.pr = 0.7; s.nu = 1.81e-5;
+  s.dt = std::numeric_limits<R>::max(); s.Rgas = 287.058;
+  s.gamma1 = 1. / (s.gamma - 1.);
+  return s;
+}
+
+// State<Euler,2> (conservationLaws/euler/euler.h:62-83)
+template <class R> struct State { R p, r, t, h, u2, a2, u[2]; };
+
+// geom::Surface / geom::Volume (geometry/geometry.h:64-81)
+template <class R> struct Face { R area; R c[2]; R n[2]; R t[2]; };
+template <class R> struct Cell { R vol; R c[2]; };
+
+// FluxResult (conservationLaws/base/base.h:57-83)
+template <class R> struct FluxRes { R f[4]; R lam; };
+
+// ---------------------------------------------------------------- geometry
+// geom::surface(p0,p1) (geometry/surface.ipp:12-29)
+template <class R> Face<R> surface(const R* p0, const R* p1) {
+  Face<R> s;
+  const R t0x = p1[0] - p0[0], t0y = p1[1] - p0[1];
+  const R t1x = p0[0] - p1[0], t1y = p0[1] - p1[1];
+  R d = 0; d += t0x * t0x; d += t0y * t0y;
+  const R l = std::sqrt(d);
+  const R l1 = 1. / l;
+  s.area = l;
+  s.c[0] = p0[0] + 0.5 * t0x;
+  s.c[1] = p0[1] + 0.5 * t0y;
+  const R ux = l1 * t1x, uy = l1 * t1y;  // l1*tangent1
+  s.n[0] = -uy; s.n[1] = ux;               // orthog (geometry/operations.ipp:140-144)
+  s.t[0] = l1 * t0x; s.t[1] = l1 * t0y;
+  return s;
+}
+
+// geom::volume(p0..p3) (geometry/volume.ipp:55-96): bilinear shape functions
+// at the element centre (fem/fem.h:14-77).  The value is |J(0,0)|, which is a
+// quarter of the quad's area; it is kept as the reference defines it.
+template <class R> Cell<R> volume(const R* p0, const R* p1, const R* p2, const R* p3) {
+  // shape functions n2 and derivatives dn2 evaluated at (0,0): exact binary fractions
+  const R u[4] = {0.25, 0.25, 0.25, 0.25};
+  const R du[4][2] = {{-0.25, -0.25}, {0.25, -0.25}, {-0.25, 0.25}, {0.25, 0.25}};
+  const R* p[4] = {p0, p1, p2, p3};
+  Cell<R> c;
+  for (int i = 0; i < 2; ++i) {
+    R com = 0;
+    for (int k = 0; k < 4; ++k) com += u[k] * p[k][i];
+    c.c[i] = com;
+  }
+  R tg[2][2] = {{0, 0}, {0, 0}};
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j)
+      for (int k = 0; k < 4; ++k) tg[i][j] += du[k][i] * p[k][j];
+  c.vol = std::fabs(tg[0][0] * tg[1][1] - tg[0][1] * tg[1][0]);
+  return c;
+}
+
+// ---------------------------------------------------------------- transforms
+// set2State(primitive) (conservationLaws/euler/transforms/primitive.ipp:101-137)
+template <class R> State<R> prim2state(const Species<R>& sp, const R* q) {
+  State<R> s;
+  s.u2 = 0;
+  for (int i = 0; i < 2; ++i) { s.u[i] = q[i]; s.u2 += q[i] * q[i]; }
+  const R k = 0.5 * s.u2;
+  const R r = q[2], p = q[3];
+  const R t = p / (r * sp.Rgas);
+  const R a2 = sp.gamma * sp.Rgas * t;
+  const R h = a2 * sp.gamma1 + k;
+  s.h = h; s.p = p; s.r = r; s.t = t; s.a2 = a2;
+  return s;
+}
+
+// set2State(conserved) (conservationLaws/euler/transforms/conserved.ipp:31-76)
+template <class R> State<R> cons2state(const Species<R>& sp, const R* qc) {
+  State<R> s;
+  const R r = qc[2], re = qc[3];
+  const R r1 = 1. / r;
+  s.u2 = 0;
+  for (int i = 0; i < 2; ++i) s.u[i] = qc[i] * r1;
+  for (int i = 0; i < 2; ++i) s.u2 += s.u[i] * s.u[i];
+  const R k = 0.5 * s.u2;
+  const R p = (sp.gamma - 1.) * (re - r * k);
+  const R t = p / (sp.Rgas * r);
+  const R a2 = sp.gamma * sp.Rgas * t;
+  const R h = a2 * sp.gamma1 + k;
+  s.p = p; s.r = r; s.t = t; s.h = h; s.a2 = a2;
+  return s;
+}
+
+// state2Set<conserved> (conservationLaws/euler/transforms/conserved.ipp:2-29)
+template <class R> void state2cons(const State<R>& s, R* qc) {
+  const R re = s.r * s.h - s.p;
+  for (int i = 0; i < 2; ++i) qc[i] = s.r * s.u[i];
+  qc[2] = s.r; qc[3] = re;
+}
+
+// state2Set<primitive> (conservationLaws/euler/transforms/primitive.ipp:82-98)
+template <class R> void state2prim(const State<R>& s, R* qp) {
+  qp[0] = s.u[0]; qp[1] = s.u[1]; qp[2] = s.r; qp[3] = s.p;
+}
+
+template <class R> void prim2cons(const Species<R>& sp, const R* qp, R* qc) {
+  state2cons(prim2state(sp, qp), qc);
+}
+template <class R> void cons2prim(const Species<R>& sp, const R* qc, R* qp) {
+  state2prim(cons2state(sp, qc), qp);
+}
+
+// projectedVelocity (conservationLaws/base/base.h:148-158)
+template <class R> R proj_vel(const R* n, const State<R>& s) {
+  R un = 0;
+  for (int i = 0; i < 2; ++i) un += n[i] * s.u[i];
+  return un;
+}
+
+// spectralRadius (conservationLaws/euler/euler.h:161-166)
+template <class R> R spec_rad(const R* n, const State<R>& s) {
+  return std::abs(proj_vel(n, s)) + std::sqrt(s.a2);
+}
+
+// wavespeeds (conservationLaws/euler/euler.h:168-181)
+template <class R> void wavespeeds(const R* n, const State<R>& s, R* w) {
+  const R u = proj_vel(n, s);
+  const R a = std::sqrt(s.a2);
+  w[0] = u; w[1] = u - a; w[2] = u + a; w[3] = u;
+}
+
+// rotateToFace / rotateFromFace of the vector part (conservationLaws/base/base.h:171-232)
+template <class R> void rotate_to(const Face<R>& f, const R* q0, R* q1) {
+  const R* m[2] = {f.n, f.t};
+  for (int k = 2; k < 4; ++k) q1[k] = q0[k];
+  for (int i = 0; i < 2; ++i) {
+    R a = 0;
+    for (int j = 0; j < 2; ++j) a += m[i][j] * q0[j];
+    q1[i] = a;
+  }
+}
+template <class R> void rotate_from(const Face<R>& f, const R* q0, R* q1) {
+  const R* m[2] = {f.n, f.t};
+  for (int k = 2; k < 4; ++k) q1[k] = q0[k];
+  for (int i = 0; i < 2; ++i) {
+    R a = 0;
+    for (int j = 0; j < 2; ++j) a += m[j][i] * q0[j];
+    q1[i] = a;
+  }
+}
+
+// delta2Delta conserved -> primitive (primitive.ipp:142-184)
+template <class R> void dcons2dprim(const Species<R>& sp, const State<R>& s, const R* dqc, R* dqp) {
+  const R dr = dqc[2], dre = dqc[3];
+  const R rho1 = 1. / s.r;
+  const R k = 0.5 * s.u2;
+  R c = k * dr + dre;
+  for (int i = 0; i < 2; ++i) {
+    const R u = s.u[i], dru = dqc[i];
+    const R du = (dru - u * dr) * rho1;
+    dqp[i] = du;
+    c -= u * dru;
+  }
+  const R dp = c * (sp.gamma - 1.);
+  dqp[2] = dr; dqp[3] = dp;
+}
+
+// delta2Delta primitive -> conserved (primitive.ipp:187-233)
+template <class R> void dprim2dcons(const Species<R>& sp, const State<R>& s, const R* dqp, R* dqc) {
+  const R dr = dqp[2], dp = dqp[3];
+  const R r = s.r;
+  R dk = 0;
+  for (int i = 0; i < 2; ++i) {
+    const R u = s.u[i], du = dqp[i];
+    const R dru = r * du + u * dr;
+    dqc[i] = dru;
+    dk += u * du;
+  }
+  const R k = 0.5 * s.u2;
+  const R dre = dp * sp.gamma1 + r * dk + k * dr;
+  dqc[2] = dr; dqc[3] = dre;
+}
+
+// delta2Delta characteristic -> primitive (primitive.ipp:238-275)
+template <class R> void dchar2dprim(const Species<R>& sp, const State<R>& s, const R* dqw, R* dqp) {
+  const R r = s.r;
+  const R a = std::sqrt(s.a2);
+  const R dp = 0.5 * r * a * (dqw[2] - dqw[1]);
+  const R dr = dp / (a * a) - r * dqw[0] / sp.gamma;
+  dqp[0] = 0.5 * (dqw[1] + dqw[2]);
+  dqp[1] = dqw[3];
+  dqp[2] = dr; dqp[3] = dp;
+}
+
+// delta2Delta primitive -> characteristic (primitive.ipp:277-313)
+template <class R> void dprim2dchar(const Species<R>& sp, const State<R>& s, const R* dqp, R* dqw) {
+  const R r1 = 1. / s.r;
+  const R a1 = 1. / std::sqrt(s.a2);
+  const R du = dqp[0], dr = dqp[2], dp = dqp[3];
+  dqw[0] = sp.gamma * (dp * a1 * a1 - dr) * r1;
+  dqw[1] = du - dp * r1 * a1;
+  dqw[2] = du + dp * r1 * a1;
+  dqw[3] = dqp[1];
+}
+
+// ---------------------------------------------------------------- fluxes
+// exactFlux (conservationLaws/euler/fluxes/exactFlux.ipp:231-263)
+template <class R> FluxRes<R> exact_flux(const R* n, const State<R>& s) {
+  const R r = s.r, p = s.p, h = s.h;
+  const R a = std::sqrt(s.a2);
+  const R un = proj_vel(n, s);
+  const R mn = r * un;
+  FluxRes<R> fr;
+  for (int i = 0; i < 2; ++i) fr.f[i] = mn * s.u[i] + p * n[i];
+  fr.f[2] = mn; fr.f[3] = mn * h;
+  fr.lam = std::abs(un) + a;
+  return fr;
+}
+
+// CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:25-37)
+template <class R> FluxRes<R> central_flux(const Face<R>& f, const State<R>& sl, const State<R>& sr) {
+  const FluxRes<R> fl = exact_flux(f.n, sl), fr = exact_flux(f.n, sr);
+  FluxRes<R> o;
+  for (int i = 0; i < 4; ++i) o.f[i] = (R)(0.5 * (fl.f[i] + fr.f[i])) * f.area;
+  o.lam = std::max(fl.lam, fr.lam) * f.area;
+  return o;
+}
+
+// roeAverage (conservationLaws/euler/fluxes/roe.ipp:150-196)
+template <class R> State<R> roe_average(const Species<R>& sp, const State<R>& sl, const State<R>& sr) {
+  State<R> a;
+  const R cr = std::sqrt(sr.r / sl.r);
+  const R wl = 1. / (1. + cr);
+  const R wr = 1. - wl;
+  const R ra = cr * sl.r;
+  R ka = 0;
+  for (int i = 0; i < 2; ++i) {
+    const R ua = wl * sl.u[i] + wr * sr.u[i];
+    ka += ua * ua;
+    a.u[i] = ua;
+  }
+  ka *= 0.5;
+  const R ha = wl * sl.h + wr * sr.h;
+  const R a2a = (sp.gamma - 1.) * (ha - ka);
+  const R ta = a2a / (sp.Rgas * sp.gamma);
+  const R pa = ra * sp.Rgas * ta;
+  a.p = pa; a.r = ra; a.t = ta; a.h = ha; a.u2 = 2. * ka; a.a2 = a2a;
+  return a;
+}
+
+// entropyfix, Harten eps=0.05 (conservationLaws/euler/fluxes/roe.ipp:198-226)
+template <class R> void entropy_fix(const R* la, const R* ll, const R* lr, R* sp) {
+  const R ua = std::fabs(la[0]);
+  sp[0] = ua; sp[3] = ua;
+  sp[1] = std::fabs(la[1]); sp[2] = std::fabs(la[2]);
+  constexpr R eps = 0.05;
+  for (int i = 1; i < 3; ++i) {
+    const R le = eps * std::fmax((R)0., std::fmax(la[i] - ll[i], lr[i] - la[i]));
+    const R laa = std::fabs(la[i]);
+    sp[i] = (laa > le) ? laa : (R)(0.5 * (le + laa * laa / le));
+  }
+}
+
+// RoeDissipation (conservationLaws/base/fluxes/roeFlux.ipp:59-95)
+template <class R> FluxRes<R> roe_dissipation(const Species<R>& sp, const Face<R>& f,
+                                              const State<R>& sl, const State<R>& sr) {
+  const State<R> ra = roe_average(sp, sl, sr);
+  R wa[4], wl[4], wr[4], lam[4];
+  wavespeeds(f.n, ra, wa); wavespeeds(f.n, sl, wl); wavespeeds(f.n, sr, wr);
+  entropy_fix(wa, wl, wr, lam);
+  R cl[4], cr[4], dq[4], dqc[4];
+  state2cons(sr, cr); state2cons(sl, cl);
+  for (int i = 0; i < 4; ++i) dq[i] = cr[i] - cl[i];
+  rotate_to(f, dq, dqc);
+  R dqp[4], dqw[4];
+  dcons2dprim(sp, ra, dqc, dqp);
+  dprim2dchar(sp, ra, dqp, dqw);
+  for (int i = 0; i < 4; ++i) dqw[i] = lam[i] * dqw[i];
+  R dp2[4], dc2[4], fd[4];
+  dchar2dprim(sp, ra, dqw, dp2);
+  dprim2dcons(sp, ra, dp2, dc2);
+  rotate_from(f, dc2, fd);
+  FluxRes<R> o;
+  const R s = -0.5 * f.area;
+  for (int i = 0; i < 4; ++i) o.f[i] = s * fd[i];
+  o.lam = spec_rad(f.n, ra) * f.area;
+  return o;
+}
+
+// RoeFlux = Central + RoeDissipation (conservationLaws/base/fluxes/roeFlux.ipp:39-56)
+template <class R> FluxRes<R> roe_flux(const Species<R>& sp, const Face<R>& f,
+                                       const State<R>& sl, const State<R>& sr) {
+  const FluxRes<R> c = central_flux(f, sl, sr);
+  const FluxRes<R> d = roe_dissipation(sp, f, sl, sr);
+  FluxRes<R> o;
+  for (int i = 0; i < 4; ++i) o.f[i] = c.f[i] + d.f[i];
+  o.lam = std::fmax(c.lam, d.lam);
+  return o;
+}
+
+// RusanovFlux (conservationLaws/base/fluxes/rusanovFlux.ipp:99-147)
+template <class R> FluxRes<R> rusanov_flux(const Species<R>& sp, const Face<R>& f,
+                                           const State<R>& sl, const State<R>& sr) {
+  FluxRes<R> o = central_flux(f, sl, sr);
+  const R lambda = std::max(spec_rad(f.n, sl), spec_rad(f.n, sr));
+  R cl[4], cr[4];
+  state2cons(sr, cr); state2cons(sl, cl);
+  const R la = lambda * f.area;
+  const R s = -0.5 * la;
+  for (int i = 0; i < 4; ++i) o.f[i] += s * (cr[i] - cl[i]);
+  (void)sp;
+  return o;
+}
+
+// Mach-number splittings (conservationLaws/euler/fluxes/machSplittings.ipp:163-204)
+template <class R> R msplit_m1(int s, R M) { return 0.5 * (M + s * std::fabs(M)); }
+template <class R> R msplit_m2(int s, R M) { return s * 0.25 * (M + s) * (M + s); }
+template <class R> R msplit_m4(int s, R M, R beta) {
+  return msplit_m2(s, M) * (1. - s * 16. * beta * msplit_m2(-s, M));
+}
+template <class R> R msplit_p1(int s, R M) {
+  constexpr R eps = std::numeric_limits<R>::max();
+  return (msplit_m1(s, M) + eps) / (std::fabs(M) + eps);
+}
+template <class R> R msplit_p3(int s, R M) { return msplit_m2(s, M) * (s * 2. - M); }
+template <class R> R msplit_p5(int s, R M, R alpha) {
+  return msplit_p3(s, M) - s * 16. * alpha * M * msplit_m2(s, M) * msplit_m2(-s, M);
+}
+
+// SLAU2 with (Convective, Acoustic) low-Mach tags
+// (conservationLaws/euler/fluxes/slau.ipp:4-161).  upwind_by_mdot=false is the
+// literal reference form that selects the convected state by the sign of
+// ua = sqrt(0.5(|u_l|^2+|u_r|^2)) (slau.ipp:124-125), which is never negative;
+// upwind_by_mdot=true selects it by the sign of the interface mass flux.
+template <class R> FluxRes<R> slau_flux(const Species<R>& sp, const Face<R>& f,
+                                        const State<R>& sl, const State<R>& sr, bool upwind_by_mdot) {
+  const R ua = std::sqrt(0.5 * (sl.u2 + sr.u2));
+  const R aa = 0.5 * (std::sqrt(sl.a2) + std::sqrt(sr.a2));
+  const R aa1 = 1.0 / aa;
+  const R ma = ua * aa1;
+  const R ma_hat = std::fmin((R)1.0, ma);
+  const R unl = proj_vel(f.n, sl), unr = proj_vel(f.n, sr);
+  const R ml = unl * aa1, mr = unr * aa1;
+  const R una = (sl.r * std::fabs(unl) + sr.r * std::fabs(unr)) / (sl.r + sr.r);
+  const R chi = (1. - ma_hat) * (1. - ma_hat);
+  const R g = -std::fmax(std::fmin(ml, (R)0.), (R)-1.) * std::fmin(std::fmax(mr, (R)0.), (R)1.);
+  const R dr = sr.r - sl.r;
+  const R dp = sr.p - sl.p;
+  const R mdot_c = sl.r * unl + sr.r * unr;
+  const R mdot_dr = una * dr;
+  const R mdot_dp = chi * dp * aa1;
+  const R mdot = 0.5 * ((mdot_c - mdot_dr) * (1. - g) - mdot_dp) * f.area;
+  const unsigned mlsup = std::fabs(ml) > 1 ? 1 : 0, mlsub = 1 - mlsup;
+  const unsigned mrsup = std::fabs(mr) > 1 ? 1 : 0, mrsub = 1 - mrsup;
+  const R betal = mlsub * msplit_p3(1, ml) + mlsup * msplit_p1(1, ml);
+  const R betar = mrsub * msplit_p3(-1, mr) + mrsup * msplit_p1(-1, mr);
+  const R p_c = sl.p + sr.p;
+  const R p_dp = (betal - betar) * dp;
+  const R p_du = -ma * (betal + betar - 1.) * (p_c);
+  const R pa = 0.5 * (p_c - p_dp - p_du) * f.area;
+  const bool left = upwind_by_mdot ? (mdot > 0) : (ua > 0);
+  const int m1l = left ? 1 : 0, m1r = left ? 0 : 1;
+  FluxRes<R> o;
+  for (int i = 0; i < 2; ++i) o.f[i] = mdot * (m1l * sl.u[i] + m1r * sr.u[i]) + pa * f.n[i];
+  o.f[2] = mdot;
+  o.f[3] = mdot * (m1l * sl.h + m1r * sr.h);
+  const R lmax = std::sqrt(std::fmax(sl.a2, sr.a2)) + std::fmax(std::fabs(unl), std::fabs(unr));
+  o.lam = lmax * f.area;
+  return o;
+}
+
+// AUSM+up, Liou 2006, (Convective, Convective) tags
+// (conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171)
+template <class R> FluxRes<R> ausmpup_flux(const Species<R>& sp, const Face<R>& f,
+                                           const State<R>& sl, const State<R>& sr) {
+  const R alpha0 = 0.1875, beta = 0.125, Ku = 0.75 * 2., Kp = 0.25, sigma = 1.0;
+  const R ascoeff = 2. * (sp.gamma - 1.) / (sp.gamma + 1.);
+  const R unl = proj_vel(f.n, sl), unr = proj_vel(f.n, sr);
+  const R als2 = ascoeff * sl.h, ars2 = ascoeff * sr.h;
+  const R als = als2 / std::fmax(unl, std::sqrt(als2));
+  const R ars = ars2 / std::fmax(-unr, std::sqrt(ars2));
+  const R ra = 0.5 * (sl.r + sr.r);
+  const R as = std::fmin(ars, als);
+  const R ml = unl / as, mr = unr / as;
+  const R minf = sp.minf;
+  const R m0 = std::sqrt(0.5 * (ml * ml + mr * mr));
+  const R m0_c = std::clamp<R>(m0, minf, 1.);
+  const R m0_p = m0_c, m0_u = m0_c;
+  const R fa_p = m0_p * (2. - m0_p);
+  const R fa_u = m0_u * (2. - m0_u);
+  const unsigned mlsup = std::fabs(ml) > 1 ? 1 : 0, mlsub = 1 - mlsup;
+  const unsigned mrsup = std::fabs(mr) > 1 ? 1 : 0, mrsub = 1 - mrsup;
+  const R mlp = mlsub * msplit_m4(1, ml, beta) + mlsup * msplit_m1(1, ml);
+  const R mrm = mrsub * msplit_m4(-1, mr, beta) + mrsup * msplit_m1(-1, mr);
+  const R delp = sr.p - sl.p;
+  const R mp = Kp * std::fmax(1. - sigma * m0 * m0, (R)0.) * delp / (fa_p * ra * as * as);
+  const R uaf = as * (mlp + mrm - mp) * f.area;
+  const R alpha = alpha0 * (5. * fa_u * fa_u - 4.);
+  const R plp = mlsub * msplit_p5(1, ml, alpha) + mlsup * msplit_p1(1, ml);
+  const R prm = mrsub * msplit_p5(-1, mr, alpha) + mrsup * msplit_p1(-1, mr);
+  const R delu = unr - unl;
+  const R pu = Ku * plp * prm * ra * (fa_u * as) * delu;
+  const R pa = (plp * sl.p + prm * sr.p - pu) * f.area;
+  const int m1l = (uaf > 0) ? 1 : 0, m1r = (uaf > 0) ? 0 : 1;
+  const R mdot = uaf * (m1l * sl.r + m1r * sr.r);
+  FluxRes<R> o;
+  for (int i = 0; i < 2; ++i) o.f[i] = mdot * (m1l * sl.u[i] + m1r * sr.u[i]) + pa * f.n[i];
+  o.f[2] = mdot;
+  o.f[3] = mdot * (m1l * sl.h + m1r * sr.h);
+  const R lmd = 0.5 * (m0_p + 1) / fa_p;
+  const R amax = std::sqrt(std::fmax(as * as, std::fmax(sl.a2, sr.a2)));
+  const R lmax = lmd * amax + std::fmax(std::fabs(uaf), std::fmax(std::fabs(unl), std::fabs(unr)));
+  o.lam = lmax * f.area;
+  return o;
+}
+
+template <class R> FluxRes<R> face_flux(int kind, const Species<R>& sp, const Face<R>& f,
+                                        const State<R>& sl, const State<R>& sr) {
+  switch (kind) {
+    case FLUX_ROE: return roe_flux(sp, f, sl, sr);
+    case FLUX_SLAU: return slau_flux(sp, f, sl, sr, true);
+    case FLUX_SLAU_REF: return slau_flux(sp, f, sl, sr, false);
+    case FLUX_AUSMPUP: return ausmpup_flux(sp, f, sl, sr);
+    case FLUX_RUSANOV: return rusanov_flux(sp, f, sl, sr);
+    default: return central_flux(f, sl, sr);
+  }
+}
+
+// ---------------------------------------------------------------- limiters
+// limiters/limiter.ipp:141-297.  VANLEER is the textbook harmonic-mean slope
+// (a|b|+|a|b)/(|a|+|b|+eps) with the reference's eps convention; VANLEER_REF
+// is the literal reference expression (b+|b|)/(a+|b|+eps) (limiter.ipp:216-224).
+template <class R> R limit(int kind, R a, R b) {
+  switch (kind) {
+    case LIM_NOLIMIT1: return 0;
+    case LIM_NOLIMIT2: return 0.5 * (a + b);
+    case LIM_NOLIMIT3: return 0.33333333333333333 * (2. * a + b);
+    case LIM_VANALBADA: {
+      const R eps = std::numeric_limits<R>::min();
+      return a * b < 0 ? (R)0 : (b * (a * a) + a * (b * b)) / (a * a + b * b + eps);
+    }
+    case LIM_MINMOD:
+      return a > 0 ? (R)std::fmin(a, (R)std::fmax(b, (R)0.)) : (R)std::fmax(a, (R)std::fmin(b, (R)0.));
+    case LIM_SUPERBEE:
+      return a > 0 ? (R)std::fmax((R)0., std::fmax(std::fmin(2 * a, b), std::fmin(2 * b, a)))
+                   : (R)std::fmin((R)0., std::fmin(std::fmax(2 * a, b), std::fmax(2 * b, a)));
+    case LIM_MC:
+      return a > 0 ? (R)std::fmax((R)0., std::fmin((R)(0.5 * (a + b)), std::fmin(2 * b, 2 * a)))
+                   : (R)std::fmin((R)0., std::fmax((R)(0.5 * (a + b)), std::fmax(2 * b, 2 * a)));
+    case LIM_VANLEER: {
+      const R eps = std::numeric_limits<R>::min();
+      return (a * std::fabs(b) + std::fabs(a) * b) / (std::fabs(a) + std::fabs(b) + eps);
+    }
+    case LIM_VANLEER_REF: {
+      const R eps = std::numeric_limits<R>::min();
+      return (b + std::fabs(b)) / (a + std::fabs(b) + eps);
+    }
+    case LIM_CADA3: {
+      const R t = 0.0, gam = 1.5, c1 = -2. / 7., c2 = 0.4, c3 = 3 * gam - 2;
+      R u, v, w, p, q;
+      if (a > 0) { u = a; v = b; } else { u = -a; v = -b; }
+      p = (v + 2. * u) / 3.;
+      q = std::fabs(a) + std::fabs(b);
+      if (q > t) {
+        if (v < -2 * u) w = 0;
+        else if (v < c1 * u) w = (v + 2. * u) / 3.;
+        else if (v < 0) w = -2. * v;
+        else if (v < c2 * u) w = 2. * v;
+        else if (v < c3 * u) w = (v + 2. * u) / 3.;
+        else w = gam * u;
+      } else {
+        w = p;
+      }
+      if (a <= 0) w = -w;
+      return w;
+    }
+    default: return 0;
+  }
+}
+
+// ---------------------------------------------------------------- LSQ
+// lsq::xmetric (lsq/lsq.h:302-318), lsq::qmetric (lsq/lsq.h:367-389),
+// lsq::factor (lsq/lsq.h:403-412), lsq::solve (lsq/lsq.h:437-459).
+// QMetric index is q[2*var+dim] (the intent of lsq/lsq.h:72).
+template <class R> struct XM { R x[3]; };
+template <class R> struct QM { R q[8]; };
+
+template <class R> XM<R> xmetric(R dx, R dy) { return XM<R>{{dx * dx, dx * dy, dy * dy}}; }
+template <class R> QM<R> qmetric(R dx, R dy, const R* dq) {
+  QM<R> m;
+  for (int i = 0; i < 4; ++i) { m.q[2 * i] = dq[i] * dx; m.q[2 * i + 1] = dq[i] * dy; }
+  return m;
+}
+template <class R> XM<R> factor(const XM<R>& xm) {
+  const R d = 1. / (xm.x[0] * xm.x[2] - xm.x[1] * xm.x[1]);
+  return XM<R>{{d * xm.x[2], -d * xm.x[1], d * xm.x[0]}};
+}
+template <class R> void solve(const XM<R>& xf, const QM<R>& qm, const R* dir, R* g) {
+  for (int i = 0; i < 4; ++i)
+    g[i] = (xf.x[0] * qm.q[2 * i] + xf.x[1] * qm.q[2 * i + 1]) * dir[0] +
+           (xf.x[1] * qm.q[2 * i] + xf.x[2] * qm.q[2 * i + 1]) * dir[1];
+}
+
+// ---------------------------------------------------------------- RK tables
+// ODE::Explicit ssp11/ssp22/ssp33/ssp34 (ode.h:107-197)
+template <class R> struct RKTable { int nstages; R maxcfl; R alpha[4][4]; R beta[4]; };
+template <class R> RKTable<R> rk_table(int kind) {
+  RKTable<R> t{};
+  if (kind == RK_SSP11) { t.nstages = 1; t.maxcfl = 1.; t.beta[0] = 1.0; t.alpha[0][0] = 1.0; }
+  else if (kind == RK_SSP22) {
+    t.nstages = 2; t.maxcfl = 1.; t.beta[0] = 1.0; t.beta[1] = 1.0;
+    t.alpha[0][0] = 1.0; t.alpha[1][0] = 0.5; t.alpha[1][1] = 0.5;
+  } else if (kind == RK_SSP33) {
+    t.nstages = 3; t.maxcfl = 1.; t.beta[0] = 1.0; t.beta[1] = 0.5; t.beta[2] = 1.0;
+    t.alpha[0][0] = 1.; t.alpha[1][0] = 0.5; t.alpha[1][1] = 0.5;
+    t.alpha[2][0] = 1. / 6.; t.alpha[2][1] = 1. / 6.; t.alpha[2][2] = 2. / 3.;
+  } else {
+    t.nstages = 4; t.maxcfl = 2.; t.beta[0] = 0.5; t.beta[1] = 1.0; t.beta[2] = 0.5; t.beta[3] = 1.0;
+    t.alpha[0][0] = 1.0; t.alpha[1][0] = 0.5; t.alpha[1][1] = 0.5;
+    t.alpha[2][0] = 1. / 3.; t.alpha[2][1] = 1. / 3.; t.alpha[2][2] = 1. / 3.;
+    t.alpha[3][0] = 1. / 6.; t.alpha[3][1] = 1. / 6.; t.alpha[3][2] = 1. / 6.; t.alpha[3][3] = 1. / 2.;
+  }
+  return t;
+}
+
+// ---------------------------------------------------------------- boundary physics
+// boundaryUpdate for Riemann invariants (conservationLaws/euler/boundary/riemann.ipp:18-113),
+// entropy/pressure (entropy.ipp:18-88); qi/qf are primitive, face normal points into the domain.
+template <class R> void bc_riemann(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf, R* qb) {
+  const R gam = sp.gamma, gam1 = sp.gamma1;
+  R ri[4], rf[4];
+  rotate_to(f, qi, ri); rotate_to(f, qf, rf);
+  const State<R> sA = roe_average(sp, prim2state(sp, ri), prim2state(sp, rf));
+  if ((sA.u[0] / std::sqrt(sA.u2)) < 0.001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; return; }
+  const R ma = sA.u[0] / std::sqrt(sA.a2);
+  const bool inflow = ma > 0;
+  const R* quw = inflow ? qf : qi;
+  if (std::abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; return; }
+  const State<R> sI = prim2state(sp, ri), sF = prim2state(sp, rf);
+  const R ai = std::sqrt(sI.a2), af = std::sqrt(sF.a2);
+  const R uni = sI.u[0], unf = sF.u[0];
+  const R rim = uni - 2. * ai * gam1;
+  const R rip = unf + 2. * af * gam1;
+  const R ub = 0.5 * (rim + rip);
+  const R ab = 0.25 * (gam - 1.) * (rip - rim);
+  R ru[4];
+  rotate_to(f, quw, ru);
+  const State<R> sU = prim2state(sp, ru);
+  const R sb = sU.a2 / (gam * std::pow(sU.r, gam - 1.));
+  const R vb = sU.u[1];
+  const R rb = std::pow(ab * ab / (gam * sb), gam1);
+  const R pb = rb * ab * ab / gam;
+  const R qbr[4] = {ub, vb, rb, pb};
+  rotate_from(f, qbr, qb);
+}
+
+template <class R> void bc_entropy(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf, R* qb) {
+  const R gam = sp.gamma;
+  R ri[4], rf[4];
+  rotate_to(f, qi, ri); rotate_to(f, qf, rf);
+  const State<R> sA = roe_average(sp, prim2state(sp, ri), prim2state(sp, rf));
+  if ((sA.u[0] / std::sqrt(sA.u2)) < 0.0001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; return; }
+  const R ma = sA.u[0] / std::sqrt(sA.a2);
+  const bool inflow = ma > 0;
+  const R* quw = inflow ? qf : qi;
+  const R* qdw = inflow ? qi : qf;
+  if (std::abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; return; }
+  R ru[4], rd[4];
+  rotate_to(f, quw, ru); rotate_to(f, qdw, rd);
+  const State<R> sU = prim2state(sp, ru), sD = prim2state(sp, rd);
+  const R pb = sD.p;
+  const R sb = sU.a2 / (gam * std::pow(sU.r, gam - 1.));
+  const R rb = std::pow(pb / sb, 1. / gam);
+  const R qbr[4] = {sU.u[0], sU.u[1], rb, pb};
+  rotate_from(f, qbr, qb);
+}
+
+// boundaryFlux for an inviscid wall (conservationLaws/euler/boundary/inviscidWall.ipp:33-72):
+// pressure-only flux from q_wall = q_interior - dq, dq the gradient increment
+// from the face to the cell centre.
+template <class R> FluxRes<R> wall_flux(const Species<R>& sp, const Face<R>& f, const R* qi, const R* dq) {
+  const int direction = -1;
+  R qw[4];
+  for (int k = 0; k < 4; ++k) qw[k] = qi[k] + direction * dq[k];
+  const State<R> sw = prim2state(sp, qw);
+  const R pw = sw.p;
+  FluxRes<R> o;
+  for (int i = 0; i < 2; ++i) o.f[i] = f.area * pw * f.n[i];
+  o.f[2] = 0.; o.f[3] = 0.;
+  o.lam = f.area * spec_rad(f.n, sw);
+  return o;
+}
+
+}  // namespace hco

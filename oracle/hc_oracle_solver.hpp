@@ -1,0 +1,382 @@
+// hc_oracle_solver.hpp -- CPU oracle: the residual / RK glue of the reference.
+//
+// TEST INFRASTRUCTURE ONLY (see hc_oracle.hpp).  The reference's spatial glue
+// (lsq/*, spatial/*, timestepping/rungeKutta.h) does not compile at its HEAD;
+// this file restates its intent with the decisions below, which the CUDA path
+// implements identically:
+//   D2  LSQ stencil = the 4 face neighbours, periodic wrap neighbours included
+//       (their centres translated by the periodic shift); non-periodic sides
+//       add the mirrored-point xmetric with zero q contribution
+//       (spatial/lsqMetrics.h:155-251, qmetrics spatial/lsqMetrics.h:269-301).
+//   D3  QMetric index q[2*var+dim]; biased gradient projected on face.metric[0].
+//   D4  ghost faces: ghost side unreconstructed, interior side MUSCL with the
+//       mirror term removed; wall pressure from the interior state extrapolated
+//       to the face with the cell's full LSQ gradient.
+//   D5  alpha/beta RK accumulation form; global dt from stage 0
+//       (timestepping/rungeKutta.h:96-197); local dt from the stage-0 spectral
+//       radius sum, eulerForwardUpdateLocal semantics (spatial/eulerForwardUpdate.h:117-168).
+#pragma once
+
+#include "hc_oracle.hpp"
+
+#include <omp.h>
+
+namespace hco {
+
+template <class R> struct Solver {
+  int ni = 0, nj = 0;
+  std::vector<R> nodes;  // (ni+1)*(nj+1)*2
+  Species<R> sp{};
+  int flux = FLUX_ROE, lim = LIM_VANLEER, rk = RK_SSP34, dtmode = DT_GLOBAL;
+  R cfl = 0.5;
+  int bc[4] = {BC_PERIODIC, BC_PERIODIC, BC_PERIODIC, BC_PERIODIC};
+  // ghost arrays per side: [side][face][layer][var]; layer 0 = ghost value,
+  // layer 1 = reference (far-field) value (solutionField/solutionField.h:20-31)
+  std::vector<R> ghost[4];
+  std::vector<Cell<R>> cells;
+  std::vector<XM<R>> xm;       // full xmetric per cell
+  std::vector<R> q0, q1, q2;   // primitive AoS [cell][4]
+  std::vector<R> lam0;         // stage-0 spectral radius sums (local dt)
+  std::vector<FluxRes<R>> res[4], rtot;
+  std::vector<QM<R>> qm;
+  R t = 0, last_dt = 0;
+
+  const R* node(int i, int j) const { return &nodes[(size_t(i) * (nj + 1) + j) * 2]; }
+  size_t cid(int i, int j) const { return size_t(i) * nj + j; }
+  int nface(int side) const { return side < 2 ? nj : ni; }
+
+  // periodic shift across the i (or j) boundary at face index k: image of the
+  // last cell = its centre minus the shift (average over the face's two nodes)
+  void shift_i(int j, R* s) const {
+    for (int d = 0; d < 2; ++d)
+      s[d] = 0.5 * ((node(ni, j)[d] - node(0, j)[d]) + (node(ni, j + 1)[d] - node(0, j + 1)[d]));
+  }
+  void shift_j(int i, R* s) const {
+    for (int d = 0; d < 2; ++d)
+      s[d] = 0.5 * ((node(i, nj)[d] - node(i, 0)[d]) + (node(i + 1, nj)[d] - node(i + 1, 0)[d]));
+  }
+  // mirrored-point displacement of a boundary cell (spatial/lsqMetrics.h:204-212)
+  void mirror(int side, int k, R* m) const {
+    int i0, j0, i1, j1;
+    if (side == 0) { i0 = 0; j0 = k; i1 = 1; j1 = k; }
+    else if (side == 1) { i0 = ni - 1; j0 = k; i1 = ni - 2; j1 = k; }
+    else if (side == 2) { i0 = k; j0 = 0; i1 = k; j1 = 1; }
+    else { i0 = k; j0 = nj - 1; i1 = k; j1 = nj - 2; }
+    const Cell<R>& c0 = cells[cid(i0, j0)];
+    const Cell<R>& c1 = cells[cid(i1, j1)];
+    for (int d = 0; d < 2; ++d) {
+      const R disp = c0.c[d] - c1.c[d];
+      const R bp = c0.c[d] + disp;
+      m[d] = bp - c0.c[d];
+    }
+  }
+  int side_cell(int side, int k) const {
+    if (side == 0) return (int)cid(0, k);
+    if (side == 1) return (int)cid(ni - 1, k);
+    if (side == 2) return (int)cid(k, 0);
+    return (int)cid(k, nj - 1);
+  }
+  // boundary face as used by the flux loops (ghostCellLoop.h:133-224): sides 0/2
+  // have normals pointing into the domain, sides 1/3 out of it
+  Face<R> bface_flux(int side, int k) const {
+    if (side == 0) return surface(node(0, k), node(0, k + 1));
+    if (side == 1) return surface(node(ni, k), node(ni, k + 1));
+    if (side == 2) return surface(node(k + 1, 0), node(k, 0));
+    return surface(node(k + 1, nj), node(k, nj));
+  }
+  // boundary face with the normal into the domain (boundaryUpdate.h:171-262,
+  // boundaryFluxLoop.h:150-261)
+  Face<R> bface_in(int side, int k) const {
+    if (side == 0) return surface(node(0, k), node(0, k + 1));
+    if (side == 1) return surface(node(ni, k + 1), node(ni, k));
+    if (side == 2) return surface(node(k + 1, 0), node(k, 0));
+    return surface(node(k, nj), node(k + 1, nj));
+  }
+
+  void setup() {
+    cells.resize(size_t(ni) * nj);
+    for (int i = 0; i < ni; ++i)
+      for (int j = 0; j < nj; ++j)
+        cells[cid(i, j)] = volume(node(i, j), node(i + 1, j), node(i, j + 1), node(i + 1, j + 1));
+    xm.assign(size_t(ni) * nj, XM<R>{{0, 0, 0}});
+    auto addx = [&](size_t a, const XM<R>& v) { for (int k = 0; k < 3; ++k) xm[a].x[k] += v.x[k]; };
+    // neighbour_accumulation order (parallalg/neighbour_algorithm.h:243-317)
+    for (int j = 0; j < nj; ++j)
+      for (int i = 0; i < ni - 1; ++i) {
+        const Cell<R>& a = cells[cid(i, j)];
+        const Cell<R>& b = cells[cid(i + 1, j)];
+        const XM<R> v = xmetric<R>(b.c[0] - a.c[0], b.c[1] - a.c[1]);
+        addx(cid(i, j), v); addx(cid(i + 1, j), v);
+      }
+    for (int i = 0; i < ni; ++i)
+      for (int j = 0; j < nj - 1; ++j) {
+        const Cell<R>& a = cells[cid(i, j)];
+        const Cell<R>& b = cells[cid(i, j + 1)];
+        const XM<R> v = xmetric<R>(b.c[0] - a.c[0], b.c[1] - a.c[1]);
+        addx(cid(i, j), v); addx(cid(i, j + 1), v);
+      }
+    if (bc[0] == BC_PERIODIC)
+      for (int j = 0; j < nj; ++j) {
+        R s[2]; shift_i(j, s);
+        const Cell<R>& a = cells[cid(ni - 1, j)];
+        const Cell<R>& b = cells[cid(0, j)];
+        const XM<R> v = xmetric<R>(b.c[0] - (a.c[0] - s[0]), b.c[1] - (a.c[1] - s[1]));
+        addx(cid(ni - 1, j), v); addx(cid(0, j), v);
+      }
+    if (bc[2] == BC_PERIODIC)
+      for (int i = 0; i < ni; ++i) {
+        R s[2]; shift_j(i, s);
+        const Cell<R>& a = cells[cid(i, nj - 1)];
+        const Cell<R>& b = cells[cid(i, 0)];
+        const XM<R> v = xmetric<R>(b.c[0] - (a.c[0] - s[0]), b.c[1] - (a.c[1] - s[1]));
+        addx(cid(i, nj - 1), v); addx(cid(i, 0), v);
+      }
+    // boundary_xmetrics order (spatial/lsqMetrics.h:214-249): left/right per j, then bottom/top per i
+    for (int j = 0; j < nj; ++j)
+      for (int side = 0; side < 2; ++side)
+        if (bc[side] != BC_PERIODIC) { R m[2]; mirror(side, j, m); addx(side_cell(side, j), xmetric<R>(m[0], m[1])); }
+    for (int i = 0; i < ni; ++i)
+      for (int side = 2; side < 4; ++side)
+        if (bc[side] != BC_PERIODIC) { R m[2]; mirror(side, i, m); addx(side_cell(side, i), xmetric<R>(m[0], m[1])); }
+    const size_t n = size_t(ni) * nj;
+    q0.assign(n * 4, 0); q1.assign(n * 4, 0); q2.assign(n * 4, 0);
+    lam0.assign(n, 0);
+    for (auto& r : res) r.assign(n, FluxRes<R>{});
+    rtot.assign(n, FluxRes<R>{});
+    qm.assign(n, QM<R>{});
+    for (int s = 0; s < 4; ++s)
+      if (ghost[s].size() != size_t(nface(s)) * 8) ghost[s].assign(size_t(nface(s)) * 8, 0);
+  }
+
+  // ---- boundaryUpdate (spatial/boundary/boundaryUpdate.h:137-266)
+  void boundary_update(const std::vector<R>& q) {
+    for (int side = 0; side < 4; ++side) {
+      if (bc[side] == BC_PERIODIC) continue;
+      for (int k = 0; k < nface(side); ++k) {
+        R* g = &ghost[side][size_t(k) * 8];
+        const R* ref = g + 4;
+        const R* qi = &q[size_t(side_cell(side, k)) * 4];
+        if (bc[side] == BC_RIEMANN) bc_riemann(sp, bface_in(side, k), qi, ref, g);
+        else if (bc[side] == BC_ENTROPY) bc_entropy(sp, bface_in(side, k), qi, ref, g);
+        else for (int v = 0; v < 4; ++v) g[v] = ref[v];  // Fixed (boundaryCondition.h:63-80); wall ghost unused
+      }
+    }
+  }
+
+  // ---- qmetrics with periodic wrap (spatial/lsqMetrics.h:269-301, D2)
+  void qmetrics(const std::vector<R>& q) {
+    for (auto& m : qm) m = QM<R>{};
+    auto addq = [&](size_t a, const QM<R>& v) { for (int k = 0; k < 8; ++k) qm[a].q[k] += v.q[k]; };
+    auto pair = [&](size_t a, size_t b, R dx, R dy) {
+      R dq[4];
+      for (int v = 0; v < 4; ++v) dq[v] = q[b * 4 + v] - q[a * 4 + v];
+      const QM<R> m = qmetric<R>(dx, dy, dq);
+      addq(a, m); addq(b, m);
+    };
+    for (int j = 0; j < nj; ++j)
+      for (int i = 0; i < ni - 1; ++i) {
+        const Cell<R>& a = cells[cid(i, j)]; const Cell<R>& b = cells[cid(i + 1, j)];
+        pair(cid(i, j), cid(i + 1, j), b.c[0] - a.c[0], b.c[1] - a.c[1]);
+      }
+    for (int i = 0; i < ni; ++i)
+      for (int j = 0; j < nj - 1; ++j) {
+        const Cell<R>& a = cells[cid(i, j)]; const Cell<R>& b = cells[cid(i, j + 1)];
+        pair(cid(i, j), cid(i, j + 1), b.c[0] - a.c[0], b.c[1] - a.c[1]);
+      }
+    if (bc[0] == BC_PERIODIC)
+      for (int j = 0; j < nj; ++j) {
+        R s[2]; shift_i(j, s);
+        const Cell<R>& a = cells[cid(ni - 1, j)]; const Cell<R>& b = cells[cid(0, j)];
+        pair(cid(ni - 1, j), cid(0, j), b.c[0] - (a.c[0] - s[0]), b.c[1] - (a.c[1] - s[1]));
+      }
+    if (bc[2] == BC_PERIODIC)
+      for (int i = 0; i < ni; ++i) {
+        R s[2]; shift_j(i, s);
+        const Cell<R>& a = cells[cid(i, nj - 1)]; const Cell<R>& b = cells[cid(i, 0)];
+        pair(cid(i, nj - 1), cid(i, 0), b.c[0] - (a.c[0] - s[0]), b.c[1] - (a.c[1] - s[1]));
+      }
+  }
+
+  // ---- make_muscl_flux (spatial/muscl.h:13-59) with bias_solves (lsq/lsq.h:461-490)
+  FluxRes<R> muscl(const Face<R>& f, const R* cl, const R* cr, const R* ql, const R* qr,
+                   const XM<R>& xl, const XM<R>& xr, const QM<R>& ml, const QM<R>& mr) const {
+    if (lim == LIM_NOLIMIT1)  // first-order overload (spatial/muscl.h:62-87)
+      return face_flux(flux, sp, f, prim2state(sp, ql), prim2state(sp, qr));
+    const R dxc[2] = {cr[0] - cl[0], cr[1] - cl[1]};
+    R dqc[4];
+    for (int v = 0; v < 4; ++v) dqc[v] = qr[v] - ql[v];
+    R d;
+    d = 0; d += (f.c[0] - cl[0]) * (f.c[0] - cl[0]); d += (f.c[1] - cl[1]) * (f.c[1] - cl[1]);
+    const R dl = std::sqrt(d);
+    d = 0; d += (cr[0] - f.c[0]) * (cr[0] - f.c[0]); d += (cr[1] - f.c[1]) * (cr[1] - f.c[1]);
+    const R dr = std::sqrt(d);
+    const R idlr = 1. / (dl + dr);
+    R gc[4];
+    for (int v = 0; v < 4; ++v) gc[v] = dqc[v] * idlr;
+    const XM<R> xc = xmetric<R>(dxc[0], dxc[1]);
+    const QM<R> mc = qmetric<R>(dxc[0], dxc[1], dqc);
+    XM<R> xbl, xbr; QM<R> mbl, mbr;
+    for (int k = 0; k < 3; ++k) { xbl.x[k] = xl.x[k] - xc.x[k]; xbr.x[k] = xr.x[k] - xc.x[k]; }
+    for (int k = 0; k < 8; ++k) { mbl.q[k] = ml.q[k] - mc.q[k]; mbr.q[k] = mr.q[k] - mc.q[k]; }
+    R gl[4], gr[4];
+    solve(factor(xbl), mbl, f.n, gl);
+    solve(factor(xbr), mbr, f.n, gr);
+    R qL[4], qR[4];
+    for (int v = 0; v < 4; ++v) {
+      const R sl = limit<R>(lim, gc[v], gl[v]);
+      const R sr = limit<R>(lim, gc[v], gr[v]);
+      qL[v] = ql[v] + dl * sl;
+      qR[v] = qr[v] - dr * sr;
+    }
+    return face_flux(flux, sp, f, prim2state(sp, qL), prim2state(sp, qR));
+  }
+
+  // ghost face (D4): ghost side is not reconstructed, interior side is MUSCL
+  // with the mirror term removed from its xmetric.  ghost_left says whether the
+  // ghost is the face's left state (sides 0/2) or right state (sides 1/3).
+  FluxRes<R> muscl_ghost(int side, int k, const Face<R>& f, const R* qi, const R* qg) const {
+    const size_t c = side_cell(side, k);
+    const bool ghost_left = (side == 0 || side == 2);
+    const R* ql = ghost_left ? qg : qi;
+    const R* qr = ghost_left ? qi : qg;
+    if (lim == LIM_NOLIMIT1) return face_flux(flux, sp, f, prim2state(sp, ql), prim2state(sp, qr));
+    const R* cc = cells[c].c;
+    R d = 0; d += (f.c[0] - cc[0]) * (f.c[0] - cc[0]); d += (f.c[1] - cc[1]) * (f.c[1] - cc[1]);
+    const R dd = std::sqrt(d);
+    R dqc[4];
+    for (int v = 0; v < 4; ++v) dqc[v] = qr[v] - ql[v];
+    const R idlr = 1. / (dd + dd);
+    R m[2]; mirror(side, k, m);
+    const XM<R> xc = xmetric<R>(m[0], m[1]);
+    XM<R> xb;
+    for (int q = 0; q < 3; ++q) xb.x[q] = xm[c].x[q] - xc.x[q];
+    R g[4];
+    solve(factor(xb), qm[c], f.n, g);
+    R qL[4], qR[4];
+    for (int v = 0; v < 4; ++v) {
+      const R s = limit<R>(lim, dqc[v] * idlr, g[v]);
+      if (ghost_left) { qL[v] = qg[v]; qR[v] = qi[v] - dd * s; }
+      else { qL[v] = qi[v] + dd * s; qR[v] = qg[v]; }
+    }
+    return face_flux(flux, sp, f, prim2state(sp, qL), prim2state(sp, qR));
+  }
+
+  static void acc_sub(FluxRes<R>& a, const FluxRes<R>& f) { for (int v = 0; v < 4; ++v) a.f[v] -= f.f[v]; a.lam += f.lam; }
+  static void acc_add(FluxRes<R>& a, const FluxRes<R>& f) { for (int v = 0; v < 4; ++v) a.f[v] += f.f[v]; a.lam += f.lam; }
+
+  // ---- residualCalc (spatial/residualCalc.h:45-307)
+  void residual(const std::vector<R>& q, std::vector<FluxRes<R>>& r) {
+    boundary_update(q);
+    qmetrics(q);
+    for (auto& x : r) x = FluxRes<R>{};
+    // i-normal faces (spatial/residualCalc.h:199-225); each j row is independent
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < nj; ++j)
+      for (int i = 0; i < ni - 1; ++i) {
+        const size_t a = cid(i, j), b = cid(i + 1, j);
+        const FluxRes<R> f = muscl(surface(node(i + 1, j), node(i + 1, j + 1)), cells[a].c, cells[b].c,
+                                   &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b]);
+        acc_sub(r[a], f); acc_add(r[b], f);
+      }
+    // j-normal faces (spatial/residualCalc.h:227-253)
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < ni; ++i)
+      for (int j = 0; j < nj - 1; ++j) {
+        const size_t a = cid(i, j), b = cid(i, j + 1);
+        const FluxRes<R> f = muscl(surface(node(i + 1, j + 1), node(i, j + 1)), cells[a].c, cells[b].c,
+                                   &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b]);
+        acc_sub(r[a], f); acc_add(r[b], f);
+      }
+    // boundary residuals in boundary-id order (spatial/residualCalc.h:279-307)
+    for (int side = 0; side < 4; ++side) {
+      const int t = bc[side];
+      if (t == BC_PERIODIC) {
+        // only the lower face of each periodic pair (periodicLoop.h:263-324)
+        if (side == 0)
+          for (int j = 0; j < nj; ++j) {
+            R s[2]; shift_i(j, s);
+            const size_t a = cid(ni - 1, j), b = cid(0, j);
+            const R cl[2] = {cells[a].c[0] - s[0], cells[a].c[1] - s[1]};
+            const FluxRes<R> f = muscl(surface(node(0, j), node(0, j + 1)), cl, cells[b].c,
+                                       &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b]);
+            acc_sub(r[a], f); acc_add(r[b], f);
+          }
+        else if (side == 2)
+          for (int i = 0; i < ni; ++i) {
+            R s[2]; shift_j(i, s);
+            const size_t a = cid(i, nj - 1), b = cid(i, 0);
+            const R cl[2] = {cells[a].c[0] - s[0], cells[a].c[1] - s[1]};
+            const FluxRes<R> f = muscl(surface(node(i + 1, 0), node(i, 0)), cl, cells[b].c,
+                                       &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b]);
+            acc_sub(r[a], f); acc_add(r[b], f);
+          }
+      } else if (t == BC_WALL) {
+        // boundary flux loop (boundaryFluxLoop.h:122-265): normal into the domain, res += F
+        for (int k = 0; k < nface(side); ++k) {
+          const size_t c = side_cell(side, k);
+          const Face<R> f = bface_in(side, k);
+          const R dir[2] = {cells[c].c[0] - f.c[0], cells[c].c[1] - f.c[1]};
+          R dq[4];
+          solve(factor(xm[c]), qm[c], dir, dq);
+          acc_add(r[c], wall_flux(sp, f, &q[c * 4], dq));
+        }
+      } else {
+        // ghost-cell loop (ghostCellLoop.h:109-228)
+        for (int k = 0; k < nface(side); ++k) {
+          const size_t c = side_cell(side, k);
+          const FluxRes<R> f = muscl_ghost(side, k, bface_flux(side, k), &q[c * 4], &ghost[side][size_t(k) * 8]);
+          if (side == 0 || side == 2) acc_add(r[c], f); else acc_sub(r[c], f);
+        }
+      }
+    }
+  }
+
+  // ---- spectralRadius (spatial/spectralRadius.h:19-48)
+  R spectral_radius(const std::vector<FluxRes<R>>& r) const {
+    R m = std::numeric_limits<R>::min();
+    for (size_t c = 0; c < r.size(); ++c) m = std::max(m, r[c].lam / cells[c].vol);
+    return m;
+  }
+
+  // ---- integrate (timestepping/rungeKutta.h:37-197); returns the last dt
+  void step(int nsteps) {
+    const RKTable<R> tab = rk_table<R>(rk);
+    const size_t n = size_t(ni) * nj;
+    for (int st = 0; st < nsteps; ++st) {
+      R dt = 0;
+      q1 = q0;
+      for (int s = 0; s < tab.nstages; ++s) {
+        residual(q1, res[s]);
+        if (s == 0) {
+          if (dtmode == DT_GLOBAL) dt = cfl / spectral_radius(res[0]);
+          else for (size_t c = 0; c < n; ++c) lam0[c] = res[0][c].lam;
+        }
+#pragma omp parallel for schedule(static)
+        for (long c = 0; c < (long)n; ++c) {
+          // rungeKuttaAccumulation (timestepping/rungeKutta.h:172-197)
+          R tot[4] = {0, 0, 0, 0};
+          for (int k = 0; k <= s; ++k)
+            for (int v = 0; v < 4; ++v) tot[v] += tab.alpha[s][k] * res[k][c].f[v];
+          // eulerForwardUpdateGlobal / Local (spatial/eulerForwardUpdate.h:38-168)
+          R fac;
+          if (dtmode == DT_GLOBAL) { const R dts = tab.beta[s] * dt; fac = dts / cells[c].vol; }
+          else { const R cs = tab.beta[s] * cfl; fac = cs / lam0[c]; }
+          R qc[4];
+          prim2cons(sp, &q0[c * 4], qc);
+          for (int v = 0; v < 4; ++v) qc[v] = qc[v] + tot[v] * fac;
+          cons2prim(sp, qc, &q2[c * 4]);
+        }
+        std::swap(q1, q2);
+      }
+      q0 = q1;
+      if (dtmode == DT_GLOBAL) { t += dt; last_dt = dt; }
+      else {
+        R m = std::numeric_limits<R>::max();
+        for (size_t c = 0; c < n; ++c) m = std::min(m, cfl * cells[c].vol / lam0[c]);
+        last_dt = m;
+      }
+    }
+  }
+};
+
+}  // namespace hco

@@ -1,0 +1,232 @@
+"""ctypes wrapper over the CPU oracle (oracle/_build/libhcoracle*.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by the CPU-baseline leg of ``bench.py``, always as the checker or the
+timed CPU baseline, never as the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_SO = os.path.join(HERE, "_ref", "libhcref.so")
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+# enum values shared with oracle/hc_oracle.hpp and include/hc.h
+FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5}
+LIMITER = {"nolimit1": 0, "nolimit2": 1, "nolimit3": 2, "vanalbada": 3, "minmod": 4,
+           "superbee": 5, "mc": 6, "vanleer": 7, "vanleer_ref": 8, "cada3": 9}
+BC = {"periodic": 0, "fixed": 1, "riemann": 2, "entropy": 3, "wall": 4}
+RK = {"ssp11": 0, "ssp22": 1, "ssp33": 2, "ssp34": 3}
+DT = {"global": 0, "local": 1}
+
+
+def build(quiet: bool = True) -> None:
+    """Compile the oracle with make (parity and timing variants)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+
+
+def _declare(lib: C.CDLL, prefix: str) -> None:
+    d, i, v = C.c_double, C.c_int, C.c_void_p
+    sigs = {
+        "flux": (None, [i, _dp, _dp, _dp, _dp, _dp]),
+        "exact_flux": (None, [_dp, _dp, _dp, _dp]),
+        "limit": (d, [i, d, d]),
+        "surface": (None, [_dp, _dp, _dp]),
+        "volume": (None, [_dp, _dp]),
+        "prim2state": (None, [_dp, _dp, _dp]),
+        "prim2cons": (None, [_dp, _dp, _dp]),
+        "cons2prim": (None, [_dp, _dp, _dp]),
+        "bc_update": (None, [i, _dp, _dp, _dp, _dp, _dp]),
+        "wall_flux": (None, [_dp, _dp, _dp, _dp, _dp]),
+        "delta": (None, [i, _dp, _dp, _dp, _dp]),
+        "rk_table": (None, [i, _dp]),
+        "linspace_nodes": (None, [i, i, d, d, d, d, _dp]),
+    }
+    for name, (res, args) in sigs.items():
+        f = getattr(lib, prefix + name)
+        f.restype = res
+        f.argtypes = args
+
+
+class Pointwise:
+    """Pointwise functions of either the oracle (prefix hco_) or the reference probe (ref_)."""
+
+    def __init__(self, lib: C.CDLL, prefix: str):
+        self.lib, self.p = lib, prefix
+        _declare(lib, prefix)
+        if prefix == "hco_":
+            lib.hco_cylinder_nodes.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, _dp]
+        else:
+            lib.ref_cylinder_nodes.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp]
+
+    def fn(self, name):
+        return getattr(self.lib, self.p + name)
+
+    def flux(self, kind, species, face, ql, qr):
+        out = np.empty(5)
+        self.fn("flux")(kind, species, face, ql, qr, out)
+        return out
+
+    def exact_flux(self, species, normal, q):
+        out = np.empty(5)
+        self.fn("exact_flux")(species, normal, q, out)
+        return out
+
+    def limit(self, kind, a, b):
+        return self.fn("limit")(kind, float(a), float(b))
+
+    def surface(self, p0, p1):
+        out = np.empty(7)
+        self.fn("surface")(p0, p1, out)
+        return out
+
+    def volume(self, p):
+        out = np.empty(3)
+        self.fn("volume")(p, out)
+        return out
+
+    def prim2state(self, species, q):
+        out = np.empty(8)
+        self.fn("prim2state")(species, q, out)
+        return out
+
+    def prim2cons(self, species, q):
+        out = np.empty(4)
+        self.fn("prim2cons")(species, q, out)
+        return out
+
+    def cons2prim(self, species, qc):
+        out = np.empty(4)
+        self.fn("cons2prim")(species, qc, out)
+        return out
+
+    def bc_update(self, kind, species, face, qi, qf):
+        out = np.empty(4)
+        self.fn("bc_update")(kind, species, face, qi, qf, out)
+        return out
+
+    def wall_flux(self, species, face, qi, dq):
+        out = np.empty(5)
+        self.fn("wall_flux")(species, face, qi, dq, out)
+        return out
+
+    def delta(self, kind, species, q, din):
+        out = np.empty(4)
+        self.fn("delta")(kind, species, q, din, out)
+        return out
+
+    def rk_table(self, kind):
+        out = np.empty(22)
+        self.fn("rk_table")(kind, out)
+        return out
+
+    def cylinder_nodes(self, nr, nth, rc, rb, stretch=1.0):
+        out = np.empty((nr + 1) * (nth + 1) * 2)
+        if self.p == "hco_":
+            self.fn("cylinder_nodes")(nr, nth, rc, rb, stretch, out)
+        else:
+            self.fn("cylinder_nodes")(nr, nth, rc, rb, out)
+        return out
+
+    def linspace_nodes(self, nx, ny, lox, hix, loy, hiy):
+        out = np.empty((nx + 1) * (ny + 1) * 2)
+        self.fn("linspace_nodes")(nx, ny, lox, hix, loy, hiy, out)
+        return out
+
+
+_libs: dict = {}
+
+
+def load(fast: bool = False) -> C.CDLL:
+    """Load the oracle library (building it if missing)."""
+    name = "libhcoracle_fast.so" if fast else "libhcoracle.so"
+    if name in _libs:
+        return _libs[name]
+    path = os.path.join(BUILD, name)
+    if not os.path.exists(path):
+        build()
+    lib = C.CDLL(path)
+    v, i, d = C.c_void_p, C.c_int, C.c_double
+    lib.hco_create.restype = v
+    lib.hco_create.argtypes = [i, i, _dp, _ip, i, i, i, i, d, _dp]
+    lib.hco_destroy.argtypes = [v]
+    lib.hco_set_ghost_ref.argtypes = [v, i, _dp]
+    lib.hco_get_ghost.argtypes = [v, i, _dp]
+    lib.hco_set_state.argtypes = [v, _dp]
+    lib.hco_get_state.argtypes = [v, _dp]
+    lib.hco_residual.argtypes = [v, _dp]
+    lib.hco_step.argtypes = [v, i, _dp]
+    lib.hco_cells.argtypes = [v, _dp]
+    lib.hco_set_threads.argtypes = [i]
+    lib.hco_get_threads.restype = i
+    _libs[name] = lib
+    return lib
+
+
+def pointwise(fast: bool = False) -> Pointwise:
+    return Pointwise(load(fast), "hco_")
+
+
+def reference_pointwise() -> Pointwise | None:
+    """The reference's own pointwise code, when oracle/_ref was built here."""
+    if not os.path.exists(REF_SO):
+        return None
+    return Pointwise(C.CDLL(REF_SO), "ref_")
+
+
+class OracleSolver:
+    """CPU restatement of the reference integrate() over one 2D structured mesh."""
+
+    def __init__(self, ni, nj, nodes, bc, flux="roe", limiter="vanleer", rk="ssp34", dt="global",
+                 cfl=0.5, species=(1.4, 287.058, 1e-4), ghost_ref=None, fast=False):
+        self.lib = load(fast)
+        self.ni, self.nj = ni, nj
+        bcv = np.array([BC[b] if isinstance(b, str) else int(b) for b in bc], dtype=np.int32)
+        self.h = self.lib.hco_create(ni, nj, np.ascontiguousarray(nodes, dtype=np.float64), bcv,
+                                     FLUX[flux] if isinstance(flux, str) else flux,
+                                     LIMITER[limiter] if isinstance(limiter, str) else limiter,
+                                     RK[rk] if isinstance(rk, str) else rk,
+                                     DT[dt] if isinstance(dt, str) else dt,
+                                     float(cfl), np.asarray(species, dtype=np.float64))
+        if ghost_ref is not None:
+            for side in range(4):
+                if ghost_ref[side] is not None:
+                    self.lib.hco_set_ghost_ref(self.h, side,
+                                               np.ascontiguousarray(ghost_ref[side], dtype=np.float64))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.hco_destroy(self.h)
+            self.h = None
+
+    def set_state(self, prim_soa):
+        self.lib.hco_set_state(self.h, np.ascontiguousarray(prim_soa, dtype=np.float64))
+
+    def get_state(self):
+        out = np.empty((4, self.ni, self.nj))
+        self.lib.hco_get_state(self.h, out)
+        return out
+
+    def residual(self):
+        out = np.empty((5, self.ni, self.nj))
+        self.lib.hco_residual(self.h, out)
+        return out
+
+    def step(self, n=1):
+        out = np.empty(2)
+        self.lib.hco_step(self.h, int(n), out)
+        return float(out[0]), float(out[1])
+
+    def cells(self):
+        out = np.empty((3, self.ni, self.nj))
+        self.lib.hco_cells(self.h, out)
+        return out

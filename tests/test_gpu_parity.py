@@ -1,0 +1,167 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+FP64 bar: relative L-inf error per step on the conserved variables, per
+variable ||q_gpu - q_oracle||_inf / ||q_oracle||_inf <= 1e-12.  Residuals are
+compared against the scale of the face fluxes they sum (same bar).  FP32
+results are compared with the FP64 oracle and their error is bounded loosely.
+"""
+import numpy as np
+import pytest
+
+from hyperboliconvergence_gb300 import cases
+from hyperboliconvergence_gb300.solver import Mesh, Solver
+from oracle import oracle_py
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+GAMMA, RGAS = 1.4, 287.058
+
+
+def prim2cons(q, gamma=GAMMA):
+    u, v, r, p = q
+    return np.stack([r * u, r * v, r, p / (gamma - 1) + 0.5 * r * (u * u + v * v)])
+
+
+def rel_linf(a, b):
+    """Per-variable ||a-b||_inf / ||b||_inf, maximised over variables."""
+    num = np.abs(a - b).reshape(a.shape[0], -1).max(axis=1)
+    den = np.abs(b).reshape(b.shape[0], -1).max(axis=1)
+    return float((num / np.maximum(den, 1e-300)).max())
+
+
+def make_pair(case, flux="roe", limiter="vanleer", rk="ssp34", dt="global", cfl=0.5, precision="fp64"):
+    mesh, bc, ref, q, species = case
+    gpu = Solver(mesh, bc, ref, flux=flux, limiter=limiter, rk=rk, precision=precision, dt=dt, cfl=cfl,
+                 species=species)
+    gpu.set_state(q)
+    ora = oracle_py.OracleSolver(mesh.ni, mesh.nj, mesh.nodes.ravel(), bc, flux=flux, limiter=limiter, rk=rk,
+                                 dt=dt, cfl=cfl, species=species, ghost_ref=ref)
+    ora.set_state(q)
+    return gpu, ora
+
+
+def small_cases():
+    rng = np.random.default_rng(7)
+    vort = cases.isentropic_vortex(24)
+    cyl = cases.cylinder(12, 40, mach=0.5, rb=6.0)
+    # perturb the cylinder state so every face sees a jump
+    mesh, bc, ref, q, sp = cyl
+    q = q * (1 + 0.05 * rng.standard_normal(q.shape))
+    q[2:] = np.abs(q[2:])
+    cyl = (mesh, bc, ref, q, sp)
+    quad = cases.quadrant_riemann(13, 11, rng)
+    return {"vortex": vort, "cylinder": cyl, "quadrant": quad}
+
+
+CASES = small_cases()
+FLUXES = ["roe", "slau", "slau_ref", "ausmpup", "rusanov", "central"]
+LIMITERS = ["nolimit1", "nolimit2", "nolimit3", "vanalbada", "minmod", "superbee", "mc", "vanleer",
+            "vanleer_ref", "cada3"]
+
+
+def residual_scale(r):
+    return np.abs(r[:4]).reshape(4, -1).max(axis=1)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("flux", FLUXES)
+def test_residual_parity_fluxes(name, flux):
+    gpu, ora = make_pair(CASES[name], flux=flux, limiter="vanalbada")
+    rg, ro = gpu.residual(), ora.residual()
+    scale = np.maximum(residual_scale(ro), 1e-300)
+    err = (np.abs(rg[:4] - ro[:4]).reshape(4, -1).max(axis=1) / scale).max()
+    assert err <= 1e-11, err
+    assert np.abs(rg[4] - ro[4]).max() <= 1e-12 * np.abs(ro[4]).max()
+
+
+@pytest.mark.parametrize("limiter", LIMITERS)
+def test_residual_parity_limiters(limiter):
+    gpu, ora = make_pair(CASES["cylinder"], flux="roe", limiter=limiter)
+    rg, ro = gpu.residual(), ora.residual()
+    err = (np.abs(rg[:4] - ro[:4]).reshape(4, -1).max(axis=1) / residual_scale(ro)).max()
+    assert err <= 1e-11, err
+
+
+@pytest.mark.parametrize("name,dt", [("vortex", "global"), ("cylinder", "local"), ("quadrant", "global"),
+                                     ("cylinder", "global")])
+@pytest.mark.parametrize("rk", ["ssp11", "ssp22", "ssp33", "ssp34"])
+def test_one_step_parity(name, dt, rk):
+    gpu, ora = make_pair(CASES[name], flux="roe" if name != "quadrant" else "slau", limiter="vanleer", rk=rk,
+                         dt=dt)
+    st = gpu.step(1)
+    dto, _ = ora.step(1)
+    err = rel_linf(prim2cons(gpu.get_state()), prim2cons(ora.get_state()))
+    assert err <= TOL64, err
+    assert st.dt == pytest.approx(dto, rel=1e-12)
+
+
+def test_vortex_ten_steps_each_step_parity():
+    """Per-step parity over 10 steps: each GPU step starts from the oracle's state."""
+    gpu, ora = make_pair(CASES["vortex"], flux="roe", limiter="vanleer")
+    for _ in range(10):
+        gpu.set_state(ora.get_state())
+        gpu.step(1)
+        ora.step(1)
+        err = rel_linf(prim2cons(gpu.get_state()), prim2cons(ora.get_state()))
+        assert err <= TOL64, err
+
+
+def test_vortex_free_running_parity():
+    """30 free-running steps: accumulated drift stays at round-off."""
+    gpu, ora = make_pair(CASES["vortex"], flux="roe", limiter="vanleer")
+    gpu.step(30)
+    ora.step(30)
+    err = rel_linf(prim2cons(gpu.get_state()), prim2cons(ora.get_state()))
+    assert err <= 1e-11, err
+
+
+def test_periodic_conservation():
+    mesh, bc, ref, q, sp = CASES["vortex"]
+    gpu = Solver(mesh, bc, ref, flux="roe", limiter="vanleer", species=sp)
+    gpu.set_state(q)
+    before = prim2cons(gpu.get_state()).reshape(4, -1).sum(axis=1)
+    gpu.step(5)
+    after = prim2cons(gpu.get_state()).reshape(4, -1).sum(axis=1)
+    assert np.allclose(after, before, rtol=1e-13, atol=1e-11)
+
+
+def test_freestream_preserved_on_ogrid():
+    mesh, bc, ref, q, sp = cases.cylinder(16, 48, mach=0.4, rb=8.0)
+    # far field everywhere: no wall, so the uniform state is an exact solution
+    gpu = Solver(mesh, ["riemann", "riemann", "periodic", "periodic"], [ref[1][:, :1].repeat(48, 1)] + ref[1:],
+                 flux="roe", limiter="vanalbada", dt="local", species=sp)
+    gpu.set_state(q)
+    gpu.step(3)
+    assert np.abs(gpu.get_state() - q).max() < 1e-12
+
+
+def test_deterministic():
+    outs = []
+    for _ in range(2):
+        gpu, _ = make_pair(CASES["cylinder"], flux="ausmpup", limiter="minmod", dt="local")
+        gpu.step(4)
+        outs.append(gpu.get_state())
+    assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("name,dt", [("vortex", "global"), ("cylinder", "local")])
+def test_fp32_error_vs_fp64_oracle(name, dt):
+    gpu, ora = make_pair(CASES[name], flux="roe", limiter="vanalbada", dt=dt, precision="fp32")
+    gpu.step(3)
+    ora.step(3)
+    err = rel_linf(prim2cons(gpu.get_state()), prim2cons(ora.get_state()))
+    assert err < 1e-4, err
+
+
+def test_nonphysical_state_is_reported():
+    """A poisoned input (negative pressure) is reported as HC_ERR_NONPHYSICAL; the context stays usable."""
+    from hyperboliconvergence_gb300 import HCError
+    mesh, bc, ref, q, sp = CASES["vortex"]
+    gpu = Solver(mesh, bc, ref, flux="roe", limiter="vanleer", species=sp)
+    bad = q.copy()
+    bad[3, 5, 5] = -1.0
+    gpu.set_state(bad)
+    with pytest.raises(HCError) as e:
+        gpu.step(1)
+    assert e.value.code == 3

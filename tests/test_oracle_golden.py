@@ -1,0 +1,84 @@
+"""Pin the CPU oracle to the reference: every pointwise function of the oracle
+must reproduce the golden vectors produced by the reference's own headers
+(tests/golden/make_golden.py) bit for bit."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle_py
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "pointwise_golden.npz")
+
+
+@pytest.fixture(scope="module")
+def g():
+    return np.load(GOLD)
+
+
+@pytest.fixture(scope="module")
+def o():
+    return oracle_py.pointwise()
+
+
+def same(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape
+    assert np.array_equal(a, b, equal_nan=True), f"max abs diff {np.nanmax(np.abs(a - b))}"
+
+
+def test_surface_volume(g, o):
+    same([o.surface(a, b) for a, b in zip(g["surface_p0"], g["surface_p1"])], g["surface_out"])
+    same([o.volume(q) for q in g["volume_in"]], g["volume_out"])
+
+
+@pytest.mark.parametrize("kind", [0, 2, 3, 4, 5])
+def test_fluxes(g, o, kind):
+    f, sp = g["surface_out"], g["species"]
+    got = [o.flux(kind, sp, f[m], g["flux_ql"][m], g["flux_qr"][m]) for m in range(len(f))]
+    same(got, g[f"flux_{kind}"])
+
+
+def test_exact_flux(g, o):
+    f, sp = g["surface_out"], g["species"]
+    same([o.exact_flux(sp, f[m][3:5].copy(), g["flux_ql"][m]) for m in range(len(f))], g["exact_flux"])
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2, 3, 4, 5, 6, 8, 9])
+def test_limiters(g, o, kind):
+    same([o.limit(kind, a, b) for a, b in g["limit_ab"]], g[f"limit_{kind}"])
+
+
+def test_transforms(g, o):
+    sp = g["species"]
+    same([o.prim2state(sp, q) for q in g["flux_ql"]], g["state_out"])
+    same([o.prim2cons(sp, q) for q in g["flux_ql"]], g["prim2cons_out"])
+    same([o.cons2prim(sp, q) for q in g["cons2prim_in"]], g["cons2prim_out"])
+    for k in range(4):
+        same([o.delta(k, sp, q, d) for q, d in zip(g["flux_ql"], g["delta_in"])], g[f"delta_{k}"])
+
+
+@pytest.mark.parametrize("kind", [2, 3])
+def test_farfield_updates(g, o, kind):
+    f, sp = g["surface_out"], g["species"]
+    same([o.bc_update(kind, sp, f[m], g["flux_ql"][m], g["bc_qf"][m]) for m in range(len(f))], g[f"bc_{kind}"])
+
+
+def test_wall_flux(g, o):
+    f, sp = g["surface_out"], g["species"]
+    same([o.wall_flux(sp, f[m], g["flux_ql"][m], g["wall_dq"][m]) for m in range(len(f))], g["wall_out"])
+
+
+def test_rk_tables_and_meshes(g, o):
+    for k in range(4):
+        same(o.rk_table(k), g[f"rk_{k}"])
+    same(o.cylinder_nodes(12, 16, 0.5, 20.0), g["cyl_nodes"])
+    same(o.linspace_nodes(9, 7, 0.0, 10.0, -1.0, 3.0), g["lin_nodes"])
+
+
+def test_vanleer_decision(o):
+    """The harmonic-mean van Leer slope used for the van Leer configs, and the
+    literal reference expression kept beside it."""
+    assert o.limit(7, 0.2, 0.5) == pytest.approx(2 * 0.2 * 0.5 / 0.7)
+    assert o.limit(7, 0.2, -0.5) == 0.0
+    assert o.limit(8, 0.2, 0.5) == pytest.approx((0.5 + 0.5) / (0.2 + 0.5))
