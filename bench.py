@@ -184,7 +184,8 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         pg = dist
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     mesh, bc, ref, q, species = cases.cylinder(NR, NTH, mach=MACH)
     s = Solver(mesh, bc, ref, flux=FLUX, limiter=LIMITER, rk=RKT, precision="fp64", dt=DTMODE, cfl=CFL,
                species=species, stream=stream.cuda_stream)
@@ -239,13 +240,13 @@ def run_gpu(args):
     for _ in range(2):
         s.set_state(in_np)
         s.step(1)
-        out_np[...] = s.get_state()
+        s.get_state(out=out_np)
     barrier()
     t0 = time.perf_counter()
     for _ in range(ke):
         s.set_state(in_np)
         s.step(1)
-        out_np[...] = s.get_state()
+        s.get_state(out=out_np)
     barrier()
     el = time.perf_counter() - t0
     tt = torch.tensor([el], dtype=torch.float64, device="cuda")

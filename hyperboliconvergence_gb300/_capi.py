@@ -51,6 +51,7 @@ def _declare(lib):
         "hc_context_create": [C.POINTER(Config), C.POINTER(p)],
         "hc_context_destroy": [p],
         "hc_set_stream": [p, v],
+        "hc_get_stream": [p, C.POINTER(C.c_void_p)],
         "hc_mesh_upload": [p, i, i, dp],
         "hc_set_species": [p, d, d, d],
         "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],

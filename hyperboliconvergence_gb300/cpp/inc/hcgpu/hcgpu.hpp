@@ -1,0 +1,197 @@
+// hcgpu.hpp -- C++20 host adapter with the reference's interfaces for the
+// residual-and-timestep path, forwarding to the C ABI of include/hc.h.
+//
+// A driver written against the reference (cpp/script/euler/cylinder2D.cpp,
+// gresho2D.cpp) changes its namespace and its execution policy:
+//
+//   const auto rk  = hcgpu::ODE::Explicit::ssp34<double>();
+//   const hcgpu::UnsteadyTimeControls<double> tc{.nTimesteps = 100, .cfl = 0.5};
+//   const auto species = hcgpu::get_air_species<double>();
+//   const auto mesh = hcgpu::make_cylinder_mesh<double>({0.5, 20.}, {512, 1024}, 1.01);
+//   hcgpu::SolutionField<double> q(mesh.ni, mesh.nj);      // primitive basis
+//   q.bcTypes = {BC::InviscidWall, BC::Riemann, BC::Periodic, BC::Periodic};
+//   const auto hoflux = hcgpu::make_muscl_flux(hcgpu::Limiters::VanAlbada2{}, hcgpu::RoeFlux{});
+//   hcgpu::integrate(hcgpu::execution::gpu, tc, rk, hoflux, species, mesh, q);
+//
+// Errors: the reference asserts; here every failing C-ABI status throws
+// hcgpu::Error carrying the status and hc_last_error_string().
+#pragma once
+
+#include <hc.h>
+
+#include <array>
+#include <cmath>
+#include <cstddef>
+#include <limits>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace hcgpu {
+
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+inline void check(int status) {
+  if (status != HC_OK) throw Error(status, hc_last_error_string());
+}
+
+// Species<Euler> (conservationLaws/euler/euler.h:48-60) and get_air_species
+// (conservationLaws/euler/species.ipp:363-379)
+template <class Real> struct Species {
+  Real gamma, minf, lref, nu, pr, dt, R, gamma1;
+};
+template <class Real> Species<Real> get_air_species() {
+  Species<Real> s{};
+  s.gamma = 1.4; s.minf = 0.0001; s.lref = 1.; s.pr = 0.7; s.nu = 1.81e-5;
+  s.dt = std::numeric_limits<Real>::max(); s.R = 287.058; s.gamma1 = 1. / (s.gamma - 1.);
+  return s;
+}
+
+// Flux tags: the FluxFunctor plug-in point (conservationLaws/base/concepts.h:97-107)
+struct RoeFlux { static constexpr int id = HC_FLUX_ROE; };
+struct Slau { static constexpr int id = HC_FLUX_SLAU; };
+struct SlauRef { static constexpr int id = HC_FLUX_SLAU_REF; };
+struct AusmPlusUP { static constexpr int id = HC_FLUX_AUSMPUP; };
+struct RusanovFlux { static constexpr int id = HC_FLUX_RUSANOV; };
+struct CentralFlux { static constexpr int id = HC_FLUX_CENTRAL; };
+
+// Limiter tags (limiters/limiter.h:46-131)
+namespace Limiters {
+struct NoLimit1 { static constexpr int id = HC_LIM_NOLIMIT1; };
+struct NoLimit2 { static constexpr int id = HC_LIM_NOLIMIT2; };
+struct NoLimit3 { static constexpr int id = HC_LIM_NOLIMIT3; };
+struct VanAlbada2 { static constexpr int id = HC_LIM_VANALBADA; };
+struct MinMod2 { static constexpr int id = HC_LIM_MINMOD; };
+struct Superbee2 { static constexpr int id = HC_LIM_SUPERBEE; };
+struct MonotonizedCentral2 { static constexpr int id = HC_LIM_MC; };
+struct VanLeer2 { static constexpr int id = HC_LIM_VANLEER; };
+struct VanLeer2Ref { static constexpr int id = HC_LIM_VANLEER_REF; };
+struct Cada3 { static constexpr int id = HC_LIM_CADA3; };
+}  // namespace Limiters
+
+// make_muscl_flux (spatial/muscl.h:10-87): the second-order flux descriptor
+struct MusclFlux {
+  int limiter;
+  int flux;
+};
+template <class Limiter, class Flux> MusclFlux make_muscl_flux(const Limiter&, const Flux&) {
+  return MusclFlux{Limiter::id, Flux::id};
+}
+
+// ODE::Explicit::RungeKutta tables (ode.h:85-197); the id selects the device table
+namespace ODE::Explicit {
+template <class Real> struct RungeKutta {
+  unsigned order, nstages;
+  Real maxCFL;
+  int id;
+};
+template <class Real> RungeKutta<Real> ssp11() { return {1, 1, Real(1), HC_RK_SSP11}; }
+template <class Real> RungeKutta<Real> ssp22() { return {2, 2, Real(1), HC_RK_SSP22}; }
+template <class Real> RungeKutta<Real> ssp33() { return {3, 3, Real(1), HC_RK_SSP33}; }
+template <class Real> RungeKutta<Real> ssp34() { return {3, 4, Real(2), HC_RK_SSP34}; }
+}  // namespace ODE::Explicit
+
+// UnsteadyTimeControls (controls.h:11-19)
+template <class Real> struct UnsteadyTimeControls {
+  std::size_t nTimesteps;
+  Real cfl;
+};
+
+// execution policies: the GPU path in global or local timestepping
+namespace execution {
+struct gpu_policy { int dt_mode = HC_DT_GLOBAL; int precision = HC_FP64; };
+inline constexpr gpu_policy gpu{HC_DT_GLOBAL, HC_FP64};
+inline constexpr gpu_policy gpu_local_dt{HC_DT_LOCAL, HC_FP64};
+inline constexpr gpu_policy gpu_fp32{HC_DT_GLOBAL, HC_FP32};
+inline constexpr gpu_policy gpu_fp32_local_dt{HC_DT_LOCAL, HC_FP32};
+}  // namespace execution
+
+// Mesh<2,Real> nodes (mesh/mesh.h:283-321)
+template <class Real> struct Mesh {
+  int ni = 0, nj = 0;
+  std::vector<double> nodes;  // (ni+1)*(nj+1) x,y pairs
+};
+template <class Real>
+Mesh<Real> make_cylinder_mesh(const std::array<Real, 2> lengths, const std::array<std::size_t, 2> ncells,
+                              double stretch = 1.0) {
+  Mesh<Real> m;
+  m.ni = int(ncells[0]); m.nj = int(ncells[1]);
+  m.nodes.resize(std::size_t(m.ni + 1) * (m.nj + 1) * 2);
+  check(hc_mesh_cylinder_nodes(m.ni, m.nj, lengths[0], lengths[1], stretch, m.nodes.data()));
+  return m;
+}
+template <class Real>
+Mesh<Real> make_linspace_mesh(const std::array<std::size_t, 2> cellDims, Real lox, Real hix, Real loy, Real hiy) {
+  Mesh<Real> m;
+  m.ni = int(cellDims[0]); m.nj = int(cellDims[1]);
+  m.nodes.resize(std::size_t(m.ni + 1) * (m.nj + 1) * 2);
+  check(hc_mesh_linspace_nodes(m.ni, m.nj, lox, hix, loy, hiy, m.nodes.data()));
+  return m;
+}
+
+// EulerBCs (conservationLaws/euler/euler.h:34-41)
+enum class BC { Periodic = HC_BC_PERIODIC, Riemann = HC_BC_RIEMANN, Entropy = HC_BC_ENTROPY,
+                Fixed = HC_BC_FIXED, InviscidWall = HC_BC_WALL };
+
+// SolutionField (solutionField/solutionField.h:56-91) in the primitive basis:
+// interior as 4 planes {u, v, rho, p}; boundary[side] the reference layer,
+// 4 planes per side face (nj faces on sides 0/1, ni on 2/3).
+template <class Real> struct SolutionField {
+  int ni, nj;
+  std::vector<double> interior;
+  std::array<std::vector<double>, 4> boundary;
+  std::array<BC, 4> bcTypes{BC::Periodic, BC::Periodic, BC::Periodic, BC::Periodic};
+  SolutionField(int ni_, int nj_) : ni(ni_), nj(nj_), interior(std::size_t(4) * ni_ * nj_) {
+    for (int s = 0; s < 4; ++s) boundary[s].assign(std::size_t(4) * (s < 2 ? nj_ : ni_), 0.0);
+  }
+  double& operator()(int var, int i, int j) { return interior[(std::size_t(var) * ni + i) * nj + j]; }
+  void fill_boundary(int side, const std::array<double, 4>& prim) {
+    const std::size_t n = boundary[side].size() / 4;
+    for (int v = 0; v < 4; ++v)
+      for (std::size_t k = 0; k < n; ++k) boundary[side][v * n + k] = prim[v];
+  }
+};
+
+// RAII context over the C ABI
+class Context {
+ public:
+  Context(const hc_config& cfg) { check(hc_context_create(&cfg, &ctx_)); }
+  ~Context() { hc_context_destroy(ctx_); }
+  Context(const Context&) = delete;
+  Context& operator=(const Context&) = delete;
+  hc_ctx* get() const { return ctx_; }
+
+ private:
+  hc_ctx* ctx_ = nullptr;
+};
+
+// integrate (timestepping/rungeKutta.h:37-167): advances q by nTimesteps RK
+// steps on the GPU and returns the last step's statistics.
+template <class Real>
+hc_step_stats integrate(const execution::gpu_policy policy, const UnsteadyTimeControls<Real>& timeControls,
+                        const ODE::Explicit::RungeKutta<Real>& rungeKutta, const MusclFlux& flux2,
+                        const Species<Real>& species, const Mesh<Real>& mesh, SolutionField<Real>& q) {
+  if (q.ni != mesh.ni || q.nj != mesh.nj) throw Error(HC_ERR_ARG, "solution field and mesh shapes differ");
+  hc_config cfg{flux2.flux, flux2.limiter, rungeKutta.id, policy.precision, policy.dt_mode,
+                double(timeControls.cfl)};
+  Context ctx(cfg);
+  check(hc_mesh_upload(ctx.get(), mesh.ni, mesh.nj, mesh.nodes.data()));
+  check(hc_set_species(ctx.get(), species.gamma, species.R, species.minf));
+  int bct[4];
+  const double* refs[4];
+  for (int s = 0; s < 4; ++s) {
+    bct[s] = int(q.bcTypes[s]);
+    refs[s] = q.boundary[s].data();
+  }
+  check(hc_set_bcs(ctx.get(), bct, refs));
+  check(hc_state_upload(ctx.get(), q.interior.data()));
+  hc_step_stats st{};
+  check(hc_step(ctx.get(), int(timeControls.nTimesteps), &st));
+  check(hc_state_download(ctx.get(), q.interior.data()));
+  return st;
+}
+
+}  // namespace hcgpu

@@ -325,7 +325,15 @@ int hc_context_destroy(hc_ctx* c) {
 
 int hc_set_stream(hc_ctx* c, void* stream) {
   if (int st = check_ctx(c)) return st;
-  c->stream = stream ? (cudaStream_t)stream : c->own;
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  c->stream = (cudaStream_t)stream;
+  return HC_OK;
+}
+
+int hc_get_stream(hc_ctx* c, void** stream) {
+  if (int st = check_ctx(c)) return st;
+  if (!stream) return fail(HC_ERR_ARG, "null output");
+  *stream = (void*)c->stream;
   return HC_OK;
 }
 

@@ -269,7 +269,9 @@ template <class R> __device__ __forceinline__ Flux5<R> ausmpup_flux(const Gas<R>
   const R as = fmin(ars, als);
   const R ml = unl / as, mr = unr / as;
   const R m0 = sqrt(R(0.5) * (ml * ml + mr * mr));
-  const R m0c = (m0 < g.minf) ? g.minf : ((R(1) < m0) ? R(1) : m0);
+  // std::clamp(m0, minf, 1) as libstdc++ evaluates it: min(max(m0, minf), 1)
+  const R mlo = (m0 < g.minf) ? g.minf : m0;
+  const R m0c = (R(1) < mlo) ? R(1) : mlo;
   const R fa = m0c * (R(2) - m0c);
   const bool lsup = fabs(ml) > R(1), rsup = fabs(mr) > R(1);
   const R mlp = lsup ? ms_m1(R(1), ml) : ms_m4(R(1), ml, beta);

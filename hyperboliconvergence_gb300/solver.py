@@ -75,7 +75,7 @@ class Solver:
         check(self.lib.hc_context_create(C.byref(cfg), C.byref(h)))
         self.h = h
         if stream is not None:
-            check(self.lib.hc_set_stream(self.h, C.c_void_p(int(stream))))
+            self.set_stream(stream)
         check(self.lib.hc_mesh_upload(self.h, mesh.ni, mesh.nj, _dptr(mesh.nodes)))
         check(self.lib.hc_set_species(self.h, *[float(s) for s in species]))
         bct = (C.c_int * 4)(*[BC[b] if isinstance(b, str) else int(b) for b in bc])
@@ -100,7 +100,13 @@ class Solver:
     __del__ = close
 
     def set_stream(self, stream) -> None:
-        check(self.lib.hc_set_stream(self.h, C.c_void_p(int(stream) if stream else 0)))
+        """Run on this cudaStream_t handle (0 = the legacy default stream)."""
+        check(self.lib.hc_set_stream(self.h, C.c_void_p(int(stream) if stream else None)))
+
+    def get_stream(self) -> int:
+        out = C.c_void_p()
+        check(self.lib.hc_get_stream(self.h, C.byref(out)))
+        return out.value or 0
 
     # -- solution field ------------------------------------------------------
     def set_state(self, prim: np.ndarray) -> None:
@@ -109,8 +115,13 @@ class Solver:
             raise ValueError(f"state must have shape (4, {self.mesh.ni}, {self.mesh.nj})")
         check(self.lib.hc_state_upload(self.h, _dptr(a)))
 
-    def get_state(self) -> np.ndarray:
-        out = np.empty((4, self.mesh.ni, self.mesh.nj))
+    def get_state(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Download the primitive state (into ``out`` when given: C-contiguous float64)."""
+        if out is None:
+            out = np.empty((4, self.mesh.ni, self.mesh.nj))
+        elif out.shape != (4, self.mesh.ni, self.mesh.nj) or out.dtype != np.float64 or \
+                not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a C-contiguous float64 array of the state's shape")
         check(self.lib.hc_state_download(self.h, _dptr(out)))
         return out
 

@@ -87,8 +87,11 @@ typedef struct {
 /* Context lifetime.  Replaces the integrate() set-up of timestepping/rungeKutta.h:44-79. */
 int hc_context_create(const hc_config* cfg, hc_ctx** out);
 int hc_context_destroy(hc_ctx* ctx);
-/* Run the context's kernels on this CUDA stream (a cudaStream_t; 0 = the context's own). */
+/* Run the context's kernels on this CUDA stream (a cudaStream_t; NULL = the legacy
+ * default stream).  A new context runs on a non-blocking stream of its own, which
+ * hc_get_stream returns. */
 int hc_set_stream(hc_ctx* ctx, void* stream);
+int hc_get_stream(hc_ctx* ctx, void** stream);
 
 /* Mesh<2,Real> nodes (mesh/mesh.h:283-321); cells and face metrics are derived on the
  * device: geom::volume/surface, dual, xmetrics (geometry/volume.ipp:55-96,

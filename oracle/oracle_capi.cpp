@@ -43,16 +43,19 @@ void* hco_create(int ni, int nj, const double* nodes, const int* bc, int flux, i
 }
 void hco_destroy(void* h) { delete static_cast<S*>(h); }
 
-// reference (layer-1) values of side `side`: nface x 4 primitive values
+// reference (layer-1) values of side `side`: 4 planes of nface primitive values
 void hco_set_ghost_ref(void* h, int side, const double* prim) {
   S* s = static_cast<S*>(h);
-  for (int k = 0; k < s->nface(side); ++k)
-    for (int v = 0; v < 4; ++v) s->ghost[side][size_t(k) * 8 + 4 + v] = prim[size_t(k) * 4 + v];
+  const size_t nf = s->nface(side);
+  for (size_t k = 0; k < nf; ++k)
+    for (int v = 0; v < 4; ++v) s->ghost[side][k * 8 + 4 + v] = prim[v * nf + k];
 }
+// ghost (layer-0) values of side `side` after the last boundary update: 4 planes
 void hco_get_ghost(void* h, int side, double* prim) {
   S* s = static_cast<S*>(h);
-  for (int k = 0; k < s->nface(side); ++k)
-    for (int v = 0; v < 4; ++v) prim[size_t(k) * 4 + v] = s->ghost[side][size_t(k) * 8 + v];
+  const size_t nf = s->nface(side);
+  for (size_t k = 0; k < nf; ++k)
+    for (int v = 0; v < 4; ++v) prim[v * nf + k] = s->ghost[side][k * 8 + v];
 }
 // state as 4 planes of ni*nj primitive values
 void hco_set_state(void* h, const double* soa) {

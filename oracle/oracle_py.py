@@ -200,8 +200,10 @@ class OracleSolver:
         if ghost_ref is not None:
             for side in range(4):
                 if ghost_ref[side] is not None:
-                    self.lib.hco_set_ghost_ref(self.h, side,
-                                               np.ascontiguousarray(ghost_ref[side], dtype=np.float64))
+                    nf = nj if side < 2 else ni
+                    arr = np.ascontiguousarray(np.broadcast_to(
+                        np.asarray(ghost_ref[side], dtype=np.float64).reshape(4, -1), (4, nf)))
+                    self.lib.hco_set_ghost_ref(self.h, side, arr)
 
     def __del__(self):
         if getattr(self, "h", None):
