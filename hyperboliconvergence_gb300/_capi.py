@@ -88,6 +88,7 @@ def load(build_if_missing: bool = True):
         _build.build()
     lib = C.CDLL(LIB_PATH)
     _declare(lib)
+    _declare_batch(lib)
     _lib = lib
     return lib
 
@@ -102,3 +103,38 @@ def header_symbols() -> list[str]:
     import re
     txt = open(HEADER).read()
     return sorted(set(re.findall(r"\b(hc_[a-z0-9_]+)\s*\(", txt)))
+
+
+class Schedule(C.Structure):
+    _fields_ = [("tile", C.c_int), ("ctas_per_sm", C.c_int), ("order", C.c_int), ("ms_per_step", C.c_float)]
+
+
+TILE = {"8x32": 0, "4x32": 1, "16x16": 2}
+ORDER = {"natural": 0, "largest_first": 1}
+BATCH_MODE = {"persistent": 0, "per_instance": 1}
+
+
+def _declare_batch(lib):
+    p, i, d = C.c_void_p, C.c_int, C.c_double
+    dp = C.POINTER(C.c_double)
+    sig = {
+        "hc_batch_create": [C.POINTER(Config), i, C.POINTER(i), C.POINTER(i), C.POINTER(dp), C.POINTER(i),
+                            C.POINTER(dp), d, d, d, C.POINTER(p)],
+        "hc_batch_destroy": [p],
+        "hc_batch_set_stream": [p, p],
+        "hc_batch_state_upload": [p, i, dp],
+        "hc_batch_state_download": [p, i, dp],
+        "hc_batch_set_schedule": [p, C.POINTER(Schedule)],
+        "hc_batch_get_schedule": [p, C.POINTER(Schedule)],
+        "hc_batch_step_async": [p, i, i],
+        "hc_batch_graph_capture": [p, i],
+        "hc_batch_graph_launch": [p],
+        "hc_batch_sync": [p, C.POINTER(StepStats)],
+        "hc_batch_autotune": [p, i, C.POINTER(Schedule)],
+    }
+    for name, args in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    lib.hc_batch_kernel_launches.argtypes = [p]
+    lib.hc_batch_kernel_launches.restype = C.c_longlong

@@ -1,0 +1,124 @@
+"""Batched path: many independent meshes of uneven sizes in one set of device
+buffers, advanced by one persistent launch per RK stage (include/hc.h,
+hc_batch_*).  The reference runs one mesh per process and has no counterpart.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import (BATCH_MODE, BC, DTMODE, FLUX, LIMITER, ORDER, PRECISION, RK, TILE, Config, Schedule,
+                    StepStats, check)
+from .solver import Mesh, _dptr
+
+
+class Batch:
+    """Instances = list of (mesh, bc, ref, state); shared flux/limiter/RK/CFL/species."""
+
+    def __init__(self, instances, flux="slau", limiter="vanalbada", rk="ssp34", precision="fp32", dt="global",
+                 cfl=0.5, species=(1.4, 287.058, 0.5), stream=None):
+        self.lib = _capi.load()
+        self.meshes = [inst[0] for inst in instances]
+        n = len(instances)
+        cfg = Config(FLUX[flux], LIMITER[limiter], RK[rk], PRECISION[precision], DTMODE[dt], float(cfl))
+        ni = (C.c_int * n)(*[m.ni for m in self.meshes])
+        nj = (C.c_int * n)(*[m.nj for m in self.meshes])
+        nodes = (C.POINTER(C.c_double) * n)(*[_dptr(m.nodes) for m in self.meshes])
+        bcs = (C.c_int * (4 * n))()
+        refs = (C.POINTER(C.c_double) * (4 * n))()
+        self._keep = []
+        for k, (mesh, bc, ref, _q) in enumerate(instances):
+            for s in range(4):
+                bcs[4 * k + s] = BC[bc[s]] if isinstance(bc[s], str) else int(bc[s])
+                r = None if ref is None else ref[s]
+                if r is None:
+                    refs[4 * k + s] = C.POINTER(C.c_double)()
+                else:
+                    arr = np.ascontiguousarray(np.broadcast_to(np.asarray(r, dtype=np.float64).reshape(4, -1),
+                                                               (4, mesh.nface(s))))
+                    self._keep.append(arr)
+                    refs[4 * k + s] = _dptr(arr)
+        h = C.c_void_p()
+        check(self.lib.hc_batch_create(C.byref(cfg), n, ni, nj, nodes, bcs, refs, *[float(x) for x in species],
+                                       C.byref(h)))
+        self.h = h
+        self.n = n
+        if stream is not None:
+            check(self.lib.hc_batch_set_stream(self.h, C.c_void_p(int(stream) if stream else None)))
+        for k, inst in enumerate(instances):
+            self.set_state(k, inst[3])
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.hc_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    @property
+    def cells(self) -> int:
+        return sum(m.ni * m.nj for m in self.meshes)
+
+    def set_state(self, k: int, prim: np.ndarray) -> None:
+        a = np.ascontiguousarray(prim, dtype=np.float64)
+        m = self.meshes[k]
+        if a.shape != (4, m.ni, m.nj):
+            raise ValueError("state shape mismatch")
+        check(self.lib.hc_batch_state_upload(self.h, k, _dptr(a)))
+
+    def get_state(self, k: int) -> np.ndarray:
+        m = self.meshes[k]
+        out = np.empty((4, m.ni, m.nj))
+        check(self.lib.hc_batch_state_download(self.h, k, _dptr(out)))
+        return out
+
+    def schedule(self) -> dict:
+        s = Schedule()
+        check(self.lib.hc_batch_get_schedule(self.h, C.byref(s)))
+        inv_t = {v: k for k, v in TILE.items()}
+        inv_o = {v: k for k, v in ORDER.items()}
+        return {"tile": inv_t[s.tile], "ctas_per_sm": s.ctas_per_sm, "order": inv_o[s.order],
+                "ms_per_step": float(s.ms_per_step)}
+
+    def set_schedule(self, tile="8x32", ctas_per_sm=2, order="largest_first") -> None:
+        s = Schedule(TILE[tile], int(ctas_per_sm), ORDER[order], 0.0)
+        check(self.lib.hc_batch_set_schedule(self.h, C.byref(s)))
+
+    def autotune(self, steps: int = 2) -> dict:
+        s = Schedule()
+        check(self.lib.hc_batch_autotune(self.h, int(steps), C.byref(s)))
+        return self.schedule() | {"ms_per_step": float(s.ms_per_step)}
+
+    def step_async(self, n: int = 1, mode: str = "persistent") -> None:
+        check(self.lib.hc_batch_step_async(self.h, int(n), BATCH_MODE[mode]))
+
+    def capture(self, n: int) -> None:
+        check(self.lib.hc_batch_graph_capture(self.h, int(n)))
+
+    def replay(self) -> None:
+        check(self.lib.hc_batch_graph_launch(self.h))
+
+    def sync(self):
+        st = (StepStats * self.n)()
+        check(self.lib.hc_batch_sync(self.h, st))
+        return list(st)
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.hc_batch_kernel_launches(self.h))
+
+
+def uneven_riemann_batch(n: int, seed: int, sizes=tuple(range(64, 1025, 32))):
+    """n four-quadrant Riemann instances with Ni, Nj drawn uniformly from `sizes`."""
+    from . import cases
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        ni, nj = int(rng.choice(sizes)), int(rng.choice(sizes))
+        mesh, bc, ref, q, _sp = cases.quadrant_riemann(ni, nj, rng)
+        out.append((mesh, bc, ref, q))
+    return out
+
+
+__all__ = ["Batch", "uneven_riemann_batch", "Mesh"]

@@ -1,7 +1,6 @@
 // hc_api.cu -- the C ABI of include/hc.h: contexts, mesh/state transfer and
 // the explicit RK time loop over the fused stage kernels.
-#include "../../include/hc.h"
-#include "hc_launch.h"
+#include "hc_host.h"
 #include "hc_geometry.cuh"
 
 #include <cmath>
@@ -13,69 +12,31 @@
 using namespace hc;
 
 namespace {
-
 thread_local std::string g_last_error;
-
-int fail(int code, const std::string& msg) {
-  g_last_error = msg;
-  return code;
-}
-
-#define HC_CUDA(call)                                                                              \
-  do {                                                                                             \
-    cudaError_t e_ = (call);                                                                       \
-    if (e_ != cudaSuccess) return fail(HC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
-
-// RK tables ssp11..ssp34 (ode.h:107-197)
-struct RKTab {
-  int nst;
-  double alpha[4][4];
-  double beta[4];
-};
-RKTab rk_table(int kind) {
-  RKTab t{};
-  if (kind == HC_RK_SSP11) { t.nst = 1; t.beta[0] = 1.0; t.alpha[0][0] = 1.0; }
-  else if (kind == HC_RK_SSP22) {
-    t.nst = 2; t.beta[0] = 1.0; t.beta[1] = 1.0;
-    t.alpha[0][0] = 1.0; t.alpha[1][0] = 0.5; t.alpha[1][1] = 0.5;
-  } else if (kind == HC_RK_SSP33) {
-    t.nst = 3; t.beta[0] = 1.0; t.beta[1] = 0.5; t.beta[2] = 1.0;
-    t.alpha[0][0] = 1.; t.alpha[1][0] = 0.5; t.alpha[1][1] = 0.5;
-    t.alpha[2][0] = 1. / 6.; t.alpha[2][1] = 1. / 6.; t.alpha[2][2] = 2. / 3.;
-  } else {
-    t.nst = 4; t.beta[0] = 0.5; t.beta[1] = 1.0; t.beta[2] = 0.5; t.beta[3] = 1.0;
-    t.alpha[0][0] = 1.0; t.alpha[1][0] = 0.5; t.alpha[1][1] = 0.5;
-    t.alpha[2][0] = 1. / 3.; t.alpha[2][1] = 1. / 3.; t.alpha[2][2] = 1. / 3.;
-    t.alpha[3][0] = 1. / 6.; t.alpha[3][1] = 1. / 6.; t.alpha[3][2] = 1. / 6.; t.alpha[3][3] = 1. / 2.;
-  }
-  return t;
-}
-
-template <class R> using StageFn = cudaError_t (*)(const StageArgs<R>&, int, cudaStream_t);
-
-template <class R> StageFn<R> stage_fn(int flux) {
-  switch (flux) {
-    case FLUX_ROE: return launch_stage<R, FLUX_ROE>;
-    case FLUX_SLAU: return launch_stage<R, FLUX_SLAU>;
-    case FLUX_SLAU_REF: return launch_stage<R, FLUX_SLAU_REF>;
-    case FLUX_AUSMPUP: return launch_stage<R, FLUX_AUSMPUP>;
-    case FLUX_RUSANOV: return launch_stage<R, FLUX_RUSANOV>;
-    default: return launch_stage<R, FLUX_CENTRAL>;
-  }
-}
-template <class R> cudaError_t prepare(int flux) {
-  switch (flux) {
-    case FLUX_ROE: return prepare_stage<R, FLUX_ROE>();
-    case FLUX_SLAU: return prepare_stage<R, FLUX_SLAU>();
-    case FLUX_SLAU_REF: return prepare_stage<R, FLUX_SLAU_REF>();
-    case FLUX_AUSMPUP: return prepare_stage<R, FLUX_AUSMPUP>();
-    case FLUX_RUSANOV: return prepare_stage<R, FLUX_RUSANOV>();
-    default: return prepare_stage<R, FLUX_CENTRAL>();
-  }
-}
-
 }  // namespace
+
+namespace hc {
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+int enqueue_geometry(const GeomBuffers& b, int ni, int nj, const int bc[4], cudaStream_t s) {
+  const size_t n = size_t(ni) * nj;
+  const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
+  const int B = 256;
+  geom_cells_kernel<<<unsigned((n + B - 1) / B), B, 0, s>>>(b.nodes, ni, nj, b.vol, b.cx, b.cy);
+  GeomArgs g{};
+  g.nodes = b.nodes; g.ni = ni; g.nj = nj;
+  for (int k = 0; k < 4; ++k) g.bc[k] = bc[k];
+  g.cx = b.cx; g.cy = b.cy; g.fi = b.fi; g.fj = b.fj; g.xm = b.xm;
+  geom_faces1_kernel<<<(nfi + B - 1) / B, B, 0, s>>>(g, 0);
+  geom_faces1_kernel<<<(nfj + B - 1) / B, B, 0, s>>>(g, 1);
+  geom_xm_kernel<<<unsigned((n + B - 1) / B), B, 0, s>>>(g);
+  geom_faces2_kernel<<<(nfi + B - 1) / B, B, 0, s>>>(g, 0);
+  geom_faces2_kernel<<<(nfj + B - 1) / B, B, 0, s>>>(g, 1);
+  return 6;
+}
+
+}  // namespace hc
 
 struct hc_ctx {
   hc_config cfg{};
@@ -141,17 +102,8 @@ int build_geometry(hc_ctx* c) {
   const int ni = c->ni, nj = c->nj;
   const size_t n = c->ncell();
   const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
-  const int B = 256;
-  geom_cells_kernel<<<unsigned((n + B - 1) / B), B, 0, c->stream>>>(c->nodes, ni, nj, c->vol64, c->cx, c->cy);
-  GeomArgs g{};
-  g.nodes = c->nodes; g.ni = ni; g.nj = nj;
-  for (int k = 0; k < 4; ++k) g.bc[k] = c->bc[k];
-  g.cx = c->cx; g.cy = c->cy; g.fi = c->fi64; g.fj = c->fj64; g.xm = c->xm;
-  geom_faces1_kernel<<<(nfi + B - 1) / B, B, 0, c->stream>>>(g, 0);
-  geom_faces1_kernel<<<(nfj + B - 1) / B, B, 0, c->stream>>>(g, 1);
-  geom_xm_kernel<<<unsigned((n + B - 1) / B), B, 0, c->stream>>>(g);
-  geom_faces2_kernel<<<(nfi + B - 1) / B, B, 0, c->stream>>>(g, 0);
-  geom_faces2_kernel<<<(nfj + B - 1) / B, B, 0, c->stream>>>(g, 1);
+  const GeomBuffers gb{c->nodes, c->cx, c->cy, c->xm, c->vol64, c->fi64, c->fj64};
+  enqueue_geometry(gb, ni, nj, c->bc, c->stream);
   c->launches += 6;
   if (c->fp32) {
     convert_kernel<float><<<1024, 256, 0, c->stream>>>(c->fi64, (float*)c->fi, size_t(FREC) * nfi);
@@ -259,7 +211,14 @@ int read_stats(hc_ctx* c, hc_step_stats* st) {
   HC_CUDA(cudaMemcpyAsync(&info, c->info, sizeof(StepInfo), cudaMemcpyDeviceToHost, c->stream));
   HC_CUDA(cudaStreamSynchronize(c->stream));
   if (st) {
-    st->dt = info.dt;
+    if (c->cfg.dt_mode == HC_DT_LOCAL) {
+      // smallest local timestep of the last step: cfl / max(lambda/V)
+      double rate;
+      std::memcpy(&rate, &info.maxrate, sizeof(double));
+      st->dt = c->cfg.cfl / std::fmax(rate, 2.2250738585072014e-308);
+    } else {
+      st->dt = info.dt;
+    }
     st->t = info.t;
     st->resnorm = std::sqrt(info.resnorm2);
     st->status = info.status == ST_OK ? HC_OK : HC_ERR_NONPHYSICAL;

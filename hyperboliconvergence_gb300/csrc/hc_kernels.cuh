@@ -111,10 +111,11 @@ template <class R> __device__ __forceinline__ void forward_update(const Gas<R>& 
   qn[0] = s1.u; qn[1] = s1.v; qn[2] = s1.r; qn[3] = s1.p;
 }
 
+// One tile (TI x TJ cells, tile coordinates (bi, bj)) of one RK stage.  Called
+// by every thread of the block; smem_raw holds StageSmem<TI,TJ,R>::bytes.
 template <int TI, int TJ, class R, int FK>
-__global__ void __launch_bounds__(TI * TJ) stage_kernel(const StageArgs<R> a) {
+__device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj, unsigned char* smem_raw) {
   using SM = StageSmem<TI, TJ, R>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   R* sq = reinterpret_cast<R*>(smem_raw);
   R* sm = sq + SM::q_elems;
   R* sfi = sm + SM::m_elems;
@@ -123,7 +124,7 @@ __global__ void __launch_bounds__(TI * TJ) stage_kernel(const StageArgs<R> a) {
   constexpr int NT = TI * TJ;
   const int ni = a.ni, nj = a.nj;
   const size_t ncell = size_t(ni) * nj;
-  const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
+  const int i0 = bi * TI, j0 = bj * TJ;
   const int tid = threadIdx.x;
   const bool per_i = a.bc[0] == BC_PERIODIC, per_j = a.bc[2] == BC_PERIODIC;
   const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
@@ -333,6 +334,13 @@ __global__ void __launch_bounds__(TI * TJ) stage_kernel(const StageArgs<R> a) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) r2 += __shfl_xor_sync(0xffffffffu, r2, o);
     if ((tid & 31) == 0) atomicAdd(&a.info->resnorm2, double(r2));
+    if (a.mode == MODE_FUSED_LOCAL) {
+      // largest lambda/V: the smallest local timestep is cfl over it
+      R rate = own ? lam / a.vol[c] : R(0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) rate = fmax(rate, __shfl_xor_sync(0xffffffffu, rate, o));
+      if ((tid & 31) == 0) atomic_max_rate<R>(a.info, rate);
+    }
   }
   if (!own) return;
   // rungeKuttaAccumulation (timestepping/rungeKutta.h:172-197)
@@ -361,32 +369,150 @@ __global__ void __launch_bounds__(TI * TJ) stage_kernel(const StageArgs<R> a) {
   flag_nonphysical(a.info, qn, int(c));
 }
 
-// Stage-0 update with the global timestep dt = cfl / max(lambda/V)
+template <int TI, int TJ, class R, int FK>
+__global__ void __launch_bounds__(TI * TJ) stage_kernel(const StageArgs<R> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  stage_tile<TI, TJ, R, FK>(a, blockIdx.y, blockIdx.x, smem_raw);
+}
+
+// Stage-0 update of one cell with the global timestep dt = cfl / max(lambda/V)
 // (timestepping/rungeKutta.h:131-154).
+template <class R>
+__device__ __forceinline__ void update0_cell(size_t c, size_t ncell, const Gas<R>& g, const R* __restrict__ q0,
+                                             const R* __restrict__ res0, const R* __restrict__ vol, R alpha00,
+                                             R dts, StepInfo* info, R* __restrict__ q_out) {
+  R tot[4], q[4], qn[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    tot[v] = R(0) + alpha00 * res0[v * ncell + c];
+    q[v] = q0[v * ncell + c];
+  }
+  const R fac = dts / vol[c];
+  forward_update(g, q, tot, fac, qn);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) q_out[v * ncell + c] = qn[v];
+  flag_nonphysical(info, qn, int(c));
+}
+
+template <class R> __device__ __forceinline__ R global_dt(const StepInfo* info, double cfl) {
+  const double rate = fmax(DBL_MIN, __longlong_as_double((long long)info->maxrate));
+  return R(cfl / rate);
+}
+
 template <class R>
 __global__ void update0_kernel(int ni, int nj, Gas<R> g, const R* __restrict__ q0, const R* __restrict__ res0,
                                const R* __restrict__ vol, R alpha00, R beta0, double cfl, StepInfo* info,
                                R* __restrict__ q_out, int advance_time) {
   const size_t ncell = size_t(ni) * nj;
-  const double rate = fmax(DBL_MIN, __longlong_as_double((long long)info->maxrate));
-  const R dt = R(cfl / rate);
+  const R dt = global_dt<R>(info, cfl);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     info->dt = double(dt);
     if (advance_time) info->t += double(dt);
   }
-  for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < ncell; c += size_t(gridDim.x) * blockDim.x) {
-    R tot[4], q[4], qn[4];
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      tot[v] = R(0) + alpha00 * res0[v * ncell + c];
-      q[v] = q0[v * ncell + c];
+  const R dts = beta0 * dt;
+  for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < ncell; c += size_t(gridDim.x) * blockDim.x)
+    update0_cell(c, ncell, g, q0, res0, vol, alpha00, dts, info, q_out);
+}
+
+// ---------------------------------------------------------------- batched path
+// Many independent meshes of uneven sizes advanced by one persistent launch per
+// stage: the tiles of all instances form one work list that a grid of
+// (SMs x ctas_per_sm) CTAs walks round-robin.  Per-instance data live at
+// offsets in pooled buffers; each instance has its own StepInfo (global dt).
+struct BatchInst {
+  int ni, nj;
+  int bc[4];
+  int tiles_i, tiles_j;  // tile grid of this instance for the launch's tile shape
+  long long cell;        // offset of the instance's cells in the cell pools
+  long long fi, fj;      // offsets of its i-/j-face records (records, not values)
+  long long gref[4];     // offsets of its ghost-reference planes (values)
+};
+
+template <class R> struct BatchArgs {
+  const BatchInst* inst;
+  const int* order;        // work list: packed (instance << 16 | tile index within the instance) entries
+  int nwork;
+  const int* tile_begin;   // not used by the kernels (host bookkeeping)
+  Gas<R> gas;
+  int limiter;
+  const R* q;              // stage input pool
+  const R* q0;
+  R* q_out;
+  R* res_out;
+  const R* res_prev[4];
+  const R* fi;
+  const R* fj;
+  const R* vol;
+  const R* gref;
+  R alpha[4];
+  int stage, mode;
+  R beta, cfl;
+  StepInfo* info;          // one per instance
+};
+
+template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const BatchArgs<R>& b, int k) {
+  const BatchInst& in = b.inst[k];
+  StageArgs<R> a;
+  a.ni = in.ni; a.nj = in.nj;
+  for (int s = 0; s < 4; ++s) a.bc[s] = in.bc[s];
+  a.gas = b.gas;
+  a.limiter = b.limiter;
+  const long long n = (long long)in.ni * in.nj;
+  const long long off4 = 4 * in.cell, off5 = 5 * in.cell;
+  a.q = b.q + off4;
+  a.q0 = b.q0 + off4;
+  a.q_out = b.q_out ? b.q_out + off4 : nullptr;
+  a.res_out = b.res_out ? b.res_out + off5 : nullptr;
+  for (int s = 0; s < 4; ++s) a.res_prev[s] = b.res_prev[s] ? b.res_prev[s] + off5 : nullptr;
+  const long long nfi = (long long)(in.ni + 1) * in.nj, nfj = (long long)in.ni * (in.nj + 1);
+  (void)nfi; (void)nfj; (void)n;
+  a.fi = b.fi + (long long)FREC * in.fi;
+  a.fj = b.fj + (long long)FREC * in.fj;
+  a.vol = b.vol + in.cell;
+  for (int s = 0; s < 4; ++s) a.gref[s] = b.gref + in.gref[s];
+  for (int s = 0; s < 4; ++s) a.alpha[s] = b.alpha[s];
+  a.stage = b.stage;
+  a.mode = b.mode;
+  a.beta = b.beta;
+  a.cfl = b.cfl;
+  a.info = b.info + k;
+  a.norm_stage0 = (b.stage == 0);
+  return a;
+}
+
+template <int TI, int TJ, class R, int FK>
+__global__ void __launch_bounds__(TI * TJ) batch_stage_kernel(const BatchArgs<R> b) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  for (int w = blockIdx.x; w < b.nwork; w += gridDim.x) {
+    const int packed = b.order[w];
+    const int k = packed >> 16, t = packed & 0xffff;
+    const StageArgs<R> a = instance_args(b, k);
+    const int tj = b.inst[k].tiles_j;
+    __syncthreads();  // the previous work item may still read shared memory
+    stage_tile<TI, TJ, R, FK>(a, t / tj, t % tj, smem_raw);
+  }
+}
+
+// Stage-0 update of the batch with each instance's own global dt.
+template <int TI, int TJ, class R>
+__global__ void __launch_bounds__(TI * TJ) batch_update0_kernel(const BatchArgs<R> b, double cfl, R alpha00, R beta0) {
+  for (int w = blockIdx.x; w < b.nwork; w += gridDim.x) {
+    const int packed = b.order[w];
+    const int k = packed >> 16, t = packed & 0xffff;
+    const BatchInst& in = b.inst[k];
+    StepInfo* info = b.info + k;
+    const R dt = global_dt<R>(info, cfl);
+    if (t == 0 && threadIdx.x == 0) {
+      info->dt = double(dt);
+      info->t += double(dt);
     }
-    const R dts = beta0 * dt;
-    const R fac = dts / vol[c];
-    forward_update(g, q, tot, fac, qn);
-#pragma unroll
-    for (int v = 0; v < 4; ++v) q_out[v * ncell + c] = qn[v];
-    flag_nonphysical(info, qn, int(c));
+    const int bi = t / in.tiles_j, bj = t % in.tiles_j;
+    const int gi = bi * TI + int(threadIdx.x) / TJ, gj = bj * TJ + int(threadIdx.x) % TJ;
+    if (gi >= in.ni || gj >= in.nj) continue;
+    const size_t ncell = size_t(in.ni) * in.nj;
+    const size_t c = size_t(gi) * in.nj + gj;
+    update0_cell(c, ncell, b.gas, b.q0 + 4 * in.cell, b.res_out + 5 * in.cell, b.vol + in.cell, alpha00,
+                 beta0 * dt, info, b.q_out + 4 * in.cell);
   }
 }
 

@@ -12,6 +12,8 @@ enum TileShape { TILE_8x32 = 0, TILE_4x32 = 1, TILE_16x16 = 2, TILE_COUNT = 3 };
 
 template <class R, int FK> cudaError_t launch_stage(const StageArgs<R>& a, int tile, cudaStream_t s);
 template <class R, int FK> cudaError_t prepare_stage();
+// persistent batched stage: `grid` CTAs walk the work list of b
+template <class R, int FK> cudaError_t launch_batch_stage(const BatchArgs<R>& b, int tile, int grid, cudaStream_t s);
 
 inline void tile_dims(int tile, int* ti, int* tj) {
   switch (tile) {
@@ -26,8 +28,30 @@ inline void tile_dims(int tile, int* ti, int* tj) {
 #define HC_STAGE_INSTANTIATE(FK)                                                                         \
   namespace hc {                                                                                         \
   template <class R, int TI, int TJ> static cudaError_t prep_one() {                                     \
-    return cudaFuncSetAttribute(stage_kernel<TI, TJ, R, FK>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+    cudaError_t e = cudaFuncSetAttribute(stage_kernel<TI, TJ, R, FK>,                                    \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,                    \
+                                         int(StageSmem<TI, TJ, R>::bytes));                              \
+    if (e != cudaSuccess) return e;                                                                      \
+    return cudaFuncSetAttribute(batch_stage_kernel<TI, TJ, R, FK>,                                       \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,                             \
                                 int(StageSmem<TI, TJ, R>::bytes));                                       \
+  }                                                                                                      \
+  template <class R, int TI, int TJ> static void gob(const BatchArgs<R>& b, int grid, cudaStream_t s) {  \
+    batch_stage_kernel<TI, TJ, R, FK><<<grid, TI * TJ, StageSmem<TI, TJ, R>::bytes, s>>>(b);             \
+  }                                                                                                      \
+  template <> cudaError_t launch_batch_stage<double, FK>(const BatchArgs<double>& b, int tile, int grid, \
+                                                         cudaStream_t s) {                               \
+    if (tile == TILE_4x32) gob<double, 4, 32>(b, grid, s);                                               \
+    else if (tile == TILE_16x16) gob<double, 16, 16>(b, grid, s);                                        \
+    else gob<double, 8, 32>(b, grid, s);                                                                 \
+    return cudaGetLastError();                                                                           \
+  }                                                                                                      \
+  template <> cudaError_t launch_batch_stage<float, FK>(const BatchArgs<float>& b, int tile, int grid,   \
+                                                        cudaStream_t s) {                                \
+    if (tile == TILE_4x32) gob<float, 4, 32>(b, grid, s);                                                \
+    else if (tile == TILE_16x16) gob<float, 16, 16>(b, grid, s);                                         \
+    else gob<float, 8, 32>(b, grid, s);                                                                  \
+    return cudaGetLastError();                                                                           \
   }                                                                                                      \
   template <class R, int TI, int TJ> static void go(const StageArgs<R>& a, cudaStream_t s) {             \
     const dim3 grid((a.nj + TJ - 1) / TJ, (a.ni + TI - 1) / TI);                                         \

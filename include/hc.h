@@ -131,6 +131,51 @@ int hc_sync(hc_ctx* ctx, hc_step_stats* stats);
 int hc_mesh_cylinder_nodes(int nr, int nth, double rc, double rb, double stretch, double* nodes_xy);
 int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, double hiy, double* nodes_xy);
 
+/* ---------------------------------------------------------------------------
+ * Batched path: many independent meshes of uneven sizes in one set of buffers.
+ * No counterpart in the reference (it runs one mesh per process).  Each instance
+ * has its own mesh, boundary conditions, state and global dt; all instances
+ * share the configuration and the species.  One persistent launch per RK stage
+ * walks the tiles of every instance; a step sequence can be captured in a CUDA
+ * graph and replayed.  HC_BATCH_PER_INSTANCE runs the same kernels as plain
+ * per-instance launches, for comparison.
+ * ------------------------------------------------------------------------- */
+typedef struct hc_batch hc_batch;
+
+typedef enum { HC_BATCH_PERSISTENT = 0, HC_BATCH_PER_INSTANCE = 1 } hc_batch_mode;
+typedef enum { HC_ORDER_NATURAL = 0, HC_ORDER_LARGEST_FIRST = 1 } hc_batch_order;
+typedef enum { HC_TILE_8x32 = 0, HC_TILE_4x32 = 1, HC_TILE_16x16 = 2 } hc_tile;
+
+typedef struct {
+  int tile;         /* hc_tile: cells per CTA tile */
+  int ctas_per_sm;  /* persistent grid = SM count x ctas_per_sm */
+  int order;        /* hc_batch_order of the work list */
+  float ms_per_step;/* measured by hc_batch_autotune (0 when not measured) */
+} hc_schedule;
+
+/* ninst meshes; nodes[k] as for hc_mesh_upload; bc[4k..4k+3] and ref[4k..4k+3]
+ * as for hc_set_bcs (ref entries may be NULL where hc_set_bcs allows it). */
+int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* nj, const double* const* nodes,
+                    const int* bc, const double* const* ref, double gamma, double gas_constant, double minf,
+                    hc_batch** out);
+int hc_batch_destroy(hc_batch* b);
+int hc_batch_set_stream(hc_batch* b, void* stream);
+int hc_batch_state_upload(hc_batch* b, int inst, const double* prim_soa);
+int hc_batch_state_download(hc_batch* b, int inst, double* prim_soa);
+int hc_batch_set_schedule(hc_batch* b, const hc_schedule* s);
+int hc_batch_get_schedule(hc_batch* b, hc_schedule* s);
+/* Enqueue nsteps RK steps of every instance (hc_batch_mode). */
+int hc_batch_step_async(hc_batch* b, int nsteps, int mode);
+/* Capture nsteps persistent steps into a CUDA graph (replacing any earlier one) and replay it. */
+int hc_batch_graph_capture(hc_batch* b, int nsteps);
+int hc_batch_graph_launch(hc_batch* b);
+/* Wait; stats may be NULL or hold ninst entries (per-instance dt, t, status). */
+int hc_batch_sync(hc_batch* b, hc_step_stats* stats);
+/* Time every schedule candidate on `steps` persistent steps from the current
+ * states (restored afterwards), keep the fastest and return it. */
+int hc_batch_autotune(hc_batch* b, int steps, hc_schedule* best);
+long long hc_batch_kernel_launches(hc_batch* b);
+
 const char* hc_last_error_string(void);
 const char* hc_version(void);
 
