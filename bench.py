@@ -148,6 +148,112 @@ def cpu_baseline(steps_budget_s: float = 12.0, threads: int | None = None):
                       f"-O3 -ffast-math -fopenmp"}
 
 
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def measure_fp32(stream, steps: int):
+    """The same workload in FP32: throughput, HBM roofline and error against FP64."""
+    import torch
+    from hyperboliconvergence_gb300 import cases
+    from hyperboliconvergence_gb300.solver import Solver
+    mesh, bc, ref, q, species = cases.cylinder(NR, NTH, mach=MACH)
+    out = {}
+    states = {}
+    for prec in ("fp32", "fp64"):
+        s = Solver(mesh, bc, ref, flux=FLUX, limiter=LIMITER, rk=RKT, precision=prec, dt=DTMODE, cfl=CFL,
+                   species=species, stream=stream.cuda_stream)
+        s.set_state(q)
+        s.step(3)
+        if prec == "fp32":
+            e0, e1 = _events()
+            torch.cuda.synchronize()
+            e0.record(stream)
+            s.step_async(steps)
+            e1.record(stream)
+            s.sync()
+            ms = e0.elapsed_time(e1) / steps
+            cells = NR * NTH
+            stage_ms = ms / NSTAGES
+            ach = (3 * 4 + 2) * 4 * cells / (stage_ms / 1e3) / 1e9
+            peak, _ = measured_peaks()
+            out = {"value": cells / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+                   "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                                "frac": ach / peak, "alg_bytes_per_cell_stage": 56}}
+            s.set_state(q)
+        s.step(20)
+        states[prec] = s.get_state()
+        s.close()
+    a, b = states["fp32"], states["fp64"]
+    g = 1.4
+
+    def cons(w):
+        u, v, r, p = w
+        return np.stack([r * u, r * v, r, p / (g - 1) + 0.5 * r * (u * u + v * v)])
+    ca, cb = cons(a), cons(b)
+    err = (np.abs(ca - cb).reshape(4, -1).max(1) / np.abs(cb).reshape(4, -1).max(1)).max()
+    out["error_vs_fp64_after_20_steps"] = float(err)
+    return out
+
+
+def measure_batched(stream, ninst: int = 256, steps: int = 3, seed: int = 2026):
+    """The uneven batch: 256 four-quadrant Riemann instances, Ni, Nj from {64,96,...,1024},
+    SLAU + van Albada, ssp34, global dt per instance, FP32.  Persistent batched launches
+    replayed from a CUDA graph against plain per-instance launches."""
+    import torch
+    from hyperboliconvergence_gb300.batch import Batch, uneven_riemann_batch
+    insts = uneven_riemann_batch(ninst, seed)
+    b = Batch(insts, flux="slau", limiter="vanalbada", rk="ssp34", precision="fp32", dt="global", cfl=0.5,
+              stream=stream.cuda_stream)
+    cells = b.cells
+    tuned = b.autotune(steps=1)
+    res = {"instances": ninst, "cells": cells, "schedule": tuned}
+    b.capture(steps)
+    b.replay()
+    b.sync()
+    for mode in ("graph", "per_instance"):
+        e0, e1 = _events()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        if mode == "graph":
+            b.replay()
+        else:
+            b.step_async(steps, "per_instance")
+        e1.record(stream)
+        b.sync()
+        ms = e0.elapsed_time(e1) / steps
+        res[mode] = {"ms_per_step": ms, "value": cells / (ms / 1e3), "unit": UNIT}
+    res["batched_over_per_instance"] = res["per_instance"]["ms_per_step"] / res["graph"]["ms_per_step"]
+    b.close()
+    return res
+
+
+def measure_adjoint(nsteps: int = 400, snapshots: int = 20):
+    """Differentiated case: 256x512 O-grid (0.5 to 20), M 0.4, Roe + van Albada, ssp34,
+    nsteps from uniform freestream; drag averaged over the steps; gradient with
+    respect to every cell's initial state and the far-field state; binomial
+    checkpointing with `snapshots` stored states; FP64."""
+    from hyperboliconvergence_gb300.solver import Mesh, Solver
+    nr, nth, mach = 256, 512, 0.4
+    mesh = Mesh.cylinder(nr, nth, 0.5, 20.0, 1.01)
+    qinf = np.array([mach, 0.0, 1.0, 1.0 / 1.4])
+    ref = [None, np.broadcast_to(qinf[:, None], (4, nth)).copy(), None, None]
+    s = Solver(mesh, ["wall", "fixed", "periodic", "periodic"], ref, flux="roe", limiter="vanalbada", rk="ssp34",
+               precision="fp64", dt="global", cfl=0.5, species=(1.4, 287.058, mach))
+    s.set_state(np.broadcast_to(qinf[:, None, None], (4, nr, nth)).copy())
+    scale = 1.0 / (0.5 * mach * mach * 2 * 0.5)
+    J, g, refb, rates, st = s.gradient(nsteps, snapshots=snapshots, kind="drag", scale=scale)
+    fwd_ms = st.ms_forward
+    adj_ms = st.ms_total - st.ms_forward
+    s.close()
+    return {"workload": f"cylinder O-grid {nr}x{nth}, M{mach}, {nsteps} ssp34 steps, {snapshots} snapshots",
+            "J_time_avg_cd": J, "forward_ms": fwd_ms, "reverse_ms": adj_ms,
+            "adjoint_over_forward": adj_ms / fwd_ms,
+            "forward_steps_total": int(st.forward_steps), "adjoint_steps": int(st.adjoint_steps),
+            "grad_norm_q0": float(np.linalg.norm(g))}
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -267,6 +373,15 @@ def run_gpu(args):
                 "clocks": clk.summary()}
         if world == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline()
+        extras = [] if args.no_extras else [e for e in args.extras.split(",") if e]
+        if world == 1 and extras:
+            s.close()
+            if "fp32" in extras:
+                line["fp32"] = measure_fp32(stream, args.steps)
+            if "batched" in extras:
+                line["batched"] = measure_batched(stream)
+            if "adjoint" in extras:
+                line["adjoint"] = measure_adjoint()
         print(json.dumps(line), flush=True)
     s.close()
     if pg is not None:
@@ -281,6 +396,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the FP32, batched and adjoint measurements reported beside the headline")
+    ap.add_argument("--extras", default="fp32,batched,adjoint",
+                    help="comma-separated subset of fp32,batched,adjoint to measure beside the headline")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -63,6 +63,7 @@ def _declare(lib):
         "hc_step": [p, i, C.POINTER(StepStats)],
         "hc_step_async": [p, i],
         "hc_sync": [p, C.POINTER(StepStats)],
+        "hc_spectral_radius": [v, v, C.c_longlong, v, v],
         "hc_mesh_cylinder_nodes": [i, i, d, d, d, dp],
         "hc_mesh_linspace_nodes": [i, i, d, d, d, d, dp],
     }
@@ -89,6 +90,7 @@ def load(build_if_missing: bool = True):
     lib = C.CDLL(LIB_PATH)
     _declare(lib)
     _declare_batch(lib)
+    _declare_adjoint(lib)
     _lib = lib
     return lib
 
@@ -138,3 +140,25 @@ def _declare_batch(lib):
         f.restype = C.c_int
     lib.hc_batch_kernel_launches.argtypes = [p]
     lib.hc_batch_kernel_launches.restype = C.c_longlong
+
+
+class Objective(C.Structure):
+    _fields_ = [("kind", C.c_int), ("scale", C.c_double), ("dir", C.c_double * 2),
+                ("target", C.POINTER(C.c_double)), ("weight", C.c_double * 4)]
+
+
+class AdjointStats(C.Structure):
+    _fields_ = [("J", C.c_double), ("forward_steps", C.c_longlong), ("adjoint_steps", C.c_longlong),
+                ("kernel_launches", C.c_longlong), ("ms_forward", C.c_double), ("ms_total", C.c_double)]
+
+
+OBJECTIVE = {"drag": 0, "l2": 1}
+
+
+def _declare_adjoint(lib):
+    p, i = C.c_void_p, C.c_int
+    dp = C.POINTER(C.c_double)
+    lib.hc_objective_forward.argtypes = [p, i, C.POINTER(Objective), dp, dp, dp]
+    lib.hc_objective_forward.restype = C.c_int
+    lib.hc_adjoint_gradient.argtypes = [p, i, i, C.POINTER(Objective), dp, dp, dp, dp, C.POINTER(AdjointStats)]
+    lib.hc_adjoint_gradient.restype = C.c_int

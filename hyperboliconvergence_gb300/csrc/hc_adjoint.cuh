@@ -120,7 +120,7 @@ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R ny, R A, c
   const R X2 = du0 + dp * rho1 * a1;
   const R w0 = lam0 * X0, w1 = lam1 * X1, w2 = lam2 * X2, w3 = lam3 * du1;
   const R dpp = R(0.5) * ra * aa * (w2 - w1);
-  const R drr = dpp / (aa * aa) - ra * w0 / g.gamma;
+  const R drr = dpp * (a1 * a1) - ra * w0 * g.inv_gamma;
   const R du = R(0.5) * (w1 + w2);
   const R dv = w3;
   const R dk = ua * du + va * dv;

@@ -1,0 +1,379 @@
+// hc_adjoint_kernels.cuh -- discrete adjoint of one residual evaluation and of
+// the RK stage update, with the timestep frozen.
+//
+// Forward structure being reversed (stage kernel, hc_kernels.cuh):
+//   QM_c = sum over c's pair faces h of (q_R(h) - q_L(h)) (x) dx_h
+//   per face: gc = dq*idlr, g_side = QM_side . w_side - dq*s_side,
+//             q_side' = q_side +/- d_side * limit(gc, g_side), F = flux(q_L', q_R')
+//   Res_c = sum of +F (c right of the face) and -F (c left of the face)
+// Reverse, three passes over the mesh:
+//   1. faces: F_bar = Rbar_R - Rbar_L; flux, limiter and reconstruction
+//      reversed; per face the direct adjoints of the two cells (dL, dR) and the
+//      adjoints of their biased gradients (gL, gR) are written out (16 planes);
+//      boundary faces add the ghost side's adjoint to the reference-state
+//      adjoint of their side.
+//   2. cells: QMbar_c = sum over c's faces of g_{c,f} (x) w_{c,f}.
+//   3. cells: qbar_c = sum of direct terms + sum over pair faces h of c of
+//      sgn_c(h) (QMbar_c + QMbar_nbr(h)) . dx_h.
+#pragma once
+
+#include "hc_adjoint.cuh"
+#include "hc_kernels.cuh"
+
+namespace hc {
+
+enum { ADJ_FIELDS = 16 };  // dL[4], dR[4], gL[4], gR[4]
+
+template <class R> struct AdjArgs {
+  int ni, nj;
+  int bc[4];
+  Gas<R> gas;
+  int limiter;
+  const R* q;        // stage state (primitive, 4 planes)
+  const R* qm;       // its qmetric, 8 planes (var-major: 2*v+dim)
+  const R* rbar;     // residual adjoint, 4 planes
+  const R* fi;       // face records
+  const R* fj;
+  const R* gref[4];  // ghost reference planes per side
+  R* refbar[4];      // adjoint of the ghost reference planes per side (accumulated)
+  R* ai;             // face adjoint outputs, ADJ_FIELDS planes of (ni+1)*nj
+  R* aj;             // ADJ_FIELDS planes of ni*(nj+1)
+  R* qmbar;          // 8 planes
+  R* qbar;           // output 4 planes
+  const R* qbar_add; // optional: added to qbar (4 planes) or null
+  int objective;     // 1: only wall faces, F_bar = -(+/-) scale * (dirx, diry, 0, 0)
+  R obj_scale, obj_dirx, obj_diry;
+};
+
+// qmetric of every cell (phase 2 of the stage kernel, without tiling)
+template <class R> __global__ void adj_qm_kernel(const AdjArgs<R> a, R* qm) {
+  const int ni = a.ni, nj = a.nj;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ni * nj) return;
+  const int gi = c / nj, gj = c % nj;
+  const size_t n = size_t(ni) * nj;
+  const bool per_i = a.bc[0] == BC_PERIODIC, per_j = a.bc[2] == BC_PERIODIC;
+  const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
+  R m[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) m[k] = R(0);
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    const bool idir = f < 2;
+    const int hi = f & 1;
+    int fidx, nb;
+    bool pair;
+    if (idir) {
+      const int fi = gi + hi;
+      pair = (fi > 0 && fi < ni) || per_i;
+      fidx = fi * nj + gj;
+      nb = wrapi(gi + (hi ? 1 : -1), ni) * nj + gj;
+    } else {
+      const int fj = gj + hi;
+      pair = (fj > 0 && fj < nj) || per_j;
+      fidx = gi * (nj + 1) + fj;
+      nb = gi * nj + wrapi(gj + (hi ? 1 : -1), nj);
+    }
+    if (!pair) continue;
+    const R* rec = idir ? a.fi : a.fj;
+    const int nf = idir ? nfi : nfj;
+    const R dx = rec[size_t(F_DXX) * nf + fidx], dy = rec[size_t(F_DXY) * nf + fidx];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const R dq = hi ? (a.q[v * n + nb] - a.q[v * n + c]) : (a.q[v * n + c] - a.q[v * n + nb]);
+      m[2 * v] += dq * dx;
+      m[2 * v + 1] += dq * dy;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) qm[k * n + c] = m[k];
+}
+
+template <class R, int FK>
+__device__ __forceinline__ void flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql, const R* qr, const R* Fb,
+                                         R* qlb, R* qrb) {
+  if constexpr (FK == FLUX_ROE) roe_flux_adj(g, nx, ny, A, ql, qr, Fb, qlb, qrb);
+  else rusanov_flux_adj(g, nx, ny, A, ql, qr, Fb, qlb, qrb);
+}
+
+// pass 1: one thread per face of direction dir (0 = i-faces, 1 = j-faces)
+template <class R, int FK> __global__ void adj_face_kernel(const AdjArgs<R> a, int dir) {
+  const int ni = a.ni, nj = a.nj;
+  const size_t n = size_t(ni) * nj;
+  const bool idir = dir == 0;
+  const int nf = idir ? (ni + 1) * nj : ni * (nj + 1);
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  int i, j;
+  if (idir) { i = f / nj; j = f % nj; } else { i = f / (nj + 1); j = f % (nj + 1); }
+  const R* rec = idir ? a.fi : a.fj;
+  R* out = idir ? a.ai : a.aj;
+  auto rd = [&](int fld) -> R { return rec[size_t(fld) * nf + f]; };
+  const R nx = rd(F_NX), ny = rd(F_NY), A = rd(F_A);
+  const int lo = idir ? i : j, nalong = idir ? ni : nj;
+  const int side = idir ? (lo == 0 ? 0 : 1) : (lo == 0 ? 2 : 3);
+  const bool bnd = (lo == 0 || lo == nalong) && a.bc[side] != BC_PERIODIC;
+  R res[ADJ_FIELDS];
+#pragma unroll
+  for (int k = 0; k < ADJ_FIELDS; ++k) res[k] = R(0);
+  R* dL = res; R* dR = res + 4; R* gL = res + 8; R* gR = res + 12;
+  const Gas<R> g = a.gas;
+  const int lim = a.limiter;
+  if (!bnd) {
+    if (!a.objective) {
+      // left/right cells (periodic wrap on the boundary lines)
+      int cl, cr;
+      if (idir) { cl = wrapi(i - 1, ni) * nj + j; cr = wrapi(i, ni) * nj + j; }
+      else { cl = i * nj + wrapi(j - 1, nj); cr = i * nj + wrapi(j, nj); }
+      R Fb[4], ql[4], qr[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        Fb[v] = a.rbar[v * n + cr] - a.rbar[v * n + cl];
+        ql[v] = a.q[v * n + cl];
+        qr[v] = a.q[v * n + cr];
+      }
+      if (lim == LIM_NOLIMIT1) {
+        flux_adj<R, FK>(g, nx, ny, A, ql, qr, Fb, dL, dR);
+      } else {
+        const R dl = rd(F_DL), dr = rd(F_DR), idlr = rd(F_IDLR);
+        const R wlx = rd(F_WLX), wly = rd(F_WLY), sl = rd(F_SL);
+        const R wrx = rd(F_WRX), wry = rd(F_WRY), sr = rd(F_SR);
+        R qL[4], qR[4], gc[4], gl[4], gr[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const R dq = qr[v] - ql[v];
+          gc[v] = dq * idlr;
+          gl[v] = (a.qm[(2 * v) * n + cl] * wlx + a.qm[(2 * v + 1) * n + cl] * wly) - dq * sl;
+          gr[v] = (a.qm[(2 * v) * n + cr] * wrx + a.qm[(2 * v + 1) * n + cr] * wry) - dq * sr;
+          qL[v] = ql[v] + dl * limit<R>(lim, gc[v], gl[v]);
+          qR[v] = qr[v] - dr * limit<R>(lim, gc[v], gr[v]);
+        }
+        R qLb[4] = {R(0), R(0), R(0), R(0)}, qRb[4] = {R(0), R(0), R(0), R(0)};
+        flux_adj<R, FK>(g, nx, ny, A, qL, qR, Fb, qLb, qRb);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          R da, db;
+          limit_grad<R>(lim, gc[v], gl[v], &da, &db);
+          const R zlb = dl * qLb[v];
+          R gcb = zlb * da;
+          const R glb = zlb * db;
+          limit_grad<R>(lim, gc[v], gr[v], &da, &db);
+          const R zrb = -dr * qRb[v];
+          gcb += zrb * da;
+          const R grb = zrb * db;
+          const R dqb = gcb * idlr - glb * sl - grb * sr;
+          dL[v] = qLb[v] - dqb;
+          dR[v] = qRb[v] + dqb;
+          gL[v] = glb;
+          gR[v] = grb;
+        }
+      }
+    }
+  } else {
+    const bool int_right = lo == 0;
+    const int ci = idir ? (int_right ? 0 : ni - 1) * nj + j : i * nj + (int_right ? 0 : nj - 1);
+    const int kf = idir ? j : i;
+    const int nfs = idir ? nj : ni;
+    const int bct = a.bc[side];
+    R qi[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) qi[v] = a.q[v * n + ci];
+    R* dI = int_right ? dR : dL;
+    R* gI = int_right ? gR : gL;
+    if (bct == BC_WALL) {
+      R Fb[4];
+      if (a.objective) {
+        const R sgn_in = int_right ? R(1) : R(-1);
+        Fb[0] = -sgn_in * a.obj_scale * a.obj_dirx;
+        Fb[1] = -sgn_in * a.obj_scale * a.obj_diry;
+      } else {
+#pragma unroll
+        for (int v = 0; v < 2; ++v) Fb[v] = int_right ? a.rbar[v * n + ci] : -a.rbar[v * n + ci];
+      }
+      const R wx = int_right ? rd(F_WLX) : rd(F_WRX), wy = int_right ? rd(F_WLY) : rd(F_WRY);
+      (void)wx; (void)wy;
+      const R pb = A * (nx * Fb[0] + ny * Fb[1]);
+      dI[3] += pb;
+      gI[3] = -pb;  // pass 2 pairs it with the wall extrapolation weights
+    } else if (!a.objective) {
+      R Fb[4], qg[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        Fb[v] = int_right ? a.rbar[v * n + ci] : -a.rbar[v * n + ci];
+        qg[v] = a.gref[side][size_t(v) * nfs + kf];  // fixed ghost = reference state
+      }
+      R qLb[4] = {R(0), R(0), R(0), R(0)}, qRb[4] = {R(0), R(0), R(0), R(0)};
+      R gb_ref[4] = {R(0), R(0), R(0), R(0)};
+      if (lim == LIM_NOLIMIT1) {
+        if (int_right) { flux_adj<R, FK>(g, nx, ny, A, qg, qi, Fb, qLb, qRb); }
+        else { flux_adj<R, FK>(g, nx, ny, A, qi, qg, Fb, qLb, qRb); }
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          dI[v] += int_right ? qRb[v] : qLb[v];
+          gb_ref[v] = int_right ? qLb[v] : qRb[v];
+        }
+      } else {
+        const R d = rd(F_DL), idlr = rd(F_IDLR);
+        const R wx = int_right ? rd(F_WRX) : rd(F_WLX), wy = int_right ? rd(F_WRY) : rd(F_WLY);
+        R qL[4], qR[4], gc[4], gbv[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const R dq = int_right ? (qi[v] - qg[v]) : (qg[v] - qi[v]);
+          gc[v] = dq * idlr;
+          gbv[v] = a.qm[(2 * v) * n + ci] * wx + a.qm[(2 * v + 1) * n + ci] * wy;
+          const R s = limit<R>(lim, gc[v], gbv[v]);
+          if (int_right) { qL[v] = qg[v]; qR[v] = qi[v] - d * s; }
+          else { qL[v] = qi[v] + d * s; qR[v] = qg[v]; }
+        }
+        flux_adj<R, FK>(g, nx, ny, A, qL, qR, Fb, qLb, qRb);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          R da, db;
+          limit_grad<R>(lim, gc[v], gbv[v], &da, &db);
+          const R zb = int_right ? -d * qRb[v] : d * qLb[v];
+          const R gcb = zb * da;
+          gI[v] = zb * db;
+          const R dqb = gcb * idlr;
+          if (int_right) { dI[v] += qRb[v] + dqb; gb_ref[v] = qLb[v] - dqb; }
+          else { dI[v] += qLb[v] - dqb; gb_ref[v] = qRb[v] + dqb; }
+        }
+      }
+      if (bct == BC_FIXED) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) a.refbar[side][size_t(v) * nfs + kf] += gb_ref[v];
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < ADJ_FIELDS; ++k) out[size_t(k) * nf + f] = res[k];
+}
+
+// pass 2: qmetric adjoint per cell
+template <class R> __global__ void adj_qmbar_kernel(const AdjArgs<R> a) {
+  const int ni = a.ni, nj = a.nj;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ni * nj) return;
+  const int gi = c / nj, gj = c % nj;
+  const size_t n = size_t(ni) * nj;
+  const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
+  R m[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) m[k] = R(0);
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    const bool idir = f < 2;
+    const int hi = f & 1;  // hi: c is the left cell of this face
+    const int lo = idir ? gi + hi : gj + hi;
+    const int nalong = idir ? ni : nj;
+    const int side = idir ? (lo == 0 ? 0 : 1) : (lo == 0 ? 2 : 3);
+    const bool bnd = (lo == 0 || lo == nalong) && a.bc[side] != BC_PERIODIC;
+    const int fidx = idir ? lo * nj + gj : gi * (nj + 1) + lo;
+    const int nf = idir ? nfi : nfj;
+    const R* rec = idir ? a.fi : a.fj;
+    const R* adj = idir ? a.ai : a.aj;
+    const bool wall = bnd && a.bc[side] == BC_WALL;
+    // c is left (hi) -> gL with wL, right -> gR with wR; wall faces keep the
+    // extrapolation weights in the other side's slots
+    const bool use_left_slot = wall ? !hi : hi;
+    const R wx = rec[size_t(use_left_slot ? F_WLX : F_WRX) * nf + fidx];
+    const R wy = rec[size_t(use_left_slot ? F_WLY : F_WRY) * nf + fidx];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const R gv = adj[size_t(hi ? 8 + v : 12 + v) * nf + fidx];
+      m[2 * v] += gv * wx;
+      m[2 * v + 1] += gv * wy;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a.qmbar[k * n + c] = m[k];
+}
+
+// pass 3: gather the state adjoint per cell
+template <class R> __global__ void adj_gather_kernel(const AdjArgs<R> a) {
+  const int ni = a.ni, nj = a.nj;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ni * nj) return;
+  const int gi = c / nj, gj = c % nj;
+  const size_t n = size_t(ni) * nj;
+  const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
+  const bool per_i = a.bc[0] == BC_PERIODIC, per_j = a.bc[2] == BC_PERIODIC;
+  R qb[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) qb[v] = a.qbar_add ? a.qbar_add[v * n + c] : R(0);
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    const bool idir = f < 2;
+    const int hi = f & 1;
+    const int lo = idir ? gi + hi : gj + hi;
+    const int fidx = idir ? lo * nj + gj : gi * (nj + 1) + lo;
+    const int nf = idir ? nfi : nfj;
+    const R* adj = idir ? a.ai : a.aj;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) qb[v] += adj[size_t(hi ? v : 4 + v) * nf + fidx];
+    const bool pair = idir ? ((lo > 0 && lo < ni) || per_i) : ((lo > 0 && lo < nj) || per_j);
+    if (!pair) continue;
+    const R* rec = idir ? a.fi : a.fj;
+    const R dx = rec[size_t(F_DXX) * nf + fidx], dy = rec[size_t(F_DXY) * nf + fidx];
+    const int nb = idir ? wrapi(gi + (hi ? 1 : -1), ni) * nj + gj : gi * nj + wrapi(gj + (hi ? 1 : -1), nj);
+    const R sg = hi ? R(-1) : R(1);  // c left of the face -> -1
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+      qb[v] += sg * ((a.qmbar[(2 * v) * n + c] + a.qmbar[(2 * v) * n + nb]) * dx +
+                     (a.qmbar[(2 * v + 1) * n + c] + a.qmbar[(2 * v + 1) * n + nb]) * dy);
+  }
+#pragma unroll
+  for (int v = 0; v < 4; ++v) a.qbar[v * n + c] = qb[v];
+}
+
+// Reverse of one stage update q_out = prim(cons(q0) + (sum_k alpha_k R_k) * fac),
+// fac = beta*dt/V frozen: qbar_out -> q0bar (accumulated) and rbar_k (accumulated).
+template <class R>
+__global__ void adj_update_kernel(int ncell, Gas<R> g, const R* __restrict__ q_out, const R* __restrict__ q0,
+                                  const R* __restrict__ vol, const R* __restrict__ qbar_out, R* __restrict__ q0bar,
+                                  R* rbar0, R* rbar1, R* rbar2, R* rbar3, R alpha0, R alpha1, R alpha2, R alpha3,
+                                  int stage, R dts) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const size_t n = size_t(ncell);
+  R q[4], qz[4], pb[4], cb[4], z[4] = {R(0), R(0), R(0), R(0)};
+#pragma unroll
+  for (int v = 0; v < 4; ++v) { q[v] = q_out[v * n + c]; qz[v] = q0[v * n + c]; pb[v] = qbar_out[v * n + c]; }
+  cons2prim_adj(g, q, pb, cb);
+  prim2cons_adj(g, qz, cb, z);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) q0bar[v * n + c] += z[v];
+  const R fac = dts / vol[c];
+  R* rb[4] = {rbar0, rbar1, rbar2, rbar3};
+  const R al[4] = {alpha0, alpha1, alpha2, alpha3};
+  for (int k = 0; k <= stage; ++k)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) rb[k][v * n + c] += al[k] * cb[v] * fac;
+}
+
+// Drag of the wall faces of the state q (force on the body along (dirx, diry)
+// times scale): per face -sgn_in * A * p_wall * (n . dir) * scale, written to
+// out[k] for wall face k of the flattened wall-face list of the side.
+template <class R>
+__global__ void wall_force_kernel(const AdjArgs<R> a, const R* qm, int side, R* out) {
+  const int ni = a.ni, nj = a.nj;
+  const size_t n = size_t(ni) * nj;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nfs = side < 2 ? nj : ni;
+  if (k >= nfs) return;
+  const bool idir = side < 2;
+  const bool int_right = side == 0 || side == 2;
+  const int i = idir ? (int_right ? 0 : ni) : k;
+  const int j = idir ? k : (int_right ? 0 : nj);
+  const int nf = idir ? (ni + 1) * nj : ni * (nj + 1);
+  const int fidx = idir ? i * nj + j : i * (nj + 1) + j;
+  const R* rec = idir ? a.fi : a.fj;
+  const R nx = rec[size_t(F_NX) * nf + fidx], ny = rec[size_t(F_NY) * nf + fidx], A = rec[size_t(F_A) * nf + fidx];
+  const R wx = rec[size_t(int_right ? F_WLX : F_WRX) * nf + fidx];
+  const R wy = rec[size_t(int_right ? F_WLY : F_WRY) * nf + fidx];
+  const int ci = idir ? (int_right ? 0 : ni - 1) * nj + j : i * nj + (int_right ? 0 : nj - 1);
+  const R pw = a.q[3 * n + ci] - (qm[6 * n + ci] * wx + qm[7 * n + ci] * wy);
+  const R sgn_in = int_right ? R(1) : R(-1);
+  out[k] = -sgn_in * A * pw * (nx * a.obj_dirx + ny * a.obj_diry) * a.obj_scale;
+}
+
+}  // namespace hc

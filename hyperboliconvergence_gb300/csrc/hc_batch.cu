@@ -120,11 +120,7 @@ template <class R> BatchArgs<R> batch_args(hc_batch* b) {
   a.inst = b->inst_d;
   a.order = b->order_d;
   a.nwork = b->nwork;
-  a.gas.gamma = R(b->gamma);
-  a.gas.gm1 = R(b->gamma - 1.);
-  a.gas.gamma1 = R(1. / (b->gamma - 1.));
-  a.gas.Rgas = R(b->Rgas);
-  a.gas.minf = R(b->minf);
+  a.gas = make_gas<R>(b->gamma, b->Rgas, b->minf);
   a.limiter = b->cfg.limiter;
   a.q0 = (const R*)b->q[0];
   a.fi = (const R*)b->fi; a.fj = (const R*)b->fj; a.vol = (const R*)b->vol;
@@ -194,8 +190,7 @@ template <class R> int per_instance_step(hc_batch* b) {
       base.bc[s] = b->bc[4 * k + s];
       base.gref[s] = (const R*)b->gref + b->gref_off[4 * k + s];
     }
-    base.gas.gamma = R(b->gamma); base.gas.gm1 = R(b->gamma - 1.); base.gas.gamma1 = R(1. / (b->gamma - 1.));
-    base.gas.Rgas = R(b->Rgas); base.gas.minf = R(b->minf);
+    base.gas = make_gas<R>(b->gamma, b->Rgas, b->minf);
     base.limiter = b->cfg.limiter;
     base.fi = (const R*)b->fi + (long long)FREC * b->fi_off[k];
     base.fj = (const R*)b->fj + (long long)FREC * b->fj_off[k];

@@ -1,0 +1,61 @@
+// hc_ctx.h -- the context of the C ABI (one mesh, its state and buffers),
+// shared by the translation units of the single-mesh path.
+#pragma once
+
+#include "hc_host.h"
+
+#include <vector>
+
+struct hc_ctx {
+  hc_config cfg{};
+  bool fp32 = false;
+  size_t rsz = 8;
+  int ni = 0, nj = 0;
+  int bc[4] = {-1, -1, -1, -1};
+  bool have_mesh = false, have_bcs = false, have_state = false, geom_dirty = true;
+  double gamma = 1.4, Rgas = 287.058, minf = 1e-4;
+  cudaStream_t own = nullptr, stream = nullptr;
+  int tile = hc::TILE_8x32;
+  // device buffers
+  double* nodes = nullptr;
+  double* cx = nullptr;
+  double* cy = nullptr;
+  double* xm = nullptr;
+  double* fi64 = nullptr;
+  double* fj64 = nullptr;
+  double* vol64 = nullptr;
+  void* fi = nullptr;   // face records in R (aliases fi64 for FP64)
+  void* fj = nullptr;
+  void* vol = nullptr;
+  void* q[3] = {nullptr, nullptr, nullptr};
+  void* res[4] = {nullptr, nullptr, nullptr, nullptr};
+  void* gref[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* staging = nullptr;  // FP64 staging for FP32 transfers (4 planes)
+  hc::StepInfo* info = nullptr;
+  std::vector<double> href[4];
+  long long launches = 0;
+
+  size_t ncell() const { return size_t(ni) * nj; }
+  int nface(int side) const { return side < 2 ? nj : ni; }
+};
+
+namespace hc {
+
+// geometry built and state present (builds the geometry on first use)
+int ctx_ensure_ready(hc_ctx* c);
+
+template <class R> StageArgs<R> base_args(hc_ctx* c) {
+  StageArgs<R> a{};
+  a.ni = c->ni; a.nj = c->nj;
+  for (int k = 0; k < 4; ++k) a.bc[k] = c->bc[k];
+  a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf);
+  a.limiter = c->cfg.limiter;
+  a.fi = (const R*)c->fi; a.fj = (const R*)c->fj; a.vol = (const R*)c->vol;
+  for (int k = 0; k < 4; ++k) a.gref[k] = (const R*)c->gref[k];
+  a.q0 = (const R*)c->q[0];
+  a.info = c->info;
+  a.cfl = R(c->cfg.cfl);
+  return a;
+}
+
+}  // namespace hc

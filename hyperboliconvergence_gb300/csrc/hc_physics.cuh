@@ -32,12 +32,24 @@ template <> struct Lim<float> {
 
 // Species<Euler> subset used on the path (conservationLaws/euler/euler.h:48-60)
 template <class R> struct Gas {
-  R gamma;   // ratio of specific heats
-  R gm1;     // gamma - 1
-  R gamma1;  // 1/(gamma-1)
-  R Rgas;    // gas constant
-  R minf;    // cut-off Mach number (AUSM+up)
+  R gamma;      // ratio of specific heats
+  R gm1;        // gamma - 1
+  R gamma1;     // 1/(gamma-1)
+  R Rgas;       // gas constant
+  R minf;       // cut-off Mach number (AUSM+up)
+  R inv_gamma;  // 1/gamma
 };
+
+template <class R> __host__ __device__ inline Gas<R> make_gas(double gamma, double Rgas, double minf) {
+  Gas<R> g;
+  g.gamma = R(gamma);
+  g.gm1 = R(gamma - 1.);
+  g.gamma1 = R(1. / (gamma - 1.));
+  g.Rgas = R(Rgas);
+  g.minf = R(minf);
+  g.inv_gamma = R(1. / gamma);
+  return g;
+}
 
 // State<Euler,2> without the unused temperature (conservationLaws/euler/euler.h:62-83)
 template <class R> struct St { R p, r, h, u2, a2, u, v; };
@@ -171,7 +183,7 @@ template <class R> __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g,
   const R w3 = lam[3] * du1;
   // characteristic -> primitive -> conserved
   const R dpp = R(0.5) * ra * aa * (w2 - w1);
-  const R drr = dpp / (aa * aa) - ra * w0 / g.gamma;
+  const R drr = dpp * (a1 * a1) - ra * w0 * g.inv_gamma;
   const R du = R(0.5) * (w1 + w2);
   const R dv = w3;
   const R e0 = ra * du + ua * drr;

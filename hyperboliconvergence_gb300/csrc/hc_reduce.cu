@@ -1,0 +1,84 @@
+// hc_reduce.cu -- context-free spectral radius: max over cells of lambda/V
+// (spectralRadius, spatial/spectralRadius.h:19-48), the quantity the global
+// timestep divides the CFL number by.  Two passes: every block reduces a fixed
+// chunk of cells to one partial maximum, then one block reduces the partials.
+#include "hc_host.h"
+
+#include <cfloat>
+
+namespace hc {
+
+constexpr int SR_THREADS = 256;
+constexpr int SR_PER_THREAD = 8;
+constexpr long long SR_CHUNK = (long long)SR_THREADS * SR_PER_THREAD;  // cells per block
+
+__device__ __forceinline__ double block_max(double m) {
+  __shared__ double red[SR_THREADS / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double x = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (m < x) ? x : m;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = (threadIdx.x < SR_THREADS / 32) ? red[threadIdx.x] : DBL_MIN;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double x = __shfl_xor_sync(0xffffffffu, m, o);
+      m = (m < x) ? x : m;
+    }
+  }
+  return m;
+}
+
+// partial[b] = max(DBL_MIN, max over the block's chunk of lambda/V); the fold
+// starts at numeric_limits<double>::min() as the reference does.
+__global__ void __launch_bounds__(SR_THREADS)
+spectral_radius_partial(const double* __restrict__ lam, const double* __restrict__ vol, long long n,
+                        double* __restrict__ partial) {
+  double m = DBL_MIN;
+  const long long base = blockIdx.x * SR_CHUNK;
+#pragma unroll
+  for (int k = 0; k < SR_PER_THREAD; ++k) {
+    const long long c = base + (long long)k * SR_THREADS + threadIdx.x;
+    if (c < n) {
+      const double r = lam[c] / vol[c];
+      m = (m < r) ? r : m;
+    }
+  }
+  m = block_max(m);
+  if (threadIdx.x == 0) partial[blockIdx.x] = m;
+}
+
+__global__ void __launch_bounds__(SR_THREADS)
+spectral_radius_final(const double* __restrict__ partial, int nb, double* __restrict__ out) {
+  double m = DBL_MIN;
+  for (int b = threadIdx.x; b < nb; b += SR_THREADS) m = (m < partial[b]) ? partial[b] : m;
+  m = block_max(m);
+  if (threadIdx.x == 0) out[0] = m;
+}
+
+}  // namespace hc
+
+using namespace hc;
+
+extern "C" {
+
+int hc_spectral_radius(const double* lambda_sum, const double* vol, long long ncell, double* out, void* stream) {
+  if (!lambda_sum || !vol || !out) return fail(HC_ERR_ARG, "null pointer");
+  if (ncell < 1) return fail(HC_ERR_ARG, "ncell must be positive");
+  const long long nb = (ncell + SR_CHUNK - 1) / SR_CHUNK;
+  if (nb > (1LL << 30)) return fail(HC_ERR_ARG, "ncell too large");
+  const cudaStream_t s = (cudaStream_t)stream;
+  double* partial = nullptr;
+  HC_CUDA(cudaMallocAsync((void**)&partial, size_t(nb) * sizeof(double), s));
+  spectral_radius_partial<<<unsigned(nb), SR_THREADS, 0, s>>>(lambda_sum, vol, ncell, partial);
+  spectral_radius_final<<<1, SR_THREADS, 0, s>>>(partial, int(nb), out);
+  const cudaError_t e = cudaGetLastError();
+  cudaFreeAsync(partial, s);
+  HC_CUDA(e);
+  return HC_OK;
+}
+
+}  // extern "C"

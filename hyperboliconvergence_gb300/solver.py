@@ -78,6 +78,12 @@ class Solver:
             self.set_stream(stream)
         check(self.lib.hc_mesh_upload(self.h, mesh.ni, mesh.nj, _dptr(mesh.nodes)))
         check(self.lib.hc_set_species(self.h, *[float(s) for s in species]))
+        self.bc = list(bc)
+        self.set_bcs(bc, ref)
+
+    def set_bcs(self, bc, ref=None) -> None:
+        """Boundary types per side and their reference (ghost) states, 4 planes per side."""
+        mesh = self.mesh
         bct = (C.c_int * 4)(*[BC[b] if isinstance(b, str) else int(b) for b in bc])
         self._refs = []
         ptrs = (C.POINTER(C.c_double) * 4)()
@@ -91,6 +97,53 @@ class Solver:
                 self._refs.append(arr)
                 ptrs[s] = _dptr(arr)
         check(self.lib.hc_set_bcs(self.h, bct, ptrs))
+        self.bc = list(bc)
+
+    # -- discrete adjoint -----------------------------------------------------
+    def _objective(self, kind, scale=1.0, direction=(1.0, 0.0), target=None, weight=(1.0, 1.0, 1.0, 1.0)):
+        from ._capi import OBJECTIVE, Objective
+        o = Objective()
+        o.kind = OBJECTIVE[kind]
+        o.scale = float(scale)
+        o.dir[0], o.dir[1] = float(direction[0]), float(direction[1])
+        self._target = None
+        if target is not None:
+            self._target = np.ascontiguousarray(target, dtype=np.float64)
+            o.target = _dptr(self._target)
+        for k in range(4):
+            o.weight[k] = float(weight[k])
+        return o
+
+    def objective(self, nsteps, kind="drag", rates=None, **kw):
+        """J over nsteps from the current state; returns (J, per-step max rates)."""
+        o = self._objective(kind, **kw)
+        J = C.c_double()
+        rout = np.empty(int(nsteps))
+        rin = None if rates is None else np.ascontiguousarray(rates, dtype=np.float64)
+        check(self.lib.hc_objective_forward(self.h, int(nsteps), C.byref(o),
+                                            _dptr(rin) if rin is not None else None, _dptr(rout), C.byref(J)))
+        return J.value, rout
+
+    def gradient(self, nsteps, snapshots=20, kind="drag", rates=None, **kw):
+        """J and its gradient with respect to the current state and the fixed-ghost
+        reference states; returns (J, q0_bar, [ref_bar per side], rates, stats)."""
+        from ._capi import AdjointStats
+        o = self._objective(kind, **kw)
+        m = self.mesh
+        q0b = np.empty((4, m.ni, m.nj))
+        rb = np.empty(sum(4 * m.nface(s) for s in range(4)))
+        rout = np.empty(int(nsteps))
+        st = AdjointStats()
+        rin = None if rates is None else np.ascontiguousarray(rates, dtype=np.float64)
+        check(self.lib.hc_adjoint_gradient(self.h, int(nsteps), int(snapshots), C.byref(o),
+                                           _dptr(rin) if rin is not None else None, _dptr(q0b), _dptr(rb),
+                                           _dptr(rout), C.byref(st)))
+        refb, off = [], 0
+        for s in range(4):
+            nf = m.nface(s)
+            refb.append(rb[off:off + 4 * nf].reshape(4, nf).copy())
+            off += 4 * nf
+        return st.J, q0b, refb, rout, st
 
     def close(self):
         if getattr(self, "h", None):

@@ -125,11 +125,58 @@ int hc_step(hc_ctx* ctx, int nsteps, hc_step_stats* stats);
 int hc_step_async(hc_ctx* ctx, int nsteps);
 int hc_sync(hc_ctx* ctx, hc_step_stats* stats);
 
+/* spectralRadius (spatial/spectralRadius.h:19-48): out_device[0] = max over the
+ * ncell cells of lambda_sum[c] / vol[c], the fold starting at the smallest
+ * positive double.  All three pointers are device memory; the call is
+ * asynchronous on `stream` (a cudaStream_t, NULL = legacy default stream) and
+ * takes its reduction scratch from the stream-ordered allocator. */
+int hc_spectral_radius(const double* lambda_sum_device, const double* vol_device, long long ncell,
+                       double* out_device, void* stream);
+
+
 /* Mesh generators: make_cylinder_mesh (mesh/generate/twoD.h:223-263), radial
  * spacing stretched geometrically when stretch != 1; make_linspace_mesh
  * (mesh/generate/twoD.h:99-124). */
 int hc_mesh_cylinder_nodes(int nr, int nth, double rc, double rb, double stretch, double* nodes_xy);
 int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, double hiy, double* nodes_xy);
+
+/* ---------------------------------------------------------------------------
+ * Discrete adjoint.  No counterpart in the reference.  The objective J is
+ * evaluated on nsteps RK steps from the context's current state (which is left
+ * unchanged); its gradient with respect to that initial state and to the
+ * fixed-ghost reference states comes from the hand-written reverse of the
+ * residual and of the RK update, with the timestep of every step frozen at the
+ * value of the forward run ("rates": the per-step max lambda/V, returned so a
+ * finite-difference check can replay them).  Binomial checkpointing keeps
+ * `snapshots` states.  FP64 contexts; Roe or Rusanov; NoLimit1/2/3, van Albada,
+ * MinMod, van Leer; periodic, fixed and wall boundaries; global timestep.
+ * ------------------------------------------------------------------------- */
+typedef enum { HC_OBJ_DRAG = 0, HC_OBJ_L2 = 1 } hc_objective_kind;
+
+typedef struct {
+  int kind;              /* hc_objective_kind */
+  double scale;          /* drag: J = scale/N * sum_{n=1..N} wall force of q_n along dir */
+  double dir[2];         /* drag: force direction */
+  const double* target;  /* L2: J = sum_cells sum_v weight[v] (q_N - target)^2, target 4 planes (host) */
+  double weight[4];
+} hc_objective;
+
+typedef struct {
+  double J;
+  long long forward_steps;   /* RK steps run forward, checkpointing recomputation included */
+  long long adjoint_steps;
+  long long kernel_launches;
+  double ms_forward;         /* first forward sweep */
+  double ms_total;           /* forward sweep + reverse sweep */
+} hc_adjoint_stats;
+
+/* J only; rates_in NULL = compute the timesteps (rates_out receives them, nsteps values). */
+int hc_objective_forward(hc_ctx* ctx, int nsteps, const hc_objective* obj, const double* rates_in,
+                         double* rates_out, double* J);
+/* J and its gradient: q0_bar (4 planes of the primitive state) and ref_bar (per side 0..3,
+ * 4 planes of nface values, concatenated; zero where the side is not fixed). */
+int hc_adjoint_gradient(hc_ctx* ctx, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
+                        double* q0_bar, double* ref_bar, double* rates_out, hc_adjoint_stats* stats);
 
 /* ---------------------------------------------------------------------------
  * Batched path: many independent meshes of uneven sizes in one set of buffers.

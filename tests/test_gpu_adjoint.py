@@ -1,0 +1,147 @@
+"""Discrete adjoint: gradients against central finite differences (h = 1e-6,
+relative agreement 1e-6), checkpointed versus fully stored reversal, and the
+torch.autograd.Function for dJ/dMach, dJ/dalpha and dJ/dq0."""
+import math
+
+import numpy as np
+import pytest
+
+from hyperboliconvergence_gb300 import cases
+from hyperboliconvergence_gb300.solver import Mesh, Solver
+
+pytestmark = pytest.mark.gpu
+
+H = 1e-6
+GAMMA = 1.4
+
+
+def cylinder_case(nr=10, nth=32, mach=0.4, seed=0):
+    mesh = Mesh.cylinder(nr, nth, 0.5, 4.0, 1.05)
+    qinf = np.array([mach, 0.0, 1.0, 1.0 / GAMMA])
+    rng = np.random.default_rng(seed)
+    c = mesh.centres()
+    # smooth non-uniform start so the limiter is differentiable everywhere
+    bump = np.exp(-((c[0] - 1.0) ** 2 + c[1] ** 2))
+    q = qinf[:, None, None] * (1 + 0.03 * bump[None] * (1 + 0.1 * rng.standard_normal((4, nr, nth))))
+    ref = [None, np.broadcast_to(qinf[:, None], (4, nth)).copy(), None, None]
+    return mesh, ["wall", "fixed", "periodic", "periodic"], ref, q
+
+
+def make(case, flux="roe", limiter="vanalbada", rk="ssp34"):
+    mesh, bc, ref, q = case
+    s = Solver(mesh, bc, ref, flux=flux, limiter=limiter, rk=rk, precision="fp64", dt="global", cfl=0.5,
+               species=(GAMMA, 287.058, 0.4))
+    s.set_state(q)
+    return s
+
+
+def fd_check(s, q0, nsteps, kind, kw, seed=1):
+    J, g, refb, rates, st = s.gradient(nsteps, snapshots=3, kind=kind, **kw)
+    rng = np.random.default_rng(seed)
+    d = rng.standard_normal(q0.shape) * np.abs(q0).max(axis=(1, 2), keepdims=True) * 1e-2
+    s.set_state(q0 + H * d)
+    jp, _ = s.objective(nsteps, kind=kind, rates=rates, **kw)
+    s.set_state(q0 - H * d)
+    jm, _ = s.objective(nsteps, kind=kind, rates=rates, **kw)
+    s.set_state(q0)
+    fd = (jp - jm) / (2 * H)
+    ad = float(np.sum(g * d))
+    return J, fd, ad, st
+
+
+@pytest.mark.parametrize("flux,limiter,rk", [("roe", "vanalbada", "ssp34"), ("roe", "vanleer", "ssp22"),
+                                             ("rusanov", "minmod", "ssp33"), ("roe", "nolimit1", "ssp11")])
+def test_drag_gradient_matches_central_fd(flux, limiter, rk):
+    case = cylinder_case()
+    s = make(case, flux, limiter, rk)
+    J, fd, ad, st = fd_check(s, case[3], 12, "drag", {"scale": 1.0 / (0.5 * 0.4 ** 2 * 1.0)})
+    assert np.isfinite(J) and abs(ad) > 0
+    assert abs(fd - ad) <= 1e-6 * abs(fd), (fd, ad)
+    assert st.adjoint_steps == 12
+
+
+def test_l2_gradient_on_periodic_vortex():
+    mesh, bc, ref, q, sp = cases.isentropic_vortex(20)
+    s = Solver(mesh, bc, ref, flux="rusanov", limiter="vanalbada", rk="ssp34", dt="global", species=sp)
+    s.set_state(q)
+    target = q * 0.98
+    J, fd, ad, _ = fd_check(s, q, 8, "l2", {"target": target, "weight": (1.0, 1.0, 2.0, 1.0)})
+    assert abs(fd - ad) <= 1e-6 * abs(fd), (fd, ad)
+
+
+def test_checkpointed_equals_stored_reversal():
+    case = cylinder_case(seed=4)
+    s = make(case)
+    kw = {"scale": 1.0}
+    a = s.gradient(16, snapshots=2, kind="drag", **kw)
+    b = s.gradient(16, snapshots=16, kind="drag", **kw)
+    assert a[0] == b[0]
+    assert np.array_equal(a[1], b[1])
+    assert a[4].forward_steps > b[4].forward_steps
+
+
+def test_reference_state_gradient_matches_fd():
+    case = cylinder_case(seed=2)
+    s = make(case)
+    mesh, bc, ref, q = case
+    kw = {"scale": 1.0}
+    J, g, refb, rates, _ = s.gradient(10, snapshots=3, kind="drag", **kw)
+    d = np.zeros_like(ref[1])
+    d[0] = 0.01  # far-field u
+    d[3] = 0.002  # far-field p
+    s.set_bcs(bc, [None, ref[1] + H * d, None, None]); s.set_state(q)
+    jp, _ = s.objective(10, kind="drag", rates=rates, **kw)
+    s.set_bcs(bc, [None, ref[1] - H * d, None, None]); s.set_state(q)
+    jm, _ = s.objective(10, kind="drag", rates=rates, **kw)
+    fd = (jp - jm) / (2 * H)
+    ad = float(np.sum(refb[1] * d))
+    assert abs(fd - ad) <= 1e-6 * abs(fd), (fd, ad)
+
+
+def test_autograd_mach_alpha():
+    torch = pytest.importorskip("torch")
+    from hyperboliconvergence_gb300.autograd import freestream, run_objective
+    nr, nth, n = 10, 32, 10
+    mesh = Mesh.cylinder(nr, nth, 0.5, 4.0, 1.05)
+    s = Solver(mesh, ["wall", "fixed", "periodic", "periodic"],
+               [None, np.zeros((4, nth)), None, None], flux="roe", limiter="vanalbada", dt="global",
+               species=(GAMMA, 287.058, 0.4))
+
+    def J_of(m, a, rates=None):
+        qinf = freestream(m, a)
+        q0 = qinf[:, None, None].expand(4, nr, nth).contiguous()
+        ref1 = qinf[:, None].expand(4, nth).contiguous()
+        cd = run_objective(s, q0, [None, ref1, None, None], n, snapshots=4, kind="drag",
+                           scale=1.0, direction=(1.0, 0.0))
+        return cd / (0.5 * m * m * 1.0)
+
+    m = torch.tensor(0.4, dtype=torch.float64, requires_grad=True)
+    a = torch.tensor(0.05, dtype=torch.float64, requires_grad=True)
+    J = J_of(m, a)
+    J.backward()
+    # finite differences at frozen timesteps: replay the forward run's rates
+    qinf = freestream(m.detach(), a.detach()).numpy()
+    s.set_bcs(s.bc, [None, np.broadcast_to(qinf[:, None], (4, nth)).copy(), None, None])
+    s.set_state(np.broadcast_to(qinf[:, None, None], (4, nr, nth)).copy())
+    _, rates = s.objective(n, kind="drag", scale=1.0)
+
+    def J_np(mv, av):
+        q = np.array([mv * math.cos(av), mv * math.sin(av), 1.0, 1.0 / GAMMA])
+        s.set_bcs(s.bc, [None, np.broadcast_to(q[:, None], (4, nth)).copy(), None, None])
+        s.set_state(np.broadcast_to(q[:, None, None], (4, nr, nth)).copy())
+        j, _ = s.objective(n, kind="drag", rates=rates, scale=1.0)
+        return j / (0.5 * mv * mv)
+
+    fdm = (J_np(0.4 + H, 0.05) - J_np(0.4 - H, 0.05)) / (2 * H)
+    fda = (J_np(0.4, 0.05 + H) - J_np(0.4, 0.05 - H)) / (2 * H)
+    assert abs(m.grad.item() - fdm) <= 1e-6 * abs(fdm), (m.grad.item(), fdm)
+    assert abs(a.grad.item() - fda) <= 1e-6 * max(abs(fda), 1e-12), (a.grad.item(), fda)
+
+
+def test_unsupported_configuration_is_reported():
+    from hyperboliconvergence_gb300 import HCError
+    case = cylinder_case()
+    s = make(case, flux="slau")
+    with pytest.raises(HCError) as e:
+        s.gradient(2, snapshots=1, kind="drag", scale=1.0)
+    assert e.value.code == 5
