@@ -64,6 +64,7 @@ def _declare(lib):
         "hc_step_async": [p, i],
         "hc_sync": [p, C.POINTER(StepStats)],
         "hc_spectral_radius": [v, v, C.c_longlong, v, v],
+        "hc_spectral_radius_noalloc": [v, v, C.c_longlong, v, v],
         "hc_mesh_cylinder_nodes": [i, i, d, d, d, dp],
         "hc_mesh_linspace_nodes": [i, i, d, d, d, d, dp],
     }

@@ -59,11 +59,61 @@ spectral_radius_final(const double* __restrict__ partial, int nb, double* __rest
   if (threadIdx.x == 0) out[0] = m;
 }
 
+// Scratch of hc_spectral_radius_noalloc: one partial maximum per block of
+// SR_CHUNK cells, at most SR_NOALLOC_BLOCKS blocks (32 KiB).  It is static
+// device memory, so every GPU that loads this library holds it until the
+// process exits.  Each call writes every entry it later reads, so nothing has
+// to be cleared between calls; calls that overlap on the GPU share the array
+// and race.
+constexpr int SR_NOALLOC_BLOCKS = 4096;
+constexpr long long SR_NOALLOC_MAX_CELLS = SR_NOALLOC_BLOCKS * SR_CHUNK;  // 8,388,608
+static __device__ __align__(256) double g_sr_noalloc_scratch[SR_NOALLOC_BLOCKS];
+
 }  // namespace hc
+
+#include <mutex>
+#include <vector>
+
+namespace {
+std::mutex g_sr_scratch_mutex;
+std::vector<double*> g_sr_scratch_ptr;  // device address of the scratch array, per device
+}  // namespace
 
 using namespace hc;
 
 extern "C" {
+
+// The array's name is only a host-side stand-in for host code; its device
+// address is looked up once per device (with that device current) on the
+// first call made on the device, so that first call should come before any
+// stream capture.
+int hc_spectral_radius_noalloc(const double* lambda_sum, const double* vol, long long ncell, double* out,
+                               void* stream) {
+  if (!lambda_sum || !vol || !out) return fail(HC_ERR_ARG, "null pointer");
+  if (ncell < 1) return fail(HC_ERR_ARG, "ncell must be positive");
+  if (ncell > SR_NOALLOC_MAX_CELLS)
+    return fail(HC_ERR_ARG, "ncell " + std::to_string(ncell) + " exceeds the no-allocation maximum of " +
+                                std::to_string(SR_NOALLOC_MAX_CELLS) + " cells");
+  int dev = 0;
+  HC_CUDA(cudaGetDevice(&dev));
+  double* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_sr_scratch_mutex);
+    if (g_sr_scratch_ptr.size() <= size_t(dev)) g_sr_scratch_ptr.resize(size_t(dev) + 1, nullptr);
+    if (!g_sr_scratch_ptr[dev]) {
+      void* p = nullptr;
+      HC_CUDA(cudaGetSymbolAddress(&p, g_sr_noalloc_scratch));
+      g_sr_scratch_ptr[dev] = static_cast<double*>(p);
+    }
+    scratch = g_sr_scratch_ptr[dev];
+  }
+  const long long nb = (ncell + SR_CHUNK - 1) / SR_CHUNK;
+  const cudaStream_t s = (cudaStream_t)stream;
+  spectral_radius_partial<<<unsigned(nb), SR_THREADS, 0, s>>>(lambda_sum, vol, ncell, scratch);
+  spectral_radius_final<<<1, SR_THREADS, 0, s>>>(scratch, int(nb), out);
+  HC_CUDA(cudaGetLastError());
+  return HC_OK;
+}
 
 int hc_spectral_radius(const double* lambda_sum, const double* vol, long long ncell, double* out, void* stream) {
   if (!lambda_sum || !vol || !out) return fail(HC_ERR_ARG, "null pointer");

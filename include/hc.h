@@ -133,6 +133,18 @@ int hc_sync(hc_ctx* ctx, hc_step_stats* stats);
 int hc_spectral_radius(const double* lambda_sum_device, const double* vol_device, long long ncell,
                        double* out_device, void* stream);
 
+/* hc_spectral_radius for callers that cannot allocate device memory -- code that
+ * runs while a framework owns the whole device memory pool, a fixed-budget or
+ * real-time loop that must not call cudaMalloc/cudaFree, or a stream being
+ * captured where allocation is not allowed.  No counterpart in the reference.
+ * It allocates nothing: its 32 KiB of reduction scratch is a static device array
+ * that every GPU loading this library keeps until the process exits, which caps
+ * ncell at 8,388,608 (larger sizes return HC_ERR_ARG).  The first call on a
+ * device looks the array's device address up, so make that first call before
+ * any stream capture.  All calls share the array: calls that overlap on the GPU
+ * (other streams, other threads) race. */
+int hc_spectral_radius_noalloc(const double* lambda_sum_device, const double* vol_device, long long ncell,
+                               double* out_device, void* stream);
 
 /* Mesh generators: make_cylinder_mesh (mesh/generate/twoD.h:223-263), radial
  * spacing stretched geometrically when stretch != 1; make_linspace_mesh
