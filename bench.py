@@ -376,12 +376,14 @@ def run_gpu(args):
         extras = [] if args.no_extras else [e for e in args.extras.split(",") if e]
         if world == 1 and extras:
             s.close()
-            if "fp32" in extras:
-                line["fp32"] = measure_fp32(stream, args.steps)
-            if "batched" in extras:
-                line["batched"] = measure_batched(stream)
-            if "adjoint" in extras:
-                line["adjoint"] = measure_adjoint()
+            for name, fn in (("fp32", lambda: measure_fp32(stream, args.steps)),
+                             ("batched", lambda: measure_batched(stream)),
+                             ("adjoint", measure_adjoint)):
+                if name in extras:
+                    try:
+                        line[name] = fn()
+                    except Exception as exc:  # reported, not fatal: the headline stands alone
+                        line[name] = {"error": f"{type(exc).__name__}: {exc}"}
         print(json.dumps(line), flush=True)
     s.close()
     if pg is not None:

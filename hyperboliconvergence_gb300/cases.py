@@ -60,13 +60,33 @@ def cylinder(nr: int = 512, nth: int = 1024, mach: float = 0.3, rc: float = 0.5,
     return mesh, ["wall", far, "periodic", "periodic"], ref, q, species
 
 
+def _opens_vacuum(quad, gamma=GAMMA, margin=0.5):
+    """True when a quadrant interface separates faster than `margin` times the
+    vacuum-formation speed 2(a_L + a_R)/(gamma - 1) of its 1D Riemann problem."""
+    a = np.sqrt(gamma * quad[:, 3] / quad[:, 2])
+    lim = lambda l, r: margin * 2.0 * (a[l] + a[r]) / (gamma - 1.0)  # noqa: E731
+    # quadrant k = 2*(x >= 0.5) + (y >= 0.5)
+    for lo, hi, comp in ((0, 2, 0), (1, 3, 0), (0, 1, 1), (2, 3, 1)):
+        if quad[hi, comp] - quad[lo, comp] >= lim(lo, hi):
+            return True
+    return False
+
+
 def quadrant_riemann(ni: int, nj: int, rng: np.random.Generator):
-    """Four-quadrant Riemann problem on [0,1]^2 split at (0.5, 0.5), fixed ghost states."""
+    """Four-quadrant Riemann problem on [0,1]^2 split at (0.5, 0.5), fixed ghost states.
+
+    Quadrant states: rho in [0.5, 2], p in [0.1, 2], |u|, |v| <= 1 (uniform draws);
+    draws whose interfaces would separate faster than half the vacuum-formation
+    speed are redrawn, since no finite-volume scheme keeps p > 0 there.
+    """
     mesh = Mesh.linspace(ni, nj, 0.0, 1.0, 0.0, 1.0)
     quad = np.empty((4, 4))  # quadrant x (u, v, rho, p)
-    quad[:, 2] = rng.uniform(0.5, 2.0, 4)
-    quad[:, 3] = rng.uniform(0.1, 2.0, 4)
-    quad[:, 0:2] = rng.uniform(-1.0, 1.0, (4, 2))
+    while True:
+        quad[:, 2] = rng.uniform(0.5, 2.0, 4)
+        quad[:, 3] = rng.uniform(0.1, 2.0, 4)
+        quad[:, 0:2] = rng.uniform(-1.0, 1.0, (4, 2))
+        if not _opens_vacuum(quad):
+            break
     c = mesh.centres()
     qi = (c[0] >= 0.5).astype(int)
     qj = (c[1] >= 0.5).astype(int)

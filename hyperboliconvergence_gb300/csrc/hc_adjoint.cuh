@@ -272,9 +272,11 @@ template <class R> __device__ __forceinline__ void limit_grad(int kind, R a, R b
     case LIM_NOLIMIT3: *da = R(0.33333333333333333) * R(2); *db = R(0.33333333333333333); return;
     case LIM_VANALBADA: {
       if (a * b < R(0)) return;
+      // z = num/den; dz = (dnum - z*dden)/den (no den^2: it underflows at a = b = 0)
       const R num = b * (a * a) + a * (b * b), den = a * a + b * b + tiny;
-      *da = ((R(2) * a * b + b * b) * den - num * R(2) * a) / (den * den);
-      *db = ((a * a + R(2) * a * b) * den - num * R(2) * b) / (den * den);
+      const R z = num / den;
+      *da = ((R(2) * a * b + b * b) - z * R(2) * a) / den;
+      *db = ((a * a + R(2) * a * b) - z * R(2) * b) / den;
       return;
     }
     case LIM_MINMOD:
@@ -283,8 +285,9 @@ template <class R> __device__ __forceinline__ void limit_grad(int kind, R a, R b
       return;
     case LIM_VANLEER: {
       const R num = a * fabs(b) + fabs(a) * b, den = fabs(a) + fabs(b) + tiny;
-      *da = ((fabs(b) + sgn(a) * b) * den - num * sgn(a)) / (den * den);
-      *db = ((a * sgn(b) + fabs(a)) * den - num * sgn(b)) / (den * den);
+      const R z = num / den;
+      *da = ((fabs(b) + sgn(a) * b) - z * sgn(a)) / den;
+      *db = ((a * sgn(b) + fabs(a)) - z * sgn(b)) / den;
       return;
     }
     default: return;  // other limiters are not differentiated
