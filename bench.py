@@ -153,20 +153,23 @@ def _events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
-def measure_fp32(stream, steps: int):
-    """The same workload in FP32: throughput, HBM roofline and error against FP64."""
+def measure_precision(stream, steps: int, prec: str):
+    """The same workload at another precision ("fp32": everything FP32; "fp64_df":
+    FP64 storage with double-float stage arithmetic): throughput, HBM roofline
+    and the relative L-inf difference of the conserved variables from FP64 after
+    one step and after 20 steps from the same start."""
     import torch
     from hyperboliconvergence_gb300 import cases
     from hyperboliconvergence_gb300.solver import Solver
     mesh, bc, ref, q, species = cases.cylinder(NR, NTH, mach=MACH)
     out = {}
     states = {}
-    for prec in ("fp32", "fp64"):
-        s = Solver(mesh, bc, ref, flux=FLUX, limiter=LIMITER, rk=RKT, precision=prec, dt=DTMODE, cfl=CFL,
+    for p in (prec, "fp64"):
+        s = Solver(mesh, bc, ref, flux=FLUX, limiter=LIMITER, rk=RKT, precision=p, dt=DTMODE, cfl=CFL,
                    species=species, stream=stream.cuda_stream)
         s.set_state(q)
         s.step(3)
-        if prec == "fp32":
+        if p == prec:
             e0, e1 = _events()
             torch.cuda.synchronize()
             e0.record(stream)
@@ -176,24 +179,29 @@ def measure_fp32(stream, steps: int):
             ms = e0.elapsed_time(e1) / steps
             cells = NR * NTH
             stage_ms = ms / NSTAGES
-            ach = (3 * 4 + 2) * 4 * cells / (stage_ms / 1e3) / 1e9
+            esz = 4 if prec == "fp32" else 8
+            ach = (3 * 4 + 2) * esz * cells / (stage_ms / 1e3) / 1e9
             peak, _ = measured_peaks()
             out = {"value": cells / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
                    "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                                "frac": ach / peak, "alg_bytes_per_cell_stage": 56}}
-            s.set_state(q)
-        s.step(20)
-        states[prec] = s.get_state()
+                                "frac": ach / peak, "alg_bytes_per_cell_stage": 14 * esz}}
+        s.set_state(q)
+        s.step(1)
+        one = s.get_state()
+        s.step(19)
+        states[p] = (one, s.get_state())
         s.close()
-    a, b = states["fp32"], states["fp64"]
     g = 1.4
 
     def cons(w):
         u, v, r, p = w
         return np.stack([r * u, r * v, r, p / (g - 1) + 0.5 * r * (u * u + v * v)])
-    ca, cb = cons(a), cons(b)
-    err = (np.abs(ca - cb).reshape(4, -1).max(1) / np.abs(cb).reshape(4, -1).max(1)).max()
-    out["error_vs_fp64_after_20_steps"] = float(err)
+
+    def rel(a, b):
+        ca, cb = cons(a), cons(b)
+        return float((np.abs(ca - cb).reshape(4, -1).max(1) / np.abs(cb).reshape(4, -1).max(1)).max())
+    out["error_vs_fp64_after_1_step"] = rel(states[prec][0], states["fp64"][0])
+    out["error_vs_fp64_after_20_steps"] = rel(states[prec][1], states["fp64"][1])
     return out
 
 
@@ -376,7 +384,8 @@ def run_gpu(args):
         extras = [] if args.no_extras else [e for e in args.extras.split(",") if e]
         if world == 1 and extras:
             s.close()
-            for name, fn in (("fp32", lambda: measure_fp32(stream, args.steps)),
+            for name, fn in (("fp32", lambda: measure_precision(stream, args.steps, "fp32")),
+                             ("fp64_df", lambda: measure_precision(stream, args.steps, "fp64_df")),
                              ("batched", lambda: measure_batched(stream)),
                              ("adjoint", measure_adjoint)):
                 if name in extras:
@@ -399,9 +408,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the FP32, batched and adjoint measurements reported beside the headline")
-    ap.add_argument("--extras", default="fp32,batched,adjoint",
-                    help="comma-separated subset of fp32,batched,adjoint to measure beside the headline")
+                    help="skip the FP32, double-float, batched and adjoint measurements beside the headline")
+    ap.add_argument("--extras", default="fp32,fp64_df,batched,adjoint",
+                    help="comma-separated subset of fp32,fp64_df,batched,adjoint to measure beside the headline")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

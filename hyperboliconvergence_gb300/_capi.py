@@ -20,7 +20,7 @@ FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central
 LIMITER = {"nolimit1": 0, "nolimit2": 1, "nolimit3": 2, "vanalbada": 3, "minmod": 4,
            "superbee": 5, "mc": 6, "vanleer": 7, "vanleer_ref": 8, "cada3": 9}
 RK = {"ssp11": 0, "ssp22": 1, "ssp33": 2, "ssp34": 3}
-PRECISION = {"fp64": 0, "fp32": 1}
+PRECISION = {"fp64": 0, "fp32": 1, "fp64_df": 2}
 DTMODE = {"global": 0, "local": 1}
 BC = {"periodic": 0, "fixed": 1, "riemann": 2, "entropy": 3, "wall": 4}
 

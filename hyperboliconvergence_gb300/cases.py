@@ -60,7 +60,7 @@ def cylinder(nr: int = 512, nth: int = 1024, mach: float = 0.3, rc: float = 0.5,
     return mesh, ["wall", far, "periodic", "periodic"], ref, q, species
 
 
-def _opens_vacuum(quad, gamma=GAMMA, margin=0.5):
+def _opens_vacuum(quad, gamma=GAMMA, margin=0.2):
     """True when a quadrant interface separates faster than `margin` times the
     vacuum-formation speed 2(a_L + a_R)/(gamma - 1) of its 1D Riemann problem."""
     a = np.sqrt(gamma * quad[:, 3] / quad[:, 2])
@@ -76,8 +76,12 @@ def quadrant_riemann(ni: int, nj: int, rng: np.random.Generator):
     """Four-quadrant Riemann problem on [0,1]^2 split at (0.5, 0.5), fixed ghost states.
 
     Quadrant states: rho in [0.5, 2], p in [0.1, 2], |u|, |v| <= 1 (uniform draws);
-    draws whose interfaces would separate faster than half the vacuum-formation
-    speed are redrawn, since no finite-volume scheme keeps p > 0 there.
+    draws whose interfaces separate faster than a fifth of the 1D vacuum-formation
+    speed are redrawn: where the four rarefactions meet at the centre the 2D
+    expansion is stronger than any 1D one, and at half that speed MUSCL schemes
+    (the CPU oracle in FP64 included) drive the pressure negative within a few
+    steps.  With this bound the 256-instance batch of seed 2026 stays physical
+    for 15 SLAU/van Albada ssp34 steps at CFL 0.5 in the oracle.
     """
     mesh = Mesh.linspace(ni, nj, 0.0, 1.0, 0.0, 1.0)
     quad = np.empty((4, 4))  # quadrant x (u, v, rho, p)

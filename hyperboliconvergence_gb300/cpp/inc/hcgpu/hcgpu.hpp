@@ -107,6 +107,9 @@ inline constexpr gpu_policy gpu{HC_DT_GLOBAL, HC_FP64};
 inline constexpr gpu_policy gpu_local_dt{HC_DT_LOCAL, HC_FP64};
 inline constexpr gpu_policy gpu_fp32{HC_DT_GLOBAL, HC_FP32};
 inline constexpr gpu_policy gpu_fp32_local_dt{HC_DT_LOCAL, HC_FP32};
+// FP64 state and update, stage arithmetic in double-float
+inline constexpr gpu_policy gpu_df{HC_DT_GLOBAL, HC_FP64_DF};
+inline constexpr gpu_policy gpu_df_local_dt{HC_DT_LOCAL, HC_FP64_DF};
 }  // namespace execution
 
 // Mesh<2,Real> nodes (mesh/mesh.h:283-321)

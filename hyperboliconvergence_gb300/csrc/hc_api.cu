@@ -53,8 +53,10 @@ void free_buffers(hc_ctx* c) {
     if (c->fj) cudaFree(c->fj);
     if (c->vol) cudaFree(c->vol);
   }
+  if (c->fic) cudaFree(c->fic);
+  if (c->fjc) cudaFree(c->fjc);
   c->nodes = c->cx = c->cy = c->xm = c->fi64 = c->fj64 = c->vol64 = c->staging = nullptr;
-  c->fi = c->fj = c->vol = nullptr;
+  c->fi = c->fj = c->vol = c->fic = c->fjc = nullptr;
   for (int k = 0; k < 3; ++k) c->q[k] = nullptr;
   for (int k = 0; k < 4; ++k) c->res[k] = c->gref[k] = nullptr;
   c->info = nullptr;
@@ -79,6 +81,11 @@ int build_geometry(hc_ctx* c) {
     convert_kernel<float><<<1024, 256, 0, c->stream>>>(c->fj64, (float*)c->fj, size_t(FREC) * nfj);
     convert_kernel<float><<<1024, 256, 0, c->stream>>>(c->vol64, (float*)c->vol, n);
     c->launches += 3;
+  }
+  if (c->df) {
+    convert_kernel<df64><<<1024, 256, 0, c->stream>>>(c->fi64, (df64*)c->fic, size_t(FREC) * nfi);
+    convert_kernel<df64><<<1024, 256, 0, c->stream>>>(c->fj64, (df64*)c->fjc, size_t(FREC) * nfj);
+    c->launches += 2;
   }
   HC_CUDA(cudaGetLastError());
   // ghost reference planes in the context precision
@@ -208,12 +215,14 @@ int hc_context_create(const hc_config* cfg, hc_ctx** out) {
   if (cfg->flux < 0 || cfg->flux >= FLUX_COUNT) return fail(HC_ERR_ARG, "unknown flux");
   if (cfg->limiter < 0 || cfg->limiter >= LIM_COUNT) return fail(HC_ERR_ARG, "unknown limiter");
   if (cfg->rk < HC_RK_SSP11 || cfg->rk > HC_RK_SSP34) return fail(HC_ERR_ARG, "unknown RK table");
-  if (cfg->precision != HC_FP64 && cfg->precision != HC_FP32) return fail(HC_ERR_ARG, "unknown precision");
+  if (cfg->precision != HC_FP64 && cfg->precision != HC_FP32 && cfg->precision != HC_FP64_DF)
+    return fail(HC_ERR_ARG, "unknown precision");
   if (cfg->dt_mode != HC_DT_GLOBAL && cfg->dt_mode != HC_DT_LOCAL) return fail(HC_ERR_ARG, "unknown dt mode");
   if (!(cfg->cfl > 0)) return fail(HC_ERR_ARG, "cfl must be positive");
   hc_ctx* c = new hc_ctx();
   c->cfg = *cfg;
   c->fp32 = cfg->precision == HC_FP32;
+  c->df = cfg->precision == HC_FP64_DF;
   c->rsz = c->fp32 ? sizeof(float) : sizeof(double);
   cudaError_t e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = c->fp32 ? prepare<float>(cfg->flux) : prepare<double>(cfg->flux);
@@ -280,6 +289,10 @@ int hc_mesh_upload(hc_ctx* c, int ni, int nj, const double* nodes_xy) {
     HC_CUDA(cudaMalloc(&c->staging, 5 * n * sizeof(double)));
   } else {
     c->fi = c->fi64; c->fj = c->fj64; c->vol = c->vol64;
+  }
+  if (c->df) {
+    HC_CUDA(cudaMalloc(&c->fic, FREC * nfi * sizeof(df64)));
+    HC_CUDA(cudaMalloc(&c->fjc, FREC * nfj * sizeof(df64)));
   }
   for (int k = 0; k < 3; ++k) HC_CUDA(cudaMalloc(&c->q[k], 4 * n * c->rsz));
   for (int k = 0; k < 4; ++k) HC_CUDA(cudaMalloc(&c->res[k], 5 * n * c->rsz));

@@ -26,6 +26,9 @@ struct hc_ctx {
   double* vol64 = nullptr;
   void* fi = nullptr;   // face records in R (aliases fi64 for FP64)
   void* fj = nullptr;
+  bool df = false;      // HC_FP64_DF: stages compute in double-float
+  void* fic = nullptr;  // face records as double-float (HC_FP64_DF)
+  void* fjc = nullptr;
   void* vol = nullptr;
   void* q[3] = {nullptr, nullptr, nullptr};
   void* res[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -51,6 +54,7 @@ template <class R> StageArgs<R> base_args(hc_ctx* c) {
   a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf);
   a.limiter = c->cfg.limiter;
   a.fi = (const R*)c->fi; a.fj = (const R*)c->fj; a.vol = (const R*)c->vol;
+  a.fic = c->fic; a.fjc = c->fjc;
   for (int k = 0; k < 4; ++k) a.gref[k] = (const R*)c->gref[k];
   a.q0 = (const R*)c->q[0];
   a.info = c->info;

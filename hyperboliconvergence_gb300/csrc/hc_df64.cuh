@@ -11,6 +11,9 @@
 // ACM TOMS 23(4), 1997).  The exponent range is FP32's.
 //
 // Written for __host__ and __device__ so the same code is testable on a CPU.
+// The type and its functions live in hc::dd and are found by argument-dependent
+// lookup, so code in namespace hc keeps calling the global sqrt/fabs/fmax for
+// double and float.
 #pragma once
 
 #include <cfloat>
@@ -18,6 +21,7 @@
 #include <cuda_runtime.h>
 
 namespace hc {
+namespace dd {
 
 struct df64 {
   float hi, lo;
@@ -104,4 +108,6 @@ __host__ __device__ __forceinline__ df64 sqrt(df64 a) {
 }
 __host__ __device__ __forceinline__ bool isfinite(df64 a) { return ::isfinite(a.hi); }
 
+}  // namespace dd
+using dd::df64;
 }  // namespace hc

@@ -18,6 +18,7 @@
 #include "hc_physics.cuh"
 
 #include <cstdint>
+#include <type_traits>
 
 namespace hc {
 
@@ -47,6 +48,8 @@ template <class R> struct StageArgs {
   const R* q0;        // state at the start of the step
   const R* fi;        // i-face records
   const R* fj;        // j-face records
+  const void* fic;    // i-face records in the compute type when it differs from R
+  const void* fjc;    // j-face records in the compute type when it differs from R
   const R* vol;       // cell volumes
   const R* gref[4];   // per side: far-field/fixed primitive values, 4 planes of nface
   R* res_out;         // residual of this stage (5 planes) or null
@@ -111,15 +114,31 @@ template <class R> __device__ __forceinline__ void forward_update(const Gas<R>& 
   qn[0] = s1.u; qn[1] = s1.v; qn[2] = s1.r; qn[3] = s1.p;
 }
 
+// conversions between the storage type R and the compute type C of a stage
+template <class To, class From> __device__ __forceinline__ To cvt(From x) { return To(x); }
+template <> __device__ __forceinline__ double cvt<double, df64>(df64 x) { return x.to_double(); }
+template <class C, class R> __device__ __forceinline__ Gas<C> gas_as(const Gas<R>& g) {
+  Gas<C> o;
+  o.gamma = cvt<C>(g.gamma); o.gm1 = cvt<C>(g.gm1); o.gamma1 = cvt<C>(g.gamma1);
+  o.Rgas = cvt<C>(g.Rgas); o.minf = cvt<C>(g.minf); o.inv_gamma = cvt<C>(g.inv_gamma);
+  return o;
+}
+
 // One tile (TI x TJ cells, tile coordinates (bi, bj)) of one RK stage.  Called
-// by every thread of the block; smem_raw holds StageSmem<TI,TJ,R>::bytes.
-template <int TI, int TJ, class R, int FK>
+// by every thread of the block; smem_raw holds StageSmem<TI,TJ,C>::bytes.
+// R is the storage type (state, residuals, update); C the type the tile's
+// gradients, reconstruction and fluxes are computed in (C = R, or double-float
+// for FP64 storage, reading the face records from a.fic / a.fjc).
+template <int TI, int TJ, class R, int FK, class C = R>
 __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj, unsigned char* smem_raw) {
-  using SM = StageSmem<TI, TJ, R>;
-  R* sq = reinterpret_cast<R*>(smem_raw);
-  R* sm = sq + SM::q_elems;
-  R* sfi = sm + SM::m_elems;
-  R* sfj = sfi + SM::fi_elems;
+  constexpr bool same = std::is_same<C, R>::value;
+  using SM = StageSmem<TI, TJ, C>;
+  C* sq = reinterpret_cast<C*>(smem_raw);
+  C* sm = sq + SM::q_elems;
+  C* sfi = sm + SM::m_elems;
+  C* sfj = sfi + SM::fi_elems;
+  const C* cfi = same ? reinterpret_cast<const C*>(a.fi) : reinterpret_cast<const C*>(a.fic);
+  const C* cfj = same ? reinterpret_cast<const C*>(a.fj) : reinterpret_cast<const C*>(a.fjc);
   constexpr int QI = SM::QI, QJ = SM::QJ, MI = SM::MI, MJ = SM::MJ;
   constexpr int NT = TI * TJ;
   const int ni = a.ni, nj = a.nj;
@@ -138,12 +157,12 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     if (gj < 0 || gj >= nj) { if (per_j) gj = wrapi(gj, nj); else ok = false; }
     const size_t c = size_t(gi) * nj + gj;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) sq[(v * QI + la) * QJ + lb] = ok ? a.q[v * ncell + c] : R(0);
+    for (int v = 0; v < 4; ++v) sq[(v * QI + la) * QJ + lb] = ok ? cvt<C>(a.q[v * ncell + c]) : C(0);
   }
   __syncthreads();
 
-  auto Q = [&](int v, int la, int lb) -> R { return sq[(v * QI + la + 2) * QJ + lb + 2]; };  // tile coords
-  auto M = [&](int k, int la, int lb) -> R& { return sm[(k * MI + la + 1) * MJ + lb + 1]; };
+  auto Q = [&](int v, int la, int lb) -> C { return sq[(v * QI + la + 2) * QJ + lb + 2]; };  // tile coords
+  auto M = [&](int k, int la, int lb) -> C& { return sm[(k * MI + la + 1) * MJ + lb + 1]; };
 
   // ---- phase 2: qmetric of the tile cells and of the 1-cell halo strips
   // (lsq/qmetric.ipp via spatial/lsqMetrics.h:269-301; D2 periodic wrap)
@@ -154,9 +173,9 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     bool ok = !corner;
     if (gi < 0 || gi >= ni) { if (per_i) gi = wrapi(gi, ni); else ok = false; }
     if (gj < 0 || gj >= nj) { if (per_j) gj = wrapi(gj, nj); else ok = false; }
-    R m[8];
+    C m[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) m[q] = R(0);
+    for (int q = 0; q < 8; ++q) m[q] = C(0);
     if (ok) {
       // the cell's four faces: (face index, neighbour offset, is pair face)
 #pragma unroll
@@ -175,14 +194,14 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
           fidx = gi * (nj + 1) + fj;
         }
         if (!pair) continue;
-        const R* rec = idir ? a.fi : a.fj;
+        const C* rec = idir ? cfi : cfj;
         const int nf = idir ? nfi : nfj;
-        const R dx = rec[size_t(F_DXX) * nf + fidx], dy = rec[size_t(F_DXY) * nf + fidx];
+        const C dx = rec[size_t(F_DXX) * nf + fidx], dy = rec[size_t(F_DXY) * nf + fidx];
         const int na = la + (idir ? (hi ? 1 : -1) : 0), nb = lb + (idir ? 0 : (hi ? 1 : -1));
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
           // (q_right - q_left) of the face
-          const R dq = hi ? (Q(v, na, nb) - Q(v, la, lb)) : (Q(v, la, lb) - Q(v, na, nb));
+          const C dq = hi ? (Q(v, na, nb) - Q(v, la, lb)) : (Q(v, la, lb) - Q(v, na, nb));
           m[2 * v] += dq * dx;
           m[2 * v + 1] += dq * dy;
         }
@@ -194,7 +213,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   __syncthreads();
 
   // ---- phase 3: face fluxes (i-faces then j-faces of the tile, each once)
-  const Gas<R> g = a.gas;
+  const Gas<C> g = gas_as<C>(a.gas);
   const int lim = a.limiter;
   constexpr int NFI = (TI + 1) * TJ, NFJ = TI * (TJ + 1);
   for (int k = tid; k < NFI + NFJ; k += NT) {
@@ -203,78 +222,83 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     if (idir) { la = k / TJ; lb = k % TJ; } else { const int kk = k - NFI; la = kk / (TJ + 1); lb = kk % (TJ + 1); }
     const int gi = i0 + la, gj = j0 + lb;
     bool valid = idir ? (gi <= ni && gj < nj) : (gi < ni && gj <= nj);
-    Flux5<R> F;
-    F.f[0] = F.f[1] = F.f[2] = F.f[3] = F.lam = R(0);
+    Flux5<C> F;
+    F.f[0] = F.f[1] = F.f[2] = F.f[3] = F.lam = C(0);
     if (valid) {
-      const R* rec = idir ? a.fi : a.fj;
+      const C* rec = idir ? cfi : cfj;
       const int nf = idir ? nfi : nfj;
       const int fidx = idir ? gi * nj + gj : gi * (nj + 1) + gj;
-      auto rd = [&](int fld) -> R { return rec[size_t(fld) * nf + fidx]; };
-      const R nx = rd(F_NX), ny = rd(F_NY), A = rd(F_A);
+      auto rd = [&](int fld) -> C { return rec[size_t(fld) * nf + fidx]; };
+      const C nx = rd(F_NX), ny = rd(F_NY), A = rd(F_A);
       const int lo = idir ? gi : gj, nalong = idir ? ni : nj;
       const int side = idir ? (lo == 0 ? 0 : 1) : (lo == 0 ? 2 : 3);
       const bool bnd = (lo == 0 || lo == nalong) && a.bc[side] != BC_PERIODIC;
       const int la_l = idir ? la - 1 : la, lb_l = idir ? lb : lb - 1;  // left cell
       if (!bnd) {
-        R ql[4], qr[4];
+        C ql[4], qr[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) { ql[v] = Q(v, la_l, lb_l); qr[v] = Q(v, la, lb); }
         if (lim != LIM_NOLIMIT1) {
-          const R dl = rd(F_DL), dr = rd(F_DR), idlr = rd(F_IDLR);
-          const R wlx = rd(F_WLX), wly = rd(F_WLY), sl = rd(F_SL);
-          const R wrx = rd(F_WRX), wry = rd(F_WRY), sr = rd(F_SR);
-          R qL[4], qR[4];
+          const C dl = rd(F_DL), dr = rd(F_DR), idlr = rd(F_IDLR);
+          const C wlx = rd(F_WLX), wly = rd(F_WLY), sl = rd(F_SL);
+          const C wrx = rd(F_WRX), wry = rd(F_WRY), sr = rd(F_SR);
+          C qL[4], qR[4];
 #pragma unroll
           for (int v = 0; v < 4; ++v) {
-            const R dq = qr[v] - ql[v];
-            const R gc = dq * idlr;
-            const R gl = (M(2 * v, la_l, lb_l) * wlx + M(2 * v + 1, la_l, lb_l) * wly) - dq * sl;
-            const R gr = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
-            qL[v] = ql[v] + dl * limit<R>(lim, gc, gl);
-            qR[v] = qr[v] - dr * limit<R>(lim, gc, gr);
+            const C dq = qr[v] - ql[v];
+            const C gc = dq * idlr;
+            const C gl = (M(2 * v, la_l, lb_l) * wlx + M(2 * v + 1, la_l, lb_l) * wly) - dq * sl;
+            const C gr = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
+            qL[v] = ql[v] + dl * limit<C>(lim, gc, gl);
+            qR[v] = qr[v] - dr * limit<C>(lim, gc, gr);
           }
-          F = face_flux<R, FK>(g, nx, ny, A, prim_state(g, qL[0], qL[1], qL[2], qL[3]),
+          F = face_flux<C, FK>(g, nx, ny, A, prim_state(g, qL[0], qL[1], qL[2], qL[3]),
                                prim_state(g, qR[0], qR[1], qR[2], qR[3]));
         } else {
-          F = face_flux<R, FK>(g, nx, ny, A, prim_state(g, ql[0], ql[1], ql[2], ql[3]),
+          F = face_flux<C, FK>(g, nx, ny, A, prim_state(g, ql[0], ql[1], ql[2], ql[3]),
                                prim_state(g, qr[0], qr[1], qr[2], qr[3]));
         }
       } else {
         // boundary face: interior cell is the right cell on sides 0/2, the left on 1/3
         const bool int_right = lo == 0;
         const int ia = int_right ? la : la_l, ib = int_right ? lb : lb_l;
-        R qi[4];
+        C qi[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) qi[v] = Q(v, ia, ib);
         const int kf = idir ? gj : gi;  // face index along the side
         const int bct = a.bc[side];
         if (bct == BC_WALL) {
-          const R wx = int_right ? rd(F_WLX) : rd(F_WRX), wy = int_right ? rd(F_WLY) : rd(F_WRY);
-          R qw[4];
+          const C wx = int_right ? rd(F_WLX) : rd(F_WRX), wy = int_right ? rd(F_WLY) : rd(F_WRY);
+          C qw[4];
 #pragma unroll
           for (int v = 0; v < 4; ++v) qw[v] = qi[v] - (M(2 * v, ia, ib) * wx + M(2 * v + 1, ia, ib) * wy);
           F = wall_flux(g, nx, ny, A, qw);
         } else {
           const int nfs = idir ? nj : ni;
-          R qref[4], qg[4];
+          C qg[4];
+          // ghost state in the storage type (the far-field updates call pow)
+          R qref[4], qgr[4], qir[4];
 #pragma unroll
-          for (int v = 0; v < 4; ++v) qref[v] = a.gref[side][size_t(v) * nfs + kf];
+          for (int v = 0; v < 4; ++v) { qref[v] = a.gref[side][size_t(v) * nfs + kf]; qir[v] = cvt<R>(qi[v]); }
           const R sgn = int_right ? R(1) : R(-1);  // normal into the domain
-          if (bct == BC_RIEMANN) farfield_update<R, BC_RIEMANN>(g, sgn * nx, sgn * ny, qi, qref, qg);
-          else if (bct == BC_ENTROPY) farfield_update<R, BC_ENTROPY>(g, sgn * nx, sgn * ny, qi, qref, qg);
+          const R nxr = cvt<R>(nx), nyr = cvt<R>(ny);
+          if (bct == BC_RIEMANN) farfield_update<R, BC_RIEMANN>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr);
+          else if (bct == BC_ENTROPY) farfield_update<R, BC_ENTROPY>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr);
           else {
 #pragma unroll
-            for (int v = 0; v < 4; ++v) qg[v] = qref[v];
+            for (int v = 0; v < 4; ++v) qgr[v] = qref[v];
           }
-          R qL[4], qR[4];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) qg[v] = cvt<C>(qgr[v]);
+          C qL[4], qR[4];
           if (lim != LIM_NOLIMIT1) {
-            const R d = rd(F_DL), idlr = rd(F_IDLR);
-            const R wx = int_right ? rd(F_WRX) : rd(F_WLX), wy = int_right ? rd(F_WRY) : rd(F_WLY);
+            const C d = rd(F_DL), idlr = rd(F_IDLR);
+            const C wx = int_right ? rd(F_WRX) : rd(F_WLX), wy = int_right ? rd(F_WRY) : rd(F_WLY);
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
-              const R dq = int_right ? (qi[v] - qg[v]) : (qg[v] - qi[v]);
-              const R gb = M(2 * v, ia, ib) * wx + M(2 * v + 1, ia, ib) * wy;
-              const R s = limit<R>(lim, dq * idlr, gb);
+              const C dq = int_right ? (qi[v] - qg[v]) : (qg[v] - qi[v]);
+              const C gb = M(2 * v, ia, ib) * wx + M(2 * v + 1, ia, ib) * wy;
+              const C s = limit<C>(lim, dq * idlr, gb);
               if (int_right) { qL[v] = qg[v]; qR[v] = qi[v] - d * s; }
               else { qL[v] = qi[v] + d * s; qR[v] = qg[v]; }
             }
@@ -282,12 +306,12 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
 #pragma unroll
             for (int v = 0; v < 4; ++v) { qL[v] = int_right ? qg[v] : qi[v]; qR[v] = int_right ? qi[v] : qg[v]; }
           }
-          F = face_flux<R, FK>(g, nx, ny, A, prim_state(g, qL[0], qL[1], qL[2], qL[3]),
+          F = face_flux<C, FK>(g, nx, ny, A, prim_state(g, qL[0], qL[1], qL[2], qL[3]),
                                prim_state(g, qR[0], qR[1], qR[2], qR[3]));
         }
       }
     }
-    R* dst = idir ? sfi : sfj;
+    C* dst = idir ? sfi : sfj;
     const int slot = idir ? (la * TJ + lb) : (la * (TJ + 1) + lb);
     const int pl = idir ? NFI : NFJ;
 #pragma unroll
@@ -305,8 +329,9 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     const int s0 = la * TJ + lb, s1 = (la + 1) * TJ + lb;
     const int t0 = la * (TJ + 1) + lb, t1 = t0 + 1;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) res[v] = ((sfi[v * NFI + s0] - sfi[v * NFI + s1]) + sfj[v * NFJ + t0]) - sfj[v * NFJ + t1];
-    lam = ((sfi[4 * NFI + s0] + sfi[4 * NFI + s1]) + sfj[4 * NFJ + t0]) + sfj[4 * NFJ + t1];
+    for (int v = 0; v < 4; ++v)
+      res[v] = cvt<R>(((sfi[v * NFI + s0] - sfi[v * NFI + s1]) + sfj[v * NFJ + t0]) - sfj[v * NFJ + t1]);
+    lam = cvt<R>(((sfi[4 * NFI + s0] + sfi[4 * NFI + s1]) + sfj[4 * NFJ + t0]) + sfj[4 * NFJ + t1]);
   }
   const size_t c = size_t(gi) * nj + gj;
   if (own && a.res_out) {
@@ -363,16 +388,16 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   R q0[4], qn[4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) q0[v] = a.q0[v * ncell + c];
-  forward_update(g, q0, tot, fac, qn);
+  forward_update(a.gas, q0, tot, fac, qn);
 #pragma unroll
   for (int v = 0; v < 4; ++v) a.q_out[v * ncell + c] = qn[v];
   flag_nonphysical(a.info, qn, int(c));
 }
 
-template <int TI, int TJ, class R, int FK>
+template <int TI, int TJ, class R, int FK, class C = R>
 __global__ void __launch_bounds__(TI * TJ) stage_kernel(const StageArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_tile<TI, TJ, R, FK>(a, blockIdx.y, blockIdx.x, smem_raw);
+  stage_tile<TI, TJ, R, FK, C>(a, blockIdx.y, blockIdx.x, smem_raw);
 }
 
 // Stage-0 update of one cell with the global timestep dt = cfl / max(lambda/V)

@@ -5,6 +5,8 @@
 
 #include "hc_kernels.cuh"
 
+#include <type_traits>
+
 namespace hc {
 
 // Tile shapes the stage kernel is built for (cells along i x cells along j).
@@ -32,6 +34,12 @@ inline void tile_dims(int tile, int* ti, int* tj) {
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,                    \
                                          int(StageSmem<TI, TJ, R>::bytes));                              \
     if (e != cudaSuccess) return e;                                                                      \
+    if (std::is_same<R, double>::value && TI == 8 && TJ == 32) {                                          \
+      e = cudaFuncSetAttribute(stage_kernel<8, 32, double, FK, df64>,                                    \
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,                              \
+                               int(StageSmem<8, 32, df64>::bytes));                                      \
+      if (e != cudaSuccess) return e;                                                                    \
+    }                                                                                                    \
     return cudaFuncSetAttribute(batch_stage_kernel<TI, TJ, R, FK>,                                       \
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,                             \
                                 int(StageSmem<TI, TJ, R>::bytes));                                       \
@@ -70,6 +78,13 @@ inline void tile_dims(int tile, int* ti, int* tj) {
     return e;                                                                                            \
   }                                                                                                      \
   template <class R> static cudaError_t dispatch(const StageArgs<R>& a, int tile, cudaStream_t s) {     \
+    if (std::is_same<R, double>::value && a.fic) {                                                       \
+      /* double-float compute type, 8x32 tiles */                                                        \
+      const dim3 grid((a.nj + 31) / 32, (a.ni + 7) / 8);                                                 \
+      stage_kernel<8, 32, double, FK, df64><<<grid, 256, StageSmem<8, 32, df64>::bytes, s>>>(           \
+          *reinterpret_cast<const StageArgs<double>*>(&a));                                              \
+      return cudaGetLastError();                                                                         \
+    }                                                                                                    \
     if (tile == TILE_4x32) go<R, 4, 32>(a, s);                                                           \
     else if (tile == TILE_16x16) go<R, 16, 16>(a, s);                                                    \
     else go<R, 8, 32>(a, s);                                                                             \

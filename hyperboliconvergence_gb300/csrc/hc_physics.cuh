@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <cfloat>
 
+#include "hc_df64.cuh"
+
 namespace hc {
 
 enum FluxKind { FLUX_ROE = 0, FLUX_SLAU = 1, FLUX_SLAU_REF = 2, FLUX_AUSMPUP = 3,
@@ -28,6 +30,11 @@ template <> struct Lim<double> {
 template <> struct Lim<float> {
   __host__ __device__ static constexpr float tiny() { return FLT_MIN; }
   __host__ __device__ static constexpr float huge() { return FLT_MAX; }
+};
+// double-float has FP32's exponent range
+template <> struct Lim<df64> {
+  __host__ __device__ static constexpr df64 tiny() { return df64(FLT_MIN, 0.f); }
+  __host__ __device__ static constexpr df64 huge() { return df64(FLT_MAX, 0.f); }
 };
 
 // Species<Euler> subset used on the path (conservationLaws/euler/euler.h:48-60)

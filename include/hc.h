@@ -56,7 +56,11 @@ typedef enum {
 /* Runge-Kutta table (ODE::Explicit, ode.h:107-197) */
 typedef enum { HC_RK_SSP11 = 0, HC_RK_SSP22 = 1, HC_RK_SSP33 = 2, HC_RK_SSP34 = 3 } hc_rk;
 
-typedef enum { HC_FP64 = 0, HC_FP32 = 1 } hc_precision;
+/* HC_FP64_DF: FP64 state, residuals and update (the FP64 interface); gradients,
+ * reconstruction and fluxes in double-float (pairs of FP32, ~2^-47 relative
+ * rounding, FP32 exponent range) on the FP32 pipes.  Single-mesh contexts only;
+ * the stage kernel uses the 8x32 tile whatever the tile setting. */
+typedef enum { HC_FP64 = 0, HC_FP32 = 1, HC_FP64_DF = 2 } hc_precision;
 
 /* global: dt = cfl / max(lambda/V) at stage 0 (timestepping/rungeKutta.h:131-133);
  * local: per-cell cfl/lambda (spatial/eulerForwardUpdate.h:117-168) */

@@ -22,7 +22,7 @@ int main() {
         std::fabs((A - Cc).to_double() - (a - c)) / scale_add,
         std::fabs((A * B).to_double() - a * b) / std::fabs(a * b),
         std::fabs((A / B).to_double() - a / b) / std::fabs(a / b),
-        std::fabs(sqrt(hc::fabs(A)).to_double() - std::sqrt(std::fabs(a))) / std::sqrt(std::fabs(a))};
+        std::fabs(sqrt(fabs(A)).to_double() - std::sqrt(std::fabs(a))) / std::sqrt(std::fabs(a))};
     for (int i = 0; i < 5; ++i) worst[i] = std::fmax(worst[i], r[i]);
   }
   std::printf("add %.3e sub %.3e mul %.3e div %.3e sqrt %.3e\n", worst[0], worst[1], worst[2], worst[3], worst[4]);

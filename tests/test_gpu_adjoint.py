@@ -16,13 +16,19 @@ GAMMA = 1.4
 
 
 def cylinder_case(nr=10, nth=32, mach=0.4, seed=0):
+    """Cylinder at 0.1 rad incidence from a smooth start whose every variable has
+    gradients of order 1e-2 per unit length: limiter arguments then sit away from
+    the kinks (a = 0, b = 0, a*b = 0) that central differences cannot resolve,
+    except on a few zero-crossing curves."""
     mesh = Mesh.cylinder(nr, nth, 0.5, 4.0, 1.05)
-    qinf = np.array([mach, 0.0, 1.0, 1.0 / GAMMA])
+    alpha = 0.1
+    qinf = np.array([mach * math.cos(alpha), mach * math.sin(alpha), 1.0, 1.0 / GAMMA])
     rng = np.random.default_rng(seed)
     c = mesh.centres()
-    # smooth non-uniform start so the limiter is differentiable everywhere
     bump = np.exp(-((c[0] - 1.0) ** 2 + c[1] ** 2))
-    q = qinf[:, None, None] * (1 + 0.03 * bump[None] * (1 + 0.1 * rng.standard_normal((4, nr, nth))))
+    amp = np.array([0.02, 0.02, 0.03, 0.02]) * (1 + 0.2 * rng.random(4))
+    shape = 0.5 * bump + 0.1 * c[0] + 0.07 * c[1]
+    q = qinf[:, None, None] + amp[:, None, None] * shape[None]
     ref = [None, np.broadcast_to(qinf[:, None], (4, nth)).copy(), None, None]
     return mesh, ["wall", "fixed", "periodic", "periodic"], ref, q
 
@@ -51,9 +57,9 @@ def fd_check(s, q0, nsteps, kind, kw, seed=1):
 
 @pytest.mark.parametrize("flux,limiter,rk,tol", [
     ("roe", "nolimit1", "ssp11", 1e-6), ("roe", "nolimit2", "ssp34", 1e-6), ("rusanov", "nolimit3", "ssp33", 1e-6),
-    # limiters with kinks (sign changes, min/max switches): cells whose gradients are
-    # ~1e-9 can switch branch inside the +/-h perturbation, so the bound is looser
-    ("roe", "vanalbada", "ssp34", 1e-3), ("roe", "vanleer", "ssp22", 1e-3), ("rusanov", "minmod", "ssp33", 1e-3)])
+    # limiters with kinks: a face whose argument crosses a kink inside +/-h shifts the
+    # central difference by O(kink jump) whatever h, so the bound is looser
+    ("roe", "vanalbada", "ssp34", 1e-4), ("roe", "vanleer", "ssp22", 1e-4), ("rusanov", "minmod", "ssp33", 1e-4)])
 def test_drag_gradient_matches_central_fd(flux, limiter, rk, tol):
     case = cylinder_case()
     s = make(case, flux, limiter, rk)
@@ -84,18 +90,21 @@ def test_checkpointed_equals_stored_reversal():
 
 
 def test_reference_state_gradient_matches_fd():
+    """Fixed-ghost reference states: an L2 objective over every cell, so the cells
+    next to the far field carry the sensitivity (a wall-drag objective would see
+    the far field only after the signal crossed the mesh)."""
     case = cylinder_case(seed=2)
     s = make(case, limiter="nolimit2")
     mesh, bc, ref, q = case
-    kw = {"scale": 1.0}
-    J, g, refb, rates, _ = s.gradient(10, snapshots=3, kind="drag", **kw)
+    kw = {"target": q * 0.98, "weight": (1.0, 1.0, 1.0, 1.0)}
+    J, g, refb, rates, _ = s.gradient(10, snapshots=3, kind="l2", **kw)
     d = np.zeros_like(ref[1])
     d[0] = 0.01  # far-field u
     d[3] = 0.002  # far-field p
     s.set_bcs(bc, [None, ref[1] + H * d, None, None]); s.set_state(q)
-    jp, _ = s.objective(10, kind="drag", rates=rates, **kw)
+    jp, _ = s.objective(10, kind="l2", rates=rates, **kw)
     s.set_bcs(bc, [None, ref[1] - H * d, None, None]); s.set_state(q)
-    jm, _ = s.objective(10, kind="drag", rates=rates, **kw)
+    jm, _ = s.objective(10, kind="l2", rates=rates, **kw)
     fd = (jp - jm) / (2 * H)
     ad = float(np.sum(refb[1] * d))
     assert abs(fd - ad) <= 1e-6 * abs(fd), (fd, ad)

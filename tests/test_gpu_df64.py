@@ -1,0 +1,66 @@
+"""Parity of the double-float stage path (precision "fp64_df": FP64 state and
+update, gradients/reconstruction/fluxes in pairs of FP32) with the FP64 oracle,
+held to the FP64 bar: relative L-inf error per step on the conserved variables
+<= 1e-12, residuals within 1e-11 of the face-flux scale.
+
+The literal reference van Leer ratio (vanleer_ref) is left out: where its
+denominator vanishes the result depends on the smallest normal number of the
+arithmetic (DBL_MIN in FP64, FLT_MIN here), so the set of non-finite faces is
+not the FP64 one.
+"""
+import numpy as np
+import pytest
+
+from test_gpu_parity import CASES, FLUXES, TOL64, make_pair, prim2cons, rel_linf, residual_scale
+
+pytestmark = pytest.mark.gpu
+
+DF_LIMITERS = ["nolimit1", "nolimit2", "nolimit3", "vanalbada", "minmod", "superbee", "mc", "vanleer", "cada3"]
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("flux", FLUXES)
+def test_df_residual_parity_fluxes(name, flux):
+    gpu, ora = make_pair(CASES[name], flux=flux, limiter="vanalbada", precision="fp64_df")
+    rg, ro = gpu.residual(), ora.residual()
+    scale = np.maximum(residual_scale(ro), 1e-300)
+    err = (np.abs(rg[:4] - ro[:4]).reshape(4, -1).max(axis=1) / scale).max()
+    assert err <= 1e-11, err
+    assert np.abs(rg[4] - ro[4]).max() <= 1e-12 * np.abs(ro[4]).max()
+
+
+@pytest.mark.parametrize("limiter", DF_LIMITERS)
+def test_df_residual_parity_limiters(limiter):
+    gpu, ora = make_pair(CASES["cylinder"], flux="roe", limiter=limiter, precision="fp64_df")
+    rg, ro = gpu.residual(), ora.residual()
+    err = (np.abs(rg[:4] - ro[:4]).reshape(4, -1).max(axis=1) / np.maximum(residual_scale(ro), 1e-300)).max()
+    assert err <= 1e-11, err
+
+
+@pytest.mark.parametrize("name,dt", [("vortex", "global"), ("cylinder", "local"), ("quadrant", "global"),
+                                     ("cylinder", "global")])
+@pytest.mark.parametrize("flux", ["roe", "slau", "ausmpup", "rusanov"])
+def test_df_one_step_parity(name, dt, flux):
+    gpu, ora = make_pair(CASES[name], flux=flux, limiter="vanalbada", rk="ssp34", dt=dt, precision="fp64_df")
+    st = gpu.step(1)
+    dto, _ = ora.step(1)
+    err = rel_linf(prim2cons(gpu.get_state()), prim2cons(ora.get_state()))
+    assert err <= TOL64, err
+    assert st.dt == pytest.approx(dto, rel=1e-12)
+
+
+def test_df_vortex_ten_steps_each_step_parity():
+    gpu, ora = make_pair(CASES["vortex"], flux="roe", limiter="vanleer", precision="fp64_df")
+    for _ in range(10):
+        gpu.set_state(ora.get_state())
+        gpu.step(1)
+        ora.step(1)
+        err = rel_linf(prim2cons(gpu.get_state()), prim2cons(ora.get_state()))
+        assert err <= TOL64, err
+
+
+def test_df_adjoint_is_refused():
+    from hyperboliconvergence_gb300 import HCError
+    gpu, _ = make_pair(CASES["vortex"], flux="roe", limiter="nolimit2", precision="fp64_df")
+    with pytest.raises(HCError):
+        gpu.objective(2, kind="l2")
