@@ -49,6 +49,7 @@ struct Adj {
   int nsteps = 0;
   long long fwd_steps = 0, adj_steps = 0, launches = 0;
   std::vector<void*> allocs;
+  std::vector<cudaEvent_t> adv_events;  // (start, end) pairs around checkpoint recomputation
 
   int alloc(double** p, size_t count) {
     HC_CUDA(cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(double)));
@@ -57,6 +58,16 @@ struct Adj {
   }
   ~Adj() {
     for (void* p : allocs) cudaFree(p);
+    for (cudaEvent_t e : adv_events) cudaEventDestroy(e);
+  }
+  // time of the recorded recomputation segments (call after the stream is idle)
+  double recompute_ms() const {
+    double t = 0;
+    for (size_t k = 0; k + 1 < adv_events.size(); k += 2) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, adv_events[k], adv_events[k + 1]) == cudaSuccess) t += ms;
+    }
+    return t;
   }
   cudaStream_t s() const { return c->stream; }
 };
@@ -251,10 +262,18 @@ int store(Adj& A, int slot) {
   return HC_OK;
 }
 int advance(Adj& A, int from, int to) {
+  if (to <= from) return HC_OK;
+  cudaEvent_t ev[2];
+  HC_CUDA(cudaEventCreate(&ev[0]));
+  A.adv_events.push_back(ev[0]);
+  HC_CUDA(cudaEventCreate(&ev[1]));
+  A.adv_events.push_back(ev[1]);
+  HC_CUDA(cudaEventRecord(ev[0], A.s()));
   for (int k = from; k < to; ++k) {
     if (int st = forward_step(A, k, false)) return st;
     swap_out(A);
   }
+  HC_CUDA(cudaEventRecord(ev[1], A.s()));
   return HC_OK;
 }
 
@@ -438,6 +457,7 @@ int hc_adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective
   if (stats) {
     stats->ms_forward = ms_f;
     stats->ms_total = ms_t;
+    stats->ms_recompute = A.recompute_ms();
   }
   return HC_OK;
 }

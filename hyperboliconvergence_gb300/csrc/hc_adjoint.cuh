@@ -11,12 +11,12 @@
 
 namespace hc {
 
-template <class R> __device__ __forceinline__ R sgn(R x) { return x > R(0) ? R(1) : (x < R(0) ? R(-1) : R(0)); }
+template <class R> __host__ __device__ __forceinline__ R sgn(R x) { return x > R(0) ? R(1) : (x < R(0) ? R(-1) : R(0)); }
 
 // primitive state adjoint: (u2, a2, h) -> (u, v, r, p); p and r also pass through
 template <class R> struct StBar { R u, v, r, p, u2, a2, h; };
 
-template <class R> __device__ __forceinline__ void prim_state_adj(const Gas<R>& g, const R* q, StBar<R>& sb,
+template <class R> __host__ __device__ __forceinline__ void prim_state_adj(const Gas<R>& g, const R* q, StBar<R>& sb,
                                                                   R* qbar) {
   // h = a2*gamma1 + 0.5*u2
   sb.a2 += g.gamma1 * sb.h;
@@ -36,7 +36,7 @@ template <class R> __device__ __forceinline__ void prim_state_adj(const Gas<R>& 
 }
 
 // exact flux adjoint, accumulating into the state adjoint of one side
-template <class R> __device__ __forceinline__ void exact_flux_adj(R nx, R ny, const St<R>& s, const R* fbar,
+template <class R> __host__ __device__ __forceinline__ void exact_flux_adj(R nx, R ny, const St<R>& s, const R* fbar,
                                                                   StBar<R>& sb) {
   const R un = nx * s.u + ny * s.v;
   const R mn = s.r * un;
@@ -52,7 +52,7 @@ template <class R> __device__ __forceinline__ void exact_flux_adj(R nx, R ny, co
 }
 
 // Harten entropy fix of one nonlinear wave (roe.ipp:214-223) reversed
-template <class R> __device__ __forceinline__ void entropy_fix_adj(R la, R ll, R lr, R lbar, R* labar, R* llbar,
+template <class R> __host__ __device__ __forceinline__ void entropy_fix_adj(R la, R ll, R lr, R lbar, R* labar, R* llbar,
                                                                    R* lrbar) {
   const R d1 = la - ll, d2 = lr - la;
   const R mx = fmax(d1, d2);
@@ -76,7 +76,7 @@ template <class R> __device__ __forceinline__ void entropy_fix_adj(R la, R ll, R
 // Reverse of roe_flux (hc_physics.cuh) for the four conserved flux components,
 // with respect to the two primitive face states.
 template <class R>
-__device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql, const R* qr,
+__host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql, const R* qr,
                                              const R* Fbar, R* qlbar, R* qrbar) {
   const St<R> l = prim_state(g, ql[0], ql[1], ql[2], ql[3]);
   const St<R> r = prim_state(g, qr[0], qr[1], qr[2], qr[3]);
@@ -227,7 +227,7 @@ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R ny, R A, c
 
 // Reverse of rusanov_flux (conservationLaws/base/fluxes/rusanovFlux.ipp:99-147)
 template <class R>
-__device__ __forceinline__ void rusanov_flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql, const R* qr,
+__host__ __device__ __forceinline__ void rusanov_flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql, const R* qr,
                                                  const R* Fbar, R* qlbar, R* qrbar) {
   const St<R> l = prim_state(g, ql[0], ql[1], ql[2], ql[3]);
   const St<R> r = prim_state(g, qr[0], qr[1], qr[2], qr[3]);
@@ -263,7 +263,7 @@ __device__ __forceinline__ void rusanov_flux_adj(const Gas<R>& g, R nx, R ny, R 
 }
 
 // derivative of limit(kind, a, b) along the taken branch: *da, *db
-template <class R> __device__ __forceinline__ void limit_grad(int kind, R a, R b, R* da, R* db) {
+template <class R> __host__ __device__ __forceinline__ void limit_grad(int kind, R a, R b, R* da, R* db) {
   const R tiny = Lim<R>::tiny();
   *da = R(0); *db = R(0);
   switch (kind) {
@@ -297,14 +297,14 @@ template <class R> __device__ __forceinline__ void limit_grad(int kind, R a, R b
 // Jacobian transposes of the primitive <-> conserved maps (the RK update
 // cons(q0) + R*f -> prim): prim adjoint at state q -> conserved adjoint, and
 // conserved adjoint at state q0 -> prim adjoint.
-template <class R> __device__ __forceinline__ void cons2prim_adj(const Gas<R>& g, const R* q, const R* pb, R* cb) {
+template <class R> __host__ __device__ __forceinline__ void cons2prim_adj(const Gas<R>& g, const R* q, const R* pb, R* cb) {
   const R u = q[0], v = q[1], r = q[2];
   cb[0] = pb[0] / r - g.gm1 * u * pb[3];
   cb[1] = pb[1] / r - g.gm1 * v * pb[3];
   cb[2] = pb[2] - (u * pb[0] + v * pb[1]) / r + R(0.5) * g.gm1 * (u * u + v * v) * pb[3];
   cb[3] = g.gm1 * pb[3];
 }
-template <class R> __device__ __forceinline__ void prim2cons_adj(const Gas<R>& g, const R* q, const R* cb, R* pb) {
+template <class R> __host__ __device__ __forceinline__ void prim2cons_adj(const Gas<R>& g, const R* q, const R* cb, R* pb) {
   const R u = q[0], v = q[1], r = q[2];
   pb[0] += r * cb[0] + r * u * cb[3];
   pb[1] += r * cb[1] + r * v * cb[3];

@@ -505,16 +505,32 @@ template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const B
   return a;
 }
 
+// resident CTAs per SM the persistent kernel is compiled for: the plain FP32
+// stage kernel's 64 registers a thread (4 CTAs of 256 threads), FP64 2 CTAs
+template <class R, int NT> struct BatchResidency {
+  static constexpr int value = (sizeof(R) == 4 ? 1024 : 512) / NT;
+};
+
 template <int TI, int TJ, class R, int FK>
-__global__ void __launch_bounds__(TI * TJ) batch_stage_kernel(const BatchArgs<R> b) {
+__global__ void __launch_bounds__(TI * TJ, (BatchResidency<R, TI * TJ>::value))
+    batch_stage_kernel(const BatchArgs<R> b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // the work item's arguments live in shared memory, read field by field as the
+  // tile needs them (a register or stack copy per thread costs occupancy)
+  __shared__ StageArgs<R> sa;
+  __shared__ int tile_ij[2];
   for (int w = blockIdx.x; w < b.nwork; w += gridDim.x) {
-    const int packed = b.order[w];
-    const int k = packed >> 16, t = packed & 0xffff;
-    const StageArgs<R> a = instance_args(b, k);
-    const int tj = b.inst[k].tiles_j;
     __syncthreads();  // the previous work item may still read shared memory
-    stage_tile<TI, TJ, R, FK>(a, t / tj, t % tj, smem_raw);
+    if (threadIdx.x == 0) {
+      const int packed = b.order[w];
+      const int k = packed >> 16, t = packed & 0xffff;
+      const int tj = b.inst[k].tiles_j;
+      sa = instance_args(b, k);
+      tile_ij[0] = t / tj;
+      tile_ij[1] = t % tj;
+    }
+    __syncthreads();
+    stage_tile<TI, TJ, R, FK>(sa, tile_ij[0], tile_ij[1], smem_raw);
   }
 }
 

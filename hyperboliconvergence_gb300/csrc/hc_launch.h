@@ -5,6 +5,7 @@
 
 #include "hc_kernels.cuh"
 
+#include <algorithm>
 #include <type_traits>
 
 namespace hc {
@@ -45,7 +46,17 @@ inline void tile_dims(int tile, int* ti, int* tj) {
                                 int(StageSmem<TI, TJ, R>::bytes));                                       \
   }                                                                                                      \
   template <class R, int TI, int TJ> static void gob(const BatchArgs<R>& b, int grid, cudaStream_t s) {  \
-    batch_stage_kernel<TI, TJ, R, FK><<<grid, TI * TJ, StageSmem<TI, TJ, R>::bytes, s>>>(b);             \
+    /* a persistent grid larger than what stays resident would run a second, partial wave */           \
+    static int cap = 0;                                                                                  \
+    if (cap == 0) {                                                                                      \
+      int dev = 0, sms = 0, occ = 0;                                                                     \
+      cudaGetDevice(&dev);                                                                               \
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);                                 \
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_stage_kernel<TI, TJ, R, FK>, TI * TJ,    \
+                                                    StageSmem<TI, TJ, R>::bytes);                        \
+      cap = (sms > 0 && occ > 0) ? sms * occ : grid;                                                     \
+    }                                                                                                    \
+    batch_stage_kernel<TI, TJ, R, FK><<<std::min(grid, cap), TI * TJ, StageSmem<TI, TJ, R>::bytes, s>>>(b); \
   }                                                                                                      \
   template <> cudaError_t launch_batch_stage<double, FK>(const BatchArgs<double>& b, int tile, int grid, \
                                                          cudaStream_t s) {                               \

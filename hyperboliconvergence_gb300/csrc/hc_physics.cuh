@@ -64,7 +64,7 @@ template <class R> struct St { R p, r, h, u2, a2, u, v; };
 template <class R> struct Flux5 { R f[4]; R lam; };
 
 // set2State(primitive) (conservationLaws/euler/transforms/primitive.ipp:101-137)
-template <class R> __device__ __forceinline__ St<R> prim_state(const Gas<R>& g, R u, R v, R r, R p) {
+template <class R> __host__ __device__ __forceinline__ St<R> prim_state(const Gas<R>& g, R u, R v, R r, R p) {
   St<R> s;
   s.u = u; s.v = v;
   s.u2 = u * u;
@@ -78,7 +78,7 @@ template <class R> __device__ __forceinline__ St<R> prim_state(const Gas<R>& g, 
 }
 
 // set2State(conserved) (conservationLaws/euler/transforms/conserved.ipp:31-76)
-template <class R> __device__ __forceinline__ St<R> cons_state(const Gas<R>& g, const R* qc) {
+template <class R> __host__ __device__ __forceinline__ St<R> cons_state(const Gas<R>& g, const R* qc) {
   St<R> s;
   const R r = qc[2], re = qc[3];
   const R r1 = R(1) / r;
@@ -95,15 +95,15 @@ template <class R> __device__ __forceinline__ St<R> cons_state(const Gas<R>& g, 
 }
 
 // state2Set<conserved> (conservationLaws/euler/transforms/conserved.ipp:2-29)
-template <class R> __device__ __forceinline__ void state_cons(const St<R>& s, R* qc) {
+template <class R> __host__ __device__ __forceinline__ void state_cons(const St<R>& s, R* qc) {
   qc[0] = s.r * s.u; qc[1] = s.r * s.v; qc[2] = s.r; qc[3] = s.r * s.h - s.p;
 }
 
 // projectedVelocity (conservationLaws/base/base.h:148-158)
-template <class R> __device__ __forceinline__ R proj(R nx, R ny, const St<R>& s) { return nx * s.u + ny * s.v; }
+template <class R> __host__ __device__ __forceinline__ R proj(R nx, R ny, const St<R>& s) { return nx * s.u + ny * s.v; }
 
 // exactFlux (conservationLaws/euler/fluxes/exactFlux.ipp:231-263)
-template <class R> __device__ __forceinline__ Flux5<R> exact_flux(R nx, R ny, const St<R>& s) {
+template <class R> __host__ __device__ __forceinline__ Flux5<R> exact_flux(R nx, R ny, const St<R>& s) {
   Flux5<R> o;
   const R a = sqrt(s.a2);
   const R un = proj(nx, ny, s);
@@ -117,7 +117,7 @@ template <class R> __device__ __forceinline__ Flux5<R> exact_flux(R nx, R ny, co
 }
 
 // CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:25-37)
-template <class R> __device__ __forceinline__ Flux5<R> central_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
+template <class R> __host__ __device__ __forceinline__ Flux5<R> central_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
   const Flux5<R> fl = exact_flux(nx, ny, l), fr = exact_flux(nx, ny, r);
   Flux5<R> o;
 #pragma unroll
@@ -131,7 +131,7 @@ template <class R> __device__ __forceinline__ Flux5<R> central_flux(R nx, R ny, 
 // and the characteristic transforms (conservationLaws/euler/transforms/primitive.ipp:142-313).
 // The Roe-averaged state keeps its velocity in the global frame while the jump
 // is rotated to the face frame, exactly as the reference composes them.
-template <class R> __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g, R nx, R ny, R A,
+template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g, R nx, R ny, R A,
                                                                const St<R>& l, const St<R>& r) {
   const Flux5<R> c = central_flux(nx, ny, A, l, r);
   // roe average
@@ -212,7 +212,7 @@ template <class R> __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g,
 }
 
 // RusanovFlux (conservationLaws/base/fluxes/rusanovFlux.ipp:99-147)
-template <class R> __device__ __forceinline__ Flux5<R> rusanov_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
+template <class R> __host__ __device__ __forceinline__ Flux5<R> rusanov_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
   Flux5<R> o = central_flux(nx, ny, A, l, r);
   const R lambda = fmax(fabs(proj(nx, ny, l)) + sqrt(l.a2), fabs(proj(nx, ny, r)) + sqrt(r.a2));
   const R s = R(-0.5) * (lambda * A);
@@ -224,18 +224,18 @@ template <class R> __device__ __forceinline__ Flux5<R> rusanov_flux(R nx, R ny, 
 }
 
 // Mach splittings (conservationLaws/euler/fluxes/machSplittings.ipp:163-204)
-template <class R> __device__ __forceinline__ R ms_m1(R s, R M) { return R(0.5) * (M + s * fabs(M)); }
-template <class R> __device__ __forceinline__ R ms_m2(R s, R M) { return s * R(0.25) * (M + s) * (M + s); }
-template <class R> __device__ __forceinline__ R ms_m4(R s, R M, R beta) {
+template <class R> __host__ __device__ __forceinline__ R ms_m1(R s, R M) { return R(0.5) * (M + s * fabs(M)); }
+template <class R> __host__ __device__ __forceinline__ R ms_m2(R s, R M) { return s * R(0.25) * (M + s) * (M + s); }
+template <class R> __host__ __device__ __forceinline__ R ms_m4(R s, R M, R beta) {
   return ms_m2(s, M) * (R(1) - s * R(16) * beta * ms_m2(-s, M));
 }
 // (M1 + eps)/(|M| + eps) with eps the largest finite value
-template <class R> __device__ __forceinline__ R ms_p1(R s, R M) {
+template <class R> __host__ __device__ __forceinline__ R ms_p1(R s, R M) {
   const R eps = Lim<R>::huge();
   return (ms_m1(s, M) + eps) / (fabs(M) + eps);
 }
-template <class R> __device__ __forceinline__ R ms_p3(R s, R M) { return ms_m2(s, M) * (s * R(2) - M); }
-template <class R> __device__ __forceinline__ R ms_p5(R s, R M, R alpha) {
+template <class R> __host__ __device__ __forceinline__ R ms_p3(R s, R M) { return ms_m2(s, M) * (s * R(2) - M); }
+template <class R> __host__ __device__ __forceinline__ R ms_p5(R s, R M, R alpha) {
   return ms_p3(s, M) - s * R(16) * alpha * M * ms_m2(s, M) * ms_m2(-s, M);
 }
 
@@ -243,7 +243,7 @@ template <class R> __device__ __forceinline__ R ms_p5(R s, R M, R alpha) {
 // by_mdot=false: literal reference upwinding by the sign of ua (slau.ipp:124-125);
 // by_mdot=true: upwinding by the sign of the interface mass flux.
 template <class R, bool by_mdot>
-__device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
+__host__ __device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
   const R ua = sqrt(R(0.5) * (l.u2 + r.u2));
   const R al = sqrt(l.a2), ar = sqrt(r.a2);
   const R aa = R(0.5) * (al + ar);
@@ -276,7 +276,7 @@ __device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St<R>& l, c
 }
 
 // AUSM+up with (Convective, Convective) tags (conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171)
-template <class R> __device__ __forceinline__ Flux5<R> ausmpup_flux(const Gas<R>& g, R nx, R ny, R A,
+template <class R> __host__ __device__ __forceinline__ Flux5<R> ausmpup_flux(const Gas<R>& g, R nx, R ny, R A,
                                                                    const St<R>& l, const St<R>& r) {
   const R alpha0 = R(0.1875), beta = R(0.125), Ku = R(0.75 * 2.), Kp = R(0.25), sigma = R(1.0);
   const R ascoeff = R(2) * g.gm1 / (g.gamma + R(1));
@@ -317,7 +317,7 @@ template <class R> __device__ __forceinline__ Flux5<R> ausmpup_flux(const Gas<R>
 }
 
 template <class R, int FK>
-__device__ __forceinline__ Flux5<R> face_flux(const Gas<R>& g, R nx, R ny, R A, const St<R>& l, const St<R>& r) {
+__host__ __device__ __forceinline__ Flux5<R> face_flux(const Gas<R>& g, R nx, R ny, R A, const St<R>& l, const St<R>& r) {
   if constexpr (FK == FLUX_ROE) return roe_flux(g, nx, ny, A, l, r);
   else if constexpr (FK == FLUX_SLAU) return slau_flux<R, true>(nx, ny, A, l, r);
   else if constexpr (FK == FLUX_SLAU_REF) return slau_flux<R, false>(nx, ny, A, l, r);
@@ -329,7 +329,7 @@ __device__ __forceinline__ Flux5<R> face_flux(const Gas<R>& g, R nx, R ny, R A, 
 // Slope limiters (limiters/limiter.ipp:141-297), called as limit(central, biased).
 // LIM_VANLEER is the harmonic-mean slope (a|b|+|a|b)/(|a|+|b|+eps);
 // LIM_VANLEER_REF the literal reference expression (limiter.ipp:216-224).
-template <class R> __device__ __forceinline__ R limit(int kind, R a, R b) {
+template <class R> __host__ __device__ __forceinline__ R limit(int kind, R a, R b) {
   const R tiny = Lim<R>::tiny();
   switch (kind) {
     case LIM_NOLIMIT1: return R(0);
@@ -368,7 +368,7 @@ template <class R> __device__ __forceinline__ R limit(int kind, R a, R b) {
 
 // Roe average of two primitive states in the face frame, used by the far-field
 // boundary updates (conservationLaws/euler/fluxes/roe.ipp:150-196).
-template <class R> __device__ __forceinline__ void roe_avg_vel(const St<R>& l, const St<R>& r, R* uav, R* u2,
+template <class R> __host__ __device__ __forceinline__ void roe_avg_vel(const St<R>& l, const St<R>& r, R* uav, R* u2,
                                                               R* a2, const Gas<R>& g) {
   const R cr = sqrt(r.r / l.r);
   const R wl = R(1) / (R(1) + cr);
@@ -388,7 +388,7 @@ template <class R> __device__ __forceinline__ void roe_avg_vel(const St<R>& l, c
 // and entropy/pressure far field (entropy.ipp:18-88).  (nx,ny) points into the
 // domain; qi, qf, qb are primitive.
 template <class R, int BK>
-__device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, R ny, const R* qi, const R* qf, R* qb) {
+__host__ __device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, R ny, const R* qi, const R* qf, R* qb) {
   const R tx = -ny, ty = nx;
   const R ri[4] = {nx * qi[0] + ny * qi[1], tx * qi[0] + ty * qi[1], qi[2], qi[3]};
   const R rf[4] = {nx * qf[0] + ny * qf[1], tx * qf[0] + ty * qf[1], qf[2], qf[3]};
@@ -436,7 +436,7 @@ __device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, R ny, con
 
 // Inviscid wall (conservationLaws/euler/boundary/inviscidWall.ipp:33-72): pressure
 // flux only, from the interior state moved to the face (qw primitive).
-template <class R> __device__ __forceinline__ Flux5<R> wall_flux(const Gas<R>& g, R nx, R ny, R A, const R* qw) {
+template <class R> __host__ __device__ __forceinline__ Flux5<R> wall_flux(const Gas<R>& g, R nx, R ny, R A, const R* qw) {
   const St<R> s = prim_state(g, qw[0], qw[1], qw[2], qw[3]);
   Flux5<R> o;
   o.f[0] = A * s.p * nx;

@@ -184,6 +184,7 @@ typedef struct {
   long long kernel_launches;
   double ms_forward;         /* first forward sweep */
   double ms_total;           /* forward sweep + reverse sweep */
+  double ms_recompute;       /* part of the reverse sweep spent re-advancing from checkpoints */
 } hc_adjoint_stats;
 
 /* J only; rates_in NULL = compute the timesteps (rates_out receives them, nsteps values). */
