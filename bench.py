@@ -237,29 +237,100 @@ def measure_batched(stream, ninst: int = 256, steps: int = 3, seed: int = 2026):
     return res
 
 
+def measure_variants(stream, steps: int = 10):
+    """The O-grid workload with each flux at M 0.3 and 0.8: FP64 cell-updates/s over
+    `steps` RK steps after 3 warm-up steps, and the FP32 relative L-inf difference of
+    the conserved variables from FP64 after 20 steps from the freestream.  SLAU runs
+    the literal reference form first and the mass-flux-upwinded form if the literal
+    one goes non-physical."""
+    import torch
+    from hyperboliconvergence_gb300 import HCError, cases
+    from hyperboliconvergence_gb300.solver import Solver
+    g = 1.4
+
+    def cons(w):
+        u, v, r, p = w
+        return np.stack([r * u, r * v, r, p / (g - 1) + 0.5 * r * (u * u + v * v)])
+
+    out = {}
+    for mach in (0.3, 0.8):
+        mesh, bc, ref, q, species = cases.cylinder(NR, NTH, mach=mach)
+        for flux in ("roe", ("slau_ref", "slau"), "ausmpup"):
+            tries = flux if isinstance(flux, tuple) else (flux,)
+            for fl in tries:
+                key = f"{fl}_M{mach}"
+                try:
+                    states = {}
+                    res = {}
+                    for prec in ("fp64", "fp32"):
+                        s = Solver(mesh, bc, ref, flux=fl, limiter=LIMITER, rk=RKT, precision=prec, dt=DTMODE,
+                                   cfl=CFL, species=species, stream=stream.cuda_stream)
+                        s.set_state(q)
+                        if prec == "fp64":
+                            s.step(3)
+                            e0, e1 = _events()
+                            torch.cuda.synchronize()
+                            e0.record(stream)
+                            s.step_async(steps)
+                            e1.record(stream)
+                            s.sync()
+                            ms = e0.elapsed_time(e1) / steps
+                            res = {"value": NR * NTH / (ms / 1e3), "unit": UNIT, "ms_per_step": ms}
+                            s.set_state(q)
+                        s.step(20)
+                        states[prec] = cons(s.get_state())
+                        s.close()
+                    a, b = states["fp32"], states["fp64"]
+                    res["fp32_error_vs_fp64_after_20_steps"] = float(
+                        (np.abs(a - b).reshape(4, -1).max(1) / np.abs(b).reshape(4, -1).max(1)).max())
+                    out[key] = res
+                    break
+                except HCError as exc:
+                    out[key] = {"error": str(exc)}
+    return out
+
+
 def measure_adjoint(nsteps: int = 400, snapshots: int = 20):
     """Differentiated case: 256x512 O-grid (0.5 to 20), M 0.4, Roe + van Albada, ssp34,
-    nsteps from uniform freestream; drag averaged over the steps; gradient with
-    respect to every cell's initial state and the far-field state; binomial
-    checkpointing with `snapshots` stored states; FP64."""
+    nsteps from uniform freestream; drag coefficient averaged over the steps; gradient
+    with respect to every cell's initial state and the far-field state (hence Mach and
+    angle of attack); binomial checkpointing with `snapshots` stored states.  Run with
+    FP64 stages and with double-float forward stages (the reverse sweep is FP64 in
+    both).  The adjoint-step metric is reverse-sweep time (checkpoint recomputation
+    included) per step over forward-sweep time per step."""
+    import math
     from hyperboliconvergence_gb300.solver import Mesh, Solver
-    nr, nth, mach = 256, 512, 0.4
+    nr, nth, mach, alpha = 256, 512, 0.4, 0.0
     mesh = Mesh.cylinder(nr, nth, 0.5, 20.0, 1.01)
-    qinf = np.array([mach, 0.0, 1.0, 1.0 / 1.4])
+    qinf = np.array([mach * math.cos(alpha), mach * math.sin(alpha), 1.0, 1.0 / 1.4])
     ref = [None, np.broadcast_to(qinf[:, None], (4, nth)).copy(), None, None]
-    s = Solver(mesh, ["wall", "fixed", "periodic", "periodic"], ref, flux="roe", limiter="vanalbada", rk="ssp34",
-               precision="fp64", dt="global", cfl=0.5, species=(1.4, 287.058, mach))
-    s.set_state(np.broadcast_to(qinf[:, None, None], (4, nr, nth)).copy())
-    scale = 1.0 / (0.5 * mach * mach * 2 * 0.5)
-    J, g, refb, rates, st = s.gradient(nsteps, snapshots=snapshots, kind="drag", scale=scale)
-    fwd_ms = st.ms_forward
-    adj_ms = st.ms_total - st.ms_forward
-    s.close()
-    return {"workload": f"cylinder O-grid {nr}x{nth}, M{mach}, {nsteps} ssp34 steps, {snapshots} snapshots",
-            "J_time_avg_cd": J, "forward_ms": fwd_ms, "reverse_ms": adj_ms,
-            "adjoint_over_forward": adj_ms / fwd_ms,
-            "forward_steps_total": int(st.forward_steps), "adjoint_steps": int(st.adjoint_steps),
-            "grad_norm_q0": float(np.linalg.norm(g))}
+    out = {"workload": f"cylinder O-grid {nr}x{nth}, M{mach}, {nsteps} ssp34 steps, {snapshots} snapshots"}
+    for prec in ("fp64", "fp64_df"):
+        s = Solver(mesh, ["wall", "fixed", "periodic", "periodic"], ref, flux="roe", limiter="vanalbada",
+                   rk="ssp34", precision=prec, dt="global", cfl=0.5, species=(1.4, 287.058, mach))
+        s.set_state(np.broadcast_to(qinf[:, None, None], (4, nr, nth)).copy())
+        scale = 1.0 / (0.5 * mach * mach * 2 * 0.5)
+        J, g, refb, rates, st = s.gradient(nsteps, snapshots=snapshots, kind="drag", scale=scale)
+        s.close()
+        fwd, rev, rec = st.ms_forward, st.ms_total - st.ms_forward, st.ms_recompute
+        # freestream derivatives: q0 and the far-field layer both equal qinf(M, alpha);
+        # Cd = scale(M) * D with scale ~ 1/M^2
+        dq_dm = np.array([math.cos(alpha), math.sin(alpha), 0.0, 0.0])
+        dq_da = np.array([-mach * math.sin(alpha), mach * math.cos(alpha), 0.0, 0.0])
+        gsum = g.reshape(4, -1).sum(axis=1) + refb[1].reshape(4, -1).sum(axis=1)
+        out[prec] = {
+            "J_time_avg_cd": J,
+            "dJ_dmach": float(gsum @ dq_dm - 2.0 * J / mach), "dJ_dalpha": float(gsum @ dq_da),
+            "grad_norm_q0": float(np.linalg.norm(g)),
+            "forward_ms": fwd, "reverse_ms": rev, "recompute_ms": rec,
+            "forward_step_ms": fwd / nsteps,
+            "adjoint_step_over_forward_step": rev / fwd,
+            "adjoint_step_over_forward_step_excl_recompute": (rev - rec) / fwd,
+            "forward_steps_total": int(st.forward_steps), "adjoint_steps": int(st.adjoint_steps)}
+    a, b = out["fp64"], out["fp64_df"]
+    out["df_vs_fp64_grad_rel_diff"] = {k: abs(b[k] - a[k]) / max(abs(a[k]), 1e-300)
+                                       for k in ("J_time_avg_cd", "dJ_dmach", "grad_norm_q0")}
+    return out
 
 
 def dist_setup():
@@ -387,6 +458,7 @@ def run_gpu(args):
             for name, fn in (("fp32", lambda: measure_precision(stream, args.steps, "fp32")),
                              ("fp64_df", lambda: measure_precision(stream, args.steps, "fp64_df")),
                              ("batched", lambda: measure_batched(stream)),
+                             ("variants", lambda: measure_variants(stream)),
                              ("adjoint", measure_adjoint)):
                 if name in extras:
                     try:
@@ -409,8 +481,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP32, double-float, batched and adjoint measurements beside the headline")
-    ap.add_argument("--extras", default="fp32,fp64_df,batched,adjoint",
-                    help="comma-separated subset of fp32,fp64_df,batched,adjoint to measure beside the headline")
+    ap.add_argument("--extras", default="fp32,fp64_df,batched,variants,adjoint",
+                    help="comma-separated subset of fp32,fp64_df,batched,variants,adjoint to measure beside the "
+                         "headline")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -63,6 +63,7 @@ def _declare(lib):
         "hc_step": [p, i, C.POINTER(StepStats)],
         "hc_step_async": [p, i],
         "hc_sync": [p, C.POINTER(StepStats)],
+        "hc_steady_run": [p, C.POINTER(SteadyControls), dp, C.c_longlong, C.POINTER(SteadyStats)],
         "hc_spectral_radius": [v, v, C.c_longlong, v, v],
         "hc_spectral_radius_noalloc": [v, v, C.c_longlong, v, v],
         "hc_mesh_cylinder_nodes": [i, i, d, d, d, dp],
@@ -146,6 +147,16 @@ def _declare_batch(lib):
 class Objective(C.Structure):
     _fields_ = [("kind", C.c_int), ("scale", C.c_double), ("dir", C.c_double * 2),
                 ("target", C.POINTER(C.c_double)), ("weight", C.c_double * 4)]
+
+
+class SteadyControls(C.Structure):
+    _fields_ = [("max_steps", C.c_longlong), ("residual_drop", C.c_double), ("check_every", C.c_int),
+                ("use_residual_smoothing", C.c_int), ("smoothing_factor", C.c_double)]
+
+
+class SteadyStats(C.Structure):
+    _fields_ = [("res0", C.c_double), ("res", C.c_double), ("steps", C.c_longlong),
+                ("history_len", C.c_longlong), ("converged", C.c_int)]
 
 
 class AdjointStats(C.Structure):

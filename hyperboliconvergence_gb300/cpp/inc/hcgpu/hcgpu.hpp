@@ -100,6 +100,15 @@ template <class Real> struct UnsteadyTimeControls {
   Real cfl;
 };
 
+// SteadyTimeControls (controls.h:31-48)
+template <class Real> struct SteadyTimeControls {
+  std::size_t nTimesteps;
+  Real cfl;
+  Real residual_drop;
+  bool use_residual_smoothing = false;
+  Real smoothing_factor = 0;
+};
+
 // execution policies: the GPU path in global or local timestepping
 namespace execution {
 struct gpu_policy { int dt_mode = HC_DT_GLOBAL; int precision = HC_FP64; };
@@ -194,6 +203,37 @@ hc_step_stats integrate(const execution::gpu_policy policy, const UnsteadyTimeCo
   hc_step_stats st{};
   check(hc_step(ctx.get(), int(timeControls.nTimesteps), &st));
   check(hc_state_download(ctx.get(), q.interior.data()));
+  return st;
+}
+
+// Steady-state integrate: the convergence loop SteadyTimeControls describes, on the
+// GPU; returns the residual history (read every check_every steps) and the stats.
+template <class Real>
+hc_steady_stats integrate(const execution::gpu_policy policy, const SteadyTimeControls<Real>& timeControls,
+                          const ODE::Explicit::RungeKutta<Real>& rungeKutta, const MusclFlux& flux2,
+                          const Species<Real>& species, const Mesh<Real>& mesh, SolutionField<Real>& q,
+                          std::vector<double>* history = nullptr, int check_every = 100) {
+  if (q.ni != mesh.ni || q.nj != mesh.nj) throw Error(HC_ERR_ARG, "solution field and mesh shapes differ");
+  hc_config cfg{flux2.flux, flux2.limiter, rungeKutta.id, policy.precision, policy.dt_mode,
+                double(timeControls.cfl)};
+  Context ctx(cfg);
+  check(hc_mesh_upload(ctx.get(), mesh.ni, mesh.nj, mesh.nodes.data()));
+  check(hc_set_species(ctx.get(), species.gamma, species.R, species.minf));
+  int bct[4];
+  const double* refs[4];
+  for (int s = 0; s < 4; ++s) {
+    bct[s] = int(q.bcTypes[s]);
+    refs[s] = q.boundary[s].data();
+  }
+  check(hc_set_bcs(ctx.get(), bct, refs));
+  check(hc_state_upload(ctx.get(), q.interior.data()));
+  const hc_steady_controls ctl{(long long)timeControls.nTimesteps, double(timeControls.residual_drop), check_every,
+                               timeControls.use_residual_smoothing ? 1 : 0, double(timeControls.smoothing_factor)};
+  std::vector<double> h(timeControls.nTimesteps / std::size_t(check_every) + 2);
+  hc_steady_stats st{};
+  check(hc_steady_run(ctx.get(), &ctl, h.data(), (long long)h.size(), &st));
+  check(hc_state_download(ctx.get(), q.interior.data()));
+  if (history) history->assign(h.begin(), h.begin() + st.history_len);
   return st;
 }
 

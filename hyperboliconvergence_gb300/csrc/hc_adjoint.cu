@@ -309,7 +309,7 @@ int reverse(Adj& A, int a, int b, int slot, std::vector<int>& stack) {
 }
 
 int check_support(hc_ctx* c) {
-  if (c->fp32 || c->df) return fail(HC_ERR_UNSUPPORTED, "the adjoint runs on HC_FP64 contexts");
+  if (c->fp32) return fail(HC_ERR_UNSUPPORTED, "the adjoint runs on HC_FP64 and HC_FP64_DF contexts");
   if (c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV)
     return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");
   const int l = c->cfg.limiter;

@@ -3,6 +3,7 @@
 #include "hc_host.h"
 #include "hc_geometry.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -428,6 +429,40 @@ int hc_step(hc_ctx* c, int nsteps, hc_step_stats* stats) {
   const int st = hc_step_async(c, nsteps);
   if (st != HC_OK) return st;
   return hc_sync(c, stats);
+}
+
+// Steady driver: the convergence loop SteadyTimeControls describes (controls.h:31-48)
+int hc_steady_run(hc_ctx* c, const hc_steady_controls* ctl, double* history, long long history_len,
+                  hc_steady_stats* out) {
+  if (int st = check_ctx(c)) return st;
+  if (!ctl || ctl->max_steps < 1 || ctl->check_every < 1 || !(ctl->residual_drop > 0.0))
+    return fail(HC_ERR_ARG, "invalid steady controls");
+  if (ctl->use_residual_smoothing)
+    return fail(HC_ERR_UNSUPPORTED, "residual smoothing exists only in the reference's 1D path");
+  hc_steady_stats res{};
+  auto record = [&](double r) {
+    if (history && res.history_len < history_len) history[res.history_len] = r;
+    if (history && res.history_len < history_len) ++res.history_len;
+  };
+  hc_step_stats s{};
+  int st = hc_step(c, 1, &s);
+  if (st == HC_OK) {
+    res.res0 = res.res = s.resnorm;
+    res.steps = 1;
+    record(s.resnorm);
+    res.converged = !(res.res0 > 0.0);
+    while (!res.converged && res.steps < ctl->max_steps) {
+      const int n = int(std::min<long long>(ctl->check_every, ctl->max_steps - res.steps));
+      st = hc_step(c, n, &s);
+      if (st != HC_OK) break;
+      res.steps += n;
+      res.res = s.resnorm;
+      record(s.resnorm);
+      res.converged = res.res <= ctl->residual_drop * res.res0;
+    }
+  }
+  if (out) *out = res;
+  return st;
 }
 
 // make_cylinder_mesh (mesh/generate/twoD.h:223-263) with geometric radial stretching

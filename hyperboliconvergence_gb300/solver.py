@@ -67,6 +67,8 @@ class Solver:
         self.lib = _capi.load()
         self.mesh = mesh
         self.precision = precision
+        self.flux, self.limiter, self.rk, self.dt, self.cfl = flux, limiter, rk, dt, float(cfl)
+        self.species = tuple(float(x) for x in species)
         cfg = Config(FLUX[flux] if isinstance(flux, str) else int(flux),
                      LIMITER[limiter] if isinstance(limiter, str) else int(limiter),
                      RK[rk] if isinstance(rk, str) else int(rk),
@@ -98,6 +100,9 @@ class Solver:
                 ptrs[s] = _dptr(arr)
         check(self.lib.hc_set_bcs(self.h, bct, ptrs))
         self.bc = list(bc)
+        self.ref = [None if ref is None or ref[s] is None else
+                    np.broadcast_to(np.asarray(ref[s], dtype=np.float64).reshape(4, -1), (4, mesh.nface(s))).copy()
+                    for s in range(4)]
 
     # -- discrete adjoint -----------------------------------------------------
     def _objective(self, kind, scale=1.0, direction=(1.0, 0.0), target=None, weight=(1.0, 1.0, 1.0, 1.0)):
@@ -195,6 +200,17 @@ class Solver:
         st = StepStats()
         check(self.lib.hc_step(self.h, int(n), C.byref(st)))
         return st
+
+    def steady(self, max_steps: int, residual_drop: float = 1e-10, check_every: int = 100):
+        """Run to a steady state (SteadyTimeControls, controls.h:31-48): steps until the
+        stage-0 density-residual L2 norm drops by residual_drop or max_steps; returns
+        (SteadyStats, residual-norm history read every check_every steps)."""
+        from ._capi import SteadyControls, SteadyStats
+        ctl = SteadyControls(int(max_steps), float(residual_drop), int(check_every), 0, 0.0)
+        hist = np.empty(int(max_steps) // int(check_every) + 2)
+        st = SteadyStats()
+        check(self.lib.hc_steady_run(self.h, C.byref(ctl), _dptr(hist), hist.size, C.byref(st)))
+        return st, hist[:st.history_len].copy()
 
     def step_async(self, n: int = 1) -> None:
         check(self.lib.hc_step_async(self.h, int(n)))

@@ -129,6 +129,32 @@ int hc_step(hc_ctx* ctx, int nsteps, hc_step_stats* stats);
 int hc_step_async(hc_ctx* ctx, int nsteps);
 int hc_sync(hc_ctx* ctx, hc_step_stats* stats);
 
+/* SteadyTimeControls (controls.h:31-48), which the reference declares but no driver
+ * consumes: RK steps in the context's timestep mode (normally HC_DT_LOCAL) until the
+ * L2 norm of the stage-0 density residual falls to residual_drop times its value at
+ * the first step, or max_steps steps.  The norm is read on the host every
+ * check_every steps; history (may be NULL) receives those reads, at most
+ * history_len of them.  Residual smoothing exists only in the reference's legacy 1D
+ * path: use_residual_smoothing != 0 returns HC_ERR_UNSUPPORTED. */
+typedef struct {
+  long long max_steps;        /* nTimesteps */
+  double residual_drop;       /* residual_drop */
+  int check_every;
+  int use_residual_smoothing; /* use_residual_smoothing */
+  double smoothing_factor;    /* smoothing_factor (unused) */
+} hc_steady_controls;
+
+typedef struct {
+  double res0;          /* density-residual norm of the first step */
+  double res;           /* at the last read */
+  long long steps;      /* steps taken */
+  long long history_len;/* entries written to history */
+  int converged;        /* res <= residual_drop * res0 */
+} hc_steady_stats;
+
+int hc_steady_run(hc_ctx* ctx, const hc_steady_controls* controls, double* history, long long history_len,
+                  hc_steady_stats* stats);
+
 /* spectralRadius (spatial/spectralRadius.h:19-48): out_device[0] = max over the
  * ncell cells of lambda_sum[c] / vol[c], the fold starting at the smallest
  * positive double.  All three pointers are device memory; the call is
@@ -164,8 +190,10 @@ int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, d
  * residual and of the RK update, with the timestep of every step frozen at the
  * value of the forward run ("rates": the per-step max lambda/V, returned so a
  * finite-difference check can replay them).  Binomial checkpointing keeps
- * `snapshots` states.  FP64 contexts; Roe or Rusanov; NoLimit1/2/3, van Albada,
- * MinMod, van Leer; periodic, fixed and wall boundaries; global timestep.
+ * `snapshots` states.  HC_FP64 contexts, or HC_FP64_DF contexts (forward,
+ * replayed and recomputed steps in double-float stage arithmetic, the reverse
+ * sweep in FP64); Roe or Rusanov; NoLimit1/2/3, van Albada, MinMod, van Leer;
+ * periodic, fixed and wall boundaries; global timestep.
  * ------------------------------------------------------------------------- */
 typedef enum { HC_OBJ_DRAG = 0, HC_OBJ_L2 = 1 } hc_objective_kind;
 

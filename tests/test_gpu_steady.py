@@ -1,0 +1,41 @@
+"""Steady-state driver (SteadyTimeControls, controls.h:31-48): convergence of the
+density residual on a small O-grid with local timestepping, the step cap, and the
+refusal of residual smoothing."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from hyperboliconvergence_gb300 import cases
+from hyperboliconvergence_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+
+def small_cylinder(**kw):
+    mesh, bc, ref, q, sp = cases.cylinder(24, 48, mach=0.3, rb=8.0)
+    s = Solver(mesh, bc, ref, flux="roe", limiter="vanalbada", dt="local", cfl=0.5, species=sp, **kw)
+    s.set_state(q)
+    return s
+
+
+def test_steady_cylinder_converges():
+    s = small_cylinder()
+    st, hist = s.steady(60000, residual_drop=1e-8, check_every=500)
+    assert st.converged, (st.steps, (hist[-5:] / hist[0]).tolist())
+    assert st.res <= 1e-8 * st.res0 and hist[0] == st.res0 and hist[-1] == st.res
+    assert len(hist) == st.history_len
+
+
+def test_steady_stops_at_step_cap():
+    s = small_cylinder()
+    st, hist = s.steady(10, residual_drop=1e-30, check_every=4)
+    assert not st.converged and st.steps == 10 and len(hist) == 4  # steps 1, 5, 9, 10
+
+
+def test_steady_refuses_residual_smoothing():
+    from hyperboliconvergence_gb300._capi import SteadyControls, SteadyStats
+    s = small_cylinder()
+    ctl = SteadyControls(100, 1e-6, 10, 1, 0.5)
+    st = SteadyStats()
+    assert s.lib.hc_steady_run(s.h, C.byref(ctl), None, 0, C.byref(st)) == 5
