@@ -244,12 +244,66 @@ int adjoint_step(Adj& A, int step) {
 }
 
 // ---- binomial checkpointing
+// Reversing n steps whose start state is restorable, with s free snapshot slots,
+// costs T(n, s) recomputed forward steps under the best schedule:
+//   T(1, s) = 0,  T(n, 0) = n(n-1)/2 (every state re-advanced from the start),
+//   T(n, s) = min_k [k + T(n-k, s-1) + T(k, s)]
+// (advance k steps and store, reverse the right part with one slot fewer, then
+// the left part with the slot freed).  The first forward sweep passes every
+// state, so it stores the checkpoints of the schedule's first descent (the
+// right-most path) as it goes; for that path the advance is free:
+//   F(n, s) = min_k [F(n-k, s-1) + T(k, s)],  F(n, 0) = T(n, 0).
+// Both tables and their minimising splits are computed by dynamic programming
+// (O(n^2 s)); beyond kDpLimit operations the split falls back to the binomial
+// rule k = n - C(s-1+t, s-1), t the smallest with C(s+t, s) >= n.
+constexpr double kDpLimit = 4e8;
+
 double binom(int n, int k) {
   if (k < 0 || k > n) return 0;
   double r = 1;
   for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
   return r;
 }
+
+int binomial_split(int n, int s) {
+  int t = 1;
+  while (binom(s + t, s) < n) ++t;
+  const int k = n - int(binom(s - 1 + t, s - 1));
+  return std::max(1, std::min(k, n - 1));
+}
+
+struct Schedule {
+  int N = 0, S = 0;
+  bool dp = false;
+  std::vector<long long> T, F;
+  std::vector<int> kT, kF;
+  size_t at(int n, int s) const { return size_t(s) * (N + 1) + n; }
+  void build(int n_max, int s_max) {
+    N = n_max; S = s_max;
+    dp = double(N) * N * (S + 1) <= kDpLimit;
+    if (!dp) return;
+    const size_t m = size_t(N + 1) * (S + 1);
+    T.assign(m, 0); F.assign(m, 0); kT.assign(m, 1); kF.assign(m, 1);
+    for (int n = 0; n <= N; ++n) T[at(n, 0)] = F[at(n, 0)] = (long long)n * (n - 1) / 2;
+    for (int s = 1; s <= S; ++s)
+      for (int n = 2; n <= N; ++n) {
+        long long bt = -1, bf = -1;
+        int kt = 1, kf = 1;
+        for (int k = 1; k < n; ++k) {
+          const long long right_t = T[at(n - k, s - 1)], right_f = F[at(n - k, s - 1)], left = T[at(k, s)];
+          const long long ct = k + right_t + left, cf = right_f + left;
+          if (bt < 0 || ct < bt) { bt = ct; kt = k; }
+          if (bf < 0 || cf < bf) { bf = cf; kf = k; }
+        }
+        T[at(n, s)] = bt; kT[at(n, s)] = kt;
+        F[at(n, s)] = bf; kF[at(n, s)] = kf;
+      }
+  }
+  int split(int n, int s, bool first) const {
+    if (!dp) return binomial_split(n, s);
+    return first ? kF[at(n, s)] : kT[at(n, s)];
+  }
+};
 
 double* slot_ptr(Adj& A, int slot) { return slot < 0 ? A.base : A.snaps + size_t(slot) * 4 * A.n; }
 
@@ -277,8 +331,24 @@ int advance(Adj& A, int from, int to) {
   return HC_OK;
 }
 
-// reverse steps [a, b) whose start state is in `slot`; `free_slots` unused snapshot slots on `stack`
-int reverse(Adj& A, int a, int b, int slot, std::vector<int>& stack) {
+// The first descent of the schedule for n steps and s slots: (position, slot)
+// pairs, slots taken from the back of `stack` as reverse() takes them.
+std::vector<std::pair<int, int>> first_descent(const Schedule& sc, int n, int s, std::vector<int> stack) {
+  std::vector<std::pair<int, int>> out;
+  int a = 0;
+  while (n - a > 1 && !stack.empty()) {
+    const int k = sc.split(n - a, int(stack.size()), true);
+    out.push_back({a + k, stack.back()});
+    stack.pop_back();
+    a += k;
+  }
+  return out;
+}
+
+// reverse steps [a, b) whose start state is in `slot`, with the free slots on
+// `stack`; `first`: the split points of this call's right-most path were stored
+// by the forward sweep
+int reverse(Adj& A, const Schedule& sc, int a, int b, int slot, std::vector<int>& stack, bool first) {
   const int n = b - a;
   const int sfree = int(stack.size());
   if (n <= 0) return HC_OK;
@@ -294,18 +364,17 @@ int reverse(Adj& A, int a, int b, int slot, std::vector<int>& stack) {
     }
     return HC_OK;
   }
-  int t = 1;
-  while (binom(sfree + t, sfree) < n) ++t;
-  int k = n - int(binom(sfree - 1 + t, sfree - 1));
-  k = std::max(1, std::min(k, n - 1));
-  if (int st = restore(A, slot)) return st;
-  if (int st = advance(A, a, a + k)) return st;
+  const int k = sc.split(n, sfree, first);
   const int mid = stack.back();
   stack.pop_back();
-  if (int st = store(A, mid)) return st;
-  if (int st = reverse(A, a + k, b, mid, stack)) return st;
+  if (!first) {
+    if (int st = restore(A, slot)) return st;
+    if (int st = advance(A, a, a + k)) return st;
+    if (int st = store(A, mid)) return st;
+  }
+  if (int st = reverse(A, sc, a + k, b, mid, stack, first)) return st;
   stack.push_back(mid);
-  return reverse(A, a, a + k, slot, stack);
+  return reverse(A, sc, a, a + k, slot, stack, false);
 }
 
 int check_support(hc_ctx* c) {
@@ -366,13 +435,19 @@ int setup(Adj& A, hc_ctx* c, int nsteps, int nsnap, const hc_objective* obj) {
   return HC_OK;
 }
 
-// forward pass from the base state: J and (rates == nullptr) the max-rate history
-int forward_pass(Adj& A, const double* rates_in) {
+// forward pass from the base state: J and (rates == nullptr) the max-rate
+// history; the states at the positions of `stores` go to their snapshot slots
+int forward_pass(Adj& A, const double* rates_in, const std::vector<std::pair<int, int>>& stores = {}) {
   if (rates_in) HC_CUDA(cudaMemcpyAsync(A.rates, rates_in, A.nsteps * sizeof(double), cudaMemcpyHostToDevice, A.s()));
   if (int st = restore(A, -1)) return st;
+  size_t next = 0;
   for (int k = 0; k < A.nsteps; ++k) {
     if (int st = forward_step(A, k, rates_in == nullptr)) return st;
     swap_out(A);
+    while (next < stores.size() && stores[next].first == k + 1) {
+      if (int st = store(A, stores[next].second)) return st;
+      ++next;
+    }
     if (A.obj.kind == HC_OBJ_DRAG)
       if (int st = add_drag(A, A.sq[0], A.obj.scale / A.nsteps)) return st;
   }
@@ -424,8 +499,13 @@ int hc_adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective
   HC_CUDA(cudaEventCreate(&e0));
   HC_CUDA(cudaEventCreate(&e1));
   HC_CUDA(cudaEventCreate(&e2));
+  std::vector<int> stack;
+  for (int k = snapshots - 1; k >= 0; --k) stack.push_back(k);
+  Schedule sched;
+  sched.build(nsteps, snapshots);
+  const std::vector<std::pair<int, int>> stores = first_descent(sched, nsteps, snapshots, stack);
   cudaEventRecord(e0, A.s());
-  if (int st = forward_pass(A, rates_in)) return st;
+  if (int st = forward_pass(A, rates_in, stores)) return st;
   cudaEventRecord(e1, A.s());
   // adjoint of the final state
   if (A.obj.kind == HC_OBJ_DRAG) {
@@ -435,9 +515,7 @@ int hc_adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective
                                                A.obj.weight[2], A.obj.weight[3], nullptr, 1, A.lam);
     A.launches += 1;
   }
-  std::vector<int> stack;
-  for (int k = snapshots - 1; k >= 0; --k) stack.push_back(k);
-  if (int st = reverse(A, 0, nsteps, -1, stack)) return st;
+  if (int st = reverse(A, sched, 0, nsteps, -1, stack, true)) return st;
   cudaEventRecord(e2, A.s());
   HC_CUDA(cudaStreamSynchronize(A.s()));
   float ms_f = 0, ms_t = 0;

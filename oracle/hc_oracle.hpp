@@ -30,6 +30,18 @@
 
 namespace hco {
 
+// unqualified math calls: double resolves to <cmath>, other arithmetic types
+// (the forward-mode Dual of hc_dual.hpp) to their own overloads
+using std::abs;
+using std::fabs;
+using std::fmax;
+using std::fmin;
+using std::pow;
+using std::sqrt;
+
+// the per-step timestep is held fixed when differentiating (identity here)
+template <class R> R freeze(const R& x) { return x; }
+
 // ---------------------------------------------------------------- enums
 enum Flux { FLUX_ROE = 0, FLUX_SLAU = 1, FLUX_SLAU_REF = 2, FLUX_AUSMPUP = 3,
             FLUX_RUSANOV = 4, FLUX_CENTRAL = 5 };
@@ -72,7 +84,7 @@ template <class R> Face<R> surface(const R* p0, const R* p1) {
   const R t0x = p1[0] - p0[0], t0y = p1[1] - p0[1];
   const R t1x = p0[0] - p1[0], t1y = p0[1] - p1[1];
   R d = 0; d += t0x * t0x; d += t0y * t0y;
-  const R l = std::sqrt(d);
+  const R l = sqrt(d);
   const R l1 = 1. / l;
   s.area = l;
   s.c[0] = p0[0] + 0.5 * t0x;
@@ -101,7 +113,7 @@ template <class R> Cell<R> volume(const R* p0, const R* p1, const R* p2, const R
   for (int i = 0; i < 2; ++i)
     for (int j = 0; j < 2; ++j)
       for (int k = 0; k < 4; ++k) tg[i][j] += du[k][i] * p[k][j];
-  c.vol = std::fabs(tg[0][0] * tg[1][1] - tg[0][1] * tg[1][0]);
+  c.vol = fabs(tg[0][0] * tg[1][1] - tg[0][1] * tg[1][0]);
   return c;
 }
 
@@ -165,13 +177,13 @@ template <class R> R proj_vel(const R* n, const State<R>& s) {
 
 // spectralRadius (conservationLaws/euler/euler.h:161-166)
 template <class R> R spec_rad(const R* n, const State<R>& s) {
-  return std::abs(proj_vel(n, s)) + std::sqrt(s.a2);
+  return abs(proj_vel(n, s)) + sqrt(s.a2);
 }
 
 // wavespeeds (conservationLaws/euler/euler.h:168-181)
 template <class R> void wavespeeds(const R* n, const State<R>& s, R* w) {
   const R u = proj_vel(n, s);
-  const R a = std::sqrt(s.a2);
+  const R a = sqrt(s.a2);
   w[0] = u; w[1] = u - a; w[2] = u + a; w[3] = u;
 }
 
@@ -230,7 +242,7 @@ template <class R> void dprim2dcons(const Species<R>& sp, const State<R>& s, con
 // delta2Delta characteristic -> primitive (primitive.ipp:238-275)
 template <class R> void dchar2dprim(const Species<R>& sp, const State<R>& s, const R* dqw, R* dqp) {
   const R r = s.r;
-  const R a = std::sqrt(s.a2);
+  const R a = sqrt(s.a2);
   const R dp = 0.5 * r * a * (dqw[2] - dqw[1]);
   const R dr = dp / (a * a) - r * dqw[0] / sp.gamma;
   dqp[0] = 0.5 * (dqw[1] + dqw[2]);
@@ -241,7 +253,7 @@ template <class R> void dchar2dprim(const Species<R>& sp, const State<R>& s, con
 // delta2Delta primitive -> characteristic (primitive.ipp:277-313)
 template <class R> void dprim2dchar(const Species<R>& sp, const State<R>& s, const R* dqp, R* dqw) {
   const R r1 = 1. / s.r;
-  const R a1 = 1. / std::sqrt(s.a2);
+  const R a1 = 1. / sqrt(s.a2);
   const R du = dqp[0], dr = dqp[2], dp = dqp[3];
   dqw[0] = sp.gamma * (dp * a1 * a1 - dr) * r1;
   dqw[1] = du - dp * r1 * a1;
@@ -253,13 +265,13 @@ template <class R> void dprim2dchar(const Species<R>& sp, const State<R>& s, con
 // exactFlux (conservationLaws/euler/fluxes/exactFlux.ipp:231-263)
 template <class R> FluxRes<R> exact_flux(const R* n, const State<R>& s) {
   const R r = s.r, p = s.p, h = s.h;
-  const R a = std::sqrt(s.a2);
+  const R a = sqrt(s.a2);
   const R un = proj_vel(n, s);
   const R mn = r * un;
   FluxRes<R> fr;
   for (int i = 0; i < 2; ++i) fr.f[i] = mn * s.u[i] + p * n[i];
   fr.f[2] = mn; fr.f[3] = mn * h;
-  fr.lam = std::abs(un) + a;
+  fr.lam = abs(un) + a;
   return fr;
 }
 
@@ -275,7 +287,7 @@ template <class R> FluxRes<R> central_flux(const Face<R>& f, const State<R>& sl,
 // roeAverage (conservationLaws/euler/fluxes/roe.ipp:150-196)
 template <class R> State<R> roe_average(const Species<R>& sp, const State<R>& sl, const State<R>& sr) {
   State<R> a;
-  const R cr = std::sqrt(sr.r / sl.r);
+  const R cr = sqrt(sr.r / sl.r);
   const R wl = 1. / (1. + cr);
   const R wr = 1. - wl;
   const R ra = cr * sl.r;
@@ -296,13 +308,13 @@ template <class R> State<R> roe_average(const Species<R>& sp, const State<R>& sl
 
 // entropyfix, Harten eps=0.05 (conservationLaws/euler/fluxes/roe.ipp:198-226)
 template <class R> void entropy_fix(const R* la, const R* ll, const R* lr, R* sp) {
-  const R ua = std::fabs(la[0]);
+  const R ua = fabs(la[0]);
   sp[0] = ua; sp[3] = ua;
-  sp[1] = std::fabs(la[1]); sp[2] = std::fabs(la[2]);
+  sp[1] = fabs(la[1]); sp[2] = fabs(la[2]);
   constexpr R eps = 0.05;
   for (int i = 1; i < 3; ++i) {
-    const R le = eps * std::fmax((R)0., std::fmax(la[i] - ll[i], lr[i] - la[i]));
-    const R laa = std::fabs(la[i]);
+    const R le = eps * fmax((R)0., fmax(la[i] - ll[i], lr[i] - la[i]));
+    const R laa = fabs(la[i]);
     sp[i] = (laa > le) ? laa : (R)(0.5 * (le + laa * laa / le));
   }
 }
@@ -340,7 +352,7 @@ template <class R> FluxRes<R> roe_flux(const Species<R>& sp, const Face<R>& f,
   const FluxRes<R> d = roe_dissipation(sp, f, sl, sr);
   FluxRes<R> o;
   for (int i = 0; i < 4; ++i) o.f[i] = c.f[i] + d.f[i];
-  o.lam = std::fmax(c.lam, d.lam);
+  o.lam = fmax(c.lam, d.lam);
   return o;
 }
 
@@ -359,14 +371,14 @@ template <class R> FluxRes<R> rusanov_flux(const Species<R>& sp, const Face<R>& 
 }
 
 // Mach-number splittings (conservationLaws/euler/fluxes/machSplittings.ipp:163-204)
-template <class R> R msplit_m1(int s, R M) { return 0.5 * (M + s * std::fabs(M)); }
+template <class R> R msplit_m1(int s, R M) { return 0.5 * (M + s * fabs(M)); }
 template <class R> R msplit_m2(int s, R M) { return s * 0.25 * (M + s) * (M + s); }
 template <class R> R msplit_m4(int s, R M, R beta) {
   return msplit_m2(s, M) * (1. - s * 16. * beta * msplit_m2(-s, M));
 }
 template <class R> R msplit_p1(int s, R M) {
   constexpr R eps = std::numeric_limits<R>::max();
-  return (msplit_m1(s, M) + eps) / (std::fabs(M) + eps);
+  return (msplit_m1(s, M) + eps) / (fabs(M) + eps);
 }
 template <class R> R msplit_p3(int s, R M) { return msplit_m2(s, M) * (s * 2. - M); }
 template <class R> R msplit_p5(int s, R M, R alpha) {
@@ -380,24 +392,24 @@ template <class R> R msplit_p5(int s, R M, R alpha) {
 // upwind_by_mdot=true selects it by the sign of the interface mass flux.
 template <class R> FluxRes<R> slau_flux(const Species<R>& sp, const Face<R>& f,
                                         const State<R>& sl, const State<R>& sr, bool upwind_by_mdot) {
-  const R ua = std::sqrt(0.5 * (sl.u2 + sr.u2));
-  const R aa = 0.5 * (std::sqrt(sl.a2) + std::sqrt(sr.a2));
+  const R ua = sqrt(0.5 * (sl.u2 + sr.u2));
+  const R aa = 0.5 * (sqrt(sl.a2) + sqrt(sr.a2));
   const R aa1 = 1.0 / aa;
   const R ma = ua * aa1;
-  const R ma_hat = std::fmin((R)1.0, ma);
+  const R ma_hat = fmin((R)1.0, ma);
   const R unl = proj_vel(f.n, sl), unr = proj_vel(f.n, sr);
   const R ml = unl * aa1, mr = unr * aa1;
-  const R una = (sl.r * std::fabs(unl) + sr.r * std::fabs(unr)) / (sl.r + sr.r);
+  const R una = (sl.r * fabs(unl) + sr.r * fabs(unr)) / (sl.r + sr.r);
   const R chi = (1. - ma_hat) * (1. - ma_hat);
-  const R g = -std::fmax(std::fmin(ml, (R)0.), (R)-1.) * std::fmin(std::fmax(mr, (R)0.), (R)1.);
+  const R g = -fmax(fmin(ml, (R)0.), (R)-1.) * fmin(fmax(mr, (R)0.), (R)1.);
   const R dr = sr.r - sl.r;
   const R dp = sr.p - sl.p;
   const R mdot_c = sl.r * unl + sr.r * unr;
   const R mdot_dr = una * dr;
   const R mdot_dp = chi * dp * aa1;
   const R mdot = 0.5 * ((mdot_c - mdot_dr) * (1. - g) - mdot_dp) * f.area;
-  const unsigned mlsup = std::fabs(ml) > 1 ? 1 : 0, mlsub = 1 - mlsup;
-  const unsigned mrsup = std::fabs(mr) > 1 ? 1 : 0, mrsub = 1 - mrsup;
+  const unsigned mlsup = fabs(ml) > 1 ? 1 : 0, mlsub = 1 - mlsup;
+  const unsigned mrsup = fabs(mr) > 1 ? 1 : 0, mrsub = 1 - mrsup;
   const R betal = mlsub * msplit_p3(1, ml) + mlsup * msplit_p1(1, ml);
   const R betar = mrsub * msplit_p3(-1, mr) + mrsup * msplit_p1(-1, mr);
   const R p_c = sl.p + sr.p;
@@ -410,7 +422,7 @@ template <class R> FluxRes<R> slau_flux(const Species<R>& sp, const Face<R>& f,
   for (int i = 0; i < 2; ++i) o.f[i] = mdot * (m1l * sl.u[i] + m1r * sr.u[i]) + pa * f.n[i];
   o.f[2] = mdot;
   o.f[3] = mdot * (m1l * sl.h + m1r * sr.h);
-  const R lmax = std::sqrt(std::fmax(sl.a2, sr.a2)) + std::fmax(std::fabs(unl), std::fabs(unr));
+  const R lmax = sqrt(fmax(sl.a2, sr.a2)) + fmax(fabs(unl), fabs(unr));
   o.lam = lmax * f.area;
   return o;
 }
@@ -423,23 +435,23 @@ template <class R> FluxRes<R> ausmpup_flux(const Species<R>& sp, const Face<R>& 
   const R ascoeff = 2. * (sp.gamma - 1.) / (sp.gamma + 1.);
   const R unl = proj_vel(f.n, sl), unr = proj_vel(f.n, sr);
   const R als2 = ascoeff * sl.h, ars2 = ascoeff * sr.h;
-  const R als = als2 / std::fmax(unl, std::sqrt(als2));
-  const R ars = ars2 / std::fmax(-unr, std::sqrt(ars2));
+  const R als = als2 / fmax(unl, sqrt(als2));
+  const R ars = ars2 / fmax(-unr, sqrt(ars2));
   const R ra = 0.5 * (sl.r + sr.r);
-  const R as = std::fmin(ars, als);
+  const R as = fmin(ars, als);
   const R ml = unl / as, mr = unr / as;
   const R minf = sp.minf;
-  const R m0 = std::sqrt(0.5 * (ml * ml + mr * mr));
+  const R m0 = sqrt(0.5 * (ml * ml + mr * mr));
   const R m0_c = std::clamp<R>(m0, minf, 1.);
   const R m0_p = m0_c, m0_u = m0_c;
   const R fa_p = m0_p * (2. - m0_p);
   const R fa_u = m0_u * (2. - m0_u);
-  const unsigned mlsup = std::fabs(ml) > 1 ? 1 : 0, mlsub = 1 - mlsup;
-  const unsigned mrsup = std::fabs(mr) > 1 ? 1 : 0, mrsub = 1 - mrsup;
+  const unsigned mlsup = fabs(ml) > 1 ? 1 : 0, mlsub = 1 - mlsup;
+  const unsigned mrsup = fabs(mr) > 1 ? 1 : 0, mrsub = 1 - mrsup;
   const R mlp = mlsub * msplit_m4(1, ml, beta) + mlsup * msplit_m1(1, ml);
   const R mrm = mrsub * msplit_m4(-1, mr, beta) + mrsup * msplit_m1(-1, mr);
   const R delp = sr.p - sl.p;
-  const R mp = Kp * std::fmax(1. - sigma * m0 * m0, (R)0.) * delp / (fa_p * ra * as * as);
+  const R mp = Kp * fmax(1. - sigma * m0 * m0, (R)0.) * delp / (fa_p * ra * as * as);
   const R uaf = as * (mlp + mrm - mp) * f.area;
   const R alpha = alpha0 * (5. * fa_u * fa_u - 4.);
   const R plp = mlsub * msplit_p5(1, ml, alpha) + mlsup * msplit_p1(1, ml);
@@ -454,8 +466,8 @@ template <class R> FluxRes<R> ausmpup_flux(const Species<R>& sp, const Face<R>& 
   o.f[2] = mdot;
   o.f[3] = mdot * (m1l * sl.h + m1r * sr.h);
   const R lmd = 0.5 * (m0_p + 1) / fa_p;
-  const R amax = std::sqrt(std::fmax(as * as, std::fmax(sl.a2, sr.a2)));
-  const R lmax = lmd * amax + std::fmax(std::fabs(uaf), std::fmax(std::fabs(unl), std::fabs(unr)));
+  const R amax = sqrt(fmax(as * as, fmax(sl.a2, sr.a2)));
+  const R lmax = lmd * amax + fmax(fabs(uaf), fmax(fabs(unl), fabs(unr)));
   o.lam = lmax * f.area;
   return o;
 }
@@ -486,27 +498,27 @@ template <class R> R limit(int kind, R a, R b) {
       return a * b < 0 ? (R)0 : (b * (a * a) + a * (b * b)) / (a * a + b * b + eps);
     }
     case LIM_MINMOD:
-      return a > 0 ? (R)std::fmin(a, (R)std::fmax(b, (R)0.)) : (R)std::fmax(a, (R)std::fmin(b, (R)0.));
+      return a > 0 ? (R)fmin(a, (R)fmax(b, (R)0.)) : (R)fmax(a, (R)fmin(b, (R)0.));
     case LIM_SUPERBEE:
-      return a > 0 ? (R)std::fmax((R)0., std::fmax(std::fmin(2 * a, b), std::fmin(2 * b, a)))
-                   : (R)std::fmin((R)0., std::fmin(std::fmax(2 * a, b), std::fmax(2 * b, a)));
+      return a > 0 ? (R)fmax((R)0., fmax(fmin(2 * a, b), fmin(2 * b, a)))
+                   : (R)fmin((R)0., fmin(fmax(2 * a, b), fmax(2 * b, a)));
     case LIM_MC:
-      return a > 0 ? (R)std::fmax((R)0., std::fmin((R)(0.5 * (a + b)), std::fmin(2 * b, 2 * a)))
-                   : (R)std::fmin((R)0., std::fmax((R)(0.5 * (a + b)), std::fmax(2 * b, 2 * a)));
+      return a > 0 ? (R)fmax((R)0., fmin((R)(0.5 * (a + b)), fmin(2 * b, 2 * a)))
+                   : (R)fmin((R)0., fmax((R)(0.5 * (a + b)), fmax(2 * b, 2 * a)));
     case LIM_VANLEER: {
       const R eps = std::numeric_limits<R>::min();
-      return (a * std::fabs(b) + std::fabs(a) * b) / (std::fabs(a) + std::fabs(b) + eps);
+      return (a * fabs(b) + fabs(a) * b) / (fabs(a) + fabs(b) + eps);
     }
     case LIM_VANLEER_REF: {
       const R eps = std::numeric_limits<R>::min();
-      return (b + std::fabs(b)) / (a + std::fabs(b) + eps);
+      return (b + fabs(b)) / (a + fabs(b) + eps);
     }
     case LIM_CADA3: {
       const R t = 0.0, gam = 1.5, c1 = -2. / 7., c2 = 0.4, c3 = 3 * gam - 2;
       R u, v, w, p, q;
       if (a > 0) { u = a; v = b; } else { u = -a; v = -b; }
       p = (v + 2. * u) / 3.;
-      q = std::fabs(a) + std::fabs(b);
+      q = fabs(a) + fabs(b);
       if (q > t) {
         if (v < -2 * u) w = 0;
         else if (v < c1 * u) w = (v + 2. * u) / 3.;
@@ -577,13 +589,13 @@ template <class R> void bc_riemann(const Species<R>& sp, const Face<R>& f, const
   R ri[4], rf[4];
   rotate_to(f, qi, ri); rotate_to(f, qf, rf);
   const State<R> sA = roe_average(sp, prim2state(sp, ri), prim2state(sp, rf));
-  if ((sA.u[0] / std::sqrt(sA.u2)) < 0.001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; return; }
-  const R ma = sA.u[0] / std::sqrt(sA.a2);
+  if ((sA.u[0] / sqrt(sA.u2)) < 0.001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; return; }
+  const R ma = sA.u[0] / sqrt(sA.a2);
   const bool inflow = ma > 0;
   const R* quw = inflow ? qf : qi;
-  if (std::abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; return; }
+  if (abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; return; }
   const State<R> sI = prim2state(sp, ri), sF = prim2state(sp, rf);
-  const R ai = std::sqrt(sI.a2), af = std::sqrt(sF.a2);
+  const R ai = sqrt(sI.a2), af = sqrt(sF.a2);
   const R uni = sI.u[0], unf = sF.u[0];
   const R rim = uni - 2. * ai * gam1;
   const R rip = unf + 2. * af * gam1;
@@ -592,9 +604,9 @@ template <class R> void bc_riemann(const Species<R>& sp, const Face<R>& f, const
   R ru[4];
   rotate_to(f, quw, ru);
   const State<R> sU = prim2state(sp, ru);
-  const R sb = sU.a2 / (gam * std::pow(sU.r, gam - 1.));
+  const R sb = sU.a2 / (gam * pow(sU.r, gam - 1.));
   const R vb = sU.u[1];
-  const R rb = std::pow(ab * ab / (gam * sb), gam1);
+  const R rb = pow(ab * ab / (gam * sb), gam1);
   const R pb = rb * ab * ab / gam;
   const R qbr[4] = {ub, vb, rb, pb};
   rotate_from(f, qbr, qb);
@@ -605,18 +617,18 @@ template <class R> void bc_entropy(const Species<R>& sp, const Face<R>& f, const
   R ri[4], rf[4];
   rotate_to(f, qi, ri); rotate_to(f, qf, rf);
   const State<R> sA = roe_average(sp, prim2state(sp, ri), prim2state(sp, rf));
-  if ((sA.u[0] / std::sqrt(sA.u2)) < 0.0001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; return; }
-  const R ma = sA.u[0] / std::sqrt(sA.a2);
+  if ((sA.u[0] / sqrt(sA.u2)) < 0.0001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; return; }
+  const R ma = sA.u[0] / sqrt(sA.a2);
   const bool inflow = ma > 0;
   const R* quw = inflow ? qf : qi;
   const R* qdw = inflow ? qi : qf;
-  if (std::abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; return; }
+  if (abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; return; }
   R ru[4], rd[4];
   rotate_to(f, quw, ru); rotate_to(f, qdw, rd);
   const State<R> sU = prim2state(sp, ru), sD = prim2state(sp, rd);
   const R pb = sD.p;
-  const R sb = sU.a2 / (gam * std::pow(sU.r, gam - 1.));
-  const R rb = std::pow(pb / sb, 1. / gam);
+  const R sb = sU.a2 / (gam * pow(sU.r, gam - 1.));
+  const R rb = pow(pb / sb, 1. / gam);
   const R qbr[4] = {sU.u[0], sU.u[1], rb, pb};
   rotate_from(f, qbr, qb);
 }

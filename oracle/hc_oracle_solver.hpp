@@ -207,9 +207,9 @@ template <class R> struct Solver {
     for (int v = 0; v < 4; ++v) dqc[v] = qr[v] - ql[v];
     R d;
     d = 0; d += (f.c[0] - cl[0]) * (f.c[0] - cl[0]); d += (f.c[1] - cl[1]) * (f.c[1] - cl[1]);
-    const R dl = std::sqrt(d);
+    const R dl = sqrt(d);
     d = 0; d += (cr[0] - f.c[0]) * (cr[0] - f.c[0]); d += (cr[1] - f.c[1]) * (cr[1] - f.c[1]);
-    const R dr = std::sqrt(d);
+    const R dr = sqrt(d);
     const R idlr = 1. / (dl + dr);
     R gc[4];
     for (int v = 0; v < 4; ++v) gc[v] = dqc[v] * idlr;
@@ -242,7 +242,7 @@ template <class R> struct Solver {
     if (lim == LIM_NOLIMIT1) return face_flux(flux, sp, f, prim2state(sp, ql), prim2state(sp, qr));
     const R* cc = cells[c].c;
     R d = 0; d += (f.c[0] - cc[0]) * (f.c[0] - cc[0]); d += (f.c[1] - cc[1]) * (f.c[1] - cc[1]);
-    const R dd = std::sqrt(d);
+    const R dd = sqrt(d);
     R dqc[4];
     for (int v = 0; v < 4; ++v) dqc[v] = qr[v] - ql[v];
     const R idlr = 1. / (dd + dd);
@@ -348,8 +348,8 @@ template <class R> struct Solver {
       for (int s = 0; s < tab.nstages; ++s) {
         residual(q1, res[s]);
         if (s == 0) {
-          if (dtmode == DT_GLOBAL) dt = cfl / spectral_radius(res[0]);
-          else for (size_t c = 0; c < n; ++c) lam0[c] = res[0][c].lam;
+          if (dtmode == DT_GLOBAL) dt = freeze(cfl / spectral_radius(res[0]));
+          else for (size_t c = 0; c < n; ++c) lam0[c] = freeze(res[0][c].lam);
         }
 #pragma omp parallel for schedule(static)
         for (long c = 0; c < (long)n; ++c) {

@@ -232,3 +232,62 @@ class OracleSolver:
         out = np.empty((3, self.ni, self.nj))
         self.lib.hco_cells(self.h, out)
         return out
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _sides(arrs, ni, nj):
+    """Per-side 4-plane arrays (None for unused sides) as a C array of pointers."""
+    keep, ptrs = [], (C.c_void_p * 4)()
+    for side in range(4):
+        a = None if arrs is None else arrs[side]
+        if a is None:
+            ptrs[side] = None
+            continue
+        nf = nj if side < 2 else ni
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64).reshape(4, -1), (4, nf)))
+        keep.append(a)
+        ptrs[side] = a.ctypes.data
+    return ptrs, keep
+
+
+def objective(mesh_nodes, ni, nj, bc, q0, nsteps, kind="drag", flux="roe", limiter="vanalbada", rk="ssp34",
+              cfl=0.5, species=(1.4, 287.058, 0.4), ref=None, scale=1.0, direction=(1.0, 0.0), target=None,
+              weight=(1.0, 1.0, 1.0, 1.0), dq0=None, dref=None, freeze_dt=True):
+    """J of an RK run of the oracle with the global timestep (drag: scale/N times the
+    wall force along `direction` summed over steps 1..N; l2: weighted squared distance
+    of the final primitive state from `target`).  With a direction (dq0 and/or dref)
+    also returns the exact derivative of J along it (forward-mode dual numbers
+    through the same oracle code), with the timesteps frozen at their values (the
+    discrete adjoint's convention) unless freeze_dt is False.  Returns (J, dJ or None)."""
+    lib = load(False)
+    if not getattr(lib, "_obj_declared", False):
+        v, i, d = C.c_void_p, C.c_int, C.c_double
+        lib.hco_objective.argtypes = [i, i, v, v, i, i, i, d, v, v, v, i, i, d, d, d, v, v, v]
+        lib.hco_objective_jvp.argtypes = [i, i, v, v, i, i, i, d, v, v, v, v, v, i, i, d, d, d, v, v, i, v]
+        lib._obj_declared = True
+    nodes = np.ascontiguousarray(mesh_nodes, dtype=np.float64)
+    bcv = np.array([BC[b] if isinstance(b, str) else int(b) for b in bc], dtype=np.int32)
+    sp = np.asarray(species, dtype=np.float64)
+    q = np.ascontiguousarray(q0, dtype=np.float64)
+    refp, keep_r = _sides(ref, ni, nj)
+    tgt = None if target is None else np.ascontiguousarray(target, dtype=np.float64)
+    w = np.asarray(weight, dtype=np.float64)
+    out = np.zeros(2)
+    fl = FLUX[flux] if isinstance(flux, str) else flux
+    lm = LIMITER[limiter] if isinstance(limiter, str) else limiter
+    r = RK[rk] if isinstance(rk, str) else rk
+    k = {"drag": 0, "l2": 1}[kind]
+    if dq0 is None and dref is None:
+        lib.hco_objective(ni, nj, _ptr(nodes), _ptr(bcv), fl, lm, r, float(cfl), _ptr(sp), refp, _ptr(q),
+                          int(nsteps), k, float(scale), float(direction[0]), float(direction[1]), _ptr(tgt),
+                          _ptr(w), _ptr(out))
+        return float(out[0]), None
+    dq = None if dq0 is None else np.ascontiguousarray(dq0, dtype=np.float64)
+    drefp, keep_d = _sides(dref, ni, nj)
+    lib.hco_objective_jvp(ni, nj, _ptr(nodes), _ptr(bcv), fl, lm, r, float(cfl), _ptr(sp), refp, drefp, _ptr(q),
+                          _ptr(dq), int(nsteps), k, float(scale), float(direction[0]), float(direction[1]),
+                          _ptr(tgt), _ptr(w), 1 if freeze_dt else 0, _ptr(out))
+    return float(out[0]), float(out[1])
