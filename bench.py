@@ -205,18 +205,14 @@ def measure_precision(stream, steps: int, prec: str):
     return out
 
 
-def measure_batched(stream, ninst: int = 256, steps: int = 3, seed: int = 2026):
-    """The uneven batch: 256 four-quadrant Riemann instances, Ni, Nj from {64,96,...,1024},
-    SLAU + van Albada, ssp34, global dt per instance, FP32.  Persistent batched launches
-    replayed from a CUDA graph against plain per-instance launches."""
+def _time_batch(stream, insts, steps, precision="fp32"):
     import torch
-    from hyperboliconvergence_gb300.batch import Batch, uneven_riemann_batch
-    insts = uneven_riemann_batch(ninst, seed)
-    b = Batch(insts, flux="slau", limiter="vanalbada", rk="ssp34", precision="fp32", dt="global", cfl=0.5,
+    from hyperboliconvergence_gb300.batch import Batch
+    b = Batch(insts, flux="slau", limiter="vanalbada", rk="ssp34", precision=precision, dt="global", cfl=0.5,
               stream=stream.cuda_stream)
     cells = b.cells
     tuned = b.autotune(steps=1)
-    res = {"instances": ninst, "cells": cells, "schedule": tuned}
+    res = {"instances": len(insts), "cells": cells, "schedule": tuned}
     b.capture(steps)
     b.replay()
     b.sync()
@@ -234,6 +230,19 @@ def measure_batched(stream, ninst: int = 256, steps: int = 3, seed: int = 2026):
         res[mode] = {"ms_per_step": ms, "value": cells / (ms / 1e3), "unit": UNIT}
     res["batched_over_per_instance"] = res["per_instance"]["ms_per_step"] / res["graph"]["ms_per_step"]
     b.close()
+    return res
+
+
+def measure_batched(stream, ninst: int = 256, steps: int = 3, seed: int = 2026):
+    """The uneven batch: 256 four-quadrant Riemann instances, Ni, Nj from {64,96,...,1024},
+    SLAU + van Albada, ssp34, global dt per instance, FP32.  Persistent batched launches
+    replayed from a CUDA graph against plain per-instance launches.  Beside it, a
+    launch-bound batch of 1024 small instances (Ni, Nj from {16,32,...,128}), where
+    per-instance launches cannot fill the GPU."""
+    from hyperboliconvergence_gb300.batch import uneven_riemann_batch
+    res = _time_batch(stream, uneven_riemann_batch(ninst, seed), steps)
+    res["small_instances"] = _time_batch(stream, uneven_riemann_batch(1024, seed, sizes=tuple(range(16, 129, 16))),
+                                         steps)
     return res
 
 

@@ -195,8 +195,13 @@ int residual_adjoint(Adj& A, const double* q, const double* rbar, const double* 
   a.obj_dirx = A.obj.dir[0];
   a.obj_diry = A.obj.dir[1];
   adj_qm_kernel<double><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
-  adj_face_kernel<double, FK><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
-  adj_face_kernel<double, FK><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+  if (A.c->df) {  // double-float face arithmetic on HC_FP64_DF contexts
+    adj_face_kernel<double, FK, df64><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
+    adj_face_kernel<double, FK, df64><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+  } else {
+    adj_face_kernel<double, FK><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
+    adj_face_kernel<double, FK><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+  }
   adj_qmbar_kernel<double><<<blocks(A.n), 256, 0, A.s()>>>(a);
   adj_gather_kernel<double><<<blocks(A.n), 256, 0, A.s()>>>(a);
   A.launches += 5;

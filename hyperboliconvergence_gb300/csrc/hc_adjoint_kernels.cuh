@@ -97,7 +97,9 @@ __device__ __forceinline__ void flux_adj(const Gas<R>& g, R nx, R ny, R A, const
 }
 
 // pass 1: one thread per face of direction dir (0 = i-faces, 1 = j-faces)
-template <class R, int FK> __global__ void adj_face_kernel(const AdjArgs<R> a, int dir) {
+// C: the type the face's reconstruction, flux and their reverse are computed in
+// (R, or double-float for FP64 storage); loads and stores stay in R.
+template <class R, int FK, class C = R> __global__ void adj_face_kernel(const AdjArgs<R> a, int dir) {
   const int ni = a.ni, nj = a.nj;
   const size_t n = size_t(ni) * nj;
   const bool idir = dir == 0;
@@ -108,16 +110,16 @@ template <class R, int FK> __global__ void adj_face_kernel(const AdjArgs<R> a, i
   if (idir) { i = f / nj; j = f % nj; } else { i = f / (nj + 1); j = f % (nj + 1); }
   const R* rec = idir ? a.fi : a.fj;
   R* out = idir ? a.ai : a.aj;
-  auto rd = [&](int fld) -> R { return rec[size_t(fld) * nf + f]; };
-  const R nx = rd(F_NX), ny = rd(F_NY), A = rd(F_A);
+  auto rd = [&](int fld) -> C { return rec[size_t(fld) * nf + f]; };
+  const C nx = rd(F_NX), ny = rd(F_NY), A = rd(F_A);
   const int lo = idir ? i : j, nalong = idir ? ni : nj;
   const int side = idir ? (lo == 0 ? 0 : 1) : (lo == 0 ? 2 : 3);
   const bool bnd = (lo == 0 || lo == nalong) && a.bc[side] != BC_PERIODIC;
-  R res[ADJ_FIELDS];
+  C res[ADJ_FIELDS];
 #pragma unroll
-  for (int k = 0; k < ADJ_FIELDS; ++k) res[k] = R(0);
-  R* dL = res; R* dR = res + 4; R* gL = res + 8; R* gR = res + 12;
-  const Gas<R> g = a.gas;
+  for (int k = 0; k < ADJ_FIELDS; ++k) res[k] = C(0);
+  C* dL = res; C* dR = res + 4; C* gL = res + 8; C* gR = res + 12;
+  const Gas<C> g = gas_as<C>(a.gas);
   const int lim = a.limiter;
   if (!bnd) {
     if (!a.objective) {
@@ -125,7 +127,7 @@ template <class R, int FK> __global__ void adj_face_kernel(const AdjArgs<R> a, i
       int cl, cr;
       if (idir) { cl = wrapi(i - 1, ni) * nj + j; cr = wrapi(i, ni) * nj + j; }
       else { cl = i * nj + wrapi(j - 1, nj); cr = i * nj + wrapi(j, nj); }
-      R Fb[4], ql[4], qr[4];
+      C Fb[4], ql[4], qr[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         Fb[v] = a.rbar[v * n + cr] - a.rbar[v * n + cl];
@@ -133,35 +135,35 @@ template <class R, int FK> __global__ void adj_face_kernel(const AdjArgs<R> a, i
         qr[v] = a.q[v * n + cr];
       }
       if (lim == LIM_NOLIMIT1) {
-        flux_adj<R, FK>(g, nx, ny, A, ql, qr, Fb, dL, dR);
+        flux_adj<C, FK>(g, nx, ny, A, ql, qr, Fb, dL, dR);
       } else {
-        const R dl = rd(F_DL), dr = rd(F_DR), idlr = rd(F_IDLR);
-        const R wlx = rd(F_WLX), wly = rd(F_WLY), sl = rd(F_SL);
-        const R wrx = rd(F_WRX), wry = rd(F_WRY), sr = rd(F_SR);
-        R qL[4], qR[4], gc[4], gl[4], gr[4];
+        const C dl = rd(F_DL), dr = rd(F_DR), idlr = rd(F_IDLR);
+        const C wlx = rd(F_WLX), wly = rd(F_WLY), sl = rd(F_SL);
+        const C wrx = rd(F_WRX), wry = rd(F_WRY), sr = rd(F_SR);
+        C qL[4], qR[4], gc[4], gl[4], gr[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-          const R dq = qr[v] - ql[v];
+          const C dq = qr[v] - ql[v];
           gc[v] = dq * idlr;
           gl[v] = (a.qm[(2 * v) * n + cl] * wlx + a.qm[(2 * v + 1) * n + cl] * wly) - dq * sl;
           gr[v] = (a.qm[(2 * v) * n + cr] * wrx + a.qm[(2 * v + 1) * n + cr] * wry) - dq * sr;
-          qL[v] = ql[v] + dl * limit<R>(lim, gc[v], gl[v]);
-          qR[v] = qr[v] - dr * limit<R>(lim, gc[v], gr[v]);
+          qL[v] = ql[v] + dl * limit<C>(lim, gc[v], gl[v]);
+          qR[v] = qr[v] - dr * limit<C>(lim, gc[v], gr[v]);
         }
-        R qLb[4] = {R(0), R(0), R(0), R(0)}, qRb[4] = {R(0), R(0), R(0), R(0)};
-        flux_adj<R, FK>(g, nx, ny, A, qL, qR, Fb, qLb, qRb);
+        C qLb[4] = {C(0), C(0), C(0), C(0)}, qRb[4] = {C(0), C(0), C(0), C(0)};
+        flux_adj<C, FK>(g, nx, ny, A, qL, qR, Fb, qLb, qRb);
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-          R da, db;
-          limit_grad<R>(lim, gc[v], gl[v], &da, &db);
-          const R zlb = dl * qLb[v];
-          R gcb = zlb * da;
-          const R glb = zlb * db;
-          limit_grad<R>(lim, gc[v], gr[v], &da, &db);
-          const R zrb = -dr * qRb[v];
+          C da, db;
+          limit_grad<C>(lim, gc[v], gl[v], &da, &db);
+          const C zlb = dl * qLb[v];
+          C gcb = zlb * da;
+          const C glb = zlb * db;
+          limit_grad<C>(lim, gc[v], gr[v], &da, &db);
+          const C zrb = -dr * qRb[v];
           gcb += zrb * da;
-          const R grb = zrb * db;
-          const R dqb = gcb * idlr - glb * sl - grb * sr;
+          const C grb = zrb * db;
+          const C dqb = gcb * idlr - glb * sl - grb * sr;
           dL[v] = qLb[v] - dqb;
           dR[v] = qRb[v] + dqb;
           gL[v] = glb;
@@ -175,77 +177,77 @@ template <class R, int FK> __global__ void adj_face_kernel(const AdjArgs<R> a, i
     const int kf = idir ? j : i;
     const int nfs = idir ? nj : ni;
     const int bct = a.bc[side];
-    R qi[4];
+    C qi[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) qi[v] = a.q[v * n + ci];
-    R* dI = int_right ? dR : dL;
-    R* gI = int_right ? gR : gL;
+    C* dI = int_right ? dR : dL;
+    C* gI = int_right ? gR : gL;
     if (bct == BC_WALL) {
-      R Fb[4];
+      C Fb[4];
       if (a.objective) {
-        const R sgn_in = int_right ? R(1) : R(-1);
-        Fb[0] = -sgn_in * a.obj_scale * a.obj_dirx;
-        Fb[1] = -sgn_in * a.obj_scale * a.obj_diry;
+        const C sgn_in = int_right ? C(1) : C(-1);
+        Fb[0] = -sgn_in * C(a.obj_scale) * C(a.obj_dirx);
+        Fb[1] = -sgn_in * C(a.obj_scale) * C(a.obj_diry);
       } else {
 #pragma unroll
         for (int v = 0; v < 2; ++v) Fb[v] = int_right ? a.rbar[v * n + ci] : -a.rbar[v * n + ci];
       }
-      const R wx = int_right ? rd(F_WLX) : rd(F_WRX), wy = int_right ? rd(F_WLY) : rd(F_WRY);
+      const C wx = int_right ? rd(F_WLX) : rd(F_WRX), wy = int_right ? rd(F_WLY) : rd(F_WRY);
       (void)wx; (void)wy;
-      const R pb = A * (nx * Fb[0] + ny * Fb[1]);
+      const C pb = A * (nx * Fb[0] + ny * Fb[1]);
       dI[3] += pb;
       gI[3] = -pb;  // pass 2 pairs it with the wall extrapolation weights
     } else if (!a.objective) {
-      R Fb[4], qg[4];
+      C Fb[4], qg[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         Fb[v] = int_right ? a.rbar[v * n + ci] : -a.rbar[v * n + ci];
         qg[v] = a.gref[side][size_t(v) * nfs + kf];  // fixed ghost = reference state
       }
-      R qLb[4] = {R(0), R(0), R(0), R(0)}, qRb[4] = {R(0), R(0), R(0), R(0)};
-      R gb_ref[4] = {R(0), R(0), R(0), R(0)};
+      C qLb[4] = {C(0), C(0), C(0), C(0)}, qRb[4] = {C(0), C(0), C(0), C(0)};
+      C gb_ref[4] = {C(0), C(0), C(0), C(0)};
       if (lim == LIM_NOLIMIT1) {
-        if (int_right) { flux_adj<R, FK>(g, nx, ny, A, qg, qi, Fb, qLb, qRb); }
-        else { flux_adj<R, FK>(g, nx, ny, A, qi, qg, Fb, qLb, qRb); }
+        if (int_right) { flux_adj<C, FK>(g, nx, ny, A, qg, qi, Fb, qLb, qRb); }
+        else { flux_adj<C, FK>(g, nx, ny, A, qi, qg, Fb, qLb, qRb); }
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
           dI[v] += int_right ? qRb[v] : qLb[v];
           gb_ref[v] = int_right ? qLb[v] : qRb[v];
         }
       } else {
-        const R d = rd(F_DL), idlr = rd(F_IDLR);
-        const R wx = int_right ? rd(F_WRX) : rd(F_WLX), wy = int_right ? rd(F_WRY) : rd(F_WLY);
-        R qL[4], qR[4], gc[4], gbv[4];
+        const C d = rd(F_DL), idlr = rd(F_IDLR);
+        const C wx = int_right ? rd(F_WRX) : rd(F_WLX), wy = int_right ? rd(F_WRY) : rd(F_WLY);
+        C qL[4], qR[4], gc[4], gbv[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-          const R dq = int_right ? (qi[v] - qg[v]) : (qg[v] - qi[v]);
+          const C dq = int_right ? (qi[v] - qg[v]) : (qg[v] - qi[v]);
           gc[v] = dq * idlr;
           gbv[v] = a.qm[(2 * v) * n + ci] * wx + a.qm[(2 * v + 1) * n + ci] * wy;
-          const R s = limit<R>(lim, gc[v], gbv[v]);
+          const C s = limit<C>(lim, gc[v], gbv[v]);
           if (int_right) { qL[v] = qg[v]; qR[v] = qi[v] - d * s; }
           else { qL[v] = qi[v] + d * s; qR[v] = qg[v]; }
         }
-        flux_adj<R, FK>(g, nx, ny, A, qL, qR, Fb, qLb, qRb);
+        flux_adj<C, FK>(g, nx, ny, A, qL, qR, Fb, qLb, qRb);
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-          R da, db;
-          limit_grad<R>(lim, gc[v], gbv[v], &da, &db);
-          const R zb = int_right ? -d * qRb[v] : d * qLb[v];
-          const R gcb = zb * da;
+          C da, db;
+          limit_grad<C>(lim, gc[v], gbv[v], &da, &db);
+          const C zb = int_right ? -d * qRb[v] : d * qLb[v];
+          const C gcb = zb * da;
           gI[v] = zb * db;
-          const R dqb = gcb * idlr;
+          const C dqb = gcb * idlr;
           if (int_right) { dI[v] += qRb[v] + dqb; gb_ref[v] = qLb[v] - dqb; }
           else { dI[v] += qLb[v] - dqb; gb_ref[v] = qRb[v] + dqb; }
         }
       }
       if (bct == BC_FIXED) {
 #pragma unroll
-        for (int v = 0; v < 4; ++v) a.refbar[side][size_t(v) * nfs + kf] += gb_ref[v];
+        for (int v = 0; v < 4; ++v) a.refbar[side][size_t(v) * nfs + kf] += cvt<R>(gb_ref[v]);
       }
     }
   }
 #pragma unroll
-  for (int k = 0; k < ADJ_FIELDS; ++k) out[size_t(k) * nf + f] = res[k];
+  for (int k = 0; k < ADJ_FIELDS; ++k) out[size_t(k) * nf + f] = cvt<R>(res[k]);
 }
 
 // pass 2: qmetric adjoint per cell
