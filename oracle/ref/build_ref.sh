@@ -34,3 +34,6 @@ grep -q 'norm( const Direction<nDim,Real>& d );' "$OUT/overlay/geometry/geometry
 ${CXX:-g++} -std=c++2a -fconcepts-ts -O2 -ffp-contract=off -fno-fast-math -fPIC -shared \
     -w -I"$OUT/overlay" -I"$INC" -o "$OUT/libhcref.so" "$HERE/ref_probe.cpp"
 echo "built $OUT/libhcref.so"
+${CXX:-g++} -std=c++2a -fconcepts-ts -O2 -ffp-contract=off -fno-fast-math -fPIC -shared \
+    -w -I"$OUT/overlay" -I"$INC" -o "$OUT/libhcref_scalar.so" "$HERE/ref_probe_scalar.cpp"
+echo "built $OUT/libhcref_scalar.so"

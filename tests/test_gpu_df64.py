@@ -60,17 +60,25 @@ def test_df_vortex_ten_steps_each_step_parity():
         assert err <= TOL64, err
 
 
-def test_df_adjoint_matches_fp64():
-    """Adjoint on a double-float context (forward and recomputed steps in
-    double-float, reverse sweep in FP64) against the FP64 context's gradient."""
-    mesh, bc, ref, q, sp = CASES["vortex"]
+@pytest.mark.parametrize("flux,limiter", [("roe", "nolimit2"), ("rusanov", "nolimit3")])
+def test_df_adjoint_matches_fp64(flux, limiter):
+    """Adjoint on a double-float context (forward, replayed and recomputed steps and
+    the face reverse in double-float, other reverse passes in FP64) against the
+    FP64 context's gradient, for smooth reconstructions.  (With a limiter, faces
+    whose arguments sit at round-off level -- zero crossings, exactly uniform
+    regions -- can take different branches in the two precisions, and the
+    gradient at those cells differs by up to ~1%.)"""
+    from test_gpu_adjoint import cylinder_case, make
+    case = cylinder_case(nr=12, nth=32, seed=5)
     out = {}
     for prec in ("fp64", "fp64_df"):
-        s = Solver(mesh, bc, ref, flux="roe", limiter="vanalbada", rk="ssp34", precision=prec, dt="global",
-                   species=sp)
+        mesh, bc, ref, q = case
+        s = Solver(mesh, bc, ref, flux=flux, limiter=limiter, rk="ssp34", precision=prec, dt="global", cfl=0.5,
+                   species=(1.4, 287.058, 0.4))
         s.set_state(q)
-        J, g, refb, rates, st = s.gradient(6, snapshots=2, kind="l2", target=q * 0.98, weight=(1, 1, 1, 1))
-        out[prec] = (J, g)
-    (ja, ga), (jb, gb) = out["fp64"], out["fp64_df"]
-    assert abs(jb - ja) <= 1e-11 * abs(ja)
+        J, g, refb, rates, st = s.gradient(8, snapshots=2, kind="drag", scale=2.0)
+        out[prec] = (J, g, refb[1])
+    (ja, ga, ra), (jb, gb, rb) = out["fp64"], out["fp64_df"]
+    assert abs(jb - ja) <= 1e-12 * abs(ja)
     assert np.abs(gb - ga).max() <= 1e-9 * np.abs(ga).max()
+    assert np.abs(rb - ra).max() <= 1e-9 * np.abs(ra).max()
