@@ -23,6 +23,7 @@ RK = {"ssp11": 0, "ssp22": 1, "ssp33": 2, "ssp34": 3}
 PRECISION = {"fp64": 0, "fp32": 1, "fp64_df": 2}
 DTMODE = {"global": 0, "local": 1}
 BC = {"periodic": 0, "fixed": 1, "riemann": 2, "entropy": 3, "wall": 4}
+LAW = {"euler": 0, "scalar": 1}
 
 
 class HCError(RuntimeError):
@@ -33,7 +34,7 @@ class HCError(RuntimeError):
 
 class Config(C.Structure):
     _fields_ = [("flux", C.c_int), ("limiter", C.c_int), ("rk", C.c_int), ("precision", C.c_int),
-                ("dt_mode", C.c_int), ("cfl", C.c_double)]
+                ("dt_mode", C.c_int), ("cfl", C.c_double), ("law", C.c_int)]
 
 
 class StepStats(C.Structure):

@@ -383,6 +383,7 @@ int reverse(Adj& A, const Schedule& sc, int a, int b, int slot, std::vector<int>
 }
 
 int check_support(hc_ctx* c) {
+  if (c->scalar) return fail(HC_ERR_UNSUPPORTED, "the adjoint covers the Euler law");
   if (c->fp32) return fail(HC_ERR_UNSUPPORTED, "the adjoint runs on HC_FP64 and HC_FP64_DF contexts");
   if (c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV)
     return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");

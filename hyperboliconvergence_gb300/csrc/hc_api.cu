@@ -92,7 +92,7 @@ int build_geometry(hc_ctx* c) {
   // ghost reference planes in the context precision
   for (int s = 0; s < 4; ++s) {
     if (c->bc[s] == HC_BC_PERIODIC || c->bc[s] == HC_BC_WALL || c->href[s].empty()) continue;
-    const size_t m = size_t(4) * c->nface(s);
+    const size_t m = size_t(c->nv) * c->nface(s);
     if (c->fp32) {
       std::vector<float> tmp(m);
       for (size_t k = 0; k < m; ++k) tmp[k] = float(c->href[s][k]);
@@ -126,7 +126,8 @@ template <class R> int run_residual(hc_ctx* c) {
   a.q = (const R*)c->q[0];
   a.res_out = (R*)c->res[0];
   a.mode = MODE_RESIDUAL;
-  HC_CUDA(stage_fn<R>(c->cfg.flux)(a, c->tile, c->stream));
+  if (c->scalar) HC_CUDA(launch_scalar_stage<R>(a, c->cfg.flux, c->tile, c->stream));
+  else HC_CUDA(stage_fn<R>(c->cfg.flux)(a, c->tile, c->stream));
   c->launches += 1;
   return HC_OK;
 }
@@ -136,7 +137,10 @@ template <class R> int run_step(hc_ctx* c) {
   const RKTab tab = rk_table(c->cfg.rk);
   const int nst = tab.nst;
   const bool global = c->cfg.dt_mode == HC_DT_GLOBAL;
-  const StageFn<R> fn = stage_fn<R>(c->cfg.flux);
+  const StageFn<R> euler_fn = stage_fn<R>(c->cfg.flux);
+  auto fn = [c, euler_fn](const StageArgs<R>& a, int tile, cudaStream_t s) -> cudaError_t {
+    return c->scalar ? launch_scalar_stage<R>(a, c->cfg.flux, tile, s) : euler_fn(a, tile, s);
+  };
   HC_CUDA(cudaMemsetAsync(&c->info->maxrate, 0, sizeof(unsigned long long), c->stream));
   HC_CUDA(cudaMemsetAsync(&c->info->resnorm2, 0, sizeof(double), c->stream));
   auto out_of = [&](int s) -> R* { return (R*)((s == nst - 1) ? c->q[0] : c->q[1 + (s % 2)]); };
@@ -156,9 +160,15 @@ template <class R> int run_step(hc_ctx* c) {
       const size_t n = c->ncell();
       const int B = 256;
       const unsigned grid = unsigned(std::min<size_t>((n + B - 1) / B, 152 * 16));
-      update0_kernel<R><<<grid, B, 0, c->stream>>>(c->ni, c->nj, a.gas, (const R*)c->q[0], (const R*)c->res[0],
-                                                   (const R*)c->vol, R(tab.alpha[0][0]), R(tab.beta[0]),
-                                                   c->cfg.cfl, c->info, out_of(0), 1);
+      if (c->scalar) {
+        HC_CUDA(launch_scalar_update0<R>(c->ni, c->nj, (const R*)c->q[0], (const R*)c->res[0], (const R*)c->vol,
+                                         R(tab.alpha[0][0]), R(tab.beta[0]), c->cfg.cfl, c->info, out_of(0), 1,
+                                         c->stream));
+      } else {
+        update0_kernel<R><<<grid, B, 0, c->stream>>>(c->ni, c->nj, a.gas, (const R*)c->q[0], (const R*)c->res[0],
+                                                     (const R*)c->vol, R(tab.alpha[0][0]), R(tab.beta[0]),
+                                                     c->cfg.cfl, c->info, out_of(0), 1);
+      }
       HC_CUDA(cudaGetLastError());
       c->launches += 2;
     } else {
@@ -220,13 +230,24 @@ int hc_context_create(const hc_config* cfg, hc_ctx** out) {
     return fail(HC_ERR_ARG, "unknown precision");
   if (cfg->dt_mode != HC_DT_GLOBAL && cfg->dt_mode != HC_DT_LOCAL) return fail(HC_ERR_ARG, "unknown dt mode");
   if (!(cfg->cfl > 0)) return fail(HC_ERR_ARG, "cfl must be positive");
+  if (cfg->law != HC_LAW_EULER && cfg->law != HC_LAW_SCALAR) return fail(HC_ERR_ARG, "unknown law");
+  if (cfg->law == HC_LAW_SCALAR) {
+    if (cfg->flux != HC_FLUX_RUSANOV && cfg->flux != HC_FLUX_CENTRAL)
+      return fail(HC_ERR_UNSUPPORTED, "the scalar advection law uses the Rusanov or central flux");
+    if (cfg->precision == HC_FP64_DF) return fail(HC_ERR_UNSUPPORTED, "the scalar advection law runs in FP64 or FP32");
+  }
   hc_ctx* c = new hc_ctx();
   c->cfg = *cfg;
+  c->scalar = cfg->law == HC_LAW_SCALAR;
+  c->nv = c->scalar ? 3 : 4;
   c->fp32 = cfg->precision == HC_FP32;
   c->df = cfg->precision == HC_FP64_DF;
   c->rsz = c->fp32 ? sizeof(float) : sizeof(double);
   cudaError_t e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = c->fp32 ? prepare<float>(cfg->flux) : prepare<double>(cfg->flux);
+  if (e == cudaSuccess) {
+    if (c->scalar) e = c->fp32 ? prepare_scalar_stage<float>() : prepare_scalar_stage<double>();
+    else e = c->fp32 ? prepare<float>(cfg->flux) : prepare<double>(cfg->flux);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&c->info, sizeof(StepInfo));
   if (e == cudaSuccess) e = cudaMemset(c->info, 0, sizeof(StepInfo));
   if (e != cudaSuccess) {
@@ -319,8 +340,11 @@ int hc_set_bcs(hc_ctx* c, const int bc_type[4], const double* const ref[4]) {
   if (int st = check_ctx(c)) return st;
   if (!c->have_mesh) return fail(HC_ERR_ARG, "upload the mesh before the boundary conditions");
   if (!bc_type) return fail(HC_ERR_ARG, "null bc types");
-  for (int s = 0; s < 4; ++s)
+  for (int s = 0; s < 4; ++s) {
     if (bc_type[s] < HC_BC_PERIODIC || bc_type[s] > HC_BC_WALL) return fail(HC_ERR_ARG, "unknown bc type");
+    if (c->scalar && (bc_type[s] == HC_BC_ENTROPY || bc_type[s] == HC_BC_WALL))
+      return fail(HC_ERR_UNSUPPORTED, "the scalar advection law has periodic, fixed and Riemann boundaries");
+  }
   if ((bc_type[0] == HC_BC_PERIODIC) != (bc_type[1] == HC_BC_PERIODIC) ||
       (bc_type[2] == HC_BC_PERIODIC) != (bc_type[3] == HC_BC_PERIODIC))
     return fail(HC_ERR_ARG, "periodic sides must come in pairs (0,1) and (2,3)");
@@ -330,7 +354,7 @@ int hc_set_bcs(hc_ctx* c, const int bc_type[4], const double* const ref[4]) {
     const bool needs = bc_type[s] != HC_BC_PERIODIC && bc_type[s] != HC_BC_WALL;
     if (needs) {
       if (!ref || !ref[s]) return fail(HC_ERR_ARG, "side " + std::to_string(s) + " needs reference values");
-      c->href[s].assign(ref[s], ref[s] + size_t(4) * c->nface(s));
+      c->href[s].assign(ref[s], ref[s] + size_t(c->nv) * c->nface(s));
     }
   }
   c->have_bcs = true;
@@ -342,7 +366,7 @@ int hc_state_upload(hc_ctx* c, const double* prim) {
   if (int st = check_ctx(c)) return st;
   if (!c->have_mesh) return fail(HC_ERR_ARG, "upload the mesh first");
   if (!prim) return fail(HC_ERR_ARG, "null state");
-  const size_t m = 4 * c->ncell();
+  const size_t m = size_t(c->nv) * c->ncell();
   if (c->fp32) {
     HC_CUDA(cudaMemcpyAsync(c->staging, prim, m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     d2r_kernel<float><<<1024, 256, 0, c->stream>>>(c->staging, (float*)c->q[0], m);
@@ -360,7 +384,7 @@ int hc_state_download(hc_ctx* c, double* prim) {
   if (int st = check_ctx(c)) return st;
   if (!c->have_state) return fail(HC_ERR_ARG, "no state");
   if (!prim) return fail(HC_ERR_ARG, "null output");
-  const size_t m = 4 * c->ncell();
+  const size_t m = size_t(c->nv) * c->ncell();
   if (c->fp32) {
     r2d_kernel<float><<<1024, 256, 0, c->stream>>>((const float*)c->q[0], c->staging, m);
     HC_CUDA(cudaGetLastError());
@@ -376,7 +400,7 @@ int hc_state_download(hc_ctx* c, double* prim) {
 int hc_state_upload_device(hc_ctx* c, const void* prim) {
   if (int st = check_ctx(c)) return st;
   if (!c->have_mesh || !prim) return fail(HC_ERR_ARG, "mesh and a state pointer are required");
-  HC_CUDA(cudaMemcpyAsync(c->q[0], prim, 4 * c->ncell() * c->rsz, cudaMemcpyDeviceToDevice, c->stream));
+  HC_CUDA(cudaMemcpyAsync(c->q[0], prim, size_t(c->nv) * c->ncell() * c->rsz, cudaMemcpyDeviceToDevice, c->stream));
   c->have_state = true;
   return HC_OK;
 }
@@ -384,7 +408,7 @@ int hc_state_upload_device(hc_ctx* c, const void* prim) {
 int hc_state_download_device(hc_ctx* c, void* prim) {
   if (int st = check_ctx(c)) return st;
   if (!c->have_state || !prim) return fail(HC_ERR_ARG, "no state or null output");
-  HC_CUDA(cudaMemcpyAsync(prim, c->q[0], 4 * c->ncell() * c->rsz, cudaMemcpyDeviceToDevice, c->stream));
+  HC_CUDA(cudaMemcpyAsync(prim, c->q[0], size_t(c->nv) * c->ncell() * c->rsz, cudaMemcpyDeviceToDevice, c->stream));
   return HC_OK;
 }
 
@@ -394,7 +418,7 @@ int hc_residual(hc_ctx* c, double* out5) {
   if (!out5) return fail(HC_ERR_ARG, "null output");
   const int st = c->fp32 ? run_residual<float>(c) : run_residual<double>(c);
   if (st != HC_OK) return st;
-  const size_t m = 5 * c->ncell();
+  const size_t m = size_t(c->nv + 1) * c->ncell();
   if (c->fp32) {
     r2d_kernel<float><<<1024, 256, 0, c->stream>>>((const float*)c->res[0], c->staging, m);
     HC_CUDA(cudaGetLastError());

@@ -254,6 +254,7 @@ int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* n
       cfg->rk < HC_RK_SSP11 || cfg->rk > HC_RK_SSP34 || (cfg->precision != HC_FP64 && cfg->precision != HC_FP32) ||
       (cfg->dt_mode != HC_DT_GLOBAL && cfg->dt_mode != HC_DT_LOCAL) || !(cfg->cfl > 0))
     return fail(HC_ERR_ARG, "invalid configuration");
+  if (cfg->law != HC_LAW_EULER) return fail(HC_ERR_UNSUPPORTED, "batches hold Euler instances");
   if (!(gamma > 1.0) || !(gas_constant > 0.0) || !(minf > 0.0)) return fail(HC_ERR_ARG, "invalid species");
   for (int k = 0; k < ninst; ++k) {
     if (ni[k] < 3 || nj[k] < 3 || !nodes[k]) return fail(HC_ERR_ARG, "instance " + std::to_string(k) + ": bad mesh");

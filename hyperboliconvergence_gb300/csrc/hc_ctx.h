@@ -8,6 +8,8 @@
 
 struct hc_ctx {
   hc_config cfg{};
+  int nv = 4;           // conserved variables of the law (Euler 4, scalar advection 3)
+  bool scalar = false;  // HC_LAW_SCALAR
   bool fp32 = false;
   size_t rsz = 8;
   int ni = 0, nj = 0;

@@ -18,6 +18,13 @@ template <class R, int FK> cudaError_t prepare_stage();
 // persistent batched stage: `grid` CTAs walk the work list of b
 template <class R, int FK> cudaError_t launch_batch_stage(const BatchArgs<R>& b, int tile, int grid, cudaStream_t s);
 
+// scalar advection law (hc_stage_scalar.cu): flux is FLUX_RUSANOV or FLUX_CENTRAL
+template <class R> cudaError_t prepare_scalar_stage();
+template <class R> cudaError_t launch_scalar_stage(const StageArgs<R>& a, int flux, int tile, cudaStream_t s);
+template <class R>
+cudaError_t launch_scalar_update0(int ni, int nj, const R* q0, const R* res0, const R* vol, R alpha00, R beta0,
+                                  double cfl, StepInfo* info, R* q_out, int advance_time, cudaStream_t s);
+
 inline void tile_dims(int tile, int* ti, int* tj) {
   switch (tile) {
     case TILE_4x32: *ti = 4; *tj = 32; break;

@@ -63,7 +63,7 @@ class Solver:
     """One mesh, its boundary conditions and state, advanced by explicit RK on the GPU."""
 
     def __init__(self, mesh: Mesh, bc, ref=None, flux="roe", limiter="vanleer", rk="ssp34",
-                 precision="fp64", dt="global", cfl=0.5, species=(1.4, 287.058, 1e-4), stream=None):
+                 precision="fp64", dt="global", cfl=0.5, species=(1.4, 287.058, 1e-4), stream=None, law="euler"):
         self.lib = _capi.load()
         self.mesh = mesh
         self.precision = precision
@@ -72,7 +72,9 @@ class Solver:
         cfg = Config(FLUX[flux] if isinstance(flux, str) else int(flux),
                      LIMITER[limiter] if isinstance(limiter, str) else int(limiter),
                      RK[rk] if isinstance(rk, str) else int(rk),
-                     PRECISION[precision], DTMODE[dt], float(cfl))
+                     PRECISION[precision], DTMODE[dt], float(cfl), _capi.LAW[law])
+        self.law = law
+        self.nv = 3 if law == "scalar" else 4  # conserved variables: {u, v, q} or {u, v, rho, p}
         h = C.c_void_p()
         check(self.lib.hc_context_create(C.byref(cfg), C.byref(h)))
         self.h = h
@@ -95,13 +97,14 @@ class Solver:
                 ptrs[s] = C.POINTER(C.c_double)()
             else:
                 arr = np.ascontiguousarray(np.broadcast_to(
-                    np.asarray(r, dtype=np.float64).reshape(4, -1), (4, mesh.nface(s))))
+                    np.asarray(r, dtype=np.float64).reshape(self.nv, -1), (self.nv, mesh.nface(s))))
                 self._refs.append(arr)
                 ptrs[s] = _dptr(arr)
         check(self.lib.hc_set_bcs(self.h, bct, ptrs))
         self.bc = list(bc)
         self.ref = [None if ref is None or ref[s] is None else
-                    np.broadcast_to(np.asarray(ref[s], dtype=np.float64).reshape(4, -1), (4, mesh.nface(s))).copy()
+                    np.broadcast_to(np.asarray(ref[s], dtype=np.float64).reshape(self.nv, -1),
+                                    (self.nv, mesh.nface(s))).copy()
                     for s in range(4)]
 
     # -- discrete adjoint -----------------------------------------------------
@@ -168,16 +171,19 @@ class Solver:
 
     # -- solution field ------------------------------------------------------
     def set_state(self, prim: np.ndarray) -> None:
+        """Upload the state: primitive {u, v, rho, p} (Euler) or conserved {u, v, q}
+        (scalar advection), shape (nv, ni, nj)."""
         a = np.ascontiguousarray(prim, dtype=np.float64)
-        if a.shape != (4, self.mesh.ni, self.mesh.nj):
-            raise ValueError(f"state must have shape (4, {self.mesh.ni}, {self.mesh.nj})")
+        if a.shape != (self.nv, self.mesh.ni, self.mesh.nj):
+            raise ValueError(f"state must have shape ({self.nv}, {self.mesh.ni}, {self.mesh.nj})")
         check(self.lib.hc_state_upload(self.h, _dptr(a)))
 
     def get_state(self, out: np.ndarray | None = None) -> np.ndarray:
-        """Download the primitive state (into ``out`` when given: C-contiguous float64)."""
+        """Download the state (into ``out`` when given: C-contiguous float64)."""
+        shape = (self.nv, self.mesh.ni, self.mesh.nj)
         if out is None:
-            out = np.empty((4, self.mesh.ni, self.mesh.nj))
-        elif out.shape != (4, self.mesh.ni, self.mesh.nj) or out.dtype != np.float64 or \
+            out = np.empty(shape)
+        elif out.shape != shape or out.dtype != np.float64 or \
                 not out.flags["C_CONTIGUOUS"]:
             raise ValueError("out must be a C-contiguous float64 array of the state's shape")
         check(self.lib.hc_state_download(self.h, _dptr(out)))
@@ -191,8 +197,8 @@ class Solver:
 
     # -- path ----------------------------------------------------------------
     def residual(self) -> np.ndarray:
-        """Flux sums (4 conserved planes) and spectral-radius sum of the current state."""
-        out = np.empty((5, self.mesh.ni, self.mesh.nj))
+        """Flux sums (nv conserved planes) and spectral-radius sum of the current state."""
+        out = np.empty((self.nv + 1, self.mesh.ni, self.mesh.nj))
         check(self.lib.hc_residual(self.h, _dptr(out)))
         return out
 

@@ -70,6 +70,16 @@ typedef enum { HC_DT_GLOBAL = 0, HC_DT_LOCAL = 1 } hc_dtmode;
  * Sides: 0 = i low, 1 = i high, 2 = j low, 3 = j high; periodic pairs (0,1), (2,3). */
 typedef enum { HC_BC_PERIODIC = 0, HC_BC_FIXED = 1, HC_BC_RIEMANN = 2, HC_BC_ENTROPY = 3, HC_BC_WALL = 4 } hc_bc;
 
+/* Conservation law (LawType).  HC_LAW_SCALAR is ScalarAdvection
+ * (conservationLaws/scalarAdvection/scalarAdvection.h:45-98): an advected scalar q
+ * with its advecting velocity, constant in time; its states are 3 planes of the
+ * conserved set {u, v, q} (reference layers 3 planes per side, hc_residual 4
+ * planes: 3 flux sums and lambda); fluxes HC_FLUX_RUSANOV or HC_FLUX_CENTRAL;
+ * boundaries periodic, fixed or Riemann (inflow takes the reference value,
+ * outflow the interior one, scalarAdvection/boundary/riemann.ipp); HC_FP64 or
+ * HC_FP32; single-mesh contexts, no adjoint. */
+typedef enum { HC_LAW_EULER = 0, HC_LAW_SCALAR = 1 } hc_law;
+
 typedef struct {
   int flux;      /* hc_flux */
   int limiter;   /* hc_limiter */
@@ -77,6 +87,7 @@ typedef struct {
   int precision; /* hc_precision */
   int dt_mode;   /* hc_dtmode */
   double cfl;    /* UnsteadyTimeControls::cfl (controls.h:11-19) */
+  int law;       /* hc_law; 0 = Euler */
 } hc_config;
 
 typedef struct {

@@ -291,3 +291,88 @@ def objective(mesh_nodes, ni, nj, bc, q0, nsteps, kind="drag", flux="roe", limit
                           _ptr(dq), int(nsteps), k, float(scale), float(direction[0]), float(direction[1]),
                           _ptr(tgt), _ptr(w), 1 if freeze_dt else 0, _ptr(out))
     return float(out[0]), float(out[1])
+
+
+SBC = {"periodic": 0, "fixed": 1, "riemann": 2}
+SFLUX = {"rusanov": 0, "central": 1}
+
+
+def _declare_scalar(lib):
+    if getattr(lib, "_scalar_declared", False):
+        return
+    v, i, d = C.c_void_p, C.c_int, C.c_double
+    lib.hcos_create.restype = v
+    lib.hcos_create.argtypes = [i, i, _dp, _ip, i, i, i, i, d]
+    lib.hcos_destroy.argtypes = [v]
+    lib.hcos_set_ghost_ref.argtypes = [v, i, _dp]
+    lib.hcos_set_state.argtypes = [v, _dp]
+    lib.hcos_get_state.argtypes = [v, _dp]
+    lib.hcos_residual.argtypes = [v, _dp]
+    lib.hcos_step.argtypes = [v, i, _dp]
+    lib.hcos_flux.argtypes = [i, _dp, _dp, _dp, _dp]
+    lib.hcos_bc_riemann.argtypes = [_dp, _dp, _dp, _dp]
+    lib._scalar_declared = True
+
+
+def scalar_flux(kind, face, ql, qr):
+    lib = load(False)
+    _declare_scalar(lib)
+    out = np.empty(4)
+    lib.hcos_flux(int(kind), np.ascontiguousarray(face, dtype=np.float64), np.ascontiguousarray(ql, dtype=np.float64),
+                  np.ascontiguousarray(qr, dtype=np.float64), out)
+    return out
+
+
+def scalar_bc_riemann(face, qi, qb):
+    lib = load(False)
+    _declare_scalar(lib)
+    out = np.empty(3)
+    lib.hcos_bc_riemann(np.ascontiguousarray(face, dtype=np.float64), np.ascontiguousarray(qi, dtype=np.float64),
+                        np.ascontiguousarray(qb, dtype=np.float64), out)
+    return out
+
+
+class ScalarOracleSolver:
+    """CPU restatement of integrate() for the scalar advection law (conserved {u, v, q})."""
+
+    def __init__(self, ni, nj, nodes, bc, flux="rusanov", limiter="nolimit3", rk="ssp34", dt="global", cfl=0.5,
+                 ghost_ref=None, fast=False):
+        self.lib = load(fast)
+        _declare_scalar(self.lib)
+        self.ni, self.nj = ni, nj
+        bcv = np.array([SBC[b] if isinstance(b, str) else int(b) for b in bc], dtype=np.int32)
+        self.h = self.lib.hcos_create(ni, nj, np.ascontiguousarray(nodes, dtype=np.float64), bcv,
+                                      SFLUX[flux] if isinstance(flux, str) else flux,
+                                      LIMITER[limiter] if isinstance(limiter, str) else limiter,
+                                      RK[rk] if isinstance(rk, str) else rk, DT[dt] if isinstance(dt, str) else dt,
+                                      float(cfl))
+        if ghost_ref is not None:
+            for side in range(4):
+                if ghost_ref[side] is not None:
+                    nf = nj if side < 2 else ni
+                    arr = np.ascontiguousarray(np.broadcast_to(
+                        np.asarray(ghost_ref[side], dtype=np.float64).reshape(3, -1), (3, nf)))
+                    self.lib.hcos_set_ghost_ref(self.h, side, arr)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.hcos_destroy(self.h)
+            self.h = None
+
+    def set_state(self, soa):
+        self.lib.hcos_set_state(self.h, np.ascontiguousarray(soa, dtype=np.float64))
+
+    def get_state(self):
+        out = np.empty((3, self.ni, self.nj))
+        self.lib.hcos_get_state(self.h, out)
+        return out
+
+    def residual(self):
+        out = np.empty((4, self.ni, self.nj))
+        self.lib.hcos_residual(self.h, out)
+        return out
+
+    def step(self, n=1):
+        out = np.empty(2)
+        self.lib.hcos_step(self.h, int(n), out)
+        return float(out[0]), float(out[1])
