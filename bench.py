@@ -342,6 +342,60 @@ def measure_adjoint(nsteps: int = 400, snapshots: int = 20):
     return out
 
 
+def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int = 20, seed: int = 2027):
+    """Batched and differentiated case: `ninst` periodic Euler instances on [0,1]^2,
+    n x n cells with n drawn from {128, 192, ..., 1024}, density = 5 plus 8 seeded
+    Gaussians (widths 0.02..0.2, amplitudes -0.5..0.5) on u = 0.5, v = 0.25, p = 1;
+    Rusanov + van Albada, ssp34, global dt, CFL 0.5.  L2 loss of the state after
+    `nsteps` steps against a seeded target of the same kind; gradient with respect
+    to every instance's initial state in FP32 (one adjoint call per instance,
+    `snapshots` checkpoints), and the FP32 gradient of the smallest instance
+    against its FP64 gradient."""
+    from hyperboliconvergence_gb300 import cases
+    from hyperboliconvergence_gb300.solver import Solver
+    rng = np.random.default_rng(seed)
+    sizes = [int(n) for n in rng.choice(np.arange(128, 1025, 64), ninst)]
+    base = (0.5, 0.25, 5.0, 1.0)
+    cells = 0
+    fwd_ms = rev_ms = 0.0
+    t0 = time.perf_counter()
+    for k, n in enumerate(sizes):
+        mesh, bc, ref, q, sp = cases.gaussian_sum(n, n, rng, base=base)
+        target = cases.gaussian_sum(n, n, rng, base=base)[3]
+        s = Solver(mesh, bc, ref, flux="rusanov", limiter="vanalbada", rk="ssp34", precision="fp32", dt="global",
+                   cfl=0.5, species=sp)
+        s.set_state(q)
+        J, g, refb, rates, st = s.gradient(nsteps, snapshots=snapshots, kind="l2", target=target)
+        s.close()
+        if not np.isfinite(J) or not np.all(np.isfinite(g)):
+            raise RuntimeError(f"instance {k}: non-finite objective or gradient")
+        cells += n * n
+        fwd_ms += st.ms_forward
+        rev_ms += st.ms_total - st.ms_forward
+    wall = time.perf_counter() - t0
+    # FP64 check on the smallest instance
+    n = min(sizes)
+    crng = np.random.default_rng(seed + 1)
+    mesh, bc, ref, q, sp = cases.gaussian_sum(n, n, crng, base=base)
+    target = cases.gaussian_sum(n, n, crng, base=base)[3]
+    grads = {}
+    for prec in ("fp32", "fp64"):
+        s = Solver(mesh, bc, ref, flux="rusanov", limiter="vanalbada", rk="ssp34", precision=prec, dt="global",
+                   cfl=0.5, species=sp)
+        s.set_state(q)
+        grads[prec] = s.gradient(nsteps, snapshots=snapshots, kind="l2", target=target)[:2]
+        s.close()
+    (j32, g32), (j64, g64) = grads["fp32"], grads["fp64"]
+    return {"workload": f"{ninst} Gaussian-sum Euler instances, n x n with n in 128..1024, L2 loss after "
+                        f"{nsteps} ssp34 steps, {snapshots} snapshots, FP32",
+            "cells": cells, "forward_ms": fwd_ms, "reverse_ms": rev_ms, "wall_s": wall,
+            "forward_cell_updates_per_s": cells * nsteps / (fwd_ms / 1e3),
+            "adjoint_step_over_forward_step": rev_ms / fwd_ms,
+            "fp64_check": {"cells": n * n, "J_rel_diff": abs(j32 - j64) / abs(j64),
+                           "grad_max_rel_diff": float(np.abs(g32 - g64).max() / np.abs(g64).max())},
+            "note": "one adjoint call per instance; the adjoint has no batched launch"}
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -468,7 +522,8 @@ def run_gpu(args):
                              ("fp64_df", lambda: measure_precision(stream, args.steps, "fp64_df")),
                              ("batched", lambda: measure_batched(stream)),
                              ("variants", lambda: measure_variants(stream)),
-                             ("adjoint", measure_adjoint)):
+                             ("adjoint", measure_adjoint),
+                             ("batched_adjoint", measure_batched_adjoint)):
                 if name in extras:
                     try:
                         line[name] = fn()
@@ -490,9 +545,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP32, double-float, batched and adjoint measurements beside the headline")
-    ap.add_argument("--extras", default="fp32,fp64_df,batched,variants,adjoint",
-                    help="comma-separated subset of fp32,fp64_df,batched,variants,adjoint to measure beside the "
-                         "headline")
+    ap.add_argument("--extras", default="fp32,fp64_df,batched,variants,adjoint,batched_adjoint",
+                    help="comma-separated subset of fp32,fp64_df,batched,variants,adjoint,batched_adjoint to "
+                         "measure beside the headline")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -1,0 +1,577 @@
+// hc_adjoint_driver.cuh -- discrete adjoint of the RK time loop of one context with
+// binomial checkpointing (Griewank & Walther, "Algorithm 799: revolve", ACM TOMS
+// 26(1), 2000: with s snapshots and t forward repetitions, C(s+t, s) steps can
+// be reversed), templated on the context's storage type R (double or float);
+// per-step max rates, timesteps and the objective stay in FP64.  The timestep of
+// every step is frozen at the value of the forward run (the max-rate history is
+// recorded and replayed), so the gradient is that of the objective at fixed
+// timesteps.
+//
+// Objectives: time-averaged wall force (drag) over steps 1..N, or a weighted
+// L2 distance of the final state to a target.  Supported: Euler law; HC_FP64,
+// HC_FP64_DF and HC_FP32 contexts; Roe or Rusanov flux; limiters NoLimit1/2/3,
+// van Albada, MinMod, van Leer; periodic / fixed / inviscid-wall boundaries;
+// global timestep.  hc_adjoint.cu instantiates R = double and the C ABI,
+// hc_adjoint_f32.cu R = float.
+#pragma once
+
+#include "hc_adjoint_kernels.cuh"
+#include "hc_ctx.h"
+
+#include <cfloat>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+namespace hc {
+namespace adj {
+
+template <class R> struct Adj {
+  hc_ctx* c = nullptr;
+  int nst = 4;
+  RKTab tab{};
+  size_t n = 0;
+  int nfi = 0, nfj = 0;
+  R* sq[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // stage states; sq[nst] = step output
+  R* rbar[4] = {nullptr, nullptr, nullptr, nullptr};
+  R* qm = nullptr;
+  R* qmbar = nullptr;
+  R* ai = nullptr;
+  R* aj = nullptr;
+  R* lam = nullptr;
+  R* qbs = nullptr;
+  R* q0bar = nullptr;
+  R* refbar[4] = {nullptr, nullptr, nullptr, nullptr};
+  R* base = nullptr;
+  R* snaps = nullptr;
+  int nsnap = 0;
+  double* rates = nullptr;   // device, one max-rate per step
+  R* wall = nullptr;    // per wall face partial forces
+  double* jacc = nullptr;    // device accumulator of the objective
+  R* target = nullptr;
+  std::vector<double> hrates;
+  hc_objective obj{};
+  int nsteps = 0;
+  long long fwd_steps = 0, adj_steps = 0, launches = 0;
+  std::vector<void*> allocs;
+  std::vector<cudaEvent_t> adv_events;  // (start, end) pairs around checkpoint recomputation
+
+  template <class T> int alloc(T** p, size_t count) {
+    HC_CUDA(cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T)));
+    allocs.push_back(*p);
+    return HC_OK;
+  }
+  ~Adj() {
+    for (void* p : allocs) cudaFree(p);
+    for (cudaEvent_t e : adv_events) cudaEventDestroy(e);
+  }
+  // time of the recorded recomputation segments (call after the stream is idle)
+  double recompute_ms() const {
+    double t = 0;
+    for (size_t k = 0; k + 1 < adv_events.size(); k += 2) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, adv_events[k], adv_events[k + 1]) == cudaSuccess) t += ms;
+    }
+    return t;
+  }
+  cudaStream_t s() const { return c->stream; }
+};
+
+template <class R> AdjArgs<R> adj_args(Adj<R>& A) {
+  hc_ctx* c = A.c;
+  AdjArgs<R> a{};
+  a.ni = c->ni; a.nj = c->nj;
+  for (int k = 0; k < 4; ++k) a.bc[k] = c->bc[k];
+  a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf);
+  a.limiter = c->cfg.limiter;
+  a.fi = (const R*)c->fi; a.fj = (const R*)c->fj;
+  for (int k = 0; k < 4; ++k) { a.gref[k] = (const R*)c->gref[k]; a.refbar[k] = A.refbar[k]; }
+  a.qm = A.qm; a.qmbar = A.qmbar; a.ai = A.ai; a.aj = A.aj;
+  return a;
+}
+
+inline unsigned blocks(size_t n) { return unsigned((n + 255) / 256); }
+
+// one forward step from sq[0] to sq[nst]; record (rec=true) or replay the max rate of step `step`
+template <class R> int forward_step(Adj<R>& A, int step, bool rec) {
+  hc_ctx* c = A.c;
+  const StageFn<R> fn = stage_fn<R>(c->cfg.flux);
+  for (int s = 0; s < A.nst; ++s) {
+    StageArgs<R> a = base_args<R>(c);
+    a.q = A.sq[s];
+    a.q0 = A.sq[0];
+    a.stage = s;
+    a.beta = R(A.tab.beta[s]);
+    for (int k = 0; k <= s; ++k) a.alpha[k] = R(A.tab.alpha[s][k]);
+    for (int k = 0; k < s; ++k) a.res_prev[k] = (const R*)c->res[k];
+    a.res_out = (s < A.nst - 1) ? (R*)c->res[s] : nullptr;
+    a.norm_stage0 = 0;
+    if (s == 0) {
+      a.res_out = (R*)c->res[0];
+      if (rec) {
+        HC_CUDA(cudaMemsetAsync(&c->info->maxrate, 0, sizeof(unsigned long long), A.s()));
+        a.mode = MODE_RES_MAXRATE;
+        HC_CUDA(fn(a, c->tile, A.s()));
+        HC_CUDA(cudaMemcpyAsync(A.rates + step, &c->info->maxrate, sizeof(double), cudaMemcpyDeviceToDevice, A.s()));
+      } else {
+        HC_CUDA(cudaMemcpyAsync(&c->info->maxrate, A.rates + step, sizeof(double), cudaMemcpyDeviceToDevice, A.s()));
+        a.mode = MODE_RESIDUAL;
+        HC_CUDA(fn(a, c->tile, A.s()));
+      }
+      update0_kernel<R><<<std::min<unsigned>(blocks(A.n), 152 * 16), 256, 0, A.s()>>>(
+          c->ni, c->nj, a.gas, A.sq[0], (const R*)c->res[0], (const R*)c->vol, R(A.tab.alpha[0][0]),
+          R(A.tab.beta[0]), c->cfg.cfl, c->info, A.sq[1], 0);
+      HC_CUDA(cudaGetLastError());
+      A.launches += 2;
+    } else {
+      a.mode = MODE_FUSED_GLOBAL;
+      a.q_out = A.sq[s + 1];
+      HC_CUDA(fn(a, c->tile, A.s()));
+      A.launches += 1;
+    }
+  }
+  A.fwd_steps += 1;
+  return HC_OK;
+}
+
+// sq[nst] -> sq[0] (the step output becomes the next step's start)
+template <class R> void swap_out(Adj<R>& A) { std::swap(A.sq[0], A.sq[A.nst]); }
+
+template <class R> __global__ void sum_into_kernel(const R* __restrict__ v, int m, double* __restrict__ acc) {
+  // one block, fixed order: deterministic
+  __shared__ double part[256];
+  double s = 0;
+  for (int k = threadIdx.x; k < m; k += 256) s += double(v[k]);
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) acc[0] += part[0];
+}
+
+// J += scale * wall force of the state q (drag objective)
+template <class R> int add_drag(Adj<R>& A, const R* q, double scale) {
+  AdjArgs<R> a = adj_args(A);
+  a.q = q;
+  a.obj_scale = R(scale);
+  a.obj_dirx = R(A.obj.dir[0]);
+  a.obj_diry = R(A.obj.dir[1]);
+  adj_qm_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
+  A.launches += 1;
+  for (int side = 0; side < 4; ++side) {
+    if (A.c->bc[side] != HC_BC_WALL) continue;
+    const int m = A.c->nface(side);
+    wall_force_kernel<R><<<blocks(m), 256, 0, A.s()>>>(a, A.qm, side, A.wall);
+    sum_into_kernel<R><<<1, 256, 0, A.s()>>>(A.wall, m, A.jacc);
+    A.launches += 2;
+  }
+  HC_CUDA(cudaGetLastError());
+  return HC_OK;
+}
+
+template <class R>
+__global__ void l2_kernel(const R* q, const R* t, size_t n, double w0, double w1, double w2, double w3, R* part,
+                          int mode_grad, R* lam) {
+  const size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (c >= n) return;
+  const double w[4] = {w0, w1, w2, w3};
+  double s = 0;
+  for (int v = 0; v < 4; ++v) {
+    const double d = double(q[v * n + c]) - double(t[v * n + c]);
+    s += w[v] * d * d;
+    if (mode_grad) lam[v * n + c] = R(2.0 * w[v] * d);
+  }
+  if (part) part[c] = R(s);
+}
+
+// residual adjoint: qbar_out = (dRes/dq at q)^T rbar (+ qbar_add); objective mode
+// uses only the wall faces with the drag weights instead of rbar
+template <class R, int FK>
+int residual_adjoint(Adj<R>& A, const R* q, const R* rbar, const R* qbar_add, R* qbar_out, bool objective,
+                     double obj_scale) {
+  AdjArgs<R> a = adj_args(A);
+  a.q = q;
+  a.rbar = rbar;
+  a.qbar = qbar_out;
+  a.qbar_add = qbar_add;
+  a.objective = objective ? 1 : 0;
+  a.obj_scale = R(obj_scale);
+  a.obj_dirx = R(A.obj.dir[0]);
+  a.obj_diry = R(A.obj.dir[1]);
+  adj_qm_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
+  if constexpr (std::is_same<R, double>::value) {
+    if (A.c->df) {  // double-float face arithmetic on HC_FP64_DF contexts
+      adj_face_kernel<double, FK, df64><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
+      adj_face_kernel<double, FK, df64><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+    } else {
+      adj_face_kernel<double, FK><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
+      adj_face_kernel<double, FK><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+    }
+  } else {
+    adj_face_kernel<R, FK><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
+    adj_face_kernel<R, FK><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+  }
+  adj_qmbar_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a);
+  adj_gather_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a);
+  A.launches += 5;
+  HC_CUDA(cudaGetLastError());
+  return HC_OK;
+}
+
+template <class R> int res_adj(Adj<R>& A, const R* q, const R* rbar, const R* add, R* out, bool obj, double sc) {
+  if (A.c->cfg.flux == HC_FLUX_ROE) return residual_adjoint<R, FLUX_ROE>(A, q, rbar, add, out, obj, sc);
+  return residual_adjoint<R, FLUX_RUSANOV>(A, q, rbar, add, out, obj, sc);
+}
+
+template <class R> double step_dt(const Adj<R>& A, int step) {
+  const double rate = std::fmax(DBL_MIN, A.hrates[step]);
+  return A.c->cfg.cfl / rate;
+}
+
+// lam holds the adjoint of q_{step+1}; sq[0] holds q_step.  On return lam holds
+// the adjoint of q_step (objective terms of q_step included).
+template <class R> int adjoint_step(Adj<R>& A, int step) {
+  if (int st = forward_step(A, step, false)) return st;
+  const size_t bytes4 = 4 * A.n * sizeof(R);
+  for (int k = 0; k < A.nst; ++k) HC_CUDA(cudaMemsetAsync(A.rbar[k], 0, bytes4, A.s()));
+  HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
+  const double dt = step_dt(A, step);
+  const Gas<R> g = make_gas<R>(A.c->gamma, A.c->Rgas, A.c->minf);
+  for (int s = A.nst - 1; s >= 0; --s) {
+    const R* qbar_out = (s == A.nst - 1) ? A.lam : A.qbs;
+    R al[4] = {R(0), R(0), R(0), R(0)};
+    for (int k = 0; k <= s; ++k) al[k] = R(A.tab.alpha[s][k]);
+    adj_update_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(
+        int(A.n), g, A.sq[s + 1], A.sq[0], (const R*)A.c->vol, qbar_out, A.q0bar, A.rbar[0], A.rbar[1],
+        A.rbar[2], A.rbar[3], al[0], al[1], al[2], al[3], s, R(A.tab.beta[s] * dt));
+    A.launches += 1;
+    HC_CUDA(cudaGetLastError());
+    if (int st = res_adj<R>(A, A.sq[s], A.rbar[s], s == 0 ? A.q0bar : nullptr, A.qbs, false, 0.0)) return st;
+  }
+  if (A.obj.kind == HC_OBJ_DRAG && step >= 1) {
+    if (int st = res_adj<R>(A, A.sq[0], nullptr, A.qbs, A.lam, true, A.obj.scale / A.nsteps)) return st;
+  } else {
+    HC_CUDA(cudaMemcpyAsync(A.lam, A.qbs, bytes4, cudaMemcpyDeviceToDevice, A.s()));
+  }
+  A.adj_steps += 1;
+  return HC_OK;
+}
+
+// ---- binomial checkpointing
+// Reversing n steps whose start state is restorable, with s free snapshot slots,
+// costs T(n, s) recomputed forward steps under the best schedule:
+//   T(1, s) = 0,  T(n, 0) = n(n-1)/2 (every state re-advanced from the start),
+//   T(n, s) = min_k [k + T(n-k, s-1) + T(k, s)]
+// (advance k steps and store, reverse the right part with one slot fewer, then
+// the left part with the slot freed).  The first forward sweep passes every
+// state, so it stores the checkpoints of the schedule's first descent (the
+// right-most path) as it goes; for that path the advance is free:
+//   F(n, s) = min_k [F(n-k, s-1) + T(k, s)],  F(n, 0) = T(n, 0).
+// Both tables and their minimising splits are computed by dynamic programming
+// (O(n^2 s)); beyond kDpLimit operations the split falls back to the binomial
+// rule k = n - C(s-1+t, s-1), t the smallest with C(s+t, s) >= n.
+constexpr double kDpLimit = 4e8;
+
+inline double binom(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  double r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+  return r;
+}
+
+inline int binomial_split(int n, int s) {
+  int t = 1;
+  while (binom(s + t, s) < n) ++t;
+  const int k = n - int(binom(s - 1 + t, s - 1));
+  return std::max(1, std::min(k, n - 1));
+}
+
+struct Schedule {
+  int N = 0, S = 0;
+  bool dp = false;
+  std::vector<long long> T, F;
+  std::vector<int> kT, kF;
+  size_t at(int n, int s) const { return size_t(s) * (N + 1) + n; }
+  void build(int n_max, int s_max) {
+    N = n_max; S = s_max;
+    dp = double(N) * N * (S + 1) <= kDpLimit;
+    if (!dp) return;
+    const size_t m = size_t(N + 1) * (S + 1);
+    T.assign(m, 0); F.assign(m, 0); kT.assign(m, 1); kF.assign(m, 1);
+    for (int n = 0; n <= N; ++n) T[at(n, 0)] = F[at(n, 0)] = (long long)n * (n - 1) / 2;
+    for (int s = 1; s <= S; ++s)
+      for (int n = 2; n <= N; ++n) {
+        long long bt = -1, bf = -1;
+        int kt = 1, kf = 1;
+        for (int k = 1; k < n; ++k) {
+          const long long right_t = T[at(n - k, s - 1)], right_f = F[at(n - k, s - 1)], left = T[at(k, s)];
+          const long long ct = k + right_t + left, cf = right_f + left;
+          if (bt < 0 || ct < bt) { bt = ct; kt = k; }
+          if (bf < 0 || cf < bf) { bf = cf; kf = k; }
+        }
+        T[at(n, s)] = bt; kT[at(n, s)] = kt;
+        F[at(n, s)] = bf; kF[at(n, s)] = kf;
+      }
+  }
+  int split(int n, int s, bool first) const {
+    if (!dp) return binomial_split(n, s);
+    return first ? kF[at(n, s)] : kT[at(n, s)];
+  }
+};
+
+template <class R> R* slot_ptr(Adj<R>& A, int slot) { return slot < 0 ? A.base : A.snaps + size_t(slot) * 4 * A.n; }
+
+template <class R> int restore(Adj<R>& A, int slot) {
+  HC_CUDA(cudaMemcpyAsync(A.sq[0], slot_ptr(A, slot), 4 * A.n * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
+  return HC_OK;
+}
+template <class R> int store(Adj<R>& A, int slot) {
+  HC_CUDA(cudaMemcpyAsync(slot_ptr(A, slot), A.sq[0], 4 * A.n * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
+  return HC_OK;
+}
+template <class R> int advance(Adj<R>& A, int from, int to) {
+  if (to <= from) return HC_OK;
+  cudaEvent_t ev[2];
+  HC_CUDA(cudaEventCreate(&ev[0]));
+  A.adv_events.push_back(ev[0]);
+  HC_CUDA(cudaEventCreate(&ev[1]));
+  A.adv_events.push_back(ev[1]);
+  HC_CUDA(cudaEventRecord(ev[0], A.s()));
+  for (int k = from; k < to; ++k) {
+    if (int st = forward_step(A, k, false)) return st;
+    swap_out(A);
+  }
+  HC_CUDA(cudaEventRecord(ev[1], A.s()));
+  return HC_OK;
+}
+
+// The first descent of the schedule for n steps and s slots: (position, slot)
+// pairs, slots taken from the back of `stack` as reverse() takes them.
+inline std::vector<std::pair<int, int>> first_descent(const Schedule& sc, int n, int s, std::vector<int> stack) {
+  std::vector<std::pair<int, int>> out;
+  int a = 0;
+  while (n - a > 1 && !stack.empty()) {
+    const int k = sc.split(n - a, int(stack.size()), true);
+    out.push_back({a + k, stack.back()});
+    stack.pop_back();
+    a += k;
+  }
+  return out;
+}
+
+// reverse steps [a, b) whose start state is in `slot`, with the free slots on
+// `stack`; `first`: the split points of this call's right-most path were stored
+// by the forward sweep
+template <class R>
+int reverse(Adj<R>& A, const Schedule& sc, int a, int b, int slot, std::vector<int>& stack, bool first) {
+  const int n = b - a;
+  const int sfree = int(stack.size());
+  if (n <= 0) return HC_OK;
+  if (n == 1) {
+    if (int st = restore(A, slot)) return st;
+    return adjoint_step(A, a);
+  }
+  if (sfree == 0) {
+    for (int i = b - 1; i >= a; --i) {
+      if (int st = restore(A, slot)) return st;
+      if (int st = advance(A, a, i)) return st;
+      if (int st = adjoint_step(A, i)) return st;
+    }
+    return HC_OK;
+  }
+  const int k = sc.split(n, sfree, first);
+  const int mid = stack.back();
+  stack.pop_back();
+  if (!first) {
+    if (int st = restore(A, slot)) return st;
+    if (int st = advance(A, a, a + k)) return st;
+    if (int st = store(A, mid)) return st;
+  }
+  if (int st = reverse(A, sc, a + k, b, mid, stack, first)) return st;
+  stack.push_back(mid);
+  return reverse(A, sc, a, a + k, slot, stack, false);
+}
+
+inline int check_support(hc_ctx* c) {
+  if (c->scalar) return fail(HC_ERR_UNSUPPORTED, "the adjoint covers the Euler law");
+  if (c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV)
+    return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");
+  const int l = c->cfg.limiter;
+  if (!(l == HC_LIM_NOLIMIT1 || l == HC_LIM_NOLIMIT2 || l == HC_LIM_NOLIMIT3 || l == HC_LIM_VANALBADA ||
+        l == HC_LIM_MINMOD || l == HC_LIM_VANLEER))
+    return fail(HC_ERR_UNSUPPORTED, "limiter not differentiated by the adjoint");
+  if (c->cfg.dt_mode != HC_DT_GLOBAL) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the global timestep");
+  for (int s = 0; s < 4; ++s)
+    if (c->bc[s] == HC_BC_RIEMANN || c->bc[s] == HC_BC_ENTROPY)
+      return fail(HC_ERR_UNSUPPORTED, "the adjoint supports periodic, fixed and wall boundaries");
+  return HC_OK;
+}
+
+template <class R> int setup(Adj<R>& A, hc_ctx* c, int nsteps, int nsnap, const hc_objective* obj) {
+  if (!c || !obj || nsteps < 1 || nsnap < 0) return fail(HC_ERR_ARG, "bad adjoint arguments");
+  if (obj->kind != HC_OBJ_DRAG && obj->kind != HC_OBJ_L2) return fail(HC_ERR_ARG, "unknown objective");
+  if (int st = ctx_ensure_ready(c)) return st;
+  if (int st = check_support(c)) return st;
+  A.c = c;
+  A.tab = rk_table(c->cfg.rk);
+  A.nst = A.tab.nst;
+  A.n = c->ncell();
+  A.nfi = (c->ni + 1) * c->nj;
+  A.nfj = c->ni * (c->nj + 1);
+  A.obj = *obj;
+  A.nsteps = nsteps;
+  A.nsnap = nsnap;
+  const size_t n4 = 4 * A.n;
+  for (int k = 0; k <= A.nst; ++k) if (int st = A.alloc(&A.sq[k], n4)) return st;
+  for (int k = 0; k < 4; ++k) if (int st = A.alloc(&A.rbar[k], n4)) return st;
+  if (int st = A.alloc(&A.qm, 8 * A.n)) return st;
+  if (int st = A.alloc(&A.qmbar, 8 * A.n)) return st;
+  if (int st = A.alloc(&A.ai, size_t(ADJ_FIELDS) * A.nfi)) return st;
+  if (int st = A.alloc(&A.aj, size_t(ADJ_FIELDS) * A.nfj)) return st;
+  if (int st = A.alloc(&A.lam, n4)) return st;
+  if (int st = A.alloc(&A.qbs, n4)) return st;
+  if (int st = A.alloc(&A.q0bar, n4)) return st;
+  for (int s = 0; s < 4; ++s) {
+    if (int st = A.alloc(&A.refbar[s], 4 * size_t(c->nface(s)))) return st;
+    HC_CUDA(cudaMemsetAsync(A.refbar[s], 0, 4 * c->nface(s) * sizeof(R), A.s()));
+  }
+  if (int st = A.alloc(&A.base, n4)) return st;
+  if (nsnap > 0) if (int st = A.alloc(&A.snaps, size_t(nsnap) * n4)) return st;
+  if (int st = A.alloc(&A.rates, size_t(nsteps))) return st;
+  if (int st = A.alloc(&A.wall, size_t(std::max(c->ni, c->nj)))) return st;
+  if (int st = A.alloc(&A.jacc, 1)) return st;
+  HC_CUDA(cudaMemsetAsync(A.jacc, 0, sizeof(double), A.s()));
+  if (obj->kind == HC_OBJ_L2) {
+    if (!obj->target) return fail(HC_ERR_ARG, "the L2 objective needs a target state");
+    if (int st = A.alloc(&A.target, n4)) return st;
+    double* t64 = nullptr;
+    if (int st = A.alloc(&t64, n4)) return st;
+    HC_CUDA(cudaMemcpyAsync(t64, obj->target, n4 * sizeof(double), cudaMemcpyHostToDevice, A.s()));
+    convert_kernel<R><<<1024, 256, 0, A.s()>>>(t64, A.target, n4);
+    HC_CUDA(cudaGetLastError());
+  }
+  HC_CUDA(cudaMemcpyAsync(A.base, c->q[0], n4 * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
+  return HC_OK;
+}
+
+// forward pass from the base state: J and (rates == nullptr) the max-rate
+// history; the states at the positions of `stores` go to their snapshot slots
+template <class R>
+int forward_pass(Adj<R>& A, const double* rates_in, const std::vector<std::pair<int, int>>& stores = {}) {
+  if (rates_in) HC_CUDA(cudaMemcpyAsync(A.rates, rates_in, A.nsteps * sizeof(double), cudaMemcpyHostToDevice, A.s()));
+  if (int st = restore(A, -1)) return st;
+  size_t next = 0;
+  for (int k = 0; k < A.nsteps; ++k) {
+    if (int st = forward_step(A, k, rates_in == nullptr)) return st;
+    swap_out(A);
+    while (next < stores.size() && stores[next].first == k + 1) {
+      if (int st = store(A, stores[next].second)) return st;
+      ++next;
+    }
+    if (A.obj.kind == HC_OBJ_DRAG)
+      if (int st = add_drag(A, A.sq[0], A.obj.scale / A.nsteps)) return st;
+  }
+  if (A.obj.kind == HC_OBJ_L2) {
+    l2_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(A.sq[0], A.target, A.n, A.obj.weight[0], A.obj.weight[1],
+                                                  A.obj.weight[2], A.obj.weight[3], A.qbs, 0, nullptr);
+    sum_into_kernel<R><<<1, 256, 0, A.s()>>>(A.qbs, int(A.n), A.jacc);
+    A.launches += 2;
+  }
+  A.hrates.resize(A.nsteps);
+  HC_CUDA(cudaMemcpyAsync(A.hrates.data(), A.rates, A.nsteps * sizeof(double), cudaMemcpyDeviceToHost, A.s()));
+  HC_CUDA(cudaStreamSynchronize(A.s()));
+  return HC_OK;
+}
+
+template <class R> int finish_stats(Adj<R>& A, double* J, double* rates_out, hc_adjoint_stats* stats) {
+  double j = 0;
+  HC_CUDA(cudaMemcpyAsync(&j, A.jacc, sizeof(double), cudaMemcpyDeviceToHost, A.s()));
+  HC_CUDA(cudaStreamSynchronize(A.s()));
+  if (J) *J = j;
+  if (rates_out) std::memcpy(rates_out, A.hrates.data(), A.nsteps * sizeof(double));
+  A.c->launches += A.launches;
+  if (stats) {
+    stats->J = j;
+    stats->forward_steps = A.fwd_steps;
+    stats->adjoint_steps = A.adj_steps;
+    stats->kernel_launches = A.launches;
+  }
+  return HC_OK;
+}
+
+
+template <class R>
+int objective_forward(hc_ctx* c, int nsteps, const hc_objective* obj, const double* rates_in, double* rates_out,
+                      double* J) {
+  Adj<R> A;
+  if (int st = setup(A, c, nsteps, 0, obj)) return st;
+  if (int st = forward_pass(A, rates_in)) return st;
+  return finish_stats(A, J, rates_out, nullptr);
+}
+
+template <class R>
+int adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
+                     double* q0_bar, double* ref_bar, double* rates_out, hc_adjoint_stats* stats) {
+  Adj<R> A;
+  if (int st = setup(A, c, nsteps, snapshots, obj)) return st;
+  cudaEvent_t e0, e1, e2;
+  HC_CUDA(cudaEventCreate(&e0));
+  HC_CUDA(cudaEventCreate(&e1));
+  HC_CUDA(cudaEventCreate(&e2));
+  std::vector<int> stack;
+  for (int k = snapshots - 1; k >= 0; --k) stack.push_back(k);
+  Schedule sched;
+  sched.build(nsteps, snapshots);
+  const std::vector<std::pair<int, int>> stores = first_descent(sched, nsteps, snapshots, stack);
+  cudaEventRecord(e0, A.s());
+  if (int st = forward_pass(A, rates_in, stores)) return st;
+  cudaEventRecord(e1, A.s());
+  // adjoint of the final state
+  if (A.obj.kind == HC_OBJ_DRAG) {
+    if (int st = res_adj<R>(A, A.sq[0], nullptr, nullptr, A.lam, true, A.obj.scale / A.nsteps)) return st;
+  } else {
+    l2_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(A.sq[0], A.target, A.n, A.obj.weight[0], A.obj.weight[1],
+                                                  A.obj.weight[2], A.obj.weight[3], nullptr, 1, A.lam);
+    A.launches += 1;
+  }
+  if (int st = reverse(A, sched, 0, nsteps, -1, stack, true)) return st;
+  cudaEventRecord(e2, A.s());
+  HC_CUDA(cudaStreamSynchronize(A.s()));
+  float ms_f = 0, ms_t = 0;
+  cudaEventElapsedTime(&ms_f, e0, e1);
+  cudaEventElapsedTime(&ms_t, e0, e2);
+  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+  auto fetch = [&](double* dst, const R* src, size_t m) -> int {
+    if constexpr (std::is_same<R, double>::value) {
+      HC_CUDA(cudaMemcpy(dst, src, m * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+      std::vector<R> tmp(m);
+      HC_CUDA(cudaMemcpy(tmp.data(), src, m * sizeof(R), cudaMemcpyDeviceToHost));
+      for (size_t k = 0; k < m; ++k) dst[k] = double(tmp[k]);
+    }
+    return HC_OK;
+  };
+  if (q0_bar) if (int st = fetch(q0_bar, A.lam, 4 * A.n)) return st;
+  if (ref_bar) {
+    size_t off = 0;
+    for (int s = 0; s < 4; ++s) {
+      const size_t m = 4 * size_t(c->nface(s));
+      if (int st = fetch(ref_bar + off, A.refbar[s], m)) return st;
+      off += m;
+    }
+  }
+  if (int st = finish_stats(A, nullptr, rates_out, stats)) return st;
+  if (stats) {
+    stats->ms_forward = ms_f;
+    stats->ms_total = ms_t;
+    stats->ms_recompute = A.recompute_ms();
+  }
+  return HC_OK;
+}
+
+
+}  // namespace adj
+}  // namespace hc

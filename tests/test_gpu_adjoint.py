@@ -200,3 +200,21 @@ def test_gradient_matches_fp64_reference(flux, limiter, rk, kind):
     ad = float(np.sum(g * dq) + np.sum(refb[1] * dref[1]))
     assert abs(J - Jo) <= 1e-12 * abs(Jo)
     assert abs(ad - dJo) <= 1e-9 * abs(dJo), (ad, dJo)
+
+
+def test_fp32_adjoint_matches_fp64():
+    """FP32 context: forward, recomputation and reverse sweep in FP32 (rates, timesteps
+    and J in FP64) against the FP64 gradient on a Gaussian-sum instance."""
+    rng = np.random.default_rng(8)
+    mesh, bc, ref, q, sp = cases.gaussian_sum(48, 40, rng, base=(0.5, 0.25, 5.0, 1.0))
+    target = cases.gaussian_sum(48, 40, np.random.default_rng(9), base=(0.5, 0.25, 5.0, 1.0))[3]
+    out = {}
+    for prec in ("fp64", "fp32"):
+        s = Solver(mesh, bc, ref, flux="rusanov", limiter="vanalbada", rk="ssp34", precision=prec, dt="global",
+                   cfl=0.5, species=sp)
+        s.set_state(q)
+        J, g, refb, rates, st = s.gradient(20, snapshots=4, kind="l2", target=target)
+        out[prec] = (J, g)
+    (ja, ga), (jb, gb) = out["fp64"], out["fp32"]
+    assert abs(jb - ja) <= 1e-5 * abs(ja)
+    assert np.abs(gb - ga).max() <= 1e-3 * np.abs(ga).max()
