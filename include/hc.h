@@ -201,10 +201,12 @@ int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, d
  * residual and of the RK update, with the timestep of every step frozen at the
  * value of the forward run ("rates": the per-step max lambda/V, returned so a
  * finite-difference check can replay them).  Binomial checkpointing keeps
- * `snapshots` states.  HC_FP64 contexts, or HC_FP64_DF contexts (forward,
- * replayed and recomputed steps in double-float stage arithmetic, the reverse
- * sweep in FP64); Roe or Rusanov; NoLimit1/2/3, van Albada, MinMod, van Leer;
- * periodic, fixed and wall boundaries; global timestep.
+ * `snapshots` states.  HC_FP64 contexts, HC_FP64_DF contexts (forward, replayed
+ * and recomputed steps in double-float stage arithmetic, the face reverse in
+ * double-float, the other reverse passes in FP64) or HC_FP32 contexts (FP32
+ * throughout; rates, timesteps and J in FP64); Euler law; Roe or Rusanov;
+ * NoLimit1/2/3, van Albada, MinMod, van Leer; periodic, fixed and wall
+ * boundaries; global timestep.
  * ------------------------------------------------------------------------- */
 typedef enum { HC_OBJ_DRAG = 0, HC_OBJ_L2 = 1 } hc_objective_kind;
 

@@ -204,13 +204,16 @@ def test_gradient_matches_fp64_reference(flux, limiter, rk, kind):
 
 def test_fp32_adjoint_matches_fp64():
     """FP32 context: forward, recomputation and reverse sweep in FP32 (rates, timesteps
-    and J in FP64) against the FP64 gradient on a Gaussian-sum instance."""
+    and J in FP64) against the FP64 gradient on a Gaussian-sum instance, with a smooth
+    reconstruction.  (With a limiter the two precisions can take different branches
+    where the state is uniform up to round-off -- far from the Gaussians -- and the
+    gradients there differ by O(1) of the local adjoint.)"""
     rng = np.random.default_rng(8)
     mesh, bc, ref, q, sp = cases.gaussian_sum(48, 40, rng, base=(0.5, 0.25, 5.0, 1.0))
     target = cases.gaussian_sum(48, 40, np.random.default_rng(9), base=(0.5, 0.25, 5.0, 1.0))[3]
     out = {}
     for prec in ("fp64", "fp32"):
-        s = Solver(mesh, bc, ref, flux="rusanov", limiter="vanalbada", rk="ssp34", precision=prec, dt="global",
+        s = Solver(mesh, bc, ref, flux="rusanov", limiter="nolimit3", rk="ssp34", precision=prec, dt="global",
                    cfl=0.5, species=sp)
         s.set_state(q)
         J, g, refb, rates, st = s.gradient(20, snapshots=4, kind="l2", target=target)
