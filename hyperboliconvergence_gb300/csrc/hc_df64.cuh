@@ -5,10 +5,10 @@
 // Algorithms: error-free transformations of Knuth (TwoSum, TAOCP vol. 2,
 // 4.2.2) and Dekker ("A floating-point technique for extending the available
 // precision", Numer. Math. 18, 1971; Fast2Sum), products through the fused
-// multiply-add (the residual a*b - fl(a*b) is one FMA), division by one Newton
-// correction of the FP32 quotient and square root by one Newton correction of
-// the FP32 root (Karp & Markstein, "High-precision division and square root",
-// ACM TOMS 23(4), 1997).  The exponent range is FP32's.
+// multiply-add (the residual a*b - fl(a*b) is one FMA), division by two
+// remainder corrections of an FP32 quotient estimate and square root by one
+// Newton correction of the FP32 root (Karp & Markstein, "High-precision division
+// and square root", ACM TOMS 23(4), 1997).  The exponent range is FP32's.
 //
 // Written for __host__ and __device__ so the same code is testable on a CPU.
 // The type and its functions live in hc::dd and are found by argument-dependent
@@ -55,11 +55,14 @@ __host__ __device__ __forceinline__ df64 fast_two_sum(float a, float b) {
   return df64(s, e);
 }
 
+// One TwoSum on the high parts, the low parts added in FP32: the error is bounded
+// by ~2^-47 (|a| + |b|), relative to the operands rather than to the sum (the
+// form with a second TwoSum on the low parts is relative to the sum but costs
+// twice the instructions; no quantity of the stage needs more than
+// operand-relative accuracy in a difference).
 __host__ __device__ __forceinline__ df64 operator+(df64 a, df64 b) {
   const df64 s = two_sum(a.hi, b.hi);
-  const df64 t = two_sum(a.lo, b.lo);
-  df64 r = fast_two_sum(s.hi, s.lo + t.hi);
-  return fast_two_sum(r.hi, r.lo + t.lo);
+  return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
 }
 __host__ __device__ __forceinline__ df64 operator-(df64 a) { return df64(-a.hi, -a.lo); }
 __host__ __device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + (-b); }
@@ -76,14 +79,31 @@ __host__ __device__ __forceinline__ df64 mul_f(df64 a, float b) {
   e = df_fma(a.lo, b, e);
   return fast_two_sum(p, e);
 }
+// FP32 reciprocal estimate of b.hi from the approximate-reciprocal instruction
+__host__ __device__ __forceinline__ float approx_rcp(float x) {
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return 1.0f / x;
+#endif
+}
+// Quotient estimate q1 = a.hi / b.hi from the reciprocal estimate, then two
+// corrections by the remainders a - b q (Karp & Markstein): each multiplies the
+// relative error by that of the estimate (~2^-22), ending near 2^-47.
 __host__ __device__ __forceinline__ df64 operator/(df64 a, df64 b) {
-  const float q1 = a.hi / b.hi;
+  // the approximate reciprocal flushes subnormal inputs and results: take it of
+  // b.hi scaled by a power of two into range, then undo the scaling (exact)
+  const float bh = fabsf(b.hi);
+  const float sc = bh > 0x1p125f ? 0x1p-64f : (bh < 0x1p-125f ? 0x1p64f : 1.0f);
+  const float rb = approx_rcp(b.hi * sc) * sc;
+  const float q1 = a.hi * rb;
   const df64 r = a - mul_f(b, q1);
-  const float q2 = r.hi / b.hi;
+  const float q2 = r.hi * rb;
   const df64 q = fast_two_sum(q1, q2);
-  // second correction brings the quotient to ~2^-47 relative
   const df64 r2 = a - b * q;
-  return fast_two_sum(q.hi, q.lo + r2.hi / b.hi);
+  return fast_two_sum(q.hi, q.lo + r2.hi * rb);
 }
 __host__ __device__ __forceinline__ df64& operator+=(df64& a, df64 b) { return a = a + b; }
 __host__ __device__ __forceinline__ df64& operator-=(df64& a, df64 b) { return a = a - b; }

@@ -394,8 +394,18 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   flag_nonphysical(a.info, qn, int(c));
 }
 
+// Resident CTAs per SM the stage kernel is compiled for (measured on the 512x1024
+// O-grid, 256-thread tiles): FP64 2 (its 122 registers; a looser bound lets the
+// compiler take more and costs 13%), double-float 3 and FP32 5 (latency-bound
+// kernels: the extra warps outweigh the few spilled registers, 10-12% faster).
+template <class R, class C, int NT> struct StageResidency {
+  static constexpr int value = std::is_same<R, float>::value ? 1280 / NT
+                               : (std::is_same<C, R>::value ? 512 / NT : 768 / NT);
+};
+
 template <int TI, int TJ, class R, int FK, class C = R>
-__global__ void __launch_bounds__(TI * TJ) stage_kernel(const StageArgs<R> a) {
+__global__ void __launch_bounds__(TI * TJ, (StageResidency<R, C, TI * TJ>::value))
+    stage_kernel(const StageArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   stage_tile<TI, TJ, R, FK, C>(a, blockIdx.y, blockIdx.x, smem_raw);
 }
@@ -505,10 +515,10 @@ template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const B
   return a;
 }
 
-// resident CTAs per SM the persistent kernel is compiled for: the plain FP32
-// stage kernel's 64 registers a thread (4 CTAs of 256 threads), FP64 2 CTAs
+// resident CTAs per SM the persistent kernel is compiled for: those of the plain
+// stage kernel (StageResidency)
 template <class R, int NT> struct BatchResidency {
-  static constexpr int value = (sizeof(R) == 4 ? 1024 : 512) / NT;
+  static constexpr int value = StageResidency<R, R, NT>::value;
 };
 
 template <int TI, int TJ, class R, int FK>
