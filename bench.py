@@ -56,14 +56,40 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic_per_cell():
-    """dram bytes per cell per stage launch from the committed ncu summary, if any."""
+def profile_value(key: str):
+    """A figure recorded in the committed FP64 stage-kernel summary, if any."""
     if not os.path.exists(PROFILE_TRAFFIC):
         return None
     for line in open(PROFILE_TRAFFIC):
-        if line.startswith("traffic_bytes_per_cell_stage:"):
+        if line.startswith(key + ":"):
             return float(line.split(":", 1)[1].split()[0])
     return None
+
+
+def profiled_traffic_per_cell():
+    """dram bytes per cell per stage launch from the committed ncu summary, if any."""
+    return profile_value("traffic_bytes_per_cell_stage")
+
+
+def fp64_peak_tflops(n: int = 4096, reps: int = 5):
+    """FP64 peak measured here: a float64 GEMM through cuBLAS (2 n^3 per call), best
+    of `reps`, CUDA events."""
+    import torch
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = None
+    for _ in range(reps):
+        e0, e1 = _events()
+        torch.cuda.synchronize()
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del a, b
+    return 2.0 * n ** 3 / (best / 1e3) / 1e12
 
 
 class ClockSampler:
@@ -156,8 +182,10 @@ def _events():
 def measure_precision(stream, steps: int, prec: str):
     """The same workload at another precision ("fp32": everything FP32; "fp64_df":
     FP64 storage with double-float stage arithmetic): throughput, HBM roofline
-    and the relative L-inf difference of the conserved variables from FP64 after
-    one step and after 20 steps from the same start."""
+    and the relative L-inf difference of the conserved quantities from FP64 after
+    one step and after 20 steps from the same start (the two momentum components
+    against the momentum scale: one step from the uniform freestream the normal
+    momentum is still small)."""
     import torch
     from hyperboliconvergence_gb300 import cases
     from hyperboliconvergence_gb300.solver import Solver
@@ -198,8 +226,13 @@ def measure_precision(stream, steps: int, prec: str):
         return np.stack([r * u, r * v, r, p / (g - 1) + 0.5 * r * (u * u + v * v)])
 
     def rel(a, b):
+        # relative L-inf per conserved quantity: mass, momentum (both components
+        # against the momentum scale), energy
         ca, cb = cons(a), cons(b)
-        return float((np.abs(ca - cb).reshape(4, -1).max(1) / np.abs(cb).reshape(4, -1).max(1)).max())
+        err = np.abs(ca - cb).reshape(4, -1).max(1)
+        scale = np.abs(cb).reshape(4, -1).max(1)
+        scale[0:2] = scale[0:2].max()
+        return float((err / scale).max())
     out["error_vs_fp64_after_1_step"] = rel(states[prec][0], states["fp64"][0])
     out["error_vs_fp64_after_20_steps"] = rel(states[prec][1], states["fp64"][1])
     return out
@@ -514,6 +547,18 @@ def run_gpu(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": cfg, "roofline": roof, "e2e": e2e, "gpu_launches": int(launches),
                 "clocks": clk.summary()}
+        # the roof that binds the FP64 stage kernel: FP64 arithmetic, with the
+        # algorithmic FLOPs of the oracle's operation tally (recorded in profiles/)
+        fpc = profile_value("algorithmic_flops_per_cell_stage")
+        if fpc is not None:
+            try:
+                pk = fp64_peak_tflops()
+                ach = fpc * ncell / (stage_ms / 1e3) / 1e12
+                line["fp64_roofline"] = {"bound": "fp64", "achieved": ach, "peak": pk, "unit": "TFLOP/s",
+                                         "frac": ach / pk, "flops_per_cell_stage": fpc,
+                                         "peak_source": "measured here: float64 GEMM 4096^3 (cuBLAS), best of 5"}
+            except Exception as exc:  # reported, not fatal
+                line["fp64_roofline"] = {"error": f"{type(exc).__name__}: {exc}"}
         if world == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline()
         extras = [] if args.no_extras else [e for e in args.extras.split(",") if e]

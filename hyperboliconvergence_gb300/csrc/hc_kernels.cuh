@@ -515,10 +515,11 @@ template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const B
   return a;
 }
 
-// resident CTAs per SM the persistent kernel is compiled for: those of the plain
-// stage kernel (StageResidency)
+// resident CTAs per SM the persistent kernel is compiled for (measured on the
+// uneven 256-instance batch): FP32 4 -- 64 registers; its per-work-item loop
+// spills more than the plain kernel at 5 CTAs/SM and runs 6% slower -- and FP64 2
 template <class R, int NT> struct BatchResidency {
-  static constexpr int value = StageResidency<R, R, NT>::value;
+  static constexpr int value = (sizeof(R) == 4 ? 1024 : 512) / NT;
 };
 
 template <int TI, int TJ, class R, int FK>
