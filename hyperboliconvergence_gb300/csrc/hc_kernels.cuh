@@ -105,9 +105,12 @@ template <class R> __device__ __forceinline__ void flag_nonphysical(StepInfo* in
 // cons(q0) + tot*fac -> primitive (spatial/eulerForwardUpdate.h:76-85)
 template <class R> __device__ __forceinline__ void forward_update(const Gas<R>& g, const R* q0, const R* tot, R fac,
                                                                   R* qn) {
-  const St<R> s0 = prim_state(g, q0[0], q0[1], q0[2], q0[3]);
+  // conserved set of q0: r u, r v, r, r h - p = p/(gamma-1) + r |u|^2/2
   R qc[4];
-  state_cons(s0, qc);
+  R u2 = q0[0] * q0[0];
+  u2 += q0[1] * q0[1];
+  qc[0] = q0[2] * q0[0]; qc[1] = q0[2] * q0[1]; qc[2] = q0[2];
+  qc[3] = fma(q0[3], g.gamma1, q0[2] * (R(0.5) * u2));  // one contraction, whatever the kernel
 #pragma unroll
   for (int v = 0; v < 4; ++v) qc[v] = qc[v] + tot[v] * fac;
   const St<R> s1 = cons_state(g, qc);
@@ -243,14 +246,33 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
           const C wlx = rd(F_WLX), wly = rd(F_WLY), sl = rd(F_SL);
           const C wrx = rd(F_WRX), wry = rd(F_WRY), sr = rd(F_SR);
           C qL[4], qR[4];
+          if constexpr (std::is_same<C, double>::value) {
+            // FP64: the four variables of each side share the limiter's division
+            C gc[4], gl[4], gr[4], sL[4], sR[4];
 #pragma unroll
-          for (int v = 0; v < 4; ++v) {
-            const C dq = qr[v] - ql[v];
-            const C gc = dq * idlr;
-            const C gl = (M(2 * v, la_l, lb_l) * wlx + M(2 * v + 1, la_l, lb_l) * wly) - dq * sl;
-            const C gr = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
-            qL[v] = ql[v] + dl * limit<C>(lim, gc, gl);
-            qR[v] = qr[v] - dr * limit<C>(lim, gc, gr);
+            for (int v = 0; v < 4; ++v) {
+              const C dq = qr[v] - ql[v];
+              gc[v] = dq * idlr;
+              gl[v] = (M(2 * v, la_l, lb_l) * wlx + M(2 * v + 1, la_l, lb_l) * wly) - dq * sl;
+              gr[v] = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
+            }
+            limit4<C>(lim, gc, gl, sL);
+            limit4<C>(lim, gc, gr, sR);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+              qL[v] = ql[v] + dl * sL[v];
+              qR[v] = qr[v] - dr * sR[v];
+            }
+          } else {
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+              const C dq = qr[v] - ql[v];
+              const C gc = dq * idlr;
+              const C gl = (M(2 * v, la_l, lb_l) * wlx + M(2 * v + 1, la_l, lb_l) * wly) - dq * sl;
+              const C gr = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
+              qL[v] = ql[v] + dl * limit<C>(lim, gc, gl);
+              qR[v] = qr[v] - dr * limit<C>(lim, gc, gr);
+            }
           }
           F = face_flux<C, FK>(g, nx, ny, A, prim_state(g, qL[0], qL[1], qL[2], qL[3]),
                                prim_state(g, qR[0], qR[1], qR[2], qR[3]));

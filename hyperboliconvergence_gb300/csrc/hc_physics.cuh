@@ -59,7 +59,7 @@ template <class R> __host__ __device__ inline Gas<R> make_gas(double gamma, doub
 }
 
 // State<Euler,2> without the unused temperature (conservationLaws/euler/euler.h:62-83)
-template <class R> struct St { R p, r, h, u2, a2, u, v; };
+template <class R> struct St { R p, r, h, u2, a2, u, v, ir; };  // ir = 1/r
 
 template <class R> struct Flux5 { R f[4]; R lam; };
 
@@ -70,8 +70,9 @@ template <class R> __host__ __device__ __forceinline__ St<R> prim_state(const Ga
   s.u2 = u * u;
   s.u2 += v * v;
   const R k = R(0.5) * s.u2;
-  const R t = p / (r * g.Rgas);
-  s.a2 = g.gamma * g.Rgas * t;
+  // a2 = gamma R T with T = p/(r R): gamma p / r, through 1/r (kept for the flux)
+  s.ir = R(1) / r;
+  s.a2 = g.gamma * (p * s.ir);
   s.h = s.a2 * g.gamma1 + k;
   s.p = p; s.r = r;
   return s;
@@ -87,8 +88,8 @@ template <class R> __host__ __device__ __forceinline__ St<R> cons_state(const Ga
   s.u2 += s.v * s.v;
   const R k = R(0.5) * s.u2;
   const R p = g.gm1 * (re - r * k);
-  const R t = p / (g.Rgas * r);
-  s.a2 = g.gamma * g.Rgas * t;
+  s.ir = r1;
+  s.a2 = g.gamma * (p * r1);
   s.h = s.a2 * g.gamma1 + k;
   s.p = p; s.r = r;
   return s;
@@ -102,10 +103,9 @@ template <class R> __host__ __device__ __forceinline__ void state_cons(const St<
 // projectedVelocity (conservationLaws/base/base.h:148-158)
 template <class R> __host__ __device__ __forceinline__ R proj(R nx, R ny, const St<R>& s) { return nx * s.u + ny * s.v; }
 
-// exactFlux (conservationLaws/euler/fluxes/exactFlux.ipp:231-263)
-template <class R> __host__ __device__ __forceinline__ Flux5<R> exact_flux(R nx, R ny, const St<R>& s) {
+// exactFlux (conservationLaws/euler/fluxes/exactFlux.ipp:231-263); a = sqrt(a2)
+template <class R> __host__ __device__ __forceinline__ Flux5<R> exact_flux_a(R nx, R ny, const St<R>& s, R a) {
   Flux5<R> o;
-  const R a = sqrt(s.a2);
   const R un = proj(nx, ny, s);
   const R mn = s.r * un;
   o.f[0] = mn * s.u + s.p * nx;
@@ -115,15 +115,23 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> exact_flux(R nx,
   o.lam = fabs(un) + a;
   return o;
 }
+template <class R> __host__ __device__ __forceinline__ Flux5<R> exact_flux(R nx, R ny, const St<R>& s) {
+  return exact_flux_a(nx, ny, s, sqrt(s.a2));
+}
 
-// CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:25-37)
-template <class R> __host__ __device__ __forceinline__ Flux5<R> central_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
-  const Flux5<R> fl = exact_flux(nx, ny, l), fr = exact_flux(nx, ny, r);
+// CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:25-37), sound speeds given
+template <class R>
+__host__ __device__ __forceinline__ Flux5<R> central_flux_a(R nx, R ny, R A, const St<R>& l, const St<R>& r, R al,
+                                                            R ar) {
+  const Flux5<R> fl = exact_flux_a(nx, ny, l, al), fr = exact_flux_a(nx, ny, r, ar);
   Flux5<R> o;
 #pragma unroll
   for (int i = 0; i < 4; ++i) o.f[i] = (R(0.5) * (fl.f[i] + fr.f[i])) * A;
   o.lam = fmax(fl.lam, fr.lam) * A;
   return o;
+}
+template <class R> __host__ __device__ __forceinline__ Flux5<R> central_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
+  return central_flux_a(nx, ny, A, l, r, sqrt(l.a2), sqrt(r.a2));
 }
 
 // Roe flux = central + matrix dissipation (conservationLaws/base/fluxes/roeFlux.ipp:39-95),
@@ -133,9 +141,10 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> central_flux(R n
 // is rotated to the face frame, exactly as the reference composes them.
 template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g, R nx, R ny, R A,
                                                                const St<R>& l, const St<R>& r) {
-  const Flux5<R> c = central_flux(nx, ny, A, l, r);
-  // roe average
-  const R cr = sqrt(r.r / l.r);
+  const R al = sqrt(l.a2), ar = sqrt(r.a2);
+  const Flux5<R> c = central_flux_a(nx, ny, A, l, r, al, ar);
+  // roe average: cr = sqrt(rR/rL), ra = cr rL, 1/ra = cr/rR
+  const R cr = sqrt(r.r * l.ir);
   const R wl = R(1) / (R(1) + cr);
   const R wr = R(1) - wl;
   const R ra = cr * l.r;
@@ -150,7 +159,6 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const G
   // wave speeds and entropy fix
   const R una = nx * ua + ny * va;
   const R unl = proj(nx, ny, l), unr = proj(nx, ny, r);
-  const R al = sqrt(l.a2), ar = sqrt(r.a2);
   R lam[4];
   const R la0 = fabs(una);
   lam[0] = la0; lam[3] = la0;
@@ -175,7 +183,7 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const G
   const R c0 = nx * d0 + ny * d1;
   const R c1 = tx * d0 + ty * d1;
   // conserved -> primitive about the average state
-  const R rho1 = R(1) / ra;
+  const R rho1 = cr * r.ir;
   R cc = ka * d2 + d3;
   const R du0 = (c0 - ua * d2) * rho1;
   cc -= ua * c0;
@@ -324,6 +332,50 @@ __host__ __device__ __forceinline__ Flux5<R> face_flux(const Gas<R>& g, R nx, R 
   else if constexpr (FK == FLUX_AUSMPUP) return ausmpup_flux(g, nx, ny, A, l, r);
   else if constexpr (FK == FLUX_RUSANOV) return rusanov_flux(nx, ny, A, l, r);
   else return central_flux(nx, ny, A, l, r);
+}
+
+template <class R> __host__ __device__ __forceinline__ R limit(int kind, R a, R b);
+
+// The limiter of the four variables of one face side, limit(a[v], b[v]).  van
+// Albada's four quotients share one division (batched inversion: 1/d_v from the
+// inverse of the product of the denominators and the partial products), when that
+// product and its partial products stay within [1e-280, 1e280]; otherwise, and for
+// the other limiters, one call per variable.
+template <class R> __host__ __device__ __forceinline__ void limit4(int kind, const R* a, const R* b, R* out) {
+  if (kind == LIM_VANALBADA) {
+    const R tiny = Lim<R>::tiny();
+    R num[4], den[4], pre[4];
+    R acc = R(1);
+    bool ok = true, any = false;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const bool on = !(a[v] * b[v] <= R(0));  // a*b <= 0: the limited slope is 0 exactly
+      // explicit contractions: the same rounding in every kernel that inlines this
+      num[v] = on ? fma(b[v], a[v] * a[v], a[v] * (b[v] * b[v])) : R(0);
+      den[v] = on ? fma(a[v], a[v], b[v] * b[v]) + tiny : R(1);
+      any = any || on;
+      pre[v] = acc;
+      acc = acc * den[v];
+      ok = ok && acc >= R(1e-280) && acc <= R(1e280);
+    }
+    if (!any) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) out[v] = R(0);
+    } else if (ok) {
+      R inv = R(1) / acc;
+#pragma unroll
+      for (int v = 3; v >= 0; --v) {
+        out[v] = num[v] * (inv * pre[v]);
+        inv = inv * den[v];
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) out[v] = num[v] / den[v];
+    }
+    return;
+  }
+#pragma unroll
+  for (int v = 0; v < 4; ++v) out[v] = limit<R>(kind, a[v], b[v]);
 }
 
 // Slope limiters (limiters/limiter.ipp:141-297), called as limit(central, biased).
