@@ -24,11 +24,11 @@ template <class R> __host__ __device__ __forceinline__ void prim_state_adj(const
   // u2 = u*u + v*v
   sb.u += R(2) * q[0] * sb.u2;
   sb.v += R(2) * q[1] * sb.u2;
-  // a2 = gamma*R*t, t = p/(r*R)
-  const R tbar = g.gamma * g.Rgas * sb.a2;
-  const R t = q[3] / (q[2] * g.Rgas);
-  sb.p += tbar / (q[2] * g.Rgas);
-  sb.r -= tbar * t / q[2];
+  // a2 = gamma*R*t, t = p/(r*R): d a2/dp = gamma/r, d a2/dr = -gamma p/r^2
+  const R ir = R(1) / q[2];
+  const R gb = g.gamma * ir * sb.a2;
+  sb.p += gb;
+  sb.r -= gb * (q[3] * ir);
   qbar[0] += sb.u;
   qbar[1] += sb.v;
   qbar[2] += sb.r;
@@ -80,8 +80,10 @@ __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R n
                                              const R* Fbar, R* qlbar, R* qrbar) {
   const St<R> l = prim_state(g, ql[0], ql[1], ql[2], ql[3]);
   const St<R> r = prim_state(g, qr[0], qr[1], qr[2], qr[3]);
-  // ---- forward recomputation
-  const R cr = sqrt(r.r / l.r);
+  // ---- forward recomputation (reciprocals: l.ir = 1/rL, r.ir = 1/rR, a1 = 1/aa)
+  const R z = r.r * l.ir;
+  const R cr = sqrt(z);
+  const R icr = cr * l.r * r.ir;  // 1/cr
   const R wl = R(1) / (R(1) + cr);
   const R wr = R(1) - wl;
   const R ra = cr * l.r;
@@ -109,7 +111,7 @@ __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R n
   const R d3 = (r.r * r.h - r.p) - (l.r * l.h - l.p);
   const R c0 = nx * d0 + ny * d1;
   const R c1 = tx * d0 + ty * d1;
-  const R rho1 = R(1) / ra;
+  const R rho1 = cr * r.ir;  // 1/ra
   const R cc = ka * d2 + d3 - ua * c0 - va * c1;
   const R du0 = (c0 - ua * d2) * rho1;
   const R du1 = (c1 - va * d2) * rho1;
@@ -142,10 +144,10 @@ __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R n
   rab += du * e0b; dub += ra * e0b; uab += drr * e0b; drrb += ua * e0b;
   R w3b = dvb;
   R w1b = R(0.5) * dub, w2b = R(0.5) * dub;
-  dppb += drrb / (aa * aa);
-  R aab = R(-2) * dpp / (aa * aa * aa) * drrb;
-  rab += -w0 / g.gamma * drrb;
-  R w0b = -ra / g.gamma * drrb;
+  dppb += drrb * (a1 * a1);
+  R aab = R(-2) * dpp * (a1 * a1 * a1) * drrb;
+  rab += -w0 * g.inv_gamma * drrb;
+  R w0b = -ra * g.inv_gamma * drrb;
   rab += R(0.5) * aa * (w2 - w1) * dppb;
   aab += R(0.5) * ra * (w2 - w1) * dppb;
   w2b += R(0.5) * ra * aa * dppb;
@@ -193,12 +195,12 @@ __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R n
   aab += la2b - la1b;
   const R unlb = ll1b + ll2b, unrb = lr1b + lr2b;
   const R alb = ll2b - ll1b, arb = lr2b - lr1b;
-  lb.a2 += alb / (R(2) * al);
-  rb.a2 += arb / (R(2) * ar);
+  lb.a2 += alb * (R(0.5) / al);
+  rb.a2 += arb * (R(0.5) / ar);
   lb.u += nx * unlb; lb.v += ny * unlb;
   rb.u += nx * unrb; rb.v += ny * unrb;
   uab += nx * unab; vab += ny * unab;
-  const R a2ab = aab / (R(2) * aa);
+  const R a2ab = aab * (R(0.5) * a1);
   const R hab = g.gm1 * a2ab;
   kab -= g.gm1 * a2ab;
   uab += ua * kab; vab += va * kab;
@@ -211,10 +213,9 @@ __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R n
   lb.r += cr * rab;
   wlb -= wrb;
   crb += -wl * wl * wlb;
-  const R z = r.r / l.r;
-  const R zb = crb / (R(2) * cr);
-  rb.r += zb / l.r;
-  lb.r -= zb * z / l.r;
+  const R zb = crb * (R(0.5) * icr);
+  rb.r += zb * l.ir;
+  lb.r -= zb * z * l.ir;
   // central part: c.f[i] = 0.5*(fl[i]+fr[i])*A
   R fe[4];
 #pragma unroll
@@ -274,9 +275,10 @@ template <class R> __host__ __device__ __forceinline__ void limit_grad(int kind,
       if (a * b < R(0)) return;
       // z = num/den; dz = (dnum - z*dden)/den (no den^2: it underflows at a = b = 0)
       const R num = b * (a * a) + a * (b * b), den = a * a + b * b + tiny;
-      const R z = num / den;
-      *da = ((R(2) * a * b + b * b) - z * R(2) * a) / den;
-      *db = ((a * a + R(2) * a * b) - z * R(2) * b) / den;
+      const R iden = R(1) / den;
+      const R z = num * iden;
+      *da = ((R(2) * a * b + b * b) - z * R(2) * a) * iden;
+      *db = ((a * a + R(2) * a * b) - z * R(2) * b) * iden;
       return;
     }
     case LIM_MINMOD:
@@ -285,9 +287,10 @@ template <class R> __host__ __device__ __forceinline__ void limit_grad(int kind,
       return;
     case LIM_VANLEER: {
       const R num = a * fabs(b) + fabs(a) * b, den = fabs(a) + fabs(b) + tiny;
-      const R z = num / den;
-      *da = ((fabs(b) + sgn(a) * b) - z * sgn(a)) / den;
-      *db = ((a * sgn(b) + fabs(a)) - z * sgn(b)) / den;
+      const R iden = R(1) / den;
+      const R z = num * iden;
+      *da = ((fabs(b) + sgn(a) * b) - z * sgn(a)) * iden;
+      *db = ((a * sgn(b) + fabs(a)) - z * sgn(b)) * iden;
       return;
     }
     default: return;  // other limiters are not differentiated
