@@ -92,6 +92,10 @@ template <class R> AdjArgs<R> adj_args(Adj<R>& A) {
 }
 
 inline unsigned blocks(size_t n) { return unsigned((n + 255) / 256); }
+// the face-adjoint kernel holds ~180 registers a thread: small blocks let more
+// warps share an SM than one 256-thread block would
+constexpr int kFaceThreads = 64;
+inline unsigned face_blocks(size_t n) { return unsigned((n + kFaceThreads - 1) / kFaceThreads); }
 
 // one forward step from sq[0] to sq[nst]; record (rec=true) or replay the max rate of step `step`
 template <class R> int forward_step(Adj<R>& A, int step, bool rec) {
@@ -204,15 +208,15 @@ int residual_adjoint(Adj<R>& A, const R* q, const R* rbar, const R* qbar_add, R*
   adj_qm_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
   if constexpr (std::is_same<R, double>::value) {
     if (A.c->df) {  // double-float face arithmetic on HC_FP64_DF contexts
-      adj_face_kernel<double, FK, df64><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
-      adj_face_kernel<double, FK, df64><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+      adj_face_kernel<double, FK, df64><<<face_blocks(A.nfi), kFaceThreads, 0, A.s()>>>(a, 0);
+      adj_face_kernel<double, FK, df64><<<face_blocks(A.nfj), kFaceThreads, 0, A.s()>>>(a, 1);
     } else {
-      adj_face_kernel<double, FK><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
-      adj_face_kernel<double, FK><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+      adj_face_kernel<double, FK><<<face_blocks(A.nfi), kFaceThreads, 0, A.s()>>>(a, 0);
+      adj_face_kernel<double, FK><<<face_blocks(A.nfj), kFaceThreads, 0, A.s()>>>(a, 1);
     }
   } else {
-    adj_face_kernel<R, FK><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
-    adj_face_kernel<R, FK><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+    adj_face_kernel<R, FK><<<face_blocks(A.nfi), kFaceThreads, 0, A.s()>>>(a, 0);
+    adj_face_kernel<R, FK><<<face_blocks(A.nfj), kFaceThreads, 0, A.s()>>>(a, 1);
   }
   adj_qmbar_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a);
   adj_gather_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a);
