@@ -16,7 +16,8 @@ HC_OK, HC_ERR_ARG, HC_ERR_CUDA, HC_ERR_NONPHYSICAL, HC_ERR_TIMEOUT, HC_ERR_UNSUP
 STATUS_NAMES = {0: "HC_OK", 1: "HC_ERR_ARG", 2: "HC_ERR_CUDA", 3: "HC_ERR_NONPHYSICAL",
                 4: "HC_ERR_TIMEOUT", 5: "HC_ERR_UNSUPPORTED"}
 
-FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5}
+FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5, "roe_ws": 6}
+SCALING = {"convective": 0, "acoustic": 1, "adaptive": 2}
 LIMITER = {"nolimit1": 0, "nolimit2": 1, "nolimit3": 2, "vanalbada": 3, "minmod": 4,
            "superbee": 5, "mc": 6, "vanleer": 7, "vanleer_ref": 8, "cada3": 9}
 RK = {"ssp11": 0, "ssp22": 1, "ssp33": 2, "ssp34": 3}
@@ -55,6 +56,7 @@ def _declare(lib):
         "hc_get_stream": [p, C.POINTER(C.c_void_p)],
         "hc_mesh_upload": [p, i, i, dp],
         "hc_set_species": [p, d, d, d],
+        "hc_set_low_mach": [p, i, i, d, d],
         "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],
         "hc_state_upload": [p, dp],
         "hc_state_download": [p, dp],

@@ -19,7 +19,7 @@ import numpy as np
 from .solver import Mesh
 
 GAMMA = 1.4
-R_AIR = 287.058  # get_air_species (conservationLaws/euler/species.ipp:363-379)
+R_AIR = 287.058  # get_air_species (conservationLaws/euler/species.ipp:1-17)
 
 
 def vortex_state(x, y, t=0.0, gamma=GAMMA, beta=5.0, centre=(5.0, 5.0), uinf=(1.0, 1.0), period=10.0):

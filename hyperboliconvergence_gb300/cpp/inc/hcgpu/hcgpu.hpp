@@ -39,7 +39,7 @@ inline void check(int status) {
 }
 
 // Species<Euler> (conservationLaws/euler/euler.h:48-60) and get_air_species
-// (conservationLaws/euler/species.ipp:363-379)
+// (conservationLaws/euler/species.ipp:1-17)
 template <class Real> struct Species {
   Real gamma, minf, lref, nu, pr, dt, R, gamma1;
 };
@@ -50,13 +50,23 @@ template <class Real> Species<Real> get_air_species() {
   return s;
 }
 
+// LowMachScaling (conservationLaws/euler/euler.h:334-339)
+enum class LowMachScaling { Convective = HC_SCALING_CONVECTIVE, Acoustic = HC_SCALING_ACOUSTIC,
+                            Adaptive = HC_SCALING_ADAPTIVE };
+
 // Flux tags: the FluxFunctor plug-in point (conservationLaws/base/concepts.h:97-107)
 struct RoeFlux { static constexpr int id = HC_FLUX_ROE; };
 struct Slau { static constexpr int id = HC_FLUX_SLAU; };
 struct SlauRef { static constexpr int id = HC_FLUX_SLAU_REF; };
-struct AusmPlusUP { static constexpr int id = HC_FLUX_AUSMPUP; };
+template <LowMachScaling VFluxScaling = LowMachScaling::Convective,
+          LowMachScaling PFluxScaling = LowMachScaling::Convective>
+struct AusmPlusUP {
+  static constexpr int id = HC_FLUX_AUSMPUP;
+  static constexpr int vscale = int(VFluxScaling), pscale = int(PFluxScaling);
+};
 struct RusanovFlux { static constexpr int id = HC_FLUX_RUSANOV; };
 struct CentralFlux { static constexpr int id = HC_FLUX_CENTRAL; };
+struct RoeUnprecWS { static constexpr int id = HC_FLUX_ROE_WS; };
 
 // Limiter tags (limiters/limiter.h:46-131)
 namespace Limiters {
@@ -76,9 +86,11 @@ struct Cada3 { static constexpr int id = HC_LIM_CADA3; };
 struct MusclFlux {
   int limiter;
   int flux;
+  int vscale = HC_SCALING_CONVECTIVE, pscale = HC_SCALING_CONVECTIVE;  // AUSM+up's scalings
 };
 template <class Limiter, class Flux> MusclFlux make_muscl_flux(const Limiter&, const Flux&) {
-  return MusclFlux{Limiter::id, Flux::id};
+  if constexpr (requires { Flux::vscale; }) return MusclFlux{Limiter::id, Flux::id, Flux::vscale, Flux::pscale};
+  else return MusclFlux{Limiter::id, Flux::id};
 }
 
 // ODE::Explicit::RungeKutta tables (ode.h:85-197); the id selects the device table
@@ -192,6 +204,7 @@ hc_step_stats integrate(const execution::gpu_policy policy, const UnsteadyTimeCo
   Context ctx(cfg);
   check(hc_mesh_upload(ctx.get(), mesh.ni, mesh.nj, mesh.nodes.data()));
   check(hc_set_species(ctx.get(), species.gamma, species.R, species.minf));
+  check(hc_set_low_mach(ctx.get(), flux2.vscale, flux2.pscale, double(species.lref), double(species.dt)));
   int bct[4];
   const double* refs[4];
   for (int s = 0; s < 4; ++s) {
@@ -219,6 +232,7 @@ hc_steady_stats integrate(const execution::gpu_policy policy, const SteadyTimeCo
   Context ctx(cfg);
   check(hc_mesh_upload(ctx.get(), mesh.ni, mesh.nj, mesh.nodes.data()));
   check(hc_set_species(ctx.get(), species.gamma, species.R, species.minf));
+  check(hc_set_low_mach(ctx.get(), flux2.vscale, flux2.pscale, double(species.lref), double(species.dt)));
   int bct[4];
   const double* refs[4];
   for (int s = 0; s < 4; ++s) {

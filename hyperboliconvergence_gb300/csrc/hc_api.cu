@@ -336,6 +336,16 @@ int hc_set_species(hc_ctx* c, double gamma, double gas_constant, double minf) {
   return HC_OK;
 }
 
+int hc_set_low_mach(hc_ctx* c, int velocity_scaling, int pressure_scaling, double lref, double dt) {
+  if (int st = check_ctx(c)) return st;
+  auto ok = [](int k) { return k >= HC_SCALING_CONVECTIVE && k <= HC_SCALING_ADAPTIVE; };
+  if (!ok(velocity_scaling) || !ok(pressure_scaling)) return fail(HC_ERR_ARG, "unknown low-Mach scaling");
+  if (!(lref > 0.0) || !(dt > 0.0) || !std::isfinite(lref) || !std::isfinite(dt))
+    return fail(HC_ERR_ARG, "lref and dt must be positive and finite");
+  c->vscale = velocity_scaling; c->pscale = pressure_scaling; c->lref = lref; c->sdt = dt;
+  return HC_OK;
+}
+
 int hc_set_bcs(hc_ctx* c, const int bc_type[4], const double* const ref[4]) {
   if (int st = check_ctx(c)) return st;
   if (!c->have_mesh) return fail(HC_ERR_ARG, "upload the mesh before the boundary conditions");

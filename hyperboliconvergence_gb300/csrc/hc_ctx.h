@@ -16,6 +16,8 @@ struct hc_ctx {
   int bc[4] = {-1, -1, -1, -1};
   bool have_mesh = false, have_bcs = false, have_state = false, geom_dirty = true;
   double gamma = 1.4, Rgas = 287.058, minf = 1e-4;
+  double lref = 1., sdt = 1.7976931348623157e308;  // species lref and dt (AUSM+up scaling)
+  int vscale = 0, pscale = 0;                       // AUSM+up LowMachScaling pair
   cudaStream_t own = nullptr, stream = nullptr;
   int tile = hc::TILE_8x32;
   // device buffers
@@ -53,7 +55,7 @@ template <class R> StageArgs<R> base_args(hc_ctx* c) {
   StageArgs<R> a{};
   a.ni = c->ni; a.nj = c->nj;
   for (int k = 0; k < 4; ++k) a.bc[k] = c->bc[k];
-  a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf);
+  a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale);
   a.limiter = c->cfg.limiter;
   a.fi = (const R*)c->fi; a.fj = (const R*)c->fj; a.vol = (const R*)c->vol;
   a.fic = c->fic; a.fjc = c->fjc;

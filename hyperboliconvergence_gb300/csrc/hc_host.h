@@ -58,6 +58,7 @@ template <class R> StageFn<R> stage_fn(int flux) {
     case FLUX_SLAU_REF: return launch_stage<R, FLUX_SLAU_REF>;
     case FLUX_AUSMPUP: return launch_stage<R, FLUX_AUSMPUP>;
     case FLUX_RUSANOV: return launch_stage<R, FLUX_RUSANOV>;
+    case FLUX_ROE_WS: return launch_stage<R, FLUX_ROE_WS>;
     default: return launch_stage<R, FLUX_CENTRAL>;
   }
 }
@@ -68,6 +69,7 @@ template <class R> BatchFn<R> batch_fn(int flux) {
     case FLUX_SLAU_REF: return launch_batch_stage<R, FLUX_SLAU_REF>;
     case FLUX_AUSMPUP: return launch_batch_stage<R, FLUX_AUSMPUP>;
     case FLUX_RUSANOV: return launch_batch_stage<R, FLUX_RUSANOV>;
+    case FLUX_ROE_WS: return launch_batch_stage<R, FLUX_ROE_WS>;
     default: return launch_batch_stage<R, FLUX_CENTRAL>;
   }
 }
@@ -78,6 +80,7 @@ template <class R> cudaError_t prepare(int flux) {
     case FLUX_SLAU_REF: return prepare_stage<R, FLUX_SLAU_REF>();
     case FLUX_AUSMPUP: return prepare_stage<R, FLUX_AUSMPUP>();
     case FLUX_RUSANOV: return prepare_stage<R, FLUX_RUSANOV>();
+    case FLUX_ROE_WS: return prepare_stage<R, FLUX_ROE_WS>();
     default: return prepare_stage<R, FLUX_CENTRAL>();
   }
 }

@@ -124,6 +124,7 @@ template <class C, class R> __device__ __forceinline__ Gas<C> gas_as(const Gas<R
   Gas<C> o;
   o.gamma = cvt<C>(g.gamma); o.gm1 = cvt<C>(g.gm1); o.gamma1 = cvt<C>(g.gamma1);
   o.Rgas = cvt<C>(g.Rgas); o.minf = cvt<C>(g.minf); o.inv_gamma = cvt<C>(g.inv_gamma);
+  o.lref_dt = cvt<C>(g.lref_dt); o.vscale = g.vscale; o.pscale = g.pscale;
   return o;
 }
 

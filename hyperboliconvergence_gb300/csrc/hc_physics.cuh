@@ -16,7 +16,9 @@
 namespace hc {
 
 enum FluxKind { FLUX_ROE = 0, FLUX_SLAU = 1, FLUX_SLAU_REF = 2, FLUX_AUSMPUP = 3,
-                FLUX_RUSANOV = 4, FLUX_CENTRAL = 5, FLUX_COUNT = 6 };
+                FLUX_RUSANOV = 4, FLUX_CENTRAL = 5, FLUX_ROE_WS = 6, FLUX_COUNT = 7 };
+// LowMachScaling (conservationLaws/euler/euler.h:334-339) of AUSM+up's two diffusion terms
+enum LowMachScaling { SCALING_CONVECTIVE = 0, SCALING_ACOUSTIC = 1, SCALING_ADAPTIVE = 2 };
 enum LimiterKind { LIM_NOLIMIT1 = 0, LIM_NOLIMIT2 = 1, LIM_NOLIMIT3 = 2, LIM_VANALBADA = 3,
                    LIM_MINMOD = 4, LIM_SUPERBEE = 5, LIM_MC = 6, LIM_VANLEER = 7,
                    LIM_VANLEER_REF = 8, LIM_CADA3 = 9, LIM_COUNT = 10 };
@@ -43,11 +45,18 @@ template <class R> struct Gas {
   R gm1;        // gamma - 1
   R gamma1;     // 1/(gamma-1)
   R Rgas;       // gas constant
-  R minf;       // cut-off Mach number (AUSM+up)
+  R minf;       // cut-off Mach number (AUSM+up, RoeUnprecWS)
   R inv_gamma;  // 1/gamma
+  R lref_dt;    // lref / dt of the species: AUSM+up's adaptive scaling mu = lref / (as dt)
+  int vscale;   // AUSM+up velocity-diffusion scaling (LowMachScaling)
+  int pscale;   // AUSM+up pressure-diffusion scaling (LowMachScaling)
 };
 
-template <class R> __host__ __device__ inline Gas<R> make_gas(double gamma, double Rgas, double minf) {
+// lref and dt default to the reference's air species (1 and the largest double,
+// conservationLaws/euler/species.ipp:12), where the adaptive ratio vanishes
+template <class R>
+__host__ __device__ inline Gas<R> make_gas(double gamma, double Rgas, double minf, double lref = 1.,
+                                           double dt = 1.7976931348623157e308, int vscale = 0, int pscale = 0) {
   Gas<R> g;
   g.gamma = R(gamma);
   g.gm1 = R(gamma - 1.);
@@ -55,6 +64,9 @@ template <class R> __host__ __device__ inline Gas<R> make_gas(double gamma, doub
   g.Rgas = R(Rgas);
   g.minf = R(minf);
   g.inv_gamma = R(1. / gamma);
+  g.lref_dt = R(lref / dt);
+  g.vscale = vscale;
+  g.pscale = pscale;
   return g;
 }
 
@@ -283,7 +295,8 @@ __host__ __device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St
   return o;
 }
 
-// AUSM+up with (Convective, Convective) tags (conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171)
+// AusmPlusUP<VFluxScaling, PFluxScaling> (conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171), the
+// two scalings chosen at run time (g.vscale, g.pscale; uniform across a launch)
 template <class R> __host__ __device__ __forceinline__ Flux5<R> ausmpup_flux(const Gas<R>& g, R nx, R ny, R A,
                                                                    const St<R>& l, const St<R>& r) {
   const R alpha0 = R(0.1875), beta = R(0.125), Ku = R(0.75 * 2.), Kp = R(0.25), sigma = R(1.0);
@@ -299,17 +312,29 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> ausmpup_flux(con
   // std::clamp(m0, minf, 1) as libstdc++ evaluates it: min(max(m0, minf), 1)
   const R mlo = (m0 < g.minf) ? g.minf : m0;
   const R m0c = (R(1) < mlo) ? R(1) : mlo;
-  const R fa = m0c * (R(2) - m0c);
+  R m0p = m0c, m0u = m0c;
+  if (g.vscale != SCALING_CONVECTIVE || g.pscale != SCALING_CONVECTIVE) {
+    // adaptive: clamp(max(m0, mu), minf, 1), mu = lref / (as dt) the ratio of the acoustic
+    // time scale to the step
+    const R mu = g.lref_dt / as;
+    const R mx = fmax(m0, mu);
+    const R alo = (mx < g.minf) ? g.minf : mx;
+    const R m0a = (R(1) < alo) ? R(1) : alo;
+    m0p = g.pscale == SCALING_CONVECTIVE ? m0c : (g.pscale == SCALING_ACOUSTIC ? R(1) : m0a);
+    m0u = g.vscale == SCALING_CONVECTIVE ? m0c : (g.vscale == SCALING_ACOUSTIC ? R(1) : m0a);
+  }
+  const R fa = m0p * (R(2) - m0p);
+  const R fu = (g.vscale == g.pscale) ? fa : m0u * (R(2) - m0u);
   const bool lsup = fabs(ml) > R(1), rsup = fabs(mr) > R(1);
   const R mlp = lsup ? ms_m1(R(1), ml) : ms_m4(R(1), ml, beta);
   const R mrm = rsup ? ms_m1(R(-1), mr) : ms_m4(R(-1), mr, beta);
   const R delp = r.p - l.p;
   const R mp = Kp * fmax(R(1) - sigma * m0 * m0, R(0)) * delp / (fa * ra * as * as);
   const R uaf = as * (mlp + mrm - mp) * A;
-  const R alpha = alpha0 * (R(5) * fa * fa - R(4));
+  const R alpha = alpha0 * (R(5) * fu * fu - R(4));
   const R plp = lsup ? ms_p1(R(1), ml) : ms_p5(R(1), ml, alpha);
   const R prm = rsup ? ms_p1(R(-1), mr) : ms_p5(R(-1), mr, alpha);
-  const R pu = Ku * plp * prm * ra * (fa * as) * (unr - unl);
+  const R pu = Ku * plp * prm * ra * (fu * as) * (unr - unl);
   const R pa = (plp * l.p + prm * r.p - pu) * A;
   const St<R>& w = (uaf > R(0)) ? l : r;
   const R mdot = uaf * w.r;
@@ -318,9 +343,52 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> ausmpup_flux(con
   o.f[1] = mdot * w.v + pa * ny;
   o.f[2] = mdot;
   o.f[3] = mdot * w.h;
-  const R lmd = R(0.5) * (m0c + R(1)) / fa;
+  const R lmd = R(0.5) * (m0p + R(1)) / fa;
   const R amax = sqrt(fmax(as * as, fmax(l.a2, r.a2)));
   o.lam = (lmd * amax + fmax(fabs(uaf), fmax(fabs(unl), fabs(unr)))) * A;
+  return o;
+}
+
+// RoeUnprecWS (conservationLaws/euler/fluxes/roeUnprecWS.ipp:2-109): the central flux minus a
+// scalar dissipation, |un| times the conserved jump plus velocity and pressure perturbations
+// scaled by the cut-off Mach number (Weiss & Smith's low-Mach form with fixed coefficients)
+template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_ws_flux(const Gas<R>& g, R nx, R ny, R A,
+                                                                  const St<R>& l, const St<R>& r) {
+  const R al = sqrt(l.a2), ar = sqrt(r.a2);
+  const Flux5<R> c = central_flux_a(nx, ny, A, l, r, al, ar);
+  // roe average (conservationLaws/euler/fluxes/roe.ipp:150-196)
+  const R cr = sqrt(r.r * l.ir);
+  const R wl = R(1) / (R(1) + cr);
+  const R wr = R(1) - wl;
+  const R ra = cr * l.r;
+  const R ua = wl * l.u + wr * r.u;
+  const R va = wl * l.v + wr * r.v;
+  R ka = ua * ua;
+  ka += va * va;
+  ka *= R(0.5);
+  const R ha = wl * l.h + wr * r.h;
+  const R aa = sqrt(g.gm1 * (ha - ka));
+  const R una = nx * ua + ny * va;
+  const R dp = r.p - l.p;
+  const R du = proj(nx, ny, r) - proj(nx, ny, l);
+  const R uinf = g.minf * aa;
+  // nu_p = minf / (ra uinf^2), nu_u = 0.05, mu_p = 0.02 minf, mu_u = 0.1 ra uinf minf
+  const R nu_p = (R(1) / (ra * uinf * uinf)) * g.minf;
+  const R mu_u = (R(0.10) * (ra * uinf)) * g.minf;
+  const R dU = nu_p * dp + R(0.05) * du;
+  const R dP = (R(0.02) * g.minf) * dp + mu_u * du;
+  const R aun = fabs(una);
+  const R d0 = r.r * r.u - l.r * l.u;
+  const R d1 = r.r * r.v - l.r * l.v;
+  const R d2 = r.r - l.r;
+  const R d3 = (r.r * r.h - r.p) - (l.r * l.h - l.p);
+  const R s = R(0.5) * A;
+  Flux5<R> o;
+  o.f[0] = c.f[0] - s * ((aun * d0 + dU * (ra * ua)) + dP * nx);
+  o.f[1] = c.f[1] - s * ((aun * d1 + dU * (ra * va)) + dP * ny);
+  o.f[2] = c.f[2] - s * (aun * d2 + dU * ra);
+  o.f[3] = c.f[3] - s * ((aun * d3 + dU * (ra * ha)) + dP * una);
+  o.lam = fmax(c.lam, (aun + aa) * A);
   return o;
 }
 
@@ -331,6 +399,7 @@ __host__ __device__ __forceinline__ Flux5<R> face_flux(const Gas<R>& g, R nx, R 
   else if constexpr (FK == FLUX_SLAU_REF) return slau_flux<R, false>(nx, ny, A, l, r);
   else if constexpr (FK == FLUX_AUSMPUP) return ausmpup_flux(g, nx, ny, A, l, r);
   else if constexpr (FK == FLUX_RUSANOV) return rusanov_flux(nx, ny, A, l, r);
+  else if constexpr (FK == FLUX_ROE_WS) return roe_ws_flux(g, nx, ny, A, l, r);
   else return central_flux(nx, ny, A, l, r);
 }
 

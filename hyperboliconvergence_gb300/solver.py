@@ -63,7 +63,8 @@ class Solver:
     """One mesh, its boundary conditions and state, advanced by explicit RK on the GPU."""
 
     def __init__(self, mesh: Mesh, bc, ref=None, flux="roe", limiter="vanleer", rk="ssp34",
-                 precision="fp64", dt="global", cfl=0.5, species=(1.4, 287.058, 1e-4), stream=None, law="euler"):
+                 precision="fp64", dt="global", cfl=0.5, species=(1.4, 287.058, 1e-4), stream=None, law="euler",
+                 low_mach=None):
         self.lib = _capi.load()
         self.mesh = mesh
         self.precision = precision
@@ -82,8 +83,21 @@ class Solver:
             self.set_stream(stream)
         check(self.lib.hc_mesh_upload(self.h, mesh.ni, mesh.nj, _dptr(mesh.nodes)))
         check(self.lib.hc_set_species(self.h, *[float(s) for s in species]))
+        self.low_mach = None
+        if low_mach is not None:
+            self.set_low_mach(*low_mach)
         self.bc = list(bc)
         self.set_bcs(bc, ref)
+
+    def set_low_mach(self, velocity="convective", pressure="convective", lref=1.0,
+                     dt=np.finfo(np.float64).max) -> None:
+        """AUSM+up's low-Mach scalings, AusmPlusUP<velocity, pressure> with "convective",
+        "acoustic" or "adaptive", and the species lref and dt of the adaptive ratio
+        lref/(as dt) (conservationLaws/euler/fluxes/ausmPlusUP.ipp:61-87)."""
+        vs = _capi.SCALING[velocity] if isinstance(velocity, str) else int(velocity)
+        ps = _capi.SCALING[pressure] if isinstance(pressure, str) else int(pressure)
+        check(self.lib.hc_set_low_mach(self.h, vs, ps, float(lref), float(dt)))
+        self.low_mach = (velocity, pressure, float(lref), float(dt))
 
     def set_bcs(self, bc, ref=None) -> None:
         """Boundary types per side and their reference (ghost) states, 4 planes per side."""

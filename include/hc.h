@@ -39,10 +39,16 @@ typedef enum {
   HC_FLUX_ROE = 0,      /* RoeFlux<Euler>, conservationLaws/base/fluxes/roeFlux.ipp:39-95 */
   HC_FLUX_SLAU = 1,     /* SLAU2 upwinded by the sign of the mass flux */
   HC_FLUX_SLAU_REF = 2, /* Slau<Convective,Acoustic> as written, conservationLaws/euler/fluxes/slau.ipp:4-161 */
-  HC_FLUX_AUSMPUP = 3,  /* AusmPlusUP<Convective,Convective>, conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171 */
+  HC_FLUX_AUSMPUP = 3,  /* AusmPlusUP<V,P>, conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171;
+                           (Convective,Convective) unless hc_set_low_mach chooses V and P */
   HC_FLUX_RUSANOV = 4,  /* RusanovFlux<Euler>, conservationLaws/base/fluxes/rusanovFlux.ipp:99-147 */
-  HC_FLUX_CENTRAL = 5   /* CentralFlux<Euler>, conservationLaws/base/fluxes/centralFlux.ipp:25-37 */
+  HC_FLUX_CENTRAL = 5,  /* CentralFlux<Euler>, conservationLaws/base/fluxes/centralFlux.ipp:25-37 */
+  HC_FLUX_ROE_WS = 6    /* RoeUnprecWS, conservationLaws/euler/fluxes/roeUnprecWS.ipp:2-109 */
 } hc_flux;
+
+/* LowMachScaling (conservationLaws/euler/euler.h:334-339): AUSM+up's velocity (V) and
+ * pressure (P) diffusion scalings */
+typedef enum { HC_SCALING_CONVECTIVE = 0, HC_SCALING_ACOUSTIC = 1, HC_SCALING_ADAPTIVE = 2 } hc_scaling;
 
 /* Slope limiter (VariableLimiterInterface, limiters/limiter.h:14-28) */
 typedef enum {
@@ -115,6 +121,12 @@ int hc_mesh_upload(hc_ctx* ctx, int ni, int nj, const double* nodes_xy);
 
 /* Species<Euler> (conservationLaws/euler/euler.h:48-60): gamma, R, minf. */
 int hc_set_species(hc_ctx* ctx, double gamma, double gas_constant, double minf);
+
+/* The AusmPlusUP<VFluxScaling, PFluxScaling> template arguments (hc_scaling) and the
+ * Species<Euler> fields lref and dt that its adaptive scaling reads, mu = lref/(as dt)
+ * (conservationLaws/euler/fluxes/ausmPlusUP.ipp:61-87).  Defaults: Convective,
+ * Convective, lref 1, dt the largest double (conservationLaws/euler/species.ipp:12). */
+int hc_set_low_mach(hc_ctx* ctx, int velocity_scaling, int pressure_scaling, double lref, double dt);
 
 /* SolutionField::bcTypes and the reference layer of SolutionField::boundary
  * (solutionField/solutionField.h:56-91).  ref[side] holds 4 planes of primitive

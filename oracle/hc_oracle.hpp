@@ -44,7 +44,9 @@ template <class R> R freeze(const R& x) { return x; }
 
 // ---------------------------------------------------------------- enums
 enum Flux { FLUX_ROE = 0, FLUX_SLAU = 1, FLUX_SLAU_REF = 2, FLUX_AUSMPUP = 3,
-            FLUX_RUSANOV = 4, FLUX_CENTRAL = 5 };
+            FLUX_RUSANOV = 4, FLUX_CENTRAL = 5, FLUX_ROE_WS = 6 };
+// LowMachScaling (conservationLaws/euler/euler.h:334-339)
+enum Scaling { SCALING_CONVECTIVE = 0, SCALING_ACOUSTIC = 1, SCALING_ADAPTIVE = 2 };
 enum Limiter { LIM_NOLIMIT1 = 0, LIM_NOLIMIT2 = 1, LIM_NOLIMIT3 = 2, LIM_VANALBADA = 3,
                LIM_MINMOD = 4, LIM_SUPERBEE = 5, LIM_MC = 6, LIM_VANLEER = 7,
                LIM_VANLEER_REF = 8, LIM_CADA3 = 9 };
@@ -58,7 +60,7 @@ template <class R> struct Species {
   R gamma, minf, lref, nu, pr, dt, Rgas, gamma1;
 };
 
-// get_air_species (conservationLaws/euler/species.ipp:363-379)
+// get_air_species (conservationLaws/euler/species.ipp:1-17)
 template <class R> Species<R> air_species() {
   Species<R> s;
   s.gamma = 1.4; s.minf = 0.0001; s.lref = 1.; s.pr = 0.7; s.nu = 1.81e-5;
@@ -427,10 +429,14 @@ template <class R> FluxRes<R> slau_flux(const Species<R>& sp, const Face<R>& f,
   return o;
 }
 
-// AUSM+up, Liou 2006, (Convective, Convective) tags
-// (conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171)
+// AUSM+up, Liou 2006: AusmPlusUP<VFluxScaling, PFluxScaling>
+// (conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171); vscale / pscale select the template
+// arguments (SCALING_*).  The acoustic-to-step time-scale ratio lref / (as dt) of the adaptive
+// scaling reads the species' dt, which the reference leaves at its largest value
+// (conservationLaws/euler/species.ipp:12) unless a caller sets it.
 template <class R> FluxRes<R> ausmpup_flux(const Species<R>& sp, const Face<R>& f,
-                                           const State<R>& sl, const State<R>& sr) {
+                                           const State<R>& sl, const State<R>& sr,
+                                           int vscale = SCALING_CONVECTIVE, int pscale = SCALING_CONVECTIVE) {
   const R alpha0 = 0.1875, beta = 0.125, Ku = 0.75 * 2., Kp = 0.25, sigma = 1.0;
   const R ascoeff = 2. * (sp.gamma - 1.) / (sp.gamma + 1.);
   const R unl = proj_vel(f.n, sl), unr = proj_vel(f.n, sr);
@@ -442,8 +448,11 @@ template <class R> FluxRes<R> ausmpup_flux(const Species<R>& sp, const Face<R>& 
   const R ml = unl / as, mr = unr / as;
   const R minf = sp.minf;
   const R m0 = sqrt(0.5 * (ml * ml + mr * mr));
+  const R mu = sp.lref / (as * sp.dt);
   const R m0_c = std::clamp<R>(m0, minf, 1.);
-  const R m0_p = m0_c, m0_u = m0_c;
+  const R m0_a = std::clamp<R>(fmax(m0, mu), minf, 1.);
+  auto pick = [&](int k) -> R { return k == SCALING_CONVECTIVE ? m0_c : (k == SCALING_ACOUSTIC ? R(1.0) : m0_a); };
+  const R m0_p = pick(pscale), m0_u = pick(vscale);
   const R fa_p = m0_p * (2. - m0_p);
   const R fa_u = m0_u * (2. - m0_u);
   const unsigned mlsup = fabs(ml) > 1 ? 1 : 0, mlsub = 1 - mlsup;
@@ -472,14 +481,52 @@ template <class R> FluxRes<R> ausmpup_flux(const Species<R>& sp, const Face<R>& 
   return o;
 }
 
+// RoeUnprecWS (conservationLaws/euler/fluxes/roeUnprecWS.ipp:2-109): central flux minus a
+// Weiss & Smith / Li & Gu scalar dissipation scaled by the cut-off Mach number
+template <class R> FluxRes<R> roe_ws_flux(const Species<R>& sp, const Face<R>& f,
+                                          const State<R>& sl, const State<R>& sr) {
+  const State<R> ravg = roe_average(sp, sl, sr);
+  const FluxRes<R> central = central_flux(f, sl, sr);
+  const R dp = sr.p - sl.p;
+  const R du = proj_vel(f.n, sr) - proj_vel(f.n, sl);
+  const R una = proj_vel(f.n, ravg);
+  const R ra = ravg.r;
+  const R aa = sqrt(ravg.a2);
+  const R minf = sp.minf;
+  const R uinf = minf * aa;
+  R ql[4], qr[4], dqc[4];
+  state2cons(sl, ql);
+  state2cons(sr, qr);
+  for (int v = 0; v < 4; ++v) dqc[v] = qr[v] - ql[v];
+  const int A11 = 1, A12 = 0, A21 = 1, A22 = 1;
+  const R nu_p = 1.00 * (1. / (ra * uinf * uinf)) * pow(minf, R(A11));
+  const R nu_u = 0.05 * pow(minf, R(A12));
+  const R mu_p = 0.02 * pow(minf, R(A21));
+  const R mu_u = 0.10 * (ra * uinf) * pow(minf, R(A22));
+  const R deltaU = nu_p * dp + nu_u * du;
+  const R ruvh[4] = {ra * ravg.u[0], ra * ravg.u[1], ra, ra * ravg.h};
+  const R deltaP = mu_p * dp + mu_u * du;
+  const R onu[4] = {f.n[0], f.n[1], R(0.), una};
+  FluxRes<R> o;
+  for (int v = 0; v < 4; ++v) {
+    const R d = 0.5 * ((fabs(una) * dqc[v] + deltaU * ruvh[v]) + deltaP * onu[v]) * f.area;
+    o.f[v] = central.f[v] - d;
+  }
+  const R dlam = spec_rad(f.n, ravg) * f.area * pow(minf, R(A11 - 1));
+  o.lam = fmax(central.lam, dlam);
+  return o;
+}
+
 template <class R> FluxRes<R> face_flux(int kind, const Species<R>& sp, const Face<R>& f,
-                                        const State<R>& sl, const State<R>& sr) {
+                                        const State<R>& sl, const State<R>& sr,
+                                        int vscale = SCALING_CONVECTIVE, int pscale = SCALING_CONVECTIVE) {
   switch (kind) {
     case FLUX_ROE: return roe_flux(sp, f, sl, sr);
     case FLUX_SLAU: return slau_flux(sp, f, sl, sr, true);
     case FLUX_SLAU_REF: return slau_flux(sp, f, sl, sr, false);
-    case FLUX_AUSMPUP: return ausmpup_flux(sp, f, sl, sr);
+    case FLUX_AUSMPUP: return ausmpup_flux(sp, f, sl, sr, vscale, pscale);
     case FLUX_RUSANOV: return rusanov_flux(sp, f, sl, sr);
+    case FLUX_ROE_WS: return roe_ws_flux(sp, f, sl, sr);
     default: return central_flux(f, sl, sr);
   }
 }

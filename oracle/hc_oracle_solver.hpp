@@ -28,6 +28,7 @@ template <class R> struct Solver {
   std::vector<R> nodes;  // (ni+1)*(nj+1)*2
   Species<R> sp{};
   int flux = FLUX_ROE, lim = LIM_VANLEER, rk = RK_SSP34, dtmode = DT_GLOBAL;
+  int vscale = SCALING_CONVECTIVE, pscale = SCALING_CONVECTIVE;  // AUSM+up low-Mach scaling
   R cfl = 0.5;
   int bc[4] = {BC_PERIODIC, BC_PERIODIC, BC_PERIODIC, BC_PERIODIC};
   // ghost arrays per side: [side][face][layer][var]; layer 0 = ghost value,
@@ -201,7 +202,7 @@ template <class R> struct Solver {
   FluxRes<R> muscl(const Face<R>& f, const R* cl, const R* cr, const R* ql, const R* qr,
                    const XM<R>& xl, const XM<R>& xr, const QM<R>& ml, const QM<R>& mr) const {
     if (lim == LIM_NOLIMIT1)  // first-order overload (spatial/muscl.h:62-87)
-      return face_flux(flux, sp, f, prim2state(sp, ql), prim2state(sp, qr));
+      return face_flux(flux, sp, f, prim2state(sp, ql), prim2state(sp, qr), vscale, pscale);
     const R dxc[2] = {cr[0] - cl[0], cr[1] - cl[1]};
     R dqc[4];
     for (int v = 0; v < 4; ++v) dqc[v] = qr[v] - ql[v];
@@ -228,7 +229,7 @@ template <class R> struct Solver {
       qL[v] = ql[v] + dl * sl;
       qR[v] = qr[v] - dr * sr;
     }
-    return face_flux(flux, sp, f, prim2state(sp, qL), prim2state(sp, qR));
+    return face_flux(flux, sp, f, prim2state(sp, qL), prim2state(sp, qR), vscale, pscale);
   }
 
   // ghost face (D4): ghost side is not reconstructed, interior side is MUSCL
@@ -239,7 +240,7 @@ template <class R> struct Solver {
     const bool ghost_left = (side == 0 || side == 2);
     const R* ql = ghost_left ? qg : qi;
     const R* qr = ghost_left ? qi : qg;
-    if (lim == LIM_NOLIMIT1) return face_flux(flux, sp, f, prim2state(sp, ql), prim2state(sp, qr));
+    if (lim == LIM_NOLIMIT1) return face_flux(flux, sp, f, prim2state(sp, ql), prim2state(sp, qr), vscale, pscale);
     const R* cc = cells[c].c;
     R d = 0; d += (f.c[0] - cc[0]) * (f.c[0] - cc[0]); d += (f.c[1] - cc[1]) * (f.c[1] - cc[1]);
     const R dd = sqrt(d);
@@ -258,7 +259,7 @@ template <class R> struct Solver {
       if (ghost_left) { qL[v] = qg[v]; qR[v] = qi[v] - dd * s; }
       else { qL[v] = qi[v] + dd * s; qR[v] = qg[v]; }
     }
-    return face_flux(flux, sp, f, prim2state(sp, qL), prim2state(sp, qR));
+    return face_flux(flux, sp, f, prim2state(sp, qL), prim2state(sp, qR), vscale, pscale);
   }
 
   static void acc_sub(FluxRes<R>& a, const FluxRes<R>& f) { for (int v = 0; v < 4; ++v) a.f[v] -= f.f[v]; a.lam += f.lam; }

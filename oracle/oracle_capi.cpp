@@ -42,6 +42,12 @@ void* hco_create(int ni, int nj, const double* nodes, const int* bc, int flux, i
   return s;
 }
 void hco_destroy(void* h) { delete static_cast<S*>(h); }
+// AUSM+up low-Mach scaling pair (SCALING_*) and the species' lref and dt
+void hco_set_low_mach(void* h, int vscale, int pscale, double lref, double dt) {
+  S* s = static_cast<S*>(h);
+  s->vscale = vscale; s->pscale = pscale;
+  s->sp.lref = lref; s->sp.dt = dt;
+}
 
 // reference (layer-1) values of side `side`: 4 planes of nface primitive values
 void hco_set_ghost_ref(void* h, int side, const double* prim) {
@@ -103,6 +109,14 @@ void hco_flux(int kind, const double* species, const double* face, const double*
               double* out5) {
   const Species<double> sp = make_species(species);
   put_flux(face_flux(kind, sp, make_face(face), prim2state(sp, ql), prim2state(sp, qr)), out5);
+}
+// AUSM+up with a low-Mach scaling pair (SCALING_*); species = {gamma, R, minf, lref, dt}
+void hco_ausmpup_scaled(int vscale, int pscale, const double* species5, const double* face,
+                        const double* ql, const double* qr, double* out5) {
+  Species<double> sp = make_species(species5);
+  sp.lref = species5[3];
+  sp.dt = species5[4];
+  put_flux(ausmpup_flux(sp, make_face(face), prim2state(sp, ql), prim2state(sp, qr), vscale, pscale), out5);
 }
 void hco_exact_flux(const double* species, const double* normal, const double* q, double* out5) {
   const Species<double> sp = make_species(species);

@@ -20,7 +20,8 @@ _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 # enum values shared with oracle/hc_oracle.hpp and include/hc.h
-FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5}
+FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5, "roe_ws": 6}
+SCALING = {"convective": 0, "acoustic": 1, "adaptive": 2}
 LIMITER = {"nolimit1": 0, "nolimit2": 1, "nolimit3": 2, "vanalbada": 3, "minmod": 4,
            "superbee": 5, "mc": 6, "vanleer": 7, "vanleer_ref": 8, "cada3": 9}
 BC = {"periodic": 0, "fixed": 1, "riemann": 2, "entropy": 3, "wall": 4}
@@ -50,6 +51,7 @@ def _declare(lib: C.CDLL, prefix: str) -> None:
         "delta": (None, [i, _dp, _dp, _dp, _dp]),
         "rk_table": (None, [i, _dp]),
         "linspace_nodes": (None, [i, i, d, d, d, d, _dp]),
+        "ausmpup_scaled": (None, [i, i, _dp, _dp, _dp, _dp, _dp]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, prefix + name)
@@ -74,6 +76,13 @@ class Pointwise:
     def flux(self, kind, species, face, ql, qr):
         out = np.empty(5)
         self.fn("flux")(kind, species, face, ql, qr, out)
+        return out
+
+    def ausmpup_scaled(self, vscale, pscale, species5, face, ql, qr):
+        """AUSM+up with low-Mach scalings (SCALING); species5 = (gamma, R, minf, lref, dt)."""
+        out = np.empty(5)
+        self.fn("ausmpup_scaled")(int(vscale), int(pscale), np.asarray(species5, dtype=np.float64),
+                                  face, ql, qr, out)
         return out
 
     def exact_flux(self, species, normal, q):
@@ -187,7 +196,7 @@ class OracleSolver:
     """CPU restatement of the reference integrate() over one 2D structured mesh."""
 
     def __init__(self, ni, nj, nodes, bc, flux="roe", limiter="vanleer", rk="ssp34", dt="global",
-                 cfl=0.5, species=(1.4, 287.058, 1e-4), ghost_ref=None, fast=False):
+                 cfl=0.5, species=(1.4, 287.058, 1e-4), ghost_ref=None, fast=False, low_mach=None):
         self.lib = load(fast)
         self.ni, self.nj = ni, nj
         bcv = np.array([BC[b] if isinstance(b, str) else int(b) for b in bc], dtype=np.int32)
@@ -197,6 +206,13 @@ class OracleSolver:
                                      RK[rk] if isinstance(rk, str) else rk,
                                      DT[dt] if isinstance(dt, str) else dt,
                                      float(cfl), np.asarray(species, dtype=np.float64))
+        if low_mach is not None:
+            # (velocity scaling, pressure scaling, lref, species dt) of AUSM+up
+            vs, ps, lref, sdt = low_mach
+            self.lib.hco_set_low_mach.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double]
+            self.lib.hco_set_low_mach(self.h, SCALING.get(vs, vs) if isinstance(vs, str) else int(vs),
+                                      SCALING.get(ps, ps) if isinstance(ps, str) else int(ps),
+                                      float(lref), float(sdt))
         if ghost_ref is not None:
             for side in range(4):
                 if ghost_ref[side] is not None:

@@ -52,6 +52,36 @@ static void put(const Fr& r, double* out) {
   out[4] = r.lambda;
 }
 
+// AusmPlusUP<V, P> for the nine low-Mach scalings (0 Convective, 1 Acoustic, 2 Adaptive);
+// species = {gamma, R, minf, lref, dt}
+template <LowMachScaling V, LowMachScaling P>
+static void ausm_vp(const Species<Law, Real>& sp, const geom::Surface<2, Real>& f, const PrimSet& l,
+                    const PrimSet& r, double* out5) {
+  put(AusmPlusUP<V, P>{}(sp, f, l, r), out5);
+}
+template <LowMachScaling V, LowMachScaling P>
+static void slau_vp(const Species<Law, Real>& sp, const geom::Surface<2, Real>& f, const PrimSet& l,
+                    const PrimSet& r, double* out5) {
+  put(Slau<V, P>{}(sp, f, l, r), out5);
+}
+template <LowMachScaling V>
+static void slau_v(int pscale, const Species<Law, Real>& sp, const geom::Surface<2, Real>& f,
+                   const PrimSet& l, const PrimSet& r, double* out5) {
+  switch (pscale) {
+    case 0: slau_vp<V, LowMachScaling::Convective>(sp, f, l, r, out5); break;
+    case 1: slau_vp<V, LowMachScaling::Acoustic>(sp, f, l, r, out5); break;
+    default: slau_vp<V, LowMachScaling::Adaptive>(sp, f, l, r, out5);
+  }
+}
+template <LowMachScaling V>
+static void ausm_v(int pscale, const Species<Law, Real>& sp, const geom::Surface<2, Real>& f,
+                   const PrimSet& l, const PrimSet& r, double* out5) {
+  switch (pscale) {
+    case 0: ausm_vp<V, LowMachScaling::Convective>(sp, f, l, r, out5); break;
+    case 1: ausm_vp<V, LowMachScaling::Acoustic>(sp, f, l, r, out5); break;
+    default: ausm_vp<V, LowMachScaling::Adaptive>(sp, f, l, r, out5);
+  }
+}
 extern "C" {
 
 // kind numbering follows oracle/hc_oracle.hpp (FLUX_*); kind 1 (SLAU upwinded
@@ -67,7 +97,36 @@ void ref_flux(int kind, const double* species, const double* face, const double*
     case 3: put(AusmPlusUP<LowMachScaling::Convective, LowMachScaling::Convective>{}(sp, f, l, r), out5); break;
     case 4: put(RusanovFlux<Law>{}(sp, f, l, r), out5); break;
     case 5: put(CentralFlux<Law>{}(sp, f, l, r), out5); break;
+    case 6: put(RoeUnprecWS{}(sp, f, l, r), out5); break;
     default: for (int v = 0; v < 5; ++v) out5[v] = std::nan("");
+  }
+}
+
+// Slau<V, P> for the nine low-Mach scalings; species = {gamma, R, minf, lref, dt}
+void ref_slau_scaled(int vscale, int pscale, const double* species5, const double* face,
+                     const double* ql, const double* qr, double* out5) {
+  auto sp = species_of(species5);
+  sp.lref = species5[3];
+  sp.dt = species5[4];
+  const auto f = face_of(face);
+  const PrimSet l = prim_of(ql), r = prim_of(qr);
+  switch (vscale) {
+    case 0: slau_v<LowMachScaling::Convective>(pscale, sp, f, l, r, out5); break;
+    case 1: slau_v<LowMachScaling::Acoustic>(pscale, sp, f, l, r, out5); break;
+    default: slau_v<LowMachScaling::Adaptive>(pscale, sp, f, l, r, out5);
+  }
+}
+void ref_ausmpup_scaled(int vscale, int pscale, const double* species5, const double* face,
+                        const double* ql, const double* qr, double* out5) {
+  auto sp = species_of(species5);
+  sp.lref = species5[3];
+  sp.dt = species5[4];
+  const auto f = face_of(face);
+  const PrimSet l = prim_of(ql), r = prim_of(qr);
+  switch (vscale) {
+    case 0: ausm_v<LowMachScaling::Convective>(pscale, sp, f, l, r, out5); break;
+    case 1: ausm_v<LowMachScaling::Acoustic>(pscale, sp, f, l, r, out5); break;
+    default: ausm_v<LowMachScaling::Adaptive>(pscale, sp, f, l, r, out5);
   }
 }
 void ref_exact_flux(const double* species, const double* normal, const double* q, double* out5) {

@@ -20,7 +20,7 @@ sys.path.insert(0, ROOT)
 from oracle import oracle_py  # noqa: E402
 
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "pointwise_golden.npz")
-REF_FLUXES = [0, 2, 3, 4, 5]          # Roe, SLAU (literal), AUSM+up, Rusanov, Central
+REF_FLUXES = [0, 2, 3, 4, 5, 6]       # Roe, SLAU (literal), AUSM+up, Rusanov, Central, RoeUnprecWS
 REF_LIMITERS = [0, 1, 2, 3, 4, 5, 6, 8, 9]
 
 
@@ -99,6 +99,29 @@ def main():
 
     for k in range(4):
         g[f"rk_{k}"] = ref.rk_table(k)
+    # RoeUnprecWS at lower cut-off Mach numbers; AUSM+up at its nine (velocity, pressure)
+    # low-Mach scalings for three (lref, species dt) pairs
+    g["roews_minf"] = np.array([0.05, 1e-3])
+    g["roews_out"] = np.stack([np.stack([ref.flux(6, np.array([1.4, 287.058, mi]), faces[m], ql[m], qr[m])
+                                         for m in range(nf)]) for mi in g["roews_minf"]])
+    ns = 160
+    g["ausm_species"] = np.array([[1.4, 287.058, 0.05, 1.0, np.finfo(np.float64).max],
+                                  [1.4, 287.058, 0.05, 1.0, 0.5],
+                                  [1.4, 287.058, 0.01, 3.0, 0.01]])
+    g["ausm_scaled"] = np.stack([np.stack([np.stack([np.stack([
+        ref.ausmpup_scaled(vs, ps, sp5, faces[m], ql[m], qr[m]) for m in range(ns)])
+        for ps in range(3)]) for vs in range(3)]) for sp5 in g["ausm_species"]])
+    # the reference computes SLAU's scalings and never reads them: its nine
+    # instantiations are one flux (checked against flux_2 by the tests)
+    ref.lib.ref_slau_scaled.argtypes = ref.fn("ausmpup_scaled").argtypes
+
+    def slau_scaled(vs, ps, sp5, m):
+        out = np.empty(5)
+        ref.lib.ref_slau_scaled(vs, ps, np.asarray(sp5, dtype=np.float64), faces[m], ql[m], qr[m], out)
+        return out
+    g["slau_scaled"] = np.stack([np.stack([np.stack([np.stack([slau_scaled(vs, ps, sp5, m) for m in range(ns)])
+                                                     for ps in range(3)]) for vs in range(3)])
+                                 for sp5 in g["ausm_species"]])
     g["cyl_nodes"] = ref.cylinder_nodes(12, 16, 0.5, 20.0)
     g["lin_nodes"] = ref.linspace_nodes(9, 7, 0.0, 10.0, -1.0, 3.0)
     np.savez_compressed(OUT, **g)

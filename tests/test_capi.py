@@ -50,6 +50,7 @@ def test_argument_errors_without_gpu():
     cfg = _capi.Config(0, 0, 0, 0, 0, -1.0)
     assert lib.hc_context_create(C.byref(cfg), C.byref(h)) == _capi.HC_ERR_ARG
     assert lib.hc_residual(None, None) == _capi.HC_ERR_ARG
+    assert lib.hc_set_low_mach(None, 0, 0, 1.0, 1.0) == _capi.HC_ERR_ARG
     bad = np.empty(4)
     assert lib.hc_mesh_cylinder_nodes(0, 4, 0.5, 1.0, 1.0, bad.ctypes.data_as(C.POINTER(C.c_double))) \
         == _capi.HC_ERR_ARG

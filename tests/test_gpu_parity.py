@@ -55,7 +55,7 @@ def small_cases():
 
 
 CASES = small_cases()
-FLUXES = ["roe", "slau", "slau_ref", "ausmpup", "rusanov", "central"]
+FLUXES = ["roe", "slau", "slau_ref", "ausmpup", "rusanov", "central", "roe_ws"]
 LIMITERS = ["nolimit1", "nolimit2", "nolimit3", "vanalbada", "minmod", "superbee", "mc", "vanleer",
             "vanleer_ref", "cada3"]
 

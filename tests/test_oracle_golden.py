@@ -32,11 +32,41 @@ def test_surface_volume(g, o):
     same([o.volume(q) for q in g["volume_in"]], g["volume_out"])
 
 
-@pytest.mark.parametrize("kind", [0, 2, 3, 4, 5])
+@pytest.mark.parametrize("kind", [0, 2, 3, 4, 5, 6])
 def test_fluxes(g, o, kind):
     f, sp = g["surface_out"], g["species"]
     got = [o.flux(kind, sp, f[m], g["flux_ql"][m], g["flux_qr"][m]) for m in range(len(f))]
     same(got, g[f"flux_{kind}"])
+
+
+def test_roe_ws_low_mach(g, o):
+    f = g["surface_out"]
+    for mi, want in zip(g["roews_minf"], g["roews_out"]):
+        sp = np.array([1.4, 287.058, mi])
+        same([o.flux(6, sp, f[m], g["flux_ql"][m], g["flux_qr"][m]) for m in range(len(f))], want)
+
+
+def test_slau_scalings_are_one_flux(g, o):
+    """Slau<V, P> of the reference for all nine scalings equals the oracle's literal SLAU
+    (flux kind 2): the reference leaves SLAU's scaling parameters unused."""
+    f = g["surface_out"]
+    for sp5, got in zip(g["ausm_species"], g["slau_scaled"]):
+        ns = got.shape[2]
+        sp = np.asarray(sp5[:3])
+        want = np.stack([o.flux(2, sp, f[m], g["flux_ql"][m], g["flux_qr"][m]) for m in range(ns)])
+        for vs in range(3):
+            for ps in range(3):
+                same(got[vs, ps], want)
+
+
+@pytest.mark.parametrize("vs", [0, 1, 2])
+@pytest.mark.parametrize("ps", [0, 1, 2])
+def test_ausmpup_scalings(g, o, vs, ps):
+    f = g["surface_out"]
+    for sp5, want in zip(g["ausm_species"], g["ausm_scaled"]):
+        ns = want.shape[2]
+        same([o.ausmpup_scaled(vs, ps, sp5, f[m], g["flux_ql"][m], g["flux_qr"][m]) for m in range(ns)],
+             want[vs, ps])
 
 
 def test_exact_flux(g, o):
