@@ -404,59 +404,73 @@ def measure_adjoint(nsteps: int = 400, snapshots: int = 20):
     return out
 
 
-def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int = 20, seed: int = 2027):
+def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int = 20, seed: int = 2027,
+                            compare: int = 8):
     """Batched and differentiated case: `ninst` periodic Euler instances on [0,1]^2,
     n x n cells with n drawn from {128, 192, ..., 1024}, density = 5 plus 8 seeded
     Gaussians (widths 0.02..0.2, amplitudes -0.5..0.5) on u = 0.5, v = 0.25, p = 1;
     Rusanov with NoLimit3 reconstruction (smooth, so FP32 and FP64 differentiate the
-    same branches), ssp34, global dt, CFL 0.5.  L2 loss of the state after
-    `nsteps` steps against a seeded target of the same kind; gradient with respect
-    to every instance's initial state in FP32 (one adjoint call per instance,
-    `snapshots` checkpoints), and the FP32 gradient of the smallest instance
-    against its FP64 gradient."""
+    same branches), ssp34, global dt, CFL 0.5.  L2 loss of each instance's state after
+    `nsteps` steps against its own seeded target; gradient with respect to every
+    instance's initial state in FP32 from one batched adjoint (hc_batch_adjoint_gradient:
+    one persistent launch per forward stage and one launch per reverse pass over all
+    instances, `snapshots` checkpoints of the whole batch).  Checks: the smallest
+    instance's FP32 gradient from the batch against its FP64 single-mesh gradient, and
+    the first `compare` instances timed as single-mesh adjoints against the batched
+    adjoint of the same instances."""
     from hyperboliconvergence_gb300 import cases
+    from hyperboliconvergence_gb300.batch import Batch
     from hyperboliconvergence_gb300.solver import Solver
     rng = np.random.default_rng(seed)
     sizes = [int(n) for n in rng.choice(np.arange(128, 1025, 64), ninst)]
     base = (0.5, 0.25, 5.0, 1.0)
-    cells = 0
-    fwd_ms = rev_ms = 0.0
-    t0 = time.perf_counter()
-    for k, n in enumerate(sizes):
+    insts, targets = [], []
+    sp = None
+    for n in sizes:
         mesh, bc, ref, q, sp = cases.gaussian_sum(n, n, rng, base=base)
-        target = cases.gaussian_sum(n, n, rng, base=base)[3]
-        s = Solver(mesh, bc, ref, flux="rusanov", limiter="nolimit3", rk="ssp34", precision="fp32", dt="global",
-                   cfl=0.5, species=sp)
-        s.set_state(q)
-        J, g, refb, rates, st = s.gradient(nsteps, snapshots=snapshots, kind="l2", target=target)
-        s.close()
-        if not np.isfinite(J) or not np.all(np.isfinite(g)):
-            raise RuntimeError(f"instance {k}: non-finite objective or gradient")
-        cells += n * n
-        fwd_ms += st.ms_forward
-        rev_ms += st.ms_total - st.ms_forward
+        insts.append((mesh, bc, ref, q))
+        targets.append(cases.gaussian_sum(n, n, rng, base=base)[3])
+    kw = dict(flux="rusanov", limiter="nolimit3", rk="ssp34", dt="global", cfl=0.5, species=sp)
+    kmin = int(np.argmin(sizes))
+    t0 = time.perf_counter()
+    bt = Batch(insts, precision="fp32", **kw)
+    J, grads, st = bt.gradient(nsteps, targets, snapshots=snapshots, want=[kmin])
     wall = time.perf_counter() - t0
-    # FP64 check on the smallest instance
-    n = min(sizes)
-    crng = np.random.default_rng(seed + 1)
-    mesh, bc, ref, q, sp = cases.gaussian_sum(n, n, crng, base=base)
-    target = cases.gaussian_sum(n, n, crng, base=base)[3]
-    grads = {}
-    for prec in ("fp32", "fp64"):
-        s = Solver(mesh, bc, ref, flux="rusanov", limiter="nolimit3", rk="ssp34", precision=prec, dt="global",
-                   cfl=0.5, species=sp)
+    bt.close()
+    if not np.all(np.isfinite(J)) or not np.all(np.isfinite(grads[kmin])):
+        raise RuntimeError("non-finite objective or gradient")
+    cells = sum(n * n for n in sizes)
+    fwd_ms, rev_ms = st.ms_forward, st.ms_total - st.ms_forward
+    # FP64 single-mesh check of the smallest instance
+    mesh, bc, ref, q = insts[kmin]
+    s = Solver(mesh, bc, ref, precision="fp64", **kw)
+    s.set_state(q)
+    j64, g64 = s.gradient(nsteps, snapshots=snapshots, kind="l2", target=targets[kmin])[:2]
+    s.close()
+    g32 = grads[kmin]
+    # single-mesh adjoints of the first `compare` instances against one batched adjoint of them
+    single_ms = 0.0
+    for k in range(compare):
+        mesh, bc, ref, q = insts[k]
+        s = Solver(mesh, bc, ref, precision="fp32", **kw)
         s.set_state(q)
-        grads[prec] = s.gradient(nsteps, snapshots=snapshots, kind="l2", target=target)[:2]
+        single_ms += s.gradient(nsteps, snapshots=snapshots, kind="l2", target=targets[k])[4].ms_total
         s.close()
-    (j32, g32), (j64, g64) = grads["fp32"], grads["fp64"]
+    sub = Batch(insts[:compare], precision="fp32", **kw)
+    sub_ms = sub.gradient(nsteps, targets[:compare], snapshots=snapshots, want=[])[2].ms_total
+    sub.close()
     return {"workload": f"{ninst} Gaussian-sum Euler instances, n x n with n in 128..1024, L2 loss after "
-                        f"{nsteps} ssp34 steps, {snapshots} snapshots, FP32",
+                        f"{nsteps} ssp34 steps, {snapshots} snapshots, FP32, one batched adjoint",
             "cells": cells, "forward_ms": fwd_ms, "reverse_ms": rev_ms, "wall_s": wall,
+            "recompute_ms": st.ms_recompute, "kernel_launches": int(st.kernel_launches),
             "forward_cell_updates_per_s": cells * nsteps / (fwd_ms / 1e3),
             "adjoint_step_over_forward_step": rev_ms / fwd_ms,
-            "fp64_check": {"cells": n * n, "J_rel_diff": abs(j32 - j64) / abs(j64),
+            "fp64_check": {"instance": kmin, "cells": sizes[kmin] ** 2,
+                           "J_rel_diff": abs(float(J[kmin]) - j64) / abs(j64),
                            "grad_max_rel_diff": float(np.abs(g32 - g64).max() / np.abs(g64).max())},
-            "note": "one adjoint call per instance; the adjoint has no batched launch"}
+            "batched_vs_single_mesh": {"instances": compare, "cells": sum(n * n for n in sizes[:compare]),
+                                       "single_mesh_ms": single_ms, "batched_ms": sub_ms,
+                                       "speedup": single_ms / sub_ms}}
 
 
 def dist_setup():

@@ -178,3 +178,6 @@ def _declare_adjoint(lib):
     lib.hc_objective_forward.restype = C.c_int
     lib.hc_adjoint_gradient.argtypes = [p, i, i, C.POINTER(Objective), dp, dp, dp, dp, C.POINTER(AdjointStats)]
     lib.hc_adjoint_gradient.restype = C.c_int
+    lib.hc_batch_adjoint_gradient.argtypes = [p, i, i, C.POINTER(Objective), C.POINTER(dp), dp, C.POINTER(dp),
+                                              C.POINTER(AdjointStats)]
+    lib.hc_batch_adjoint_gradient.restype = C.c_int

@@ -108,6 +108,34 @@ class Batch:
     def kernel_launches(self) -> int:
         return int(self.lib.hc_batch_kernel_launches(self.h))
 
+    def gradient(self, nsteps, targets, snapshots=20, weight=(1.0, 1.0, 1.0, 1.0), want=None):
+        """Every instance's L2 objective J_k = sum w_v (q_k(N) - target_k)^2 after nsteps
+        steps and its gradient with respect to the instance's current state, from one
+        batched adjoint (hc_batch_adjoint_gradient).  `want`: indices whose gradients
+        are copied back (default all).  Returns (J array, {k: q0_bar}, stats)."""
+        from ._capi import AdjointStats, Objective
+        n = self.n
+        tg = [np.ascontiguousarray(t, dtype=np.float64) for t in targets]
+        for k, t in enumerate(tg):
+            m = self.meshes[k]
+            if t.shape != (4, m.ni, m.nj):
+                raise ValueError(f"target {k} must have shape (4, {m.ni}, {m.nj})")
+        tptr = (C.POINTER(C.c_double) * n)(*[_dptr(t) for t in tg])
+        want = range(n) if want is None else list(want)
+        grads = {k: np.empty((4, self.meshes[k].ni, self.meshes[k].nj)) for k in want}
+        gptr = (C.POINTER(C.c_double) * n)()
+        for k, g in grads.items():
+            gptr[k] = _dptr(g)
+        o = Objective()
+        o.kind = _capi.OBJECTIVE["l2"]
+        for v in range(4):
+            o.weight[v] = float(weight[v])
+        J = np.empty(n)
+        st = AdjointStats()
+        check(self.lib.hc_batch_adjoint_gradient(self.h, int(nsteps), int(snapshots), C.byref(o), tptr, _dptr(J),
+                                                 gptr, C.byref(st)))
+        return J, grads, st
+
 
 def uneven_riemann_batch(n: int, seed: int, sizes=tuple(range(64, 1025, 32))):
     """n four-quadrant Riemann instances with Ni, Nj drawn uniformly from `sizes`."""

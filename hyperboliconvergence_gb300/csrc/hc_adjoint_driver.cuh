@@ -27,7 +27,32 @@
 namespace hc {
 namespace adj {
 
-template <class R> struct Adj {
+// buffers and recomputation timing shared by the single-mesh and batched drivers
+struct AdjCommon {
+  std::vector<void*> allocs;
+  std::vector<cudaEvent_t> adv_events;  // (start, end) pairs around checkpoint recomputation
+
+  template <class T> int alloc(T** p, size_t count) {
+    HC_CUDA(cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T)));
+    allocs.push_back(*p);
+    return HC_OK;
+  }
+  ~AdjCommon() {
+    for (void* p : allocs) cudaFree(p);
+    for (cudaEvent_t e : adv_events) cudaEventDestroy(e);
+  }
+  // time of the recorded recomputation segments (call after the stream is idle)
+  double recompute_ms() const {
+    double t = 0;
+    for (size_t k = 0; k + 1 < adv_events.size(); k += 2) {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, adv_events[k], adv_events[k + 1]) == cudaSuccess) t += ms;
+    }
+    return t;
+  }
+};
+
+template <class R> struct Adj : AdjCommon {
   hc_ctx* c = nullptr;
   int nst = 4;
   RKTab tab{};
@@ -54,27 +79,7 @@ template <class R> struct Adj {
   hc_objective obj{};
   int nsteps = 0;
   long long fwd_steps = 0, adj_steps = 0, launches = 0;
-  std::vector<void*> allocs;
-  std::vector<cudaEvent_t> adv_events;  // (start, end) pairs around checkpoint recomputation
-
-  template <class T> int alloc(T** p, size_t count) {
-    HC_CUDA(cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T)));
-    allocs.push_back(*p);
-    return HC_OK;
-  }
-  ~Adj() {
-    for (void* p : allocs) cudaFree(p);
-    for (cudaEvent_t e : adv_events) cudaEventDestroy(e);
-  }
-  // time of the recorded recomputation segments (call after the stream is idle)
-  double recompute_ms() const {
-    double t = 0;
-    for (size_t k = 0; k + 1 < adv_events.size(); k += 2) {
-      float ms = 0;
-      if (cudaEventElapsedTime(&ms, adv_events[k], adv_events[k + 1]) == cudaSuccess) t += ms;
-    }
-    return t;
-  }
+  size_t state_values() const { return 4 * n; }  // one stored state
   cudaStream_t s() const { return c->stream; }
 };
 
@@ -140,10 +145,10 @@ template <class R> int forward_step(Adj<R>& A, int step, bool rec) {
 }
 
 // sq[nst] -> sq[0] (the step output becomes the next step's start)
-template <class R> void swap_out(Adj<R>& A) { std::swap(A.sq[0], A.sq[A.nst]); }
+template <class AD> void swap_out(AD& A) { std::swap(A.sq[0], A.sq[A.nst]); }
 
-template <class R> __global__ void sum_into_kernel(const R* __restrict__ v, int m, double* __restrict__ acc) {
-  // one block, fixed order: deterministic
+// acc[0] += sum of v[0..m) by one 256-thread block in a fixed order (deterministic)
+template <class R> __device__ __forceinline__ void block_sum_into(const R* __restrict__ v, int m, double* acc) {
   __shared__ double part[256];
   double s = 0;
   for (int k = threadIdx.x; k < m; k += 256) s += double(v[k]);
@@ -154,6 +159,9 @@ template <class R> __global__ void sum_into_kernel(const R* __restrict__ v, int 
     __syncthreads();
   }
   if (threadIdx.x == 0) acc[0] += part[0];
+}
+template <class R> __global__ void sum_into_kernel(const R* __restrict__ v, int m, double* __restrict__ acc) {
+  block_sum_into(v, m, acc);
 }
 
 // J += scale * wall force of the state q (drag objective)
@@ -176,10 +184,11 @@ template <class R> int add_drag(Adj<R>& A, const R* q, double scale) {
   return HC_OK;
 }
 
+// cell c of the L2 objective: part[c] = sum_v w_v (q - t)^2, or (mode_grad) its
+// gradient 2 w_v (q - t) into lam
 template <class R>
-__global__ void l2_kernel(const R* q, const R* t, size_t n, double w0, double w1, double w2, double w3, R* part,
-                          int mode_grad, R* lam) {
-  const size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+__device__ __forceinline__ void l2_cell(const R* q, const R* t, size_t n, double w0, double w1, double w2, double w3,
+                                        R* part, int mode_grad, R* lam, size_t c) {
   if (c >= n) return;
   const double w[4] = {w0, w1, w2, w3};
   double s = 0;
@@ -189,6 +198,11 @@ __global__ void l2_kernel(const R* q, const R* t, size_t n, double w0, double w1
     if (mode_grad) lam[v * n + c] = R(2.0 * w[v] * d);
   }
   if (part) part[c] = R(s);
+}
+template <class R>
+__global__ void l2_kernel(const R* q, const R* t, size_t n, double w0, double w1, double w2, double w3, R* part,
+                          int mode_grad, R* lam) {
+  l2_cell(q, t, n, w0, w1, w2, w3, part, mode_grad, lam, blockIdx.x * size_t(blockDim.x) + threadIdx.x);
 }
 
 // residual adjoint: qbar_out = (dRes/dq at q)^T rbar (+ qbar_add); objective mode
@@ -326,17 +340,25 @@ struct Schedule {
   }
 };
 
-template <class R> R* slot_ptr(Adj<R>& A, int slot) { return slot < 0 ? A.base : A.snaps + size_t(slot) * 4 * A.n; }
+// The checkpointing below is written once for both drivers (Adj, and the batched
+// BAdj of hc_batch_adjoint.cu): AD supplies sq, base, snaps, state_values(), s(),
+// adv_events, and the overloads forward_step(AD&, step, record) and
+// adjoint_step(AD&, step), found by argument-dependent lookup.
+template <class AD> auto slot_ptr(AD& A, int slot) {
+  return slot < 0 ? A.base : A.snaps + size_t(slot) * A.state_values();
+}
 
-template <class R> int restore(Adj<R>& A, int slot) {
-  HC_CUDA(cudaMemcpyAsync(A.sq[0], slot_ptr(A, slot), 4 * A.n * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
+template <class AD> int restore(AD& A, int slot) {
+  HC_CUDA(cudaMemcpyAsync(A.sq[0], slot_ptr(A, slot), A.state_values() * sizeof(*A.sq[0]), cudaMemcpyDeviceToDevice,
+                          A.s()));
   return HC_OK;
 }
-template <class R> int store(Adj<R>& A, int slot) {
-  HC_CUDA(cudaMemcpyAsync(slot_ptr(A, slot), A.sq[0], 4 * A.n * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
+template <class AD> int store(AD& A, int slot) {
+  HC_CUDA(cudaMemcpyAsync(slot_ptr(A, slot), A.sq[0], A.state_values() * sizeof(*A.sq[0]), cudaMemcpyDeviceToDevice,
+                          A.s()));
   return HC_OK;
 }
-template <class R> int advance(Adj<R>& A, int from, int to) {
+template <class AD> int advance(AD& A, int from, int to) {
   if (to <= from) return HC_OK;
   cudaEvent_t ev[2];
   HC_CUDA(cudaEventCreate(&ev[0]));
@@ -369,8 +391,8 @@ inline std::vector<std::pair<int, int>> first_descent(const Schedule& sc, int n,
 // reverse steps [a, b) whose start state is in `slot`, with the free slots on
 // `stack`; `first`: the split points of this call's right-most path were stored
 // by the forward sweep
-template <class R>
-int reverse(Adj<R>& A, const Schedule& sc, int a, int b, int slot, std::vector<int>& stack, bool first) {
+template <class AD>
+int reverse(AD& A, const Schedule& sc, int a, int b, int slot, std::vector<int>& stack, bool first) {
   const int n = b - a;
   const int sfree = int(stack.size());
   if (n <= 0) return HC_OK;

@@ -20,6 +20,8 @@
 #include "hc_adjoint.cuh"
 #include "hc_kernels.cuh"
 
+#include <cfloat>
+
 namespace hc {
 
 enum { ADJ_FIELDS = 16 };  // dL[4], dR[4], gL[4], gR[4]
@@ -45,10 +47,9 @@ template <class R> struct AdjArgs {
   R obj_scale, obj_dirx, obj_diry;
 };
 
-// qmetric of every cell (phase 2 of the stage kernel, without tiling)
-template <class R> __global__ void adj_qm_kernel(const AdjArgs<R> a, R* qm) {
+// qmetric of cell c (phase 2 of the stage kernel, without tiling)
+template <class R> __device__ __forceinline__ void adj_qm_cell(const AdjArgs<R>& a, R* qm, int c) {
   const int ni = a.ni, nj = a.nj;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ni * nj) return;
   const int gi = c / nj, gj = c % nj;
   const size_t n = size_t(ni) * nj;
@@ -88,6 +89,9 @@ template <class R> __global__ void adj_qm_kernel(const AdjArgs<R> a, R* qm) {
 #pragma unroll
   for (int k = 0; k < 8; ++k) qm[k * n + c] = m[k];
 }
+template <class R> __global__ void adj_qm_kernel(const AdjArgs<R> a, R* qm) {
+  adj_qm_cell(a, qm, int(blockIdx.x * blockDim.x + threadIdx.x));
+}
 
 template <class R, int FK>
 __device__ __forceinline__ void flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql, const R* qr, const R* Fb,
@@ -99,12 +103,12 @@ __device__ __forceinline__ void flux_adj(const Gas<R>& g, R nx, R ny, R A, const
 // pass 1: one thread per face of direction dir (0 = i-faces, 1 = j-faces)
 // C: the type the face's reconstruction, flux and their reverse are computed in
 // (R, or double-float for FP64 storage); loads and stores stay in R.
-template <class R, int FK, class C = R> __global__ void adj_face_kernel(const AdjArgs<R> a, int dir) {
+template <class R, int FK, class C = R>
+__device__ __forceinline__ void adj_face_one(const AdjArgs<R>& a, int dir, int f) {
   const int ni = a.ni, nj = a.nj;
   const size_t n = size_t(ni) * nj;
   const bool idir = dir == 0;
   const int nf = idir ? (ni + 1) * nj : ni * (nj + 1);
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   int i, j;
   if (idir) { i = f / nj; j = f % nj; } else { i = f / (nj + 1); j = f % (nj + 1); }
@@ -249,11 +253,13 @@ template <class R, int FK, class C = R> __global__ void adj_face_kernel(const Ad
 #pragma unroll
   for (int k = 0; k < ADJ_FIELDS; ++k) out[size_t(k) * nf + f] = cvt<R>(res[k]);
 }
+template <class R, int FK, class C = R> __global__ void adj_face_kernel(const AdjArgs<R> a, int dir) {
+  adj_face_one<R, FK, C>(a, dir, int(blockIdx.x * blockDim.x + threadIdx.x));
+}
 
-// pass 2: qmetric adjoint per cell
-template <class R> __global__ void adj_qmbar_kernel(const AdjArgs<R> a) {
+// pass 2: qmetric adjoint of cell c
+template <class R> __device__ __forceinline__ void adj_qmbar_cell(const AdjArgs<R>& a, int c) {
   const int ni = a.ni, nj = a.nj;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ni * nj) return;
   const int gi = c / nj, gj = c % nj;
   const size_t n = size_t(ni) * nj;
@@ -289,11 +295,13 @@ template <class R> __global__ void adj_qmbar_kernel(const AdjArgs<R> a) {
 #pragma unroll
   for (int k = 0; k < 8; ++k) a.qmbar[k * n + c] = m[k];
 }
+template <class R> __global__ void adj_qmbar_kernel(const AdjArgs<R> a) {
+  adj_qmbar_cell(a, int(blockIdx.x * blockDim.x + threadIdx.x));
+}
 
-// pass 3: gather the state adjoint per cell
-template <class R> __global__ void adj_gather_kernel(const AdjArgs<R> a) {
+// pass 3: gather the state adjoint of cell c
+template <class R> __device__ __forceinline__ void adj_gather_cell(const AdjArgs<R>& a, int c) {
   const int ni = a.ni, nj = a.nj;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ni * nj) return;
   const int gi = c / nj, gj = c % nj;
   const size_t n = size_t(ni) * nj;
@@ -326,15 +334,18 @@ template <class R> __global__ void adj_gather_kernel(const AdjArgs<R> a) {
 #pragma unroll
   for (int v = 0; v < 4; ++v) a.qbar[v * n + c] = qb[v];
 }
+template <class R> __global__ void adj_gather_kernel(const AdjArgs<R> a) {
+  adj_gather_cell(a, int(blockIdx.x * blockDim.x + threadIdx.x));
+}
 
 // Reverse of one stage update q_out = prim(cons(q0) + (sum_k alpha_k R_k) * fac),
 // fac = beta*dt/V frozen: qbar_out -> q0bar (accumulated) and rbar_k (accumulated).
 template <class R>
-__global__ void adj_update_kernel(int ncell, Gas<R> g, const R* __restrict__ q_out, const R* __restrict__ q0,
-                                  const R* __restrict__ vol, const R* __restrict__ qbar_out, R* __restrict__ q0bar,
-                                  R* rbar0, R* rbar1, R* rbar2, R* rbar3, R alpha0, R alpha1, R alpha2, R alpha3,
-                                  int stage, R dts) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void adj_update_cell(int ncell, const Gas<R>& g, const R* __restrict__ q_out,
+                                                const R* __restrict__ q0, const R* __restrict__ vol,
+                                                const R* __restrict__ qbar_out, R* __restrict__ q0bar, R* rbar0,
+                                                R* rbar1, R* rbar2, R* rbar3, R alpha0, R alpha1, R alpha2,
+                                                R alpha3, int stage, R dts, int c) {
   if (c >= ncell) return;
   const size_t n = size_t(ncell);
   R q[4], qz[4], pb[4], cb[4], z[4] = {R(0), R(0), R(0), R(0)};
@@ -347,9 +358,19 @@ __global__ void adj_update_kernel(int ncell, Gas<R> g, const R* __restrict__ q_o
   const R fac = dts / vol[c];
   R* rb[4] = {rbar0, rbar1, rbar2, rbar3};
   const R al[4] = {alpha0, alpha1, alpha2, alpha3};
-  for (int k = 0; k <= stage; ++k)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) rb[k][v * n + c] += al[k] * cb[v] * fac;
+  for (int k = 0; k < 4; ++k)
+    if (k <= stage)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) rb[k][v * n + c] += al[k] * cb[v] * fac;
+}
+template <class R>
+__global__ void adj_update_kernel(int ncell, Gas<R> g, const R* __restrict__ q_out, const R* __restrict__ q0,
+                                  const R* __restrict__ vol, const R* __restrict__ qbar_out, R* __restrict__ q0bar,
+                                  R* rbar0, R* rbar1, R* rbar2, R* rbar3, R alpha0, R alpha1, R alpha2, R alpha3,
+                                  int stage, R dts) {
+  adj_update_cell(ncell, g, q_out, q0, vol, qbar_out, q0bar, rbar0, rbar1, rbar2, rbar3, alpha0, alpha1, alpha2,
+                  alpha3, stage, dts, int(blockIdx.x * blockDim.x + threadIdx.x));
 }
 
 // Drag of the wall faces of the state q (force on the body along (dirx, diry)
@@ -376,6 +397,133 @@ __global__ void wall_force_kernel(const AdjArgs<R> a, const R* qm, int side, R* 
   const R pw = a.q[3 * n + ci] - (qm[6 * n + ci] * wx + qm[7 * n + ci] * wy);
   const R sgn_in = int_right ? R(1) : R(-1);
   out[k] = -sgn_in * A * pw * (nx * a.obj_dirx + ny * a.obj_diry) * a.obj_scale;
+}
+
+// ---------------------------------------------------------------- batched launches
+// The reverse passes of every instance of a batch (hc_batch_adjoint.cu), one grid
+// per pass.  The grid is cut into segments -- one per instance for the cell
+// passes, one per instance and face direction for the face pass -- with seg[s]
+// the first block of segment s (nseg + 1 ascending entries).  A block finds its
+// segment by binary search, thread 0 writes the instance's AdjArgs (its slices of
+// the pools) to shared memory, and the block runs the single-mesh body on them:
+// every instance gets exactly the arithmetic of a single-mesh adjoint.
+template <class R> struct AdjBatchArgs {
+  const BatchInst* inst;
+  const int* seg;
+  int nseg;
+  Gas<R> gas;
+  int limiter;
+  const R* q;         // stage state pool (4 planes per instance at 4*cell)
+  R* qm;              // qmetric pool (8 planes per instance at 8*cell)
+  const R* rbar;      // residual adjoint pool (4*cell)
+  const R* fi;        // face records (FREC planes per instance at FREC*fi / FREC*fj)
+  const R* fj;
+  const R* gref;      // ghost reference pool (per side at inst.gref[side])
+  R* refbar;          // its adjoint, same layout
+  R* ai;              // face adjoint pools (ADJ_FIELDS planes per instance at ADJ_FIELDS*fi / *fj)
+  R* aj;
+  R* qmbar;           // 8*cell
+  R* qbar;            // 4*cell
+  const R* qbar_add;  // 4*cell or null
+};
+
+__device__ __forceinline__ int find_segment(const int* seg, int nseg, int block) {
+  int lo = 0, hi = nseg - 1;  // the largest s with seg[s] <= block
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (seg[mid] <= block) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <class R> __device__ __forceinline__ void batch_adj_args(const AdjBatchArgs<R>& b, int k, AdjArgs<R>& a) {
+  const BatchInst& in = b.inst[k];
+  a.ni = in.ni; a.nj = in.nj;
+  for (int s = 0; s < 4; ++s) a.bc[s] = in.bc[s];
+  a.gas = b.gas;
+  a.limiter = b.limiter;
+  const long long c4 = 4 * in.cell, c8 = 8 * in.cell;
+  a.q = b.q + c4;
+  a.qm = b.qm + c8;
+  a.rbar = b.rbar ? b.rbar + c4 : nullptr;
+  a.fi = b.fi + (long long)FREC * in.fi;
+  a.fj = b.fj + (long long)FREC * in.fj;
+  for (int s = 0; s < 4; ++s) { a.gref[s] = b.gref + in.gref[s]; a.refbar[s] = b.refbar + in.gref[s]; }
+  a.ai = b.ai + (long long)ADJ_FIELDS * in.fi;
+  a.aj = b.aj + (long long)ADJ_FIELDS * in.fj;
+  a.qmbar = b.qmbar + c8;
+  a.qbar = b.qbar ? b.qbar + c4 : nullptr;
+  a.qbar_add = b.qbar_add ? b.qbar_add + c4 : nullptr;
+  a.objective = 0;
+  a.obj_scale = a.obj_dirx = a.obj_diry = R(0);
+}
+
+// the block's instance arguments in shared memory and its block index within the segment
+template <class R> struct AdjBlock {
+  AdjArgs<R> a;
+  int local;  // block index within the segment
+  int seg;
+};
+template <class R> __device__ __forceinline__ void adj_block_setup(const AdjBatchArgs<R>& b, int per_inst,
+                                                                   AdjBlock<R>& sb) {
+  if (threadIdx.x == 0) {
+    const int s = find_segment(b.seg, b.nseg, int(blockIdx.x));
+    batch_adj_args(b, s / per_inst, sb.a);
+    sb.local = int(blockIdx.x) - b.seg[s];
+    sb.seg = s;
+  }
+  __syncthreads();
+}
+
+template <class R> __global__ void adj_qm_batch_kernel(const AdjBatchArgs<R> b) {
+  __shared__ AdjBlock<R> sb;
+  adj_block_setup(b, 1, sb);
+  adj_qm_cell(sb.a, const_cast<R*>(sb.a.qm), sb.local * int(blockDim.x) + int(threadIdx.x));
+}
+template <class R, int FK, class C = R> __global__ void adj_face_batch_kernel(const AdjBatchArgs<R> b) {
+  __shared__ AdjBlock<R> sb;
+  adj_block_setup(b, 2, sb);
+  adj_face_one<R, FK, C>(sb.a, sb.seg & 1, sb.local * int(blockDim.x) + int(threadIdx.x));
+}
+template <class R> __global__ void adj_qmbar_batch_kernel(const AdjBatchArgs<R> b) {
+  __shared__ AdjBlock<R> sb;
+  adj_block_setup(b, 1, sb);
+  adj_qmbar_cell(sb.a, sb.local * int(blockDim.x) + int(threadIdx.x));
+}
+template <class R> __global__ void adj_gather_batch_kernel(const AdjBatchArgs<R> b) {
+  __shared__ AdjBlock<R> sb;
+  adj_block_setup(b, 1, sb);
+  adj_gather_cell(sb.a, sb.local * int(blockDim.x) + int(threadIdx.x));
+}
+
+// Reverse of one stage update for every instance; the frozen timestep of each
+// instance is cfl / max rate of the step, as the forward run took it.
+template <class R> struct AdjUpdateBatch {
+  const BatchInst* inst;
+  const int* seg;  // the cell-pass segments
+  int nseg;
+  Gas<R> g;
+  const R* q_out;
+  const R* q0;
+  const R* vol;
+  const R* qbar_out;
+  R* q0bar;
+  R* rbar[4];
+  R alpha[4];
+  int stage;
+  double beta, cfl;
+  const double* rates;  // max rates of the step, one per instance
+};
+template <class R> __global__ void adj_update_batch_kernel(const AdjUpdateBatch<R> u) {
+  const int s = find_segment(u.seg, u.nseg, int(blockIdx.x));
+  const BatchInst& in = u.inst[s];
+  const long long c4 = 4 * in.cell;
+  const double dt = u.cfl / fmax(DBL_MIN, u.rates[s]);
+  const int c = (int(blockIdx.x) - u.seg[s]) * int(blockDim.x) + int(threadIdx.x);
+  adj_update_cell(in.ni * in.nj, u.g, u.q_out + c4, u.q0 + c4, u.vol + in.cell, u.qbar_out + c4, u.q0bar + c4,
+                  u.rbar[0] + c4, u.rbar[1] + c4, u.rbar[2] + c4, u.rbar[3] + c4, u.alpha[0], u.alpha[1], u.alpha[2],
+                  u.alpha[3], u.stage, R(u.beta * dt), c);
 }
 
 }  // namespace hc

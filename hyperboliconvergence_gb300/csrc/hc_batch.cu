@@ -1,7 +1,7 @@
 // hc_batch.cu -- batched path of include/hc.h: many uneven meshes advanced by
 // one persistent launch per RK stage over a shared work list of tiles, with
 // CUDA-graph capture and a schedule autotuner.
-#include "hc_host.h"
+#include "hc_batch.h"
 
 #include <algorithm>
 #include <cstring>
@@ -10,38 +10,6 @@
 #include <vector>
 
 using namespace hc;
-
-struct hc_batch {
-  hc_config cfg{};
-  bool fp32 = false;
-  size_t rsz = 8;
-  int ninst = 0;
-  std::vector<int> ni, nj, bc;
-  std::vector<std::vector<double>> href;  // 4 per instance
-  double gamma = 1.4, Rgas = 287.058, minf = 1e-4;
-  cudaStream_t own = nullptr, stream = nullptr;
-  int sms = 152;
-  hc_schedule sched{HC_TILE_8x32, 2, HC_ORDER_LARGEST_FIRST, 0.f};
-  std::vector<long long> cell_off, fi_off, fj_off, node_off, gref_off;
-  size_t ncell = 0, nfi = 0, nfj = 0, nnode = 0, ngref = 0;
-  double *nodes = nullptr, *cx = nullptr, *cy = nullptr, *xm = nullptr, *vol64 = nullptr, *fi64 = nullptr,
-         *fj64 = nullptr;
-  void *fi = nullptr, *fj = nullptr, *vol = nullptr, *gref = nullptr;
-  void* q[3] = {nullptr, nullptr, nullptr};
-  void* res[3] = {nullptr, nullptr, nullptr};
-  double* staging = nullptr;
-  StepInfo* info = nullptr;
-  BatchInst* inst_d = nullptr;
-  int* order_d = nullptr;
-  int nwork = 0, nwork_cap = 0;
-  std::vector<BatchInst> inst_h;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t graph_exec = nullptr;
-  int graph_steps = 0;
-  long long launches = 0;
-
-  size_t icells(int k) const { return size_t(ni[k]) * nj[k]; }
-};
 
 namespace {
 
@@ -54,13 +22,6 @@ template <class R> __global__ void batch_r2d(const R* a, double* b, size_t n) {
     b[k] = double(a[k]);
 }
 
-template <class R> cudaError_t launch_batch_update0(const BatchArgs<R>& b, int tile, int grid, double cfl,
-                                                    R alpha00, R beta0, cudaStream_t s) {
-  if (tile == HC_TILE_4x32) batch_update0_kernel<4, 32, R><<<grid, 128, 0, s>>>(b, cfl, alpha00, beta0);
-  else if (tile == HC_TILE_16x16) batch_update0_kernel<16, 16, R><<<grid, 256, 0, s>>>(b, cfl, alpha00, beta0);
-  else batch_update0_kernel<8, 32, R><<<grid, 256, 0, s>>>(b, cfl, alpha00, beta0);
-  return cudaGetLastError();
-}
 
 void free_all(hc_batch* b) {
   if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
@@ -115,28 +76,7 @@ int build_worklist(hc_batch* b) {
   return HC_OK;
 }
 
-template <class R> BatchArgs<R> batch_args(hc_batch* b) {
-  BatchArgs<R> a{};
-  a.inst = b->inst_d;
-  a.order = b->order_d;
-  a.nwork = b->nwork;
-  a.gas = make_gas<R>(b->gamma, b->Rgas, b->minf);
-  a.limiter = b->cfg.limiter;
-  a.q0 = (const R*)b->q[0];
-  a.fi = (const R*)b->fi; a.fj = (const R*)b->fj; a.vol = (const R*)b->vol;
-  a.gref = (const R*)b->gref;
-  a.cfl = R(b->cfg.cfl);
-  a.info = b->info;
-  return a;
-}
 
-int zero_step_words(hc_batch* b) {
-  // maxrate and resnorm2 of every instance's StepInfo (strided)
-  HC_CUDA(cudaMemset2DAsync(&b->info[0].maxrate, sizeof(StepInfo), 0, sizeof(unsigned long long), b->ninst,
-                            b->stream));
-  HC_CUDA(cudaMemset2DAsync(&b->info[0].resnorm2, sizeof(StepInfo), 0, sizeof(double), b->ninst, b->stream));
-  return HC_OK;
-}
 
 template <class R> int persistent_step(hc_batch* b) {
   const RKTab tab = rk_table(b->cfg.rk);

@@ -1,0 +1,379 @@
+// hc_batch_adjoint.cu -- discrete adjoint of every instance of a batch at once.
+//
+// The instances share the RK table, the step count and the checkpoint schedule, so
+// the single-mesh driver's sequence of operations (forward steps, stores, restores,
+// reversed steps) is the same for all of them; only the data differ.  Here each
+// operation covers the whole batch: forward, replayed and recomputed steps are the
+// batch's persistent stage launches (one per RK stage over the tiles of every
+// instance), and each reverse pass is one launch over the blocks of every instance
+// (AdjBatchArgs, hc_adjoint_kernels.cuh).  A reversed step of the batch therefore
+// costs the launches of one instance's step, and checkpoint copies move the pooled
+// states of all instances in one copy.  Timesteps stay per instance (each its own
+// global dt), frozen at the forward run's values; J and the rates are FP64.
+//
+// Objective: the weighted L2 distance of each instance's final state to its own
+// target.  Supported as for the single-mesh adjoint: Euler law, Roe or Rusanov,
+// NoLimit1/2/3, van Albada, MinMod, van Leer; periodic, fixed and wall boundaries;
+// global timestep; HC_FP64 and HC_FP32 batches.
+#include "hc_adjoint_driver.cuh"
+#include "hc_batch.h"
+
+namespace hc {
+namespace adj {
+
+template <class R> struct BAdj : AdjCommon {
+  hc_batch* b = nullptr;
+  int ninst = 0;
+  int nst = 4;
+  RKTab tab{};
+  size_t n = 0;  // cells of all instances
+  R* sq[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  R* rbar[4] = {nullptr, nullptr, nullptr, nullptr};
+  R* qm = nullptr;
+  R* qmbar = nullptr;
+  R* ai = nullptr;
+  R* aj = nullptr;
+  R* lam = nullptr;
+  R* qbs = nullptr;
+  R* q0bar = nullptr;
+  R* refbar = nullptr;
+  R* base = nullptr;
+  R* snaps = nullptr;
+  R* target = nullptr;
+  R* part = nullptr;
+  double* rates = nullptr;  // [step][instance]
+  double* jacc = nullptr;   // one per instance
+  int* seg_c = nullptr;     // cell-pass segments (256-thread blocks per instance)
+  int* seg_f = nullptr;     // face-pass segments (kFaceThreads blocks per instance and direction)
+  int blocks_c = 0, blocks_f = 0;
+  std::vector<double> hrates;
+  hc_objective obj{};
+  int nsteps = 0;
+  long long fwd_steps = 0, adj_steps = 0, launches = 0;
+  size_t state_values() const { return 4 * n; }
+  cudaStream_t s() const { return b->stream; }
+
+  AdjBatchArgs<R> args() const {
+    AdjBatchArgs<R> a{};
+    a.inst = b->inst_d;
+    a.gas = make_gas<R>(b->gamma, b->Rgas, b->minf);
+    a.limiter = b->cfg.limiter;
+    a.qm = qm;
+    a.fi = (const R*)b->fi;
+    a.fj = (const R*)b->fj;
+    a.gref = (const R*)b->gref;
+    a.refbar = refbar;
+    a.ai = ai;
+    a.aj = aj;
+    a.qmbar = qmbar;
+    return a;
+  }
+};
+
+// one forward step of every instance from sq[0] to sq[nst]; record (rec) or replay
+// the max rates of step `step`
+template <class R> int forward_step(BAdj<R>& A, int step, bool rec) {
+  hc_batch* b = A.b;
+  const BatchFn<R> fn = batch_fn<R>(b->cfg.flux);
+  // every tile a CTA: the stage launcher caps the persistent grid at full residency
+  const int grid = std::max(1, b->nwork);
+  const int tile = b->sched.tile;
+  double* rates = A.rates + size_t(step) * A.ninst;
+  for (int s = 0; s < A.nst; ++s) {
+    BatchArgs<R> a = batch_args<R>(b);
+    a.q = A.sq[s];
+    a.q0 = A.sq[0];
+    a.stage = s;
+    a.beta = R(A.tab.beta[s]);
+    for (int k = 0; k <= s; ++k) a.alpha[k] = R(A.tab.alpha[s][k]);
+    for (int k = 0; k < s; ++k) a.res_prev[k] = (const R*)b->res[k];
+    a.res_out = (s < A.nst - 1) ? (R*)b->res[s] : nullptr;
+    if (s == 0) {
+      a.res_out = (R*)b->res[0];
+      if (rec) {
+        HC_CUDA(cudaMemset2DAsync(&b->info[0].maxrate, sizeof(StepInfo), 0, sizeof(unsigned long long), A.ninst,
+                                  A.s()));
+        a.mode = MODE_RES_MAXRATE;
+        HC_CUDA(fn(a, tile, grid, A.s()));
+        HC_CUDA(cudaMemcpy2DAsync(rates, sizeof(double), &b->info[0].maxrate, sizeof(StepInfo), sizeof(double),
+                                  A.ninst, cudaMemcpyDeviceToDevice, A.s()));
+      } else {
+        HC_CUDA(cudaMemcpy2DAsync(&b->info[0].maxrate, sizeof(StepInfo), rates, sizeof(double), sizeof(double),
+                                  A.ninst, cudaMemcpyDeviceToDevice, A.s()));
+        a.mode = MODE_RESIDUAL;
+        HC_CUDA(fn(a, tile, grid, A.s()));
+      }
+      a.q_out = A.sq[1];
+      HC_CUDA(launch_batch_update0<R>(a, tile, grid, b->cfg.cfl, R(A.tab.alpha[0][0]), R(A.tab.beta[0]), A.s()));
+      A.launches += 2;
+    } else {
+      a.mode = MODE_FUSED_GLOBAL;
+      a.q_out = A.sq[s + 1];
+      HC_CUDA(fn(a, tile, grid, A.s()));
+      A.launches += 1;
+    }
+  }
+  A.fwd_steps += 1;
+  return HC_OK;
+}
+
+// qbar_out = (dRes/dq at q)^T rbar (+ qbar_add) for every instance: four launches
+template <class R, int FK>
+int residual_adjoint(BAdj<R>& A, const R* q, const R* rbar, const R* qbar_add, R* qbar_out) {
+  AdjBatchArgs<R> a = A.args();
+  a.q = q;
+  a.rbar = rbar;
+  a.qbar = qbar_out;
+  a.qbar_add = qbar_add;
+  a.seg = A.seg_c;
+  a.nseg = A.ninst;
+  adj_qm_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
+  AdjBatchArgs<R> af = a;
+  af.seg = A.seg_f;
+  af.nseg = 2 * A.ninst;
+  adj_face_batch_kernel<R, FK><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
+  adj_qmbar_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
+  adj_gather_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
+  A.launches += 4;
+  HC_CUDA(cudaGetLastError());
+  return HC_OK;
+}
+
+template <class R> int res_adj(BAdj<R>& A, const R* q, const R* rbar, const R* add, R* out) {
+  if (A.b->cfg.flux == HC_FLUX_ROE) return residual_adjoint<R, FLUX_ROE>(A, q, rbar, add, out);
+  return residual_adjoint<R, FLUX_RUSANOV>(A, q, rbar, add, out);
+}
+
+// lam holds the adjoint of every instance's q_{step+1}, sq[0] their q_step; on return
+// lam holds the adjoint of q_step
+template <class R> int adjoint_step(BAdj<R>& A, int step) {
+  if (int st = forward_step(A, step, false)) return st;
+  const size_t bytes4 = A.state_values() * sizeof(R);
+  for (int k = 0; k < A.nst; ++k) HC_CUDA(cudaMemsetAsync(A.rbar[k], 0, bytes4, A.s()));
+  HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
+  for (int s = A.nst - 1; s >= 0; --s) {
+    AdjUpdateBatch<R> u{};
+    u.inst = A.b->inst_d;
+    u.seg = A.seg_c;
+    u.nseg = A.ninst;
+    u.g = make_gas<R>(A.b->gamma, A.b->Rgas, A.b->minf);
+    u.q_out = A.sq[s + 1];
+    u.q0 = A.sq[0];
+    u.vol = (const R*)A.b->vol;
+    u.qbar_out = (s == A.nst - 1) ? A.lam : A.qbs;
+    u.q0bar = A.q0bar;
+    for (int k = 0; k < 4; ++k) {
+      u.rbar[k] = A.rbar[k];
+      u.alpha[k] = k <= s ? R(A.tab.alpha[s][k]) : R(0);
+    }
+    u.stage = s;
+    u.beta = A.tab.beta[s];
+    u.cfl = A.b->cfg.cfl;
+    u.rates = A.rates + size_t(step) * A.ninst;
+    adj_update_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(u);
+    A.launches += 1;
+    HC_CUDA(cudaGetLastError());
+    if (int st = res_adj<R>(A, A.sq[s], A.rbar[s], s == 0 ? A.q0bar : nullptr, A.qbs)) return st;
+  }
+  HC_CUDA(cudaMemcpyAsync(A.lam, A.qbs, bytes4, cudaMemcpyDeviceToDevice, A.s()));
+  A.adj_steps += 1;
+  return HC_OK;
+}
+
+template <class R>
+__global__ void l2_batch_kernel(const BatchInst* inst, const int* seg, int nseg, const R* q, const R* t, double w0,
+                                double w1, double w2, double w3, R* part, int mode_grad, R* lam) {
+  const int s = find_segment(seg, nseg, int(blockIdx.x));
+  const BatchInst& in = inst[s];
+  const long long c4 = 4 * in.cell;
+  const size_t c = size_t(int(blockIdx.x) - seg[s]) * blockDim.x + threadIdx.x;
+  l2_cell(q + c4, t + c4, size_t(in.ni) * in.nj, w0, w1, w2, w3, part ? part + in.cell : nullptr, mode_grad,
+          lam ? lam + c4 : nullptr, c);
+}
+// acc[k] += the sum of instance k's part values (one block per instance, the order
+// of the single-mesh sum)
+template <class R> __global__ void sum_batch_kernel(const BatchInst* inst, const R* part, double* acc) {
+  const BatchInst& in = inst[blockIdx.x];
+  block_sum_into(part + in.cell, in.ni * in.nj, acc + blockIdx.x);
+}
+
+template <class R> int l2_objective(BAdj<R>& A, bool grad) {
+  const double* w = A.obj.weight;
+  l2_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(A.b->inst_d, A.seg_c, A.ninst, A.sq[0], A.target, w[0], w[1],
+                                                     w[2], w[3], grad ? nullptr : A.part, grad ? 1 : 0,
+                                                     grad ? A.lam : nullptr);
+  A.launches += 1;
+  if (!grad) {
+    sum_batch_kernel<R><<<A.ninst, 256, 0, A.s()>>>(A.b->inst_d, A.part, A.jacc);
+    A.launches += 1;
+  }
+  HC_CUDA(cudaGetLastError());
+  return HC_OK;
+}
+
+inline int check_batch_support(hc_batch* b) {
+  if (b->cfg.flux != HC_FLUX_ROE && b->cfg.flux != HC_FLUX_RUSANOV)
+    return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");
+  const int l = b->cfg.limiter;
+  if (!(l == HC_LIM_NOLIMIT1 || l == HC_LIM_NOLIMIT2 || l == HC_LIM_NOLIMIT3 || l == HC_LIM_VANALBADA ||
+        l == HC_LIM_MINMOD || l == HC_LIM_VANLEER))
+    return fail(HC_ERR_UNSUPPORTED, "limiter not differentiated by the adjoint");
+  if (b->cfg.dt_mode != HC_DT_GLOBAL) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the global timestep");
+  for (int t : b->bc)
+    if (t == HC_BC_RIEMANN || t == HC_BC_ENTROPY)
+      return fail(HC_ERR_UNSUPPORTED, "the adjoint supports periodic, fixed and wall boundaries");
+  return HC_OK;
+}
+
+template <class R>
+int batch_setup(BAdj<R>& A, hc_batch* b, int nsteps, int nsnap, const hc_objective* obj,
+                const double* const* targets) {
+  if (nsteps < 1 || nsnap < 0 || !obj) return fail(HC_ERR_ARG, "bad adjoint arguments");
+  if (obj->kind != HC_OBJ_L2) return fail(HC_ERR_UNSUPPORTED, "the batched adjoint takes the L2 objective");
+  if (!targets) return fail(HC_ERR_ARG, "the L2 objective needs a target per instance");
+  for (int k = 0; k < b->ninst; ++k)
+    if (!targets[k]) return fail(HC_ERR_ARG, "instance " + std::to_string(k) + " has no target");
+  if (int st = check_batch_support(b)) return st;
+  A.b = b;
+  A.ninst = b->ninst;
+  A.tab = rk_table(b->cfg.rk);
+  A.nst = A.tab.nst;
+  A.n = b->ncell;
+  A.obj = *obj;
+  A.nsteps = nsteps;
+  // segments of the cell and face passes
+  std::vector<int> sc(1, 0), sf(1, 0);
+  for (int k = 0; k < A.ninst; ++k) {
+    const long long nc = b->icells(k);
+    const long long nfi = (long long)(b->ni[k] + 1) * b->nj[k], nfj = (long long)b->ni[k] * (b->nj[k] + 1);
+    const long long c = sc.back() + (nc + 255) / 256;
+    const long long fi = sf.back() + (nfi + kFaceThreads - 1) / kFaceThreads;
+    const long long fj = fi + (nfj + kFaceThreads - 1) / kFaceThreads;
+    if (fj > 0x7fffffffLL) return fail(HC_ERR_UNSUPPORTED, "batch too large for one adjoint grid");
+    sc.push_back(int(c));
+    sf.push_back(int(fi));
+    sf.push_back(int(fj));
+  }
+  A.blocks_c = sc.back();
+  A.blocks_f = sf.back();
+  const size_t n4 = A.state_values();
+  if (int st = A.alloc(&A.seg_c, sc.size())) return st;
+  if (int st = A.alloc(&A.seg_f, sf.size())) return st;
+  HC_CUDA(cudaMemcpyAsync(A.seg_c, sc.data(), sc.size() * sizeof(int), cudaMemcpyHostToDevice, A.s()));
+  HC_CUDA(cudaMemcpyAsync(A.seg_f, sf.data(), sf.size() * sizeof(int), cudaMemcpyHostToDevice, A.s()));
+  for (int k = 0; k <= A.nst; ++k) if (int st = A.alloc(&A.sq[k], n4)) return st;
+  for (int k = 0; k < 4; ++k) if (int st = A.alloc(&A.rbar[k], n4)) return st;
+  if (int st = A.alloc(&A.qm, 8 * A.n)) return st;
+  if (int st = A.alloc(&A.qmbar, 8 * A.n)) return st;
+  if (int st = A.alloc(&A.ai, size_t(ADJ_FIELDS) * b->nfi)) return st;
+  if (int st = A.alloc(&A.aj, size_t(ADJ_FIELDS) * b->nfj)) return st;
+  if (int st = A.alloc(&A.lam, n4)) return st;
+  if (int st = A.alloc(&A.qbs, n4)) return st;
+  if (int st = A.alloc(&A.q0bar, n4)) return st;
+  if (int st = A.alloc(&A.refbar, b->ngref)) return st;
+  HC_CUDA(cudaMemsetAsync(A.refbar, 0, b->ngref * sizeof(R), A.s()));
+  if (int st = A.alloc(&A.base, n4)) return st;
+  if (nsnap > 0) if (int st = A.alloc(&A.snaps, size_t(nsnap) * n4)) return st;
+  if (int st = A.alloc(&A.rates, size_t(nsteps) * A.ninst)) return st;
+  if (int st = A.alloc(&A.jacc, size_t(A.ninst))) return st;
+  HC_CUDA(cudaMemsetAsync(A.jacc, 0, A.ninst * sizeof(double), A.s()));
+  if (int st = A.alloc(&A.part, A.n)) return st;
+  if (int st = A.alloc(&A.target, n4)) return st;
+  // targets through the batch's FP64 staging buffer (one instance at a time)
+  for (int k = 0; k < A.ninst; ++k) {
+    const size_t m = 4 * b->icells(k);
+    HC_CUDA(cudaMemcpyAsync(b->staging, targets[k], m * sizeof(double), cudaMemcpyHostToDevice, A.s()));
+    convert_kernel<R><<<512, 256, 0, A.s()>>>(b->staging, A.target + 4 * b->cell_off[k], m);
+    HC_CUDA(cudaGetLastError());
+    HC_CUDA(cudaStreamSynchronize(A.s()));  // targets[k] and the staging buffer are reused
+  }
+  HC_CUDA(cudaMemcpyAsync(A.base, b->q[0], n4 * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
+  return HC_OK;
+}
+
+template <class R> int batch_forward_pass(BAdj<R>& A, const std::vector<std::pair<int, int>>& stores) {
+  if (int st = restore(A, -1)) return st;
+  size_t next = 0;
+  for (int k = 0; k < A.nsteps; ++k) {
+    if (int st = forward_step(A, k, true)) return st;
+    swap_out(A);
+    while (next < stores.size() && stores[next].first == k + 1) {
+      if (int st = store(A, stores[next].second)) return st;
+      ++next;
+    }
+  }
+  if (int st = l2_objective(A, false)) return st;
+  A.hrates.resize(size_t(A.nsteps) * A.ninst);
+  HC_CUDA(cudaMemcpyAsync(A.hrates.data(), A.rates, A.hrates.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                          A.s()));
+  HC_CUDA(cudaStreamSynchronize(A.s()));
+  return HC_OK;
+}
+
+template <class R>
+int batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj,
+                           const double* const* targets, double* J, double* const* q0_bar, hc_adjoint_stats* stats) {
+  BAdj<R> A;
+  if (int st = batch_setup(A, b, nsteps, snapshots, obj, targets)) return st;
+  cudaEvent_t e0, e1, e2;
+  HC_CUDA(cudaEventCreate(&e0));
+  HC_CUDA(cudaEventCreate(&e1));
+  HC_CUDA(cudaEventCreate(&e2));
+  std::vector<int> stack;
+  for (int k = snapshots - 1; k >= 0; --k) stack.push_back(k);
+  Schedule sched;
+  sched.build(nsteps, snapshots);
+  const std::vector<std::pair<int, int>> stores = first_descent(sched, nsteps, snapshots, stack);
+  cudaEventRecord(e0, A.s());
+  if (int st = batch_forward_pass(A, stores)) return st;
+  cudaEventRecord(e1, A.s());
+  if (int st = l2_objective(A, true)) return st;  // adjoint of the final states
+  if (int st = reverse(A, sched, 0, nsteps, -1, stack, true)) return st;
+  cudaEventRecord(e2, A.s());
+  HC_CUDA(cudaStreamSynchronize(A.s()));
+  float ms_f = 0, ms_t = 0;
+  cudaEventElapsedTime(&ms_f, e0, e1);
+  cudaEventElapsedTime(&ms_t, e0, e2);
+  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
+  std::vector<double> jh(A.ninst);
+  HC_CUDA(cudaMemcpy(jh.data(), A.jacc, A.ninst * sizeof(double), cudaMemcpyDeviceToHost));
+  if (J) std::memcpy(J, jh.data(), A.ninst * sizeof(double));
+  if (q0_bar) {
+    for (int k = 0; k < A.ninst; ++k) {
+      if (!q0_bar[k]) continue;
+      const size_t m = 4 * b->icells(k);
+      const R* src = A.lam + 4 * b->cell_off[k];
+      if constexpr (std::is_same<R, double>::value) {
+        HC_CUDA(cudaMemcpy(q0_bar[k], src, m * sizeof(double), cudaMemcpyDeviceToHost));
+      } else {
+        std::vector<R> tmp(m);
+        HC_CUDA(cudaMemcpy(tmp.data(), src, m * sizeof(R), cudaMemcpyDeviceToHost));
+        for (size_t v = 0; v < m; ++v) q0_bar[k][v] = double(tmp[v]);
+      }
+    }
+  }
+  b->launches += A.launches;
+  if (stats) {
+    double jsum = 0;
+    for (double v : jh) jsum += v;
+    stats->J = jsum;
+    stats->forward_steps = A.fwd_steps;
+    stats->adjoint_steps = A.adj_steps;
+    stats->kernel_launches = A.launches;
+    stats->ms_forward = ms_f;
+    stats->ms_total = ms_t;
+    stats->ms_recompute = A.recompute_ms();
+  }
+  return HC_OK;
+}
+
+}  // namespace adj
+}  // namespace hc
+
+extern "C" int hc_batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj,
+                                         const double* const* targets, double* J, double* const* q0_bar,
+                                         hc_adjoint_stats* stats) {
+  if (!b) return hc::fail(HC_ERR_ARG, "null batch");
+  if (b->fp32) return hc::adj::batch_adjoint_gradient<float>(b, nsteps, snapshots, obj, targets, J, q0_bar, stats);
+  return hc::adj::batch_adjoint_gradient<double>(b, nsteps, snapshots, obj, targets, J, q0_bar, stats);
+}

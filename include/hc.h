@@ -293,6 +293,20 @@ int hc_batch_sync(hc_batch* b, hc_step_stats* stats);
 int hc_batch_autotune(hc_batch* b, int steps, hc_schedule* best);
 long long hc_batch_kernel_launches(hc_batch* b);
 
+/* Discrete adjoint of every instance of a batch at once (no counterpart in the
+ * reference): the objective of each instance is the L2 distance of its state after
+ * nsteps RK steps to its own target (obj->kind HC_OBJ_L2, obj->weight; targets[k]
+ * 4 planes of instance k, host), each instance with its own frozen global dt.  The
+ * instances share the checkpoint schedule (`snapshots` states of the whole batch),
+ * forward steps are the batch's persistent stage launches and every reverse pass is
+ * one launch over all instances.  J[k] and q0_bar[k] (4 planes of the primitive
+ * state; NULL entries skipped) per instance; stats: summed J, launches and times.
+ * Supported as for hc_adjoint_gradient (HC_FP64 or HC_FP32 batches).  The batch's
+ * states are left unchanged. */
+int hc_batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj,
+                              const double* const* targets, double* J, double* const* q0_bar,
+                              hc_adjoint_stats* stats);
+
 const char* hc_last_error_string(void);
 const char* hc_version(void);
 
