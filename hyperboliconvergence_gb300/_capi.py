@@ -18,6 +18,7 @@ STATUS_NAMES = {0: "HC_OK", 1: "HC_ERR_ARG", 2: "HC_ERR_CUDA", 3: "HC_ERR_NONPHY
 
 FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5, "roe_ws": 6}
 SCALING = {"convective": 0, "acoustic": 1, "adaptive": 2}
+BASIS = {"primitive": 0, "conserved": 1}
 LIMITER = {"nolimit1": 0, "nolimit2": 1, "nolimit3": 2, "vanalbada": 3, "minmod": 4,
            "superbee": 5, "mc": 6, "vanleer": 7, "vanleer_ref": 8, "cada3": 9}
 RK = {"ssp11": 0, "ssp22": 1, "ssp33": 2, "ssp34": 3}
@@ -35,7 +36,7 @@ class HCError(RuntimeError):
 
 class Config(C.Structure):
     _fields_ = [("flux", C.c_int), ("limiter", C.c_int), ("rk", C.c_int), ("precision", C.c_int),
-                ("dt_mode", C.c_int), ("cfl", C.c_double), ("law", C.c_int)]
+                ("dt_mode", C.c_int), ("cfl", C.c_double), ("law", C.c_int), ("basis", C.c_int)]
 
 
 class StepStats(C.Structure):

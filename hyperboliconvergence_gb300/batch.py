@@ -18,11 +18,12 @@ class Batch:
     """Instances = list of (mesh, bc, ref, state); shared flux/limiter/RK/CFL/species."""
 
     def __init__(self, instances, flux="slau", limiter="vanalbada", rk="ssp34", precision="fp32", dt="global",
-                 cfl=0.5, species=(1.4, 287.058, 0.5), stream=None):
+                 cfl=0.5, species=(1.4, 287.058, 0.5), stream=None, basis="primitive"):
         self.lib = _capi.load()
         self.meshes = [inst[0] for inst in instances]
         n = len(instances)
-        cfg = Config(FLUX[flux], LIMITER[limiter], RK[rk], PRECISION[precision], DTMODE[dt], float(cfl))
+        cfg = Config(FLUX[flux], LIMITER[limiter], RK[rk], PRECISION[precision], DTMODE[dt], float(cfl), 0,
+                     _capi.BASIS[basis])
         ni = (C.c_int * n)(*[m.ni for m in self.meshes])
         nj = (C.c_int * n)(*[m.nj for m in self.meshes])
         nodes = (C.POINTER(C.c_double) * n)(*[_dptr(m.nodes) for m in self.meshes])

@@ -163,8 +163,12 @@ enum class BC { Periodic = HC_BC_PERIODIC, Riemann = HC_BC_RIEMANN, Entropy = HC
 // SolutionField (solutionField/solutionField.h:56-91) in the primitive basis:
 // interior as 4 planes {u, v, rho, p}; boundary[side] the reference layer,
 // 4 planes per side face (nj faces on sides 0/1, ni on 2/3).
+// the basis of a SolutionField<SolVarT,2>: its SolVarT (primitive or conserved set)
+enum class Basis { Primitive = HC_BASIS_PRIMITIVE, Conserved = HC_BASIS_CONSERVED };
+
 template <class Real> struct SolutionField {
   int ni, nj;
+  Basis basis = Basis::Primitive;  // of interior and boundary
   std::vector<double> interior;
   std::array<std::vector<double>, 4> boundary;
   std::array<BC, 4> bcTypes{BC::Periodic, BC::Periodic, BC::Periodic, BC::Periodic};
@@ -200,7 +204,7 @@ hc_step_stats integrate(const execution::gpu_policy policy, const UnsteadyTimeCo
                         const Species<Real>& species, const Mesh<Real>& mesh, SolutionField<Real>& q) {
   if (q.ni != mesh.ni || q.nj != mesh.nj) throw Error(HC_ERR_ARG, "solution field and mesh shapes differ");
   hc_config cfg{flux2.flux, flux2.limiter, rungeKutta.id, policy.precision, policy.dt_mode,
-                double(timeControls.cfl)};
+                double(timeControls.cfl), HC_LAW_EULER, int(q.basis)};
   Context ctx(cfg);
   check(hc_mesh_upload(ctx.get(), mesh.ni, mesh.nj, mesh.nodes.data()));
   check(hc_set_species(ctx.get(), species.gamma, species.R, species.minf));
@@ -228,7 +232,7 @@ hc_steady_stats integrate(const execution::gpu_policy policy, const SteadyTimeCo
                           std::vector<double>* history = nullptr, int check_every = 100) {
   if (q.ni != mesh.ni || q.nj != mesh.nj) throw Error(HC_ERR_ARG, "solution field and mesh shapes differ");
   hc_config cfg{flux2.flux, flux2.limiter, rungeKutta.id, policy.precision, policy.dt_mode,
-                double(timeControls.cfl)};
+                double(timeControls.cfl), HC_LAW_EULER, int(q.basis)};
   Context ctx(cfg);
   check(hc_mesh_upload(ctx.get(), mesh.ni, mesh.nj, mesh.nodes.data()));
   check(hc_set_species(ctx.get(), species.gamma, species.R, species.minf));

@@ -130,7 +130,7 @@ template <class R> int forward_step(Adj<R>& A, int step, bool rec) {
       }
       update0_kernel<R><<<std::min<unsigned>(blocks(A.n), 152 * 16), 256, 0, A.s()>>>(
           c->ni, c->nj, a.gas, A.sq[0], (const R*)c->res[0], (const R*)c->vol, R(A.tab.alpha[0][0]),
-          R(A.tab.beta[0]), c->cfg.cfl, c->info, A.sq[1], 0);
+          R(A.tab.beta[0]), c->cfg.cfl, c->info, A.sq[1], 0, c->cfg.basis);
       HC_CUDA(cudaGetLastError());
       A.launches += 2;
     } else {
@@ -423,6 +423,7 @@ int reverse(AD& A, const Schedule& sc, int a, int b, int slot, std::vector<int>&
 
 inline int check_support(hc_ctx* c) {
   if (c->scalar) return fail(HC_ERR_UNSUPPORTED, "the adjoint covers the Euler law");
+  if (c->cfg.basis != HC_BASIS_PRIMITIVE) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the primitive basis");
   if (c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV)
     return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");
   const int l = c->cfg.limiter;

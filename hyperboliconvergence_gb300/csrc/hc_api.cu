@@ -167,7 +167,7 @@ template <class R> int run_step(hc_ctx* c) {
       } else {
         update0_kernel<R><<<grid, B, 0, c->stream>>>(c->ni, c->nj, a.gas, (const R*)c->q[0], (const R*)c->res[0],
                                                      (const R*)c->vol, R(tab.alpha[0][0]), R(tab.beta[0]),
-                                                     c->cfg.cfl, c->info, out_of(0), 1);
+                                                     c->cfg.cfl, c->info, out_of(0), 1, c->cfg.basis);
       }
       HC_CUDA(cudaGetLastError());
       c->launches += 2;
@@ -231,7 +231,10 @@ int hc_context_create(const hc_config* cfg, hc_ctx** out) {
   if (cfg->dt_mode != HC_DT_GLOBAL && cfg->dt_mode != HC_DT_LOCAL) return fail(HC_ERR_ARG, "unknown dt mode");
   if (!(cfg->cfl > 0)) return fail(HC_ERR_ARG, "cfl must be positive");
   if (cfg->law != HC_LAW_EULER && cfg->law != HC_LAW_SCALAR) return fail(HC_ERR_ARG, "unknown law");
+  if (cfg->basis != HC_BASIS_PRIMITIVE && cfg->basis != HC_BASIS_CONSERVED) return fail(HC_ERR_ARG, "unknown basis");
   if (cfg->law == HC_LAW_SCALAR) {
+    if (cfg->basis != HC_BASIS_PRIMITIVE)
+      return fail(HC_ERR_UNSUPPORTED, "the scalar advection law has one basis (pass HC_BASIS_PRIMITIVE)");
     if (cfg->flux != HC_FLUX_RUSANOV && cfg->flux != HC_FLUX_CENTRAL)
       return fail(HC_ERR_UNSUPPORTED, "the scalar advection law uses the Rusanov or central flux");
     if (cfg->precision == HC_FP64_DF) return fail(HC_ERR_UNSUPPORTED, "the scalar advection law runs in FP64 or FP32");

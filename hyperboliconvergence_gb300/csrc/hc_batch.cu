@@ -132,6 +132,7 @@ template <class R> int per_instance_step(hc_batch* b) {
     }
     base.gas = make_gas<R>(b->gamma, b->Rgas, b->minf);
     base.limiter = b->cfg.limiter;
+    base.basis = b->cfg.basis;
     base.fi = (const R*)b->fi + (long long)FREC * b->fi_off[k];
     base.fj = (const R*)b->fj + (long long)FREC * b->fj_off[k];
     base.vol = (const R*)b->vol + b->cell_off[k];
@@ -155,7 +156,7 @@ template <class R> int per_instance_step(hc_batch* b) {
         const unsigned grid = unsigned(std::min<size_t>((n + 255) / 256, size_t(b->sms) * 16));
         update0_kernel<R><<<grid, 256, 0, b->stream>>>(base.ni, base.nj, base.gas, qp(0), rp(0), base.vol,
                                                        R(tab.alpha[0][0]), R(tab.beta[0]), b->cfg.cfl, base.info,
-                                                       out_of(0), 1);
+                                                       out_of(0), 1, b->cfg.basis);
         HC_CUDA(cudaGetLastError());
         b->launches += 2;
       } else {
@@ -192,7 +193,8 @@ int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* n
   if (ninst < 1 || ninst > 32767) return fail(HC_ERR_ARG, "instance count must be in [1, 32767]");
   if (cfg->flux < 0 || cfg->flux >= FLUX_COUNT || cfg->limiter < 0 || cfg->limiter >= LIM_COUNT ||
       cfg->rk < HC_RK_SSP11 || cfg->rk > HC_RK_SSP34 || (cfg->precision != HC_FP64 && cfg->precision != HC_FP32) ||
-      (cfg->dt_mode != HC_DT_GLOBAL && cfg->dt_mode != HC_DT_LOCAL) || !(cfg->cfl > 0))
+      (cfg->dt_mode != HC_DT_GLOBAL && cfg->dt_mode != HC_DT_LOCAL) || !(cfg->cfl > 0) ||
+      (cfg->basis != HC_BASIS_PRIMITIVE && cfg->basis != HC_BASIS_CONSERVED))
     return fail(HC_ERR_ARG, "invalid configuration");
   if (cfg->law != HC_LAW_EULER) return fail(HC_ERR_UNSUPPORTED, "batches hold Euler instances");
   if (!(gamma > 1.0) || !(gas_constant > 0.0) || !(minf > 0.0)) return fail(HC_ERR_ARG, "invalid species");

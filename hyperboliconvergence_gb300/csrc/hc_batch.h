@@ -55,6 +55,7 @@ template <class R> BatchArgs<R> batch_args(hc_batch* b) {
   a.nwork = b->nwork;
   a.gas = make_gas<R>(b->gamma, b->Rgas, b->minf);
   a.limiter = b->cfg.limiter;
+  a.basis = b->cfg.basis;
   a.q0 = (const R*)b->q[0];
   a.fi = (const R*)b->fi; a.fj = (const R*)b->fj; a.vol = (const R*)b->vol;
   a.gref = (const R*)b->gref;

@@ -212,6 +212,7 @@ template <class R> int l2_objective(BAdj<R>& A, bool grad) {
 }
 
 inline int check_batch_support(hc_batch* b) {
+  if (b->cfg.basis != HC_BASIS_PRIMITIVE) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the primitive basis");
   if (b->cfg.flux != HC_FLUX_ROE && b->cfg.flux != HC_FLUX_RUSANOV)
     return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");
   const int l = b->cfg.limiter;

@@ -57,6 +57,7 @@ template <class R> StageArgs<R> base_args(hc_ctx* c) {
   for (int k = 0; k < 4; ++k) a.bc[k] = c->bc[k];
   a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale);
   a.limiter = c->cfg.limiter;
+  a.basis = c->cfg.basis;
   a.fi = (const R*)c->fi; a.fj = (const R*)c->fj; a.vol = (const R*)c->vol;
   a.fic = c->fic; a.fjc = c->fjc;
   for (int k = 0; k < 4; ++k) a.gref[k] = (const R*)c->gref[k];

@@ -51,7 +51,7 @@ template <class R> struct StageArgs {
   const void* fic;    // i-face records in the compute type when it differs from R
   const void* fjc;    // j-face records in the compute type when it differs from R
   const R* vol;       // cell volumes
-  const R* gref[4];   // per side: far-field/fixed primitive values, 4 planes of nface
+  const R* gref[4];   // per side: far-field/fixed values in the solution basis, 4 planes of nface
   R* res_out;         // residual of this stage (5 planes) or null
   const R* res_prev[4];  // residuals of earlier stages (flux planes)
   R alpha[4];         // alpha[s][0..s]
@@ -61,6 +61,7 @@ template <class R> struct StageArgs {
   StepInfo* info;
   R* q_out;           // next stage state (fused modes)
   int norm_stage0;    // accumulate the density-residual norm
+  int basis;          // solution basis: 0 primitive, 1 conserved
 };
 
 enum { MODE_RESIDUAL = 0, MODE_RES_MAXRATE = 1, MODE_FUSED_GLOBAL = 2, MODE_FUSED_LOCAL = 3 };
@@ -102,9 +103,15 @@ template <class R> __device__ __forceinline__ void flag_nonphysical(StepInfo* in
   }
 }
 
-// cons(q0) + tot*fac -> primitive (spatial/eulerForwardUpdate.h:76-85)
+// cons(q0) + tot*fac -> solution basis (spatial/eulerForwardUpdate.h:76-85); a conserved
+// field is its own conserved set (set2Set of the same type copies)
 template <class R> __device__ __forceinline__ void forward_update(const Gas<R>& g, const R* q0, const R* tot, R fac,
-                                                                  R* qn) {
+                                                                  R* qn, bool cons) {
+  if (cons) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) qn[v] = q0[v] + tot[v] * fac;
+    return;
+  }
   // conserved set of q0: r u, r v, r, r h - p = p/(gamma-1) + r |u|^2/2
   R qc[4];
   R u2 = q0[0] * q0[0];
@@ -218,6 +225,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
 
   // ---- phase 3: face fluxes (i-faces then j-faces of the tile, each once)
   const Gas<C> g = gas_as<C>(a.gas);
+  const bool cons = a.basis != 0;  // conserved solution basis
   const int lim = a.limiter;
   constexpr int NFI = (TI + 1) * TJ, NFJ = TI * (TJ + 1);
   for (int k = tid; k < NFI + NFJ; k += NT) {
@@ -275,11 +283,9 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
               qR[v] = qr[v] - dr * limit<C>(lim, gc, gr);
             }
           }
-          F = face_flux<C, FK>(g, nx, ny, A, prim_state(g, qL[0], qL[1], qL[2], qL[3]),
-                               prim_state(g, qR[0], qR[1], qR[2], qR[3]));
+          F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, qL, cons), basis_state(g, qR, cons));
         } else {
-          F = face_flux<C, FK>(g, nx, ny, A, prim_state(g, ql[0], ql[1], ql[2], ql[3]),
-                               prim_state(g, qr[0], qr[1], qr[2], qr[3]));
+          F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, ql, cons), basis_state(g, qr, cons));
         }
       } else {
         // boundary face: interior cell is the right cell on sides 0/2, the left on 1/3
@@ -295,7 +301,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
           C qw[4];
 #pragma unroll
           for (int v = 0; v < 4; ++v) qw[v] = qi[v] - (M(2 * v, ia, ib) * wx + M(2 * v + 1, ia, ib) * wy);
-          F = wall_flux(g, nx, ny, A, qw);
+          F = wall_flux(g, nx, ny, A, qw, cons);
         } else {
           const int nfs = idir ? nj : ni;
           C qg[4];
@@ -305,8 +311,9 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
           for (int v = 0; v < 4; ++v) { qref[v] = a.gref[side][size_t(v) * nfs + kf]; qir[v] = cvt<R>(qi[v]); }
           const R sgn = int_right ? R(1) : R(-1);  // normal into the domain
           const R nxr = cvt<R>(nx), nyr = cvt<R>(ny);
-          if (bct == BC_RIEMANN) farfield_update<R, BC_RIEMANN>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr);
-          else if (bct == BC_ENTROPY) farfield_update<R, BC_ENTROPY>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr);
+          if (bct == BC_RIEMANN) farfield_update<R, BC_RIEMANN>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr, cons);
+          else if (bct == BC_ENTROPY)
+            farfield_update<R, BC_ENTROPY>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr, cons);
           else {
 #pragma unroll
             for (int v = 0; v < 4; ++v) qgr[v] = qref[v];
@@ -329,8 +336,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
 #pragma unroll
             for (int v = 0; v < 4; ++v) { qL[v] = int_right ? qg[v] : qi[v]; qR[v] = int_right ? qi[v] : qg[v]; }
           }
-          F = face_flux<C, FK>(g, nx, ny, A, prim_state(g, qL[0], qL[1], qL[2], qL[3]),
-                               prim_state(g, qR[0], qR[1], qR[2], qR[3]));
+          F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, qL, cons), basis_state(g, qR, cons));
         }
       }
     }
@@ -411,7 +417,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   R q0[4], qn[4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) q0[v] = a.q0[v * ncell + c];
-  forward_update(a.gas, q0, tot, fac, qn);
+  forward_update(a.gas, q0, tot, fac, qn, a.basis != 0);
 #pragma unroll
   for (int v = 0; v < 4; ++v) a.q_out[v * ncell + c] = qn[v];
   flag_nonphysical(a.info, qn, int(c));
@@ -438,7 +444,7 @@ __global__ void __launch_bounds__(TI * TJ, (StageResidency<R, C, TI * TJ>::value
 template <class R>
 __device__ __forceinline__ void update0_cell(size_t c, size_t ncell, const Gas<R>& g, const R* __restrict__ q0,
                                              const R* __restrict__ res0, const R* __restrict__ vol, R alpha00,
-                                             R dts, StepInfo* info, R* __restrict__ q_out) {
+                                             R dts, StepInfo* info, R* __restrict__ q_out, bool cons) {
   R tot[4], q[4], qn[4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
@@ -446,7 +452,7 @@ __device__ __forceinline__ void update0_cell(size_t c, size_t ncell, const Gas<R
     q[v] = q0[v * ncell + c];
   }
   const R fac = dts / vol[c];
-  forward_update(g, q, tot, fac, qn);
+  forward_update(g, q, tot, fac, qn, cons);
 #pragma unroll
   for (int v = 0; v < 4; ++v) q_out[v * ncell + c] = qn[v];
   flag_nonphysical(info, qn, int(c));
@@ -460,7 +466,7 @@ template <class R> __device__ __forceinline__ R global_dt(const StepInfo* info, 
 template <class R>
 __global__ void update0_kernel(int ni, int nj, Gas<R> g, const R* __restrict__ q0, const R* __restrict__ res0,
                                const R* __restrict__ vol, R alpha00, R beta0, double cfl, StepInfo* info,
-                               R* __restrict__ q_out, int advance_time) {
+                               R* __restrict__ q_out, int advance_time, int basis) {
   const size_t ncell = size_t(ni) * nj;
   const R dt = global_dt<R>(info, cfl);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -469,7 +475,7 @@ __global__ void update0_kernel(int ni, int nj, Gas<R> g, const R* __restrict__ q
   }
   const R dts = beta0 * dt;
   for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < ncell; c += size_t(gridDim.x) * blockDim.x)
-    update0_cell(c, ncell, g, q0, res0, vol, alpha00, dts, info, q_out);
+    update0_cell(c, ncell, g, q0, res0, vol, alpha00, dts, info, q_out, basis != 0);
 }
 
 // ---------------------------------------------------------------- batched path
@@ -506,6 +512,7 @@ template <class R> struct BatchArgs {
   int stage, mode;
   R beta, cfl;
   StepInfo* info;          // one per instance
+  int basis;               // solution basis: 0 primitive, 1 conserved
 };
 
 template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const BatchArgs<R>& b, int k) {
@@ -515,6 +522,7 @@ template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const B
   for (int s = 0; s < 4; ++s) a.bc[s] = in.bc[s];
   a.gas = b.gas;
   a.limiter = b.limiter;
+  a.basis = b.basis;
   const long long n = (long long)in.ni * in.nj;
   const long long off4 = 4 * in.cell, off5 = 5 * in.cell;
   a.q = b.q + off4;
@@ -587,7 +595,7 @@ __global__ void __launch_bounds__(TI * TJ) batch_update0_kernel(const BatchArgs<
     const size_t ncell = size_t(in.ni) * in.nj;
     const size_t c = size_t(gi) * in.nj + gj;
     update0_cell(c, ncell, b.gas, b.q0 + 4 * in.cell, b.res_out + 5 * in.cell, b.vol + in.cell, alpha00,
-                 beta0 * dt, info, b.q_out + 4 * in.cell);
+                 beta0 * dt, info, b.q_out + 4 * in.cell, b.basis != 0);
   }
 }
 

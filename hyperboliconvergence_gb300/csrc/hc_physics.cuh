@@ -107,6 +107,12 @@ template <class R> __host__ __device__ __forceinline__ St<R> cons_state(const Ga
   return s;
 }
 
+// set2State of the solution basis: primitive {u, v, rho, p} or conserved
+// {rho u, rho v, rho, rho E} (cons = true); the choice is uniform across a launch
+template <class R> __host__ __device__ __forceinline__ St<R> basis_state(const Gas<R>& g, const R* q, bool cons) {
+  return cons ? cons_state(g, q) : prim_state(g, q[0], q[1], q[2], q[3]);
+}
+
 // state2Set<conserved> (conservationLaws/euler/transforms/conserved.ipp:2-29)
 template <class R> __host__ __device__ __forceinline__ void state_cons(const St<R>& s, R* qc) {
   qc[0] = s.r * s.u; qc[1] = s.r * s.v; qc[2] = s.r; qc[3] = s.r * s.h - s.p;
@@ -509,12 +515,13 @@ template <class R> __host__ __device__ __forceinline__ void roe_avg_vel(const St
 // and entropy/pressure far field (entropy.ipp:18-88).  (nx,ny) points into the
 // domain; qi, qf, qb are primitive.
 template <class R, int BK>
-__host__ __device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, R ny, const R* qi, const R* qf, R* qb) {
+__host__ __device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, R ny, const R* qi, const R* qf, R* qb,
+                                                         bool cons = false) {
   const R tx = -ny, ty = nx;
   const R ri[4] = {nx * qi[0] + ny * qi[1], tx * qi[0] + ty * qi[1], qi[2], qi[3]};
   const R rf[4] = {nx * qf[0] + ny * qf[1], tx * qf[0] + ty * qf[1], qf[2], qf[3]};
-  const St<R> sI = prim_state(g, ri[0], ri[1], ri[2], ri[3]);
-  const St<R> sF = prim_state(g, rf[0], rf[1], rf[2], rf[3]);
+  const St<R> sI = basis_state(g, ri, cons);
+  const St<R> sF = basis_state(g, rf, cons);
   R uav[2], u2a, a2a;
   roe_avg_vel(sI, sF, uav, &u2a, &a2a, g);
   const R thr = (BK == BC_RIEMANN) ? R(0.001) : R(0.0001);
@@ -550,6 +557,10 @@ __host__ __device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, 
     const R rb = pow(pb / sb, R(1) / g.gamma);
     b[0] = sU.u; b[1] = sU.v; b[2] = rb; b[3] = pb;
   }
+  if (cons) {  // set2Set to the conserved basis in the face frame, then rotate back
+    const St<R> sb = prim_state(g, b[0], b[1], b[2], b[3]);
+    state_cons(sb, b);
+  }
   qb[0] = nx * b[0] + tx * b[1];
   qb[1] = ny * b[0] + ty * b[1];
   qb[2] = b[2]; qb[3] = b[3];
@@ -557,8 +568,9 @@ __host__ __device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, 
 
 // Inviscid wall (conservationLaws/euler/boundary/inviscidWall.ipp:33-72): pressure
 // flux only, from the interior state moved to the face (qw primitive).
-template <class R> __host__ __device__ __forceinline__ Flux5<R> wall_flux(const Gas<R>& g, R nx, R ny, R A, const R* qw) {
-  const St<R> s = prim_state(g, qw[0], qw[1], qw[2], qw[3]);
+template <class R>
+__host__ __device__ __forceinline__ Flux5<R> wall_flux(const Gas<R>& g, R nx, R ny, R A, const R* qw, bool cons = false) {
+  const St<R> s = basis_state(g, qw, cons);
   Flux5<R> o;
   o.f[0] = A * s.p * nx;
   o.f[1] = A * s.p * ny;

@@ -64,7 +64,7 @@ class Solver:
 
     def __init__(self, mesh: Mesh, bc, ref=None, flux="roe", limiter="vanleer", rk="ssp34",
                  precision="fp64", dt="global", cfl=0.5, species=(1.4, 287.058, 1e-4), stream=None, law="euler",
-                 low_mach=None):
+                 low_mach=None, basis="primitive"):
         self.lib = _capi.load()
         self.mesh = mesh
         self.precision = precision
@@ -73,7 +73,8 @@ class Solver:
         cfg = Config(FLUX[flux] if isinstance(flux, str) else int(flux),
                      LIMITER[limiter] if isinstance(limiter, str) else int(limiter),
                      RK[rk] if isinstance(rk, str) else int(rk),
-                     PRECISION[precision], DTMODE[dt], float(cfl), _capi.LAW[law])
+                     PRECISION[precision], DTMODE[dt], float(cfl), _capi.LAW[law], _capi.BASIS[basis])
+        self.basis = basis
         self.law = law
         self.nv = 3 if law == "scalar" else 4  # conserved variables: {u, v, q} or {u, v, rho, p}
         h = C.c_void_p()
@@ -185,7 +186,8 @@ class Solver:
 
     # -- solution field ------------------------------------------------------
     def set_state(self, prim: np.ndarray) -> None:
-        """Upload the state: primitive {u, v, rho, p} (Euler) or conserved {u, v, q}
+        """Upload the state in the solver's basis: primitive {u, v, rho, p} (Euler, the
+        default), conserved {rho u, rho v, rho, rho E} (Euler, basis="conserved"), or {u, v, q}
         (scalar advection), shape (nv, ni, nj)."""
         a = np.ascontiguousarray(prim, dtype=np.float64)
         if a.shape != (self.nv, self.mesh.ni, self.mesh.nj):

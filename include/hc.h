@@ -59,6 +59,17 @@ typedef enum {
   HC_LIM_CADA3 = 9
 } hc_limiter;
 
+/* Basis of the solution field: the SolVarT of SolutionField<SolVarT,2>
+ * (solutionField/solutionField.h:56-91).  Gradients, reconstruction and limiting act on
+ * the basis variables; fluxes reach the State through set2State of the basis
+ * (conservationLaws/euler/transforms/primitive.ipp:101-137, conserved.ipp:31-76); the RK
+ * update goes through the conserved set (spatial/eulerForwardUpdate.h:38-92).  State
+ * uploads/downloads and ghost reference layers are in the basis.  Euler law only. */
+typedef enum {
+  HC_BASIS_PRIMITIVE = 0, /* {u, v, rho, p}, the reference drivers' choice (cylinder2D.cpp:110) */
+  HC_BASIS_CONSERVED = 1  /* {rho u, rho v, rho, rho E} */
+} hc_basis;
+
 /* Runge-Kutta table (ODE::Explicit, ode.h:107-197) */
 typedef enum { HC_RK_SSP11 = 0, HC_RK_SSP22 = 1, HC_RK_SSP33 = 2, HC_RK_SSP34 = 3 } hc_rk;
 
@@ -94,6 +105,7 @@ typedef struct {
   int dt_mode;   /* hc_dtmode */
   double cfl;    /* UnsteadyTimeControls::cfl (controls.h:11-19) */
   int law;       /* hc_law; 0 = Euler */
+  int basis;     /* hc_basis of the state and ghost layers; 0 = primitive */
 } hc_config;
 
 typedef struct {
@@ -129,12 +141,13 @@ int hc_set_species(hc_ctx* ctx, double gamma, double gas_constant, double minf);
 int hc_set_low_mach(hc_ctx* ctx, int velocity_scaling, int pressure_scaling, double lref, double dt);
 
 /* SolutionField::bcTypes and the reference layer of SolutionField::boundary
- * (solutionField/solutionField.h:56-91).  ref[side] holds 4 planes of primitive
- * values, one per boundary face (nj faces on sides 0/1, ni on 2/3); NULL for
- * periodic or wall sides. */
+ * (solutionField/solutionField.h:56-91).  ref[side] holds 4 planes of values in the
+ * context's basis (hc_config.basis), one per boundary face (nj faces on sides 0/1, ni
+ * on 2/3); NULL for periodic or wall sides. */
 int hc_set_bcs(hc_ctx* ctx, const int bc_type[4], const double* const ref[4]);
 
-/* SolutionField::interior in the primitive basis {u, v, rho, p}. */
+/* SolutionField::interior, 4 planes in the context's basis: primitive {u, v, rho, p}
+ * (HC_BASIS_PRIMITIVE, the default) or conserved {rho u, rho v, rho, rho E}. */
 int hc_state_upload(hc_ctx* ctx, const double* prim_soa);
 int hc_state_download(hc_ctx* ctx, double* prim_soa);
 /* Same through device pointers of the context's precision (no host copy). */

@@ -628,20 +628,42 @@ template <class R> RKTable<R> rk_table(int kind) {
   return t;
 }
 
+// ---------------------------------------------------------------- solution basis
+// The basis of the solution field (the SolVarT of SolutionField<SolVarT,2>): primitive
+// {u, v, rho, p}, as in the reference drivers (cylinder2D.cpp:110, gresho2D.cpp:112), or
+// conserved {rho u, rho v, rho, rho E}; the residual glue, boundary updates and fluxes are
+// generic over it and reach the State through set2State of the basis.
+enum Basis { BASIS_PRIMITIVE = 0, BASIS_CONSERVED = 1 };
+template <class R> State<R> basis2state(const Species<R>& sp, const R* q, int basis) {
+  return basis == BASIS_CONSERVED ? cons2state(sp, q) : prim2state(sp, q);
+}
+
 // ---------------------------------------------------------------- boundary physics
 // boundaryUpdate for Riemann invariants (conservationLaws/euler/boundary/riemann.ipp:18-113),
-// entropy/pressure (entropy.ipp:18-88); qi/qf are primitive, face normal points into the domain.
-template <class R> void bc_riemann(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf, R* qb) {
+// entropy/pressure (entropy.ipp:18-88); qi/qf/qb in the solution basis, face normal into the domain.
+// The subsonic result is built as a primitive set in the face frame, converted to the
+// basis (set2Set) and rotated back, as the reference composes it.
+template <class R> void basis_from_face(const Species<R>& sp, const Face<R>& f, const R* qbr, R* qb, int basis) {
+  if (basis == BASIS_CONSERVED) {
+    R c[4];
+    prim2cons(sp, qbr, c);
+    rotate_from(f, c, qb);
+  } else {
+    rotate_from(f, qbr, qb);
+  }
+}
+template <class R>
+void bc_riemann(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf, R* qb, int basis = BASIS_PRIMITIVE) {
   const R gam = sp.gamma, gam1 = sp.gamma1;
   R ri[4], rf[4];
   rotate_to(f, qi, ri); rotate_to(f, qf, rf);
-  const State<R> sA = roe_average(sp, prim2state(sp, ri), prim2state(sp, rf));
+  const State<R> sA = roe_average(sp, basis2state(sp, ri, basis), basis2state(sp, rf, basis));
   if ((sA.u[0] / sqrt(sA.u2)) < 0.001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; return; }
   const R ma = sA.u[0] / sqrt(sA.a2);
   const bool inflow = ma > 0;
   const R* quw = inflow ? qf : qi;
   if (abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; return; }
-  const State<R> sI = prim2state(sp, ri), sF = prim2state(sp, rf);
+  const State<R> sI = basis2state(sp, ri, basis), sF = basis2state(sp, rf, basis);
   const R ai = sqrt(sI.a2), af = sqrt(sF.a2);
   const R uni = sI.u[0], unf = sF.u[0];
   const R rim = uni - 2. * ai * gam1;
@@ -650,20 +672,21 @@ template <class R> void bc_riemann(const Species<R>& sp, const Face<R>& f, const
   const R ab = 0.25 * (gam - 1.) * (rip - rim);
   R ru[4];
   rotate_to(f, quw, ru);
-  const State<R> sU = prim2state(sp, ru);
+  const State<R> sU = basis2state(sp, ru, basis);
   const R sb = sU.a2 / (gam * pow(sU.r, gam - 1.));
   const R vb = sU.u[1];
   const R rb = pow(ab * ab / (gam * sb), gam1);
   const R pb = rb * ab * ab / gam;
   const R qbr[4] = {ub, vb, rb, pb};
-  rotate_from(f, qbr, qb);
+  basis_from_face(sp, f, qbr, qb, basis);
 }
 
-template <class R> void bc_entropy(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf, R* qb) {
+template <class R>
+void bc_entropy(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf, R* qb, int basis = BASIS_PRIMITIVE) {
   const R gam = sp.gamma;
   R ri[4], rf[4];
   rotate_to(f, qi, ri); rotate_to(f, qf, rf);
-  const State<R> sA = roe_average(sp, prim2state(sp, ri), prim2state(sp, rf));
+  const State<R> sA = roe_average(sp, basis2state(sp, ri, basis), basis2state(sp, rf, basis));
   if ((sA.u[0] / sqrt(sA.u2)) < 0.0001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; return; }
   const R ma = sA.u[0] / sqrt(sA.a2);
   const bool inflow = ma > 0;
@@ -672,22 +695,23 @@ template <class R> void bc_entropy(const Species<R>& sp, const Face<R>& f, const
   if (abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; return; }
   R ru[4], rd[4];
   rotate_to(f, quw, ru); rotate_to(f, qdw, rd);
-  const State<R> sU = prim2state(sp, ru), sD = prim2state(sp, rd);
+  const State<R> sU = basis2state(sp, ru, basis), sD = basis2state(sp, rd, basis);
   const R pb = sD.p;
   const R sb = sU.a2 / (gam * pow(sU.r, gam - 1.));
   const R rb = pow(pb / sb, 1. / gam);
   const R qbr[4] = {sU.u[0], sU.u[1], rb, pb};
-  rotate_from(f, qbr, qb);
+  basis_from_face(sp, f, qbr, qb, basis);
 }
 
 // boundaryFlux for an inviscid wall (conservationLaws/euler/boundary/inviscidWall.ipp:33-72):
 // pressure-only flux from q_wall = q_interior - dq, dq the gradient increment
 // from the face to the cell centre.
-template <class R> FluxRes<R> wall_flux(const Species<R>& sp, const Face<R>& f, const R* qi, const R* dq) {
+template <class R>
+FluxRes<R> wall_flux(const Species<R>& sp, const Face<R>& f, const R* qi, const R* dq, int basis = BASIS_PRIMITIVE) {
   const int direction = -1;
   R qw[4];
   for (int k = 0; k < 4; ++k) qw[k] = qi[k] + direction * dq[k];
-  const State<R> sw = prim2state(sp, qw);
+  const State<R> sw = basis2state(sp, qw, basis);
   const R pw = sw.p;
   FluxRes<R> o;
   for (int i = 0; i < 2; ++i) o.f[i] = f.area * pw * f.n[i];

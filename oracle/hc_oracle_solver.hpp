@@ -29,6 +29,7 @@ template <class R> struct Solver {
   Species<R> sp{};
   int flux = FLUX_ROE, lim = LIM_VANLEER, rk = RK_SSP34, dtmode = DT_GLOBAL;
   int vscale = SCALING_CONVECTIVE, pscale = SCALING_CONVECTIVE;  // AUSM+up low-Mach scaling
+  int basis = BASIS_PRIMITIVE;  // solution basis of q and of the ghost layers
   R cfl = 0.5;
   int bc[4] = {BC_PERIODIC, BC_PERIODIC, BC_PERIODIC, BC_PERIODIC};
   // ghost arrays per side: [side][face][layer][var]; layer 0 = ghost value,
@@ -36,7 +37,7 @@ template <class R> struct Solver {
   std::vector<R> ghost[4];
   std::vector<Cell<R>> cells;
   std::vector<XM<R>> xm;       // full xmetric per cell
-  std::vector<R> q0, q1, q2;   // primitive AoS [cell][4]
+  std::vector<R> q0, q1, q2;   // solution-basis AoS [cell][4]
   std::vector<R> lam0;         // stage-0 spectral radius sums (local dt)
   std::vector<FluxRes<R>> res[4], rtot;
   std::vector<QM<R>> qm;
@@ -45,6 +46,7 @@ template <class R> struct Solver {
   const R* node(int i, int j) const { return &nodes[(size_t(i) * (nj + 1) + j) * 2]; }
   size_t cid(int i, int j) const { return size_t(i) * nj + j; }
   int nface(int side) const { return side < 2 ? nj : ni; }
+  State<R> st(const R* q) const { return basis2state(sp, q, basis); }
 
   // periodic shift across the i (or j) boundary at face index k: image of the
   // last cell = its centre minus the shift (average over the face's two nodes)
@@ -157,8 +159,8 @@ template <class R> struct Solver {
         R* g = &ghost[side][size_t(k) * 8];
         const R* ref = g + 4;
         const R* qi = &q[size_t(side_cell(side, k)) * 4];
-        if (bc[side] == BC_RIEMANN) bc_riemann(sp, bface_in(side, k), qi, ref, g);
-        else if (bc[side] == BC_ENTROPY) bc_entropy(sp, bface_in(side, k), qi, ref, g);
+        if (bc[side] == BC_RIEMANN) bc_riemann(sp, bface_in(side, k), qi, ref, g, basis);
+        else if (bc[side] == BC_ENTROPY) bc_entropy(sp, bface_in(side, k), qi, ref, g, basis);
         else for (int v = 0; v < 4; ++v) g[v] = ref[v];  // Fixed (boundaryCondition.h:63-80); wall ghost unused
       }
     }
@@ -202,7 +204,7 @@ template <class R> struct Solver {
   FluxRes<R> muscl(const Face<R>& f, const R* cl, const R* cr, const R* ql, const R* qr,
                    const XM<R>& xl, const XM<R>& xr, const QM<R>& ml, const QM<R>& mr) const {
     if (lim == LIM_NOLIMIT1)  // first-order overload (spatial/muscl.h:62-87)
-      return face_flux(flux, sp, f, prim2state(sp, ql), prim2state(sp, qr), vscale, pscale);
+      return face_flux(flux, sp, f, st(ql), st(qr), vscale, pscale);
     const R dxc[2] = {cr[0] - cl[0], cr[1] - cl[1]};
     R dqc[4];
     for (int v = 0; v < 4; ++v) dqc[v] = qr[v] - ql[v];
@@ -229,7 +231,7 @@ template <class R> struct Solver {
       qL[v] = ql[v] + dl * sl;
       qR[v] = qr[v] - dr * sr;
     }
-    return face_flux(flux, sp, f, prim2state(sp, qL), prim2state(sp, qR), vscale, pscale);
+    return face_flux(flux, sp, f, st(qL), st(qR), vscale, pscale);
   }
 
   // ghost face (D4): ghost side is not reconstructed, interior side is MUSCL
@@ -240,7 +242,7 @@ template <class R> struct Solver {
     const bool ghost_left = (side == 0 || side == 2);
     const R* ql = ghost_left ? qg : qi;
     const R* qr = ghost_left ? qi : qg;
-    if (lim == LIM_NOLIMIT1) return face_flux(flux, sp, f, prim2state(sp, ql), prim2state(sp, qr), vscale, pscale);
+    if (lim == LIM_NOLIMIT1) return face_flux(flux, sp, f, st(ql), st(qr), vscale, pscale);
     const R* cc = cells[c].c;
     R d = 0; d += (f.c[0] - cc[0]) * (f.c[0] - cc[0]); d += (f.c[1] - cc[1]) * (f.c[1] - cc[1]);
     const R dd = sqrt(d);
@@ -259,7 +261,7 @@ template <class R> struct Solver {
       if (ghost_left) { qL[v] = qg[v]; qR[v] = qi[v] - dd * s; }
       else { qL[v] = qi[v] + dd * s; qR[v] = qg[v]; }
     }
-    return face_flux(flux, sp, f, prim2state(sp, qL), prim2state(sp, qR), vscale, pscale);
+    return face_flux(flux, sp, f, st(qL), st(qR), vscale, pscale);
   }
 
   static void acc_sub(FluxRes<R>& a, const FluxRes<R>& f) { for (int v = 0; v < 4; ++v) a.f[v] -= f.f[v]; a.lam += f.lam; }
@@ -319,7 +321,7 @@ template <class R> struct Solver {
           const R dir[2] = {cells[c].c[0] - f.c[0], cells[c].c[1] - f.c[1]};
           R dq[4];
           solve(factor(xm[c]), qm[c], dir, dq);
-          acc_add(r[c], wall_flux(sp, f, &q[c * 4], dq));
+          acc_add(r[c], wall_flux(sp, f, &q[c * 4], dq, basis));
         }
       } else {
         // ghost-cell loop (ghostCellLoop.h:109-228)
@@ -362,10 +364,14 @@ template <class R> struct Solver {
           R fac;
           if (dtmode == DT_GLOBAL) { const R dts = tab.beta[s] * dt; fac = dts / cells[c].vol; }
           else { const R cs = tab.beta[s] * cfl; fac = cs / lam0[c]; }
+          // solution basis -> conserved (+ increment) -> solution basis; a conserved
+          // field is its own conserved set (set2Set of the same type copies)
           R qc[4];
-          prim2cons(sp, &q0[c * 4], qc);
+          if (basis == BASIS_CONSERVED) for (int v = 0; v < 4; ++v) qc[v] = q0[c * 4 + v];
+          else prim2cons(sp, &q0[c * 4], qc);
           for (int v = 0; v < 4; ++v) qc[v] = qc[v] + tot[v] * fac;
-          cons2prim(sp, qc, &q2[c * 4]);
+          if (basis == BASIS_CONSERVED) for (int v = 0; v < 4; ++v) q2[c * 4 + v] = qc[v];
+          else cons2prim(sp, qc, &q2[c * 4]);
         }
         std::swap(q1, q2);
       }

@@ -42,6 +42,8 @@ void* hco_create(int ni, int nj, const double* nodes, const int* bc, int flux, i
   return s;
 }
 void hco_destroy(void* h) { delete static_cast<S*>(h); }
+// solution basis (BASIS_*) of the state and ghost layers
+void hco_set_basis(void* h, int basis) { static_cast<S*>(h)->basis = basis; }
 // AUSM+up low-Mach scaling pair (SCALING_*) and the species' lref and dt
 void hco_set_low_mach(void* h, int vscale, int pscale, double lref, double dt) {
   S* s = static_cast<S*>(h);
@@ -143,6 +145,22 @@ void hco_prim2cons(const double* species, const double* q, double* qc) {
 }
 void hco_cons2prim(const double* species, const double* qc, double* q) {
   cons2prim(make_species(species), qc, q);
+}
+// the pointwise functions on a field of basis `basis` (BASIS_*): flux, boundary update, wall flux
+void hco_flux_basis(int kind, int basis, const double* species, const double* face, const double* ql,
+                    const double* qr, double* out5) {
+  const Species<double> sp = make_species(species);
+  put_flux(face_flux(kind, sp, make_face(face), basis2state(sp, ql, basis), basis2state(sp, qr, basis)), out5);
+}
+void hco_bc_update_basis(int kind, int basis, const double* species, const double* face, const double* qi,
+                         const double* qf, double* qb) {
+  const Species<double> sp = make_species(species);
+  if (kind == BC_RIEMANN) bc_riemann(sp, make_face(face), qi, qf, qb, basis);
+  else bc_entropy(sp, make_face(face), qi, qf, qb, basis);
+}
+void hco_wall_flux_basis(int basis, const double* species, const double* face, const double* qi, const double* dq,
+                         double* out5) {
+  put_flux(wall_flux(make_species(species), make_face(face), qi, dq, basis), out5);
 }
 // kind: 2 = Riemann, 3 = Entropy (face normal into the domain)
 void hco_bc_update(int kind, const double* species, const double* face, const double* qi,

@@ -22,6 +22,7 @@ _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 # enum values shared with oracle/hc_oracle.hpp and include/hc.h
 FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5, "roe_ws": 6}
 SCALING = {"convective": 0, "acoustic": 1, "adaptive": 2}
+BASIS = {"primitive": 0, "conserved": 1}
 LIMITER = {"nolimit1": 0, "nolimit2": 1, "nolimit3": 2, "vanalbada": 3, "minmod": 4,
            "superbee": 5, "mc": 6, "vanleer": 7, "vanleer_ref": 8, "cada3": 9}
 BC = {"periodic": 0, "fixed": 1, "riemann": 2, "entropy": 3, "wall": 4}
@@ -83,6 +84,48 @@ class Pointwise:
         out = np.empty(5)
         self.fn("ausmpup_scaled")(int(vscale), int(pscale), np.asarray(species5, dtype=np.float64),
                                   face, ql, qr, out)
+        return out
+
+    # conserved-basis fields (BASIS "conserved"): the oracle's hco_*_basis functions or
+    # the reference probe's ref_*_cons functions
+    def _basis_fn(self, name):
+        i, dpp = C.c_int, _dp
+        if self.p == "hco_":
+            f = self.fn(name + "_basis")
+            f.argtypes = {"flux": [i, i, dpp, dpp, dpp, dpp, dpp], "bc_update": [i, i, dpp, dpp, dpp, dpp, dpp],
+                          "wall_flux": [i, dpp, dpp, dpp, dpp, dpp]}[name]
+        else:
+            f = self.fn(name + "_cons")
+            f.argtypes = {"flux": [i, dpp, dpp, dpp, dpp, dpp], "bc_update": [i, dpp, dpp, dpp, dpp, dpp],
+                          "wall_flux": [dpp, dpp, dpp, dpp, dpp]}[name]
+        f.restype = None
+        return f
+
+    def flux_cons(self, kind, species, face, ql, qr):
+        out = np.empty(5)
+        f = self._basis_fn("flux")
+        if self.p == "hco_":
+            f(kind, 1, species, face, ql, qr, out)
+        else:
+            f(kind, species, face, ql, qr, out)
+        return out
+
+    def bc_update_cons(self, kind, species, face, qi, qf):
+        out = np.empty(4)
+        f = self._basis_fn("bc_update")
+        if self.p == "hco_":
+            f(kind, 1, species, face, qi, qf, out)
+        else:
+            f(kind, species, face, qi, qf, out)
+        return out
+
+    def wall_flux_cons(self, species, face, qi, dq):
+        out = np.empty(5)
+        f = self._basis_fn("wall_flux")
+        if self.p == "hco_":
+            f(1, species, face, qi, dq, out)
+        else:
+            f(species, face, qi, dq, out)
         return out
 
     def exact_flux(self, species, normal, q):
@@ -196,7 +239,8 @@ class OracleSolver:
     """CPU restatement of the reference integrate() over one 2D structured mesh."""
 
     def __init__(self, ni, nj, nodes, bc, flux="roe", limiter="vanleer", rk="ssp34", dt="global",
-                 cfl=0.5, species=(1.4, 287.058, 1e-4), ghost_ref=None, fast=False, low_mach=None):
+                 cfl=0.5, species=(1.4, 287.058, 1e-4), ghost_ref=None, fast=False, low_mach=None,
+                 basis="primitive"):
         self.lib = load(fast)
         self.ni, self.nj = ni, nj
         bcv = np.array([BC[b] if isinstance(b, str) else int(b) for b in bc], dtype=np.int32)
@@ -206,6 +250,8 @@ class OracleSolver:
                                      RK[rk] if isinstance(rk, str) else rk,
                                      DT[dt] if isinstance(dt, str) else dt,
                                      float(cfl), np.asarray(species, dtype=np.float64))
+        self.lib.hco_set_basis.argtypes = [C.c_void_p, C.c_int]
+        self.lib.hco_set_basis(self.h, BASIS[basis] if isinstance(basis, str) else int(basis))
         if low_mach is not None:
             # (velocity scaling, pressure scaling, lref, species dt) of AUSM+up
             vs, ps, lref, sdt = low_mach

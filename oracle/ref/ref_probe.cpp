@@ -199,6 +199,50 @@ void ref_wall_flux(const double* species, const double* face, const double* qi, 
                    prim_of(qi), prim_of(qi)),
       out5);
 }
+// The same pointwise functions on a solution field in the conserved basis
+// {rho u, rho v, rho, rho E}: inputs and outputs are ConsSet / ConsDel.
+static ConsSet cons_of(const double* q) { return ConsSet{q[0], q[1], q[2], q[3]}; }
+void ref_flux_cons(int kind, const double* species, const double* face, const double* ql, const double* qr,
+                   double* out5) {
+  const auto sp = species_of(species);
+  const auto f = face_of(face);
+  const ConsSet l = cons_of(ql), r = cons_of(qr);
+  switch (kind) {
+    case 0: put(RoeFlux<Law>{}(sp, f, l, r), out5); break;
+    case 2: put(Slau<LowMachScaling::Convective, LowMachScaling::Acoustic>{}(sp, f, l, r), out5); break;
+    case 3: put(AusmPlusUP<LowMachScaling::Convective, LowMachScaling::Convective>{}(sp, f, l, r), out5); break;
+    case 4: put(RusanovFlux<Law>{}(sp, f, l, r), out5); break;
+    case 5: put(CentralFlux<Law>{}(sp, f, l, r), out5); break;
+    case 6: put(RoeUnprecWS{}(sp, f, l, r), out5); break;
+    default: for (int v = 0; v < 5; ++v) out5[v] = std::nan("");
+  }
+}
+void ref_bc_update_cons(int kind, const double* species, const double* face, const double* qi, const double* qf,
+                        double* qb) {
+  const auto sp = species_of(species);
+  const auto f = face_of(face);
+  geom::Volume<2, Real> cell;
+  cell.volume = 1.;
+  cell.centre = geom::Point<2, Real>{f.centre[0] + f.metric[0][0], f.centre[1] + f.metric[0][1]};
+  ConsSet r;
+  if (kind == 2)
+    r = boundaryUpdate(std::integral_constant<EulerBCs, EulerBCs::Riemann>{}, sp, f, cell, cons_of(qi), cons_of(qf));
+  else
+    r = boundaryUpdate(std::integral_constant<EulerBCs, EulerBCs::Entropy>{}, sp, f, cell, cons_of(qi), cons_of(qf));
+  for (int v = 0; v < 4; ++v) qb[v] = r[v];
+}
+void ref_wall_flux_cons(const double* species, const double* face, const double* qi, const double* dq,
+                        double* out5) {
+  const auto sp = species_of(species);
+  const auto f = face_of(face);
+  geom::Volume<2, Real> cell;
+  cell.volume = 1.;
+  cell.centre = f.centre;
+  const ConsDel d{dq[0], dq[1], dq[2], dq[3]};
+  put(boundaryFlux(std::integral_constant<EulerBCs, EulerBCs::InviscidWall>{}, sp, f, cell, d, cons_of(qi),
+                   cons_of(qi), cons_of(qi)),
+      out5);
+}
 // 0 cons->prim, 1 prim->cons, 2 prim->char, 3 char->prim about the state of q
 void ref_delta(int kind, const double* species, const double* q, const double* din, double* dout) {
   const auto sp = species_of(species);

@@ -122,6 +122,18 @@ def main():
     g["slau_scaled"] = np.stack([np.stack([np.stack([np.stack([slau_scaled(vs, ps, sp5, m) for m in range(ns)])
                                                      for ps in range(3)]) for vs in range(3)])
                                  for sp5 in g["ausm_species"]])
+    # a solution field in the conserved basis {rho u, rho v, rho, rho E}: fluxes, far-field
+    # updates and the wall flux on ConsSets (the reference's functions are generic over
+    # the basis and reach the State through set2State)
+    cl = np.stack([ref.prim2cons(species, q) for q in ql])
+    cr = np.stack([ref.prim2cons(species, q) for q in qr])
+    cf = np.stack([ref.prim2cons(species, q) for q in qf])
+    g["cons_ql"], g["cons_qr"], g["cons_qf"] = cl, cr, cf
+    for k in REF_FLUXES:
+        g[f"cons_flux_{k}"] = np.stack([ref.flux_cons(k, species, faces[m], cl[m], cr[m]) for m in range(nf)])
+    for k in (2, 3):
+        g[f"cons_bc_{k}"] = np.stack([ref.bc_update_cons(k, species, faces[m], cl[m], cf[m]) for m in range(nf)])
+    g["cons_wall_out"] = np.stack([ref.wall_flux_cons(species, faces[m], cl[m], dq[m]) for m in range(nf)])
     g["cyl_nodes"] = ref.cylinder_nodes(12, 16, 0.5, 20.0)
     g["lin_nodes"] = ref.linspace_nodes(9, 7, 0.0, 10.0, -1.0, 3.0)
     np.savez_compressed(OUT, **g)

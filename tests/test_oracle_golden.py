@@ -69,6 +69,25 @@ def test_ausmpup_scalings(g, o, vs, ps):
              want[vs, ps])
 
 
+@pytest.mark.parametrize("kind", [0, 2, 3, 4, 5, 6])
+def test_fluxes_conserved_basis(g, o, kind):
+    f, sp = g["surface_out"], g["species"]
+    got = [o.flux_cons(kind, sp, f[m], g["cons_ql"][m], g["cons_qr"][m]) for m in range(len(f))]
+    same(got, g[f"cons_flux_{kind}"])
+
+
+@pytest.mark.parametrize("kind", [2, 3])
+def test_boundary_updates_conserved_basis(g, o, kind):
+    f, sp = g["surface_out"], g["species"]
+    same([o.bc_update_cons(kind, sp, f[m], g["cons_ql"][m], g["cons_qf"][m]) for m in range(len(f))],
+         g[f"cons_bc_{kind}"])
+
+
+def test_wall_flux_conserved_basis(g, o):
+    f, sp = g["surface_out"], g["species"]
+    same([o.wall_flux_cons(sp, f[m], g["cons_ql"][m], g["wall_dq"][m]) for m in range(len(f))], g["cons_wall_out"])
+
+
 def test_exact_flux(g, o):
     f, sp = g["surface_out"], g["species"]
     same([o.exact_flux(sp, f[m][3:5].copy(), g["flux_ql"][m]) for m in range(len(f))], g["exact_flux"])
