@@ -235,6 +235,17 @@ def measure_precision(stream, steps: int, prec: str):
         return float((err / scale).max())
     out["error_vs_fp64_after_1_step"] = rel(states[prec][0], states["fp64"][0])
     out["error_vs_fp64_after_20_steps"] = rel(states[prec][1], states["fp64"][1])
+    # branch flips: the FP64 state after 20 steps evaluated at both precisions
+    from hyperboliconvergence_gb300.solver import branch_flips
+    sigs = {}
+    for p in (prec, "fp64"):
+        s = Solver(mesh, bc, ref, flux=FLUX, limiter=LIMITER, rk=RKT, precision=p, dt=DTMODE, cfl=CFL,
+                   species=species, stream=stream.cuda_stream)
+        s.set_state(states["fp64"][1])
+        sigs[p] = s.face_signatures()
+        s.close()
+    out["branch_flips_vs_fp64"] = branch_flips(sigs[prec], sigs["fp64"]) | {
+        "state": "the FP64 state after 20 steps, evaluated at both precisions"}
     return out
 
 

@@ -62,7 +62,15 @@ template <class R> struct StageArgs {
   R* q_out;           // next stage state (fused modes)
   int norm_stage0;    // accumulate the density-residual norm
   int basis;          // solution basis: 0 primitive, 1 conserved
+  unsigned long long* sig_i;  // branch signatures of the i-faces / j-faces (recording kernels only)
+  unsigned long long* sig_j;
 };
+
+// Branch signature of one face (recording kernels): bits 0-15 the limiter pieces of
+// the left side's four variables (limit_piece, 4 bits each), 16-31 the right side's,
+// 32-35 the flux branches (flux_bits), 36-37 the far-field path of a ghost face,
+// 63 set when the face was evaluated.
+enum : unsigned { SIG_FLUX_SHIFT = 32, SIG_BC_SHIFT = 36, SIG_VALID_SHIFT = 63 };
 
 enum { MODE_RESIDUAL = 0, MODE_RES_MAXRATE = 1, MODE_FUSED_GLOBAL = 2, MODE_FUSED_LOCAL = 3 };
 
@@ -140,7 +148,9 @@ template <class C, class R> __device__ __forceinline__ Gas<C> gas_as(const Gas<R
 // R is the storage type (state, residuals, update); C the type the tile's
 // gradients, reconstruction and fluxes are computed in (C = R, or double-float
 // for FP64 storage, reading the face records from a.fic / a.fjc).
-template <int TI, int TJ, class R, int FK, class C = R>
+// REC: the recording instantiation also writes each face's branch signature to
+// a.sig_i / a.sig_j (the production instantiations compile without it).
+template <int TI, int TJ, class R, int FK, class C = R, bool REC = false>
 __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj, unsigned char* smem_raw) {
   constexpr bool same = std::is_same<C, R>::value;
   using SM = StageSmem<TI, TJ, C>;
@@ -236,6 +246,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     bool valid = idir ? (gi <= ni && gj < nj) : (gi < ni && gj <= nj);
     Flux5<C> F;
     F.f[0] = F.f[1] = F.f[2] = F.f[3] = F.lam = C(0);
+    unsigned long long sg = 0;  // branch signature (REC)
     if (valid) {
       const C* rec = idir ? cfi : cfj;
       const int nf = idir ? nfi : nfj;
@@ -267,6 +278,12 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
             }
             limit4<C>(lim, gc, gl, sL);
             limit4<C>(lim, gc, gr, sR);
+            if constexpr (REC) {
+#pragma unroll
+              for (int v = 0; v < 4; ++v)
+                sg |= ((unsigned long long)limit_piece<C>(lim, gc[v], gl[v]) << (4 * v)) |
+                      ((unsigned long long)limit_piece<C>(lim, gc[v], gr[v]) << (16 + 4 * v));
+            }
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
               qL[v] = ql[v] + dl * sL[v];
@@ -281,11 +298,26 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
               const C gr = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
               qL[v] = ql[v] + dl * limit<C>(lim, gc, gl);
               qR[v] = qr[v] - dr * limit<C>(lim, gc, gr);
+              if constexpr (REC)
+                sg |= ((unsigned long long)limit_piece<C>(lim, gc, gl) << (4 * v)) |
+                      ((unsigned long long)limit_piece<C>(lim, gc, gr) << (16 + 4 * v));
             }
           }
-          F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, qL, cons), basis_state(g, qR, cons));
+          if constexpr (REC) {
+            const St<C> sL = basis_state(g, qL, cons), sR = basis_state(g, qR, cons);
+            F = face_flux<C, FK>(g, nx, ny, A, sL, sR);
+            sg |= (unsigned long long)flux_bits<C, FK>(g, nx, ny, sL, sR) << SIG_FLUX_SHIFT;
+          } else {
+            F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, qL, cons), basis_state(g, qR, cons));
+          }
         } else {
-          F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, ql, cons), basis_state(g, qr, cons));
+          if constexpr (REC) {
+            const St<C> sL = basis_state(g, ql, cons), sR = basis_state(g, qr, cons);
+            F = face_flux<C, FK>(g, nx, ny, A, sL, sR);
+            sg |= (unsigned long long)flux_bits<C, FK>(g, nx, ny, sL, sR) << SIG_FLUX_SHIFT;
+          } else {
+            F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, ql, cons), basis_state(g, qr, cons));
+          }
         }
       } else {
         // boundary face: interior cell is the right cell on sides 0/2, the left on 1/3
@@ -311,9 +343,13 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
           for (int v = 0; v < 4; ++v) { qref[v] = a.gref[side][size_t(v) * nfs + kf]; qir[v] = cvt<R>(qi[v]); }
           const R sgn = int_right ? R(1) : R(-1);  // normal into the domain
           const R nxr = cvt<R>(nx), nyr = cvt<R>(ny);
-          if (bct == BC_RIEMANN) farfield_update<R, BC_RIEMANN>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr, cons);
+          unsigned path = 0;
+          unsigned* pathp = REC ? &path : nullptr;
+          if (bct == BC_RIEMANN)
+            farfield_update<R, BC_RIEMANN>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr, cons, pathp);
           else if (bct == BC_ENTROPY)
-            farfield_update<R, BC_ENTROPY>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr, cons);
+            farfield_update<R, BC_ENTROPY>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr, cons, pathp);
+          if constexpr (REC) sg |= (unsigned long long)path << SIG_BC_SHIFT;
           else {
 #pragma unroll
             for (int v = 0; v < 4; ++v) qgr[v] = qref[v];
@@ -331,13 +367,25 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
               const C s = limit<C>(lim, dq * idlr, gb);
               if (int_right) { qL[v] = qg[v]; qR[v] = qi[v] - d * s; }
               else { qL[v] = qi[v] + d * s; qR[v] = qg[v]; }
+              if constexpr (REC)  // the interior side's limiter, in its side's slot
+                sg |= (unsigned long long)limit_piece<C>(lim, dq * idlr, gb) << ((int_right ? 16 : 0) + 4 * v);
             }
           } else {
 #pragma unroll
             for (int v = 0; v < 4; ++v) { qL[v] = int_right ? qg[v] : qi[v]; qR[v] = int_right ? qi[v] : qg[v]; }
           }
-          F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, qL, cons), basis_state(g, qR, cons));
+          if constexpr (REC) {
+            const St<C> sL = basis_state(g, qL, cons), sR = basis_state(g, qR, cons);
+            F = face_flux<C, FK>(g, nx, ny, A, sL, sR);
+            sg |= (unsigned long long)flux_bits<C, FK>(g, nx, ny, sL, sR) << SIG_FLUX_SHIFT;
+          } else {
+            F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, qL, cons), basis_state(g, qR, cons));
+          }
         }
+      }
+      if constexpr (REC) {
+        const int fidx_s = idir ? gi * nj + gj : gi * (nj + 1) + gj;
+        (idir ? a.sig_i : a.sig_j)[fidx_s] = sg | (1ull << SIG_VALID_SHIFT);
       }
     }
     C* dst = idir ? sfi : sfj;
@@ -437,6 +485,14 @@ __global__ void __launch_bounds__(TI * TJ, (StageResidency<R, C, TI * TJ>::value
     stage_kernel(const StageArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   stage_tile<TI, TJ, R, FK, C>(a, blockIdx.y, blockIdx.x, smem_raw);
+}
+
+// the recording variant (a diagnostic, not on the stepping path): the same tile with
+// each face's branch signature written out
+template <int TI, int TJ, class R, int FK, class C = R>
+__global__ void __launch_bounds__(TI * TJ) sig_kernel(const StageArgs<R> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  stage_tile<TI, TJ, R, FK, C, true>(a, blockIdx.y, blockIdx.x, smem_raw);
 }
 
 // Stage-0 update of one cell with the global timestep dt = cfl / max(lambda/V)

@@ -18,6 +18,10 @@ template <class R, int FK> cudaError_t prepare_stage();
 // persistent batched stage: `grid` CTAs walk the work list of b
 template <class R, int FK> cudaError_t launch_batch_stage(const BatchArgs<R>& b, int tile, int grid, cudaStream_t s);
 
+// recording stage (hc_sig_*.cu): one residual evaluation of the 8x32 tile writing the
+// face branch signatures to a.sig_i / a.sig_j; DF: double-float stage arithmetic
+template <class R, bool DF> cudaError_t launch_sig_stage(const StageArgs<R>& a, int flux, cudaStream_t s);
+
 // scalar advection law (hc_stage_scalar.cu): flux is FLUX_RUSANOV or FLUX_CENTRAL
 template <class R> cudaError_t prepare_scalar_stage();
 template <class R> cudaError_t launch_scalar_stage(const StageArgs<R>& a, int flux, int tile, cudaStream_t s);

@@ -493,6 +493,93 @@ template <class R> __host__ __device__ __forceinline__ R limit(int kind, R a, R 
   }
 }
 
+// ---------------------------------------------------------------- branch signatures
+// The parity report counts the faces (and cells) where the GPU and the oracle take a
+// different branch.  limit_piece: which piece of the limiter's piecewise definition
+// limit(a, b) evaluates, as 4 bits: bit 3 = (a > 0); bits 0-2 = the interval of the
+// ratio b/a (compared by multiplication, with u = |a| and v = b signed like a) that
+// selects the expression.  The oracle (oracle/hc_oracle.hpp) defines the same codes.
+template <class R> __host__ __device__ __forceinline__ unsigned limit_piece(int kind, R a, R b) {
+  const bool pos = a > R(0);
+  const R u = pos ? a : -a, v = pos ? b : -b;
+  unsigned p = 0;
+  switch (kind) {
+    case LIM_VANALBADA: p = (a * b < R(0)) ? 0u : 1u; break;
+    case LIM_VANLEER: p = (a * b > R(0)) ? 1u : 0u; break;
+    case LIM_MINMOD: p = (v <= R(0)) ? 0u : (v < u ? 1u : 2u); break;
+    case LIM_SUPERBEE:
+      p = (v <= R(0)) ? 0u : (R(2) * v < u ? 1u : (v < u ? 2u : (v < R(2) * u ? 3u : 4u)));
+      break;
+    case LIM_MC: p = (v <= R(0)) ? 0u : (R(3) * v < u ? 1u : (v < R(3) * u ? 2u : 3u)); break;
+    case LIM_CADA3: {
+      const R c1 = R(-2. / 7.), c2 = R(0.4), c3 = R(3) * R(1.5) - R(2);
+      if (!(fabs(a) + fabs(b) > R(0))) p = 7u;
+      else if (v < R(-2) * u) p = 1u;
+      else if (v < c1 * u) p = 2u;
+      else if (v < R(0)) p = 3u;
+      else if (v < c2 * u) p = 4u;
+      else if (v < c3 * u) p = 5u;
+      else p = 6u;
+      break;
+    }
+    default: return 0u;  // the unlimited and the literal van Leer expressions have one piece
+  }
+  return p | (pos ? 8u : 0u);
+}
+
+// Branches taken inside the interface flux of two face states (4 bits), with the
+// flux's own intermediate expressions: Roe -- Harten's fix active on the u-a and u+a
+// waves; SLAU -- |M_L| > 1, |M_R| > 1, Mach of the mean speed above 1; AUSM+up --
+// |M_L| > 1, |M_R| > 1, which side's critical speed is the interface sound speed;
+// Rusanov / central / RoeUnprecWS -- which side's spectral radius is the larger.
+template <class R, int FK>
+__host__ __device__ __forceinline__ unsigned flux_bits(const Gas<R>& g, R nx, R ny, const St<R>& l, const St<R>& r) {
+  const R unl = proj(nx, ny, l), unr = proj(nx, ny, r);
+  if constexpr (FK == FLUX_ROE) {
+    const R al = sqrt(l.a2), ar = sqrt(r.a2);
+    const R cr = sqrt(r.r * l.ir);
+    const R wl = R(1) / (R(1) + cr);
+    const R wr = R(1) - wl;
+    const R ua = wl * l.u + wr * r.u;
+    const R va = wl * l.v + wr * r.v;
+    R ka = ua * ua;
+    ka += va * va;
+    ka *= R(0.5);
+    const R ha = wl * l.h + wr * r.h;
+    const R aa = sqrt(g.gm1 * (ha - ka));
+    const R una = nx * ua + ny * va;
+    unsigned b = 0;
+    {
+      const R la1 = una - aa, ll1 = unl - al, lr1 = unr - ar;
+      const R le = R(0.05) * fmax(R(0), fmax(la1 - ll1, lr1 - la1));
+      if (!(fabs(la1) > le)) b |= 1u;
+    }
+    {
+      const R la2 = una + aa, ll2 = unl + al, lr2 = unr + ar;
+      const R le = R(0.05) * fmax(R(0), fmax(la2 - ll2, lr2 - la2));
+      if (!(fabs(la2) > le)) b |= 2u;
+    }
+    return b;
+  } else if constexpr (FK == FLUX_SLAU || FK == FLUX_SLAU_REF) {
+    const R ua = sqrt(R(0.5) * (l.u2 + r.u2));
+    const R aa = R(0.5) * (sqrt(l.a2) + sqrt(r.a2));
+    const R aa1 = R(1) / aa;
+    const R ml = unl * aa1, mr = unr * aa1;
+    return (fabs(ml) > R(1) ? 1u : 0u) | (fabs(mr) > R(1) ? 2u : 0u) | (ua * aa1 > R(1) ? 4u : 0u);
+  } else if constexpr (FK == FLUX_AUSMPUP) {
+    const R ascoeff = R(2) * g.gm1 / (g.gamma + R(1));
+    const R als2 = ascoeff * l.h, ars2 = ascoeff * r.h;
+    const R als = als2 / fmax(unl, sqrt(als2));
+    const R ars = ars2 / fmax(-unr, sqrt(ars2));
+    const R as = fmin(ars, als);
+    const R ml = unl / as, mr = unr / as;
+    return (fabs(ml) > R(1) ? 1u : 0u) | (fabs(mr) > R(1) ? 2u : 0u) | (als < ars ? 4u : 0u);
+  } else {
+    const R lamL = fabs(unl) + sqrt(l.a2), lamR = fabs(unr) + sqrt(r.a2);
+    return lamR > lamL ? 1u : 0u;
+  }
+}
+
 // Roe average of two primitive states in the face frame, used by the far-field
 // boundary updates (conservationLaws/euler/fluxes/roe.ipp:150-196).
 template <class R> __host__ __device__ __forceinline__ void roe_avg_vel(const St<R>& l, const St<R>& r, R* uav, R* u2,
@@ -516,7 +603,8 @@ template <class R> __host__ __device__ __forceinline__ void roe_avg_vel(const St
 // domain; qi, qf, qb are primitive.
 template <class R, int BK>
 __host__ __device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, R ny, const R* qi, const R* qf, R* qb,
-                                                         bool cons = false) {
+                                                         bool cons = false, unsigned* path = nullptr) {
+  // path (when asked for): 1 interior copy (transverse flow), 2 upwind copy (supersonic), 3 subsonic
   const R tx = -ny, ty = nx;
   const R ri[4] = {nx * qi[0] + ny * qi[1], tx * qi[0] + ty * qi[1], qi[2], qi[3]};
   const R rf[4] = {nx * qf[0] + ny * qf[1], tx * qf[0] + ty * qf[1], qf[2], qf[3]};
@@ -528,6 +616,7 @@ __host__ __device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, 
   if ((uav[0] / sqrt(u2a)) < thr) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) qb[k] = qi[k];
+    if (path) *path = 1u;
     return;
   }
   const R ma = uav[0] / sqrt(a2a);
@@ -536,8 +625,10 @@ __host__ __device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, 
   if (fabs(ma) > R(1)) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) qb[k] = quw[k];
+    if (path) *path = 2u;
     return;
   }
+  if (path) *path = 3u;
   const St<R>& sU = inflow ? sF : sI;
   R b[4];
   if constexpr (BK == BC_RIEMANN) {

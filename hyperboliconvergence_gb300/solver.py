@@ -218,6 +218,17 @@ class Solver:
         check(self.lib.hc_residual(self.h, _dptr(out)))
         return out
 
+    def face_signatures(self):
+        """Branch signatures of one residual evaluation of the current state (include/hc.h,
+        hc_face_signatures): uint64 arrays of shape (ni+1, nj) for the i-faces and (ni, nj+1)
+        for the j-faces."""
+        m = self.mesh
+        si = np.zeros((m.ni + 1, m.nj), dtype=np.uint64)
+        sj = np.zeros((m.ni, m.nj + 1), dtype=np.uint64)
+        u64 = C.POINTER(C.c_uint64)
+        check(self.lib.hc_face_signatures(self.h, si.ctypes.data_as(u64), sj.ctypes.data_as(u64)))
+        return si, sj
+
     def step(self, n: int = 1) -> StepStats:
         st = StepStats()
         check(self.lib.hc_step(self.h, int(n), C.byref(st)))
@@ -243,4 +254,17 @@ class Solver:
         return st
 
 
-__all__ = ["Mesh", "Solver", "HCError"]
+def branch_flips(sig_a, sig_b) -> dict:
+    """Where two evaluations of the same state took different branches: the faces whose
+    signatures differ (limiter pieces, flux branches, far-field paths), and the cells with
+    such a face.  sig_a, sig_b: (i-face, j-face) signature arrays from face_signatures."""
+    (ia, ja), (ib, jb) = sig_a, sig_b
+    fi, fj = ia != ib, ja != jb
+    cells = fi[:-1, :] | fi[1:, :] | fj[:, :-1] | fj[:, 1:]
+    lim_mask = np.uint64(0xFFFFFFFF)
+    return {"faces": int(fi.sum() + fj.sum()), "faces_total": int(fi.size + fj.size),
+            "limiter_faces": int(((ia ^ ib) & lim_mask != 0).sum() + ((ja ^ jb) & lim_mask != 0).sum()),
+            "cells": int(cells.sum()), "cells_total": int(cells.size)}
+
+
+__all__ = ["Mesh", "Solver", "HCError", "branch_flips"]

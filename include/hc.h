@@ -212,6 +212,21 @@ int hc_spectral_radius(const double* lambda_sum_device, const double* vol_device
 int hc_spectral_radius_noalloc(const double* lambda_sum_device, const double* vol_device, long long ncell,
                                double* out_device, void* stream);
 
+/* Branch signatures for the parity report (no counterpart in the reference): one
+ * residual evaluation of the current state through a recording instantiation of the
+ * stage kernel (the stepping kernels are not changed by it) that writes, per face, which
+ * branches its evaluation took: bits 0-15 the limiter pieces of the left side's four
+ * variables (4 bits each: bit 3 = (a > 0), bits 0-2 the interval of b/a that selects the
+ * limiter's expression), 16-31 the right side's, 32-35 the flux's branches (Roe:
+ * Harten's fix on the u-a / u+a waves; SLAU: |M_L| > 1, |M_R| > 1, mean-speed Mach > 1;
+ * AUSM+up: |M_L| > 1, |M_R| > 1, left critical speed below the right; others: right
+ * spectral radius larger), 36-37 the far-field path of a ghost face (1 interior copy,
+ * 2 supersonic upwind copy, 3 subsonic), bit 63 set for every face.  sig_i holds
+ * (ni+1)*nj i-faces, sig_j ni*(nj+1) j-faces (host arrays).  Comparing them with the
+ * oracle's (or another precision's) counts the faces and cells where a branch flipped.
+ * Euler law; allocates and frees a device buffer per call. */
+int hc_face_signatures(hc_ctx* ctx, unsigned long long* sig_i, unsigned long long* sig_j);
+
 /* Mesh generators: make_cylinder_mesh (mesh/generate/twoD.h:223-263), radial
  * spacing stretched geometrically when stretch != 1; make_linspace_mesh
  * (mesh/generate/twoD.h:99-124). */

@@ -628,6 +628,75 @@ template <class R> RKTable<R> rk_table(int kind) {
   return t;
 }
 
+// ---------------------------------------------------------------- branch signatures
+// Which branches one face's evaluation takes, with the same codes as the CUDA path's
+// recording kernels (limit_piece, flux_bits there): the parity report compares the two
+// per face.  limit_piece: bit 3 = (a > 0), bits 0-2 the interval of b/a (by
+// multiplication, u = |a|, v = b signed like a) that selects the limiter's expression.
+template <class R> unsigned limit_piece(int kind, R a, R b) {
+  const bool pos = a > 0;
+  const R u = pos ? a : -a, v = pos ? b : -b;
+  unsigned p = 0;
+  switch (kind) {
+    case LIM_VANALBADA: p = (a * b < 0) ? 0u : 1u; break;
+    case LIM_VANLEER: p = (a * b > 0) ? 1u : 0u; break;
+    case LIM_MINMOD: p = (v <= 0) ? 0u : (v < u ? 1u : 2u); break;
+    case LIM_SUPERBEE: p = (v <= 0) ? 0u : (2 * v < u ? 1u : (v < u ? 2u : (v < 2 * u ? 3u : 4u))); break;
+    case LIM_MC: p = (v <= 0) ? 0u : (3 * v < u ? 1u : (v < 3 * u ? 2u : 3u)); break;
+    case LIM_CADA3: {
+      const R c1 = -2. / 7., c2 = 0.4, c3 = 3 * 1.5 - 2;
+      if (!(fabs(a) + fabs(b) > 0)) p = 7u;
+      else if (v < -2 * u) p = 1u;
+      else if (v < c1 * u) p = 2u;
+      else if (v < 0) p = 3u;
+      else if (v < c2 * u) p = 4u;
+      else if (v < c3 * u) p = 5u;
+      else p = 6u;
+      break;
+    }
+    default: return 0u;
+  }
+  return p | (pos ? 8u : 0u);
+}
+
+// flux branches of two face states, with the reference's expressions: Roe -- Harten's
+// fix on waves 1 and 2 (roe.ipp:198-226); SLAU -- |M_L| > 1, |M_R| > 1, mean-speed Mach
+// > 1 (slau.ipp:18-31); AUSM+up -- |M_L| > 1, |M_R| > 1, left critical speed below the
+// right (ausmPlusUP.ipp:30-55); others -- right spectral radius larger
+template <class R> unsigned flux_bits(int kind, const Species<R>& sp, const Face<R>& f, const State<R>& sl,
+                                      const State<R>& sr) {
+  const R unl = proj_vel(f.n, sl), unr = proj_vel(f.n, sr);
+  if (kind == FLUX_ROE) {
+    const State<R> ra = roe_average(sp, sl, sr);
+    R wa[4], wl[4], wr[4];
+    wavespeeds(f.n, ra, wa); wavespeeds(f.n, sl, wl); wavespeeds(f.n, sr, wr);
+    unsigned b = 0;
+    for (int i = 1; i < 3; ++i) {
+      const R le = 0.05 * fmax((R)0., fmax(wa[i] - wl[i], wr[i] - wa[i]));
+      if (!(fabs(wa[i]) > le)) b |= 1u << (i - 1);
+    }
+    return b;
+  }
+  if (kind == FLUX_SLAU || kind == FLUX_SLAU_REF) {
+    const R ua = sqrt(0.5 * (sl.u2 + sr.u2));
+    const R aa = 0.5 * (sqrt(sl.a2) + sqrt(sr.a2));
+    const R aa1 = 1.0 / aa;
+    const R ml = unl * aa1, mr = unr * aa1;
+    return (fabs(ml) > 1 ? 1u : 0u) | (fabs(mr) > 1 ? 2u : 0u) | (ua * aa1 > 1 ? 4u : 0u);
+  }
+  if (kind == FLUX_AUSMPUP) {
+    const R ascoeff = 2. * (sp.gamma - 1.) / (sp.gamma + 1.);
+    const R als2 = ascoeff * sl.h, ars2 = ascoeff * sr.h;
+    const R als = als2 / fmax(unl, sqrt(als2));
+    const R ars = ars2 / fmax(-unr, sqrt(ars2));
+    const R as = fmin(ars, als);
+    const R ml = unl / as, mr = unr / as;
+    return (fabs(ml) > 1 ? 1u : 0u) | (fabs(mr) > 1 ? 2u : 0u) | (als < ars ? 4u : 0u);
+  }
+  return spec_rad(f.n, sr) > spec_rad(f.n, sl) ? 1u : 0u;
+}
+enum : unsigned { SIG_FLUX_SHIFT = 32, SIG_BC_SHIFT = 36, SIG_VALID_SHIFT = 63 };
+
 // ---------------------------------------------------------------- solution basis
 // The basis of the solution field (the SolVarT of SolutionField<SolVarT,2>): primitive
 // {u, v, rho, p}, as in the reference drivers (cylinder2D.cpp:110, gresho2D.cpp:112), or
@@ -653,16 +722,18 @@ template <class R> void basis_from_face(const Species<R>& sp, const Face<R>& f, 
   }
 }
 template <class R>
-void bc_riemann(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf, R* qb, int basis = BASIS_PRIMITIVE) {
+void bc_riemann(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf, R* qb, int basis = BASIS_PRIMITIVE,
+                unsigned* path = nullptr) {
   const R gam = sp.gamma, gam1 = sp.gamma1;
   R ri[4], rf[4];
   rotate_to(f, qi, ri); rotate_to(f, qf, rf);
   const State<R> sA = roe_average(sp, basis2state(sp, ri, basis), basis2state(sp, rf, basis));
-  if ((sA.u[0] / sqrt(sA.u2)) < 0.001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; return; }
+  if ((sA.u[0] / sqrt(sA.u2)) < 0.001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; if (path) *path = 1u; return; }
   const R ma = sA.u[0] / sqrt(sA.a2);
   const bool inflow = ma > 0;
   const R* quw = inflow ? qf : qi;
-  if (abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; return; }
+  if (abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; if (path) *path = 2u; return; }
+  if (path) *path = 3u;
   const State<R> sI = basis2state(sp, ri, basis), sF = basis2state(sp, rf, basis);
   const R ai = sqrt(sI.a2), af = sqrt(sF.a2);
   const R uni = sI.u[0], unf = sF.u[0];
@@ -682,17 +753,19 @@ void bc_riemann(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf
 }
 
 template <class R>
-void bc_entropy(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf, R* qb, int basis = BASIS_PRIMITIVE) {
+void bc_entropy(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf, R* qb, int basis = BASIS_PRIMITIVE,
+                unsigned* path = nullptr) {
   const R gam = sp.gamma;
   R ri[4], rf[4];
   rotate_to(f, qi, ri); rotate_to(f, qf, rf);
   const State<R> sA = roe_average(sp, basis2state(sp, ri, basis), basis2state(sp, rf, basis));
-  if ((sA.u[0] / sqrt(sA.u2)) < 0.0001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; return; }
+  if ((sA.u[0] / sqrt(sA.u2)) < 0.0001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; if (path) *path = 1u; return; }
   const R ma = sA.u[0] / sqrt(sA.a2);
   const bool inflow = ma > 0;
   const R* quw = inflow ? qf : qi;
   const R* qdw = inflow ? qi : qf;
-  if (abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; return; }
+  if (abs(ma) > 1.) { for (int k = 0; k < 4; ++k) qb[k] = quw[k]; if (path) *path = 2u; return; }
+  if (path) *path = 3u;
   R ru[4], rd[4];
   rotate_to(f, quw, ru); rotate_to(f, qdw, rd);
   const State<R> sU = basis2state(sp, ru, basis), sD = basis2state(sp, rd, basis);

@@ -30,6 +30,11 @@ template <class R> struct Solver {
   int flux = FLUX_ROE, lim = LIM_VANLEER, rk = RK_SSP34, dtmode = DT_GLOBAL;
   int vscale = SCALING_CONVECTIVE, pscale = SCALING_CONVECTIVE;  // AUSM+up low-Mach scaling
   int basis = BASIS_PRIMITIVE;  // solution basis of q and of the ghost layers
+  // branch signatures of the next residual evaluation, when set: (ni+1)*nj i-faces and
+  // ni*(nj+1) j-faces (codes of limit_piece / flux_bits in hc_oracle.hpp)
+  uint64_t* sig_i = nullptr;
+  uint64_t* sig_j = nullptr;
+  std::vector<unsigned> bc_path[4];  // far-field path per ghost face of the last boundary update
   R cfl = 0.5;
   int bc[4] = {BC_PERIODIC, BC_PERIODIC, BC_PERIODIC, BC_PERIODIC};
   // ghost arrays per side: [side][face][layer][var]; layer 0 = ghost value,
@@ -47,6 +52,13 @@ template <class R> struct Solver {
   size_t cid(int i, int j) const { return size_t(i) * nj + j; }
   int nface(int side) const { return side < 2 ? nj : ni; }
   State<R> st(const R* q) const { return basis2state(sp, q, basis); }
+  // signature slot of boundary face k of side `side` (i-faces i = 0 / ni, j-faces j = 0 / nj)
+  uint64_t* face_sig(int side, int k) const {
+    if (side == 0) return &sig_i[size_t(k)];
+    if (side == 1) return &sig_i[size_t(ni) * nj + k];
+    if (side == 2) return &sig_j[size_t(k) * (nj + 1)];
+    return &sig_j[size_t(k) * (nj + 1) + nj];
+  }
 
   // periodic shift across the i (or j) boundary at face index k: image of the
   // last cell = its centre minus the shift (average over the face's two nodes)
@@ -155,12 +167,15 @@ template <class R> struct Solver {
   void boundary_update(const std::vector<R>& q) {
     for (int side = 0; side < 4; ++side) {
       if (bc[side] == BC_PERIODIC) continue;
+      bc_path[side].resize(size_t(nface(side)));
       for (int k = 0; k < nface(side); ++k) {
         R* g = &ghost[side][size_t(k) * 8];
         const R* ref = g + 4;
         const R* qi = &q[size_t(side_cell(side, k)) * 4];
-        if (bc[side] == BC_RIEMANN) bc_riemann(sp, bface_in(side, k), qi, ref, g, basis);
-        else if (bc[side] == BC_ENTROPY) bc_entropy(sp, bface_in(side, k), qi, ref, g, basis);
+        unsigned* path = &bc_path[side][k];
+        *path = 0;
+        if (bc[side] == BC_RIEMANN) bc_riemann(sp, bface_in(side, k), qi, ref, g, basis, path);
+        else if (bc[side] == BC_ENTROPY) bc_entropy(sp, bface_in(side, k), qi, ref, g, basis, path);
         else for (int v = 0; v < 4; ++v) g[v] = ref[v];  // Fixed (boundaryCondition.h:63-80); wall ghost unused
       }
     }
@@ -202,9 +217,11 @@ template <class R> struct Solver {
 
   // ---- make_muscl_flux (spatial/muscl.h:13-59) with bias_solves (lsq/lsq.h:461-490)
   FluxRes<R> muscl(const Face<R>& f, const R* cl, const R* cr, const R* ql, const R* qr,
-                   const XM<R>& xl, const XM<R>& xr, const QM<R>& ml, const QM<R>& mr) const {
-    if (lim == LIM_NOLIMIT1)  // first-order overload (spatial/muscl.h:62-87)
+                   const XM<R>& xl, const XM<R>& xr, const QM<R>& ml, const QM<R>& mr, uint64_t* sg = nullptr) const {
+    if (lim == LIM_NOLIMIT1) {  // first-order overload (spatial/muscl.h:62-87)
+      if (sg) *sg = (uint64_t(flux_bits(flux, sp, f, st(ql), st(qr))) << SIG_FLUX_SHIFT) | (1ull << SIG_VALID_SHIFT);
       return face_flux(flux, sp, f, st(ql), st(qr), vscale, pscale);
+    }
     const R dxc[2] = {cr[0] - cl[0], cr[1] - cl[1]};
     R dqc[4];
     for (int v = 0; v < 4; ++v) dqc[v] = qr[v] - ql[v];
@@ -231,18 +248,30 @@ template <class R> struct Solver {
       qL[v] = ql[v] + dl * sl;
       qR[v] = qr[v] - dr * sr;
     }
+    if (sg) {
+      uint64_t b = 1ull << SIG_VALID_SHIFT;
+      for (int v = 0; v < 4; ++v)
+        b |= (uint64_t(limit_piece(lim, gc[v], gl[v])) << (4 * v)) |
+             (uint64_t(limit_piece(lim, gc[v], gr[v])) << (16 + 4 * v));
+      *sg = b | (uint64_t(flux_bits(flux, sp, f, st(qL), st(qR))) << SIG_FLUX_SHIFT);
+    }
     return face_flux(flux, sp, f, st(qL), st(qR), vscale, pscale);
   }
 
   // ghost face (D4): ghost side is not reconstructed, interior side is MUSCL
   // with the mirror term removed from its xmetric.  ghost_left says whether the
   // ghost is the face's left state (sides 0/2) or right state (sides 1/3).
-  FluxRes<R> muscl_ghost(int side, int k, const Face<R>& f, const R* qi, const R* qg) const {
+  FluxRes<R> muscl_ghost(int side, int k, const Face<R>& f, const R* qi, const R* qg, uint64_t* sg = nullptr) const {
     const size_t c = side_cell(side, k);
     const bool ghost_left = (side == 0 || side == 2);
     const R* ql = ghost_left ? qg : qi;
     const R* qr = ghost_left ? qi : qg;
-    if (lim == LIM_NOLIMIT1) return face_flux(flux, sp, f, st(ql), st(qr), vscale, pscale);
+    const uint64_t bcb = (uint64_t(bc_path[side].empty() ? 0u : bc_path[side][k]) << SIG_BC_SHIFT) |
+                         (1ull << SIG_VALID_SHIFT);
+    if (lim == LIM_NOLIMIT1) {
+      if (sg) *sg = bcb | (uint64_t(flux_bits(flux, sp, f, st(ql), st(qr))) << SIG_FLUX_SHIFT);
+      return face_flux(flux, sp, f, st(ql), st(qr), vscale, pscale);
+    }
     const R* cc = cells[c].c;
     R d = 0; d += (f.c[0] - cc[0]) * (f.c[0] - cc[0]); d += (f.c[1] - cc[1]) * (f.c[1] - cc[1]);
     const R dd = sqrt(d);
@@ -256,11 +285,14 @@ template <class R> struct Solver {
     R g[4];
     solve(factor(xb), qm[c], f.n, g);
     R qL[4], qR[4];
+    uint64_t pieces = 0;
     for (int v = 0; v < 4; ++v) {
       const R s = limit<R>(lim, dqc[v] * idlr, g[v]);
       if (ghost_left) { qL[v] = qg[v]; qR[v] = qi[v] - dd * s; }
       else { qL[v] = qi[v] + dd * s; qR[v] = qg[v]; }
+      pieces |= uint64_t(limit_piece(lim, dqc[v] * idlr, g[v])) << ((ghost_left ? 16 : 0) + 4 * v);
     }
+    if (sg) *sg = bcb | pieces | (uint64_t(flux_bits(flux, sp, f, st(qL), st(qR))) << SIG_FLUX_SHIFT);
     return face_flux(flux, sp, f, st(qL), st(qR), vscale, pscale);
   }
 
@@ -278,7 +310,8 @@ template <class R> struct Solver {
       for (int i = 0; i < ni - 1; ++i) {
         const size_t a = cid(i, j), b = cid(i + 1, j);
         const FluxRes<R> f = muscl(surface(node(i + 1, j), node(i + 1, j + 1)), cells[a].c, cells[b].c,
-                                   &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b]);
+                                   &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b],
+                                   sig_i ? &sig_i[size_t(i + 1) * nj + j] : nullptr);
         acc_sub(r[a], f); acc_add(r[b], f);
       }
     // j-normal faces (spatial/residualCalc.h:227-253)
@@ -287,7 +320,8 @@ template <class R> struct Solver {
       for (int j = 0; j < nj - 1; ++j) {
         const size_t a = cid(i, j), b = cid(i, j + 1);
         const FluxRes<R> f = muscl(surface(node(i + 1, j + 1), node(i, j + 1)), cells[a].c, cells[b].c,
-                                   &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b]);
+                                   &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b],
+                                   sig_j ? &sig_j[size_t(i) * (nj + 1) + j + 1] : nullptr);
         acc_sub(r[a], f); acc_add(r[b], f);
       }
     // boundary residuals in boundary-id order (spatial/residualCalc.h:279-307)
@@ -301,7 +335,8 @@ template <class R> struct Solver {
             const size_t a = cid(ni - 1, j), b = cid(0, j);
             const R cl[2] = {cells[a].c[0] - s[0], cells[a].c[1] - s[1]};
             const FluxRes<R> f = muscl(surface(node(0, j), node(0, j + 1)), cl, cells[b].c,
-                                       &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b]);
+                                       &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b],
+                                       sig_i ? &sig_i[size_t(j)] : nullptr);
             acc_sub(r[a], f); acc_add(r[b], f);
           }
         else if (side == 2)
@@ -310,7 +345,8 @@ template <class R> struct Solver {
             const size_t a = cid(i, nj - 1), b = cid(i, 0);
             const R cl[2] = {cells[a].c[0] - s[0], cells[a].c[1] - s[1]};
             const FluxRes<R> f = muscl(surface(node(i + 1, 0), node(i, 0)), cl, cells[b].c,
-                                       &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b]);
+                                       &q[a * 4], &q[b * 4], xm[a], xm[b], qm[a], qm[b],
+                                       sig_j ? &sig_j[size_t(i) * (nj + 1)] : nullptr);
             acc_sub(r[a], f); acc_add(r[b], f);
           }
       } else if (t == BC_WALL) {
@@ -322,12 +358,14 @@ template <class R> struct Solver {
           R dq[4];
           solve(factor(xm[c]), qm[c], dir, dq);
           acc_add(r[c], wall_flux(sp, f, &q[c * 4], dq, basis));
+          if (sig_i || sig_j) *face_sig(side, k) = 1ull << SIG_VALID_SHIFT;
         }
       } else {
         // ghost-cell loop (ghostCellLoop.h:109-228)
         for (int k = 0; k < nface(side); ++k) {
           const size_t c = side_cell(side, k);
-          const FluxRes<R> f = muscl_ghost(side, k, bface_flux(side, k), &q[c * 4], &ghost[side][size_t(k) * 8]);
+          const FluxRes<R> f = muscl_ghost(side, k, bface_flux(side, k), &q[c * 4], &ghost[side][size_t(k) * 8],
+                                           (sig_i || sig_j) ? face_sig(side, k) : nullptr);
           if (side == 0 || side == 2) acc_add(r[c], f); else acc_sub(r[c], f);
         }
       }

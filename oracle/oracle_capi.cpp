@@ -94,6 +94,23 @@ void hco_step(void* h, int nsteps, double* out_dt_t) {
   out_dt_t[0] = s->last_dt;
   out_dt_t[1] = s->t;
 }
+// branch signatures of one residual evaluation on the current state: (ni+1)*nj i-faces
+// and ni*(nj+1) j-faces (codes of limit_piece / flux_bits)
+void hco_face_signatures(void* h, uint64_t* sig_i, uint64_t* sig_j) {
+  S* s = static_cast<S*>(h);
+  std::fill(sig_i, sig_i + size_t(s->ni + 1) * s->nj, uint64_t(0));
+  std::fill(sig_j, sig_j + size_t(s->ni) * (s->nj + 1), uint64_t(0));
+  s->sig_i = sig_i;
+  s->sig_j = sig_j;
+  s->residual(s->q0, s->res[0]);
+  s->sig_i = s->sig_j = nullptr;
+  // the residual evaluates each periodic face pair once, at the lower index; the upper
+  // copy (i = ni, j = nj) is the same face
+  if (s->bc[0] == BC_PERIODIC)
+    for (int j = 0; j < s->nj; ++j) sig_i[size_t(s->ni) * s->nj + j] = sig_i[size_t(j)];
+  if (s->bc[2] == BC_PERIODIC)
+    for (int i = 0; i < s->ni; ++i) sig_j[size_t(i) * (s->nj + 1) + s->nj] = sig_j[size_t(i) * (s->nj + 1)];
+}
 // cell volumes and centres: 3 planes
 void hco_cells(void* h, double* out) {
   S* s = static_cast<S*>(h);

@@ -290,6 +290,15 @@ class OracleSolver:
         self.lib.hco_step(self.h, int(n), out)
         return float(out[0]), float(out[1])
 
+    def face_signatures(self):
+        """Branch signatures of one residual evaluation (the CUDA path's codes)."""
+        si = np.zeros((self.ni + 1, self.nj), dtype=np.uint64)
+        sj = np.zeros((self.ni, self.nj + 1), dtype=np.uint64)
+        u64 = C.POINTER(C.c_uint64)
+        self.lib.hco_face_signatures.argtypes = [C.c_void_p, u64, u64]
+        self.lib.hco_face_signatures(self.h, si.ctypes.data_as(u64), sj.ctypes.data_as(u64))
+        return si, sj
+
     def cells(self):
         out = np.empty((3, self.ni, self.nj))
         self.lib.hco_cells(self.h, out)

@@ -131,3 +131,27 @@ def test_vanleer_decision(o):
     assert o.limit(7, 0.2, 0.5) == pytest.approx(2 * 0.2 * 0.5 / 0.7)
     assert o.limit(7, 0.2, -0.5) == 0.0
     assert o.limit(8, 0.2, 0.5) == pytest.approx((0.5 + 0.5) / (0.2 + 0.5))
+
+
+def test_branch_flips_locate_a_planted_change():
+    """Oracle signatures of a state and of the same state with one cell changed: the
+    flips are the faces and cells near that cell (the counting on the host is right)."""
+    from hyperboliconvergence_gb300 import cases
+    from hyperboliconvergence_gb300.solver import branch_flips
+    rng = np.random.default_rng(3)
+    mesh, bc, ref, q, sp = cases.quadrant_riemann(16, 12, rng)
+    q = q * (1 + 0.02 * rng.standard_normal(q.shape))
+    a = oracle_py.OracleSolver(mesh.ni, mesh.nj, mesh.nodes.ravel(), bc, flux="ausmpup", limiter="minmod",
+                               species=sp, ghost_ref=ref)
+    a.set_state(q)
+    s0 = a.face_signatures()
+    assert branch_flips(s0, a.face_signatures())["faces"] == 0
+    q2 = q.copy()
+    q2[:, 7, 5] = q2[:, 7, 5] * np.array([-3.0, 3.0, 1.5, 1.5])
+    a.set_state(q2)
+    f = branch_flips(s0, a.face_signatures())
+    assert f["faces"] > 0
+    # a change in one cell reaches at most the faces of its 2-cell stencil
+    si = s0[0] != a.face_signatures()[0]
+    idx = np.argwhere(si)
+    assert np.all(np.abs(idx[:, 0] - 7.5) <= 3) and np.all(np.abs(idx[:, 1] - 5) <= 2)
