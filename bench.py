@@ -242,10 +242,14 @@ def measure_precision(stream, steps: int, prec: str):
         s = Solver(mesh, bc, ref, flux=FLUX, limiter=LIMITER, rk=RKT, precision=p, dt=DTMODE, cfl=CFL,
                    species=species, stream=stream.cuda_stream)
         s.set_state(states["fp64"][1])
-        sigs[p] = s.face_signatures()
+        sigs[p] = s.face_signatures(with_args=(p == "fp64"))
         s.close()
-    out["branch_flips_vs_fp64"] = branch_flips(sigs[prec], sigs["fp64"]) | {
-        "state": "the FP64 state after 20 steps, evaluated at both precisions"}
+    out["branch_flips_vs_fp64"] = branch_flips(sigs[prec], sigs["fp64"][0], args=sigs["fp64"][1],
+                                               limiter=LIMITER) | {
+        "state": "the FP64 state after 20 steps, evaluated at both precisions",
+        "faces_above_roundoff_means": "flips whose FP64 limiter arguments are more than 1e-9 of the variable's "
+                                "scale from a breakpoint (the others are round-off arguments, zero in "
+                                "exact arithmetic)"}
     return out
 
 

@@ -64,7 +64,7 @@ def _declare(lib):
         "hc_state_upload_device": [p, v],
         "hc_state_download_device": [p, v],
         "hc_residual": [p, dp],
-        "hc_face_signatures": [p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
+        "hc_face_signatures": [p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), p, p],
         "hc_step": [p, i, C.POINTER(StepStats)],
         "hc_step_async": [p, i],
         "hc_sync": [p, C.POINTER(StepStats)],

@@ -217,18 +217,26 @@ template <class R> __global__ void r2d_kernel(const R* a, double* b, size_t n) {
 }  // namespace
 
 namespace {
-template <class R> int run_signatures(hc_ctx* c, unsigned long long* sig_i, unsigned long long* sig_j) {
+template <class R>
+int run_signatures(hc_ctx* c, unsigned long long* sig_i, unsigned long long* sig_j, double* arg_i, double* arg_j) {
   const size_t nfi = size_t(c->ni + 1) * c->nj, nfj = size_t(c->ni) * (c->nj + 1);
+  const bool args = arg_i && arg_j;
   unsigned long long* d = nullptr;
+  double* da = nullptr;
   HC_CUDA(cudaMalloc(&d, (nfi + nfj) * sizeof(unsigned long long)));
-  struct Free { void* p; ~Free() { cudaFree(p); } } guard{d};
+  struct Free { void* p; ~Free() { if (p) cudaFree(p); } } guard{d};
+  if (args) HC_CUDA(cudaMalloc(&da, 16 * (nfi + nfj) * sizeof(double)));
+  Free guard_a{da};
   HC_CUDA(cudaMemsetAsync(d, 0, (nfi + nfj) * sizeof(unsigned long long), c->stream));
+  if (args) HC_CUDA(cudaMemsetAsync(da, 0, 16 * (nfi + nfj) * sizeof(double), c->stream));
   StageArgs<R> a = base_args<R>(c);
   a.q = (const R*)c->q[0];
   a.mode = MODE_RESIDUAL;
   a.res_out = nullptr;
   a.sig_i = d;
   a.sig_j = d + nfi;
+  a.arg_i = da;
+  a.arg_j = da ? da + 16 * nfi : nullptr;
   if constexpr (std::is_same<R, double>::value) {
     if (c->df) HC_CUDA((launch_sig_stage<double, true>(a, c->cfg.flux, c->stream)));
     else HC_CUDA((launch_sig_stage<double, false>(a, c->cfg.flux, c->stream)));
@@ -238,6 +246,10 @@ template <class R> int run_signatures(hc_ctx* c, unsigned long long* sig_i, unsi
   c->launches += 1;
   HC_CUDA(cudaMemcpyAsync(sig_i, d, nfi * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
   HC_CUDA(cudaMemcpyAsync(sig_j, d + nfi, nfj * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+  if (args) {
+    HC_CUDA(cudaMemcpyAsync(arg_i, da, 16 * nfi * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaMemcpyAsync(arg_j, da + 16 * nfi, 16 * nfj * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  }
   HC_CUDA(cudaStreamSynchronize(c->stream));
   return HC_OK;
 }
@@ -471,12 +483,14 @@ int hc_residual(hc_ctx* c, double* out5) {
   return HC_OK;
 }
 
-int hc_face_signatures(hc_ctx* c, unsigned long long* sig_i, unsigned long long* sig_j) {
+int hc_face_signatures(hc_ctx* c, unsigned long long* sig_i, unsigned long long* sig_j, double* arg_i,
+                       double* arg_j) {
   if (int st = check_ctx(c)) return st;
   if (!sig_i || !sig_j) return fail(HC_ERR_ARG, "null output");
   if (c->scalar) return fail(HC_ERR_UNSUPPORTED, "branch signatures cover the Euler law");
   if (int st = ensure_ready(c)) return st;
-  return c->fp32 ? run_signatures<float>(c, sig_i, sig_j) : run_signatures<double>(c, sig_i, sig_j);
+  return c->fp32 ? run_signatures<float>(c, sig_i, sig_j, arg_i, arg_j)
+                  : run_signatures<double>(c, sig_i, sig_j, arg_i, arg_j);
 }
 
 int hc_step_async(hc_ctx* c, int nsteps) {

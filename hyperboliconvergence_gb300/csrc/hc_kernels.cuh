@@ -64,6 +64,8 @@ template <class R> struct StageArgs {
   int basis;          // solution basis: 0 primitive, 1 conserved
   unsigned long long* sig_i;  // branch signatures of the i-faces / j-faces (recording kernels only)
   unsigned long long* sig_j;
+  double* arg_i;              // with them (or null): the 8 limiter calls' (a, b) per face, 16 values
+  double* arg_j;
 };
 
 // Branch signature of one face (recording kernels): bits 0-15 the limiter pieces of
@@ -279,10 +281,16 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
             limit4<C>(lim, gc, gl, sL);
             limit4<C>(lim, gc, gr, sR);
             if constexpr (REC) {
+              double* ag = a.arg_i ? (idir ? a.arg_i + size_t(16) * fidx : a.arg_j + size_t(16) * fidx) : nullptr;
 #pragma unroll
-              for (int v = 0; v < 4; ++v)
+              for (int v = 0; v < 4; ++v) {
                 sg |= ((unsigned long long)limit_piece<C>(lim, gc[v], gl[v]) << (4 * v)) |
                       ((unsigned long long)limit_piece<C>(lim, gc[v], gr[v]) << (16 + 4 * v));
+                if (ag) {
+                  ag[2 * v] = cvt<double>(gc[v]); ag[2 * v + 1] = cvt<double>(gl[v]);
+                  ag[8 + 2 * v] = cvt<double>(gc[v]); ag[9 + 2 * v] = cvt<double>(gr[v]);
+                }
+              }
             }
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
@@ -298,9 +306,15 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
               const C gr = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
               qL[v] = ql[v] + dl * limit<C>(lim, gc, gl);
               qR[v] = qr[v] - dr * limit<C>(lim, gc, gr);
-              if constexpr (REC)
+              if constexpr (REC) {
                 sg |= ((unsigned long long)limit_piece<C>(lim, gc, gl) << (4 * v)) |
                       ((unsigned long long)limit_piece<C>(lim, gc, gr) << (16 + 4 * v));
+                if (a.arg_i) {
+                  double* ag = idir ? a.arg_i + size_t(16) * fidx : a.arg_j + size_t(16) * fidx;
+                  ag[2 * v] = cvt<double>(gc); ag[2 * v + 1] = cvt<double>(gl);
+                  ag[8 + 2 * v] = cvt<double>(gc); ag[9 + 2 * v] = cvt<double>(gr);
+                }
+              }
             }
           }
           if constexpr (REC) {
@@ -345,15 +359,15 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
           const R nxr = cvt<R>(nx), nyr = cvt<R>(ny);
           unsigned path = 0;
           unsigned* pathp = REC ? &path : nullptr;
-          if (bct == BC_RIEMANN)
+          if (bct == BC_RIEMANN) {
             farfield_update<R, BC_RIEMANN>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr, cons, pathp);
-          else if (bct == BC_ENTROPY)
+          } else if (bct == BC_ENTROPY) {
             farfield_update<R, BC_ENTROPY>(a.gas, sgn * nxr, sgn * nyr, qir, qref, qgr, cons, pathp);
-          if constexpr (REC) sg |= (unsigned long long)path << SIG_BC_SHIFT;
-          else {
+          } else {
 #pragma unroll
             for (int v = 0; v < 4; ++v) qgr[v] = qref[v];
           }
+          if constexpr (REC) sg |= (unsigned long long)path << SIG_BC_SHIFT;
 #pragma unroll
           for (int v = 0; v < 4; ++v) qg[v] = cvt<C>(qgr[v]);
           C qL[4], qR[4];
@@ -367,8 +381,13 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
               const C s = limit<C>(lim, dq * idlr, gb);
               if (int_right) { qL[v] = qg[v]; qR[v] = qi[v] - d * s; }
               else { qL[v] = qi[v] + d * s; qR[v] = qg[v]; }
-              if constexpr (REC)  // the interior side's limiter, in its side's slot
+              if constexpr (REC) {  // the interior side's limiter, in its side's slot
                 sg |= (unsigned long long)limit_piece<C>(lim, dq * idlr, gb) << ((int_right ? 16 : 0) + 4 * v);
+                if (a.arg_i) {
+                  double* ag = (idir ? a.arg_i : a.arg_j) + size_t(16) * fidx + (int_right ? 8 : 0);
+                  ag[2 * v] = cvt<double>(dq * idlr); ag[2 * v + 1] = cvt<double>(gb);
+                }
+              }
             }
           } else {
 #pragma unroll

@@ -218,16 +218,21 @@ class Solver:
         check(self.lib.hc_residual(self.h, _dptr(out)))
         return out
 
-    def face_signatures(self):
+    def face_signatures(self, with_args: bool = False):
         """Branch signatures of one residual evaluation of the current state (include/hc.h,
         hc_face_signatures): uint64 arrays of shape (ni+1, nj) for the i-faces and (ni, nj+1)
-        for the j-faces."""
+        for the j-faces; with_args also returns the limiter arguments, arrays (ni+1, nj, 8, 2)
+        and (ni, nj+1, 8, 2) of (a, b) per limiter call."""
         m = self.mesh
         si = np.zeros((m.ni + 1, m.nj), dtype=np.uint64)
         sj = np.zeros((m.ni, m.nj + 1), dtype=np.uint64)
+        ai = np.zeros((m.ni + 1, m.nj, 8, 2)) if with_args else None
+        aj = np.zeros((m.ni, m.nj + 1, 8, 2)) if with_args else None
         u64 = C.POINTER(C.c_uint64)
-        check(self.lib.hc_face_signatures(self.h, si.ctypes.data_as(u64), sj.ctypes.data_as(u64)))
-        return si, sj
+        check(self.lib.hc_face_signatures(self.h, si.ctypes.data_as(u64), sj.ctypes.data_as(u64),
+                                          None if ai is None else ai.ctypes.data,
+                                          None if aj is None else aj.ctypes.data))
+        return ((si, sj), (ai, aj)) if with_args else (si, sj)
 
     def step(self, n: int = 1) -> StepStats:
         st = StepStats()
@@ -254,17 +259,46 @@ class Solver:
         return st
 
 
-def branch_flips(sig_a, sig_b) -> dict:
+# ratios b/a (b = c a, with a > 0) at which each limiter changes piece; the sign of a is
+# one more breakpoint (limit_piece in csrc/hc_physics.cuh)
+LIMITER_BREAKS = {"vanalbada": (0.0,), "vanleer": (0.0,), "minmod": (0.0, 1.0), "superbee": (0.0, 0.5, 1.0, 2.0),
+                  "mc": (0.0, 1.0 / 3.0, 3.0), "cada3": (-2.0, -2.0 / 7.0, 0.0, 0.4, 2.5)}
+
+
+def branch_flips(sig_a, sig_b, cell_mask: bool = False, args=None, limiter=None, roundoff=1e-9) -> dict:
     """Where two evaluations of the same state took different branches: the faces whose
     signatures differ (limiter pieces, flux branches, far-field paths), and the cells with
-    such a face.  sig_a, sig_b: (i-face, j-face) signature arrays from face_signatures."""
+    such a face.  sig_a, sig_b: (i-face, j-face) signature arrays from face_signatures;
+    cell_mask adds the (ni, nj) boolean mask of those cells.  With args (the reference
+    evaluation's limiter arguments from face_signatures(with_args=True)) and the limiter's
+    name, limiter flips whose arguments lie within `roundoff` of the variable's argument
+    scale from a breakpoint -- an argument zero in exact arithmetic, computed as round-off
+    -- are told apart: "faces_above_roundoff" counts the faces with another flip."""
     (ia, ja), (ib, jb) = sig_a, sig_b
     fi, fj = ia != ib, ja != jb
     cells = fi[:-1, :] | fi[1:, :] | fj[:, :-1] | fj[:, 1:]
     lim_mask = np.uint64(0xFFFFFFFF)
-    return {"faces": int(fi.sum() + fj.sum()), "faces_total": int(fi.size + fj.size),
-            "limiter_faces": int(((ia ^ ib) & lim_mask != 0).sum() + ((ja ^ jb) & lim_mask != 0).sum()),
-            "cells": int(cells.sum()), "cells_total": int(cells.size)}
+    out = {"faces": int(fi.sum() + fj.sum()), "faces_total": int(fi.size + fj.size),
+           "limiter_faces": int((((ia ^ ib) & lim_mask) != 0).sum() + (((ja ^ jb) & lim_mask) != 0).sum()),
+           "cells": int(cells.sum()), "cells_total": int(cells.size)}
+    if args is not None and limiter is not None:
+        a = np.concatenate([args[0].reshape(-1, 8, 2), args[1].reshape(-1, 8, 2)])
+        x = np.concatenate([(ia ^ ib).ravel(), (ja ^ jb).ravel()])
+        diff = np.stack([((x >> np.uint64(4 * k)) & np.uint64(15)) != 0 for k in range(8)], axis=1)
+        slot_scale = np.abs(a).max(axis=(0, 2))
+        var_scale = np.tile(np.maximum(slot_scale[:4], slot_scale[4:]), 2)  # per variable, both sides
+        lo, hi = a[..., 0], a[..., 1]
+        u = np.where(lo > 0, lo, -lo)
+        v = np.where(lo > 0, hi, -hi)
+        dist = np.abs(lo)
+        for c in LIMITER_BREAKS.get(limiter, ()):
+            dist = np.minimum(dist, np.abs(v - c * u))
+        noise = dist <= roundoff * var_scale[None, :]
+        above = (diff & ~noise).any(axis=1) | ((x >> np.uint64(32)) != 0)
+        out["faces_above_roundoff"] = int(above.sum())
+    if cell_mask:
+        out["cell_mask"] = cells
+    return out
 
 
 __all__ = ["Mesh", "Solver", "HCError", "branch_flips"]

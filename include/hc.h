@@ -224,8 +224,12 @@ int hc_spectral_radius_noalloc(const double* lambda_sum_device, const double* vo
  * 2 supersonic upwind copy, 3 subsonic), bit 63 set for every face.  sig_i holds
  * (ni+1)*nj i-faces, sig_j ni*(nj+1) j-faces (host arrays).  Comparing them with the
  * oracle's (or another precision's) counts the faces and cells where a branch flipped.
- * Euler law; allocates and frees a device buffer per call. */
-int hc_face_signatures(hc_ctx* ctx, unsigned long long* sig_i, unsigned long long* sig_j);
+ * arg_i / arg_j (both or neither may be NULL): the (a, b) arguments of each face's eight
+ * limiter calls (left side's four variables, then the right side's), 16 doubles per
+ * face, so that a flip can be told apart from round-off noise at a breakpoint.  Euler
+ * law; allocates and frees device buffers per call. */
+int hc_face_signatures(hc_ctx* ctx, unsigned long long* sig_i, unsigned long long* sig_j, double* arg_i,
+                       double* arg_j);
 
 /* Mesh generators: make_cylinder_mesh (mesh/generate/twoD.h:223-263), radial
  * spacing stretched geometrically when stretch != 1; make_linspace_mesh

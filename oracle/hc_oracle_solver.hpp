@@ -23,6 +23,13 @@
 
 namespace hco {
 
+// the value of a number of the oracle's arithmetic types (double, or the dual / counting
+// types, which hold it in .v)
+template <class T> double value_of(const T& x) {
+  if constexpr (std::is_arithmetic_v<T>) return double(x);
+  else return double(x.v);
+}
+
 template <class R> struct Solver {
   int ni = 0, nj = 0;
   std::vector<R> nodes;  // (ni+1)*(nj+1)*2
@@ -34,6 +41,10 @@ template <class R> struct Solver {
   // ni*(nj+1) j-faces (codes of limit_piece / flux_bits in hc_oracle.hpp)
   uint64_t* sig_i = nullptr;
   uint64_t* sig_j = nullptr;
+  // with the signatures, optionally the limiter arguments (a, b) of the 8 limiter calls
+  // of each face (left side's four variables, then the right side's): 16 per face
+  double* arg_i = nullptr;
+  double* arg_j = nullptr;
   std::vector<unsigned> bc_path[4];  // far-field path per ghost face of the last boundary update
   R cfl = 0.5;
   int bc[4] = {BC_PERIODIC, BC_PERIODIC, BC_PERIODIC, BC_PERIODIC};
@@ -53,6 +64,13 @@ template <class R> struct Solver {
   int nface(int side) const { return side < 2 ? nj : ni; }
   State<R> st(const R* q) const { return basis2state(sp, q, basis); }
   // signature slot of boundary face k of side `side` (i-faces i = 0 / ni, j-faces j = 0 / nj)
+  // limiter-argument slot of the face whose signature slot is sg
+  double* face_args(const uint64_t* sg) const {
+    if (!arg_i) return nullptr;
+    const size_t nfi = size_t(ni + 1) * nj;
+    if (sg >= sig_i && sg < sig_i + nfi) return arg_i + size_t(sg - sig_i) * 16;
+    return arg_j + size_t(sg - sig_j) * 16;
+  }
   uint64_t* face_sig(int side, int k) const {
     if (side == 0) return &sig_i[size_t(k)];
     if (side == 1) return &sig_i[size_t(ni) * nj + k];
@@ -254,6 +272,11 @@ template <class R> struct Solver {
         b |= (uint64_t(limit_piece(lim, gc[v], gl[v])) << (4 * v)) |
              (uint64_t(limit_piece(lim, gc[v], gr[v])) << (16 + 4 * v));
       *sg = b | (uint64_t(flux_bits(flux, sp, f, st(qL), st(qR))) << SIG_FLUX_SHIFT);
+      if (double* ag = face_args(sg))
+        for (int v = 0; v < 4; ++v) {
+          ag[2 * v] = value_of(gc[v]); ag[2 * v + 1] = value_of(gl[v]);
+          ag[8 + 2 * v] = value_of(gc[v]); ag[8 + 2 * v + 1] = value_of(gr[v]);
+        }
     }
     return face_flux(flux, sp, f, st(qL), st(qR), vscale, pscale);
   }
@@ -291,6 +314,11 @@ template <class R> struct Solver {
       if (ghost_left) { qL[v] = qg[v]; qR[v] = qi[v] - dd * s; }
       else { qL[v] = qi[v] + dd * s; qR[v] = qg[v]; }
       pieces |= uint64_t(limit_piece(lim, dqc[v] * idlr, g[v])) << ((ghost_left ? 16 : 0) + 4 * v);
+      if (sg)
+        if (double* ag = face_args(sg)) {
+          ag[(ghost_left ? 8 : 0) + 2 * v] = value_of(dqc[v] * idlr);
+          ag[(ghost_left ? 8 : 0) + 2 * v + 1] = value_of(g[v]);
+        }
     }
     if (sg) *sg = bcb | pieces | (uint64_t(flux_bits(flux, sp, f, st(qL), st(qR))) << SIG_FLUX_SHIFT);
     return face_flux(flux, sp, f, st(qL), st(qR), vscale, pscale);

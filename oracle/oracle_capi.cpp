@@ -95,15 +95,28 @@ void hco_step(void* h, int nsteps, double* out_dt_t) {
   out_dt_t[1] = s->t;
 }
 // branch signatures of one residual evaluation on the current state: (ni+1)*nj i-faces
-// and ni*(nj+1) j-faces (codes of limit_piece / flux_bits)
-void hco_face_signatures(void* h, uint64_t* sig_i, uint64_t* sig_j) {
+// and ni*(nj+1) j-faces (codes of limit_piece / flux_bits); arg_i / arg_j (or null): the
+// limiter arguments, 16 per face
+void hco_face_signatures(void* h, uint64_t* sig_i, uint64_t* sig_j, double* arg_i, double* arg_j) {
   S* s = static_cast<S*>(h);
   std::fill(sig_i, sig_i + size_t(s->ni + 1) * s->nj, uint64_t(0));
   std::fill(sig_j, sig_j + size_t(s->ni) * (s->nj + 1), uint64_t(0));
+  if (arg_i) std::fill(arg_i, arg_i + size_t(s->ni + 1) * s->nj * 16, 0.0);
+  if (arg_j) std::fill(arg_j, arg_j + size_t(s->ni) * (s->nj + 1) * 16, 0.0);
   s->sig_i = sig_i;
   s->sig_j = sig_j;
+  s->arg_i = arg_i;
+  s->arg_j = arg_j;
   s->residual(s->q0, s->res[0]);
   s->sig_i = s->sig_j = nullptr;
+  s->arg_i = s->arg_j = nullptr;
+  if (arg_i && s->bc[0] == BC_PERIODIC)
+    for (int j = 0; j < s->nj; ++j)
+      std::copy(arg_i + size_t(j) * 16, arg_i + size_t(j) * 16 + 16, arg_i + (size_t(s->ni) * s->nj + j) * 16);
+  if (arg_j && s->bc[2] == BC_PERIODIC)
+    for (int i = 0; i < s->ni; ++i)
+      std::copy(arg_j + size_t(i) * (s->nj + 1) * 16, arg_j + size_t(i) * (s->nj + 1) * 16 + 16,
+                arg_j + (size_t(i) * (s->nj + 1) + s->nj) * 16);
   // the residual evaluates each periodic face pair once, at the lower index; the upper
   // copy (i = ni, j = nj) is the same face
   if (s->bc[0] == BC_PERIODIC)

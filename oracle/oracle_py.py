@@ -290,14 +290,19 @@ class OracleSolver:
         self.lib.hco_step(self.h, int(n), out)
         return float(out[0]), float(out[1])
 
-    def face_signatures(self):
-        """Branch signatures of one residual evaluation (the CUDA path's codes)."""
+    def face_signatures(self, with_args=False):
+        """Branch signatures of one residual evaluation (the CUDA path's codes); with_args
+        also returns the limiter arguments, arrays (ni+1, nj, 8, 2) and (ni, nj+1, 8, 2) of
+        (a, b) per limiter call (left side's four variables, then the right side's)."""
         si = np.zeros((self.ni + 1, self.nj), dtype=np.uint64)
         sj = np.zeros((self.ni, self.nj + 1), dtype=np.uint64)
+        ai = np.zeros((self.ni + 1, self.nj, 8, 2)) if with_args else None
+        aj = np.zeros((self.ni, self.nj + 1, 8, 2)) if with_args else None
         u64 = C.POINTER(C.c_uint64)
-        self.lib.hco_face_signatures.argtypes = [C.c_void_p, u64, u64]
-        self.lib.hco_face_signatures(self.h, si.ctypes.data_as(u64), sj.ctypes.data_as(u64))
-        return si, sj
+        self.lib.hco_face_signatures.argtypes = [C.c_void_p, u64, u64, C.c_void_p, C.c_void_p]
+        self.lib.hco_face_signatures(self.h, si.ctypes.data_as(u64), sj.ctypes.data_as(u64),
+                                     None if ai is None else ai.ctypes.data, None if aj is None else aj.ctypes.data)
+        return ((si, sj), (ai, aj)) if with_args else (si, sj)
 
     def cells(self):
         out = np.empty((3, self.ni, self.nj))
