@@ -154,6 +154,19 @@ class Objective(C.Structure):
                 ("target", C.POINTER(C.c_double)), ("weight", C.c_double * 4)]
 
 
+class DualTimeControls(C.Structure):
+    _fields_ = [("outer_steps", C.c_int), ("dt", C.c_double), ("cfl_outer", C.c_double), ("scheme", C.c_int),
+                ("inner_max", C.c_int), ("inner_drop", C.c_double), ("check_every", C.c_int)]
+
+
+class DualTimeStats(C.Structure):
+    _fields_ = [("outer_steps", C.c_longlong), ("inner_steps", C.c_longlong), ("last_inner", C.c_int),
+                ("dt", C.c_double), ("t", C.c_double), ("res0_last", C.c_double), ("res_last", C.c_double)]
+
+
+MULTISTEP = {"bdf1": 0, "bdf2": 1, "trapezium": 2}
+
+
 class SteadyControls(C.Structure):
     _fields_ = [("max_steps", C.c_longlong), ("residual_drop", C.c_double), ("check_every", C.c_int),
                 ("use_residual_smoothing", C.c_int), ("smoothing_factor", C.c_double)]
@@ -183,3 +196,5 @@ def _declare_adjoint(lib):
     lib.hc_batch_adjoint_gradient.argtypes = [p, i, i, C.POINTER(Objective), C.POINTER(dp), dp, C.POINTER(dp),
                                               C.POINTER(AdjointStats)]
     lib.hc_batch_adjoint_gradient.restype = C.c_int
+    lib.hc_dual_time_run.argtypes = [p, C.POINTER(DualTimeControls), C.POINTER(DualTimeStats)]
+    lib.hc_dual_time_run.restype = C.c_int

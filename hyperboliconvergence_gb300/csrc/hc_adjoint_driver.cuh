@@ -130,7 +130,7 @@ template <class R> int forward_step(Adj<R>& A, int step, bool rec) {
       }
       update0_kernel<R><<<std::min<unsigned>(blocks(A.n), 152 * 16), 256, 0, A.s()>>>(
           c->ni, c->nj, a.gas, A.sq[0], (const R*)c->res[0], (const R*)c->vol, R(A.tab.alpha[0][0]),
-          R(A.tab.beta[0]), c->cfg.cfl, c->info, A.sq[1], 0, c->cfg.basis);
+          R(A.tab.beta[0]), c->cfg.cfl, c->info, A.sq[1], 0, c->cfg.basis, 0.0);
       HC_CUDA(cudaGetLastError());
       A.launches += 2;
     } else {

@@ -167,7 +167,8 @@ template <class R> int run_step(hc_ctx* c) {
       } else {
         update0_kernel<R><<<grid, B, 0, c->stream>>>(c->ni, c->nj, a.gas, (const R*)c->q[0], (const R*)c->res[0],
                                                      (const R*)c->vol, R(tab.alpha[0][0]), R(tab.beta[0]),
-                                                     c->cfg.cfl, c->info, out_of(0), 1, c->cfg.basis);
+                                                     c->cfg.cfl, c->info, out_of(0), 1, c->cfg.basis,
+                                                     c->dual_src ? c->dual_b0dt : 0.0);
       }
       HC_CUDA(cudaGetLastError());
       c->launches += 2;
@@ -254,6 +255,130 @@ int run_signatures(hc_ctx* c, unsigned long long* sig_i, unsigned long long* sig
   return HC_OK;
 }
 }  // namespace
+
+// ---------------------------------------------------------------- dual time
+// ODE::Implicit::MultiStep tables (ode.h:10-83): (b_0 u_{n+1} + b_1 u_n + b_2 u_{n-1})/dt =
+// g_0 R(u_{n+1}) + g_1 R(u_n)
+struct MultiStepTab { double beta[3], gamma[2]; };
+inline MultiStepTab multistep(int scheme) {
+  if (scheme == HC_BDF2) return {{1.5, -2.0, 0.5}, {1.0, 0.0}};
+  if (scheme == HC_TRAPEZIUM) return {{1.0, -1.0, 0.0}, {0.5, 0.5}};
+  return {{1.0, -1.0, 0.0}, {1.0, 0.0}};
+}
+
+template <class R>
+__global__ void cons_set_kernel(size_t n, Gas<R> g, const R* __restrict__ q, R* __restrict__ Q, int basis) {
+  for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < n; c += size_t(gridDim.x) * blockDim.x) {
+    R qk[4], qc[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) qk[v] = q[v * n + c];
+    basis_to_cons(g, qk, qc, basis != 0);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) Q[v * n + c] = qc[v];
+  }
+}
+
+// the earlier levels' terms of the dual-time residual, per cell:
+// src = g_1 R(u_n) - V (b_1 Q_n + b_2 Q_{n-1}) / dt
+template <class R>
+__global__ void dual_source_kernel(size_t n, const R* __restrict__ vol, const R* __restrict__ Qn,
+                                   const R* __restrict__ Qnm1, const R* __restrict__ Rn, R b1dt, R b2dt, R g1,
+                                   R* __restrict__ src) {
+  for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < n; c += size_t(gridDim.x) * blockDim.x) {
+    const R V = vol[c];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const R lev = b1dt * Qn[v * n + c] + b2dt * Qnm1[v * n + c];
+      src[v * n + c] = (Rn ? g1 * Rn[v * n + c] : R(0)) - V * lev;
+    }
+  }
+}
+
+template <class R> int dual_time_run(hc_ctx* c, const hc_dual_time_controls* ctl, hc_dual_time_stats* out) {
+  const size_t n = c->ncell();
+  const MultiStepTab ms = multistep(ctl->scheme);
+  const unsigned grid = unsigned(std::min<size_t>((n + 255) / 256, 152 * 16));
+  const Gas<R> g = make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale);
+  R* buf = nullptr;
+  const bool trap = ms.gamma[1] != 0.0;
+  HC_CUDA(cudaMalloc(&buf, (3 * 4 + (trap ? 5 : 0)) * n * sizeof(R)));
+  struct Reset {
+    hc_ctx* c; void* p;
+    ~Reset() { c->dual_src = nullptr; c->dual_g0 = 1.0; c->dual_b0dt = 0.0; cudaFree(p); }
+  } reset{c, buf};
+  R* Qn = buf;
+  R* Qnm1 = buf + 4 * n;
+  R* src = buf + 8 * n;
+  R* Rn = trap ? buf + 12 * n : nullptr;
+  // physical timestep: given, or cfl_outer / max(lambda/V) of the initial state (dualTime.ipp:54-56)
+  double dt = ctl->dt;
+  if (!(dt > 0.0)) {
+    HC_CUDA(cudaMemsetAsync(&c->info->maxrate, 0, sizeof(unsigned long long), c->stream));
+    StageArgs<R> a = base_args<R>(c);
+    a.q = (const R*)c->q[0];
+    a.res_out = (R*)c->res[0];
+    a.mode = MODE_RES_MAXRATE;
+    HC_CUDA(stage_fn<R>(c->cfg.flux)(a, c->tile, c->stream));
+    c->launches += 1;
+    unsigned long long bits = 0;
+    HC_CUDA(cudaMemcpyAsync(&bits, &c->info->maxrate, sizeof(bits), cudaMemcpyDeviceToHost, c->stream));
+    HC_CUDA(cudaStreamSynchronize(c->stream));
+    double rate;
+    std::memcpy(&rate, &bits, sizeof(rate));
+    dt = ctl->cfl_outer / std::fmax(rate, 2.2250738585072014e-308);
+  }
+  cons_set_kernel<R><<<grid, 256, 0, c->stream>>>(n, g, (const R*)c->q[0], Qn, c->cfg.basis);
+  HC_CUDA(cudaGetLastError());
+  HC_CUDA(cudaMemcpyAsync(Qnm1, Qn, 4 * n * sizeof(R), cudaMemcpyDeviceToDevice, c->stream));
+  c->launches += 1;
+  hc_dual_time_stats st{};
+  st.dt = dt;
+  HC_CUDA(cudaMemsetAsync(&c->info->status, 0, 2 * sizeof(int), c->stream));
+  for (int k = 0; k < ctl->outer_steps; ++k) {
+    if (trap) {
+      if (int e = run_residual<R>(c)) return e;
+      HC_CUDA(cudaMemcpyAsync(Rn, c->res[0], 4 * n * sizeof(R), cudaMemcpyDeviceToDevice, c->stream));
+    }
+    dual_source_kernel<R><<<grid, 256, 0, c->stream>>>(n, (const R*)c->vol, Qn, Qnm1, Rn, R(ms.beta[1] / dt),
+                                                        R(ms.beta[2] / dt), R(ms.gamma[1]), src);
+    HC_CUDA(cudaGetLastError());
+    c->launches += 1;
+    c->dual_src = src;
+    c->dual_g0 = ms.gamma[0];
+    c->dual_b0dt = ms.beta[0] / dt;
+    // pseudo-time iterations (dualTime.ipp:49-98): RK steps of the dual-time residual
+    double res0 = 0.0, res = 0.0;
+    int m = 0;
+    while (m < ctl->inner_max) {
+      const int chunk = (m == 0) ? 1 : std::min(ctl->check_every, ctl->inner_max - m);
+      for (int j = 0; j < chunk; ++j)
+        if (int e = run_step<R>(c)) return e;
+      m += chunk;
+      hc_step_stats s{};
+      if (int e = read_stats(c, &s)) return e;
+      res = s.resnorm;
+      if (m == 1) res0 = res;
+      if (ctl->inner_drop > 0.0 && res <= ctl->inner_drop * res0) break;
+    }
+    c->dual_src = nullptr;
+    c->dual_g0 = 1.0;
+    c->dual_b0dt = 0.0;
+    // next level: u_{n-1} <- u_n, u_n <- u_{n+1}
+    std::swap(Qn, Qnm1);
+    cons_set_kernel<R><<<grid, 256, 0, c->stream>>>(n, g, (const R*)c->q[0], Qn, c->cfg.basis);
+    HC_CUDA(cudaGetLastError());
+    c->launches += 1;
+    st.outer_steps += 1;
+    st.inner_steps += m;
+    st.last_inner = m;
+    st.res0_last = res0;
+    st.res_last = res;
+    st.t += dt;
+  }
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  if (out) *out = st;
+  return HC_OK;
+}
 
 extern "C" {
 
@@ -491,6 +616,17 @@ int hc_face_signatures(hc_ctx* c, unsigned long long* sig_i, unsigned long long*
   if (int st = ensure_ready(c)) return st;
   return c->fp32 ? run_signatures<float>(c, sig_i, sig_j, arg_i, arg_j)
                   : run_signatures<double>(c, sig_i, sig_j, arg_i, arg_j);
+}
+
+int hc_dual_time_run(hc_ctx* c, const hc_dual_time_controls* ctl, hc_dual_time_stats* stats) {
+  if (int st = check_ctx(c)) return st;
+  if (!ctl || ctl->outer_steps < 0 || ctl->inner_max < 1 || ctl->check_every < 1 || ctl->inner_drop < 0.0 ||
+      (ctl->scheme != HC_BDF1 && ctl->scheme != HC_BDF2 && ctl->scheme != HC_TRAPEZIUM) ||
+      (!(ctl->dt > 0.0) && !(ctl->cfl_outer > 0.0)))
+    return fail(HC_ERR_ARG, "invalid dual-time controls");
+  if (c->scalar) return fail(HC_ERR_UNSUPPORTED, "dual time covers the Euler law");
+  if (int st = ensure_ready(c)) return st;
+  return c->fp32 ? dual_time_run<float>(c, ctl, stats) : dual_time_run<double>(c, ctl, stats);
 }
 
 int hc_step_async(hc_ctx* c, int nsteps) {

@@ -156,7 +156,7 @@ template <class R> int per_instance_step(hc_batch* b) {
         const unsigned grid = unsigned(std::min<size_t>((n + 255) / 256, size_t(b->sms) * 16));
         update0_kernel<R><<<grid, 256, 0, b->stream>>>(base.ni, base.nj, base.gas, qp(0), rp(0), base.vol,
                                                        R(tab.alpha[0][0]), R(tab.beta[0]), b->cfg.cfl, base.info,
-                                                       out_of(0), 1, b->cfg.basis);
+                                                       out_of(0), 1, b->cfg.basis, 0.0);
         HC_CUDA(cudaGetLastError());
         b->launches += 2;
       } else {

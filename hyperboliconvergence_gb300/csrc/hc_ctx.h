@@ -18,6 +18,8 @@ struct hc_ctx {
   double gamma = 1.4, Rgas = 287.058, minf = 1e-4;
   double lref = 1., sdt = 1.7976931348623157e308;  // species lref and dt (AUSM+up scaling)
   int vscale = 0, pscale = 0;                       // AUSM+up LowMachScaling pair
+  void* dual_src = nullptr;                         // dual time: earlier levels' terms (4 planes, R)
+  double dual_g0 = 1.0, dual_b0dt = 0.0;            // dual time: gamma_0 and beta_0 / dt
   cudaStream_t own = nullptr, stream = nullptr;
   int tile = hc::TILE_8x32;
   // device buffers
@@ -58,6 +60,9 @@ template <class R> StageArgs<R> base_args(hc_ctx* c) {
   a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale);
   a.limiter = c->cfg.limiter;
   a.basis = c->cfg.basis;
+  a.dual_src = (const R*)c->dual_src;
+  a.dual_g0 = R(c->dual_g0);
+  a.dual_b0dt = R(c->dual_b0dt);
   a.fi = (const R*)c->fi; a.fj = (const R*)c->fj; a.vol = (const R*)c->vol;
   a.fic = c->fic; a.fjc = c->fjc;
   for (int k = 0; k < 4; ++k) a.gref[k] = (const R*)c->gref[k];

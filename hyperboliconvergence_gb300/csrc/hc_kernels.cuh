@@ -66,6 +66,10 @@ template <class R> struct StageArgs {
   unsigned long long* sig_j;
   double* arg_i;              // with them (or null): the 8 limiter calls' (a, b) per face, 16 values
   double* arg_j;
+  // dual time (null dual_src: off): the residual becomes dual_g0 R(q) - V dual_b0dt Q(q) +
+  // dual_src, Q the conserved set, dual_src (4 planes) the earlier time levels' terms
+  const R* dual_src;
+  R dual_g0, dual_b0dt;
 };
 
 // Branch signature of one face (recording kernels): bits 0-15 the limiter pieces of
@@ -132,6 +136,19 @@ template <class R> __device__ __forceinline__ void forward_update(const Gas<R>& 
   for (int v = 0; v < 4; ++v) qc[v] = qc[v] + tot[v] * fac;
   const St<R> s1 = cons_state(g, qc);
   qn[0] = s1.u; qn[1] = s1.v; qn[2] = s1.r; qn[3] = s1.p;
+}
+
+// the conserved set of a state in the solution basis
+template <class R> __device__ __forceinline__ void basis_to_cons(const Gas<R>& g, const R* q, R* qc, bool cons) {
+  if (cons) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) qc[v] = q[v];
+    return;
+  }
+  R u2 = q[0] * q[0];
+  u2 += q[1] * q[1];
+  qc[0] = q[2] * q[0]; qc[1] = q[2] * q[1]; qc[2] = q[2];
+  qc[3] = fma(q[3], g.gamma1, q[2] * (R(0.5) * u2));
 }
 
 // conversions between the storage type R and the compute type C of a stage
@@ -430,6 +447,17 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     lam = cvt<R>(((sfi[4 * NFI + s0] + sfi[4 * NFI + s1]) + sfj[4 * NFJ + t0]) + sfj[4 * NFJ + t1]);
   }
   const size_t c = size_t(gi) * nj + gj;
+  if (own && a.dual_src) {
+    // dual time (ode.h:10-83, OLD.fieldOperations/dualTimeResidual.ipp): the physical-time
+    // terms of the current iterate and of the earlier levels join the flux residual
+    R qk[4], qc[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) qk[v] = a.q[v * ncell + c];
+    basis_to_cons(a.gas, qk, qc, a.basis != 0);
+    const R vb = a.vol[c] * a.dual_b0dt;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) res[v] = a.dual_g0 * res[v] + (a.dual_src[v * ncell + c] - vb * qc[v]);
+  }
   if (own && a.res_out) {
 #pragma unroll
     for (int v = 0; v < 4; ++v) a.res_out[v * ncell + c] = res[v];
@@ -479,7 +507,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     // local timestep from the stage-0 spectral radius sum (eulerForwardUpdate.h:155-161)
     const R l0 = (a.stage == 0) ? lam : a.res_prev[0][4 * ncell + c];
     const R cs = a.beta * a.cfl;
-    fac = cs / l0;
+    // dual time: dtau / (1 + b0 dtau / dt), the physical-time term's share of the spectral radius
+    fac = a.dual_src ? cs / (l0 + a.cfl * a.vol[c] * a.dual_b0dt) : cs / l0;
   }
   R q0[4], qn[4];
 #pragma unroll
@@ -537,13 +566,15 @@ template <class R> __device__ __forceinline__ R global_dt(const StepInfo* info, 
   const double rate = fmax(DBL_MIN, __longlong_as_double((long long)info->maxrate));
   return R(cfl / rate);
 }
+__host__ __device__ __forceinline__ double dual_step(double dtau, double b0dt) { return dtau / (1.0 + b0dt * dtau); }
 
 template <class R>
 __global__ void update0_kernel(int ni, int nj, Gas<R> g, const R* __restrict__ q0, const R* __restrict__ res0,
                                const R* __restrict__ vol, R alpha00, R beta0, double cfl, StepInfo* info,
-                               R* __restrict__ q_out, int advance_time, int basis) {
+                               R* __restrict__ q_out, int advance_time, int basis, double dual_b0dt) {
   const size_t ncell = size_t(ni) * nj;
-  const R dt = global_dt<R>(info, cfl);
+  // dual time: the pseudo step dtau / (1 + b0 dtau / dt) (timestepping/dualTime.ipp:61-62)
+  const R dt = dual_b0dt > 0.0 ? R(dual_step(double(global_dt<R>(info, cfl)), dual_b0dt)) : global_dt<R>(info, cfl);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     info->dt = double(dt);
     if (advance_time) info->t += double(dt);
@@ -598,6 +629,11 @@ template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const B
   a.gas = b.gas;
   a.limiter = b.limiter;
   a.basis = b.basis;
+  a.sig_i = a.sig_j = nullptr;
+  a.arg_i = a.arg_j = nullptr;
+  a.dual_src = nullptr;  // batches have no dual time
+  a.dual_g0 = R(1);
+  a.dual_b0dt = R(0);
   const long long n = (long long)in.ni * in.nj;
   const long long off4 = 4 * in.cell, off5 = 5 * in.cell;
   a.q = b.q + off4;

@@ -218,6 +218,20 @@ class Solver:
         check(self.lib.hc_residual(self.h, _dptr(out)))
         return out
 
+    def dual_time(self, outer_steps: int, dt: float = 0.0, cfl_outer: float = 0.5, scheme: str = "bdf2",
+                  inner_max: int = 50, inner_drop: float = 0.0, check_every: int = 5):
+        """Dual-time stepping (include/hc.h, hc_dual_time_run): outer_steps physical steps of
+        the multistep scheme ("bdf1", "bdf2", "trapezium"), each solved by at most inner_max
+        pseudo-time RK steps (the solver's rk, cfl and dt mode) until the density dual-time
+        residual fell by inner_drop; dt <= 0 takes cfl_outer / max(lambda/V) of the current
+        state.  Returns the stats (dt, t, inner_steps, last_inner, res0_last, res_last)."""
+        from ._capi import MULTISTEP, DualTimeControls, DualTimeStats
+        ctl = DualTimeControls(int(outer_steps), float(dt), float(cfl_outer), MULTISTEP[scheme], int(inner_max),
+                               float(inner_drop), int(check_every))
+        st = DualTimeStats()
+        check(self.lib.hc_dual_time_run(self.h, C.byref(ctl), C.byref(st)))
+        return st
+
     def face_signatures(self, with_args: bool = False):
         """Branch signatures of one residual evaluation of the current state (include/hc.h,
         hc_face_signatures): uint64 arrays of shape (ni+1, nj) for the i-faces and (ni, nj+1)

@@ -212,6 +212,34 @@ int hc_spectral_radius(const double* lambda_sum_device, const double* vol_device
 int hc_spectral_radius_noalloc(const double* lambda_sum_device, const double* vol_device, long long ncell,
                                double* out_device, void* stream);
 
+/* Dual-time stepping: ODE::Implicit::MultiStep in physical time (ode.h:10-83) with explicit
+ * pseudo-time iterations, the scheme of the reference's legacy 1D driver
+ * (timestepping/dualTime.ipp:5-99, OLD.fieldOperations/dualTimeResidual.ipp:3-42) on this
+ * path.  Each physical step solves b_0 Q(u)/dt - g_0 R(u) = -(b_1 Q_n + b_2 Q_{n-1})/dt +
+ * g_1 R(u_n) (Q the conserved set, R the flux residual, times the cell volume) by RK steps of
+ * the context's table in pseudo time, the context's cfl and dt mode, each pseudo step
+ * dtau / (1 + b_0 dtau / dt) (dualTime.ipp:61-62; local pseudo steps take the physical term
+ * into the spectral radius); the inner loop stops after inner_max steps or once the density
+ * dual-time residual fell by inner_drop (checked every check_every steps; 0 = never).  The
+ * first step of BDF2 takes u_{n-1} = u_n, as the reference's initialisation does. */
+typedef enum { HC_BDF1 = 0, HC_BDF2 = 1, HC_TRAPEZIUM = 2 } hc_multistep;
+typedef struct {
+  int outer_steps;   /* physical steps */
+  double dt;         /* physical timestep; <= 0: cfl_outer / max(lambda/V) of the initial state */
+  double cfl_outer;
+  int scheme;        /* hc_multistep: backwardDifference1/2, trapeziumRule2 (ode.h:30-83) */
+  int inner_max;     /* pseudo-time steps per physical step at most */
+  double inner_drop; /* stop once ||R*_rho|| <= inner_drop * its first value (0: run inner_max) */
+  int check_every;   /* pseudo-time steps between convergence checks */
+} hc_dual_time_controls;
+typedef struct {
+  long long outer_steps, inner_steps;
+  int last_inner;          /* pseudo steps of the last physical step */
+  double dt, t;            /* physical timestep and time advanced */
+  double res0_last, res_last; /* first and last dual-time density residual norm of the last step */
+} hc_dual_time_stats;
+int hc_dual_time_run(hc_ctx* ctx, const hc_dual_time_controls* ctl, hc_dual_time_stats* stats);
+
 /* Branch signatures for the parity report (no counterpart in the reference): one
  * residual evaluation of the current state through a recording instantiation of the
  * stage kernel (the stepping kernels are not changed by it) that writes, per face, which

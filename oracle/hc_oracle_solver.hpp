@@ -46,6 +46,10 @@ template <class R> struct Solver {
   double* arg_i = nullptr;
   double* arg_j = nullptr;
   std::vector<unsigned> bc_path[4];  // far-field path per ghost face of the last boundary update
+  // dual time (set by dual_time): residual -> g0 R(q) - V b0dt Q(q) + src (AoS [cell][4])
+  bool dual = false;
+  R dual_g0 = 1, dual_b0dt = 0;
+  std::vector<R> dual_src;
   R cfl = 0.5;
   int bc[4] = {BC_PERIODIC, BC_PERIODIC, BC_PERIODIC, BC_PERIODIC};
   // ghost arrays per side: [side][face][layer][var]; layer 0 = ghost value,
@@ -400,6 +404,57 @@ template <class R> struct Solver {
     }
   }
 
+  // ---- dual time (ode.h:10-83, timestepping/dualTime.ipp:5-99,
+  // OLD.fieldOperations/dualTimeResidual.ipp:3-42): the flux residual of the iterate becomes
+  // g0 R(q) - V (b0/dt) Q(q) + src, src = g1 R(q_n) - V (b1 Q_n + b2 Q_{n-1}) / dt
+  void cons_of(const R* q, R* qc) const {
+    if (basis == BASIS_CONSERVED) for (int v = 0; v < 4; ++v) qc[v] = q[v];
+    else prim2cons(sp, q, qc);
+  }
+  void add_dual_terms(const std::vector<R>& q, std::vector<FluxRes<R>>& r) const {
+    const size_t n = size_t(ni) * nj;
+    for (size_t c = 0; c < n; ++c) {
+      R qc[4];
+      cons_of(&q[c * 4], qc);
+      const R vb = cells[c].vol * dual_b0dt;
+      for (int v = 0; v < 4; ++v) r[c].f[v] = dual_g0 * r[c].f[v] + (dual_src[c * 4 + v] - vb * qc[v]);
+    }
+  }
+  // outer physical steps of the multistep scheme (BDF1 / BDF2 / trapezium) with `inner`
+  // pseudo-time RK steps each; dt <= 0: cfl_outer / spectral radius of the initial state
+  R dual_time(int outer, R dtp, R cfl_outer, int scheme, int inner) {
+    R beta[3] = {1., -1., 0.}, gam[2] = {1., 0.};
+    if (scheme == 1) { beta[0] = 1.5; beta[1] = -2.; beta[2] = 0.5; }
+    else if (scheme == 2) { gam[0] = 0.5; gam[1] = 0.5; }
+    const size_t n = size_t(ni) * nj;
+    if (!(dtp > 0)) { residual(q0, res[0]); dtp = cfl_outer / spectral_radius(res[0]); }
+    std::vector<R> Qn(n * 4), Qm(n * 4), Rn(n * 4, R(0));
+    for (size_t c = 0; c < n; ++c) cons_of(&q0[c * 4], &Qn[c * 4]);
+    Qm = Qn;
+    const R tsave = t;
+    for (int k = 0; k < outer; ++k) {
+      if (gam[1] != 0) {
+        residual(q0, res[0]);
+        for (size_t c = 0; c < n; ++c) for (int v = 0; v < 4; ++v) Rn[c * 4 + v] = res[0][c].f[v];
+      }
+      dual_src.assign(n * 4, R(0));
+      const R b1dt = beta[1] / dtp, b2dt = beta[2] / dtp;
+      for (size_t c = 0; c < n; ++c)
+        for (int v = 0; v < 4; ++v) {
+          const R lev = b1dt * Qn[c * 4 + v] + b2dt * Qm[c * 4 + v];
+          dual_src[c * 4 + v] = gam[1] * Rn[c * 4 + v] - cells[c].vol * lev;
+        }
+      dual = true; dual_g0 = gam[0]; dual_b0dt = beta[0] / dtp;
+      for (int m = 0; m < inner; ++m) step(1);
+      dual = false;
+      std::swap(Qn, Qm);
+      for (size_t c = 0; c < n; ++c) cons_of(&q0[c * 4], &Qn[c * 4]);
+    }
+    t = tsave + outer * dtp;
+    last_dt = dtp;
+    return dtp;
+  }
+
   // ---- spectralRadius (spatial/spectralRadius.h:19-48)
   R spectral_radius(const std::vector<FluxRes<R>>& r) const {
     R m = std::numeric_limits<R>::min();
@@ -416,9 +471,14 @@ template <class R> struct Solver {
       q1 = q0;
       for (int s = 0; s < tab.nstages; ++s) {
         residual(q1, res[s]);
+        if (dual) add_dual_terms(q1, res[s]);
         if (s == 0) {
-          if (dtmode == DT_GLOBAL) dt = freeze(cfl / spectral_radius(res[0]));
-          else for (size_t c = 0; c < n; ++c) lam0[c] = freeze(res[0][c].lam);
+          if (dtmode == DT_GLOBAL) {
+            dt = freeze(cfl / spectral_radius(res[0]));
+            if (dual) dt = freeze(dt / (1. + dual_b0dt * dt));  // dtau / (1 + b0 dtau / dt)
+          } else {
+            for (size_t c = 0; c < n; ++c) lam0[c] = freeze(res[0][c].lam);
+          }
         }
 #pragma omp parallel for schedule(static)
         for (long c = 0; c < (long)n; ++c) {
@@ -429,7 +489,10 @@ template <class R> struct Solver {
           // eulerForwardUpdateGlobal / Local (spatial/eulerForwardUpdate.h:38-168)
           R fac;
           if (dtmode == DT_GLOBAL) { const R dts = tab.beta[s] * dt; fac = dts / cells[c].vol; }
-          else { const R cs = tab.beta[s] * cfl; fac = cs / lam0[c]; }
+          else {
+            const R cs = tab.beta[s] * cfl;
+            fac = dual ? cs / (lam0[c] + cfl * cells[c].vol * dual_b0dt) : cs / lam0[c];
+          }
           // solution basis -> conserved (+ increment) -> solution basis; a conserved
           // field is its own conserved set (set2Set of the same type copies)
           R qc[4];

@@ -132,6 +132,11 @@ void hco_cells(void* h, double* out) {
     out[c] = s->cells[c].vol; out[n + c] = s->cells[c].c[0]; out[2 * n + c] = s->cells[c].c[1];
   }
 }
+// dual-time stepping: outer physical steps of scheme (0 BDF1, 1 BDF2, 2 trapezium) with inner
+// pseudo-time RK steps each; returns the physical dt (dt <= 0: from cfl_outer)
+double hco_dual_time(void* h, int outer, double dt, double cfl_outer, int scheme, int inner) {
+  return static_cast<S*>(h)->dual_time(outer, dt, cfl_outer, scheme, inner);
+}
 void hco_set_threads(int n) { omp_set_num_threads(n); }
 int hco_get_threads(void) { return omp_get_max_threads(); }
 

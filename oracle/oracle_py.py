@@ -290,6 +290,14 @@ class OracleSolver:
         self.lib.hco_step(self.h, int(n), out)
         return float(out[0]), float(out[1])
 
+    def dual_time(self, outer, dt=0.0, cfl_outer=0.5, scheme="bdf2", inner=10):
+        """Dual-time stepping (the CUDA path's hc_dual_time_run with a fixed inner count);
+        returns the physical timestep."""
+        self.lib.hco_dual_time.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int]
+        self.lib.hco_dual_time.restype = C.c_double
+        k = {"bdf1": 0, "bdf2": 1, "trapezium": 2}[scheme] if isinstance(scheme, str) else int(scheme)
+        return self.lib.hco_dual_time(self.h, int(outer), float(dt), float(cfl_outer), k, int(inner))
+
     def face_signatures(self, with_args=False):
         """Branch signatures of one residual evaluation (the CUDA path's codes); with_args
         also returns the limiter arguments, arrays (ni+1, nj, 8, 2) and (ni, nj+1, 8, 2) of
