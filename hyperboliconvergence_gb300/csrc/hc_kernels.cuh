@@ -168,8 +168,9 @@ template <class C, class R> __device__ __forceinline__ Gas<C> gas_as(const Gas<R
 // gradients, reconstruction and fluxes are computed in (C = R, or double-float
 // for FP64 storage, reading the face records from a.fic / a.fjc).
 // REC: the recording instantiation also writes each face's branch signature to
-// a.sig_i / a.sig_j (the production instantiations compile without it).
-template <int TI, int TJ, class R, int FK, class C = R, bool REC = false>
+// a.sig_i / a.sig_j (the production instantiations compile without it).  DUAL: dual-time
+// terms are honoured (the batched instantiations, which have none, compile without them).
+template <int TI, int TJ, class R, int FK, class C = R, bool REC = false, bool DUAL = true>
 __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj, unsigned char* smem_raw) {
   constexpr bool same = std::is_same<C, R>::value;
   using SM = StageSmem<TI, TJ, C>;
@@ -447,7 +448,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     lam = cvt<R>(((sfi[4 * NFI + s0] + sfi[4 * NFI + s1]) + sfj[4 * NFJ + t0]) + sfj[4 * NFJ + t1]);
   }
   const size_t c = size_t(gi) * nj + gj;
-  if (own && a.dual_src) {
+  if (DUAL && own && a.dual_src) {
     // dual time (ode.h:10-83, OLD.fieldOperations/dualTimeResidual.ipp): the physical-time
     // terms of the current iterate and of the earlier levels join the flux residual
     R qk[4], qc[4];
@@ -508,7 +509,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     const R l0 = (a.stage == 0) ? lam : a.res_prev[0][4 * ncell + c];
     const R cs = a.beta * a.cfl;
     // dual time: dtau / (1 + b0 dtau / dt), the physical-time term's share of the spectral radius
-    fac = a.dual_src ? cs / (l0 + a.cfl * a.vol[c] * a.dual_b0dt) : cs / l0;
+    fac = (DUAL && a.dual_src) ? cs / (l0 + a.cfl * a.vol[c] * a.dual_b0dt) : cs / l0;
   }
   R q0[4], qn[4];
 #pragma unroll
@@ -683,7 +684,7 @@ __global__ void __launch_bounds__(TI * TJ, (BatchResidency<R, TI * TJ>::value))
       tile_ij[1] = t % tj;
     }
     __syncthreads();
-    stage_tile<TI, TJ, R, FK>(sa, tile_ij[0], tile_ij[1], smem_raw);
+    stage_tile<TI, TJ, R, FK, R, false, false>(sa, tile_ij[0], tile_ij[1], smem_raw);
   }
 }
 
