@@ -318,6 +318,57 @@ class OracleSolver:
         return out
 
 
+class OracleSolver1D:
+    """CPU restatement of the reference's one-dimensional Euler path (hc_oracle_1d.hpp);
+    state {u, rho, p} as 3 planes of nc values; ref: (left, right) reference states."""
+
+    def __init__(self, nodes, bc, flux="roe", limiter="vanleer", rk="ssp34", dt="global", cfl=0.5,
+                 species=(1.4, 287.058, 1e-4), ref=None, fast=False):
+        self.lib = load(fast)
+        lib = self.lib
+        lib.hco1_create.restype = C.c_void_p
+        lib.hco1_create.argtypes = [C.c_int, _dp, _ip, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, C.c_void_p]
+        lib.hco1_destroy.argtypes = [C.c_void_p]
+        lib.hco1_set_state.argtypes = [C.c_void_p, _dp]
+        lib.hco1_get_state.argtypes = [C.c_void_p, _dp]
+        lib.hco1_residual.argtypes = [C.c_void_p, _dp]
+        lib.hco1_step.argtypes = [C.c_void_p, C.c_int, _dp]
+        x = np.ascontiguousarray(nodes, dtype=np.float64)
+        self.nc = x.size - 1
+        bcv = np.array([BC[b] if isinstance(b, str) else int(b) for b in bc], dtype=np.int32)
+        refa = None if ref is None else np.ascontiguousarray(
+            [np.zeros(3) if r is None else np.asarray(r, dtype=np.float64) for r in ref], dtype=np.float64)
+        self._ref = refa
+        self.h = lib.hco1_create(self.nc, x, bcv, FLUX[flux] if isinstance(flux, str) else flux,
+                                 LIMITER[limiter] if isinstance(limiter, str) else limiter,
+                                 RK[rk] if isinstance(rk, str) else rk, DT[dt] if isinstance(dt, str) else dt,
+                                 float(cfl), np.asarray(species, dtype=np.float64),
+                                 None if refa is None else refa.ctypes.data)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.hco1_destroy(self.h)
+            self.h = None
+
+    def set_state(self, prim):
+        self.lib.hco1_set_state(self.h, np.ascontiguousarray(prim, dtype=np.float64))
+
+    def get_state(self):
+        out = np.empty((3, self.nc))
+        self.lib.hco1_get_state(self.h, out)
+        return out
+
+    def residual(self):
+        out = np.empty((4, self.nc))
+        self.lib.hco1_residual(self.h, out)
+        return out
+
+    def step(self, n=1):
+        out = np.empty(2)
+        self.lib.hco1_step(self.h, int(n), out)
+        return float(out[0]), float(out[1])
+
+
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 

@@ -243,6 +243,44 @@ void ref_wall_flux_cons(const double* species, const double* face, const double*
                    cons_of(qi), cons_of(qi)),
       out5);
 }
+// One-dimensional pointwise functions (nDim = 1: primitive sets {u, rho, p}, the face of a
+// node with area 1 and normal +1, geometry/surface.ipp:4-11)
+using Prim1 = VariableSet<Law, 1, EulerBases::Primitive, Real>;
+static Prim1 prim1_of(const double* q) { return Prim1{q[0], q[1], q[2]}; }
+static void put1(const FluxResult<Law, 1, Real>& r, double* out4) {
+  for (int v = 0; v < 3; ++v) out4[v] = r.flux[v];
+  out4[3] = r.lambda;
+}
+void ref_flux_1d(int kind, const double* species, const double* ql, const double* qr, double* out4) {
+  const auto sp = species_of(species);
+  const auto f = geom::surface(geom::Point<1, Real>{0.});
+  const Prim1 l = prim1_of(ql), r = prim1_of(qr);
+  switch (kind) {
+    case 0: put1(RoeFlux<Law>{}(sp, f, l, r), out4); break;
+    case 2: put1(Slau<LowMachScaling::Convective, LowMachScaling::Acoustic>{}(sp, f, l, r), out4); break;
+    case 3: put1(AusmPlusUP<LowMachScaling::Convective, LowMachScaling::Convective>{}(sp, f, l, r), out4); break;
+    case 4: put1(RusanovFlux<Law>{}(sp, f, l, r), out4); break;
+    case 5: put1(CentralFlux<Law>{}(sp, f, l, r), out4); break;
+    case 6: put1(RoeUnprecWS{}(sp, f, l, r), out4); break;
+    default: for (int v = 0; v < 4; ++v) out4[v] = std::nan("");
+  }
+}
+// boundary update of side 0 (left, face normal +1 into the domain) or 1 (right, the node's
+// face flipped, spatial/boundary/boundaryUpdate.h:108-131); kind 2 Riemann, 3 Entropy
+void ref_bc_update_1d(int kind, const double* species, int side, const double* qi, const double* qf, double* qb) {
+  const auto sp = species_of(species);
+  auto f = geom::surface(geom::Point<1, Real>{0.});
+  if (side == 1) f = geom::flip(f);
+  geom::Volume<1, Real> cell;
+  cell.volume = 1.;
+  cell.centre = geom::Point<1, Real>{f.metric[0][0]};
+  Prim1 r;
+  if (kind == 2)
+    r = boundaryUpdate(std::integral_constant<EulerBCs, EulerBCs::Riemann>{}, sp, f, cell, prim1_of(qi), prim1_of(qf));
+  else
+    r = boundaryUpdate(std::integral_constant<EulerBCs, EulerBCs::Entropy>{}, sp, f, cell, prim1_of(qi), prim1_of(qf));
+  for (int v = 0; v < 3; ++v) qb[v] = r[v];
+}
 // 0 cons->prim, 1 prim->cons, 2 prim->char, 3 char->prim about the state of q
 void ref_delta(int kind, const double* species, const double* q, const double* din, double* dout) {
   const auto sp = species_of(species);

@@ -134,6 +134,25 @@ def main():
     for k in (2, 3):
         g[f"cons_bc_{k}"] = np.stack([ref.bc_update_cons(k, species, faces[m], cl[m], cf[m]) for m in range(nf)])
     g["cons_wall_out"] = np.stack([ref.wall_flux_cons(species, faces[m], cl[m], dq[m]) for m in range(nf)])
+    # one-dimensional fluxes and boundary updates (nDim = 1: {u, rho, p}, the face of a node)
+    import ctypes as C
+    dpp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+    ref.lib.ref_flux_1d.argtypes = [C.c_int, dpp, dpp, dpp, dpp]
+    ref.lib.ref_bc_update_1d.argtypes = [C.c_int, dpp, C.c_int, dpp, dpp, dpp]
+    l1 = np.ascontiguousarray(ql[:, [0, 2, 3]])
+    r1 = np.ascontiguousarray(qr[:, [0, 2, 3]])
+    g["q1d_l"], g["q1d_r"] = l1, r1
+
+    def call(fn, shape, *args):
+        out = np.empty(shape)
+        fn(*args, out)
+        return out
+    for k in REF_FLUXES:
+        g[f"flux_1d_{k}"] = np.stack([call(ref.lib.ref_flux_1d, 4, k, species, l1[m], r1[m]) for m in range(nf)])
+    for side in (0, 1):
+        for k in (2, 3):
+            g[f"bc_1d_{side}_{k}"] = np.stack([call(ref.lib.ref_bc_update_1d, 3, k, species, side, l1[m], r1[m])
+                                               for m in range(nf)])
     g["cyl_nodes"] = ref.cylinder_nodes(12, 16, 0.5, 20.0)
     g["lin_nodes"] = ref.linspace_nodes(9, 7, 0.0, 10.0, -1.0, 3.0)
     np.savez_compressed(OUT, **g)

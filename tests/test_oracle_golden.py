@@ -88,6 +88,35 @@ def test_wall_flux_conserved_basis(g, o):
     same([o.wall_flux_cons(sp, f[m], g["cons_ql"][m], g["wall_dq"][m]) for m in range(len(f))], g["cons_wall_out"])
 
 
+def _emb(q):
+    return np.array([q[0], 0.0, q[1], q[2]])
+
+
+@pytest.mark.parametrize("kind", [0, 2, 3, 4, 5, 6])
+def test_one_dimensional_fluxes(g, o, kind):
+    """The reference's nDim = 1 fluxes equal the oracle's 2D fluxes with the second velocity
+    0 on the face (area 1, normal (1, 0)) of a node: the 1D oracle path reuses them."""
+    sp, face = g["species"], np.array([1.0, 0.0, 0.0, 1.0, 0.0, 0.0, 1.0])
+    got = []
+    for ql, qr in zip(g["q1d_l"], g["q1d_r"]):
+        f = o.flux(kind, sp, face, _emb(ql), _emb(qr))
+        got.append([f[0], f[2], f[3], f[4]])
+    same(got, g[f"flux_1d_{kind}"])
+
+
+@pytest.mark.parametrize("side", [0, 1])
+@pytest.mark.parametrize("kind", [2, 3])
+def test_one_dimensional_boundary_updates(g, o, side, kind):
+    sp = g["species"]
+    n = 1.0 if side == 0 else -1.0  # into the domain
+    face = np.array([1.0, 0.0, 0.0, n, 0.0, 0.0, n])
+    got = []
+    for ql, qr in zip(g["q1d_l"], g["q1d_r"]):
+        b = o.bc_update(kind, sp, face, _emb(ql), _emb(qr))
+        got.append([b[0], b[2], b[3]])
+    same(got, g[f"bc_1d_{side}_{kind}"])
+
+
 def test_exact_flux(g, o):
     f, sp = g["surface_out"], g["species"]
     same([o.exact_flux(sp, f[m][3:5].copy(), g["flux_ql"][m]) for m in range(len(f))], g["exact_flux"])
