@@ -56,6 +56,7 @@ def _declare(lib):
         "hc_set_stream": [p, v],
         "hc_get_stream": [p, C.POINTER(C.c_void_p)],
         "hc_mesh_upload": [p, i, i, dp],
+        "hc_mesh_upload_1d": [p, i, dp],
         "hc_set_species": [p, d, d, d],
         "hc_set_low_mach": [p, i, i, d, d],
         "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],

@@ -423,6 +423,7 @@ int reverse(AD& A, const Schedule& sc, int a, int b, int slot, std::vector<int>&
 
 inline int check_support(hc_ctx* c) {
   if (c->scalar) return fail(HC_ERR_UNSUPPORTED, "the adjoint covers the Euler law");
+  if (c->oned) return fail(HC_ERR_UNSUPPORTED, "the adjoint covers the 2D path");
   if (c->cfg.basis != HC_BASIS_PRIMITIVE) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the primitive basis");
   if (c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV)
     return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");

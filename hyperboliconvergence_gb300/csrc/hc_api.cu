@@ -69,8 +69,35 @@ int check_ctx(hc_ctx* c) {
 }
 
 // Derive cells, faces and least-squares weights on the device (runs once per mesh/bc set).
+int build_geometry_1d(hc_ctx* c) {
+  const int nc = c->ni;
+  std::vector<double> rec, vol;
+  oned_geometry(c->hx.data(), nc, c->bc, rec, vol);
+  HC_CUDA(cudaMemcpyAsync(c->fi64, rec.data(), rec.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  HC_CUDA(cudaMemcpyAsync(c->vol64, vol.data(), vol.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (c->fp32) {
+    convert_kernel<float><<<256, 256, 0, c->stream>>>(c->fi64, (float*)c->fi, rec.size());
+    convert_kernel<float><<<256, 256, 0, c->stream>>>(c->vol64, (float*)c->vol, vol.size());
+    c->launches += 2;
+    HC_CUDA(cudaGetLastError());
+  }
+  for (int s = 0; s < 2; ++s) {
+    if (c->bc[s] == HC_BC_PERIODIC || c->bc[s] == HC_BC_WALL || c->href[s].empty()) continue;
+    if (c->fp32) {
+      const float tmp[3] = {float(c->href[s][0]), float(c->href[s][1]), float(c->href[s][2])};
+      HC_CUDA(cudaMemcpyAsync(c->gref[s], tmp, sizeof(tmp), cudaMemcpyHostToDevice, c->stream));
+    } else {
+      HC_CUDA(cudaMemcpyAsync(c->gref[s], c->href[s].data(), 3 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    }
+  }
+  HC_CUDA(cudaStreamSynchronize(c->stream));  // the host vectors go out of scope
+  c->geom_dirty = false;
+  return HC_OK;
+}
+
 int build_geometry(hc_ctx* c) {
   if (!c->have_mesh || !c->have_bcs) return fail(HC_ERR_ARG, "mesh and boundary conditions must be set first");
+  if (c->oned) return build_geometry_1d(c);
   const int ni = c->ni, nj = c->nj;
   const size_t n = c->ncell();
   const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
@@ -121,7 +148,70 @@ int hc::ctx_ensure_ready(hc_ctx* c) { return ensure_ready(c); }
 
 namespace {
 
+template <class R> Stage1DArgs<R> args_1d(hc_ctx* c) {
+  Stage1DArgs<R> a{};
+  a.nc = c->ni;
+  a.bc[0] = c->bc[0]; a.bc[1] = c->bc[1];
+  a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale);
+  a.limiter = c->cfg.limiter;
+  a.rec = (const R*)c->fi;
+  a.vol = (const R*)c->vol;
+  a.gref[0] = (const R*)c->gref[0]; a.gref[1] = (const R*)c->gref[1];
+  a.q0 = (const R*)c->q[0];
+  a.info = c->info;
+  a.cfl = R(c->cfg.cfl);
+  return a;
+}
+
+template <class R> int run_residual_1d(hc_ctx* c) {
+  Stage1DArgs<R> a = args_1d<R>(c);
+  a.q = (const R*)c->q[0];
+  a.res_out = (R*)c->res[0];
+  a.mode = MODE_RESIDUAL;
+  HC_CUDA(launch_stage1d<R>(a, c->cfg.flux, c->stream));
+  c->launches += 1;
+  return HC_OK;
+}
+
+// one RK step of the 1D path (the same stage loop as run_step)
+template <class R> int run_step_1d(hc_ctx* c) {
+  const RKTab tab = rk_table(c->cfg.rk);
+  const int nst = tab.nst;
+  const bool global = c->cfg.dt_mode == HC_DT_GLOBAL;
+  HC_CUDA(cudaMemsetAsync(&c->info->maxrate, 0, sizeof(unsigned long long), c->stream));
+  HC_CUDA(cudaMemsetAsync(&c->info->resnorm2, 0, sizeof(double), c->stream));
+  auto out_of = [&](int s) -> R* { return (R*)((s == nst - 1) ? c->q[0] : c->q[1 + (s % 2)]); };
+  for (int s = 0; s < nst; ++s) {
+    Stage1DArgs<R> a = args_1d<R>(c);
+    a.q = (s == 0) ? (const R*)c->q[0] : out_of(s - 1);
+    a.stage = s;
+    a.beta = R(tab.beta[s]);
+    for (int k = 0; k <= s; ++k) a.alpha[k] = R(tab.alpha[s][k]);
+    for (int k = 0; k < s; ++k) a.res_prev[k] = (const R*)c->res[k];
+    a.res_out = (s < nst - 1) ? (R*)c->res[s] : nullptr;
+    a.norm_stage0 = (s == 0);
+    if (global && s == 0) {
+      a.mode = MODE_RES_MAXRATE;
+      a.res_out = (R*)c->res[0];
+      HC_CUDA(launch_stage1d<R>(a, c->cfg.flux, c->stream));
+      const unsigned grid = unsigned(std::min<size_t>((c->ncell() + 255) / 256, 152 * 16));
+      update0_1d_kernel<R><<<grid, 256, 0, c->stream>>>(c->ni, a.gas, (const R*)c->q[0], (const R*)c->res[0],
+                                                         (const R*)c->vol, R(tab.alpha[0][0]), R(tab.beta[0]),
+                                                         c->cfg.cfl, c->info, out_of(0));
+      HC_CUDA(cudaGetLastError());
+      c->launches += 2;
+    } else {
+      a.mode = global ? MODE_FUSED_GLOBAL : MODE_FUSED_LOCAL;
+      a.q_out = out_of(s);
+      HC_CUDA(launch_stage1d<R>(a, c->cfg.flux, c->stream));
+      c->launches += 1;
+    }
+  }
+  return HC_OK;
+}
+
 template <class R> int run_residual(hc_ctx* c) {
+  if (c->oned) return run_residual_1d<R>(c);
   StageArgs<R> a = base_args<R>(c);
   a.q = (const R*)c->q[0];
   a.res_out = (R*)c->res[0];
@@ -134,6 +224,7 @@ template <class R> int run_residual(hc_ctx* c) {
 
 // One RK step: the stage loop of integrate() (timestepping/rungeKutta.h:97-164).
 template <class R> int run_step(hc_ctx* c) {
+  if (c->oned) return run_step_1d<R>(c);
   const RKTab tab = rk_table(c->cfg.rk);
   const int nst = tab.nst;
   const bool global = c->cfg.dt_mode == HC_DT_GLOBAL;
@@ -458,6 +549,9 @@ int hc_mesh_upload(hc_ctx* c, int ni, int nj, const double* nodes_xy) {
   if (size_t(ni + 1) * size_t(nj + 1) > (size_t(1) << 28)) return fail(HC_ERR_ARG, "mesh too large");
   HC_CUDA(cudaStreamSynchronize(c->stream));
   free_buffers(c);
+  c->oned = false;
+  c->nv = c->scalar ? 3 : 4;
+  c->hx.clear();
   c->ni = ni; c->nj = nj;
   const size_t n = c->ncell();
   const size_t nfi = size_t(ni + 1) * nj, nfj = size_t(ni) * (nj + 1);
@@ -496,6 +590,44 @@ int hc_mesh_upload(hc_ctx* c, int ni, int nj, const double* nodes_xy) {
   return HC_OK;
 }
 
+int hc_mesh_upload_1d(hc_ctx* c, int nc, const double* nodes_x) {
+  if (int st = check_ctx(c)) return st;
+  if (!nodes_x) return fail(HC_ERR_ARG, "null nodes");
+  if (nc < 3 || nc > (1 << 28)) return fail(HC_ERR_ARG, "a 1D mesh needs 3 to 2^28 cells");
+  if (c->scalar) return fail(HC_ERR_UNSUPPORTED, "the 1D path covers the Euler law");
+  if (c->df || c->cfg.basis != HC_BASIS_PRIMITIVE)
+    return fail(HC_ERR_UNSUPPORTED, "the 1D path runs in FP64 or FP32 in the primitive basis");
+  for (int i = 0; i < nc; ++i)
+    if (!(nodes_x[i + 1] > nodes_x[i])) return fail(HC_ERR_ARG, "1D nodes must increase");
+  HC_CUDA(cudaStreamSynchronize(c->stream));
+  free_buffers(c);
+  c->oned = true;
+  c->nv = 3;
+  c->ni = nc; c->nj = 1;
+  c->hx.assign(nodes_x, nodes_x + nc + 1);
+  const size_t n = size_t(nc), nf = size_t(nc) + 1;
+  HC_CUDA(cudaMalloc(&c->info, sizeof(StepInfo)));
+  HC_CUDA(cudaMemsetAsync(c->info, 0, sizeof(StepInfo), c->stream));
+  HC_CUDA(cudaMalloc(&c->vol64, n * sizeof(double)));
+  HC_CUDA(cudaMalloc(&c->fi64, F1REC * nf * sizeof(double)));
+  if (c->fp32) {
+    HC_CUDA(cudaMalloc(&c->fi, F1REC * nf * sizeof(float)));
+    HC_CUDA(cudaMalloc(&c->vol, n * sizeof(float)));
+    HC_CUDA(cudaMalloc(&c->staging, 4 * n * sizeof(double)));
+  } else {
+    c->fi = c->fi64; c->vol = c->vol64;
+  }
+  for (int k = 0; k < 3; ++k) HC_CUDA(cudaMalloc(&c->q[k], 3 * n * c->rsz));
+  for (int k = 0; k < 4; ++k) HC_CUDA(cudaMalloc(&c->res[k], 4 * n * c->rsz));
+  for (int s = 0; s < 2; ++s) HC_CUDA(cudaMalloc(&c->gref[s], 3 * c->rsz));
+  c->have_mesh = true;
+  c->have_bcs = false;
+  c->have_state = false;
+  c->geom_dirty = true;
+  for (int s = 0; s < 4; ++s) c->href[s].clear();
+  return HC_OK;
+}
+
 int hc_set_species(hc_ctx* c, double gamma, double gas_constant, double minf) {
   if (int st = check_ctx(c)) return st;
   if (!(gamma > 1.0) || !(gas_constant > 0.0) || !(minf > 0.0)) return fail(HC_ERR_ARG, "invalid species");
@@ -517,6 +649,23 @@ int hc_set_bcs(hc_ctx* c, const int bc_type[4], const double* const ref[4]) {
   if (int st = check_ctx(c)) return st;
   if (!c->have_mesh) return fail(HC_ERR_ARG, "upload the mesh before the boundary conditions");
   if (!bc_type) return fail(HC_ERR_ARG, "null bc types");
+  if (c->oned) {  // sides 0 (left) and 1 (right); 2 and 3 do not exist
+    for (int s = 0; s < 2; ++s)
+      if (bc_type[s] < HC_BC_PERIODIC || bc_type[s] > HC_BC_WALL) return fail(HC_ERR_ARG, "unknown bc type");
+    if ((bc_type[0] == HC_BC_PERIODIC) != (bc_type[1] == HC_BC_PERIODIC))
+      return fail(HC_ERR_ARG, "periodic sides must come in pairs (0,1)");
+    for (int s = 0; s < 4; ++s) {
+      c->bc[s] = s < 2 ? bc_type[s] : HC_BC_PERIODIC;
+      c->href[s].clear();
+      if (s < 2 && bc_type[s] != HC_BC_PERIODIC && bc_type[s] != HC_BC_WALL) {
+        if (!ref || !ref[s]) return fail(HC_ERR_ARG, "side " + std::to_string(s) + " needs reference values");
+        c->href[s].assign(ref[s], ref[s] + 3);
+      }
+    }
+    c->have_bcs = true;
+    c->geom_dirty = true;
+    return HC_OK;
+  }
   for (int s = 0; s < 4; ++s) {
     if (bc_type[s] < HC_BC_PERIODIC || bc_type[s] > HC_BC_WALL) return fail(HC_ERR_ARG, "unknown bc type");
     if (c->scalar && (bc_type[s] == HC_BC_ENTROPY || bc_type[s] == HC_BC_WALL))
@@ -612,7 +761,7 @@ int hc_face_signatures(hc_ctx* c, unsigned long long* sig_i, unsigned long long*
                        double* arg_j) {
   if (int st = check_ctx(c)) return st;
   if (!sig_i || !sig_j) return fail(HC_ERR_ARG, "null output");
-  if (c->scalar) return fail(HC_ERR_UNSUPPORTED, "branch signatures cover the Euler law");
+  if (c->scalar || c->oned) return fail(HC_ERR_UNSUPPORTED, "branch signatures cover the 2D Euler path");
   if (int st = ensure_ready(c)) return st;
   return c->fp32 ? run_signatures<float>(c, sig_i, sig_j, arg_i, arg_j)
                   : run_signatures<double>(c, sig_i, sig_j, arg_i, arg_j);
@@ -624,7 +773,7 @@ int hc_dual_time_run(hc_ctx* c, const hc_dual_time_controls* ctl, hc_dual_time_s
       (ctl->scheme != HC_BDF1 && ctl->scheme != HC_BDF2 && ctl->scheme != HC_TRAPEZIUM) ||
       (!(ctl->dt > 0.0) && !(ctl->cfl_outer > 0.0)))
     return fail(HC_ERR_ARG, "invalid dual-time controls");
-  if (c->scalar) return fail(HC_ERR_UNSUPPORTED, "dual time covers the Euler law");
+  if (c->scalar || c->oned) return fail(HC_ERR_UNSUPPORTED, "dual time covers the 2D Euler path");
   if (int st = ensure_ready(c)) return st;
   return c->fp32 ? dual_time_run<float>(c, ctl, stats) : dual_time_run<double>(c, ctl, stats);
 }

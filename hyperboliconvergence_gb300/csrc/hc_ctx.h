@@ -3,6 +3,7 @@
 #pragma once
 
 #include "hc_host.h"
+#include "hc_oned.cuh"
 
 #include <vector>
 
@@ -10,6 +11,8 @@ struct hc_ctx {
   hc_config cfg{};
   int nv = 4;           // conserved variables of the law (Euler 4, scalar advection 3)
   bool scalar = false;  // HC_LAW_SCALAR
+  bool oned = false;    // one-dimensional mesh (hc_mesh_upload_1d): ni cells, nj = 1, nv = 3
+  std::vector<double> hx;  // its node coordinates
   bool fp32 = false;
   size_t rsz = 8;
   int ni = 0, nj = 0;

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <type_traits>
+#include <vector>
 
 namespace hc {
 
@@ -21,6 +22,9 @@ template <class R, int FK> cudaError_t launch_batch_stage(const BatchArgs<R>& b,
 // recording stage (hc_sig_*.cu): one residual evaluation of the 8x32 tile writing the
 // face branch signatures to a.sig_i / a.sig_j; DF: double-float stage arithmetic
 template <class R, bool DF> cudaError_t launch_sig_stage(const StageArgs<R>& a, int flux, cudaStream_t s);
+
+// one-dimensional path (hc_oned.cu): host geometry of nc cells between nodes x[0..nc]
+void oned_geometry(const double* x, int nc, const int bc[2], std::vector<double>& rec, std::vector<double>& vol);
 
 // scalar advection law (hc_stage_scalar.cu): flux is FLUX_RUSANOV or FLUX_CENTRAL
 template <class R> cudaError_t prepare_scalar_stage();

@@ -59,6 +59,32 @@ class Mesh:
         return self.nj if side < 2 else self.ni
 
 
+class Mesh1D:
+    """One-dimensional mesh (Mesh<1,Real>, mesh/generate/oneD.h:12-35): nc cells between
+    increasing nodes x[0..nc].  A Solver on it runs the 1D Euler path with states of
+    shape (3, nc), {u, rho, p}."""
+
+    one_d = True
+
+    def __init__(self, x: np.ndarray):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        if x.ndim != 1 or x.size < 4 or np.any(np.diff(x) <= 0):
+            raise ValueError("nodes must be an increasing 1D array of at least 4 points")
+        self.nodes = x
+        self.ni, self.nj = x.size - 1, 1
+
+    @classmethod
+    def linspace(cls, nc: int, lo: float, hi: float) -> "Mesh1D":
+        """Uniform 1D mesh (make_linspace_mesh, mesh/generate/oneD.h:12-35)."""
+        return cls(lo + (hi - lo) / nc * np.arange(nc + 1))
+
+    def centres(self) -> np.ndarray:
+        return 0.5 * (self.nodes[:-1] + self.nodes[1:])
+
+    def nface(self, side: int) -> int:
+        return 1 if side < 2 else 0
+
+
 class Solver:
     """One mesh, its boundary conditions and state, advanced by explicit RK on the GPU."""
 
@@ -76,13 +102,19 @@ class Solver:
                      PRECISION[precision], DTMODE[dt], float(cfl), _capi.LAW[law], _capi.BASIS[basis])
         self.basis = basis
         self.law = law
-        self.nv = 3 if law == "scalar" else 4  # conserved variables: {u, v, q} or {u, v, rho, p}
+        self.one_d = getattr(mesh, "one_d", False)
+        # variables: {u, v, q} (scalar), {u, v, rho, p} (Euler) or {u, rho, p} (1D Euler)
+        self.nv = 3 if law == "scalar" or self.one_d else 4
+        self._shape = (self.nv, mesh.ni) if self.one_d else (self.nv, mesh.ni, mesh.nj)
         h = C.c_void_p()
         check(self.lib.hc_context_create(C.byref(cfg), C.byref(h)))
         self.h = h
         if stream is not None:
             self.set_stream(stream)
-        check(self.lib.hc_mesh_upload(self.h, mesh.ni, mesh.nj, _dptr(mesh.nodes)))
+        if self.one_d:
+            check(self.lib.hc_mesh_upload_1d(self.h, mesh.ni, _dptr(mesh.nodes)))
+        else:
+            check(self.lib.hc_mesh_upload(self.h, mesh.ni, mesh.nj, _dptr(mesh.nodes)))
         check(self.lib.hc_set_species(self.h, *[float(s) for s in species]))
         self.low_mach = None
         if low_mach is not None:
@@ -103,6 +135,8 @@ class Solver:
     def set_bcs(self, bc, ref=None) -> None:
         """Boundary types per side and their reference (ghost) states, 4 planes per side."""
         mesh = self.mesh
+        bc = list(bc) + ["periodic"] * (4 - len(bc))  # a 1D mesh has sides 0 and 1 only
+        ref = None if ref is None else list(ref) + [None] * (4 - len(ref))
         bct = (C.c_int * 4)(*[BC[b] if isinstance(b, str) else int(b) for b in bc])
         self._refs = []
         ptrs = (C.POINTER(C.c_double) * 4)()
@@ -117,7 +151,7 @@ class Solver:
                 ptrs[s] = _dptr(arr)
         check(self.lib.hc_set_bcs(self.h, bct, ptrs))
         self.bc = list(bc)
-        self.ref = [None if ref is None or ref[s] is None else
+        self.ref = [None if ref is None or ref[s] is None or mesh.nface(s) == 0 else
                     np.broadcast_to(np.asarray(ref[s], dtype=np.float64).reshape(self.nv, -1),
                                     (self.nv, mesh.nface(s))).copy()
                     for s in range(4)]
@@ -190,13 +224,13 @@ class Solver:
         default), conserved {rho u, rho v, rho, rho E} (Euler, basis="conserved"), or {u, v, q}
         (scalar advection), shape (nv, ni, nj)."""
         a = np.ascontiguousarray(prim, dtype=np.float64)
-        if a.shape != (self.nv, self.mesh.ni, self.mesh.nj):
-            raise ValueError(f"state must have shape ({self.nv}, {self.mesh.ni}, {self.mesh.nj})")
+        if a.shape != self._shape:
+            raise ValueError(f"state must have shape {self._shape}")
         check(self.lib.hc_state_upload(self.h, _dptr(a)))
 
     def get_state(self, out: np.ndarray | None = None) -> np.ndarray:
         """Download the state (into ``out`` when given: C-contiguous float64)."""
-        shape = (self.nv, self.mesh.ni, self.mesh.nj)
+        shape = self._shape
         if out is None:
             out = np.empty(shape)
         elif out.shape != shape or out.dtype != np.float64 or \
@@ -214,7 +248,7 @@ class Solver:
     # -- path ----------------------------------------------------------------
     def residual(self) -> np.ndarray:
         """Flux sums (nv conserved planes) and spectral-radius sum of the current state."""
-        out = np.empty((self.nv + 1, self.mesh.ni, self.mesh.nj))
+        out = np.empty((self.nv + 1,) + self._shape[1:])
         check(self.lib.hc_residual(self.h, _dptr(out)))
         return out
 
@@ -315,4 +349,4 @@ def branch_flips(sig_a, sig_b, cell_mask: bool = False, args=None, limiter=None,
     return out
 
 
-__all__ = ["Mesh", "Solver", "HCError", "branch_flips"]
+__all__ = ["Mesh", "Mesh1D", "Solver", "HCError", "branch_flips"]

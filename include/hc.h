@@ -131,6 +131,15 @@ int hc_get_stream(hc_ctx* ctx, void** stream);
  * geometry/surface.ipp:12-29, mesh/dual.ipp:42-83, spatial/lsqMetrics.h:119-251). */
 int hc_mesh_upload(hc_ctx* ctx, int ni, int nj, const double* nodes_xy);
 
+/* Mesh<1,Real> nodes (mesh/generate/oneD.h:12-35): the one-dimensional Euler path
+ * (interiorResidual, spatial/residualCalc.h:74-127, with the 1D boundary loops and LSQ
+ * metrics).  nc cells between increasing nodes x[0..nc]; the state is 3 planes {u, rho, p}
+ * (the nDim = 1 primitive set), the residual 3 flux planes {rho u, rho, rho E} and the
+ * spectral-radius sum; hc_set_bcs reads sides 0 (left) and 1 (right) only, ref[s] holding 3
+ * values.  Euler law, FP64 or FP32, primitive basis; every flux, limiter, RK table, dt mode
+ * and boundary type of the 2D path (no adjoint, dual time or branch signatures). */
+int hc_mesh_upload_1d(hc_ctx* ctx, int nc, const double* nodes_x);
+
 /* Species<Euler> (conservationLaws/euler/euler.h:48-60): gamma, R, minf. */
 int hc_set_species(hc_ctx* ctx, double gamma, double gas_constant, double minf);
 

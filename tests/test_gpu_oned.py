@@ -1,0 +1,139 @@
+"""The one-dimensional Euler path (hc_mesh_upload_1d) against the CPU oracle's
+restatement of the reference's 1D glue (oracle/hc_oracle_1d.hpp), on the reference's
+shock-tube driver (script/euler/shocktube.cpp: Sod, 128 cells on [0, 128], Riemann
+boundaries, Roe with the MC limiter, ssp34, CFL 0.8) and on periodic, wall, entropy
+and fixed variants.  FP64 bar: residuals within 1e-11 of the flux scale, each step
+<= 1e-12 relative L-inf per conserved variable."""
+import numpy as np
+import pytest
+
+from hyperboliconvergence_gb300.solver import Mesh1D, Solver
+from oracle import oracle_py
+
+pytestmark = pytest.mark.gpu
+
+GAMMA = 1.4
+SP = (GAMMA, 287.058, 1e-4)
+SOD_L, SOD_R = np.array([0.0, 1.0, 1.0]), np.array([0.0, 0.125, 0.1])
+
+
+def cons1(q):
+    u, r, p = q
+    return np.stack([r * u, r, p / (GAMMA - 1) + 0.5 * r * u * u])
+
+
+def rel(a, b):
+    ca, cb = cons1(a), cons1(b)
+    return float((np.abs(ca - cb).max(axis=1) / np.abs(cb).max(axis=1)).max())
+
+
+def sod(nc=128):
+    q = np.empty((3, nc))
+    q[:, : nc // 2] = SOD_L[:, None]
+    q[:, nc // 2:] = SOD_R[:, None]
+    return np.linspace(0.0, float(nc), nc + 1), ["riemann", "riemann"], [SOD_L, SOD_R], q
+
+
+def wave(nc=96, seed=4):
+    rng = np.random.default_rng(seed)
+    x = np.cumsum(np.concatenate([[0.0], rng.uniform(0.8, 1.2, nc)]))  # uneven cells
+    c = 0.5 * (x[:-1] + x[1:])
+    q = np.stack([0.3 + 0.1 * np.sin(2 * np.pi * c / x[-1]), 1.0 + 0.2 * np.sin(4 * np.pi * c / x[-1]),
+                  1.0 + 0.1 * np.cos(2 * np.pi * c / x[-1])])
+    return x, ["periodic", "periodic"], None, q
+
+
+def tube(kind, nc=80, seed=6):
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0.0, 1.0, nc + 1)
+    q = np.stack([0.2 * rng.standard_normal(nc), 1.0 + 0.1 * rng.random(nc), 1.0 + 0.1 * rng.random(nc)])
+    ref = [np.array([0.1, 1.0, 1.0]), np.array([0.05, 0.9, 0.95])]
+    return x, [kind, kind], (None if kind == "wall" else ref), q
+
+
+def pair(case, flux="roe", limiter="mc", rk="ssp34", dt="global", cfl=0.8, precision="fp64"):
+    x, bc, ref, q = case
+    gpu = Solver(Mesh1D(x), bc, ref, flux=flux, limiter=limiter, rk=rk, precision=precision, dt=dt, cfl=cfl,
+                 species=SP)
+    gpu.set_state(q)
+    ora = oracle_py.OracleSolver1D(x, bc, flux=flux, limiter=limiter, rk=rk, dt=dt, cfl=cfl, species=SP, ref=ref)
+    ora.set_state(q)
+    return gpu, ora
+
+
+CASES = {"sod": sod(), "wave": wave(), "wall": tube("wall"), "entropy": tube("entropy"), "fixed": tube("fixed")}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("flux", ["roe", "slau", "slau_ref", "ausmpup", "rusanov", "central", "roe_ws"])
+def test_oned_residual_parity_fluxes(name, flux):
+    gpu, ora = pair(CASES[name], flux=flux)
+    rg, ro = gpu.residual(), ora.residual()
+    scale = np.maximum(np.abs(ro[:3]).max(axis=1), 1e-300)
+    assert (np.abs(rg[:3] - ro[:3]).max(axis=1) / scale).max() <= 1e-11
+    assert np.abs(rg[3] - ro[3]).max() <= 1e-12 * np.abs(ro[3]).max()
+
+
+@pytest.mark.parametrize("limiter", ["nolimit1", "nolimit2", "nolimit3", "vanalbada", "minmod", "superbee", "mc",
+                                     "vanleer", "cada3"])
+def test_oned_residual_parity_limiters(limiter):
+    for name in ("sod", "wave"):
+        gpu, ora = pair(CASES[name], limiter=limiter)
+        rg, ro = gpu.residual(), ora.residual()
+        scale = np.maximum(np.abs(ro[:3]).max(axis=1), 1e-300)
+        assert (np.abs(rg[:3] - ro[:3]).max(axis=1) / scale).max() <= 1e-11, name
+
+
+@pytest.mark.parametrize("name,rk,dt", [("sod", "ssp34", "global"), ("wave", "ssp22", "local"),
+                                        ("wall", "ssp33", "global"), ("entropy", "ssp11", "local"),
+                                        ("fixed", "ssp34", "local")])
+def test_oned_step_parity(name, rk, dt):
+    gpu, ora = pair(CASES[name], rk=rk, dt=dt, cfl=0.5)
+    for _ in range(10):
+        st = gpu.step(1)
+        dto, _ = ora.step(1)
+        assert rel(gpu.get_state(), ora.get_state()) <= 1e-12
+        assert st.dt == pytest.approx(dto, rel=1e-12)
+        ora.set_state(gpu.get_state())  # each step from identical inputs
+
+
+def test_sod_shocktube_driver():
+    """The reference driver's run (480 ssp34 steps at CFL 0.8) stays physical and matches
+    the oracle run free-running."""
+    gpu, ora = pair(CASES["sod"])
+    st = gpu.step(480)
+    _, t = ora.step(480)
+    q = gpu.get_state()
+    assert st.t == pytest.approx(t, rel=1e-10)
+    assert np.all(q[1] > 0) and np.all(q[2] > 0)
+    assert rel(q, ora.get_state()) <= 1e-9
+
+
+def test_oned_periodic_and_wall_conserve():
+    for name in ("wave", "wall"):
+        x, bc, ref, q = CASES[name]
+        s = Solver(Mesh1D(x), bc, ref, flux="roe", limiter="vanleer", cfl=0.5, species=SP)
+        s.set_state(q)
+        vol = np.diff(x)
+        m0 = (cons1(q)[1] * vol).sum()
+        s.step(20)
+        assert (cons1(s.get_state())[1] * vol).sum() == pytest.approx(m0, rel=1e-13), name
+
+
+def test_oned_fp32_close():
+    gpu, ora = pair(CASES["sod"], precision="fp32")
+    gpu.step(20)
+    ora.step(20)
+    assert rel(gpu.get_state(), ora.get_state()) <= 1e-4
+
+
+def test_oned_unsupported_paths():
+    x, bc, ref, q = CASES["wave"]
+    s = Solver(Mesh1D(x), bc, ref, species=SP)
+    s.set_state(q)
+    with pytest.raises(Exception, match="2D"):
+        s.dual_time(1)
+    with pytest.raises(Exception, match="2D"):
+        s.face_signatures()
+    with pytest.raises(Exception):
+        Solver(Mesh1D(x), bc, ref, species=SP, precision="fp64_df")
