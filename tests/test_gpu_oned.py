@@ -77,9 +77,15 @@ def test_oned_residual_parity_fluxes(name, flux):
 @pytest.mark.parametrize("limiter", ["nolimit1", "nolimit2", "nolimit3", "vanalbada", "minmod", "superbee", "mc",
                                      "vanleer", "cada3"])
 def test_oned_residual_parity_limiters(limiter):
+    """Unlimited reconstruction across Sod's discontinuity extrapolates to negative
+    pressures, so the face states there are non-finite: parity then means non-finite at
+    the same cells and agreement elsewhere."""
     for name in ("sod", "wave"):
         gpu, ora = pair(CASES[name], limiter=limiter)
         rg, ro = gpu.residual(), ora.residual()
+        bad_g, bad_o = ~np.isfinite(rg), ~np.isfinite(ro)
+        assert np.array_equal(bad_g, bad_o), name
+        rg, ro = np.where(bad_o, 0.0, rg), np.where(bad_o, 0.0, ro)
         scale = np.maximum(np.abs(ro[:3]).max(axis=1), 1e-300)
         assert (np.abs(rg[:3] - ro[:3]).max(axis=1) / scale).max() <= 1e-11, name
 
