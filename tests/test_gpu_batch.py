@@ -64,6 +64,23 @@ def test_batch_fp64_matches_oracle():
         assert err <= 1e-12, (k, err)
 
 
+def test_batch_fp64_matches_oracle_over_200_steps():
+    """The batched configuration's 200 steps (SLAU + van Albada, ssp34, CFL 0.5, global dt)
+    on a small four-quadrant instance, FP64 batch against the oracle free-running."""
+    insts = uneven_riemann_batch(2, 2026, sizes=(24, 40))
+    bt = Batch(insts, flux="slau", limiter="vanalbada", precision="fp64")
+    bt.step_async(200)
+    bt.sync()
+    for k, (mesh, bc, ref, q) in enumerate(insts):
+        o = oracle_py.OracleSolver(mesh.ni, mesh.nj, mesh.nodes.ravel(), bc, flux="slau", limiter="vanalbada",
+                                   species=(1.4, 287.058, 0.5), ghost_ref=ref)
+        o.set_state(q)
+        o.step(200)
+        a, b = bt.get_state(k), o.get_state()
+        err = (np.abs(a - b).reshape(4, -1).max(1) / np.abs(b).reshape(4, -1).max(1)).max()
+        assert err <= 1e-9, (k, err)
+
+
 def test_graph_replay_equals_stream_steps():
     insts = small_batch(seed=8, n=4)
     a = Batch(insts, precision="fp32")
