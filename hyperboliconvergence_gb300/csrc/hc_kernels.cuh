@@ -296,8 +296,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
               gl[v] = (M(2 * v, la_l, lb_l) * wlx + M(2 * v + 1, la_l, lb_l) * wly) - dq * sl;
               gr[v] = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
             }
-            limit4<C>(lim, gc, gl, sL);
-            limit4<C>(lim, gc, gr, sR);
+            limit4(lim, gc, gl, sL);
+            limit4(lim, gc, gr, sR);
             if constexpr (REC) {
               double* ag = a.arg_i ? (idir ? a.arg_i + size_t(16) * fidx : a.arg_j + size_t(16) * fidx) : nullptr;
 #pragma unroll
@@ -336,19 +336,25 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
             }
           }
           if constexpr (REC) {
-            const St<C> sL = basis_state(g, qL, cons), sR = basis_state(g, qR, cons);
+            St<C> sL, sR;
+            basis_state2(g, qL, qR, cons, sL, sR);
             F = face_flux<C, FK>(g, nx, ny, A, sL, sR);
             sg |= (unsigned long long)flux_bits<C, FK>(g, nx, ny, sL, sR) << SIG_FLUX_SHIFT;
           } else {
-            F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, qL, cons), basis_state(g, qR, cons));
+            St<C> sL, sR;
+            basis_state2(g, qL, qR, cons, sL, sR);
+            F = face_flux<C, FK>(g, nx, ny, A, sL, sR);
           }
         } else {
           if constexpr (REC) {
-            const St<C> sL = basis_state(g, ql, cons), sR = basis_state(g, qr, cons);
+            St<C> sL, sR;
+            basis_state2(g, ql, qr, cons, sL, sR);
             F = face_flux<C, FK>(g, nx, ny, A, sL, sR);
             sg |= (unsigned long long)flux_bits<C, FK>(g, nx, ny, sL, sR) << SIG_FLUX_SHIFT;
           } else {
-            F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, ql, cons), basis_state(g, qr, cons));
+            St<C> sL, sR;
+            basis_state2(g, ql, qr, cons, sL, sR);
+            F = face_flux<C, FK>(g, nx, ny, A, sL, sR);
           }
         }
       } else {
@@ -412,11 +418,14 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
             for (int v = 0; v < 4; ++v) { qL[v] = int_right ? qg[v] : qi[v]; qR[v] = int_right ? qi[v] : qg[v]; }
           }
           if constexpr (REC) {
-            const St<C> sL = basis_state(g, qL, cons), sR = basis_state(g, qR, cons);
+            St<C> sL, sR;
+            basis_state2(g, qL, qR, cons, sL, sR);
             F = face_flux<C, FK>(g, nx, ny, A, sL, sR);
             sg |= (unsigned long long)flux_bits<C, FK>(g, nx, ny, sL, sR) << SIG_FLUX_SHIFT;
           } else {
-            F = face_flux<C, FK>(g, nx, ny, A, basis_state(g, qL, cons), basis_state(g, qR, cons));
+            St<C> sL, sR;
+            basis_state2(g, qL, qR, cons, sL, sR);
+            F = face_flux<C, FK>(g, nx, ny, A, sL, sR);
           }
         }
       }

@@ -10,6 +10,8 @@
 
 #include <cuda_runtime.h>
 #include <cfloat>
+#include <cstring>
+#include <type_traits>
 
 #include "hc_df64.cuh"
 
@@ -76,25 +78,29 @@ template <class R> struct St { R p, r, h, u2, a2, u, v, ir; };  // ir = 1/r
 template <class R> struct Flux5 { R f[4]; R lam; };
 
 // set2State(primitive) (conservationLaws/euler/transforms/primitive.ipp:101-137)
-template <class R> __host__ __device__ __forceinline__ St<R> prim_state(const Gas<R>& g, R u, R v, R r, R p) {
+// (ir = 1/r given)
+template <class R>
+__host__ __device__ __forceinline__ St<R> prim_state_ir(const Gas<R>& g, R u, R v, R r, R p, R ir) {
   St<R> s;
   s.u = u; s.v = v;
   s.u2 = u * u;
   s.u2 += v * v;
   const R k = R(0.5) * s.u2;
   // a2 = gamma R T with T = p/(r R): gamma p / r, through 1/r (kept for the flux)
-  s.ir = R(1) / r;
+  s.ir = ir;
   s.a2 = g.gamma * (p * s.ir);
   s.h = s.a2 * g.gamma1 + k;
   s.p = p; s.r = r;
   return s;
 }
+template <class R> __host__ __device__ __forceinline__ St<R> prim_state(const Gas<R>& g, R u, R v, R r, R p) {
+  return prim_state_ir(g, u, v, r, p, R(1) / r);
+}
 
 // set2State(conserved) (conservationLaws/euler/transforms/conserved.ipp:31-76)
-template <class R> __host__ __device__ __forceinline__ St<R> cons_state(const Gas<R>& g, const R* qc) {
+template <class R> __host__ __device__ __forceinline__ St<R> cons_state_ir(const Gas<R>& g, const R* qc, R r1) {
   St<R> s;
   const R r = qc[2], re = qc[3];
-  const R r1 = R(1) / r;
   s.u = qc[0] * r1; s.v = qc[1] * r1;
   s.u2 = s.u * s.u;
   s.u2 += s.v * s.v;
@@ -109,8 +115,74 @@ template <class R> __host__ __device__ __forceinline__ St<R> cons_state(const Ga
 
 // set2State of the solution basis: primitive {u, v, rho, p} or conserved
 // {rho u, rho v, rho, rho E} (cons = true); the choice is uniform across a launch
+template <class R> __host__ __device__ __forceinline__ St<R> cons_state(const Gas<R>& g, const R* qc) {
+  return cons_state_ir(g, qc, R(1) / qc[2]);
+}
+
 template <class R> __host__ __device__ __forceinline__ St<R> basis_state(const Gas<R>& g, const R* q, bool cons) {
   return cons ? cons_state(g, q) : prim_state(g, q[0], q[1], q[2], q[3]);
+}
+
+// Bits of an FP64 value, for sign and range tests on the integer pipe (the FP64 pipe
+// bounds the FP64 stage kernels).
+__host__ __device__ __forceinline__ long long f64_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(x);
+#else
+  long long b;
+  memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+// biased exponent of x >= 0 within [1023 - e, 1023 + e] (false for negative, zero,
+// subnormal, infinite and NaN x beyond that window)
+__host__ __device__ __forceinline__ bool f64_exp_within(double x, unsigned e) {
+  const unsigned be = unsigned((unsigned long long)f64_bits(x) >> 52);  // sign bit included
+  return be - (1023u - e) <= 2u * e;
+}
+
+// s = sqrt(x) and r = 1/s.  FP64 on the device: r = rsqrt(x) (within 1 ulp), s = x r,
+// one multi-instruction sequence instead of two; otherwise sqrt and a division.
+template <class R> __host__ __device__ __forceinline__ void sqrt_rcp(R x, R& s, R& r) {
+#ifdef __CUDA_ARCH__
+  if constexpr (std::is_same<R, double>::value) {
+    r = rsqrt(x);
+    s = x * r;
+    return;
+  }
+#endif
+  s = sqrt(x);
+  r = R(1) / s;
+}
+
+// set2State of the two states of one face.  FP64: both densities' inverses from one
+// division, 1/(rL rR) times the other density, when both densities lie in
+// [2^-500, 2^500] (the product stays normal); otherwise, and for the other types, one
+// division each.
+template <class R>
+__host__ __device__ __forceinline__ void basis_state2(const Gas<R>& g, const R* ql, const R* qr, bool cons, St<R>& sl,
+                                                      St<R>& sr) {
+  R il, ir;
+  if constexpr (std::is_same<R, double>::value) {
+    if (f64_exp_within(ql[2], 500u) && f64_exp_within(qr[2], 500u)) {
+      const double inv = 1.0 / (ql[2] * qr[2]);
+      il = inv * qr[2];
+      ir = inv * ql[2];
+    } else {
+      il = 1.0 / ql[2];
+      ir = 1.0 / qr[2];
+    }
+  } else {
+    il = R(1) / ql[2];
+    ir = R(1) / qr[2];
+  }
+  if (cons) {
+    sl = cons_state_ir(g, ql, il);
+    sr = cons_state_ir(g, qr, ir);
+  } else {
+    sl = prim_state_ir(g, ql[0], ql[1], ql[2], ql[3], il);
+    sr = prim_state_ir(g, qr[0], qr[1], qr[2], qr[3], ir);
+  }
 }
 
 // state2Set<conserved> (conservationLaws/euler/transforms/conserved.ipp:2-29)
@@ -143,8 +215,9 @@ __host__ __device__ __forceinline__ Flux5<R> central_flux_a(R nx, R ny, R A, con
                                                             R ar) {
   const Flux5<R> fl = exact_flux_a(nx, ny, l, al), fr = exact_flux_a(nx, ny, r, ar);
   Flux5<R> o;
+  const R hA = R(0.5) * A;  // (0.5 s) A == s (0.5 A) in binary arithmetic, one product fewer per component
 #pragma unroll
-  for (int i = 0; i < 4; ++i) o.f[i] = (R(0.5) * (fl.f[i] + fr.f[i])) * A;
+  for (int i = 0; i < 4; ++i) o.f[i] = (fl.f[i] + fr.f[i]) * hA;
   o.lam = fmax(fl.lam, fr.lam) * A;
   return o;
 }
@@ -173,7 +246,10 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const G
   ka *= R(0.5);
   const R ha = wl * l.h + wr * r.h;
   const R a2a = g.gm1 * (ha - ka);
-  const R aa = sqrt(a2a);
+  // the averaged sound speed and its inverse: FP64 from one reciprocal square root
+  R aa, a1;
+  if constexpr (std::is_same<R, double>::value) sqrt_rcp(a2a, aa, a1);
+  else aa = sqrt(a2a);
   // wave speeds and entropy fix
   const R una = nx * ua + ny * va;
   const R unl = proj(nx, ny, l), unr = proj(nx, ny, r);
@@ -209,7 +285,7 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const G
   cc -= va * c1;
   const R dp = cc * g.gm1;
   // primitive -> characteristic, scaled by the wave speeds
-  const R a1 = R(1) / aa;
+  if constexpr (!std::is_same<R, double>::value) a1 = R(1) / aa;
   const R w0 = lam[0] * ((g.gamma * (dp * a1 * a1 - d2)) * rho1);
   const R w1 = lam[1] * (du0 - dp * rho1 * a1);
   const R w2 = lam[2] * (du0 + dp * rho1 * a1);
@@ -411,33 +487,38 @@ __host__ __device__ __forceinline__ Flux5<R> face_flux(const Gas<R>& g, R nx, R 
 
 template <class R> __host__ __device__ __forceinline__ R limit(int kind, R a, R b);
 
-// The limiter of the four variables of one face side, limit(a[v], b[v]).  van
-// Albada's four quotients share one division (batched inversion: 1/d_v from the
-// inverse of the product of the denominators and the partial products), when that
-// product and its partial products stay within [1e-280, 1e280]; otherwise, and for
-// the other limiters, one call per variable.
-template <class R> __host__ __device__ __forceinline__ void limit4(int kind, const R* a, const R* b, R* out) {
+// The limiter of the four variables of one face side, limit(a[v], b[v]), FP64.  van
+// Albada's slope a b (a + b) / (a^2 + b^2) (0 exactly where a b <= 0) takes its four
+// quotients from one division (batched inversion: 1/d_v from the inverse of the
+// product of the denominators and the partial products) when every denominator lies
+// in [2^-240, 2^240], so that all products stay normal and finite; otherwise one
+// division per variable, with the reference's tiny added to the denominator.  The
+// sign and range tests read the bits on the integer pipe.  The other limiters: one
+// call per variable.
+__host__ __device__ __forceinline__ void limit4(int kind, const double* a, const double* b, double* out) {
   if (kind == LIM_VANALBADA) {
-    const R tiny = Lim<R>::tiny();
-    R num[4], den[4], pre[4];
-    R acc = R(1);
+    double num[4], den[4], pre[4];
+    double acc = 1.0;
     bool ok = true, any = false;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const bool on = !(a[v] * b[v] <= R(0));  // a*b <= 0: the limited slope is 0 exactly
-      // explicit contractions: the same rounding in every kernel that inlines this
-      num[v] = on ? fma(b[v], a[v] * a[v], a[v] * (b[v] * b[v])) : R(0);
-      den[v] = on ? fma(a[v], a[v], b[v] * b[v]) + tiny : R(1);
+      const double ab = a[v] * b[v];
+      const long long bits = f64_bits(ab);
+      // a b > 0, or NaN (which propagates)
+      const bool on = bits > 0 || (bits & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+      // explicit contraction: the same rounding in every kernel that inlines this
+      num[v] = on ? ab * (a[v] + b[v]) : 0.0;
+      den[v] = on ? fma(a[v], a[v], b[v] * b[v]) : 1.0;
       any = any || on;
       pre[v] = acc;
       acc = acc * den[v];
-      ok = ok && acc >= R(1e-280) && acc <= R(1e280);
+      ok = ok && f64_exp_within(den[v], 240u);
     }
     if (!any) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) out[v] = R(0);
+      for (int v = 0; v < 4; ++v) out[v] = 0.0;
     } else if (ok) {
-      R inv = R(1) / acc;
+      double inv = 1.0 / acc;
 #pragma unroll
       for (int v = 3; v >= 0; --v) {
         out[v] = num[v] * (inv * pre[v]);
@@ -445,12 +526,12 @@ template <class R> __host__ __device__ __forceinline__ void limit4(int kind, con
       }
     } else {
 #pragma unroll
-      for (int v = 0; v < 4; ++v) out[v] = num[v] / den[v];
+      for (int v = 0; v < 4; ++v) out[v] = num[v] / (den[v] + Lim<double>::tiny());
     }
     return;
   }
 #pragma unroll
-  for (int v = 0; v < 4; ++v) out[v] = limit<R>(kind, a[v], b[v]);
+  for (int v = 0; v < 4; ++v) out[v] = limit<double>(kind, a[v], b[v]);
 }
 
 // Slope limiters (limiters/limiter.ipp:141-297), called as limit(central, biased).
