@@ -59,6 +59,7 @@ def _declare(lib):
         "hc_mesh_upload_1d": [p, i, dp],
         "hc_set_species": [p, d, d, d],
         "hc_set_low_mach": [p, i, i, d, d],
+        "hc_set_tile": [p, i],
         "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],
         "hc_state_upload": [p, dp],
         "hc_state_download": [p, dp],

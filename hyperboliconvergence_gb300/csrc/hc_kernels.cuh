@@ -296,8 +296,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
               gl[v] = (M(2 * v, la_l, lb_l) * wlx + M(2 * v + 1, la_l, lb_l) * wly) - dq * sl;
               gr[v] = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
             }
-            limit4(lim, gc, gl, sL);
-            limit4(lim, gc, gr, sR);
+            limit4x2(lim, gc, gl, gr, sL, sR);
             if constexpr (REC) {
               double* ag = a.arg_i ? (idir ? a.arg_i + size_t(16) * fidx : a.arg_j + size_t(16) * fidx) : nullptr;
 #pragma unroll

@@ -209,16 +209,25 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> exact_flux(R nx,
   return exact_flux_a(nx, ny, s, sqrt(s.a2));
 }
 
-// CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:25-37), sound speeds given
+// CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:25-37), sound speeds given;
+// lam left unscaled by A (the caller's max of unscaled speeds times A equals the max of
+// the scaled speeds: rounding is monotone)
 template <class R>
-__host__ __device__ __forceinline__ Flux5<R> central_flux_a(R nx, R ny, R A, const St<R>& l, const St<R>& r, R al,
+__host__ __device__ __forceinline__ Flux5<R> central_flux_u(R nx, R ny, R A, const St<R>& l, const St<R>& r, R al,
                                                             R ar) {
   const Flux5<R> fl = exact_flux_a(nx, ny, l, al), fr = exact_flux_a(nx, ny, r, ar);
   Flux5<R> o;
   const R hA = R(0.5) * A;  // (0.5 s) A == s (0.5 A) in binary arithmetic, one product fewer per component
 #pragma unroll
   for (int i = 0; i < 4; ++i) o.f[i] = (fl.f[i] + fr.f[i]) * hA;
-  o.lam = fmax(fl.lam, fr.lam) * A;
+  o.lam = fmax(fl.lam, fr.lam);
+  return o;
+}
+template <class R>
+__host__ __device__ __forceinline__ Flux5<R> central_flux_a(R nx, R ny, R A, const St<R>& l, const St<R>& r, R al,
+                                                            R ar) {
+  Flux5<R> o = central_flux_u(nx, ny, A, l, r, al, ar);
+  o.lam *= A;
   return o;
 }
 template <class R> __host__ __device__ __forceinline__ Flux5<R> central_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
@@ -233,7 +242,7 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> central_flux(R n
 template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g, R nx, R ny, R A,
                                                                const St<R>& l, const St<R>& r) {
   const R al = sqrt(l.a2), ar = sqrt(r.a2);
-  const Flux5<R> c = central_flux_a(nx, ny, A, l, r, al, ar);
+  const Flux5<R> c = central_flux_u(nx, ny, A, l, r, al, ar);
   // roe average: cr = sqrt(rR/rL), ra = cr rL, 1/ra = cr/rR
   const R cr = sqrt(r.r * l.ir);
   const R wl = R(1) / (R(1) + cr);
@@ -309,7 +318,7 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const G
   o.f[1] = c.f[1] + s * f1;
   o.f[2] = c.f[2] + s * drr;
   o.f[3] = c.f[3] + s * e3;
-  o.lam = fmax(c.lam, (fabs(una) + aa) * A);
+  o.lam = fmax(c.lam, fabs(una) + aa) * A;
   return o;
 }
 
@@ -437,7 +446,7 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> ausmpup_flux(con
 template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_ws_flux(const Gas<R>& g, R nx, R ny, R A,
                                                                   const St<R>& l, const St<R>& r) {
   const R al = sqrt(l.a2), ar = sqrt(r.a2);
-  const Flux5<R> c = central_flux_a(nx, ny, A, l, r, al, ar);
+  const Flux5<R> c = central_flux_u(nx, ny, A, l, r, al, ar);
   // roe average (conservationLaws/euler/fluxes/roe.ipp:150-196)
   const R cr = sqrt(r.r * l.ir);
   const R wl = R(1) / (R(1) + cr);
@@ -470,7 +479,7 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_ws_flux(cons
   o.f[1] = c.f[1] - s * ((aun * d1 + dU * (ra * va)) + dP * ny);
   o.f[2] = c.f[2] - s * (aun * d2 + dU * ra);
   o.f[3] = c.f[3] - s * ((aun * d3 + dU * (ra * ha)) + dP * una);
-  o.lam = fmax(c.lam, (aun + aa) * A);
+  o.lam = fmax(c.lam, aun + aa) * A;
   return o;
 }
 
@@ -487,51 +496,64 @@ __host__ __device__ __forceinline__ Flux5<R> face_flux(const Gas<R>& g, R nx, R 
 
 template <class R> __host__ __device__ __forceinline__ R limit(int kind, R a, R b);
 
-// The limiter of the four variables of one face side, limit(a[v], b[v]), FP64.  van
-// Albada's slope a b (a + b) / (a^2 + b^2) (0 exactly where a b <= 0) takes its four
-// quotients from one division (batched inversion: 1/d_v from the inverse of the
-// product of the denominators and the partial products) when every denominator lies
-// in [2^-240, 2^240], so that all products stay normal and finite; otherwise one
-// division per variable, with the reference's tiny added to the denominator.  The
-// sign and range tests read the bits on the integer pipe.  The other limiters: one
-// call per variable.
-__host__ __device__ __forceinline__ void limit4(int kind, const double* a, const double* b, double* out) {
+// van Albada's slopes a b (a + b) / (a^2 + b^2) of the four variables of one face side
+// (0 exactly where a b <= 0), a2 = a^2 given, FP64.  The four quotients come from one
+// division (batched inversion: 1/d_v from the inverse of the product of the
+// denominators and the partial products) when every denominator lies in
+// [2^-240, 2^240], so that all products stay normal and finite; otherwise one division
+// per variable, with the reference's tiny added to the denominator.  The sign and range
+// tests read the bits on the integer pipe.
+__host__ __device__ __forceinline__ void vanalbada4(const double* a, const double* a2, const double* b, double* out) {
+  double num[4], den[4], pre[4];
+  double acc = 1.0;
+  bool ok = true, any = false;
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const double ab = a[v] * b[v];
+    const long long bits = f64_bits(ab);
+    // a b > 0, or NaN (which propagates)
+    const bool on = bits > 0 || (bits & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+    // explicit contraction: the same rounding in every kernel that inlines this
+    num[v] = on ? ab * (a[v] + b[v]) : 0.0;
+    den[v] = on ? fma(b[v], b[v], a2[v]) : 1.0;
+    any = any || on;
+    pre[v] = acc;
+    acc = acc * den[v];
+    ok = ok && f64_exp_within(den[v], 240u);
+  }
+  if (!any) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[v] = 0.0;
+  } else if (ok) {
+    double inv = 1.0 / acc;
+#pragma unroll
+    for (int v = 3; v >= 0; --v) {
+      out[v] = num[v] * (inv * pre[v]);
+      inv = inv * den[v];
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[v] = num[v] / (den[v] + Lim<double>::tiny());
+  }
+}
+
+// The limited slopes of both sides of one face, FP64: outl[v] = limit(a[v], bl[v]),
+// outr[v] = limit(a[v], br[v]) (the central slope a is common to both sides).
+__host__ __device__ __forceinline__ void limit4x2(int kind, const double* a, const double* bl, const double* br,
+                                                  double* outl, double* outr) {
   if (kind == LIM_VANALBADA) {
-    double num[4], den[4], pre[4];
-    double acc = 1.0;
-    bool ok = true, any = false;
+    double a2[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const double ab = a[v] * b[v];
-      const long long bits = f64_bits(ab);
-      // a b > 0, or NaN (which propagates)
-      const bool on = bits > 0 || (bits & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
-      // explicit contraction: the same rounding in every kernel that inlines this
-      num[v] = on ? ab * (a[v] + b[v]) : 0.0;
-      den[v] = on ? fma(a[v], a[v], b[v] * b[v]) : 1.0;
-      any = any || on;
-      pre[v] = acc;
-      acc = acc * den[v];
-      ok = ok && f64_exp_within(den[v], 240u);
-    }
-    if (!any) {
-#pragma unroll
-      for (int v = 0; v < 4; ++v) out[v] = 0.0;
-    } else if (ok) {
-      double inv = 1.0 / acc;
-#pragma unroll
-      for (int v = 3; v >= 0; --v) {
-        out[v] = num[v] * (inv * pre[v]);
-        inv = inv * den[v];
-      }
-    } else {
-#pragma unroll
-      for (int v = 0; v < 4; ++v) out[v] = num[v] / (den[v] + Lim<double>::tiny());
-    }
+    for (int v = 0; v < 4; ++v) a2[v] = a[v] * a[v];
+    vanalbada4(a, a2, bl, outl);
+    vanalbada4(a, a2, br, outr);
     return;
   }
 #pragma unroll
-  for (int v = 0; v < 4; ++v) out[v] = limit<double>(kind, a[v], b[v]);
+  for (int v = 0; v < 4; ++v) {
+    outl[v] = limit<double>(kind, a[v], bl[v]);
+    outr[v] = limit<double>(kind, a[v], br[v]);
+  }
 }
 
 // Slope limiters (limiters/limiter.ipp:141-297), called as limit(central, biased).

@@ -90,7 +90,7 @@ class Solver:
 
     def __init__(self, mesh: Mesh, bc, ref=None, flux="roe", limiter="vanleer", rk="ssp34",
                  precision="fp64", dt="global", cfl=0.5, species=(1.4, 287.058, 1e-4), stream=None, law="euler",
-                 low_mach=None, basis="primitive"):
+                 low_mach=None, basis="primitive", tile=None):
         self.lib = _capi.load()
         self.mesh = mesh
         self.precision = precision
@@ -116,11 +116,18 @@ class Solver:
         else:
             check(self.lib.hc_mesh_upload(self.h, mesh.ni, mesh.nj, _dptr(mesh.nodes)))
         check(self.lib.hc_set_species(self.h, *[float(s) for s in species]))
+        if tile is not None:
+            self.set_tile(tile)
         self.low_mach = None
         if low_mach is not None:
             self.set_low_mach(*low_mach)
         self.bc = list(bc)
         self.set_bcs(bc, ref)
+
+    def set_tile(self, tile: str) -> None:
+        """Cells per CTA tile of the 2D FP64/FP32 stage kernels: "8x32", "4x32" or "16x16"
+        (the results do not depend on it)."""
+        check(self.lib.hc_set_tile(self.h, _capi.TILE[tile]))
 
     def set_low_mach(self, velocity="convective", pressure="convective", lref=1.0,
                      dt=np.finfo(np.float64).max) -> None:

@@ -339,6 +339,12 @@ typedef struct {
   float ms_per_step;/* measured by hc_batch_autotune (0 when not measured) */
 } hc_schedule;
 
+/* Tile shape (hc_tile) of a single-mesh context's stage kernels: the FP64 and FP32
+ * 2D stage, residual and adjoint-recompute launches (the double-float and 1D kernels
+ * keep their own).  Defaults: HC_TILE_16x16 in FP64 (whose 544 faces fill 17 warps of
+ * the FP64-bound face phase), HC_TILE_8x32 in FP32.  Every shape gives the same results. */
+int hc_set_tile(hc_ctx* ctx, int tile);
+
 /* ninst meshes; nodes[k] as for hc_mesh_upload; bc[4k..4k+3] and ref[4k..4k+3]
  * as for hc_set_bcs (ref entries may be NULL where hc_set_bcs allows it). */
 int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* nj, const double* const* nodes,
