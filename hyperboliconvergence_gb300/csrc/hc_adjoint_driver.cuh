@@ -8,15 +8,17 @@
 // timesteps.
 //
 // Objectives: time-averaged wall force (drag) over steps 1..N, or a weighted
-// L2 distance of the final state to a target.  Supported: Euler law; HC_FP64,
-// HC_FP64_DF and HC_FP32 contexts; Roe or Rusanov flux; limiters NoLimit1/2/3,
-// van Albada, MinMod, van Leer; periodic / fixed / inviscid-wall boundaries;
-// global timestep.  hc_adjoint.cu instantiates R = double and the C ABI,
+// L2 distance of the final state to a target.  Supported: Euler law (HC_FP64,
+// HC_FP64_DF and HC_FP32 contexts; Roe or Rusanov flux; periodic / fixed /
+// inviscid-wall boundaries) and the scalar advection law (HC_FP64 and HC_FP32;
+// Rusanov or central flux; periodic / fixed boundaries; the L2 objective); limiters
+// NoLimit1/2/3, van Albada, MinMod, van Leer; global timestep.  hc_adjoint.cu instantiates R = double and the C ABI,
 // hc_adjoint_f32.cu R = float.
 #pragma once
 
 #include "hc_adjoint_kernels.cuh"
 #include "hc_ctx.h"
+#include "hc_scalar.cuh"
 
 #include <cfloat>
 #include <cstring>
@@ -78,8 +80,9 @@ template <class R> struct Adj : AdjCommon {
   std::vector<double> hrates;
   hc_objective obj{};
   int nsteps = 0;
+  int nv = 4;  // state variables: 4 Euler, 3 scalar advection
   long long fwd_steps = 0, adj_steps = 0, launches = 0;
-  size_t state_values() const { return 4 * n; }  // one stored state
+  size_t state_values() const { return size_t(nv) * n; }  // one stored state
   cudaStream_t s() const { return c->stream; }
 };
 
@@ -105,7 +108,10 @@ inline unsigned face_blocks(size_t n) { return unsigned((n + kFaceThreads - 1) /
 // one forward step from sq[0] to sq[nst]; record (rec=true) or replay the max rate of step `step`
 template <class R> int forward_step(Adj<R>& A, int step, bool rec) {
   hc_ctx* c = A.c;
-  const StageFn<R> fn = stage_fn<R>(c->cfg.flux);
+  const StageFn<R> euler_fn = stage_fn<R>(c->cfg.flux);
+  auto fn = [c, euler_fn](const StageArgs<R>& a, int tile, cudaStream_t st) -> cudaError_t {
+    return c->scalar ? launch_scalar_stage<R>(a, c->cfg.flux, tile, st) : euler_fn(a, tile, st);
+  };
   for (int s = 0; s < A.nst; ++s) {
     StageArgs<R> a = base_args<R>(c);
     a.q = A.sq[s];
@@ -128,9 +134,14 @@ template <class R> int forward_step(Adj<R>& A, int step, bool rec) {
         a.mode = MODE_RESIDUAL;
         HC_CUDA(fn(a, c->tile, A.s()));
       }
-      update0_kernel<R><<<std::min<unsigned>(blocks(A.n), 152 * 16), 256, 0, A.s()>>>(
-          c->ni, c->nj, a.gas, A.sq[0], (const R*)c->res[0], (const R*)c->vol, R(A.tab.alpha[0][0]),
-          R(A.tab.beta[0]), c->cfg.cfl, c->info, A.sq[1], 0, c->cfg.basis, 0.0);
+      if (c->scalar)
+        scalar_update0_kernel<R><<<std::min<unsigned>(blocks(A.n), 152 * 16), 256, 0, A.s()>>>(
+            c->ni, c->nj, A.sq[0], (const R*)c->res[0], (const R*)c->vol, R(A.tab.alpha[0][0]), R(A.tab.beta[0]),
+            c->cfg.cfl, c->info, A.sq[1], 0);
+      else
+        update0_kernel<R><<<std::min<unsigned>(blocks(A.n), 152 * 16), 256, 0, A.s()>>>(
+            c->ni, c->nj, a.gas, A.sq[0], (const R*)c->res[0], (const R*)c->vol, R(A.tab.alpha[0][0]),
+            R(A.tab.beta[0]), c->cfg.cfl, c->info, A.sq[1], 0, c->cfg.basis, 0.0);
       HC_CUDA(cudaGetLastError());
       A.launches += 2;
     } else {
@@ -188,11 +199,11 @@ template <class R> int add_drag(Adj<R>& A, const R* q, double scale) {
 // gradient 2 w_v (q - t) into lam
 template <class R>
 __device__ __forceinline__ void l2_cell(const R* q, const R* t, size_t n, double w0, double w1, double w2, double w3,
-                                        R* part, int mode_grad, R* lam, size_t c) {
+                                        R* part, int mode_grad, R* lam, size_t c, int nv = 4) {
   if (c >= n) return;
   const double w[4] = {w0, w1, w2, w3};
   double s = 0;
-  for (int v = 0; v < 4; ++v) {
+  for (int v = 0; v < nv; ++v) {
     const double d = double(q[v * n + c]) - double(t[v * n + c]);
     s += w[v] * d * d;
     if (mode_grad) lam[v * n + c] = R(2.0 * w[v] * d);
@@ -201,8 +212,8 @@ __device__ __forceinline__ void l2_cell(const R* q, const R* t, size_t n, double
 }
 template <class R>
 __global__ void l2_kernel(const R* q, const R* t, size_t n, double w0, double w1, double w2, double w3, R* part,
-                          int mode_grad, R* lam) {
-  l2_cell(q, t, n, w0, w1, w2, w3, part, mode_grad, lam, blockIdx.x * size_t(blockDim.x) + threadIdx.x);
+                          int mode_grad, R* lam, int nv = 4) {
+  l2_cell(q, t, n, w0, w1, w2, w3, part, mode_grad, lam, blockIdx.x * size_t(blockDim.x) + threadIdx.x, nv);
 }
 
 // residual adjoint: qbar_out = (dRes/dq at q)^T rbar (+ qbar_add); objective mode
@@ -219,8 +230,22 @@ int residual_adjoint(Adj<R>& A, const R* q, const R* rbar, const R* qbar_add, R*
   a.obj_scale = R(obj_scale);
   a.obj_dirx = R(A.obj.dir[0]);
   a.obj_diry = R(A.obj.dir[1]);
+  if (A.c->scalar) {
+    if constexpr (FK == FLUX_RUSANOV || FK == FLUX_CENTRAL) {
+      adj_qm_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
+      adj_face_scalar_kernel<R, FK><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
+      adj_face_scalar_kernel<R, FK><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+      adj_qmbar_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(a);
+      adj_gather_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(a);
+      A.launches += 5;
+      HC_CUDA(cudaGetLastError());
+    }
+    return HC_OK;
+  }
+  if constexpr (FK == FLUX_CENTRAL) return fail(HC_ERR_UNSUPPORTED, "the Euler adjoint has no central flux");
   adj_qm_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
-  if constexpr (std::is_same<R, double>::value) {
+  if constexpr (FK == FLUX_CENTRAL) {
+  } else if constexpr (std::is_same<R, double>::value) {
     if (A.c->df) {  // double-float face arithmetic on HC_FP64_DF contexts
       adj_face_kernel<double, FK, df64><<<face_blocks(A.nfi), kFaceThreads, 0, A.s()>>>(a, 0);
       adj_face_kernel<double, FK, df64><<<face_blocks(A.nfj), kFaceThreads, 0, A.s()>>>(a, 1);
@@ -240,6 +265,8 @@ int residual_adjoint(Adj<R>& A, const R* q, const R* rbar, const R* qbar_add, R*
 }
 
 template <class R> int res_adj(Adj<R>& A, const R* q, const R* rbar, const R* add, R* out, bool obj, double sc) {
+  if (A.c->scalar && A.c->cfg.flux == HC_FLUX_CENTRAL)
+    return residual_adjoint<R, FLUX_CENTRAL>(A, q, rbar, add, out, obj, sc);
   if (A.c->cfg.flux == HC_FLUX_ROE) return residual_adjoint<R, FLUX_ROE>(A, q, rbar, add, out, obj, sc);
   return residual_adjoint<R, FLUX_RUSANOV>(A, q, rbar, add, out, obj, sc);
 }
@@ -253,7 +280,7 @@ template <class R> double step_dt(const Adj<R>& A, int step) {
 // the adjoint of q_step (objective terms of q_step included).
 template <class R> int adjoint_step(Adj<R>& A, int step) {
   if (int st = forward_step(A, step, false)) return st;
-  const size_t bytes4 = 4 * A.n * sizeof(R);
+  const size_t bytes4 = A.state_values() * sizeof(R);
   for (int k = 0; k < A.nst; ++k) HC_CUDA(cudaMemsetAsync(A.rbar[k], 0, bytes4, A.s()));
   HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
   const double dt = step_dt(A, step);
@@ -262,9 +289,14 @@ template <class R> int adjoint_step(Adj<R>& A, int step) {
     const R* qbar_out = (s == A.nst - 1) ? A.lam : A.qbs;
     R al[4] = {R(0), R(0), R(0), R(0)};
     for (int k = 0; k <= s; ++k) al[k] = R(A.tab.alpha[s][k]);
-    adj_update_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(
-        int(A.n), g, A.sq[s + 1], A.sq[0], (const R*)A.c->vol, qbar_out, A.q0bar, A.rbar[0], A.rbar[1],
-        A.rbar[2], A.rbar[3], al[0], al[1], al[2], al[3], s, R(A.tab.beta[s] * dt));
+    if (A.c->scalar)
+      adj_update_lin_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(
+          int(A.n), (const R*)A.c->vol, qbar_out, A.q0bar, A.rbar[0], A.rbar[1], A.rbar[2], A.rbar[3], al[0],
+          al[1], al[2], al[3], s, R(A.tab.beta[s] * dt));
+    else
+      adj_update_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(
+          int(A.n), g, A.sq[s + 1], A.sq[0], (const R*)A.c->vol, qbar_out, A.q0bar, A.rbar[0], A.rbar[1],
+          A.rbar[2], A.rbar[3], al[0], al[1], al[2], al[3], s, R(A.tab.beta[s] * dt));
     A.launches += 1;
     HC_CUDA(cudaGetLastError());
     if (int st = res_adj<R>(A, A.sq[s], A.rbar[s], s == 0 ? A.q0bar : nullptr, A.qbs, false, 0.0)) return st;
@@ -421,11 +453,19 @@ int reverse(AD& A, const Schedule& sc, int a, int b, int slot, std::vector<int>&
   return reverse(A, sc, a, a + k, slot, stack, false);
 }
 
-inline int check_support(hc_ctx* c) {
-  if (c->scalar) return fail(HC_ERR_UNSUPPORTED, "the adjoint covers the Euler law");
+inline int check_support(hc_ctx* c, const hc_objective* obj) {
   if (c->oned) return fail(HC_ERR_UNSUPPORTED, "the adjoint covers the 2D path");
+  if (c->scalar) {
+    if (c->df) return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint runs in FP64 or FP32");
+    if (c->cfg.flux != HC_FLUX_RUSANOV && c->cfg.flux != HC_FLUX_CENTRAL)
+      return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports the Rusanov and central fluxes");
+    if (obj->kind != HC_OBJ_L2) return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint takes the L2 objective");
+    for (int s = 0; s < 4; ++s)
+      if (c->bc[s] != HC_BC_PERIODIC && c->bc[s] != HC_BC_FIXED)
+        return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports periodic and fixed boundaries");
+  }
   if (c->cfg.basis != HC_BASIS_PRIMITIVE) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the primitive basis");
-  if (c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV)
+  if (!c->scalar && c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV)
     return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");
   const int l = c->cfg.limiter;
   if (!(l == HC_LIM_NOLIMIT1 || l == HC_LIM_NOLIMIT2 || l == HC_LIM_NOLIMIT3 || l == HC_LIM_VANALBADA ||
@@ -442,8 +482,9 @@ template <class R> int setup(Adj<R>& A, hc_ctx* c, int nsteps, int nsnap, const 
   if (!c || !obj || nsteps < 1 || nsnap < 0) return fail(HC_ERR_ARG, "bad adjoint arguments");
   if (obj->kind != HC_OBJ_DRAG && obj->kind != HC_OBJ_L2) return fail(HC_ERR_ARG, "unknown objective");
   if (int st = ctx_ensure_ready(c)) return st;
-  if (int st = check_support(c)) return st;
+  if (int st = check_support(c, obj)) return st;
   A.c = c;
+  A.nv = c->scalar ? 3 : 4;
   A.tab = rk_table(c->cfg.rk);
   A.nst = A.tab.nst;
   A.n = c->ncell();
@@ -452,19 +493,19 @@ template <class R> int setup(Adj<R>& A, hc_ctx* c, int nsteps, int nsnap, const 
   A.obj = *obj;
   A.nsteps = nsteps;
   A.nsnap = nsnap;
-  const size_t n4 = 4 * A.n;
+  const size_t n4 = A.state_values();
   for (int k = 0; k <= A.nst; ++k) if (int st = A.alloc(&A.sq[k], n4)) return st;
   for (int k = 0; k < 4; ++k) if (int st = A.alloc(&A.rbar[k], n4)) return st;
-  if (int st = A.alloc(&A.qm, 8 * A.n)) return st;
-  if (int st = A.alloc(&A.qmbar, 8 * A.n)) return st;
-  if (int st = A.alloc(&A.ai, size_t(ADJ_FIELDS) * A.nfi)) return st;
-  if (int st = A.alloc(&A.aj, size_t(ADJ_FIELDS) * A.nfj)) return st;
+  if (int st = A.alloc(&A.qm, 2 * n4)) return st;
+  if (int st = A.alloc(&A.qmbar, 2 * n4)) return st;
+  if (int st = A.alloc(&A.ai, size_t(4 * A.nv) * A.nfi)) return st;
+  if (int st = A.alloc(&A.aj, size_t(4 * A.nv) * A.nfj)) return st;
   if (int st = A.alloc(&A.lam, n4)) return st;
   if (int st = A.alloc(&A.qbs, n4)) return st;
   if (int st = A.alloc(&A.q0bar, n4)) return st;
   for (int s = 0; s < 4; ++s) {
-    if (int st = A.alloc(&A.refbar[s], 4 * size_t(c->nface(s)))) return st;
-    HC_CUDA(cudaMemsetAsync(A.refbar[s], 0, 4 * c->nface(s) * sizeof(R), A.s()));
+    if (int st = A.alloc(&A.refbar[s], size_t(A.nv) * c->nface(s))) return st;
+    HC_CUDA(cudaMemsetAsync(A.refbar[s], 0, size_t(A.nv) * c->nface(s) * sizeof(R), A.s()));
   }
   if (int st = A.alloc(&A.base, n4)) return st;
   if (nsnap > 0) if (int st = A.alloc(&A.snaps, size_t(nsnap) * n4)) return st;
@@ -504,7 +545,7 @@ int forward_pass(Adj<R>& A, const double* rates_in, const std::vector<std::pair<
   }
   if (A.obj.kind == HC_OBJ_L2) {
     l2_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(A.sq[0], A.target, A.n, A.obj.weight[0], A.obj.weight[1],
-                                                  A.obj.weight[2], A.obj.weight[3], A.qbs, 0, nullptr);
+                                                  A.obj.weight[2], A.obj.weight[3], A.qbs, 0, nullptr, A.nv);
     sum_into_kernel<R><<<1, 256, 0, A.s()>>>(A.qbs, int(A.n), A.jacc);
     A.launches += 2;
   }
@@ -562,7 +603,7 @@ int adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective* o
     if (int st = res_adj<R>(A, A.sq[0], nullptr, nullptr, A.lam, true, A.obj.scale / A.nsteps)) return st;
   } else {
     l2_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(A.sq[0], A.target, A.n, A.obj.weight[0], A.obj.weight[1],
-                                                  A.obj.weight[2], A.obj.weight[3], nullptr, 1, A.lam);
+                                                  A.obj.weight[2], A.obj.weight[3], nullptr, 1, A.lam, A.nv);
     A.launches += 1;
   }
   if (int st = reverse(A, sched, 0, nsteps, -1, stack, true)) return st;
@@ -582,11 +623,11 @@ int adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective* o
     }
     return HC_OK;
   };
-  if (q0_bar) if (int st = fetch(q0_bar, A.lam, 4 * A.n)) return st;
+  if (q0_bar) if (int st = fetch(q0_bar, A.lam, A.state_values())) return st;
   if (ref_bar) {
     size_t off = 0;
     for (int s = 0; s < 4; ++s) {
-      const size_t m = 4 * size_t(c->nface(s));
+      const size_t m = size_t(A.nv) * c->nface(s);
       if (int st = fetch(ref_bar + off, A.refbar[s], m)) return st;
       off += m;
     }

@@ -47,17 +47,18 @@ template <class R> struct AdjArgs {
   R obj_scale, obj_dirx, obj_diry;
 };
 
-// qmetric of cell c (phase 2 of the stage kernel, without tiling)
-template <class R> __device__ __forceinline__ void adj_qm_cell(const AdjArgs<R>& a, R* qm, int c) {
+// qmetric of cell c (phase 2 of the stage kernel, without tiling); NV variables
+// (4 Euler, 3 scalar advection), 2 NV planes
+template <class R, int NV = 4> __device__ __forceinline__ void adj_qm_cell(const AdjArgs<R>& a, R* qm, int c) {
   const int ni = a.ni, nj = a.nj;
   if (c >= ni * nj) return;
   const int gi = c / nj, gj = c % nj;
   const size_t n = size_t(ni) * nj;
   const bool per_i = a.bc[0] == BC_PERIODIC, per_j = a.bc[2] == BC_PERIODIC;
   const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
-  R m[8];
+  R m[2 * NV];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) m[k] = R(0);
+  for (int k = 0; k < 2 * NV; ++k) m[k] = R(0);
 #pragma unroll
   for (int f = 0; f < 4; ++f) {
     const bool idir = f < 2;
@@ -80,17 +81,17 @@ template <class R> __device__ __forceinline__ void adj_qm_cell(const AdjArgs<R>&
     const int nf = idir ? nfi : nfj;
     const R dx = rec[size_t(F_DXX) * nf + fidx], dy = rec[size_t(F_DXY) * nf + fidx];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
+    for (int v = 0; v < NV; ++v) {
       const R dq = hi ? (a.q[v * n + nb] - a.q[v * n + c]) : (a.q[v * n + c] - a.q[v * n + nb]);
       m[2 * v] += dq * dx;
       m[2 * v + 1] += dq * dy;
     }
   }
 #pragma unroll
-  for (int k = 0; k < 8; ++k) qm[k * n + c] = m[k];
+  for (int k = 0; k < 2 * NV; ++k) qm[k * n + c] = m[k];
 }
-template <class R> __global__ void adj_qm_kernel(const AdjArgs<R> a, R* qm) {
-  adj_qm_cell(a, qm, int(blockIdx.x * blockDim.x + threadIdx.x));
+template <class R, int NV = 4> __global__ void adj_qm_kernel(const AdjArgs<R> a, R* qm) {
+  adj_qm_cell<R, NV>(a, qm, int(blockIdx.x * blockDim.x + threadIdx.x));
 }
 
 template <class R, int FK>
@@ -257,16 +258,210 @@ template <class R, int FK, class C = R> __global__ void adj_face_kernel(const Ad
   adj_face_one<R, FK, C>(a, dir, int(blockIdx.x * blockDim.x + threadIdx.x));
 }
 
-// pass 2: qmetric adjoint of cell c
-template <class R> __device__ __forceinline__ void adj_qmbar_cell(const AdjArgs<R>& a, int c) {
+// ---- scalar advection law (conserved set {u, v, q}; scalar_face_flux, hc_scalar.cuh)
+enum { SADJ_FIELDS = 12 };  // dL[3], dR[3], gL[3], gR[3]
+
+// Reverse of scalar_face_flux for the three flux components (the spectral radius
+// feeds only the frozen timestep): Fb -> qlb, qrb (accumulated).  Ties of the
+// Rusanov max and the kink of |u_n| take the branches of the forward-mode reference
+// (the left side on a tie, derivative 0 at u_n = 0).
+template <class R, int FK>
+__host__ __device__ __forceinline__ void scalar_flux_adj(R nx, R ny, R A, const R* ql, const R* qr, const R* Fb,
+                                                         R* qlb, R* qrb) {
+  const R unl = nx * ql[0] + ny * ql[1];
+  const R unr = nx * qr[0] + ny * qr[1];
+  const R t = R(0.5) * A * Fb[2];
+  R unlb = t * ql[2], unrb = t * qr[2];
+  qlb[2] += t * unl;
+  qrb[2] += t * unr;
+  if constexpr (FK == FLUX_RUSANOV) {
+    const R al = fabs(unl), ar = fabs(unr);
+    const R c = R(-0.5) * (fmax(al, ar) * A);
+    R cb = R(0);
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      cb += Fb[v] * (qr[v] - ql[v]);
+      qrb[v] += c * Fb[v];
+      qlb[v] -= c * Fb[v];
+    }
+    const R mb = R(-0.5) * A * cb;
+    if (al >= ar) unlb += sgn(unl) * mb;
+    else unrb += sgn(unr) * mb;
+  }
+  qlb[0] += nx * unlb; qlb[1] += ny * unlb;
+  qrb[0] += nx * unrb; qrb[1] += ny * unrb;
+}
+
+// pass 1 of the scalar law: one thread per face of direction dir.  Interior and
+// periodic faces: flux, limiter and reconstruction reversed; Fixed boundary faces:
+// the interior side reversed and the ghost side's adjoint added to the reference
+// adjoint.  Writes SADJ_FIELDS planes (the Euler layout with three variables).
+template <class R, int FK> __device__ __forceinline__ void adj_face_scalar_one(const AdjArgs<R>& a, int dir, int f) {
+  const int ni = a.ni, nj = a.nj;
+  const size_t n = size_t(ni) * nj;
+  const bool idir = dir == 0;
+  const int nf = idir ? (ni + 1) * nj : ni * (nj + 1);
+  if (f >= nf) return;
+  int i, j;
+  if (idir) { i = f / nj; j = f % nj; } else { i = f / (nj + 1); j = f % (nj + 1); }
+  const R* rec = idir ? a.fi : a.fj;
+  R* out = idir ? a.ai : a.aj;
+  auto rd = [&](int fld) -> R { return rec[size_t(fld) * nf + f]; };
+  const R nx = rd(F_NX), ny = rd(F_NY), A = rd(F_A);
+  const int lo = idir ? i : j, nalong = idir ? ni : nj;
+  const int side = idir ? (lo == 0 ? 0 : 1) : (lo == 0 ? 2 : 3);
+  const bool bnd = (lo == 0 || lo == nalong) && a.bc[side] != BC_PERIODIC;
+  R res[SADJ_FIELDS];
+#pragma unroll
+  for (int k = 0; k < SADJ_FIELDS; ++k) res[k] = R(0);
+  R* dL = res; R* dR = res + 3; R* gL = res + 6; R* gR = res + 9;
+  const int lim = a.limiter;
+  if (!bnd) {
+    int cl, cr;
+    if (idir) { cl = wrapi(i - 1, ni) * nj + j; cr = wrapi(i, ni) * nj + j; }
+    else { cl = i * nj + wrapi(j - 1, nj); cr = i * nj + wrapi(j, nj); }
+    R Fb[3], ql[3], qr[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      Fb[v] = a.rbar[v * n + cr] - a.rbar[v * n + cl];
+      ql[v] = a.q[v * n + cl];
+      qr[v] = a.q[v * n + cr];
+    }
+    if (lim == LIM_NOLIMIT1) {
+      scalar_flux_adj<R, FK>(nx, ny, A, ql, qr, Fb, dL, dR);
+    } else {
+      const R dl = rd(F_DL), dr = rd(F_DR), idlr = rd(F_IDLR);
+      const R wlx = rd(F_WLX), wly = rd(F_WLY), sl = rd(F_SL);
+      const R wrx = rd(F_WRX), wry = rd(F_WRY), sr = rd(F_SR);
+      R qL[3], qR[3], gc[3], gl[3], gr[3];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        const R dq = qr[v] - ql[v];
+        gc[v] = dq * idlr;
+        gl[v] = (a.qm[(2 * v) * n + cl] * wlx + a.qm[(2 * v + 1) * n + cl] * wly) - dq * sl;
+        gr[v] = (a.qm[(2 * v) * n + cr] * wrx + a.qm[(2 * v + 1) * n + cr] * wry) - dq * sr;
+        qL[v] = ql[v] + dl * limit<R>(lim, gc[v], gl[v]);
+        qR[v] = qr[v] - dr * limit<R>(lim, gc[v], gr[v]);
+      }
+      R qLb[3] = {R(0), R(0), R(0)}, qRb[3] = {R(0), R(0), R(0)};
+      scalar_flux_adj<R, FK>(nx, ny, A, qL, qR, Fb, qLb, qRb);
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        R da, db;
+        limit_grad<R>(lim, gc[v], gl[v], &da, &db);
+        const R zlb = dl * qLb[v];
+        R gcb = zlb * da;
+        const R glb = zlb * db;
+        limit_grad<R>(lim, gc[v], gr[v], &da, &db);
+        const R zrb = -dr * qRb[v];
+        gcb += zrb * da;
+        const R grb = zrb * db;
+        const R dqb = gcb * idlr - glb * sl - grb * sr;
+        dL[v] = qLb[v] - dqb;
+        dR[v] = qRb[v] + dqb;
+        gL[v] = glb;
+        gR[v] = grb;
+      }
+    }
+  } else if (a.bc[side] == BC_FIXED) {
+    const bool int_right = lo == 0;
+    const int ci = idir ? (int_right ? 0 : ni - 1) * nj + j : i * nj + (int_right ? 0 : nj - 1);
+    const int kf = idir ? j : i;
+    const int nfs = idir ? nj : ni;
+    R* dI = int_right ? dR : dL;
+    R* gI = int_right ? gR : gL;
+    R Fb[3], qi[3], qg[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      Fb[v] = int_right ? a.rbar[v * n + ci] : -a.rbar[v * n + ci];
+      qi[v] = a.q[v * n + ci];
+      qg[v] = a.gref[side][size_t(v) * nfs + kf];
+    }
+    R qLb[3] = {R(0), R(0), R(0)}, qRb[3] = {R(0), R(0), R(0)};
+    R gb_ref[3] = {R(0), R(0), R(0)};
+    if (lim == LIM_NOLIMIT1) {
+      if (int_right) scalar_flux_adj<R, FK>(nx, ny, A, qg, qi, Fb, qLb, qRb);
+      else scalar_flux_adj<R, FK>(nx, ny, A, qi, qg, Fb, qLb, qRb);
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        dI[v] += int_right ? qRb[v] : qLb[v];
+        gb_ref[v] = int_right ? qLb[v] : qRb[v];
+      }
+    } else {
+      const R d = rd(F_DL), idlr = rd(F_IDLR);
+      const R wx = int_right ? rd(F_WRX) : rd(F_WLX), wy = int_right ? rd(F_WRY) : rd(F_WLY);
+      R qL[3], qR[3], gc[3], gbv[3];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        const R dq = int_right ? (qi[v] - qg[v]) : (qg[v] - qi[v]);
+        gc[v] = dq * idlr;
+        gbv[v] = a.qm[(2 * v) * n + ci] * wx + a.qm[(2 * v + 1) * n + ci] * wy;
+        const R sv = limit<R>(lim, gc[v], gbv[v]);
+        if (int_right) { qL[v] = qg[v]; qR[v] = qi[v] - d * sv; }
+        else { qL[v] = qi[v] + d * sv; qR[v] = qg[v]; }
+      }
+      scalar_flux_adj<R, FK>(nx, ny, A, qL, qR, Fb, qLb, qRb);
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        R da, db;
+        limit_grad<R>(lim, gc[v], gbv[v], &da, &db);
+        const R zb = int_right ? -d * qRb[v] : d * qLb[v];
+        gI[v] = zb * db;
+        const R dqb = zb * da * idlr;
+        if (int_right) { dI[v] += qRb[v] + dqb; gb_ref[v] = qLb[v] - dqb; }
+        else { dI[v] += qLb[v] - dqb; gb_ref[v] = qRb[v] + dqb; }
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < 3; ++v) a.refbar[side][size_t(v) * nfs + kf] += gb_ref[v];
+  }
+#pragma unroll
+  for (int k = 0; k < SADJ_FIELDS; ++k) out[size_t(k) * nf + f] = res[k];
+}
+template <class R, int FK> __global__ void adj_face_scalar_kernel(const AdjArgs<R> a, int dir) {
+  adj_face_scalar_one<R, FK>(a, dir, int(blockIdx.x * blockDim.x + threadIdx.x));
+}
+
+// Reverse of a stage update that is linear on the conserved set, q_out = q0 + (sum_k
+// alpha_k R_k) fac (the scalar law), fac = beta dt / V frozen: q0bar += qbar_out,
+// rbar_k += alpha_k fac qbar_out.
+template <class R, int NV>
+__device__ __forceinline__ void adj_update_lin_cell(int ncell, const R* __restrict__ vol,
+                                                    const R* __restrict__ qbar_out, R* __restrict__ q0bar, R* rbar0,
+                                                    R* rbar1, R* rbar2, R* rbar3, R alpha0, R alpha1, R alpha2,
+                                                    R alpha3, int stage, R dts, int c) {
+  if (c >= ncell) return;
+  const size_t n = size_t(ncell);
+  const R fac = dts / vol[c];
+  R* rb[4] = {rbar0, rbar1, rbar2, rbar3};
+  const R al[4] = {alpha0, alpha1, alpha2, alpha3};
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const R qb = qbar_out[v * n + c];
+    q0bar[v * n + c] += qb;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k <= stage) rb[k][v * n + c] += al[k] * qb * fac;
+  }
+}
+template <class R, int NV>
+__global__ void adj_update_lin_kernel(int ncell, const R* __restrict__ vol, const R* __restrict__ qbar_out,
+                                      R* __restrict__ q0bar, R* rbar0, R* rbar1, R* rbar2, R* rbar3, R alpha0,
+                                      R alpha1, R alpha2, R alpha3, int stage, R dts) {
+  adj_update_lin_cell<R, NV>(ncell, vol, qbar_out, q0bar, rbar0, rbar1, rbar2, rbar3, alpha0, alpha1, alpha2, alpha3,
+                             stage, dts, int(blockIdx.x * blockDim.x + threadIdx.x));
+}
+
+// pass 2: qmetric adjoint of cell c (NV variables; face fields dL, dR, gL, gR of NV each)
+template <class R, int NV = 4> __device__ __forceinline__ void adj_qmbar_cell(const AdjArgs<R>& a, int c) {
   const int ni = a.ni, nj = a.nj;
   if (c >= ni * nj) return;
   const int gi = c / nj, gj = c % nj;
   const size_t n = size_t(ni) * nj;
   const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
-  R m[8];
+  R m[2 * NV];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) m[k] = R(0);
+  for (int k = 0; k < 2 * NV; ++k) m[k] = R(0);
 #pragma unroll
   for (int f = 0; f < 4; ++f) {
     const bool idir = f < 2;
@@ -286,30 +481,30 @@ template <class R> __device__ __forceinline__ void adj_qmbar_cell(const AdjArgs<
     const R wx = rec[size_t(use_left_slot ? F_WLX : F_WRX) * nf + fidx];
     const R wy = rec[size_t(use_left_slot ? F_WLY : F_WRY) * nf + fidx];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const R gv = adj[size_t(hi ? 8 + v : 12 + v) * nf + fidx];
+    for (int v = 0; v < NV; ++v) {
+      const R gv = adj[size_t(hi ? 2 * NV + v : 3 * NV + v) * nf + fidx];
       m[2 * v] += gv * wx;
       m[2 * v + 1] += gv * wy;
     }
   }
 #pragma unroll
-  for (int k = 0; k < 8; ++k) a.qmbar[k * n + c] = m[k];
+  for (int k = 0; k < 2 * NV; ++k) a.qmbar[k * n + c] = m[k];
 }
-template <class R> __global__ void adj_qmbar_kernel(const AdjArgs<R> a) {
-  adj_qmbar_cell(a, int(blockIdx.x * blockDim.x + threadIdx.x));
+template <class R, int NV = 4> __global__ void adj_qmbar_kernel(const AdjArgs<R> a) {
+  adj_qmbar_cell<R, NV>(a, int(blockIdx.x * blockDim.x + threadIdx.x));
 }
 
-// pass 3: gather the state adjoint of cell c
-template <class R> __device__ __forceinline__ void adj_gather_cell(const AdjArgs<R>& a, int c) {
+// pass 3: gather the state adjoint of cell c (NV variables)
+template <class R, int NV = 4> __device__ __forceinline__ void adj_gather_cell(const AdjArgs<R>& a, int c) {
   const int ni = a.ni, nj = a.nj;
   if (c >= ni * nj) return;
   const int gi = c / nj, gj = c % nj;
   const size_t n = size_t(ni) * nj;
   const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
   const bool per_i = a.bc[0] == BC_PERIODIC, per_j = a.bc[2] == BC_PERIODIC;
-  R qb[4];
+  R qb[NV];
 #pragma unroll
-  for (int v = 0; v < 4; ++v) qb[v] = a.qbar_add ? a.qbar_add[v * n + c] : R(0);
+  for (int v = 0; v < NV; ++v) qb[v] = a.qbar_add ? a.qbar_add[v * n + c] : R(0);
 #pragma unroll
   for (int f = 0; f < 4; ++f) {
     const bool idir = f < 2;
@@ -319,7 +514,7 @@ template <class R> __device__ __forceinline__ void adj_gather_cell(const AdjArgs
     const int nf = idir ? nfi : nfj;
     const R* adj = idir ? a.ai : a.aj;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) qb[v] += adj[size_t(hi ? v : 4 + v) * nf + fidx];
+    for (int v = 0; v < NV; ++v) qb[v] += adj[size_t(hi ? v : NV + v) * nf + fidx];
     const bool pair = idir ? ((lo > 0 && lo < ni) || per_i) : ((lo > 0 && lo < nj) || per_j);
     if (!pair) continue;
     const R* rec = idir ? a.fi : a.fj;
@@ -327,15 +522,15 @@ template <class R> __device__ __forceinline__ void adj_gather_cell(const AdjArgs
     const int nb = idir ? wrapi(gi + (hi ? 1 : -1), ni) * nj + gj : gi * nj + wrapi(gj + (hi ? 1 : -1), nj);
     const R sg = hi ? R(-1) : R(1);  // c left of the face -> -1
 #pragma unroll
-    for (int v = 0; v < 4; ++v)
+    for (int v = 0; v < NV; ++v)
       qb[v] += sg * ((a.qmbar[(2 * v) * n + c] + a.qmbar[(2 * v) * n + nb]) * dx +
                      (a.qmbar[(2 * v + 1) * n + c] + a.qmbar[(2 * v + 1) * n + nb]) * dy);
   }
 #pragma unroll
-  for (int v = 0; v < 4; ++v) a.qbar[v * n + c] = qb[v];
+  for (int v = 0; v < NV; ++v) a.qbar[v * n + c] = qb[v];
 }
-template <class R> __global__ void adj_gather_kernel(const AdjArgs<R> a) {
-  adj_gather_cell(a, int(blockIdx.x * blockDim.x + threadIdx.x));
+template <class R, int NV = 4> __global__ void adj_gather_kernel(const AdjArgs<R> a) {
+  adj_gather_cell<R, NV>(a, int(blockIdx.x * blockDim.x + threadIdx.x));
 }
 
 // Reverse of one stage update q_out = prim(cons(q0) + (sum_k alpha_k R_k) * fac),

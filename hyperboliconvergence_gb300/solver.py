@@ -190,12 +190,15 @@ class Solver:
 
     def gradient(self, nsteps, snapshots=20, kind="drag", rates=None, **kw):
         """J and its gradient with respect to the current state and the fixed-ghost
-        reference states; returns (J, q0_bar, [ref_bar per side], rates, stats)."""
+        reference states; returns (J, q0_bar, [ref_bar per side], rates, stats).  Euler:
+        drag or L2 objective, 4 planes; scalar advection: L2 objective on {u, v, q}, 3 planes
+        (weight[3] unused)."""
         from ._capi import AdjointStats
         o = self._objective(kind, **kw)
         m = self.mesh
-        q0b = np.empty((4, m.ni, m.nj))
-        rb = np.empty(sum(4 * m.nface(s) for s in range(4)))
+        nv = self.nv
+        q0b = np.empty((nv, m.ni, m.nj))
+        rb = np.empty(sum(nv * m.nface(s) for s in range(4)))
         rout = np.empty(int(nsteps))
         st = AdjointStats()
         rin = None if rates is None else np.ascontiguousarray(rates, dtype=np.float64)
@@ -205,8 +208,8 @@ class Solver:
         refb, off = [], 0
         for s in range(4):
             nf = m.nface(s)
-            refb.append(rb[off:off + 4 * nf].reshape(4, nf).copy())
-            off += 4 * nf
+            refb.append(rb[off:off + nv * nf].reshape(nv, nf).copy())
+            off += nv * nf
         return st.J, q0b, refb, rout, st
 
     def close(self):

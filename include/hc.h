@@ -295,7 +295,8 @@ typedef struct {
   int kind;              /* hc_objective_kind */
   double scale;          /* drag: J = scale/N * sum_{n=1..N} wall force of q_n along dir */
   double dir[2];         /* drag: force direction */
-  const double* target;  /* L2: J = sum_cells sum_v weight[v] (q_N - target)^2, target 4 planes (host) */
+  const double* target;  /* L2: J = sum_cells sum_v weight[v] (q_N - target)^2, target 4 planes (host;
+                            3 for the scalar law) */
   double weight[4];
 } hc_objective;
 
@@ -313,7 +314,9 @@ typedef struct {
 int hc_objective_forward(hc_ctx* ctx, int nsteps, const hc_objective* obj, const double* rates_in,
                          double* rates_out, double* J);
 /* J and its gradient: q0_bar (4 planes of the primitive state) and ref_bar (per side 0..3,
- * 4 planes of nface values, concatenated; zero where the side is not fixed). */
+ * 4 planes of nface values, concatenated; zero where the side is not fixed).  Scalar
+ * advection contexts (Rusanov or central flux, periodic / fixed sides, HC_OBJ_L2 on the
+ * conserved set {u, v, q} with weight[0..2]): 3 planes each. */
 int hc_adjoint_gradient(hc_ctx* ctx, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
                         double* q0_bar, double* ref_bar, double* rates_out, hc_adjoint_stats* stats);
 

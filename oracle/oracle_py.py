@@ -373,8 +373,8 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
-def _sides(arrs, ni, nj):
-    """Per-side 4-plane arrays (None for unused sides) as a C array of pointers."""
+def _sides(arrs, ni, nj, nv=4):
+    """Per-side nv-plane arrays (None for unused sides) as a C array of pointers."""
     keep, ptrs = [], (C.c_void_p * 4)()
     for side in range(4):
         a = None if arrs is None else arrs[side]
@@ -382,7 +382,7 @@ def _sides(arrs, ni, nj):
             ptrs[side] = None
             continue
         nf = nj if side < 2 else ni
-        a = np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64).reshape(4, -1), (4, nf)))
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64).reshape(nv, -1), (nv, nf)))
         keep.append(a)
         ptrs[side] = a.ctypes.data
     return ptrs, keep
@@ -465,6 +465,38 @@ def scalar_bc_riemann(face, qi, qb):
     lib.hcos_bc_riemann(np.ascontiguousarray(face, dtype=np.float64), np.ascontiguousarray(qi, dtype=np.float64),
                         np.ascontiguousarray(qb, dtype=np.float64), out)
     return out
+
+
+def scalar_objective(mesh_nodes, ni, nj, bc, q0, nsteps, target, flux="rusanov", limiter="vanalbada", rk="ssp34",
+                     cfl=0.5, ref=None, weight=(1.0, 1.0, 1.0), dq0=None, dref=None, freeze_dt=True):
+    """L2 objective of an RK run of the scalar oracle (global timestep): J = sum over cells
+    and the three conserved variables {u, v, q} of weight[v] (q_N - target)^2.  With a
+    direction (dq0 and/or dref) also the exact derivative of J along it (forward-mode dual
+    numbers through the same oracle code), timesteps frozen unless freeze_dt is False.
+    Returns (J, dJ or None)."""
+    lib = load(False)
+    if not getattr(lib, "_sobj_declared", False):
+        v, i, d = C.c_void_p, C.c_int, C.c_double
+        lib.hcos_objective.argtypes = [i, i, v, v, i, i, i, d, v, v, v, v, i, v, v, i, v]
+        lib._sobj_declared = True
+    nodes = np.ascontiguousarray(mesh_nodes, dtype=np.float64)
+    bcv = np.array([SBC[b] if isinstance(b, str) else int(b) for b in bc], dtype=np.int32)
+    q = np.ascontiguousarray(q0, dtype=np.float64)
+    tgt = np.ascontiguousarray(target, dtype=np.float64)
+    w = np.asarray(list(weight)[:3], dtype=np.float64)
+    refp, keep_r = _sides(ref, ni, nj, 3)
+    has_dir = dq0 is not None or dref is not None
+    dq = None if dq0 is None else np.ascontiguousarray(dq0, dtype=np.float64)
+    drefp, keep_d = _sides(dref, ni, nj, 3)
+    out = np.zeros(2)
+    lib.hcos_objective(ni, nj, _ptr(nodes), _ptr(bcv), SFLUX[flux] if isinstance(flux, str) else flux,
+                       LIMITER[limiter] if isinstance(limiter, str) else limiter, RK[rk] if isinstance(rk, str) else rk,
+                       float(cfl), refp, drefp if dref is not None else None, _ptr(q),
+                       _ptr(dq) if has_dir and dq is not None else None, int(nsteps), _ptr(tgt), _ptr(w),
+                       1 if freeze_dt else 0, _ptr(out))
+    if not has_dir:
+        return float(out[0]), None
+    return float(out[0]), float(out[1])
 
 
 class ScalarOracleSolver:
