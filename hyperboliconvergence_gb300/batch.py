@@ -15,15 +15,20 @@ from .solver import Mesh, _dptr
 
 
 class Batch:
-    """Instances = list of (mesh, bc, ref, state); shared flux/limiter/RK/CFL/species."""
+    """Instances = list of (mesh, bc, ref, state); shared law/flux/limiter/RK/CFL/species.
+    law="euler": states {u, v, rho, p} (4 planes); law="scalar": scalar advection,
+    states {u, v, q} (3 planes), Rusanov or central flux."""
 
     def __init__(self, instances, flux="slau", limiter="vanalbada", rk="ssp34", precision="fp32", dt="global",
-                 cfl=0.5, species=(1.4, 287.058, 0.5), stream=None, basis="primitive"):
+                 cfl=0.5, species=(1.4, 287.058, 0.5), stream=None, basis="primitive", law="euler"):
         self.lib = _capi.load()
         self.meshes = [inst[0] for inst in instances]
+        self.law = law
+        self.nv = 3 if law == "scalar" else 4
+        nv = self.nv
         n = len(instances)
-        cfg = Config(FLUX[flux], LIMITER[limiter], RK[rk], PRECISION[precision], DTMODE[dt], float(cfl), 0,
-                     _capi.BASIS[basis])
+        cfg = Config(FLUX[flux], LIMITER[limiter], RK[rk], PRECISION[precision], DTMODE[dt], float(cfl),
+                     _capi.LAW[law], _capi.BASIS[basis])
         ni = (C.c_int * n)(*[m.ni for m in self.meshes])
         nj = (C.c_int * n)(*[m.nj for m in self.meshes])
         nodes = (C.POINTER(C.c_double) * n)(*[_dptr(m.nodes) for m in self.meshes])
@@ -37,8 +42,8 @@ class Batch:
                 if r is None:
                     refs[4 * k + s] = C.POINTER(C.c_double)()
                 else:
-                    arr = np.ascontiguousarray(np.broadcast_to(np.asarray(r, dtype=np.float64).reshape(4, -1),
-                                                               (4, mesh.nface(s))))
+                    arr = np.ascontiguousarray(np.broadcast_to(np.asarray(r, dtype=np.float64).reshape(nv, -1),
+                                                               (nv, mesh.nface(s))))
                     self._keep.append(arr)
                     refs[4 * k + s] = _dptr(arr)
         h = C.c_void_p()
@@ -65,13 +70,13 @@ class Batch:
     def set_state(self, k: int, prim: np.ndarray) -> None:
         a = np.ascontiguousarray(prim, dtype=np.float64)
         m = self.meshes[k]
-        if a.shape != (4, m.ni, m.nj):
+        if a.shape != (self.nv, m.ni, m.nj):
             raise ValueError("state shape mismatch")
         check(self.lib.hc_batch_state_upload(self.h, k, _dptr(a)))
 
     def get_state(self, k: int) -> np.ndarray:
         m = self.meshes[k]
-        out = np.empty((4, m.ni, m.nj))
+        out = np.empty((self.nv, m.ni, m.nj))
         check(self.lib.hc_batch_state_download(self.h, k, _dptr(out)))
         return out
 
@@ -113,17 +118,18 @@ class Batch:
         """Every instance's L2 objective J_k = sum w_v (q_k(N) - target_k)^2 after nsteps
         steps and its gradient with respect to the instance's current state, from one
         batched adjoint (hc_batch_adjoint_gradient).  `want`: indices whose gradients
-        are copied back (default all).  Returns (J array, {k: q0_bar}, stats)."""
+        are copied back (default all).  Returns (J array, {k: q0_bar}, stats).  Scalar
+        batches: 3 planes {u, v, q}, weight[3] unused."""
         from ._capi import AdjointStats, Objective
-        n = self.n
+        n, nv = self.n, self.nv
         tg = [np.ascontiguousarray(t, dtype=np.float64) for t in targets]
         for k, t in enumerate(tg):
             m = self.meshes[k]
-            if t.shape != (4, m.ni, m.nj):
-                raise ValueError(f"target {k} must have shape (4, {m.ni}, {m.nj})")
+            if t.shape != (nv, m.ni, m.nj):
+                raise ValueError(f"target {k} must have shape ({nv}, {m.ni}, {m.nj})")
         tptr = (C.POINTER(C.c_double) * n)(*[_dptr(t) for t in tg])
         want = range(n) if want is None else list(want)
-        grads = {k: np.empty((4, self.meshes[k].ni, self.meshes[k].nj)) for k in want}
+        grads = {k: np.empty((nv, self.meshes[k].ni, self.meshes[k].nj)) for k in want}
         gptr = (C.POINTER(C.c_double) * n)()
         for k, g in grads.items():
             gptr[k] = _dptr(g)

@@ -112,3 +112,20 @@ def gaussian_sum(ni: int, nj: int, rng: np.random.Generator, base=(0.5, 0.25, 5.
         amp = rng.uniform(-0.5, 0.5)
         q[2] += amp * np.exp(-((c[0] - cx) ** 2 + (c[1] - cy) ** 2) / (2 * w * w))
     return mesh, ["periodic"] * 4, None, q, (GAMMA, R_AIR, 0.3)
+
+
+def scalar_gaussian_sum(ni: int, nj: int, rng: np.random.Generator, velocity=(0.8, -0.5), base: float = 1.0,
+                        nbumps: int = 8):
+    """Scalar advection on the periodic unit square: a constant velocity and a scalar of
+    `base` plus 8 seeded Gaussians (centres in the domain, widths in [0.02, 0.2],
+    amplitudes in [-0.5, 0.5]); states {u, v, q}."""
+    mesh = Mesh.linspace(ni, nj, 0.0, 1.0, 0.0, 1.0)
+    c = mesh.centres()
+    q = np.empty((3, ni, nj))
+    q[0], q[1], q[2] = velocity[0], velocity[1], base
+    for _ in range(nbumps):
+        cx, cy = rng.uniform(0, 1, 2)
+        w = rng.uniform(0.02, 0.2)
+        amp = rng.uniform(-0.5, 0.5)
+        q[2] += amp * np.exp(-((c[0] - cx) ** 2 + (c[1] - cy) ** 2) / (2 * w * w))
+    return mesh, ["periodic"] * 4, None, q

@@ -671,25 +671,32 @@ template <class R> __device__ __forceinline__ void adj_block_setup(const AdjBatc
   __syncthreads();
 }
 
-template <class R> __global__ void adj_qm_batch_kernel(const AdjBatchArgs<R> b) {
+// (a scalar-law batch keeps the pools' 4-plane state, 8-plane qmetric and
+// ADJ_FIELDS-plane face slabs and uses the first NV, 2 NV and SADJ_FIELDS planes)
+template <class R, int NV = 4> __global__ void adj_qm_batch_kernel(const AdjBatchArgs<R> b) {
   __shared__ AdjBlock<R> sb;
   adj_block_setup(b, 1, sb);
-  adj_qm_cell(sb.a, const_cast<R*>(sb.a.qm), sb.local * int(blockDim.x) + int(threadIdx.x));
+  adj_qm_cell<R, NV>(sb.a, const_cast<R*>(sb.a.qm), sb.local * int(blockDim.x) + int(threadIdx.x));
 }
 template <class R, int FK, class C = R> __global__ void adj_face_batch_kernel(const AdjBatchArgs<R> b) {
   __shared__ AdjBlock<R> sb;
   adj_block_setup(b, 2, sb);
   adj_face_one<R, FK, C>(sb.a, sb.seg & 1, sb.local * int(blockDim.x) + int(threadIdx.x));
 }
-template <class R> __global__ void adj_qmbar_batch_kernel(const AdjBatchArgs<R> b) {
+template <class R, int FK> __global__ void adj_face_scalar_batch_kernel(const AdjBatchArgs<R> b) {
   __shared__ AdjBlock<R> sb;
-  adj_block_setup(b, 1, sb);
-  adj_qmbar_cell(sb.a, sb.local * int(blockDim.x) + int(threadIdx.x));
+  adj_block_setup(b, 2, sb);
+  adj_face_scalar_one<R, FK>(sb.a, sb.seg & 1, sb.local * int(blockDim.x) + int(threadIdx.x));
 }
-template <class R> __global__ void adj_gather_batch_kernel(const AdjBatchArgs<R> b) {
+template <class R, int NV = 4> __global__ void adj_qmbar_batch_kernel(const AdjBatchArgs<R> b) {
   __shared__ AdjBlock<R> sb;
   adj_block_setup(b, 1, sb);
-  adj_gather_cell(sb.a, sb.local * int(blockDim.x) + int(threadIdx.x));
+  adj_qmbar_cell<R, NV>(sb.a, sb.local * int(blockDim.x) + int(threadIdx.x));
+}
+template <class R, int NV = 4> __global__ void adj_gather_batch_kernel(const AdjBatchArgs<R> b) {
+  __shared__ AdjBlock<R> sb;
+  adj_block_setup(b, 1, sb);
+  adj_gather_cell<R, NV>(sb.a, sb.local * int(blockDim.x) + int(threadIdx.x));
 }
 
 // Reverse of one stage update for every instance; the frozen timestep of each
@@ -719,6 +726,17 @@ template <class R> __global__ void adj_update_batch_kernel(const AdjUpdateBatch<
   adj_update_cell(in.ni * in.nj, u.g, u.q_out + c4, u.q0 + c4, u.vol + in.cell, u.qbar_out + c4, u.q0bar + c4,
                   u.rbar[0] + c4, u.rbar[1] + c4, u.rbar[2] + c4, u.rbar[3] + c4, u.alpha[0], u.alpha[1], u.alpha[2],
                   u.alpha[3], u.stage, R(u.beta * dt), c);
+}
+// the same for a scalar-law batch (the update is linear on the conserved set)
+template <class R> __global__ void adj_update_lin_batch_kernel(const AdjUpdateBatch<R> u) {
+  const int s = find_segment(u.seg, u.nseg, int(blockIdx.x));
+  const BatchInst& in = u.inst[s];
+  const long long c4 = 4 * in.cell;
+  const double dt = u.cfl / fmax(DBL_MIN, u.rates[s]);
+  const int c = (int(blockIdx.x) - u.seg[s]) * int(blockDim.x) + int(threadIdx.x);
+  adj_update_lin_cell<R, 3>(in.ni * in.nj, u.vol + in.cell, u.qbar_out + c4, u.q0bar + c4, u.rbar[0] + c4,
+                            u.rbar[1] + c4, u.rbar[2] + c4, u.rbar[3] + c4, u.alpha[0], u.alpha[1], u.alpha[2],
+                            u.alpha[3], u.stage, R(u.beta * dt), c);
 }
 
 }  // namespace hc

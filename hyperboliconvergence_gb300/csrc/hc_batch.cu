@@ -82,7 +82,10 @@ template <class R> int persistent_step(hc_batch* b) {
   const RKTab tab = rk_table(b->cfg.rk);
   const int nst = tab.nst;
   const bool global = b->cfg.dt_mode == HC_DT_GLOBAL;
-  const BatchFn<R> fn = batch_fn<R>(b->cfg.flux);
+  const BatchFn<R> euler_fn = batch_fn<R>(b->cfg.flux);
+  auto fn = [b, euler_fn](const BatchArgs<R>& a, int tile, int grid, cudaStream_t st) -> cudaError_t {
+    return b->scalar ? launch_scalar_batch_stage<R>(a, b->cfg.flux, tile, grid, st) : euler_fn(a, tile, grid, st);
+  };
   const int grid = std::max(1, std::min(b->nwork, b->sms * std::max(1, b->sched.ctas_per_sm)));
   if (int st = zero_step_words(b)) return st;
   auto out_of = [&](int s) -> R* { return (R*)((s == nst - 1) ? b->q[0] : b->q[1 + (s % 2)]); };
@@ -99,8 +102,12 @@ template <class R> int persistent_step(hc_batch* b) {
       a.res_out = (R*)b->res[0];
       HC_CUDA(fn(a, b->sched.tile, grid, b->stream));
       a.q_out = out_of(0);
-      HC_CUDA(launch_batch_update0<R>(a, b->sched.tile, grid, b->cfg.cfl, R(tab.alpha[0][0]), R(tab.beta[0]),
-                                      b->stream));
+      if (b->scalar)
+        HC_CUDA(launch_scalar_batch_update0<R>(a, b->sched.tile, grid, b->cfg.cfl, R(tab.alpha[0][0]),
+                                               R(tab.beta[0]), b->stream));
+      else
+        HC_CUDA(launch_batch_update0<R>(a, b->sched.tile, grid, b->cfg.cfl, R(tab.alpha[0][0]), R(tab.beta[0]),
+                                        b->stream));
       b->launches += 2;
     } else {
       a.mode = global ? MODE_FUSED_GLOBAL : MODE_FUSED_LOCAL;
@@ -117,7 +124,10 @@ template <class R> int per_instance_step(hc_batch* b) {
   const RKTab tab = rk_table(b->cfg.rk);
   const int nst = tab.nst;
   const bool global = b->cfg.dt_mode == HC_DT_GLOBAL;
-  const StageFn<R> fn = stage_fn<R>(b->cfg.flux);
+  const StageFn<R> euler_fn = stage_fn<R>(b->cfg.flux);
+  auto fn = [b, euler_fn](const StageArgs<R>& a, int tile, cudaStream_t st) -> cudaError_t {
+    return b->scalar ? launch_scalar_stage<R>(a, b->cfg.flux, tile, st) : euler_fn(a, tile, st);
+  };
   if (int st = zero_step_words(b)) return st;
   for (int k = 0; k < b->ninst; ++k) {
     const long long c4 = 4 * b->cell_off[k], c5 = 5 * b->cell_off[k];
@@ -154,9 +164,13 @@ template <class R> int per_instance_step(hc_batch* b) {
         HC_CUDA(fn(a, b->sched.tile, b->stream));
         const size_t n = b->icells(k);
         const unsigned grid = unsigned(std::min<size_t>((n + 255) / 256, size_t(b->sms) * 16));
-        update0_kernel<R><<<grid, 256, 0, b->stream>>>(base.ni, base.nj, base.gas, qp(0), rp(0), base.vol,
-                                                       R(tab.alpha[0][0]), R(tab.beta[0]), b->cfg.cfl, base.info,
-                                                       out_of(0), 1, b->cfg.basis, 0.0);
+        if (b->scalar)
+          HC_CUDA(launch_scalar_update0<R>(base.ni, base.nj, qp(0), rp(0), base.vol, R(tab.alpha[0][0]),
+                                           R(tab.beta[0]), b->cfg.cfl, base.info, out_of(0), 1, b->stream));
+        else
+          update0_kernel<R><<<grid, 256, 0, b->stream>>>(base.ni, base.nj, base.gas, qp(0), rp(0), base.vol,
+                                                         R(tab.alpha[0][0]), R(tab.beta[0]), b->cfg.cfl, base.info,
+                                                         out_of(0), 1, b->cfg.basis, 0.0);
         HC_CUDA(cudaGetLastError());
         b->launches += 2;
       } else {
@@ -196,13 +210,22 @@ int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* n
       (cfg->dt_mode != HC_DT_GLOBAL && cfg->dt_mode != HC_DT_LOCAL) || !(cfg->cfl > 0) ||
       (cfg->basis != HC_BASIS_PRIMITIVE && cfg->basis != HC_BASIS_CONSERVED))
     return fail(HC_ERR_ARG, "invalid configuration");
-  if (cfg->law != HC_LAW_EULER) return fail(HC_ERR_UNSUPPORTED, "batches hold Euler instances");
+  const bool scalar = cfg->law == HC_LAW_SCALAR;
+  if (cfg->law != HC_LAW_EULER && !scalar) return fail(HC_ERR_ARG, "unknown conservation law");
+  if (scalar && cfg->flux != HC_FLUX_RUSANOV && cfg->flux != HC_FLUX_CENTRAL)
+    return fail(HC_ERR_UNSUPPORTED, "the scalar advection law takes the Rusanov or central flux");
+  if (scalar && cfg->basis != HC_BASIS_PRIMITIVE)
+    return fail(HC_ERR_UNSUPPORTED, "the scalar advection law has one basis (its conserved set)");
   if (!(gamma > 1.0) || !(gas_constant > 0.0) || !(minf > 0.0)) return fail(HC_ERR_ARG, "invalid species");
   for (int k = 0; k < ninst; ++k) {
     if (ni[k] < 3 || nj[k] < 3 || !nodes[k]) return fail(HC_ERR_ARG, "instance " + std::to_string(k) + ": bad mesh");
     const int* t = bc + 4 * k;
     for (int s = 0; s < 4; ++s)
       if (t[s] < HC_BC_PERIODIC || t[s] > HC_BC_WALL) return fail(HC_ERR_ARG, "unknown bc type");
+    if (scalar)
+      for (int s = 0; s < 4; ++s)
+        if (t[s] == HC_BC_WALL || t[s] == HC_BC_ENTROPY)
+          return fail(HC_ERR_UNSUPPORTED, "scalar advection boundaries are periodic, fixed or Riemann");
     if ((t[0] == HC_BC_PERIODIC) != (t[1] == HC_BC_PERIODIC) || (t[2] == HC_BC_PERIODIC) != (t[3] == HC_BC_PERIODIC))
       return fail(HC_ERR_ARG, "periodic sides must come in pairs");
     for (int s = 0; s < 4; ++s)
@@ -211,6 +234,8 @@ int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* n
   }
   hc_batch* b = new hc_batch();
   b->cfg = *cfg;
+  b->scalar = scalar;
+  b->nv = scalar ? 3 : 4;
   b->fp32 = cfg->precision == HC_FP32;
   b->rsz = b->fp32 ? 4 : 8;
   b->ninst = ninst;
@@ -224,7 +249,8 @@ int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* n
       cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(HC_ERR_CUDA, "no CUDA device"));
   b->stream = b->own;
-  cudaError_t pe = b->fp32 ? prepare<float>(cfg->flux) : prepare<double>(cfg->flux);
+  cudaError_t pe = scalar ? (b->fp32 ? prepare_scalar_stage<float>() : prepare_scalar_stage<double>())
+                          : (b->fp32 ? prepare<float>(cfg->flux) : prepare<double>(cfg->flux));
   if (pe != cudaSuccess) return bail(fail(HC_ERR_CUDA, cudaGetErrorString(pe)));
   // offsets
   size_t maxcell = 0;
@@ -276,7 +302,7 @@ int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* n
     for (int s = 0; s < 4; ++s) {
       const int t = bc[4 * k + s];
       if (t == HC_BC_PERIODIC || t == HC_BC_WALL || !ref || !ref[4 * k + s]) continue;
-      const size_t m = size_t(4) * (s < 2 ? nj[k] : ni[k]);
+      const size_t m = size_t(b->nv) * (s < 2 ? nj[k] : ni[k]);  // nv planes in the first nv of the slot's 4
       std::copy(ref[4 * k + s], ref[4 * k + s] + m, gref_h.begin() + b->gref_off[4 * k + s]);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);  // nodes[k] may be reused by the caller
@@ -319,7 +345,7 @@ int hc_batch_set_stream(hc_batch* b, void* stream) {
 int hc_batch_state_upload(hc_batch* b, int k, const double* prim) {
   if (int st = check_b(b)) return st;
   if (k < 0 || k >= b->ninst || !prim) return fail(HC_ERR_ARG, "bad instance or null state");
-  const size_t m = 4 * b->icells(k);
+  const size_t m = size_t(b->nv) * b->icells(k);
   if (b->fp32) {
     HC_CUDA(cudaMemcpyAsync(b->staging, prim, m * 8, cudaMemcpyHostToDevice, b->stream));
     batch_d2r<float><<<512, 256, 0, b->stream>>>(b->staging, (float*)b->q[0] + 4 * b->cell_off[k], m);
@@ -335,7 +361,7 @@ int hc_batch_state_upload(hc_batch* b, int k, const double* prim) {
 int hc_batch_state_download(hc_batch* b, int k, double* prim) {
   if (int st = check_b(b)) return st;
   if (k < 0 || k >= b->ninst || !prim) return fail(HC_ERR_ARG, "bad instance or null output");
-  const size_t m = 4 * b->icells(k);
+  const size_t m = size_t(b->nv) * b->icells(k);
   if (b->fp32) {
     batch_r2d<float><<<512, 256, 0, b->stream>>>((const float*)b->q[0] + 4 * b->cell_off[k], b->staging, m);
     HC_CUDA(cudaGetLastError());

@@ -9,6 +9,8 @@
 struct hc_batch {
   hc_config cfg{};
   bool fp32 = false;
+  bool scalar = false;  // scalar advection instances ({u, v, q}: 3 of the 4 state planes of a slab)
+  int nv = 4;
   size_t rsz = 8;
   int ninst = 0;
   std::vector<int> ni, nj, bc;

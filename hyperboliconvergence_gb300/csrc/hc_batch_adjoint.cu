@@ -12,9 +12,11 @@
 // global dt), frozen at the forward run's values; J and the rates are FP64.
 //
 // Objective: the weighted L2 distance of each instance's final state to its own
-// target.  Supported as for the single-mesh adjoint: Euler law, Roe or Rusanov,
-// NoLimit1/2/3, van Albada, MinMod, van Leer; periodic, fixed and wall boundaries;
-// global timestep; HC_FP64 and HC_FP32 batches.
+// target.  Supported as for the single-mesh adjoint: Euler law (Roe or Rusanov;
+// periodic, fixed and wall boundaries) and scalar advection (Rusanov or central;
+// periodic and fixed boundaries); NoLimit1/2/3, van Albada, MinMod, van Leer; global
+// timestep; HC_FP64 and HC_FP32 batches.  Scalar batches keep the pools' Euler slab
+// layout (4 state planes per cell) and use their first 3 planes.
 #include "hc_adjoint_driver.cuh"
 #include "hc_batch.h"
 
@@ -74,7 +76,10 @@ template <class R> struct BAdj : AdjCommon {
 // the max rates of step `step`
 template <class R> int forward_step(BAdj<R>& A, int step, bool rec) {
   hc_batch* b = A.b;
-  const BatchFn<R> fn = batch_fn<R>(b->cfg.flux);
+  const BatchFn<R> euler_fn = batch_fn<R>(b->cfg.flux);
+  auto fn = [b, euler_fn](const BatchArgs<R>& a, int tile, int grid, cudaStream_t st) -> cudaError_t {
+    return b->scalar ? launch_scalar_batch_stage<R>(a, b->cfg.flux, tile, grid, st) : euler_fn(a, tile, grid, st);
+  };
   // every tile a CTA: the stage launcher caps the persistent grid at full residency
   const int grid = std::max(1, b->nwork);
   const int tile = b->sched.tile;
@@ -104,7 +109,11 @@ template <class R> int forward_step(BAdj<R>& A, int step, bool rec) {
         HC_CUDA(fn(a, tile, grid, A.s()));
       }
       a.q_out = A.sq[1];
-      HC_CUDA(launch_batch_update0<R>(a, tile, grid, b->cfg.cfl, R(A.tab.alpha[0][0]), R(A.tab.beta[0]), A.s()));
+      if (b->scalar)
+        HC_CUDA(launch_scalar_batch_update0<R>(a, tile, grid, b->cfg.cfl, R(A.tab.alpha[0][0]), R(A.tab.beta[0]),
+                                               A.s()));
+      else
+        HC_CUDA(launch_batch_update0<R>(a, tile, grid, b->cfg.cfl, R(A.tab.alpha[0][0]), R(A.tab.beta[0]), A.s()));
       A.launches += 2;
     } else {
       a.mode = MODE_FUSED_GLOBAL;
@@ -127,19 +136,29 @@ int residual_adjoint(BAdj<R>& A, const R* q, const R* rbar, const R* qbar_add, R
   a.qbar_add = qbar_add;
   a.seg = A.seg_c;
   a.nseg = A.ninst;
-  adj_qm_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
   AdjBatchArgs<R> af = a;
   af.seg = A.seg_f;
   af.nseg = 2 * A.ninst;
-  adj_face_batch_kernel<R, FK><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
-  adj_qmbar_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
-  adj_gather_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
+  if (A.b->scalar) {
+    if constexpr (FK == FLUX_RUSANOV || FK == FLUX_CENTRAL) {
+      adj_qm_batch_kernel<R, 3><<<A.blocks_c, 256, 0, A.s()>>>(a);
+      adj_face_scalar_batch_kernel<R, FK><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
+      adj_qmbar_batch_kernel<R, 3><<<A.blocks_c, 256, 0, A.s()>>>(a);
+      adj_gather_batch_kernel<R, 3><<<A.blocks_c, 256, 0, A.s()>>>(a);
+    }
+  } else if constexpr (FK != FLUX_CENTRAL) {
+    adj_qm_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
+    adj_face_batch_kernel<R, FK><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
+    adj_qmbar_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
+    adj_gather_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
+  }
   A.launches += 4;
   HC_CUDA(cudaGetLastError());
   return HC_OK;
 }
 
 template <class R> int res_adj(BAdj<R>& A, const R* q, const R* rbar, const R* add, R* out) {
+  if (A.b->scalar && A.b->cfg.flux == HC_FLUX_CENTRAL) return residual_adjoint<R, FLUX_CENTRAL>(A, q, rbar, add, out);
   if (A.b->cfg.flux == HC_FLUX_ROE) return residual_adjoint<R, FLUX_ROE>(A, q, rbar, add, out);
   return residual_adjoint<R, FLUX_RUSANOV>(A, q, rbar, add, out);
 }
@@ -170,7 +189,8 @@ template <class R> int adjoint_step(BAdj<R>& A, int step) {
     u.beta = A.tab.beta[s];
     u.cfl = A.b->cfg.cfl;
     u.rates = A.rates + size_t(step) * A.ninst;
-    adj_update_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(u);
+    if (A.b->scalar) adj_update_lin_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(u);
+    else adj_update_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(u);
     A.launches += 1;
     HC_CUDA(cudaGetLastError());
     if (int st = res_adj<R>(A, A.sq[s], A.rbar[s], s == 0 ? A.q0bar : nullptr, A.qbs)) return st;
@@ -182,13 +202,13 @@ template <class R> int adjoint_step(BAdj<R>& A, int step) {
 
 template <class R>
 __global__ void l2_batch_kernel(const BatchInst* inst, const int* seg, int nseg, const R* q, const R* t, double w0,
-                                double w1, double w2, double w3, R* part, int mode_grad, R* lam) {
+                                double w1, double w2, double w3, R* part, int mode_grad, R* lam, int nv) {
   const int s = find_segment(seg, nseg, int(blockIdx.x));
   const BatchInst& in = inst[s];
   const long long c4 = 4 * in.cell;
   const size_t c = size_t(int(blockIdx.x) - seg[s]) * blockDim.x + threadIdx.x;
   l2_cell(q + c4, t + c4, size_t(in.ni) * in.nj, w0, w1, w2, w3, part ? part + in.cell : nullptr, mode_grad,
-          lam ? lam + c4 : nullptr, c);
+          lam ? lam + c4 : nullptr, c, nv);
 }
 // acc[k] += the sum of instance k's part values (one block per instance, the order
 // of the single-mesh sum)
@@ -201,7 +221,7 @@ template <class R> int l2_objective(BAdj<R>& A, bool grad) {
   const double* w = A.obj.weight;
   l2_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(A.b->inst_d, A.seg_c, A.ninst, A.sq[0], A.target, w[0], w[1],
                                                      w[2], w[3], grad ? nullptr : A.part, grad ? 1 : 0,
-                                                     grad ? A.lam : nullptr);
+                                                     grad ? A.lam : nullptr, A.b->nv);
   A.launches += 1;
   if (!grad) {
     sum_batch_kernel<R><<<A.ninst, 256, 0, A.s()>>>(A.b->inst_d, A.part, A.jacc);
@@ -213,8 +233,13 @@ template <class R> int l2_objective(BAdj<R>& A, bool grad) {
 
 inline int check_batch_support(hc_batch* b) {
   if (b->cfg.basis != HC_BASIS_PRIMITIVE) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the primitive basis");
-  if (b->cfg.flux != HC_FLUX_ROE && b->cfg.flux != HC_FLUX_RUSANOV)
+  if (b->scalar) {
+    for (int t : b->bc)
+      if (t != HC_BC_PERIODIC && t != HC_BC_FIXED)
+        return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports periodic and fixed boundaries");
+  } else if (b->cfg.flux != HC_FLUX_ROE && b->cfg.flux != HC_FLUX_RUSANOV) {
     return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");
+  }
   const int l = b->cfg.limiter;
   if (!(l == HC_LIM_NOLIMIT1 || l == HC_LIM_NOLIMIT2 || l == HC_LIM_NOLIMIT3 || l == HC_LIM_VANALBADA ||
         l == HC_LIM_MINMOD || l == HC_LIM_VANLEER))
@@ -281,8 +306,9 @@ int batch_setup(BAdj<R>& A, hc_batch* b, int nsteps, int nsnap, const hc_objecti
   if (int st = A.alloc(&A.part, A.n)) return st;
   if (int st = A.alloc(&A.target, n4)) return st;
   // targets through the batch's FP64 staging buffer (one instance at a time)
+  if (b->scalar) HC_CUDA(cudaMemsetAsync(A.target, 0, n4 * sizeof(R), A.s()));
   for (int k = 0; k < A.ninst; ++k) {
-    const size_t m = 4 * b->icells(k);
+    const size_t m = size_t(b->nv) * b->icells(k);
     HC_CUDA(cudaMemcpyAsync(b->staging, targets[k], m * sizeof(double), cudaMemcpyHostToDevice, A.s()));
     convert_kernel<R><<<512, 256, 0, A.s()>>>(b->staging, A.target + 4 * b->cell_off[k], m);
     HC_CUDA(cudaGetLastError());
@@ -342,7 +368,7 @@ int batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_obje
   if (q0_bar) {
     for (int k = 0; k < A.ninst; ++k) {
       if (!q0_bar[k]) continue;
-      const size_t m = 4 * b->icells(k);
+      const size_t m = size_t(b->nv) * b->icells(k);
       const R* src = A.lam + 4 * b->cell_off[k];
       if constexpr (std::is_same<R, double>::value) {
         HC_CUDA(cudaMemcpy(q0_bar[k], src, m * sizeof(double), cudaMemcpyDeviceToHost));

@@ -32,6 +32,12 @@ template <class R> cudaError_t launch_scalar_stage(const StageArgs<R>& a, int fl
 template <class R>
 cudaError_t launch_scalar_update0(int ni, int nj, const R* q0, const R* res0, const R* vol, R alpha00, R beta0,
                                   double cfl, StepInfo* info, R* q_out, int advance_time, cudaStream_t s);
+// batches of scalar-law instances (pools as for the Euler batch)
+template <class R>
+cudaError_t launch_scalar_batch_stage(const BatchArgs<R>& b, int flux, int tile, int grid, cudaStream_t s);
+template <class R>
+cudaError_t launch_scalar_batch_update0(const BatchArgs<R>& b, int tile, int grid, double cfl, R alpha00, R beta0,
+                                        cudaStream_t s);
 
 inline void tile_dims(int tile, int* ti, int* tj) {
   switch (tile) {

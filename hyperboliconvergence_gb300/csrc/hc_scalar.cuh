@@ -309,4 +309,61 @@ __global__ void scalar_update0_kernel(int ni, int nj, const R* __restrict__ q0, 
   }
 }
 
+// ---- batched path (a batch of scalar-law instances; pools and work list as for the
+// Euler batch, hc_kernels.cuh): each instance's slabs hold 4 state planes of which
+// the law uses 3, and 5 residual planes of which it uses 4
+template <class R, int NT> struct ScalarBatchResidency {
+  static constexpr int value = (sizeof(R) == 4 ? 1024 : 512) / NT;
+};
+
+template <int TI, int TJ, class R, int FK>
+__global__ void __launch_bounds__(TI * TJ, (ScalarBatchResidency<R, TI * TJ>::value))
+    batch_scalar_stage_kernel(const BatchArgs<R> b) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ StageArgs<R> sa;
+  __shared__ int tile_ij[2];
+  for (int w = blockIdx.x; w < b.nwork; w += gridDim.x) {
+    __syncthreads();  // the previous work item may still read shared memory
+    if (threadIdx.x == 0) {
+      const int packed = b.order[w];
+      const int k = packed >> 16, t = packed & 0xffff;
+      const int tj = b.inst[k].tiles_j;
+      sa = instance_args(b, k);
+      tile_ij[0] = t / tj;
+      tile_ij[1] = t % tj;
+    }
+    __syncthreads();
+    scalar_stage_tile<TI, TJ, R, FK>(sa, tile_ij[0], tile_ij[1], smem_raw);
+  }
+}
+
+// Stage-0 update of a scalar-law batch with each instance's own global dt
+// (scalar_update0_kernel per work item)
+template <int TI, int TJ, class R>
+__global__ void __launch_bounds__(TI * TJ)
+    batch_scalar_update0_kernel(const BatchArgs<R> b, double cfl, R alpha00, R beta0) {
+  for (int w = blockIdx.x; w < b.nwork; w += gridDim.x) {
+    const int packed = b.order[w];
+    const int k = packed >> 16, t = packed & 0xffff;
+    const BatchInst& in = b.inst[k];
+    StepInfo* info = b.info + k;
+    const R dt = global_dt<R>(info, cfl);
+    if (t == 0 && threadIdx.x == 0) {
+      info->dt = double(dt);
+      info->t += double(dt);
+    }
+    const int bi = t / in.tiles_j, bj = t % in.tiles_j;
+    const int gi = bi * TI + int(threadIdx.x) / TJ, gj = bj * TJ + int(threadIdx.x) % TJ;
+    if (gi >= in.ni || gj >= in.nj) continue;
+    const size_t ncell = size_t(in.ni) * in.nj;
+    const size_t c = size_t(gi) * in.nj + gj;
+    const R* q0 = b.q0 + 4 * in.cell;
+    const R* res0 = b.res_out + 5 * in.cell;
+    R* q_out = b.q_out + 4 * in.cell;
+    const R fac = (beta0 * dt) / b.vol[in.cell + c];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) q_out[v * ncell + c] = q0[v * ncell + c] + (R(0) + alpha00 * res0[v * ncell + c]) * fac;
+  }
+}
+
 }  // namespace hc

@@ -349,7 +349,9 @@ typedef struct {
 int hc_set_tile(hc_ctx* ctx, int tile);
 
 /* ninst meshes; nodes[k] as for hc_mesh_upload; bc[4k..4k+3] and ref[4k..4k+3]
- * as for hc_set_bcs (ref entries may be NULL where hc_set_bcs allows it). */
+ * as for hc_set_bcs (ref entries may be NULL where hc_set_bcs allows it).  cfg->law
+ * HC_LAW_SCALAR: scalar advection instances (Rusanov or central flux; periodic, fixed
+ * or Riemann sides; states and reference layers of 3 planes {u, v, q}). */
 int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* nj, const double* const* nodes,
                     const int* bc, const double* const* ref, double gamma, double gas_constant, double minf,
                     hc_batch** out);
