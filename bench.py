@@ -458,11 +458,13 @@ def measure_adjoint(nsteps: int = 400, snapshots: int = 20):
 
 
 def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int = 20, seed: int = 2027,
-                            compare: int = 8):
-    """Batched and differentiated case: `ninst` periodic Euler instances on [0,1]^2,
-    n x n cells with n drawn from {128, 192, ..., 1024}, density = 5 plus 8 seeded
+                            compare: int = 8, law: str = "euler"):
+    """Batched and differentiated case: `ninst` periodic instances on [0,1]^2, n x n
+    cells with n drawn from {128, 192, ..., 1024}.  Euler: density = 5 plus 8 seeded
     Gaussians (widths 0.02..0.2, amplitudes -0.5..0.5) on u = 0.5, v = 0.25, p = 1;
-    Rusanov with NoLimit3 reconstruction (smooth, so FP32 and FP64 differentiate the
+    scalar advection (law="scalar"): the scalar = 1 plus 8 such Gaussians, advected by
+    a seeded constant velocity per instance (|u|, |v| <= 1).  Rusanov with NoLimit3
+    reconstruction (smooth, so FP32 and FP64 differentiate the
     same branches), ssp34, global dt, CFL 0.5.  L2 loss of each instance's state after
     `nsteps` steps against its own seeded target; gradient with respect to every
     instance's initial state in FP32 from one batched adjoint (hc_batch_adjoint_gradient:
@@ -478,12 +480,18 @@ def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int =
     sizes = [int(n) for n in rng.choice(np.arange(128, 1025, 64), ninst)]
     base = (0.5, 0.25, 5.0, 1.0)
     insts, targets = [], []
-    sp = None
+    sp = (1.4, 287.058, 0.3)
     for n in sizes:
-        mesh, bc, ref, q, sp = cases.gaussian_sum(n, n, rng, base=base)
-        insts.append((mesh, bc, ref, q))
-        targets.append(cases.gaussian_sum(n, n, rng, base=base)[3])
-    kw = dict(flux="rusanov", limiter="nolimit3", rk="ssp34", dt="global", cfl=0.5, species=sp)
+        if law == "scalar":
+            vel = rng.uniform(-1.0, 1.0, 2)
+            mesh, bc, ref, q = cases.scalar_gaussian_sum(n, n, rng, velocity=vel)
+            insts.append((mesh, bc, ref, q))
+            targets.append(cases.scalar_gaussian_sum(n, n, rng, velocity=vel)[3])
+        else:
+            mesh, bc, ref, q, sp = cases.gaussian_sum(n, n, rng, base=base)
+            insts.append((mesh, bc, ref, q))
+            targets.append(cases.gaussian_sum(n, n, rng, base=base)[3])
+    kw = dict(flux="rusanov", limiter="nolimit3", rk="ssp34", dt="global", cfl=0.5, species=sp, law=law)
     kmin = int(np.argmin(sizes))
     t0 = time.perf_counter()
     bt = Batch(insts, precision="fp32", **kw)
@@ -512,7 +520,8 @@ def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int =
     sub = Batch(insts[:compare], precision="fp32", **kw)
     sub_ms = sub.gradient(nsteps, targets[:compare], snapshots=snapshots, want=[])[2].ms_total
     sub.close()
-    return {"workload": f"{ninst} Gaussian-sum Euler instances, n x n with n in 128..1024, L2 loss after "
+    what = "scalar-advection" if law == "scalar" else "Euler"
+    return {"workload": f"{ninst} Gaussian-sum {what} instances, n x n with n in 128..1024, L2 loss after "
                         f"{nsteps} ssp34 steps, {snapshots} snapshots, FP32, one batched adjoint",
             "cells": cells, "forward_ms": fwd_ms, "reverse_ms": rev_ms, "wall_s": wall,
             "recompute_ms": st.ms_recompute, "kernel_launches": int(st.kernel_launches),
@@ -666,7 +675,8 @@ def run_gpu(args):
                              ("variants", lambda: measure_variants(stream)),
                              ("developed", lambda: measure_developed(stream)),
                              ("adjoint", measure_adjoint),
-                             ("batched_adjoint", measure_batched_adjoint)):
+                             ("batched_adjoint", measure_batched_adjoint),
+                             ("batched_adjoint_scalar", lambda: measure_batched_adjoint(law="scalar"))):
                 if name in extras:
                     try:
                         line[name] = fn()
@@ -688,9 +698,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP32, double-float, batched and adjoint measurements beside the headline")
-    ap.add_argument("--extras", default="fp32,fp64_df,batched,variants,developed,adjoint,batched_adjoint",
+    ap.add_argument("--extras", default="fp32,fp64_df,batched,variants,developed,adjoint,batched_adjoint,batched_adjoint_scalar",
                     help="comma-separated subset of fp32,fp64_df,batched,variants,developed,adjoint,"
-                         "batched_adjoint to measure beside the headline")
+                         "batched_adjoint,batched_adjoint_scalar to measure beside the headline")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
