@@ -9,7 +9,8 @@
 //
 // Objectives: time-averaged wall force (drag) over steps 1..N, or a weighted
 // L2 distance of the final state to a target.  Supported: Euler law (HC_FP64,
-// HC_FP64_DF and HC_FP32 contexts; Roe or Rusanov flux; periodic / fixed /
+// HC_FP64_DF and HC_FP32 contexts; Roe or Rusanov flux reversed by hand, SLAU,
+// AUSM+up and RoeUnprecWS by tangents (not double-float); periodic / fixed /
 // inviscid-wall boundaries) and the scalar advection law (HC_FP64 and HC_FP32;
 // Rusanov or central flux; periodic / fixed boundaries; the L2 objective); limiters
 // NoLimit1/2/3, van Albada, MinMod, van Leer; global timestep.  hc_adjoint.cu instantiates R = double and the C ABI,
@@ -28,6 +29,9 @@
 
 namespace hc {
 namespace adj {
+
+// residual_adjoint's flux parameter for the fluxes reversed by tangents (the context's flux)
+constexpr int FLUX_BY_TANGENT = -1;
 
 // buffers and recomputation timing shared by the single-mesh and batched drivers
 struct AdjCommon {
@@ -245,6 +249,9 @@ int residual_adjoint(Adj<R>& A, const R* q, const R* rbar, const R* qbar_add, R*
   if constexpr (FK == FLUX_CENTRAL) return fail(HC_ERR_UNSUPPORTED, "the Euler adjoint has no central flux");
   adj_qm_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
   if constexpr (FK == FLUX_CENTRAL) {
+  } else if constexpr (FK == FLUX_BY_TANGENT) {
+    HC_CUDA(launch_adj_face_tangent<R>(A.c->cfg.flux, a, 0, face_blocks(A.nfi), kFaceThreads, A.s()));
+    HC_CUDA(launch_adj_face_tangent<R>(A.c->cfg.flux, a, 1, face_blocks(A.nfj), kFaceThreads, A.s()));
   } else if constexpr (std::is_same<R, double>::value) {
     if (A.c->df) {  // double-float face arithmetic on HC_FP64_DF contexts
       adj_face_kernel<double, FK, df64><<<face_blocks(A.nfi), kFaceThreads, 0, A.s()>>>(a, 0);
@@ -268,6 +275,7 @@ template <class R> int res_adj(Adj<R>& A, const R* q, const R* rbar, const R* ad
   if (A.c->scalar && A.c->cfg.flux == HC_FLUX_CENTRAL)
     return residual_adjoint<R, FLUX_CENTRAL>(A, q, rbar, add, out, obj, sc);
   if (A.c->cfg.flux == HC_FLUX_ROE) return residual_adjoint<R, FLUX_ROE>(A, q, rbar, add, out, obj, sc);
+  if (flux_by_tangent(A.c->cfg.flux)) return residual_adjoint<R, FLUX_BY_TANGENT>(A, q, rbar, add, out, obj, sc);
   return residual_adjoint<R, FLUX_RUSANOV>(A, q, rbar, add, out, obj, sc);
 }
 
@@ -465,8 +473,10 @@ inline int check_support(hc_ctx* c, const hc_objective* obj) {
         return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports periodic and fixed boundaries");
   }
   if (c->cfg.basis != HC_BASIS_PRIMITIVE) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the primitive basis");
-  if (!c->scalar && c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV)
-    return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");
+  if (!c->scalar && c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV && !flux_by_tangent(c->cfg.flux))
+    return fail(HC_ERR_UNSUPPORTED, "the Euler adjoint supports the Roe, Rusanov, SLAU, AUSM+up and RoeUnprecWS fluxes");
+  if (c->df && c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV)
+    return fail(HC_ERR_UNSUPPORTED, "the double-float adjoint supports the Roe and Rusanov fluxes");
   const int l = c->cfg.limiter;
   if (!(l == HC_LIM_NOLIMIT1 || l == HC_LIM_NOLIMIT2 || l == HC_LIM_NOLIMIT3 || l == HC_LIM_VANALBADA ||
         l == HC_LIM_MINMOD || l == HC_LIM_VANLEER))

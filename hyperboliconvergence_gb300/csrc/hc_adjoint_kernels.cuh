@@ -19,6 +19,7 @@
 
 #include "hc_adjoint.cuh"
 #include "hc_kernels.cuh"
+#include "hc_tangent.cuh"
 
 #include <cfloat>
 
@@ -98,7 +99,8 @@ template <class R, int FK>
 __device__ __forceinline__ void flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql, const R* qr, const R* Fb,
                                          R* qlb, R* qrb) {
   if constexpr (FK == FLUX_ROE) roe_flux_adj(g, nx, ny, A, ql, qr, Fb, qlb, qrb);
-  else rusanov_flux_adj(g, nx, ny, A, ql, qr, Fb, qlb, qrb);
+  else if constexpr (FK == FLUX_RUSANOV) rusanov_flux_adj(g, nx, ny, A, ql, qr, Fb, qlb, qrb);
+  else tangent_flux_adj<R, FK>(g, nx, ny, A, ql, qr, Fb, qlb, qrb);  // SLAU, AUSM+up, RoeUnprecWS
 }
 
 // pass 1: one thread per face of direction dir (0 = i-faces, 1 = j-faces)
@@ -727,6 +729,18 @@ template <class R> __global__ void adj_update_batch_kernel(const AdjUpdateBatch<
                   u.rbar[0] + c4, u.rbar[1] + c4, u.rbar[2] + c4, u.rbar[3] + c4, u.alpha[0], u.alpha[1], u.alpha[2],
                   u.alpha[3], u.stage, R(u.beta * dt), c);
 }
+// Face passes of the Euler fluxes reversed by tangents (flux SLAU, SLAU as written,
+// AUSM+up or RoeUnprecWS), compiled in their own unit (hc_adjoint_tangent.cu)
+template <class R>
+cudaError_t launch_adj_face_tangent(int flux, const AdjArgs<R>& a, int dir, unsigned blocks, int threads,
+                                    cudaStream_t s);
+template <class R>
+cudaError_t launch_adj_face_tangent_batch(int flux, const AdjBatchArgs<R>& b, unsigned blocks, int threads,
+                                          cudaStream_t s);
+inline bool flux_by_tangent(int flux) {
+  return flux == FLUX_SLAU || flux == FLUX_SLAU_REF || flux == FLUX_AUSMPUP || flux == FLUX_ROE_WS;
+}
+
 // the same for a scalar-law batch (the update is linear on the conserved set)
 template <class R> __global__ void adj_update_lin_batch_kernel(const AdjUpdateBatch<R> u) {
   const int s = find_segment(u.seg, u.nseg, int(blockIdx.x));

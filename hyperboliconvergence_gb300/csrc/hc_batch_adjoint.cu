@@ -12,7 +12,8 @@
 // global dt), frozen at the forward run's values; J and the rates are FP64.
 //
 // Objective: the weighted L2 distance of each instance's final state to its own
-// target.  Supported as for the single-mesh adjoint: Euler law (Roe or Rusanov;
+// target.  Supported as for the single-mesh adjoint: Euler law (Roe, Rusanov, SLAU,
+// AUSM+up or RoeUnprecWS;
 // periodic, fixed and wall boundaries) and scalar advection (Rusanov or central;
 // periodic and fixed boundaries); NoLimit1/2/3, van Albada, MinMod, van Leer; global
 // timestep; HC_FP64 and HC_FP32 batches.  Scalar batches keep the pools' Euler slab
@@ -148,7 +149,10 @@ int residual_adjoint(BAdj<R>& A, const R* q, const R* rbar, const R* qbar_add, R
     }
   } else if constexpr (FK != FLUX_CENTRAL) {
     adj_qm_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
-    adj_face_batch_kernel<R, FK><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
+    if constexpr (FK == FLUX_BY_TANGENT)
+      HC_CUDA(launch_adj_face_tangent_batch<R>(A.b->cfg.flux, af, A.blocks_f, kFaceThreads, A.s()));
+    else
+      adj_face_batch_kernel<R, FK><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
     adj_qmbar_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
     adj_gather_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
   }
@@ -160,6 +164,7 @@ int residual_adjoint(BAdj<R>& A, const R* q, const R* rbar, const R* qbar_add, R
 template <class R> int res_adj(BAdj<R>& A, const R* q, const R* rbar, const R* add, R* out) {
   if (A.b->scalar && A.b->cfg.flux == HC_FLUX_CENTRAL) return residual_adjoint<R, FLUX_CENTRAL>(A, q, rbar, add, out);
   if (A.b->cfg.flux == HC_FLUX_ROE) return residual_adjoint<R, FLUX_ROE>(A, q, rbar, add, out);
+  if (!A.b->scalar && flux_by_tangent(A.b->cfg.flux)) return residual_adjoint<R, FLUX_BY_TANGENT>(A, q, rbar, add, out);
   return residual_adjoint<R, FLUX_RUSANOV>(A, q, rbar, add, out);
 }
 
@@ -237,8 +242,8 @@ inline int check_batch_support(hc_batch* b) {
     for (int t : b->bc)
       if (t != HC_BC_PERIODIC && t != HC_BC_FIXED)
         return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports periodic and fixed boundaries");
-  } else if (b->cfg.flux != HC_FLUX_ROE && b->cfg.flux != HC_FLUX_RUSANOV) {
-    return fail(HC_ERR_UNSUPPORTED, "the adjoint supports the Roe and Rusanov fluxes");
+  } else if (b->cfg.flux != HC_FLUX_ROE && b->cfg.flux != HC_FLUX_RUSANOV && !flux_by_tangent(b->cfg.flux)) {
+    return fail(HC_ERR_UNSUPPORTED, "the Euler adjoint supports the Roe, Rusanov, SLAU, AUSM+up and RoeUnprecWS fluxes");
   }
   const int l = b->cfg.limiter;
   if (!(l == HC_LIM_NOLIMIT1 || l == HC_LIM_NOLIMIT2 || l == HC_LIM_NOLIMIT3 || l == HC_LIM_VANALBADA ||

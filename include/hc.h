@@ -285,9 +285,11 @@ int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, d
  * `snapshots` states.  HC_FP64 contexts, HC_FP64_DF contexts (forward, replayed
  * and recomputed steps in double-float stage arithmetic, the face reverse in
  * double-float, the other reverse passes in FP64) or HC_FP32 contexts (FP32
- * throughout; rates, timesteps and J in FP64); Euler law; Roe or Rusanov;
- * NoLimit1/2/3, van Albada, MinMod, van Leer; periodic, fixed and wall
- * boundaries; global timestep.
+ * throughout; rates, timesteps and J in FP64).  Euler law: Roe or Rusanov
+ * reversed by hand, SLAU, SLAU as written, AUSM+up and RoeUnprecWS by forward-mode
+ * tangents of the flux (HC_FP64 and HC_FP32); periodic, fixed and wall boundaries.
+ * Scalar advection: Rusanov or central, periodic and fixed boundaries, L2 objective.
+ * NoLimit1/2/3, van Albada, MinMod, van Leer; global timestep.
  * ------------------------------------------------------------------------- */
 typedef enum { HC_OBJ_DRAG = 0, HC_OBJ_L2 = 1 } hc_objective_kind;
 

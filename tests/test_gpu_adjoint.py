@@ -1,5 +1,6 @@
 """Discrete adjoint: gradients against central finite differences (h = 1e-6,
-relative agreement 1e-6) for every differentiated limiter and both fluxes,
+relative agreement 1e-6) for every differentiated limiter and the hand-reversed fluxes,
+against the dual-number FP64 reference for every Euler flux the adjoint takes,
 checkpointed versus fully stored reversal, fixed-ghost reference gradients, and
 the torch.autograd.Function for dJ/dMach, dJ/dalpha and dJ/dq0."""
 import math
@@ -169,7 +170,7 @@ def test_autograd_mach_alpha():
 def test_unsupported_configuration_is_reported():
     from hyperboliconvergence_gb300 import HCError
     case = cylinder_case()
-    s = make(case, flux="slau")
+    s = make(case, flux="central")
     with pytest.raises(HCError) as e:
         s.gradient(2, snapshots=1, kind="drag", scale=1.0)
     assert e.value.code == 5
@@ -177,7 +178,10 @@ def test_unsupported_configuration_is_reported():
 
 @pytest.mark.parametrize("flux,limiter,rk,kind", [
     ("roe", "nolimit2", "ssp34", "drag"), ("roe", "vanalbada", "ssp34", "drag"), ("roe", "vanleer", "ssp22", "drag"),
-    ("rusanov", "minmod", "ssp33", "drag"), ("roe", "nolimit1", "ssp11", "l2"), ("rusanov", "vanalbada", "ssp34", "l2")])
+    ("rusanov", "minmod", "ssp33", "drag"), ("roe", "nolimit1", "ssp11", "l2"), ("rusanov", "vanalbada", "ssp34", "l2"),
+    # fluxes reversed by tangents (hc_tangent.cuh)
+    ("slau", "vanalbada", "ssp34", "drag"), ("slau_ref", "minmod", "ssp33", "l2"), ("ausmpup", "vanleer", "ssp34", "drag"),
+    ("ausmpup", "nolimit1", "ssp22", "l2"), ("roe_ws", "vanalbada", "ssp34", "drag"), ("roe_ws", "nolimit3", "ssp34", "l2")])
 def test_gradient_matches_fp64_reference(flux, limiter, rk, kind):
     """<gradient, d> against the FP64 reference derivative: the CPU oracle run with
     forward-mode dual numbers (exact, timesteps frozen), along seeded noise in the
@@ -221,3 +225,39 @@ def test_fp32_adjoint_matches_fp64():
     (ja, ga), (jb, gb) = out["fp64"], out["fp32"]
     assert abs(jb - ja) <= 1e-5 * abs(ja)
     assert np.abs(gb - ga).max() <= 1e-3 * np.abs(ga).max()
+
+
+@pytest.mark.parametrize("flux", ["slau", "ausmpup", "roe_ws"])
+def test_tangent_flux_gradient_matches_central_fd(flux):
+    """The tangent-reversed fluxes against central differences of the product's own objective."""
+    case = cylinder_case(seed=4)
+    s = make(case, flux=flux, limiter="vanalbada")
+    q0 = case[3]
+    direction = (q0 - np.array([0.4 * math.cos(0.1), 0.4 * math.sin(0.1), 1.0, 1.0 / GAMMA])[:, None, None])
+    J, fd, ad, st = fd_check(s, q0, 6, "drag", {"scale": 3.0}, direction=direction)
+    assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)
+
+
+def test_tangent_flux_fp32_close_to_fp64():
+    rng = np.random.default_rng(8)
+    mesh, bc, ref, q, sp = cases.gaussian_sum(40, 36, rng, base=(0.5, 0.25, 5.0, 1.0))
+    target = cases.gaussian_sum(40, 36, np.random.default_rng(9), base=(0.5, 0.25, 5.0, 1.0))[3]
+    out = {}
+    for prec in ("fp64", "fp32"):
+        s = Solver(mesh, bc, ref, flux="slau", limiter="nolimit3", rk="ssp34", precision=prec, dt="global",
+                   cfl=0.5, species=sp)
+        s.set_state(q)
+        out[prec] = s.gradient(10, snapshots=3, kind="l2", target=target)[:2]
+    (ja, ga), (jb, gb) = out["fp64"], out["fp32"]
+    assert abs(jb - ja) <= 1e-5 * abs(ja)
+    assert np.abs(gb - ga).max() <= 1e-3 * np.abs(ga).max()
+
+
+def test_double_float_adjoint_rejects_tangent_fluxes():
+    from hyperboliconvergence_gb300 import HCError
+    mesh, bc, ref, q = cylinder_case()
+    s = Solver(mesh, bc, ref, flux="slau", limiter="vanalbada", precision="fp64_df", dt="global",
+               species=(GAMMA, 287.058, 0.4))
+    s.set_state(q)
+    with pytest.raises(HCError, match="double-float"):
+        s.gradient(2, snapshots=1, kind="drag", scale=1.0)

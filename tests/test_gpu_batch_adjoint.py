@@ -39,7 +39,8 @@ def mixed_batch(seed):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-@pytest.mark.parametrize("flux,limiter", [("rusanov", "nolimit3"), ("roe", "vanalbada"), ("roe", "minmod")])
+@pytest.mark.parametrize("flux,limiter", [("rusanov", "nolimit3"), ("roe", "vanalbada"), ("roe", "minmod"),
+                                          ("slau", "vanalbada"), ("ausmpup", "nolimit3"), ("roe_ws", "minmod")])
 def test_batch_adjoint_equals_single_mesh_adjoints(precision, flux, limiter):
     insts, targets = mixed_batch(41)
     nsteps, snaps = 7, 3
@@ -91,6 +92,6 @@ def test_batch_adjoint_unsupported_configurations():
     local = Batch(insts, flux="roe", limiter="vanalbada", precision="fp64", dt="local", species=SP)
     with pytest.raises(Exception, match="global timestep"):
         local.gradient(2, targets)
-    slau = Batch(insts, flux="slau", limiter="vanalbada", precision="fp64", species=SP)
-    with pytest.raises(Exception, match="Roe and Rusanov"):
-        slau.gradient(2, targets)
+    central = Batch(insts, flux="central", limiter="vanalbada", precision="fp64", species=SP)
+    with pytest.raises(Exception, match="Roe, Rusanov, SLAU"):
+        central.gradient(2, targets)
