@@ -16,8 +16,9 @@ template <class R> __host__ __device__ __forceinline__ R sgn(R x) { return x > R
 // primitive state adjoint: (u2, a2, h) -> (u, v, r, p); p and r also pass through
 template <class R> struct StBar { R u, v, r, p, u2, a2, h; };
 
-template <class R> __host__ __device__ __forceinline__ void prim_state_adj(const Gas<R>& g, const R* q, StBar<R>& sb,
-                                                                  R* qbar) {
+// (ir = 1/r given)
+template <class R> __host__ __device__ __forceinline__ void prim_state_adj_ir(const Gas<R>& g, const R* q, R ir,
+                                                                              StBar<R>& sb, R* qbar) {
   // h = a2*gamma1 + 0.5*u2
   sb.a2 += g.gamma1 * sb.h;
   sb.u2 += R(0.5) * sb.h;
@@ -25,7 +26,6 @@ template <class R> __host__ __device__ __forceinline__ void prim_state_adj(const
   sb.u += R(2) * q[0] * sb.u2;
   sb.v += R(2) * q[1] * sb.u2;
   // a2 = gamma*R*t, t = p/(r*R): d a2/dp = gamma/r, d a2/dr = -gamma p/r^2
-  const R ir = R(1) / q[2];
   const R gb = g.gamma * ir * sb.a2;
   sb.p += gb;
   sb.r -= gb * (q[3] * ir);
@@ -33,6 +33,10 @@ template <class R> __host__ __device__ __forceinline__ void prim_state_adj(const
   qbar[1] += sb.v;
   qbar[2] += sb.r;
   qbar[3] += sb.p;
+}
+template <class R> __host__ __device__ __forceinline__ void prim_state_adj(const Gas<R>& g, const R* q, StBar<R>& sb,
+                                                                  R* qbar) {
+  prim_state_adj_ir(g, q, R(1) / q[2], sb, qbar);
 }
 
 // exact flux adjoint, accumulating into the state adjoint of one side
@@ -78,8 +82,10 @@ template <class R> __host__ __device__ __forceinline__ void entropy_fix_adj(R la
 template <class R>
 __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql, const R* qr,
                                              const R* Fbar, R* qlbar, R* qrbar) {
-  const St<R> l = prim_state(g, ql[0], ql[1], ql[2], ql[3]);
-  const St<R> r = prim_state(g, qr[0], qr[1], qr[2], qr[3]);
+  // FP64: the two inverse densities from one division, the sound speeds and their
+  // inverses from reciprocal square roots (as the forward stage computes them)
+  St<R> l, r;
+  basis_state2(g, ql, qr, false, l, r);
   // ---- forward recomputation (reciprocals: l.ir = 1/rL, r.ir = 1/rR, a1 = 1/aa)
   const R z = r.r * l.ir;
   const R cr = sqrt(z);
@@ -92,10 +98,12 @@ __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R n
   const R ka = R(0.5) * (ua * ua + va * va);
   const R ha = wl * l.h + wr * r.h;
   const R a2a = g.gm1 * (ha - ka);
-  const R aa = sqrt(a2a);
+  R aa, a1, al, ial, ar, iar;
+  sqrt_rcp(a2a, aa, a1);
+  sqrt_rcp(l.a2, al, ial);
+  sqrt_rcp(r.a2, ar, iar);
   const R una = nx * ua + ny * va;
   const R unl = nx * l.u + ny * l.v, unr = nx * r.u + ny * r.v;
-  const R al = sqrt(l.a2), ar = sqrt(r.a2);
   const R la1 = una - aa, ll1 = unl - al, lr1 = unr - ar;
   const R la2 = una + aa, ll2 = unl + al, lr2 = unr + ar;
   auto fix = [](R la, R ll, R lr) {
@@ -116,7 +124,6 @@ __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R n
   const R du0 = (c0 - ua * d2) * rho1;
   const R du1 = (c1 - va * d2) * rho1;
   const R dp = cc * g.gm1;
-  const R a1 = R(1) / aa;
   const R X0 = g.gamma * (dp * a1 * a1 - d2) * rho1;
   const R X1 = du0 - dp * rho1 * a1;
   const R X2 = du0 + dp * rho1 * a1;
@@ -195,8 +202,8 @@ __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R n
   aab += la2b - la1b;
   const R unlb = ll1b + ll2b, unrb = lr1b + lr2b;
   const R alb = ll2b - ll1b, arb = lr2b - lr1b;
-  lb.a2 += alb * (R(0.5) / al);
-  rb.a2 += arb * (R(0.5) / ar);
+  lb.a2 += alb * (R(0.5) * ial);
+  rb.a2 += arb * (R(0.5) * iar);
   lb.u += nx * unlb; lb.v += ny * unlb;
   rb.u += nx * unrb; rb.v += ny * unrb;
   uab += nx * unab; vab += ny * unab;
@@ -222,8 +229,8 @@ __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R n
   for (int i = 0; i < 4; ++i) fe[i] = R(0.5) * A * Fbar[i];
   exact_flux_adj(nx, ny, l, fe, lb);
   exact_flux_adj(nx, ny, r, fe, rb);
-  prim_state_adj(g, ql, lb, qlbar);
-  prim_state_adj(g, qr, rb, qrbar);
+  prim_state_adj_ir(g, ql, l.ir, lb, qlbar);
+  prim_state_adj_ir(g, qr, r.ir, rb, qrbar);
 }
 
 // Reverse of rusanov_flux (conservationLaws/base/fluxes/rusanovFlux.ipp:99-147)
@@ -261,6 +268,57 @@ __host__ __device__ __forceinline__ void rusanov_flux_adj(const Gas<R>& g, R nx,
   exact_flux_adj(nx, ny, r, fe, rb);
   prim_state_adj(g, ql, lb, qlbar);
   prim_state_adj(g, qr, rb, qrbar);
+}
+
+// van Albada's value z = ab(a+b)/(a^2+b^2+tiny) and its derivatives along the taken branch
+// for four (a, b) pairs, FP64: 0 with zero derivatives where a b < 0 or a = b = 0 (the
+// formula's own derivatives there); otherwise the four inverse denominators from one
+// division (batched inversion) when every denominator lies in [2^-240, 2^240], one
+// division each when not.  The sign and range tests read the bits on the integer pipe.
+__host__ __device__ __forceinline__ void vanalbada_vg4(const double* a, const double* b, double* z, double* da,
+                                                       double* db) {
+  double den[4], pre[4], iden[4];
+  double acc = 1.0;
+  bool ok = true, any = false;
+  bool on[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const long long bits = f64_bits(a[v] * b[v]);
+    const unsigned long long mag = (unsigned long long)bits << 1;  // magnitude bits
+    // not (a b < 0): a b is +0, -0, positive or NaN (which propagates); and not a = b = 0
+    const bool both_zero = ((unsigned long long)f64_bits(a[v]) << 1) == 0 && ((unsigned long long)f64_bits(b[v]) << 1) == 0;
+    on[v] = (bits >= 0 || mag == 0 || mag > (0x7ff0000000000000ULL << 1)) && !both_zero;
+    den[v] = on[v] ? fma(a[v], a[v], b[v] * b[v]) : 1.0;
+    any = any || on[v];
+    pre[v] = acc;
+    acc = acc * den[v];
+    ok = ok && f64_exp_within(den[v], 240u);
+  }
+  if (!any) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) z[v] = da[v] = db[v] = 0.0;
+    return;
+  }
+  if (ok) {
+    double inv = 1.0 / acc;
+#pragma unroll
+    for (int v = 3; v >= 0; --v) {
+      iden[v] = inv * pre[v];
+      inv = inv * den[v];
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) iden[v] = 1.0 / (den[v] + Lim<double>::tiny());
+  }
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    if (!on[v]) { z[v] = da[v] = db[v] = 0.0; continue; }
+    const double a2 = a[v] * a[v], b2 = b[v] * b[v], ab2 = 2.0 * a[v] * b[v];
+    const double zz = (b[v] * a2 + a[v] * b2) * iden[v];
+    z[v] = zz;
+    da[v] = ((ab2 + b2) - zz * 2.0 * a[v]) * iden[v];
+    db[v] = ((a2 + ab2) - zz * 2.0 * b[v]) * iden[v];
+  }
 }
 
 // derivative of limit(kind, a, b) along the taken branch: *da, *db

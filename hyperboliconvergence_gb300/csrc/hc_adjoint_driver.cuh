@@ -76,6 +76,7 @@ template <class R> struct Adj : AdjCommon {
   R* refbar[4] = {nullptr, nullptr, nullptr, nullptr};
   R* base = nullptr;
   R* snaps = nullptr;
+  R* qnext = nullptr;  // the start state of the step reversed last (the output of the one reversed next)
   int nsnap = 0;
   double* rates = nullptr;   // device, one max-rate per step
   R* wall = nullptr;    // per wall face partial forces
@@ -109,14 +110,16 @@ inline unsigned blocks(size_t n) { return unsigned((n + 255) / 256); }
 constexpr int kFaceThreads = 64;
 inline unsigned face_blocks(size_t n) { return unsigned((n + kFaceThreads - 1) / kFaceThreads); }
 
-// one forward step from sq[0] to sq[nst]; record (rec=true) or replay the max rate of step `step`
-template <class R> int forward_step(Adj<R>& A, int step, bool rec) {
+// one forward step from sq[0] to sq[nst]; record (rec=true) or replay the max rate of step
+// `step`; nstages < nst runs only the first nstages stages (sq[1..nstages])
+template <class R> int forward_step(Adj<R>& A, int step, bool rec, int nstages = -1) {
   hc_ctx* c = A.c;
   const StageFn<R> euler_fn = stage_fn<R>(c->cfg.flux);
   auto fn = [c, euler_fn](const StageArgs<R>& a, int tile, cudaStream_t st) -> cudaError_t {
     return c->scalar ? launch_scalar_stage<R>(a, c->cfg.flux, tile, st) : euler_fn(a, tile, st);
   };
-  for (int s = 0; s < A.nst; ++s) {
+  const int ns = nstages < 0 ? A.nst : nstages;
+  for (int s = 0; s < ns; ++s) {
     StageArgs<R> a = base_args<R>(c);
     a.q = A.sq[s];
     a.q0 = A.sq[0];
@@ -287,8 +290,12 @@ template <class R> double step_dt(const Adj<R>& A, int step) {
 // lam holds the adjoint of q_{step+1}; sq[0] holds q_step.  On return lam holds
 // the adjoint of q_step (objective terms of q_step included).
 template <class R> int adjoint_step(Adj<R>& A, int step) {
-  if (int st = forward_step(A, step, false)) return st;
+  // replay the step's stages but the last: its output q_{step+1} is the start state of
+  // the step reversed before this one, kept in qnext
+  if (int st = forward_step(A, step, false, A.nst - 1)) return st;
   const size_t bytes4 = A.state_values() * sizeof(R);
+  HC_CUDA(cudaMemcpyAsync(A.sq[A.nst], A.qnext, bytes4, cudaMemcpyDeviceToDevice, A.s()));
+  HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], bytes4, cudaMemcpyDeviceToDevice, A.s()));
   for (int k = 0; k < A.nst; ++k) HC_CUDA(cudaMemsetAsync(A.rbar[k], 0, bytes4, A.s()));
   HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
   const double dt = step_dt(A, step);
@@ -518,6 +525,7 @@ template <class R> int setup(Adj<R>& A, hc_ctx* c, int nsteps, int nsnap, const 
     HC_CUDA(cudaMemsetAsync(A.refbar[s], 0, size_t(A.nv) * c->nface(s) * sizeof(R), A.s()));
   }
   if (int st = A.alloc(&A.base, n4)) return st;
+  if (int st = A.alloc(&A.qnext, n4)) return st;
   if (nsnap > 0) if (int st = A.alloc(&A.snaps, size_t(nsnap) * n4)) return st;
   if (int st = A.alloc(&A.rates, size_t(nsteps))) return st;
   if (int st = A.alloc(&A.wall, size_t(std::max(c->ni, c->nj)))) return st;
@@ -608,6 +616,7 @@ int adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective* o
   cudaEventRecord(e0, A.s());
   if (int st = forward_pass(A, rates_in, stores)) return st;
   cudaEventRecord(e1, A.s());
+  HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], A.state_values() * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
   // adjoint of the final state
   if (A.obj.kind == HC_OBJ_DRAG) {
     if (int st = res_adj<R>(A, A.sq[0], nullptr, nullptr, A.lam, true, A.obj.scale / A.nsteps)) return st;

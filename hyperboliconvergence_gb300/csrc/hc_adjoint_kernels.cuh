@@ -148,25 +148,48 @@ __device__ __forceinline__ void adj_face_one(const AdjArgs<R>& a, int dir, int f
         const C wlx = rd(F_WLX), wly = rd(F_WLY), sl = rd(F_SL);
         const C wrx = rd(F_WRX), wry = rd(F_WRY), sr = rd(F_SR);
         C qL[4], qR[4], gc[4], gl[4], gr[4];
+        // FP64 van Albada: values and derivatives of both sides from batched inversions
+        constexpr bool f64 = std::is_same<C, double>::value;
+        const bool vg = f64 && lim == LIM_VANALBADA;
+        C dal[4], dbl[4], dar[4], dbr[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
           const C dq = qr[v] - ql[v];
           gc[v] = dq * idlr;
           gl[v] = (a.qm[(2 * v) * n + cl] * wlx + a.qm[(2 * v + 1) * n + cl] * wly) - dq * sl;
           gr[v] = (a.qm[(2 * v) * n + cr] * wrx + a.qm[(2 * v + 1) * n + cr] * wry) - dq * sr;
-          qL[v] = ql[v] + dl * limit<C>(lim, gc[v], gl[v]);
-          qR[v] = qr[v] - dr * limit<C>(lim, gc[v], gr[v]);
+        }
+        if constexpr (f64) {
+          if (vg) {
+            C zl[4], zr[4];
+            vanalbada_vg4(gc, gl, zl, dal, dbl);
+            vanalbada_vg4(gc, gr, zr, dar, dbr);
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+              qL[v] = ql[v] + dl * zl[v];
+              qR[v] = qr[v] - dr * zr[v];
+            }
+          }
+        }
+        if (!vg) {
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            qL[v] = ql[v] + dl * limit<C>(lim, gc[v], gl[v]);
+            qR[v] = qr[v] - dr * limit<C>(lim, gc[v], gr[v]);
+          }
         }
         C qLb[4] = {C(0), C(0), C(0), C(0)}, qRb[4] = {C(0), C(0), C(0), C(0)};
         flux_adj<C, FK>(g, nx, ny, A, qL, qR, Fb, qLb, qRb);
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
           C da, db;
-          limit_grad<C>(lim, gc[v], gl[v], &da, &db);
+          if (vg) { da = dal[v]; db = dbl[v]; }
+          else limit_grad<C>(lim, gc[v], gl[v], &da, &db);
           const C zlb = dl * qLb[v];
           C gcb = zlb * da;
           const C glb = zlb * db;
-          limit_grad<C>(lim, gc[v], gr[v], &da, &db);
+          if (vg) { da = dar[v]; db = dbr[v]; }
+          else limit_grad<C>(lim, gc[v], gr[v], &da, &db);
           const C zrb = -dr * qRb[v];
           gcb += zrb * da;
           const C grb = zrb * db;

@@ -42,6 +42,7 @@ template <class R> struct BAdj : AdjCommon {
   R* refbar = nullptr;
   R* base = nullptr;
   R* snaps = nullptr;
+  R* qnext = nullptr;  // the start states of the step reversed last
   R* target = nullptr;
   R* part = nullptr;
   double* rates = nullptr;  // [step][instance]
@@ -74,8 +75,8 @@ template <class R> struct BAdj : AdjCommon {
 };
 
 // one forward step of every instance from sq[0] to sq[nst]; record (rec) or replay
-// the max rates of step `step`
-template <class R> int forward_step(BAdj<R>& A, int step, bool rec) {
+// the max rates of step `step`; nstages < nst runs only the first nstages stages
+template <class R> int forward_step(BAdj<R>& A, int step, bool rec, int nstages = -1) {
   hc_batch* b = A.b;
   const BatchFn<R> euler_fn = batch_fn<R>(b->cfg.flux);
   auto fn = [b, euler_fn](const BatchArgs<R>& a, int tile, int grid, cudaStream_t st) -> cudaError_t {
@@ -85,7 +86,8 @@ template <class R> int forward_step(BAdj<R>& A, int step, bool rec) {
   const int grid = std::max(1, b->nwork);
   const int tile = b->sched.tile;
   double* rates = A.rates + size_t(step) * A.ninst;
-  for (int s = 0; s < A.nst; ++s) {
+  const int ns = nstages < 0 ? A.nst : nstages;
+  for (int s = 0; s < ns; ++s) {
     BatchArgs<R> a = batch_args<R>(b);
     a.q = A.sq[s];
     a.q0 = A.sq[0];
@@ -171,8 +173,11 @@ template <class R> int res_adj(BAdj<R>& A, const R* q, const R* rbar, const R* a
 // lam holds the adjoint of every instance's q_{step+1}, sq[0] their q_step; on return
 // lam holds the adjoint of q_step
 template <class R> int adjoint_step(BAdj<R>& A, int step) {
-  if (int st = forward_step(A, step, false)) return st;
+  // the last stage's output is the start state of the step reversed before (qnext)
+  if (int st = forward_step(A, step, false, A.nst - 1)) return st;
   const size_t bytes4 = A.state_values() * sizeof(R);
+  HC_CUDA(cudaMemcpyAsync(A.sq[A.nst], A.qnext, bytes4, cudaMemcpyDeviceToDevice, A.s()));
+  HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], bytes4, cudaMemcpyDeviceToDevice, A.s()));
   for (int k = 0; k < A.nst; ++k) HC_CUDA(cudaMemsetAsync(A.rbar[k], 0, bytes4, A.s()));
   HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
   for (int s = A.nst - 1; s >= 0; --s) {
@@ -304,6 +309,7 @@ int batch_setup(BAdj<R>& A, hc_batch* b, int nsteps, int nsnap, const hc_objecti
   if (int st = A.alloc(&A.refbar, b->ngref)) return st;
   HC_CUDA(cudaMemsetAsync(A.refbar, 0, b->ngref * sizeof(R), A.s()));
   if (int st = A.alloc(&A.base, n4)) return st;
+  if (int st = A.alloc(&A.qnext, n4)) return st;
   if (nsnap > 0) if (int st = A.alloc(&A.snaps, size_t(nsnap) * n4)) return st;
   if (int st = A.alloc(&A.rates, size_t(nsteps) * A.ninst)) return st;
   if (int st = A.alloc(&A.jacc, size_t(A.ninst))) return st;
@@ -359,6 +365,7 @@ int batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_obje
   cudaEventRecord(e0, A.s());
   if (int st = batch_forward_pass(A, stores)) return st;
   cudaEventRecord(e1, A.s());
+  HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], A.state_values() * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
   if (int st = l2_objective(A, true)) return st;  // adjoint of the final states
   if (int st = reverse(A, sched, 0, nsteps, -1, stack, true)) return st;
   cudaEventRecord(e2, A.s());
