@@ -11,7 +11,8 @@
 // L2 distance of the final state to a target.  Supported: Euler law (HC_FP64,
 // HC_FP64_DF and HC_FP32 contexts; Roe or Rusanov flux reversed by hand, SLAU,
 // AUSM+up and RoeUnprecWS by tangents (not double-float); periodic / fixed /
-// inviscid-wall boundaries) and the scalar advection law (HC_FP64 and HC_FP32;
+// inviscid-wall boundaries and, by tangents, Riemann / entropy far fields (not
+// double-float)) and the scalar advection law (HC_FP64 and HC_FP32;
 // Rusanov or central flux; periodic / fixed boundaries; the L2 objective); limiters
 // NoLimit1/2/3, van Albada, MinMod, van Leer; global timestep.  hc_adjoint.cu instantiates R = double and the C ABI,
 // hc_adjoint_f32.cu R = float.
@@ -490,8 +491,8 @@ inline int check_support(hc_ctx* c, const hc_objective* obj) {
     return fail(HC_ERR_UNSUPPORTED, "limiter not differentiated by the adjoint");
   if (c->cfg.dt_mode != HC_DT_GLOBAL) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the global timestep");
   for (int s = 0; s < 4; ++s)
-    if (c->bc[s] == HC_BC_RIEMANN || c->bc[s] == HC_BC_ENTROPY)
-      return fail(HC_ERR_UNSUPPORTED, "the adjoint supports periodic, fixed and wall boundaries");
+    if (c->df && (c->bc[s] == HC_BC_RIEMANN || c->bc[s] == HC_BC_ENTROPY))
+      return fail(HC_ERR_UNSUPPORTED, "the double-float adjoint supports periodic, fixed and wall boundaries");
   return HC_OK;
 }
 

@@ -229,10 +229,19 @@ __device__ __forceinline__ void adj_face_one(const AdjArgs<R>& a, int dir, int f
       gI[3] = -pb;  // pass 2 pairs it with the wall extrapolation weights
     } else if (!a.objective) {
       C Fb[4], qg[4];
+      R qref[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         Fb[v] = int_right ? a.rbar[v * n + ci] : -a.rbar[v * n + ci];
-        qg[v] = a.gref[side][size_t(v) * nfs + kf];  // fixed ghost = reference state
+        qref[v] = a.gref[side][size_t(v) * nfs + kf];
+        qg[v] = qref[v];  // fixed ghost = reference state
+      }
+      const R sgn = int_right ? R(1) : R(-1);  // normal into the domain
+      if constexpr (std::is_same<C, R>::value) {
+        // Riemann / entropy far field: the ghost the forward stage computed from the
+        // interior state and the reference state (in the storage type, as there)
+        if (bct == BC_RIEMANN) farfield_update<R, BC_RIEMANN>(a.gas, sgn * nx, sgn * ny, qi, qref, qg);
+        else if (bct == BC_ENTROPY) farfield_update<R, BC_ENTROPY>(a.gas, sgn * nx, sgn * ny, qi, qref, qg);
       }
       C qLb[4] = {C(0), C(0), C(0), C(0)}, qRb[4] = {C(0), C(0), C(0), C(0)};
       C gb_ref[4] = {C(0), C(0), C(0), C(0)};
@@ -273,6 +282,14 @@ __device__ __forceinline__ void adj_face_one(const AdjArgs<R>& a, int dir, int f
       if (bct == BC_FIXED) {
 #pragma unroll
         for (int v = 0; v < 4; ++v) a.refbar[side][size_t(v) * nfs + kf] += cvt<R>(gb_ref[v]);
+      } else if constexpr (std::is_same<C, R>::value) {
+        // the ghost's adjoint through the far-field update, to the interior cell and the
+        // reference state (forward-mode tangents, hc_tangent.cuh)
+        R rb[4] = {R(0), R(0), R(0), R(0)};
+        if (bct == BC_RIEMANN) farfield_adj<R, BC_RIEMANN>(a.gas, sgn * nx, sgn * ny, qi, qref, gb_ref, dI, rb);
+        else farfield_adj<R, BC_ENTROPY>(a.gas, sgn * nx, sgn * ny, qi, qref, gb_ref, dI, rb);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) a.refbar[side][size_t(v) * nfs + kf] += rb[v];
       }
     }
   }

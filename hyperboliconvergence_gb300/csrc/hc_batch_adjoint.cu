@@ -13,8 +13,8 @@
 //
 // Objective: the weighted L2 distance of each instance's final state to its own
 // target.  Supported as for the single-mesh adjoint: Euler law (Roe, Rusanov, SLAU,
-// AUSM+up or RoeUnprecWS;
-// periodic, fixed and wall boundaries) and scalar advection (Rusanov or central;
+// AUSM+up or RoeUnprecWS; periodic, fixed, wall, Riemann and entropy boundaries) and
+// scalar advection (Rusanov or central;
 // periodic and fixed boundaries); NoLimit1/2/3, van Albada, MinMod, van Leer; global
 // timestep; HC_FP64 and HC_FP32 batches.  Scalar batches keep the pools' Euler slab
 // layout (4 state planes per cell) and use their first 3 planes.
@@ -255,9 +255,7 @@ inline int check_batch_support(hc_batch* b) {
         l == HC_LIM_MINMOD || l == HC_LIM_VANLEER))
     return fail(HC_ERR_UNSUPPORTED, "limiter not differentiated by the adjoint");
   if (b->cfg.dt_mode != HC_DT_GLOBAL) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the global timestep");
-  for (int t : b->bc)
-    if (t == HC_BC_RIEMANN || t == HC_BC_ENTROPY)
-      return fail(HC_ERR_UNSUPPORTED, "the adjoint supports periodic, fixed and wall boundaries");
+
   return HC_OK;
 }
 

@@ -6,8 +6,9 @@
 // tie), |x| has derivative sign(x) and 0 at 0, sqrt has derivative 0 at 0.
 //
 // The discrete adjoint of the fluxes without a hand-written reverse (SLAU, AUSM+up,
-// RoeUnprecWS) is built on it: eight tangent evaluations of a face's flux give the
-// Jacobian's columns, F_bar . dF/dq_k the adjoint of each input.
+// RoeUnprecWS) and of the Riemann and entropy far-field ghosts is built on it: eight
+// tangent evaluations give the Jacobian's columns, F_bar . dF/dq_k the adjoint of each
+// input.
 #pragma once
 
 #include "hc_physics.cuh"
@@ -60,6 +61,16 @@ template <class T> __host__ __device__ __forceinline__ Tan<T> sqrt(Tan<T> x) {
   const T s = sqrt(x.v);
   return {s, s > T(0) ? T(0.5) * x.d / s : T(0)};
 }
+// d(a^b) = b a^(b-1) da + a^b ln(a) db; the terms with a zero tangent are skipped
+template <class T> __host__ __device__ __forceinline__ Tan<T> pow(Tan<T> a, Tan<T> b) {
+  using ::log;
+  using ::pow;
+  const T p = pow(a.v, b.v);
+  T d = T(0);
+  if (a.d != T(0) && a.v != T(0)) d += b.v * (p / a.v) * a.d;
+  if (b.d != T(0) && a.v > T(0)) d += p * log(a.v) * b.d;
+  return {p, d};
+}
 template <class T> __host__ __device__ __forceinline__ bool isfinite(Tan<T> x) {
   using ::isfinite;
   return isfinite(x.v);
@@ -76,14 +87,20 @@ template <class T> struct Lim<Tan<T>> {
 // Reverse of face_flux<R, FK> on two primitive states by eight tangent evaluations:
 // qlb[k] += Fb . dF/dql[k], qrb[k] += Fb . dF/dqr[k] for the four conserved flux
 // components (the spectral radius feeds only the frozen timestep).
-template <class R, int FK>
-__host__ __device__ __forceinline__ void tangent_flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql,
-                                                          const R* qr, const R* Fb, R* qlb, R* qrb) {
+template <class R> __host__ __device__ __forceinline__ Gas<Tan<R>> tan_gas(const Gas<R>& g) {
   using T = Tan<R>;
   Gas<T> gt;
   gt.gamma = T(g.gamma, R(0)); gt.gm1 = T(g.gm1, R(0)); gt.gamma1 = T(g.gamma1, R(0));
   gt.Rgas = T(g.Rgas, R(0)); gt.minf = T(g.minf, R(0)); gt.inv_gamma = T(g.inv_gamma, R(0));
   gt.lref_dt = T(g.lref_dt, R(0)); gt.vscale = g.vscale; gt.pscale = g.pscale;
+  return gt;
+}
+
+template <class R, int FK>
+__host__ __device__ __forceinline__ void tangent_flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql,
+                                                          const R* qr, const R* Fb, R* qlb, R* qrb) {
+  using T = Tan<R>;
+  const Gas<T> gt = tan_gas(g);
   const T tnx(nx, R(0)), tny(ny, R(0)), tA(A, R(0));
 #pragma unroll 1
   for (int k = 0; k < 8; ++k) {
@@ -101,6 +118,32 @@ __host__ __device__ __forceinline__ void tangent_flux_adj(const Gas<R>& g, R nx,
     for (int v = 0; v < 4; ++v) s += Fb[v] * F.f[v].d;
     if (k < 4) qlb[k] += s;
     else qrb[k - 4] += s;
+  }
+}
+
+// Reverse of farfield_update<R, BK> (Riemann or entropy far-field ghost of the primitive
+// basis; (nx, ny) into the domain) by eight tangent evaluations: given gb, the adjoint of
+// the ghost state, qib += gb . dG/dqi and qfb += gb . dG/dqf.
+template <class R, int BK>
+__host__ __device__ __forceinline__ void farfield_adj(const Gas<R>& g, R nx, R ny, const R* qi, const R* qf,
+                                                      const R* gb, R* qib, R* qfb) {
+  using T = Tan<R>;
+  const Gas<T> gt = tan_gas(g);
+  const T tnx(nx, R(0)), tny(ny, R(0));
+#pragma unroll 1
+  for (int k = 0; k < 8; ++k) {
+    T ti[4], tf[4], qb[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      ti[v] = T(qi[v], k == v ? R(1) : R(0));
+      tf[v] = T(qf[v], k == 4 + v ? R(1) : R(0));
+    }
+    farfield_update<T, BK>(gt, tnx, tny, ti, tf, qb);
+    R s = R(0);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) s += gb[v] * qb[v].d;
+    if (k < 4) qib[k] += s;
+    else qfb[k - 4] += s;
   }
 }
 

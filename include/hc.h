@@ -287,7 +287,9 @@ int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, d
  * double-float, the other reverse passes in FP64) or HC_FP32 contexts (FP32
  * throughout; rates, timesteps and J in FP64).  Euler law: Roe or Rusanov
  * reversed by hand, SLAU, SLAU as written, AUSM+up and RoeUnprecWS by forward-mode
- * tangents of the flux (HC_FP64 and HC_FP32); periodic, fixed and wall boundaries.
+ * tangents of the flux (HC_FP64 and HC_FP32); periodic, fixed and wall boundaries,
+ * and Riemann / entropy far fields (their ghost update reversed by tangents; HC_FP64
+ * and HC_FP32).
  * Scalar advection: Rusanov or central, periodic and fixed boundaries, L2 objective.
  * NoLimit1/2/3, van Albada, MinMod, van Leer; global timestep.
  * ------------------------------------------------------------------------- */

@@ -261,3 +261,61 @@ def test_double_float_adjoint_rejects_tangent_fluxes():
     s.set_state(q)
     with pytest.raises(HCError, match="double-float"):
         s.gradient(2, snapshots=1, kind="drag", scale=1.0)
+
+
+@pytest.mark.parametrize("bc1", ["riemann", "entropy"])
+@pytest.mark.parametrize("flux,limiter,rk,kind", [("roe", "vanalbada", "ssp34", "drag"),
+                                                  ("slau", "nolimit2", "ssp33", "l2"),
+                                                  ("rusanov", "minmod", "ssp34", "l2")])
+def test_farfield_gradient_matches_fp64_reference(bc1, flux, limiter, rk, kind):
+    """Riemann-invariant and entropy far fields: the ghost update reversed by tangents,
+    against the dual-number reference in the initial state and the far-field layer."""
+    from oracle import oracle_py
+    mesh, bc, ref, q = cylinder_case(nr=12, nth=32, seed=5)
+    bc = ["wall", bc1, "periodic", "periodic"]
+    s = make((mesh, bc, ref, q), flux, limiter, rk)
+    kw = {"scale": 2.0} if kind == "drag" else {"target": q * 0.98, "weight": (1.0, 0.5, 2.0, 1.0)}
+    J, g, refb, rates, st = s.gradient(10, snapshots=3, kind=kind, **kw)
+    rng = np.random.default_rng(13)
+    dq = rng.standard_normal(q.shape) * 1e-2
+    dref = [None, rng.standard_normal(ref[1].shape) * 1e-2, None, None]
+    okw = dict(kind=kind, flux=flux, limiter=limiter, rk=rk, cfl=0.5, species=(GAMMA, 287.058, 0.4), ref=ref,
+               dq0=dq, dref=dref)
+    if kind == "drag":
+        okw["scale"] = 2.0
+    else:
+        okw["target"], okw["weight"] = kw["target"], kw["weight"]
+    Jo, dJo = oracle_py.objective(mesh.nodes, mesh.ni, mesh.nj, bc, q, 10, **okw)
+    assert abs(J - Jo) <= 1e-12 * abs(Jo)
+    ad = float(np.sum(g * dq) + np.sum(refb[1] * dref[1]))
+    assert abs(ad - dJo) <= 1e-9 * abs(dJo), (ad, dJo)
+    assert np.abs(refb[1]).max() > 0
+
+
+def test_riemann_reference_gradient_matches_fd():
+    case = cylinder_case(seed=2)
+    mesh, _, ref, q = case
+    bc = ["wall", "riemann", "periodic", "periodic"]
+    s = make((mesh, bc, ref, q), limiter="nolimit2")
+    kw = {"target": q * 0.98, "weight": (1.0, 1.0, 1.0, 1.0)}
+    J, g, refb, rates, _ = s.gradient(10, snapshots=3, kind="l2", **kw)
+    d = np.zeros_like(ref[1])
+    d[0] = 0.01
+    d[3] = 0.002
+    s.set_bcs(bc, [None, ref[1] + H * d, None, None]); s.set_state(q)
+    jp, _ = s.objective(10, kind="l2", rates=rates, **kw)
+    s.set_bcs(bc, [None, ref[1] - H * d, None, None]); s.set_state(q)
+    jm, _ = s.objective(10, kind="l2", rates=rates, **kw)
+    fd = (jp - jm) / (2 * H)
+    ad = float(np.sum(refb[1] * d))
+    assert abs(fd - ad) <= 1e-6 * abs(fd), (fd, ad)
+
+
+def test_double_float_adjoint_rejects_farfield():
+    from hyperboliconvergence_gb300 import HCError
+    mesh, _, ref, q = cylinder_case()
+    s = Solver(mesh, ["wall", "riemann", "periodic", "periodic"], ref, flux="roe", limiter="vanalbada",
+               precision="fp64_df", dt="global", species=(GAMMA, 287.058, 0.4))
+    s.set_state(q)
+    with pytest.raises(HCError, match="double-float"):
+        s.gradient(2, snapshots=1, kind="drag", scale=1.0)

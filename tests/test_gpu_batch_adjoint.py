@@ -95,3 +95,33 @@ def test_batch_adjoint_unsupported_configurations():
     central = Batch(insts, flux="central", limiter="vanalbada", precision="fp64", species=SP)
     with pytest.raises(Exception, match="Roe, Rusanov, SLAU"):
         central.gradient(2, targets)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_adjoint_with_farfield_instances(precision):
+    """Instances with Riemann and entropy far fields (the ghost update reversed by
+    tangents): every instance's J and gradient equal its single-mesh adjoint's."""
+    from hyperboliconvergence_gb300.solver import Mesh
+    insts, targets = [], []
+    rng = np.random.default_rng(21)
+    for k, (nr, nth, bc1) in enumerate([(10, 32, "riemann"), (14, 24, "entropy")]):
+        mesh = Mesh.cylinder(nr, nth, 0.5, 4.0, 1.05)
+        qinf = np.array([0.4 * np.cos(0.1), 0.4 * np.sin(0.1), 1.0, 1.0 / 1.4])
+        c = mesh.centres()
+        shape = 0.5 * np.exp(-((c[0] - 1.0) ** 2 + c[1] ** 2)) + 0.1 * c[0] + 0.07 * c[1]
+        q = qinf[:, None, None] + np.array([0.02, 0.02, 0.03, 0.02])[:, None, None] * shape[None]
+        ref = [None, np.broadcast_to(qinf[:, None], (4, nth)).copy(), None, None]
+        insts.append((mesh, ["wall", bc1, "periodic", "periodic"], ref, q))
+        targets.append(q * (1 + 0.01 * rng.standard_normal(q.shape)))
+    sp = (1.4, 287.058, 0.4)
+    bt = Batch(insts, flux="roe", limiter="vanalbada", precision=precision, species=sp)
+    J, grads, _ = bt.gradient(5, targets, snapshots=2)
+    for k, (mesh, bc, ref, q) in enumerate(insts):
+        s = Solver(mesh, bc, ref, flux="roe", limiter="vanalbada", precision=precision, species=sp)
+        s.set_state(q)
+        j1, g1 = s.gradient(5, snapshots=2, kind="l2", target=targets[k])[:2]
+        if precision == "fp64":
+            assert J[k] == j1
+            assert np.array_equal(grads[k], g1)
+        else:
+            assert J[k] == pytest.approx(j1, rel=1e-5)
