@@ -13,7 +13,7 @@
 // AUSM+up and RoeUnprecWS by tangents (not double-float); periodic / fixed /
 // inviscid-wall boundaries and, by tangents, Riemann / entropy far fields (not
 // double-float)) and the scalar advection law (HC_FP64 and HC_FP32;
-// Rusanov or central flux; periodic / fixed boundaries; the L2 objective); limiters
+// Rusanov or central flux; periodic / fixed / Riemann boundaries; the L2 objective); limiters
 // NoLimit1/2/3, van Albada, MinMod, van Leer; global timestep.  hc_adjoint.cu instantiates R = double and the C ABI,
 // hc_adjoint_f32.cu R = float.
 #pragma once
@@ -477,8 +477,8 @@ inline int check_support(hc_ctx* c, const hc_objective* obj) {
       return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports the Rusanov and central fluxes");
     if (obj->kind != HC_OBJ_L2) return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint takes the L2 objective");
     for (int s = 0; s < 4; ++s)
-      if (c->bc[s] != HC_BC_PERIODIC && c->bc[s] != HC_BC_FIXED)
-        return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports periodic and fixed boundaries");
+      if (c->bc[s] != HC_BC_PERIODIC && c->bc[s] != HC_BC_FIXED && c->bc[s] != HC_BC_RIEMANN)
+        return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports periodic, fixed and Riemann boundaries");
   }
   if (c->cfg.basis != HC_BASIS_PRIMITIVE) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the primitive basis");
   if (!c->scalar && c->cfg.flux != HC_FLUX_ROE && c->cfg.flux != HC_FLUX_RUSANOV && !flux_by_tangent(c->cfg.flux))

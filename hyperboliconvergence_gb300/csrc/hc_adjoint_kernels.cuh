@@ -19,6 +19,7 @@
 
 #include "hc_adjoint.cuh"
 #include "hc_kernels.cuh"
+#include "hc_scalar.cuh"
 #include "hc_tangent.cuh"
 
 #include <cfloat>
@@ -335,9 +336,9 @@ __host__ __device__ __forceinline__ void scalar_flux_adj(R nx, R ny, R A, const 
 }
 
 // pass 1 of the scalar law: one thread per face of direction dir.  Interior and
-// periodic faces: flux, limiter and reconstruction reversed; Fixed boundary faces:
-// the interior side reversed and the ghost side's adjoint added to the reference
-// adjoint.  Writes SADJ_FIELDS planes (the Euler layout with three variables).
+// periodic faces: flux, limiter and reconstruction reversed; Fixed and Riemann
+// boundary faces: the interior side reversed and the ghost side's adjoint added to the
+// reference adjoint (or, where the Riemann ghost copied the interior, to the cell's).  Writes SADJ_FIELDS planes (the Euler layout with three variables).
 template <class R, int FK> __device__ __forceinline__ void adj_face_scalar_one(const AdjArgs<R>& a, int dir, int f) {
   const int ni = a.ni, nj = a.nj;
   const size_t n = size_t(ni) * nj;
@@ -405,19 +406,27 @@ template <class R, int FK> __device__ __forceinline__ void adj_face_scalar_one(c
         gR[v] = grb;
       }
     }
-  } else if (a.bc[side] == BC_FIXED) {
+  } else {
     const bool int_right = lo == 0;
     const int ci = idir ? (int_right ? 0 : ni - 1) * nj + j : i * nj + (int_right ? 0 : nj - 1);
     const int kf = idir ? j : i;
     const int nfs = idir ? nj : ni;
     R* dI = int_right ? dR : dL;
     R* gI = int_right ? gR : gL;
-    R Fb[3], qi[3], qg[3];
+    R Fb[3], qi[3], qg[3], qref[3];
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
       Fb[v] = int_right ? a.rbar[v * n + ci] : -a.rbar[v * n + ci];
       qi[v] = a.q[v * n + ci];
-      qg[v] = a.gref[side][size_t(v) * nfs + kf];
+      qref[v] = a.gref[side][size_t(v) * nfs + kf];
+      qg[v] = qref[v];
+    }
+    // Riemann ghost: the reference value on inflow, the interior value on outflow (the
+    // switch itself has no derivative); the ghost's adjoint goes to whichever it copied
+    bool ghost_is_ref = true;
+    if (a.bc[side] == BC_RIEMANN) {
+      const R sgn = int_right ? R(1) : R(-1);  // normal into the domain
+      ghost_is_ref = scalar_riemann_ghost(sgn * nx, sgn * ny, qi, qref, qg);
     }
     R qLb[3] = {R(0), R(0), R(0)}, qRb[3] = {R(0), R(0), R(0)};
     R gb_ref[3] = {R(0), R(0), R(0)};
@@ -455,7 +464,10 @@ template <class R, int FK> __device__ __forceinline__ void adj_face_scalar_one(c
       }
     }
 #pragma unroll
-    for (int v = 0; v < 3; ++v) a.refbar[side][size_t(v) * nfs + kf] += gb_ref[v];
+    for (int v = 0; v < 3; ++v) {
+      if (ghost_is_ref) a.refbar[side][size_t(v) * nfs + kf] += gb_ref[v];
+      else dI[v] += gb_ref[v];
+    }
   }
 #pragma unroll
   for (int k = 0; k < SADJ_FIELDS; ++k) out[size_t(k) * nf + f] = res[k];

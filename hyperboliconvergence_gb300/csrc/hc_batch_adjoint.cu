@@ -15,7 +15,7 @@
 // target.  Supported as for the single-mesh adjoint: Euler law (Roe, Rusanov, SLAU,
 // AUSM+up or RoeUnprecWS; periodic, fixed, wall, Riemann and entropy boundaries) and
 // scalar advection (Rusanov or central;
-// periodic and fixed boundaries); NoLimit1/2/3, van Albada, MinMod, van Leer; global
+// periodic, fixed and Riemann boundaries); NoLimit1/2/3, van Albada, MinMod, van Leer; global
 // timestep; HC_FP64 and HC_FP32 batches.  Scalar batches keep the pools' Euler slab
 // layout (4 state planes per cell) and use their first 3 planes.
 #include "hc_adjoint_driver.cuh"
@@ -245,8 +245,8 @@ inline int check_batch_support(hc_batch* b) {
   if (b->cfg.basis != HC_BASIS_PRIMITIVE) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the primitive basis");
   if (b->scalar) {
     for (int t : b->bc)
-      if (t != HC_BC_PERIODIC && t != HC_BC_FIXED)
-        return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports periodic and fixed boundaries");
+      if (t != HC_BC_PERIODIC && t != HC_BC_FIXED && t != HC_BC_RIEMANN)
+        return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports periodic, fixed and Riemann boundaries");
   } else if (b->cfg.flux != HC_FLUX_ROE && b->cfg.flux != HC_FLUX_RUSANOV && !flux_by_tangent(b->cfg.flux)) {
     return fail(HC_ERR_UNSUPPORTED, "the Euler adjoint supports the Roe, Rusanov, SLAU, AUSM+up and RoeUnprecWS fluxes");
   }

@@ -52,9 +52,9 @@ __device__ __forceinline__ SFlux4<R> scalar_face_flux(R nx, R ny, R A, const R* 
 
 // Riemann ghost value (scalarAdvection/boundary/riemann.ipp): the face-averaged
 // set rotated to the face frame, its velocity projected on the inward normal as
-// written; inflow takes the boundary value, outflow the interior one
+// written; inflow takes the boundary value, outflow the interior one.  Returns inflow.
 template <class R>
-__device__ __forceinline__ void scalar_riemann_ghost(R nx, R ny, const R* qi, const R* qb, R* g) {
+__device__ __forceinline__ bool scalar_riemann_ghost(R nx, R ny, const R* qi, const R* qb, R* g) {
   const R au = qi[0] + R(0.5) * (qb[0] - qi[0]);
   const R av = qi[1] + R(0.5) * (qb[1] - qi[1]);
   const R tx = -ny, ty = nx;
@@ -63,6 +63,7 @@ __device__ __forceinline__ void scalar_riemann_ghost(R nx, R ny, const R* qi, co
   const bool inflow = (nx * rn + ny * rt) > R(0);
 #pragma unroll
   for (int v = 0; v < 3; ++v) g[v] = inflow ? qb[v] : qi[v];
+  return inflow;
 }
 
 template <int TI, int TJ, class R, int FK>

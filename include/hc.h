@@ -290,7 +290,7 @@ int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, d
  * tangents of the flux (HC_FP64 and HC_FP32); periodic, fixed and wall boundaries,
  * and Riemann / entropy far fields (their ghost update reversed by tangents; HC_FP64
  * and HC_FP32).
- * Scalar advection: Rusanov or central, periodic and fixed boundaries, L2 objective.
+ * Scalar advection: Rusanov or central, periodic / fixed / Riemann boundaries, L2 objective.
  * NoLimit1/2/3, van Albada, MinMod, van Leer; global timestep.
  * ------------------------------------------------------------------------- */
 typedef enum { HC_OBJ_DRAG = 0, HC_OBJ_L2 = 1 } hc_objective_kind;
@@ -319,8 +319,8 @@ int hc_objective_forward(hc_ctx* ctx, int nsteps, const hc_objective* obj, const
                          double* rates_out, double* J);
 /* J and its gradient: q0_bar (4 planes of the primitive state) and ref_bar (per side 0..3,
  * 4 planes of nface values, concatenated; zero where the side is not fixed).  Scalar
- * advection contexts (Rusanov or central flux, periodic / fixed sides, HC_OBJ_L2 on the
- * conserved set {u, v, q} with weight[0..2]): 3 planes each. */
+ * advection contexts (Rusanov or central flux, HC_OBJ_L2 on the
+ * conserved set {u, v, q} with weight[0..2]; periodic, fixed or Riemann sides): 3 planes each. */
 int hc_adjoint_gradient(hc_ctx* ctx, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
                         double* q0_bar, double* ref_bar, double* rates_out, hc_adjoint_stats* stats);
 
