@@ -318,9 +318,9 @@ typedef struct {
 int hc_objective_forward(hc_ctx* ctx, int nsteps, const hc_objective* obj, const double* rates_in,
                          double* rates_out, double* J);
 /* J and its gradient: q0_bar (4 planes of the primitive state) and ref_bar (per side 0..3,
- * 4 planes of nface values, concatenated; zero where the side is not fixed).  Scalar
- * advection contexts (Rusanov or central flux, HC_OBJ_L2 on the
- * conserved set {u, v, q} with weight[0..2]; periodic, fixed or Riemann sides): 3 planes each. */
+ * 4 planes of nface values, concatenated; zero where the side is periodic or a wall).
+ * Scalar advection contexts (Rusanov or central flux, HC_OBJ_L2 on the conserved set
+ * {u, v, q} with weight[0..2]; periodic, fixed or Riemann sides): 3 planes each. */
 int hc_adjoint_gradient(hc_ctx* ctx, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
                         double* q0_bar, double* ref_bar, double* rates_out, hc_adjoint_stats* stats);
 
