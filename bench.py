@@ -414,7 +414,7 @@ def measure_variants(stream, steps: int = 10):
     return out
 
 
-def measure_adjoint(nsteps: int = 400, snapshots: int = 20):
+def measure_adjoint(nsteps: int = 400, snapshots: int = 20, precisions=("fp64", "fp64_df")):
     """Differentiated case: 256x512 O-grid (0.5 to 20), M 0.4, Roe + van Albada, ssp34,
     nsteps from uniform freestream; drag coefficient averaged over the steps; gradient
     with respect to every cell's initial state and the far-field state (hence Mach and
@@ -429,7 +429,7 @@ def measure_adjoint(nsteps: int = 400, snapshots: int = 20):
     qinf = np.array([mach * math.cos(alpha), mach * math.sin(alpha), 1.0, 1.0 / 1.4])
     ref = [None, np.broadcast_to(qinf[:, None], (4, nth)).copy(), None, None]
     out = {"workload": f"cylinder O-grid {nr}x{nth}, M{mach}, {nsteps} ssp34 steps, {snapshots} snapshots"}
-    for prec in ("fp64", "fp64_df"):
+    for prec in precisions:
         s = Solver(mesh, ["wall", "fixed", "periodic", "periodic"], ref, flux="roe", limiter="vanalbada",
                    rk="ssp34", precision=prec, dt="global", cfl=0.5, species=(1.4, 287.058, mach))
         s.set_state(np.broadcast_to(qinf[:, None, None], (4, nr, nth)).copy())
@@ -451,9 +451,10 @@ def measure_adjoint(nsteps: int = 400, snapshots: int = 20):
             "adjoint_step_over_forward_step": rev / fwd,
             "adjoint_step_over_forward_step_excl_recompute": (rev - rec) / fwd,
             "forward_steps_total": int(st.forward_steps), "adjoint_steps": int(st.adjoint_steps)}
-    a, b = out["fp64"], out["fp64_df"]
-    out["df_vs_fp64_grad_rel_diff"] = {k: abs(b[k] - a[k]) / max(abs(a[k]), 1e-300)
-                                       for k in ("J_time_avg_cd", "dJ_dmach", "grad_norm_q0")}
+    if "fp64" in out and "fp64_df" in out:
+        a, b = out["fp64"], out["fp64_df"]
+        out["df_vs_fp64_grad_rel_diff"] = {k: abs(b[k] - a[k]) / max(abs(a[k]), 1e-300)
+                                           for k in ("J_time_avg_cd", "dJ_dmach", "grad_norm_q0")}
     return out
 
 
@@ -558,12 +559,25 @@ def run_reference(args):
     return 0
 
 
+def run_adjoint_only(args):
+    """`--adjoint-only`: the config-4 adjoint measurement alone (for profiling its kernels),
+    FP64, with `--adjoint-steps` steps and `--adjoint-snapshots` snapshots; prints one JSON
+    line with that measurement and no headline."""
+    import torch
+    torch.cuda.set_device(0)
+    out = measure_adjoint(args.adjoint_steps, args.adjoint_snapshots, precisions=("fp64",))
+    print(json.dumps({"adjoint_only": True, "adjoint": out}), flush=True)
+    return 0
+
+
 def run_gpu(args):
     import torch
 
     from hyperboliconvergence_gb300 import cases
     from hyperboliconvergence_gb300.solver import Solver
 
+    if args.adjoint_only:
+        return run_adjoint_only(args)
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
     pg = None
@@ -674,7 +688,7 @@ def run_gpu(args):
                              ("batched", lambda: measure_batched(stream)),
                              ("variants", lambda: measure_variants(stream)),
                              ("developed", lambda: measure_developed(stream)),
-                             ("adjoint", measure_adjoint),
+                             ("adjoint", lambda: measure_adjoint(args.adjoint_steps, args.adjoint_snapshots)),
                              ("batched_adjoint", measure_batched_adjoint),
                              ("batched_adjoint_scalar", lambda: measure_batched_adjoint(law="scalar"))):
                 if name in extras:
@@ -696,6 +710,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--adjoint-steps", type=int, default=400, help="RK steps of the adjoint measurement")
+    ap.add_argument("--adjoint-snapshots", type=int, default=20, help="checkpoints of the adjoint measurement")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run only the FP64 adjoint measurement (no headline line), for profiling its kernels")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP32, double-float, batched and adjoint measurements beside the headline")
     ap.add_argument("--extras", default="fp32,fp64_df,batched,variants,developed,adjoint,batched_adjoint,batched_adjoint_scalar",
