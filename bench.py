@@ -629,7 +629,7 @@ def run_gpu(args):
     tpc = profiled_traffic_per_cell()
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": None if tpc is None else tpc * ncell, "peak_source": peak_src,
-            "kernel": "stage_kernel<16,16,double,ROE>", "alg_bytes_per_launch": alg_bytes,
+            "kernel": "stage_kernel<16,16,double,ROE,128 threads>", "alg_bytes_per_launch": alg_bytes,
             "avg_launch_ms": stage_ms}
 
     # end to end through the C ABI with host buffers: upload the state from

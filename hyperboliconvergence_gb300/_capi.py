@@ -120,7 +120,7 @@ class Schedule(C.Structure):
     _fields_ = [("tile", C.c_int), ("ctas_per_sm", C.c_int), ("order", C.c_int), ("ms_per_step", C.c_float)]
 
 
-TILE = {"8x32": 0, "4x32": 1, "16x16": 2}
+TILE = {"8x32": 0, "4x32": 1, "16x16": 2, "16x16/128": 3}
 ORDER = {"natural": 0, "largest_first": 1}
 BATCH_MODE = {"persistent": 0, "per_instance": 1}
 

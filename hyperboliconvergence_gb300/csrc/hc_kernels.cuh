@@ -170,7 +170,7 @@ template <class C, class R> __device__ __forceinline__ Gas<C> gas_as(const Gas<R
 // REC: the recording instantiation also writes each face's branch signature to
 // a.sig_i / a.sig_j (the production instantiations compile without it).  DUAL: dual-time
 // terms are honoured (the batched instantiations, which have none, compile without them).
-template <int TI, int TJ, class R, int FK, class C = R, bool REC = false, bool DUAL = true>
+template <int TI, int TJ, class R, int FK, class C = R, bool REC = false, bool DUAL = true, int NTH = TI * TJ>
 __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj, unsigned char* smem_raw) {
   constexpr bool same = std::is_same<C, R>::value;
   using SM = StageSmem<TI, TJ, C>;
@@ -181,7 +181,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   const C* cfi = same ? reinterpret_cast<const C*>(a.fi) : reinterpret_cast<const C*>(a.fic);
   const C* cfj = same ? reinterpret_cast<const C*>(a.fj) : reinterpret_cast<const C*>(a.fjc);
   constexpr int QI = SM::QI, QJ = SM::QJ, MI = SM::MI, MJ = SM::MJ;
-  constexpr int NT = TI * TJ;
+  constexpr int NT = NTH;  // threads of the block: TI*TJ, or a divisor of it (several cells per thread)
+  static_assert((TI * TJ) % NTH == 0 && NTH % 32 == 0, "threads must divide the tile's cells in whole warps");
   const int ni = a.ni, nj = a.nj;
   const size_t ncell = size_t(ni) * nj;
   const int i0 = bi * TI, j0 = bj * TJ;
@@ -442,8 +443,11 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   }
   __syncthreads();
 
-  // ---- phase 4: accumulate to cells (residualCalc.h:199-253 signs) and update
-  const int la = tid / TJ, lb = tid % TJ;
+  // ---- phase 4: accumulate to cells (residualCalc.h:199-253 signs) and update; with
+  // fewer threads than cells each thread takes cells tid, tid + NT, ... (whole warps per
+  // pass, so the warp reductions below see every lane)
+  auto cell_update = [&](const int cidx) {
+  const int la = cidx / TJ, lb = cidx % TJ;
   const int gi = i0 + la, gj = j0 + lb;
   const bool own = gi < ni && gj < nj;
   R res[4], lam = R(0);
@@ -526,6 +530,9 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
 #pragma unroll
   for (int v = 0; v < 4; ++v) a.q_out[v * ncell + c] = qn[v];
   flag_nonphysical(a.info, qn, int(c));
+  };
+#pragma unroll 1
+  for (int cidx = tid; cidx < TI * TJ; cidx += NT) cell_update(cidx);
 }
 
 // Resident CTAs per SM the stage kernel is compiled for (measured on the 512x1024
@@ -537,11 +544,11 @@ template <class R, class C, int NT> struct StageResidency {
                                : (std::is_same<C, R>::value ? 512 / NT : 768 / NT);
 };
 
-template <int TI, int TJ, class R, int FK, class C = R>
-__global__ void __launch_bounds__(TI * TJ, (StageResidency<R, C, TI * TJ>::value))
+template <int TI, int TJ, class R, int FK, class C = R, int NT = TI * TJ>
+__global__ void __launch_bounds__(NT, (StageResidency<R, C, NT>::value))
     stage_kernel(const StageArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_tile<TI, TJ, R, FK, C>(a, blockIdx.y, blockIdx.x, smem_raw);
+  stage_tile<TI, TJ, R, FK, C, false, true, NT>(a, blockIdx.y, blockIdx.x, smem_raw);
 }
 
 // the recording variant (a diagnostic, not on the stepping path): the same tile with

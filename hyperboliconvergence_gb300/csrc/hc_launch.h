@@ -12,7 +12,8 @@
 namespace hc {
 
 // Tile shapes the stage kernel is built for (cells along i x cells along j).
-enum TileShape { TILE_8x32 = 0, TILE_4x32 = 1, TILE_16x16 = 2, TILE_COUNT = 3 };
+// TILE_16x16_H: 16 x 16 cells run by 128 threads (two cells a thread in the update)
+enum TileShape { TILE_8x32 = 0, TILE_4x32 = 1, TILE_16x16 = 2, TILE_16x16_H = 3, TILE_COUNT = 4 };
 
 template <class R, int FK> cudaError_t launch_stage(const StageArgs<R>& a, int tile, cudaStream_t s);
 template <class R, int FK> cudaError_t prepare_stage();
@@ -42,7 +43,8 @@ cudaError_t launch_scalar_batch_update0(const BatchArgs<R>& b, int tile, int gri
 inline void tile_dims(int tile, int* ti, int* tj) {
   switch (tile) {
     case TILE_4x32: *ti = 4; *tj = 32; break;
-    case TILE_16x16: *ti = 16; *tj = 16; break;
+    case TILE_16x16:
+    case TILE_16x16_H: *ti = 16; *tj = 16; break;
     default: *ti = 8; *tj = 32; break;
   }
 }
@@ -97,16 +99,23 @@ inline void tile_dims(int tile, int* ti, int* tj) {
     const dim3 grid((a.nj + TJ - 1) / TJ, (a.ni + TI - 1) / TI);                                         \
     stage_kernel<TI, TJ, R, FK><<<grid, TI * TJ, StageSmem<TI, TJ, R>::bytes, s>>>(a);                   \
   }                                                                                                      \
+  template <class R> static cudaError_t prep_half() {                                                   \
+    return cudaFuncSetAttribute(stage_kernel<16, 16, R, FK, R, 128>,                                     \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,                             \
+                                int(StageSmem<16, 16, R>::bytes));                                       \
+  }                                                                                                      \
   template <> cudaError_t prepare_stage<double, FK>() {                                                  \
     cudaError_t e = prep_one<double, 8, 32>();                                                           \
     if (e == cudaSuccess) e = prep_one<double, 4, 32>();                                                 \
     if (e == cudaSuccess) e = prep_one<double, 16, 16>();                                                \
+    if (e == cudaSuccess) e = prep_half<double>();                                                       \
     return e;                                                                                            \
   }                                                                                                      \
   template <> cudaError_t prepare_stage<float, FK>() {                                                   \
     cudaError_t e = prep_one<float, 8, 32>();                                                            \
     if (e == cudaSuccess) e = prep_one<float, 4, 32>();                                                  \
     if (e == cudaSuccess) e = prep_one<float, 16, 16>();                                                 \
+    if (e == cudaSuccess) e = prep_half<float>();                                                        \
     return e;                                                                                            \
   }                                                                                                      \
   template <class R> static cudaError_t dispatch(const StageArgs<R>& a, int tile, cudaStream_t s) {     \
@@ -119,7 +128,10 @@ inline void tile_dims(int tile, int* ti, int* tj) {
     }                                                                                                    \
     if (tile == TILE_4x32) go<R, 4, 32>(a, s);                                                           \
     else if (tile == TILE_16x16) go<R, 16, 16>(a, s);                                                    \
-    else go<R, 8, 32>(a, s);                                                                             \
+    else if (tile == TILE_16x16_H) {                                                                     \
+      const dim3 grid((a.nj + 15) / 16, (a.ni + 15) / 16);                                               \
+      stage_kernel<16, 16, R, FK, R, 128><<<grid, 128, StageSmem<16, 16, R>::bytes, s>>>(a);             \
+    } else go<R, 8, 32>(a, s);                                                                           \
     return cudaGetLastError();                                                                           \
   }                                                                                                      \
   template <> cudaError_t launch_stage<double, FK>(const StageArgs<double>& a, int tile, cudaStream_t s) { \

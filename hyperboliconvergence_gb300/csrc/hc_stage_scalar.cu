@@ -53,7 +53,7 @@ template <class R, int TI, int TJ, int FK> void go(const StageArgs<R>& a, cudaSt
 
 template <class R, int FK> void go_tile(const StageArgs<R>& a, int tile, cudaStream_t s) {
   if (tile == TILE_4x32) go<R, 4, 32, FK>(a, s);
-  else if (tile == TILE_16x16) go<R, 16, 16, FK>(a, s);
+  else if (tile == TILE_16x16 || tile == TILE_16x16_H) go<R, 16, 16, FK>(a, s);
   else go<R, 8, 32, FK>(a, s);
 }
 

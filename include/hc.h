@@ -337,7 +337,8 @@ typedef struct hc_batch hc_batch;
 
 typedef enum { HC_BATCH_PERSISTENT = 0, HC_BATCH_PER_INSTANCE = 1 } hc_batch_mode;
 typedef enum { HC_ORDER_NATURAL = 0, HC_ORDER_LARGEST_FIRST = 1 } hc_batch_order;
-typedef enum { HC_TILE_8x32 = 0, HC_TILE_4x32 = 1, HC_TILE_16x16 = 2 } hc_tile;
+/* HC_TILE_16x16_H: 16 x 16 cells run by 128 threads (single-mesh contexts only) */
+typedef enum { HC_TILE_8x32 = 0, HC_TILE_4x32 = 1, HC_TILE_16x16 = 2, HC_TILE_16x16_H = 3 } hc_tile;
 
 typedef struct {
   int tile;         /* hc_tile: cells per CTA tile */
@@ -348,8 +349,9 @@ typedef struct {
 
 /* Tile shape (hc_tile) of a single-mesh context's stage kernels: the FP64 and FP32
  * 2D stage, residual and adjoint-recompute launches (the double-float and 1D kernels
- * keep their own).  Defaults: HC_TILE_16x16 in FP64 (whose 544 faces fill 17 warps of
- * the FP64-bound face phase), HC_TILE_8x32 in FP32.  Every shape gives the same results. */
+ * keep their own).  Defaults: HC_TILE_16x16_H in FP64 (16 x 16 cells, whose 544 faces
+ * fill whole warps, on 128 threads: four CTAs per SM), HC_TILE_8x32 in FP32.  Every shape
+ * gives the same results. */
 int hc_set_tile(hc_ctx* ctx, int tile);
 
 /* ninst meshes; nodes[k] as for hc_mesh_upload; bc[4k..4k+3] and ref[4k..4k+3]

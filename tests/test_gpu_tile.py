@@ -15,7 +15,7 @@ from test_gpu_parity import CASES
 
 pytestmark = pytest.mark.gpu
 
-TILES = ["8x32", "4x32", "16x16"]
+TILES = ["8x32", "4x32", "16x16", "16x16/128"]
 
 
 def run(case, tile, precision="fp64", flux="roe", limiter="vanalbada", dt="local", steps=3):
