@@ -71,6 +71,7 @@ def _declare(lib):
         "hc_step_async": [p, i],
         "hc_sync": [p, C.POINTER(StepStats)],
         "hc_steady_run": [p, C.POINTER(SteadyControls), dp, C.c_longlong, C.POINTER(SteadyStats)],
+        "hc_smooth_1d": [p, i, v, v, C.c_longlong, i, d, i],
         "hc_spectral_radius": [v, v, C.c_longlong, v, v],
         "hc_spectral_radius_noalloc": [v, v, C.c_longlong, v, v],
         "hc_mesh_cylinder_nodes": [i, i, d, d, d, dp],

@@ -46,7 +46,8 @@ namespace {
 void free_buffers(hc_ctx* c) {
   void* ptrs[] = {c->nodes, c->cx, c->cy, c->xm, c->fi64, c->fj64, c->vol64, c->q[0], c->q[1], c->q[2],
                   c->res[0], c->res[1], c->res[2], c->res[3], c->gref[0], c->gref[1], c->gref[2], c->gref[3],
-                  c->staging, c->info};
+                  c->staging, c->info, c->smooth_buf};
+  c->smooth_buf = nullptr;
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->fp32) {
@@ -173,8 +174,55 @@ template <class R> int run_residual_1d(hc_ctx* c) {
   return HC_OK;
 }
 
+// one RK step of the 1D path with residual smoothing (SteadyTimeControls'
+// use_residual_smoothing): per stage the residual alone, its three flux planes smoothed
+// in place by centralImplicitSmoothing with alpha = smoothing_factor (ends 'p' on a
+// periodic line, 'a' otherwise), then the stage update from the smoothed residuals
+template <class R> int run_step_1d_smoothed(hc_ctx* c) {
+  const RKTab tab = rk_table(c->cfg.rk);
+  const int nst = tab.nst;
+  const bool global = c->cfg.dt_mode == HC_DT_GLOBAL;
+  const long long n = c->ni;
+  if (!c->smooth_buf) HC_CUDA(cudaMalloc(&c->smooth_buf, 6 * size_t(n) * sizeof(R)));
+  R* wrk = (R*)c->smooth_buf;
+  R* tmp = wrk + 3 * n;
+  const int ends = c->bc[0] == HC_BC_PERIODIC ? 'p' : 'a';
+  HC_CUDA(cudaMemsetAsync(&c->info->maxrate, 0, sizeof(unsigned long long), c->stream));
+  HC_CUDA(cudaMemsetAsync(&c->info->resnorm2, 0, sizeof(double), c->stream));
+  auto out_of = [&](int s) -> R* { return (R*)((s == nst - 1) ? c->q[0] : c->q[1 + (s % 2)]); };
+  for (int s = 0; s < nst; ++s) {
+    Stage1DArgs<R> a = args_1d<R>(c);
+    a.q = (s == 0) ? (const R*)c->q[0] : out_of(s - 1);
+    a.stage = s;
+    a.res_out = (R*)c->res[s];
+    a.norm_stage0 = (s == 0);
+    a.mode = (s == 0) ? MODE_RES_MAXRATE : MODE_RESIDUAL;  // stage 0: max rate and the norm
+    HC_CUDA(launch_stage1d<R>(a, c->cfg.flux, c->stream));
+    HC_CUDA(launch_smooth_1d<R>(0, (const R*)c->res[s], (R*)c->res[s], wrk, tmp, n, 3, n, c->smooth_alpha, ends,
+                                c->stream));
+    Update1DArgs<R> u{};
+    u.nc = c->ni;
+    u.gas = a.gas;
+    u.q0 = (const R*)c->q[0];
+    for (int k = 0; k <= s; ++k) { u.res[k] = (const R*)c->res[k]; u.alpha[k] = R(tab.alpha[s][k]); }
+    u.stage = s;
+    u.beta = R(tab.beta[s]);
+    u.global = global ? 1 : 0;
+    u.cfl = c->cfg.cfl;
+    u.info = c->info;
+    u.vol = (const R*)c->vol;
+    u.q_out = out_of(s);
+    const unsigned grid = unsigned(std::min<size_t>((c->ncell() + 255) / 256, 152 * 16));
+    update_stage_1d_kernel<R><<<grid, 256, 0, c->stream>>>(u);
+    HC_CUDA(cudaGetLastError());
+    c->launches += 3;
+  }
+  return HC_OK;
+}
+
 // one RK step of the 1D path (the same stage loop as run_step)
 template <class R> int run_step_1d(hc_ctx* c) {
+  if (c->smooth_alpha > 0.0) return run_step_1d_smoothed<R>(c);
   const RKTab tab = rk_table(c->cfg.rk);
   const int nst = tab.nst;
   const bool global = c->cfg.dt_mode == HC_DT_GLOBAL;
@@ -820,8 +868,18 @@ int hc_steady_run(hc_ctx* c, const hc_steady_controls* ctl, double* history, lon
   if (int st = check_ctx(c)) return st;
   if (!ctl || ctl->max_steps < 1 || ctl->check_every < 1 || !(ctl->residual_drop > 0.0))
     return fail(HC_ERR_ARG, "invalid steady controls");
-  if (ctl->use_residual_smoothing)
-    return fail(HC_ERR_UNSUPPORTED, "residual smoothing exists only in the reference's 1D path");
+  if (ctl->use_residual_smoothing) {
+    if (!c->oned) return fail(HC_ERR_UNSUPPORTED, "residual smoothing exists only in the reference's 1D path");
+    if (!(ctl->smoothing_factor >= 1.0) || !std::isfinite(ctl->smoothing_factor))
+      return fail(HC_ERR_ARG, "the smoothing factor must be finite and at least 1");
+    if (c->df) return fail(HC_ERR_UNSUPPORTED, "residual smoothing runs in FP64 or FP32");
+  }
+  // the smoothed stage loop for the duration of the run
+  struct Smooth {
+    hc_ctx* c;
+    ~Smooth() { c->smooth_alpha = 0.0; }
+  } smooth_scope{c};
+  c->smooth_alpha = ctl->use_residual_smoothing ? ctl->smoothing_factor : 0.0;
   hc_steady_stats res{};
   auto record = [&](double r) {
     if (history && res.history_len < history_len) history[res.history_len] = r;
@@ -846,6 +904,25 @@ int hc_steady_run(hc_ctx* c, const hc_steady_controls* ctl, double* history, lon
   }
   if (out) *out = res;
   return st;
+}
+
+// Residual smoothing of the legacy 1D path on device planes (hc_smooth.cu)
+int hc_smooth_1d(hc_ctx* c, int kind, const double* r0_device, double* r1_device, long long n, int nplanes,
+                 double alpha, int ends) {
+  if (int st = check_ctx(c)) return st;
+  if ((kind != HC_SMOOTH_IMPLICIT && kind != HC_SMOOTH_EXPLICIT) || !r0_device || !r1_device || n < 2 ||
+      nplanes < 1 || !(alpha > 0.0) || !std::isfinite(alpha))
+    return fail(HC_ERR_ARG, "invalid smoothing arguments");
+  double* scratch = nullptr;
+  if (kind == HC_SMOOTH_IMPLICIT)
+    HC_CUDA(cudaMallocAsync((void**)&scratch, 2 * size_t(n) * nplanes * sizeof(double), c->stream));
+  const cudaError_t e = launch_smooth_1d<double>(kind, r0_device, r1_device, scratch,
+                                                 scratch ? scratch + size_t(n) * nplanes : nullptr, n, nplanes, n,
+                                                 alpha, ends, c->stream);
+  if (scratch) cudaFreeAsync(scratch, c->stream);
+  HC_CUDA(e);
+  c->launches += 1;
+  return HC_OK;
 }
 
 // make_cylinder_mesh (mesh/generate/twoD.h:223-263) with geometric radial stretching

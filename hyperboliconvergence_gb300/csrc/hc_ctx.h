@@ -23,6 +23,8 @@ struct hc_ctx {
   int vscale = 0, pscale = 0;                       // AUSM+up LowMachScaling pair
   void* dual_src = nullptr;                         // dual time: earlier levels' terms (4 planes, R)
   double dual_g0 = 1.0, dual_b0dt = 0.0;            // dual time: gamma_0 and beta_0 / dt
+  double smooth_alpha = 0.0;                        // 1D residual smoothing factor (0: off)
+  void* smooth_buf = nullptr;                       // its sweep buffers (2 x 3 planes, R)
   cudaStream_t own = nullptr, stream = nullptr;
   int tile = hc::TILE_8x32;
   // device buffers

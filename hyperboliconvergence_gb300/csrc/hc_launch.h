@@ -33,6 +33,12 @@ template <class R> cudaError_t launch_scalar_stage(const StageArgs<R>& a, int fl
 template <class R>
 cudaError_t launch_scalar_update0(int ni, int nj, const R* q0, const R* res0, const R* vol, R alpha00, R beta0,
                                   double cfl, StepInfo* info, R* q_out, int advance_time, cudaStream_t s);
+// residual smoothing of the legacy 1D path (hc_smooth.cu): kind 0 implicit, 1 explicit;
+// nplanes planes of n values at `stride`; implicit smoothing needs wrk and tmp of
+// nplanes * n values and may run in place (r1 == r0); bc 'p', 'a' or other
+template <class R>
+cudaError_t launch_smooth_1d(int kind, const R* r0, R* r1, R* wrk, R* tmp, long long n, int nplanes, long long stride,
+                             double alpha, int bc, cudaStream_t s);
 // batches of scalar-law instances (pools as for the Euler batch)
 template <class R>
 cudaError_t launch_scalar_batch_stage(const BatchArgs<R>& b, int flux, int tile, int grid, cudaStream_t s);

@@ -250,6 +250,56 @@ __global__ void update0_1d_kernel(int nc, Gas<R> g, const R* __restrict__ q0, co
   }
 }
 
+// Stage update of the 1D path from stored stage residuals (the update of the fused
+// stage kernel as a kernel of its own, for residuals changed between the two: residual
+// smoothing).  res[k] holds 4 planes (3 flux sums and lambda) of stage k; global dt: at
+// stage 0 from the recorded max rate (and stored), later stages read it; local dt: the
+// stage-0 lambda.
+template <class R> struct Update1DArgs {
+  int nc;
+  Gas<R> gas;
+  const R* q0;
+  const R* res[4];
+  R alpha[4];
+  int stage;
+  R beta;
+  int global;
+  double cfl;
+  StepInfo* info;
+  const R* vol;
+  R* q_out;
+};
+template <class R> __global__ void update_stage_1d_kernel(const Update1DArgs<R> u) {
+  const size_t n = size_t(u.nc);
+  R dt = R(0);
+  if (u.global) {
+    if (u.stage == 0) {
+      dt = global_dt<R>(u.info, u.cfl);
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        u.info->dt = double(dt);
+        u.info->t += double(dt);
+      }
+    } else {
+      dt = R(u.info->dt);
+    }
+  }
+  for (size_t c = blockIdx.x * size_t(blockDim.x) + threadIdx.x; c < n; c += size_t(gridDim.x) * blockDim.x) {
+    R tot[3] = {R(0), R(0), R(0)};
+    for (int k = 0; k <= u.stage; ++k)
+#pragma unroll
+      for (int v = 0; v < 3; ++v) tot[v] += u.alpha[k] * u.res[k][v * n + c];
+    const R fac = u.global ? (u.beta * dt) / u.vol[c] : (u.beta * R(u.cfl)) / u.res[0][3 * n + c];
+    R q[3], qn[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) q[v] = u.q0[v * n + c];
+    update1(u.gas, q, tot, fac, qn);
+#pragma unroll
+    for (int v = 0; v < 3; ++v) u.q_out[v * n + c] = qn[v];
+    const R chk[4] = {qn[0], R(0), qn[1], qn[2]};
+    flag_nonphysical(u.info, chk, int(c));
+  }
+}
+
 template <class R> cudaError_t launch_stage1d(const Stage1DArgs<R>& a, int flux, cudaStream_t s);
 
 }  // namespace hc

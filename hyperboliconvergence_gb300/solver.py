@@ -297,16 +297,34 @@ class Solver:
         check(self.lib.hc_step(self.h, int(n), C.byref(st)))
         return st
 
-    def steady(self, max_steps: int, residual_drop: float = 1e-10, check_every: int = 100):
+    def steady(self, max_steps: int, residual_drop: float = 1e-10, check_every: int = 100, smoothing=None):
         """Run to a steady state (SteadyTimeControls, controls.h:31-48): steps until the
         stage-0 density-residual L2 norm drops by residual_drop or max_steps; returns
-        (SteadyStats, residual-norm history read every check_every steps)."""
+        (SteadyStats, residual-norm history read every check_every steps).  smoothing
+        (1D meshes): the implicit residual smoothing's alpha (>= 1) applied to every stage's
+        residual (use_residual_smoothing with smoothing_factor = alpha)."""
         from ._capi import SteadyControls, SteadyStats
-        ctl = SteadyControls(int(max_steps), float(residual_drop), int(check_every), 0, 0.0)
+        ctl = SteadyControls(int(max_steps), float(residual_drop), int(check_every), 0 if smoothing is None else 1,
+                             0.0 if smoothing is None else float(smoothing))
         hist = np.empty(int(max_steps) // int(check_every) + 2)
         st = SteadyStats()
         check(self.lib.hc_steady_run(self.h, C.byref(ctl), _dptr(hist), hist.size, C.byref(st)))
         return st, hist[:st.history_len].copy()
+
+    def smooth_1d(self, r, alpha: float, kind: str = "implicit", ends: str = "a") -> np.ndarray:
+        """Residual smoothing of the legacy 1D path (hc_smooth_1d) of each row of r (shape
+        (nplanes, n) or (n,)) on this context's device and stream: kind "implicit" or
+        "explicit", ends "p" (periodic), "a" (one-neighbour) or "n" (unscaled)."""
+        import torch
+        a = np.ascontiguousarray(r, dtype=np.float64)
+        a2 = a.reshape(-1, a.shape[-1])
+        src = torch.from_numpy(a2).cuda()
+        dst = torch.empty_like(src)
+        torch.cuda.synchronize()
+        check(self.lib.hc_smooth_1d(self.h, {"implicit": 0, "explicit": 1}[kind], C.c_void_p(src.data_ptr()),
+                                    C.c_void_p(dst.data_ptr()), a2.shape[1], a2.shape[0], float(alpha), ord(ends)))
+        torch.cuda.synchronize()
+        return dst.cpu().numpy().reshape(a.shape)
 
     def step_async(self, n: int = 1) -> None:
         check(self.lib.hc_step_async(self.h, int(n)))

@@ -179,14 +179,16 @@ int hc_sync(hc_ctx* ctx, hc_step_stats* stats);
  * L2 norm of the stage-0 density residual falls to residual_drop times its value at
  * the first step, or max_steps steps.  The norm is read on the host every
  * check_every steps; history (may be NULL) receives those reads, at most
- * history_len of them.  Residual smoothing exists only in the reference's legacy 1D
- * path: use_residual_smoothing != 0 returns HC_ERR_UNSUPPORTED. */
+ * history_len of them.  use_residual_smoothing (1D contexts, FP64 or FP32): every RK
+ * stage's residual is smoothed by hc_smooth_1d's implicit smoothing with alpha =
+ * smoothing_factor (>= 1; ends periodic on a periodic line, one-neighbour otherwise)
+ * before the stage update; the monitored norm is the unsmoothed stage-0 residual's. */
 typedef struct {
   long long max_steps;        /* nTimesteps */
   double residual_drop;       /* residual_drop */
   int check_every;
   int use_residual_smoothing; /* use_residual_smoothing */
-  double smoothing_factor;    /* smoothing_factor (unused) */
+  double smoothing_factor;    /* smoothing_factor: the smoothing's alpha */
 } hc_steady_controls;
 
 typedef struct {
@@ -199,6 +201,19 @@ typedef struct {
 
 int hc_steady_run(hc_ctx* ctx, const hc_steady_controls* controls, double* history, long long history_len,
                   hc_steady_stats* stats);
+
+/* Residual smoothing of the reference's legacy 1D path (OLD.fieldOperations/
+ * centralImplicitSmoothing.ipp:3-52, centralExplicitSmoothing.ipp:4-37) on device
+ * memory: nplanes planes of n >= 2 values (plane stride n), r1 may equal r0.
+ * HC_SMOOTH_IMPLICIT: four weighted-Jacobi sweeps (omega 2/3) of
+ * (1 - beta delta^2) r1 = r0, beta = (alpha^2 - 1)/4, the result times alpha;
+ * HC_SMOOTH_EXPLICIT: r1 = r0 + gamma delta^2 r0, gamma = ((1 + 4 beta)/alpha - 1)/4.
+ * ends: 'p' periodic line, 'a' ends normalised by their one neighbour, anything else
+ * unscaled (the reference's GridControls1D::boundaryCondition).  Asynchronous on the
+ * context's stream; the implicit sweeps take scratch from the stream-ordered allocator. */
+typedef enum { HC_SMOOTH_IMPLICIT = 0, HC_SMOOTH_EXPLICIT = 1 } hc_smooth_kind;
+int hc_smooth_1d(hc_ctx* ctx, int kind, const double* r0_device, double* r1_device, long long n, int nplanes,
+                 double alpha, int ends);
 
 /* spectralRadius (spatial/spectralRadius.h:19-48): out_device[0] = max over the
  * ncell cells of lambda_sum[c] / vol[c], the fold starting at the smallest

@@ -2,6 +2,7 @@
 //
 // TEST INFRASTRUCTURE ONLY: the product library never links this.
 #include "hc_oracle_1d.hpp"
+#include "hc_oracle_smooth.hpp"
 
 using namespace hco;
 using S1 = Solver1D<double>;
@@ -49,6 +50,17 @@ void hco1_step(void* h, int n, double* out_dt_t) {
   s->step(n);
   out_dt_t[0] = s->last_dt;
   out_dt_t[1] = s->t;
+}
+
+// residual smoothing of the legacy 1D path (hc_oracle_smooth.hpp): nplanes planes of n
+// values each; kind 0 implicit, 1 explicit; bc the reference's end character
+void hco_smooth_1d(int kind, const double* r0, double* r1, long long n, int nplanes, double alpha, int bc) {
+  for (int p = 0; p < nplanes; ++p) {
+    const double* a = r0 + size_t(p) * n;
+    double* b = r1 + size_t(p) * n;
+    if (kind == 0) smooth_implicit_1d(a, b, size_t(n), alpha, char(bc));
+    else smooth_explicit_1d(a, b, size_t(n), alpha, char(bc));
+  }
 }
 
 }  // extern "C"

@@ -499,6 +499,22 @@ def scalar_objective(mesh_nodes, ni, nj, bc, q0, nsteps, target, flux="rusanov",
     return float(out[0]), float(out[1])
 
 
+def smooth_1d(r0, alpha, kind="implicit", ends="a"):
+    """Residual smoothing of the legacy 1D path (hc_oracle_smooth.hpp) of each row of r0
+    (shape (nplanes, n) or (n,)): kind "implicit" (centralImplicitSmoothing) or "explicit"
+    (centralExplicitSmoothing); ends "p" periodic, "a" one-neighbour, "n" unscaled."""
+    lib = load(False)
+    if not getattr(lib, "_smooth_declared", False):
+        lib.hco_smooth_1d.argtypes = [C.c_int, _dp, _dp, C.c_longlong, C.c_int, C.c_double, C.c_int]
+        lib._smooth_declared = True
+    a = np.ascontiguousarray(r0, dtype=np.float64)
+    a2 = a.reshape(-1, a.shape[-1])
+    out = np.empty_like(a2)
+    lib.hco_smooth_1d({"implicit": 0, "explicit": 1}[kind], a2, out, a2.shape[1], a2.shape[0], float(alpha),
+                      ord(ends))
+    return out.reshape(a.shape)
+
+
 class ScalarOracleSolver:
     """CPU restatement of integrate() for the scalar advection law (conserved {u, v, q})."""
 
