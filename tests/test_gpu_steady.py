@@ -50,7 +50,8 @@ def test_steady_stops_at_step_cap():
     assert not st.converged and st.steps == 10 and len(hist) == 4  # steps 1, 5, 9, 10
 
 
-def test_steady_refuses_residual_smoothing():
+def test_steady_refuses_residual_smoothing_on_2d_contexts():
+    """Residual smoothing exists only for the reference's 1D path (test_gpu_smooth covers it)."""
     from hyperboliconvergence_gb300._capi import SteadyControls, SteadyStats
     s = small_cylinder()
     ctl = SteadyControls(100, 1e-6, 10, 1, 0.5)
