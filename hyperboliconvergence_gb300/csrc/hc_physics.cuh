@@ -155,6 +155,18 @@ template <class R> __host__ __device__ __forceinline__ void sqrt_rcp(R x, R& s, 
   r = R(1) / s;
 }
 
+// s = sqrt(x); FP64 on the device as x rsqrt(x) (within 1.5 ulp, fewer instructions
+// than the correctly rounded square root)
+template <class R> __host__ __device__ __forceinline__ void sqrt_fast(R x, R& s) {
+#ifdef __CUDA_ARCH__
+  if constexpr (std::is_same<R, double>::value) {
+    s = x * rsqrt(x);
+    return;
+  }
+#endif
+  s = sqrt(x);
+}
+
 // set2State of the two states of one face.  FP64: both densities' inverses from one
 // division, 1/(rL rR) times the other density, when both densities lie in
 // [2^-500, 2^500] (the product stays normal); otherwise, and for the other types, one
@@ -241,7 +253,9 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> central_flux(R n
 // is rotated to the face frame, exactly as the reference composes them.
 template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g, R nx, R ny, R A,
                                                                const St<R>& l, const St<R>& r) {
-  const R al = sqrt(l.a2), ar = sqrt(r.a2);
+  R al, ar;
+  sqrt_fast(l.a2, al);
+  sqrt_fast(r.a2, ar);
   const Flux5<R> c = central_flux_u(nx, ny, A, l, r, al, ar);
   // roe average: cr = sqrt(rR/rL), ra = cr rL, 1/ra = cr/rR
   const R cr = sqrt(r.r * l.ir);
