@@ -155,12 +155,13 @@ template <class R> __host__ __device__ __forceinline__ void sqrt_rcp(R x, R& s, 
   r = R(1) / s;
 }
 
-// s = sqrt(x); FP64 on the device as x rsqrt(x) (within 1.5 ulp, fewer instructions
-// than the correctly rounded square root)
+// s = sqrt(x); FP64 on the device as x rsqrt(x) for positive x (within 1.5 ulp, fewer
+// instructions than the correctly rounded square root), sqrt otherwise (zero stays zero)
 template <class R> __host__ __device__ __forceinline__ void sqrt_fast(R x, R& s) {
 #ifdef __CUDA_ARCH__
   if constexpr (std::is_same<R, double>::value) {
-    s = x * rsqrt(x);
+    const long long b = f64_bits(x);
+    s = (b > 0 && b < 0x7ff0000000000000LL) ? x * rsqrt(x) : sqrt(x);
     return;
   }
 #endif
@@ -370,7 +371,9 @@ template <class R> __host__ __device__ __forceinline__ R ms_p5(R s, R M, R alpha
 template <class R, bool by_mdot>
 __host__ __device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
   const R ua = sqrt(R(0.5) * (l.u2 + r.u2));
-  const R al = sqrt(l.a2), ar = sqrt(r.a2);
+  R al, ar;
+  sqrt_fast(l.a2, al);
+  sqrt_fast(r.a2, ar);
   const R aa = R(0.5) * (al + ar);
   const R aa1 = R(1) / aa;
   const R ma = ua * aa1;
@@ -396,7 +399,7 @@ __host__ __device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St
   o.f[1] = mdot * w.v + pa * ny;
   o.f[2] = mdot;
   o.f[3] = mdot * w.h;
-  o.lam = (sqrt(fmax(l.a2, r.a2)) + fmax(fabs(unl), fabs(unr))) * A;
+  o.lam = (fmax(al, ar) + fmax(fabs(unl), fabs(unr))) * A;  // sqrt of the larger a2
   return o;
 }
 
@@ -408,8 +411,11 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> ausmpup_flux(con
   const R ascoeff = R(2) * g.gm1 / (g.gamma + R(1));
   const R unl = proj(nx, ny, l), unr = proj(nx, ny, r);
   const R als2 = ascoeff * l.h, ars2 = ascoeff * r.h;
-  const R als = als2 / fmax(unl, sqrt(als2));
-  const R ars = ars2 / fmax(-unr, sqrt(ars2));
+  R sls, srs;
+  sqrt_fast(als2, sls);
+  sqrt_fast(ars2, srs);
+  const R als = als2 / fmax(unl, sls);
+  const R ars = ars2 / fmax(-unr, srs);
   const R ra = R(0.5) * (l.r + r.r);
   const R as = fmin(ars, als);
   const R ml = unl / as, mr = unr / as;
@@ -459,7 +465,9 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> ausmpup_flux(con
 // scaled by the cut-off Mach number (Weiss & Smith's low-Mach form with fixed coefficients)
 template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_ws_flux(const Gas<R>& g, R nx, R ny, R A,
                                                                   const St<R>& l, const St<R>& r) {
-  const R al = sqrt(l.a2), ar = sqrt(r.a2);
+  R al, ar;
+  sqrt_fast(l.a2, al);
+  sqrt_fast(r.a2, ar);
   const Flux5<R> c = central_flux_u(nx, ny, A, l, r, al, ar);
   // roe average (conservationLaws/euler/fluxes/roe.ipp:150-196)
   const R cr = sqrt(r.r * l.ir);
@@ -653,7 +661,9 @@ template <class R, int FK>
 __host__ __device__ __forceinline__ unsigned flux_bits(const Gas<R>& g, R nx, R ny, const St<R>& l, const St<R>& r) {
   const R unl = proj(nx, ny, l), unr = proj(nx, ny, r);
   if constexpr (FK == FLUX_ROE) {
-    const R al = sqrt(l.a2), ar = sqrt(r.a2);
+    R al, ar;
+    sqrt_fast(l.a2, al);
+    sqrt_fast(r.a2, ar);
     const R cr = sqrt(r.r * l.ir);
     const R wl = R(1) / (R(1) + cr);
     const R wr = R(1) - wl;
@@ -663,7 +673,10 @@ __host__ __device__ __forceinline__ unsigned flux_bits(const Gas<R>& g, R nx, R 
     ka += va * va;
     ka *= R(0.5);
     const R ha = wl * l.h + wr * r.h;
-    const R aa = sqrt(g.gm1 * (ha - ka));
+    R aa, a1;
+    if constexpr (std::is_same<R, double>::value) sqrt_rcp(g.gm1 * (ha - ka), aa, a1);
+    else aa = sqrt(g.gm1 * (ha - ka));
+    (void)a1;
     const R una = nx * ua + ny * va;
     unsigned b = 0;
     {
@@ -679,15 +692,21 @@ __host__ __device__ __forceinline__ unsigned flux_bits(const Gas<R>& g, R nx, R 
     return b;
   } else if constexpr (FK == FLUX_SLAU || FK == FLUX_SLAU_REF) {
     const R ua = sqrt(R(0.5) * (l.u2 + r.u2));
-    const R aa = R(0.5) * (sqrt(l.a2) + sqrt(r.a2));
+    R al, ar;
+    sqrt_fast(l.a2, al);
+    sqrt_fast(r.a2, ar);
+    const R aa = R(0.5) * (al + ar);
     const R aa1 = R(1) / aa;
     const R ml = unl * aa1, mr = unr * aa1;
     return (fabs(ml) > R(1) ? 1u : 0u) | (fabs(mr) > R(1) ? 2u : 0u) | (ua * aa1 > R(1) ? 4u : 0u);
   } else if constexpr (FK == FLUX_AUSMPUP) {
     const R ascoeff = R(2) * g.gm1 / (g.gamma + R(1));
     const R als2 = ascoeff * l.h, ars2 = ascoeff * r.h;
-    const R als = als2 / fmax(unl, sqrt(als2));
-    const R ars = ars2 / fmax(-unr, sqrt(ars2));
+    R sls, srs;
+    sqrt_fast(als2, sls);
+    sqrt_fast(ars2, srs);
+    const R als = als2 / fmax(unl, sls);
+    const R ars = ars2 / fmax(-unr, srs);
     const R as = fmin(ars, als);
     const R ml = unl / as, mr = unr / as;
     return (fabs(ml) > R(1) ? 1u : 0u) | (fabs(mr) > R(1) ? 2u : 0u) | (als < ars ? 4u : 0u);
