@@ -913,12 +913,35 @@ int hc_smooth_1d(hc_ctx* c, int kind, const double* r0_device, double* r1_device
   if ((kind != HC_SMOOTH_IMPLICIT && kind != HC_SMOOTH_EXPLICIT) || !r0_device || !r1_device || n < 2 ||
       nplanes < 1 || !(alpha > 0.0) || !std::isfinite(alpha))
     return fail(HC_ERR_ARG, "invalid smoothing arguments");
+  const size_t total = size_t(n) * nplanes;
   double* scratch = nullptr;
-  if (kind == HC_SMOOTH_IMPLICIT)
-    HC_CUDA(cudaMallocAsync((void**)&scratch, 2 * size_t(n) * nplanes * sizeof(double), c->stream));
-  const cudaError_t e = launch_smooth_1d<double>(kind, r0_device, r1_device, scratch,
-                                                 scratch ? scratch + size_t(n) * nplanes : nullptr, n, nplanes, n,
-                                                 alpha, ends, c->stream);
+  if (kind == HC_SMOOTH_IMPLICIT) {
+    // each plane's CTA reads r0 only before its last barrier and writes r1 after it,
+    // so in-place smoothing is safe; the sweeps need two lines of scratch
+    HC_CUDA(cudaMallocAsync((void**)&scratch, 2 * total * sizeof(double), c->stream));
+    const cudaError_t e = launch_smooth_1d<double>(kind, r0_device, r1_device, scratch, scratch + total, n, nplanes,
+                                                   n, alpha, ends, c->stream);
+    cudaFreeAsync(scratch, c->stream);
+    HC_CUDA(e);
+    c->launches += 1;
+    return HC_OK;
+  }
+  // explicit: every value reads its neighbours (and, on a periodic line, both ends),
+  // which other threads and blocks would overwrite when r1 overlaps r0; smooth a
+  // stream-ordered copy of r0 then
+  const double* src = r0_device;
+  const uintptr_t a0 = uintptr_t(r0_device), a1 = uintptr_t(r1_device), bytes = total * sizeof(double);
+  if (a0 < a1 + bytes && a1 < a0 + bytes) {
+    HC_CUDA(cudaMallocAsync((void**)&scratch, bytes, c->stream));
+    const cudaError_t ec = cudaMemcpyAsync(scratch, r0_device, bytes, cudaMemcpyDeviceToDevice, c->stream);
+    if (ec != cudaSuccess) {
+      cudaFreeAsync(scratch, c->stream);
+      HC_CUDA(ec);
+    }
+    src = scratch;
+  }
+  const cudaError_t e = launch_smooth_1d<double>(kind, src, r1_device, nullptr, nullptr, n, nplanes, n, alpha, ends,
+                                                 c->stream);
   if (scratch) cudaFreeAsync(scratch, c->stream);
   HC_CUDA(e);
   c->launches += 1;

@@ -141,14 +141,19 @@ __host__ __device__ __forceinline__ bool f64_exp_within(double x, unsigned e) {
   return be - (1023u - e) <= 2u * e;
 }
 
-// s = sqrt(x) and r = 1/s.  FP64 on the device: r = rsqrt(x) (within 1 ulp), s = x r,
-// one multi-instruction sequence instead of two; otherwise sqrt and a division.
+// s = sqrt(x) and r = 1/s.  FP64 on the device, for positive finite x: r = rsqrt(x)
+// (within 1 ulp), s = x r, one multi-instruction sequence instead of two.  Zero,
+// infinity, NaN and negative x take sqrt and a division there too, so they give what
+// the host gives (x = 0: s = 0, r = inf; x*rsqrt(x) would make s = 0*inf = NaN).
 template <class R> __host__ __device__ __forceinline__ void sqrt_rcp(R x, R& s, R& r) {
 #ifdef __CUDA_ARCH__
   if constexpr (std::is_same<R, double>::value) {
-    r = rsqrt(x);
-    s = x * r;
-    return;
+    const long long b = f64_bits(x);
+    if (b > 0 && b < 0x7ff0000000000000LL) {
+      r = rsqrt(x);
+      s = x * r;
+      return;
+    }
   }
 #endif
   s = sqrt(x);

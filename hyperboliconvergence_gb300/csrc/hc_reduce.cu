@@ -76,7 +76,11 @@ static __device__ __align__(256) double g_sr_noalloc_scratch[SR_NOALLOC_BLOCKS];
 
 namespace {
 std::mutex g_sr_scratch_mutex;
-std::vector<double*> g_sr_scratch_ptr;  // device address of the scratch array, per device
+// Device address of the scratch array, per device, looked up once and kept for the life
+// of the process.  cudaDeviceReset destroys the context the address belongs to, and this
+// cache is not told: a process that resets a device must not call
+// hc_spectral_radius_noalloc on that device again.
+std::vector<double*> g_sr_scratch_ptr;
 }  // namespace
 
 using namespace hc;

@@ -311,15 +311,17 @@ class Solver:
         check(self.lib.hc_steady_run(self.h, C.byref(ctl), _dptr(hist), hist.size, C.byref(st)))
         return st, hist[:st.history_len].copy()
 
-    def smooth_1d(self, r, alpha: float, kind: str = "implicit", ends: str = "a") -> np.ndarray:
+    def smooth_1d(self, r, alpha: float, kind: str = "implicit", ends: str = "a",
+                  in_place: bool = False) -> np.ndarray:
         """Residual smoothing of the legacy 1D path (hc_smooth_1d) of each row of r (shape
         (nplanes, n) or (n,)) on this context's device and stream: kind "implicit" or
-        "explicit", ends "p" (periodic), "a" (one-neighbour) or "n" (unscaled)."""
+        "explicit", ends "p" (periodic), "a" (one-neighbour) or "n" (unscaled).  in_place
+        passes the same device buffer as input and output."""
         import torch
         a = np.ascontiguousarray(r, dtype=np.float64)
         a2 = a.reshape(-1, a.shape[-1])
         src = torch.from_numpy(a2).cuda()
-        dst = torch.empty_like(src)
+        dst = src if in_place else torch.empty_like(src)
         torch.cuda.synchronize()
         check(self.lib.hc_smooth_1d(self.h, {"implicit": 0, "explicit": 1}[kind], C.c_void_p(src.data_ptr()),
                                     C.c_void_p(dst.data_ptr()), a2.shape[1], a2.shape[0], float(alpha), ord(ends)))

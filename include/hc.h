@@ -204,7 +204,8 @@ int hc_steady_run(hc_ctx* ctx, const hc_steady_controls* controls, double* histo
 
 /* Residual smoothing of the reference's legacy 1D path (OLD.fieldOperations/
  * centralImplicitSmoothing.ipp:3-52, centralExplicitSmoothing.ipp:4-37) on device
- * memory: nplanes planes of n >= 2 values (plane stride n), r1 may equal r0.
+ * memory: nplanes planes of n >= 2 values (plane stride n).  r1 may equal or overlap r0:
+ * the explicit kind then smooths a copy of r0 taken from the stream-ordered allocator.
  * HC_SMOOTH_IMPLICIT: four weighted-Jacobi sweeps (omega 2/3) of
  * (1 - beta delta^2) r1 = r0, beta = (alpha^2 - 1)/4, the result times alpha;
  * HC_SMOOTH_EXPLICIT: r1 = r0 + gamma delta^2 r0, gamma = ((1 + 4 beta)/alpha - 1)/4.
@@ -231,8 +232,10 @@ int hc_spectral_radius(const double* lambda_sum_device, const double* vol_device
  * that every GPU loading this library keeps until the process exits, which caps
  * ncell at 8,388,608 (larger sizes return HC_ERR_ARG).  The first call on a
  * device looks the array's device address up, so make that first call before
- * any stream capture.  All calls share the array: calls that overlap on the GPU
- * (other streams, other threads) race. */
+ * any stream capture.  The looked-up address is kept for the life of the process:
+ * after cudaDeviceReset on a device, do not call this entry point on that device
+ * again.  All calls share the array: calls that overlap on the GPU (other streams,
+ * other threads) race. */
 int hc_spectral_radius_noalloc(const double* lambda_sum_device, const double* vol_device, long long ncell,
                                double* out_device, void* stream);
 

@@ -1,0 +1,49 @@
+"""Device pointwise functions at the edges of their fast paths: sqrt_rcp at zero,
+subnormal, infinite, NaN and negative arguments gives what the host's sqrt and
+division give, and the device Roe flux on zero-pressure face states matches the
+oracle's (NaN in the same components, equal within 1e-12 of the flux scale
+elsewhere)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle_py
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+pytestmark = pytest.mark.gpu
+
+# the face states of tests/cpp/sqrt_guard_check.cu, {u, v, rho, p}
+QL = [[0, 0, 1, 0], [0, 0, 1, 0], [0.3, -0.2, 1, 0], [0.1, 0.2, 1, 1], [0, 0, 1, 1], [0.5, 0, 1, 0]]
+QR = [[0, 0, 2, 0], [0, 0, 1, 0], [0.3, -0.2, 2, 0], [0.2, 0.1, 2, 0.5], [0, 0, 1, 0], [-0.5, 0, 1, 0]]
+
+
+def test_sqrt_rcp_and_zero_pressure_roe_on_device(tmp_path):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = str(tmp_path / "sqrt_guard_check")
+    subprocess.run([nvcc, "-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "--expt-relaxed-constexpr",
+                    "-o", exe, os.path.join(ROOT, "tests", "cpp", "sqrt_guard_check.cu")], check=True,
+                   capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    dev = {}
+    for line in r.stdout.splitlines():
+        if line.startswith("roe "):
+            f = line.split()
+            dev[int(f[1])] = np.array([float(x) for x in f[2:]])
+    assert sorted(dev) == list(range(len(QL)))
+    pw = oracle_py.pointwise()
+    species = np.array([1.4, 287.058, 0.3])
+    face = np.array([1.5, 0.0, 0.0, 0.6, 0.8, -0.8, 0.6])
+    for k in range(len(QL)):
+        ref = pw.flux(0, species, face, np.array(QL[k], dtype=float), np.array(QR[k], dtype=float))
+        got = dev[k]
+        assert (np.isnan(got) == np.isnan(ref)).all(), (k, got, ref)
+        inf = np.isinf(ref)
+        assert (got[inf] == ref[inf]).all(), (k, got, ref)
+        fin = np.isfinite(ref)
+        if fin.any():
+            scale = max(np.abs(ref[fin]).max(), 1e-300)
+            assert np.abs(got[fin] - ref[fin]).max() <= 1e-12 * scale, (k, got, ref)

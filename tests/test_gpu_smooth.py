@@ -40,6 +40,22 @@ def test_smoothing_bit_identical_to_oracle(kind, ends, n):
         assert np.array_equal(got, ref), (alpha, np.abs(got - ref).max())
 
 
+@pytest.mark.parametrize("kind", ["implicit", "explicit"])
+@pytest.mark.parametrize("ends", ["p", "a", "n"])
+@pytest.mark.parametrize("n", [2, 3, 1000, 300_007])
+def test_smoothing_in_place_equals_out_of_place(kind, ends, n):
+    """r1 == r0: the explicit kind reads neighbours (and a periodic line's ends) that other
+    threads and blocks write, so the library smooths a copy; the result must equal the
+    out-of-place one bit for bit, on lines long enough to span many blocks."""
+    s, _, _, _ = solver()
+    rng = np.random.default_rng(7 + n)
+    r0 = rng.standard_normal((3, n))
+    for alpha in (1.7, 3.0):
+        out = s.smooth_1d(r0, alpha, kind, ends)
+        inp = s.smooth_1d(r0, alpha, kind, ends, in_place=True)
+        assert np.array_equal(inp, out), (alpha, np.abs(inp - out).max())
+
+
 def test_smoothing_rejects_bad_arguments():
     s, _, _, _ = solver()
     with pytest.raises(Exception, match="smoothing"):
