@@ -16,7 +16,8 @@ HC_OK, HC_ERR_ARG, HC_ERR_CUDA, HC_ERR_NONPHYSICAL, HC_ERR_TIMEOUT, HC_ERR_UNSUP
 STATUS_NAMES = {0: "HC_OK", 1: "HC_ERR_ARG", 2: "HC_ERR_CUDA", 3: "HC_ERR_NONPHYSICAL",
                 4: "HC_ERR_TIMEOUT", 5: "HC_ERR_UNSUPPORTED"}
 
-FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5, "roe_ws": 6}
+FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5, "roe_ws": 6,
+        "roe_face": 7}
 SCALING = {"convective": 0, "acoustic": 1, "adaptive": 2}
 BASIS = {"primitive": 0, "conserved": 1}
 LIMITER = {"nolimit1": 0, "nolimit2": 1, "nolimit3": 2, "vanalbada": 3, "minmod": 4,
@@ -44,6 +45,21 @@ class StepStats(C.Structure):
                 ("bad_cell", C.c_int), ("kernel_launches", C.c_longlong)]
 
 
+# hc_fix: corrections of the reference's defects (off by default)
+FIX = {"mach_split_p1": 1, "farfield_transverse": 2}
+
+
+def fix_mask(corrections) -> int:
+    """A correction mask from None, an int, "all", or names of FIX."""
+    if corrections is None:
+        return 0
+    if isinstance(corrections, int):
+        return corrections
+    if isinstance(corrections, str):
+        return sum(FIX.values()) if corrections == "all" else FIX[corrections]
+    return sum(FIX[c] for c in set(corrections))
+
+
 _lib = None
 
 
@@ -60,6 +76,7 @@ def _declare(lib):
         "hc_set_species": [p, d, d, d],
         "hc_set_low_mach": [p, i, i, d, d],
         "hc_set_tile": [p, i],
+        "hc_set_corrections": [p, C.c_uint],
         "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],
         "hc_state_upload": [p, dp],
         "hc_state_download": [p, dp],
@@ -137,6 +154,7 @@ def _declare_batch(lib):
         "hc_batch_state_upload": [p, i, dp],
         "hc_batch_state_download": [p, i, dp],
         "hc_batch_set_schedule": [p, C.POINTER(Schedule)],
+        "hc_batch_set_corrections": [p, C.c_uint],
         "hc_batch_get_schedule": [p, C.POINTER(Schedule)],
         "hc_batch_step_async": [p, i, i],
         "hc_batch_graph_capture": [p, i],

@@ -20,7 +20,8 @@ class Batch:
     states {u, v, q} (3 planes), Rusanov or central flux."""
 
     def __init__(self, instances, flux="slau", limiter="vanalbada", rk="ssp34", precision="fp32", dt="global",
-                 cfl=0.5, species=(1.4, 287.058, 0.5), stream=None, basis="primitive", law="euler"):
+                 cfl=0.5, species=(1.4, 287.058, 0.5), stream=None, basis="primitive", law="euler",
+                 corrections=None):
         self.lib = _capi.load()
         self.meshes = [inst[0] for inst in instances]
         self.law = law
@@ -50,6 +51,9 @@ class Batch:
         check(self.lib.hc_batch_create(C.byref(cfg), n, ni, nj, nodes, bcs, refs, *[float(x) for x in species],
                                        C.byref(h)))
         self.h = h
+        self.corrections = _capi.fix_mask(corrections)
+        if self.corrections:
+            check(self.lib.hc_batch_set_corrections(self.h, self.corrections))
         self.n = n
         if stream is not None:
             check(self.lib.hc_batch_set_stream(self.h, C.c_void_p(int(stream) if stream else None)))

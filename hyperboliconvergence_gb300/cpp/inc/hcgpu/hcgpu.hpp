@@ -50,7 +50,7 @@ template <class Real> Species<Real> get_air_species() {
   return s;
 }
 
-// LowMachScaling (conservationLaws/euler/euler.h:334-339)
+// LowMachScaling (conservationLaws/euler/euler.h:331-339)
 enum class LowMachScaling { Convective = HC_SCALING_CONVECTIVE, Acoustic = HC_SCALING_ACOUSTIC,
                             Adaptive = HC_SCALING_ADAPTIVE };
 
@@ -68,7 +68,7 @@ struct RusanovFlux { static constexpr int id = HC_FLUX_RUSANOV; };
 struct CentralFlux { static constexpr int id = HC_FLUX_CENTRAL; };
 struct RoeUnprecWS { static constexpr int id = HC_FLUX_ROE_WS; };
 
-// Limiter tags (limiters/limiter.h:46-131)
+// Limiter tags (limiters/limiter.h:43-131)
 namespace Limiters {
 struct NoLimit1 { static constexpr int id = HC_LIM_NOLIMIT1; };
 struct NoLimit2 { static constexpr int id = HC_LIM_NOLIMIT2; };
@@ -133,7 +133,7 @@ inline constexpr gpu_policy gpu_df{HC_DT_GLOBAL, HC_FP64_DF};
 inline constexpr gpu_policy gpu_df_local_dt{HC_DT_LOCAL, HC_FP64_DF};
 }  // namespace execution
 
-// Mesh<2,Real> nodes (mesh/mesh.h:283-321)
+// Mesh<2,Real> nodes (mesh/mesh.h:19-57)
 template <class Real> struct Mesh {
   int ni = 0, nj = 0;
   std::vector<double> nodes;  // (ni+1)*(nj+1) x,y pairs
@@ -156,7 +156,7 @@ Mesh<Real> make_linspace_mesh(const std::array<std::size_t, 2> cellDims, Real lo
   return m;
 }
 
-// EulerBCs (conservationLaws/euler/euler.h:34-41)
+// EulerBCs (conservationLaws/euler/euler.h:31-41)
 enum class BC { Periodic = HC_BC_PERIODIC, Riemann = HC_BC_RIEMANN, Entropy = HC_BC_ENTROPY,
                 Fixed = HC_BC_FIXED, InviscidWall = HC_BC_WALL };
 

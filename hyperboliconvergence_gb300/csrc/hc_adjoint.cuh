@@ -55,7 +55,7 @@ template <class R> __host__ __device__ __forceinline__ void exact_flux_adj(R nx,
   sb.v += ny * unbar;
 }
 
-// Harten entropy fix of one nonlinear wave (roe.ipp:214-223) reversed
+// Harten entropy fix of one nonlinear wave (roe.ipp:66-75) reversed
 template <class R> __host__ __device__ __forceinline__ void entropy_fix_adj(R la, R ll, R lr, R lbar, R* labar, R* llbar,
                                                                    R* lrbar) {
   const R d1 = la - ll, d2 = lr - la;
@@ -233,7 +233,7 @@ __host__ __device__ __forceinline__ void roe_flux_adj(const Gas<R>& g, R nx, R n
   prim_state_adj_ir(g, qr, r.ir, rb, qrbar);
 }
 
-// Reverse of rusanov_flux (conservationLaws/base/fluxes/rusanovFlux.ipp:99-147)
+// Reverse of rusanov_flux (conservationLaws/base/fluxes/rusanovFlux.ipp:2-50)
 template <class R>
 __host__ __device__ __forceinline__ void rusanov_flux_adj(const Gas<R>& g, R nx, R ny, R A, const R* ql, const R* qr,
                                                  const R* Fbar, R* qlbar, R* qrbar) {

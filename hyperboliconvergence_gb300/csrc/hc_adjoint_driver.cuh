@@ -97,7 +97,7 @@ template <class R> AdjArgs<R> adj_args(Adj<R>& A) {
   AdjArgs<R> a{};
   a.ni = c->ni; a.nj = c->nj;
   for (int k = 0; k < 4; ++k) a.bc[k] = c->bc[k];
-  a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf);
+  a.gas = with_fixes(make_gas<R>(c->gamma, c->Rgas, c->minf), c->fixes);
   a.limiter = c->cfg.limiter;
   a.fi = (const R*)c->fi; a.fj = (const R*)c->fj;
   for (int k = 0; k < 4; ++k) { a.gref[k] = (const R*)c->gref[k]; a.refbar[k] = A.refbar[k]; }
@@ -300,7 +300,7 @@ template <class R> int adjoint_step(Adj<R>& A, int step) {
   for (int k = 0; k < A.nst; ++k) HC_CUDA(cudaMemsetAsync(A.rbar[k], 0, bytes4, A.s()));
   HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
   const double dt = step_dt(A, step);
-  const Gas<R> g = make_gas<R>(A.c->gamma, A.c->Rgas, A.c->minf);
+  const Gas<R> g = with_fixes(make_gas<R>(A.c->gamma, A.c->Rgas, A.c->minf), A.c->fixes);
   for (int s = A.nst - 1; s >= 0; --s) {
     const R* qbar_out = (s == A.nst - 1) ? A.lam : A.qbs;
     R al[4] = {R(0), R(0), R(0), R(0)};

@@ -790,7 +790,8 @@ template <class R>
 cudaError_t launch_adj_face_tangent_batch(int flux, const AdjBatchArgs<R>& b, unsigned blocks, int threads,
                                           cudaStream_t s);
 inline bool flux_by_tangent(int flux) {
-  return flux == FLUX_SLAU || flux == FLUX_SLAU_REF || flux == FLUX_AUSMPUP || flux == FLUX_ROE_WS;
+  return flux == FLUX_SLAU || flux == FLUX_SLAU_REF || flux == FLUX_AUSMPUP || flux == FLUX_ROE_WS ||
+         flux == FLUX_ROE_FACE;
 }
 
 // the same for a scalar-law batch (the update is linear on the conserved set)

@@ -25,6 +25,7 @@ cudaError_t launch_adj_face_tangent(int flux, const AdjArgs<R>& a, int dir, unsi
     case FLUX_SLAU_REF: face_one<R, FLUX_SLAU_REF>(a, dir, blocks, threads, s); break;
     case FLUX_AUSMPUP: face_one<R, FLUX_AUSMPUP>(a, dir, blocks, threads, s); break;
     case FLUX_ROE_WS: face_one<R, FLUX_ROE_WS>(a, dir, blocks, threads, s); break;
+    case FLUX_ROE_FACE: face_one<R, FLUX_ROE_FACE>(a, dir, blocks, threads, s); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
@@ -38,6 +39,7 @@ cudaError_t launch_adj_face_tangent_batch(int flux, const AdjBatchArgs<R>& b, un
     case FLUX_SLAU_REF: face_batch<R, FLUX_SLAU_REF>(b, blocks, threads, s); break;
     case FLUX_AUSMPUP: face_batch<R, FLUX_AUSMPUP>(b, blocks, threads, s); break;
     case FLUX_ROE_WS: face_batch<R, FLUX_ROE_WS>(b, blocks, threads, s); break;
+    case FLUX_ROE_FACE: face_batch<R, FLUX_ROE_FACE>(b, blocks, threads, s); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -153,7 +153,7 @@ template <class R> Stage1DArgs<R> args_1d(hc_ctx* c) {
   Stage1DArgs<R> a{};
   a.nc = c->ni;
   a.bc[0] = c->bc[0]; a.bc[1] = c->bc[1];
-  a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale);
+  a.gas = with_fixes(make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale), c->fixes);
   a.limiter = c->cfg.limiter;
   a.rec = (const R*)c->fi;
   a.vol = (const R*)c->vol;
@@ -396,7 +396,7 @@ int run_signatures(hc_ctx* c, unsigned long long* sig_i, unsigned long long* sig
 }  // namespace
 
 // ---------------------------------------------------------------- dual time
-// ODE::Implicit::MultiStep tables (ode.h:10-83): (b_0 u_{n+1} + b_1 u_n + b_2 u_{n-1})/dt =
+// ODE::Implicit::MultiStep tables (ode.h:12-82): (b_0 u_{n+1} + b_1 u_n + b_2 u_{n-1})/dt =
 // g_0 R(u_{n+1}) + g_1 R(u_n)
 struct MultiStepTab { double beta[3], gamma[2]; };
 inline MultiStepTab multistep(int scheme) {
@@ -437,7 +437,8 @@ template <class R> int dual_time_run(hc_ctx* c, const hc_dual_time_controls* ctl
   const size_t n = c->ncell();
   const MultiStepTab ms = multistep(ctl->scheme);
   const unsigned grid = unsigned(std::min<size_t>((n + 255) / 256, 152 * 16));
-  const Gas<R> g = make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale);
+  const Gas<R> g =
+      with_fixes(make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale), c->fixes);
   R* buf = nullptr;
   const bool trap = ms.gamma[1] != 0.0;
   HC_CUDA(cudaMalloc(&buf, (3 * 4 + (trap ? 5 : 0)) * n * sizeof(R)));
@@ -698,6 +699,13 @@ int hc_set_low_mach(hc_ctx* c, int velocity_scaling, int pressure_scaling, doubl
   return HC_OK;
 }
 
+int hc_set_corrections(hc_ctx* c, unsigned mask) {
+  if (int st = check_ctx(c)) return st;
+  if (mask & ~unsigned(HC_FIX_ALL)) return fail(HC_ERR_ARG, "unknown correction bits");
+  c->fixes = mask;
+  return HC_OK;
+}
+
 int hc_set_tile(hc_ctx* c, int tile) {
   if (int st = check_ctx(c)) return st;
   if (tile < HC_TILE_8x32 || tile > HC_TILE_16x16_H) return fail(HC_ERR_ARG, "unknown tile shape");
@@ -948,7 +956,7 @@ int hc_smooth_1d(hc_ctx* c, int kind, const double* r0_device, double* r1_device
   return HC_OK;
 }
 
-// make_cylinder_mesh (mesh/generate/twoD.h:223-263) with geometric radial stretching
+// make_cylinder_mesh (mesh/generate/twoD.h:139-179) with geometric radial stretching
 int hc_mesh_cylinder_nodes(int nr, int nth, double rc, double rb, double stretch, double* nodes) {
   if (nr < 1 || nth < 1 || !nodes || !(rb > rc) || !(stretch > 0)) return fail(HC_ERR_ARG, "invalid cylinder mesh");
   const double dr = (rb - rc) / nr;
@@ -965,7 +973,7 @@ int hc_mesh_cylinder_nodes(int nr, int nth, double rc, double rb, double stretch
   return HC_OK;
 }
 
-// make_linspace_mesh (mesh/generate/twoD.h:99-124)
+// make_linspace_mesh (mesh/generate/twoD.h:15-40)
 int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, double hiy, double* nodes) {
   if (nx < 1 || ny < 1 || !nodes) return fail(HC_ERR_ARG, "invalid linspace mesh");
   const double dx = (hix - lox) / nx, dy = (hiy - loy) / ny;

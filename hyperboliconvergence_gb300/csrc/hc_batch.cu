@@ -140,7 +140,7 @@ template <class R> int per_instance_step(hc_batch* b) {
       base.bc[s] = b->bc[4 * k + s];
       base.gref[s] = (const R*)b->gref + b->gref_off[4 * k + s];
     }
-    base.gas = make_gas<R>(b->gamma, b->Rgas, b->minf);
+    base.gas = with_fixes(make_gas<R>(b->gamma, b->Rgas, b->minf), b->fixes);
     base.limiter = b->cfg.limiter;
     base.basis = b->cfg.basis;
     base.fi = (const R*)b->fi + (long long)FREC * b->fi_off[k];
@@ -371,6 +371,16 @@ int hc_batch_state_download(hc_batch* b, int k, double* prim) {
     HC_CUDA(cudaMemcpyAsync(prim, (const double*)b->q[0] + 4 * b->cell_off[k], m * 8, cudaMemcpyDeviceToHost, b->stream));
   }
   HC_CUDA(cudaStreamSynchronize(b->stream));
+  return HC_OK;
+}
+
+int hc_batch_set_corrections(hc_batch* b, unsigned mask) {
+  if (int st = check_b(b)) return st;
+  if (mask & ~unsigned(HC_FIX_ALL)) return fail(HC_ERR_ARG, "unknown correction bits");
+  b->fixes = mask;
+  // a captured graph holds the old launch arguments
+  if (b->graph_exec) { cudaGraphExecDestroy(b->graph_exec); b->graph_exec = nullptr; }
+  if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
   return HC_OK;
 }
 

@@ -16,6 +16,7 @@ struct hc_batch {
   std::vector<int> ni, nj, bc;
   std::vector<std::vector<double>> href;  // 4 per instance
   double gamma = 1.4, Rgas = 287.058, minf = 1e-4;
+  unsigned fixes = 0;  // HC_FIX_* corrections (hc_batch_set_corrections)
   cudaStream_t own = nullptr, stream = nullptr;
   int sms = 152;
   hc_schedule sched{HC_TILE_8x32, 2, HC_ORDER_LARGEST_FIRST, 0.f};
@@ -55,7 +56,7 @@ template <class R> BatchArgs<R> batch_args(hc_batch* b) {
   a.inst = b->inst_d;
   a.order = b->order_d;
   a.nwork = b->nwork;
-  a.gas = make_gas<R>(b->gamma, b->Rgas, b->minf);
+  a.gas = with_fixes(make_gas<R>(b->gamma, b->Rgas, b->minf), b->fixes);
   a.limiter = b->cfg.limiter;
   a.basis = b->cfg.basis;
   a.q0 = (const R*)b->q[0];

@@ -60,7 +60,7 @@ template <class R> struct BAdj : AdjCommon {
   AdjBatchArgs<R> args() const {
     AdjBatchArgs<R> a{};
     a.inst = b->inst_d;
-    a.gas = make_gas<R>(b->gamma, b->Rgas, b->minf);
+    a.gas = with_fixes(make_gas<R>(b->gamma, b->Rgas, b->minf), b->fixes);
     a.limiter = b->cfg.limiter;
     a.qm = qm;
     a.fi = (const R*)b->fi;
@@ -185,7 +185,7 @@ template <class R> int adjoint_step(BAdj<R>& A, int step) {
     u.inst = A.b->inst_d;
     u.seg = A.seg_c;
     u.nseg = A.ninst;
-    u.g = make_gas<R>(A.b->gamma, A.b->Rgas, A.b->minf);
+    u.g = with_fixes(make_gas<R>(A.b->gamma, A.b->Rgas, A.b->minf), A.b->fixes);
     u.q_out = A.sq[s + 1];
     u.q0 = A.sq[0];
     u.vol = (const R*)A.b->vol;

@@ -21,6 +21,7 @@ struct hc_ctx {
   double gamma = 1.4, Rgas = 287.058, minf = 1e-4;
   double lref = 1., sdt = 1.7976931348623157e308;  // species lref and dt (AUSM+up scaling)
   int vscale = 0, pscale = 0;                       // AUSM+up LowMachScaling pair
+  unsigned fixes = 0;                               // HC_FIX_* corrections (hc_set_corrections)
   void* dual_src = nullptr;                         // dual time: earlier levels' terms (4 planes, R)
   double dual_g0 = 1.0, dual_b0dt = 0.0;            // dual time: gamma_0 and beta_0 / dt
   double smooth_alpha = 0.0;                        // 1D residual smoothing factor (0: off)
@@ -62,7 +63,7 @@ template <class R> StageArgs<R> base_args(hc_ctx* c) {
   StageArgs<R> a{};
   a.ni = c->ni; a.nj = c->nj;
   for (int k = 0; k < 4; ++k) a.bc[k] = c->bc[k];
-  a.gas = make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale);
+  a.gas = with_fixes(make_gas<R>(c->gamma, c->Rgas, c->minf, c->lref, c->sdt, c->vscale, c->pscale), c->fixes);
   a.limiter = c->cfg.limiter;
   a.basis = c->cfg.basis;
   a.dual_src = (const R*)c->dual_src;

@@ -28,7 +28,7 @@ __device__ __forceinline__ void surface_dev(const double* p0, const double* p1, 
   n[1] = l1 * t1x;
 }
 
-// cell volume |J(0,0)| of the bilinear map and the vertex centroid (geometry/volume.ipp:55-96)
+// cell volume |J(0,0)| of the bilinear map and the vertex centroid (geometry/volume.ipp:25-66)
 __global__ void geom_cells_kernel(const double* __restrict__ nodes, int ni, int nj, double* __restrict__ vol,
                                   double* __restrict__ cx, double* __restrict__ cy) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -144,7 +144,7 @@ __device__ __forceinline__ void xm_add(double* x, double dx, double dy) {
 }
 
 // mirrored-point displacement of boundary cell (a,b) away from its neighbour
-// (na,nb) (spatial/lsqMetrics.h:204-212)
+// (na,nb) (spatial/lsqMetrics.h:119-123)
 __device__ __forceinline__ void mirror_disp(const GeomArgs& g, size_t c0, size_t c1, double* m) {
   const double x0[2] = {g.cx[c0], g.cy[c0]}, x1[2] = {g.cx[c1], g.cy[c1]};
   for (int k = 0; k < 2; ++k) {
@@ -155,7 +155,7 @@ __device__ __forceinline__ void mirror_disp(const GeomArgs& g, size_t c0, size_t
 }
 
 // Cell pass: full xmetric = pair terms of the 4 faces + mirror terms on
-// non-periodic sides (spatial/lsqMetrics.h:119-251, D2).
+// non-periodic sides (spatial/lsqMetrics.h:31-163, D2).
 __global__ void geom_xm_kernel(GeomArgs g) {
   const int ni = g.ni, nj = g.nj;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -189,7 +189,7 @@ __global__ void geom_xm_kernel(GeomArgs g) {
   g.xm[c] = x[0]; g.xm[n + c] = x[1]; g.xm[2 * n + c] = x[2];
 }
 
-// factor the 2x2 metric and project on direction d: w = X^-1 d (lsq/lsq.h:403-459)
+// factor the 2x2 metric and project on direction d: w = X^-1 d (lsq/factor_solve.ipp:13-22, 47-69)
 __device__ __forceinline__ void weights(const double* x, const double* d, double* w) {
   const double det = 1. / (x[0] * x[2] - x[1] * x[1]);
   const double f0 = det * x[2], f1 = -det * x[1], f2 = det * x[0];
@@ -198,7 +198,7 @@ __device__ __forceinline__ void weights(const double* x, const double* d, double
 }
 
 // Face pass 2: biased-gradient weights of both cells (lsq::bias_solves,
-// lsq/lsq.h:461-490) and, on wall faces, the extrapolation weights of the
+// lsq/factor_solve.ipp:71-100) and, on wall faces, the extrapolation weights of the
 // interior cell's full gradient (D4).
 __global__ void geom_faces2_kernel(GeomArgs g, int dir) {
   const int ni = g.ni, nj = g.nj;

@@ -59,6 +59,7 @@ template <class R> StageFn<R> stage_fn(int flux) {
     case FLUX_AUSMPUP: return launch_stage<R, FLUX_AUSMPUP>;
     case FLUX_RUSANOV: return launch_stage<R, FLUX_RUSANOV>;
     case FLUX_ROE_WS: return launch_stage<R, FLUX_ROE_WS>;
+    case FLUX_ROE_FACE: return launch_stage<R, FLUX_ROE_FACE>;
     default: return launch_stage<R, FLUX_CENTRAL>;
   }
 }
@@ -70,6 +71,7 @@ template <class R> BatchFn<R> batch_fn(int flux) {
     case FLUX_AUSMPUP: return launch_batch_stage<R, FLUX_AUSMPUP>;
     case FLUX_RUSANOV: return launch_batch_stage<R, FLUX_RUSANOV>;
     case FLUX_ROE_WS: return launch_batch_stage<R, FLUX_ROE_WS>;
+    case FLUX_ROE_FACE: return launch_batch_stage<R, FLUX_ROE_FACE>;
     default: return launch_batch_stage<R, FLUX_CENTRAL>;
   }
 }
@@ -81,6 +83,7 @@ template <class R> cudaError_t prepare(int flux) {
     case FLUX_AUSMPUP: return prepare_stage<R, FLUX_AUSMPUP>();
     case FLUX_RUSANOV: return prepare_stage<R, FLUX_RUSANOV>();
     case FLUX_ROE_WS: return prepare_stage<R, FLUX_ROE_WS>();
+    case FLUX_ROE_FACE: return prepare_stage<R, FLUX_ROE_FACE>();
     default: return prepare_stage<R, FLUX_CENTRAL>();
   }
 }

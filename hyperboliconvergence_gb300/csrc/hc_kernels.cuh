@@ -158,7 +158,7 @@ template <class C, class R> __device__ __forceinline__ Gas<C> gas_as(const Gas<R
   Gas<C> o;
   o.gamma = cvt<C>(g.gamma); o.gm1 = cvt<C>(g.gm1); o.gamma1 = cvt<C>(g.gamma1);
   o.Rgas = cvt<C>(g.Rgas); o.minf = cvt<C>(g.minf); o.inv_gamma = cvt<C>(g.inv_gamma);
-  o.lref_dt = cvt<C>(g.lref_dt); o.vscale = g.vscale; o.pscale = g.pscale;
+  o.lref_dt = cvt<C>(g.lref_dt); o.vscale = g.vscale; o.pscale = g.pscale; o.fixes = g.fixes;
   return o;
 }
 
@@ -207,7 +207,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   auto M = [&](int k, int la, int lb) -> C& { return sm[(k * MI + la + 1) * MJ + lb + 1]; };
 
   // ---- phase 2: qmetric of the tile cells and of the 1-cell halo strips
-  // (lsq/qmetric.ipp via spatial/lsqMetrics.h:269-301; D2 periodic wrap)
+  // (lsq/qmetric.ipp via spatial/lsqMetrics.h:181-213; D2 periodic wrap)
   for (int k = tid; k < MI * MJ; k += NT) {
     const int la = k / MJ - 1, lb = k % MJ - 1;
     const bool corner = (la < 0 || la >= TI) && (lb < 0 || lb >= TJ);
@@ -461,7 +461,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   }
   const size_t c = size_t(gi) * nj + gj;
   if (DUAL && own && a.dual_src) {
-    // dual time (ode.h:10-83, OLD.fieldOperations/dualTimeResidual.ipp): the physical-time
+    // dual time (ode.h:12-82, OLD.fieldOperations/dualTimeResidual.ipp): the physical-time
     // terms of the current iterate and of the earlier levels join the flux residual
     R qk[4], qc[4];
 #pragma unroll
@@ -589,7 +589,7 @@ __global__ void update0_kernel(int ni, int nj, Gas<R> g, const R* __restrict__ q
                                const R* __restrict__ vol, R alpha00, R beta0, double cfl, StepInfo* info,
                                R* __restrict__ q_out, int advance_time, int basis, double dual_b0dt) {
   const size_t ncell = size_t(ni) * nj;
-  // dual time: the pseudo step dtau / (1 + b0 dtau / dt) (timestepping/dualTime.ipp:61-62)
+  // dual time: the pseudo step dtau / (1 + b0 dtau / dt) (timestepping/dualTime.ipp:65-66)
   const R dt = dual_b0dt > 0.0 ? R(dual_step(double(global_dt<R>(info, cfl)), dual_b0dt)) : global_dt<R>(info, cfl);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     info->dt = double(dt);

@@ -21,6 +21,7 @@ template <class R> static cudaError_t dispatch1(const Stage1DArgs<R>& a, int flu
     case FLUX_AUSMPUP: return go1<R, FLUX_AUSMPUP>(a, s);
     case FLUX_RUSANOV: return go1<R, FLUX_RUSANOV>(a, s);
     case FLUX_ROE_WS: return go1<R, FLUX_ROE_WS>(a, s);
+    case FLUX_ROE_FACE: return go1<R, FLUX_ROE_FACE>(a, s);
     default: return go1<R, FLUX_CENTRAL>(a, s);
   }
 }

@@ -18,8 +18,8 @@
 namespace hc {
 
 enum FluxKind { FLUX_ROE = 0, FLUX_SLAU = 1, FLUX_SLAU_REF = 2, FLUX_AUSMPUP = 3,
-                FLUX_RUSANOV = 4, FLUX_CENTRAL = 5, FLUX_ROE_WS = 6, FLUX_COUNT = 7 };
-// LowMachScaling (conservationLaws/euler/euler.h:334-339) of AUSM+up's two diffusion terms
+                FLUX_RUSANOV = 4, FLUX_CENTRAL = 5, FLUX_ROE_WS = 6, FLUX_ROE_FACE = 7, FLUX_COUNT = 8 };
+// LowMachScaling (conservationLaws/euler/euler.h:331-339) of AUSM+up's two diffusion terms
 enum LowMachScaling { SCALING_CONVECTIVE = 0, SCALING_ACOUSTIC = 1, SCALING_ADAPTIVE = 2 };
 enum LimiterKind { LIM_NOLIMIT1 = 0, LIM_NOLIMIT2 = 1, LIM_NOLIMIT3 = 2, LIM_VANALBADA = 3,
                    LIM_MINMOD = 4, LIM_SUPERBEE = 5, LIM_MC = 6, LIM_VANLEER = 7,
@@ -52,7 +52,22 @@ template <class R> struct Gas {
   R lref_dt;    // lref / dt of the species: AUSM+up's adaptive scaling mu = lref / (as dt)
   int vscale;   // AUSM+up velocity-diffusion scaling (LowMachScaling)
   int pscale;   // AUSM+up pressure-diffusion scaling (LowMachScaling)
+  unsigned fixes;  // FIX_* corrections of the reference's defects (0: as the reference computes)
 };
+
+// Corrections of two defects of the reference, off by default (the reference's results are
+// reproduced as written):
+//  FIX_MACH_SPLIT_P1 -- MachSplit_P1 (machSplittings.ipp:26-31) is (M1 + eps)/(|M| + eps)
+//    with eps the largest finite value, which rounds to 1 for both signs, so SLAU and
+//    AUSM+up add both sides' pressure on supersonic faces (F(q, q) is not the exact flux);
+//    corrected, P1 is M1/M, the 1/0 split it is meant to be: (s M1 + eps)/(|M| + eps) with
+//    eps the smallest normal value (dividing by |M| alone would give -1 for s = -1, M < -1).
+//  FIX_FARFIELD_TRANSVERSE -- the Riemann and entropy far fields (conservationLaws/euler/boundary/riemann.ipp:48-50,
+//    entropy.ipp:47-49) return the interior state when u_n/|u| < threshold, a test without
+//    the absolute value, so every outflow face copies the interior (subsonic outflow then
+//    takes no far-field information); corrected, the test is |u_n|/|u| < threshold and
+//    outflow faces get the characteristic treatment the rest of the function has.
+enum : unsigned { FIX_MACH_SPLIT_P1 = 1u, FIX_FARFIELD_TRANSVERSE = 2u, FIX_ALL = 3u };
 
 // lref and dt default to the reference's air species (1 and the largest double,
 // conservationLaws/euler/species.ipp:12), where the adaptive ratio vanishes
@@ -69,6 +84,11 @@ __host__ __device__ inline Gas<R> make_gas(double gamma, double Rgas, double min
   g.lref_dt = R(lref / dt);
   g.vscale = vscale;
   g.pscale = pscale;
+  g.fixes = 0u;
+  return g;
+}
+template <class R> __host__ __device__ inline Gas<R> with_fixes(Gas<R> g, unsigned fixes) {
+  g.fixes = fixes;
   return g;
 }
 
@@ -77,7 +97,7 @@ template <class R> struct St { R p, r, h, u2, a2, u, v, ir; };  // ir = 1/r
 
 template <class R> struct Flux5 { R f[4]; R lam; };
 
-// set2State(primitive) (conservationLaws/euler/transforms/primitive.ipp:101-137)
+// set2State(primitive) (conservationLaws/euler/transforms/primitive.ipp:24-60)
 // (ir = 1/r given)
 template <class R>
 __host__ __device__ __forceinline__ St<R> prim_state_ir(const Gas<R>& g, R u, R v, R r, R p, R ir) {
@@ -211,7 +231,7 @@ template <class R> __host__ __device__ __forceinline__ void state_cons(const St<
 // projectedVelocity (conservationLaws/base/base.h:148-158)
 template <class R> __host__ __device__ __forceinline__ R proj(R nx, R ny, const St<R>& s) { return nx * s.u + ny * s.v; }
 
-// exactFlux (conservationLaws/euler/fluxes/exactFlux.ipp:231-263); a = sqrt(a2)
+// exactFlux (conservationLaws/euler/fluxes/exactFlux.ipp:4-36); a = sqrt(a2)
 template <class R> __host__ __device__ __forceinline__ Flux5<R> exact_flux_a(R nx, R ny, const St<R>& s, R a) {
   Flux5<R> o;
   const R un = proj(nx, ny, s);
@@ -227,7 +247,7 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> exact_flux(R nx,
   return exact_flux_a(nx, ny, s, sqrt(s.a2));
 }
 
-// CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:25-37), sound speeds given;
+// CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:2-14), sound speeds given;
 // lam left unscaled by A (the caller's max of unscaled speeds times A equals the max of
 // the scaled speeds: rounding is monotone)
 template <class R>
@@ -252,13 +272,18 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> central_flux(R n
   return central_flux_a(nx, ny, A, l, r, sqrt(l.a2), sqrt(r.a2));
 }
 
-// Roe flux = central + matrix dissipation (conservationLaws/base/fluxes/roeFlux.ipp:39-95),
-// with roeAverage and Harten's entropy fix (conservationLaws/euler/fluxes/roe.ipp:150-226)
-// and the characteristic transforms (conservationLaws/euler/transforms/primitive.ipp:142-313).
-// The Roe-averaged state keeps its velocity in the global frame while the jump
-// is rotated to the face frame, exactly as the reference composes them.
-template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g, R nx, R ny, R A,
-                                                               const St<R>& l, const St<R>& r) {
+// Roe flux = central + matrix dissipation (conservationLaws/base/fluxes/roeFlux.ipp:2-58),
+// with roeAverage and Harten's entropy fix (conservationLaws/euler/fluxes/roe.ipp:2-78)
+// and the characteristic transforms (conservationLaws/euler/transforms/characteristic.ipp).
+// FACE = false (RoeFlux as written): the Roe-averaged state keeps its velocity in the
+// global frame while the jump is rotated to the face frame (roeFlux.ipp:40-54), exactly as
+// the reference composes them; the dissipation is then the Roe matrix's only for a face
+// normal (1, 0).  FACE = true: the averaged velocity enters the characteristic transforms
+// by its face-normal and tangential components, the frame of the jump, so the flux is
+// invariant under rotation; for the normal (1, 0) both are the same bit for bit.
+template <class R, bool FACE = false>
+__host__ __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g, R nx, R ny, R A, const St<R>& l,
+                                                      const St<R>& r) {
   R al, ar;
   sqrt_fast(l.a2, al);
   sqrt_fast(r.a2, ar);
@@ -305,13 +330,17 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const G
   const R d3 = (r.r * r.h - r.p) - (l.r * l.h - l.p);
   const R c0 = nx * d0 + ny * d1;
   const R c1 = tx * d0 + ty * d1;
+  // the averaged velocity the transforms see: global components as written, or the
+  // face-normal and tangential ones
+  const R xa = FACE ? una : ua;
+  const R ya = FACE ? tx * ua + ty * va : va;
   // conserved -> primitive about the average state
   const R rho1 = cr * r.ir;
   R cc = ka * d2 + d3;
-  const R du0 = (c0 - ua * d2) * rho1;
-  cc -= ua * c0;
-  const R du1 = (c1 - va * d2) * rho1;
-  cc -= va * c1;
+  const R du0 = (c0 - xa * d2) * rho1;
+  cc -= xa * c0;
+  const R du1 = (c1 - ya * d2) * rho1;
+  cc -= ya * c1;
   const R dp = cc * g.gm1;
   // primitive -> characteristic, scaled by the wave speeds
   if constexpr (!std::is_same<R, double>::value) a1 = R(1) / aa;
@@ -324,10 +353,10 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const G
   const R drr = dpp * (a1 * a1) - ra * w0 * g.inv_gamma;
   const R du = R(0.5) * (w1 + w2);
   const R dv = w3;
-  const R e0 = ra * du + ua * drr;
-  const R e1 = ra * dv + va * drr;
-  R dk = ua * du;
-  dk += va * dv;
+  const R e0 = ra * du + xa * drr;
+  const R e1 = ra * dv + ya * drr;
+  R dk = xa * du;
+  dk += ya * dv;
   const R e3 = dpp * g.gamma1 + ra * dk + ka * drr;
   // rotate back
   const R f0 = nx * e0 + tx * e1;
@@ -342,7 +371,7 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_flux(const G
   return o;
 }
 
-// RusanovFlux (conservationLaws/base/fluxes/rusanovFlux.ipp:99-147)
+// RusanovFlux (conservationLaws/base/fluxes/rusanovFlux.ipp:2-50)
 template <class R> __host__ __device__ __forceinline__ Flux5<R> rusanov_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
   Flux5<R> o = central_flux(nx, ny, A, l, r);
   const R lambda = fmax(fabs(proj(nx, ny, l)) + sqrt(l.a2), fabs(proj(nx, ny, r)) + sqrt(r.a2));
@@ -354,16 +383,20 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> rusanov_flux(R n
   return o;
 }
 
-// Mach splittings (conservationLaws/euler/fluxes/machSplittings.ipp:163-204)
+// Mach splittings (conservationLaws/euler/fluxes/machSplittings.ipp:8-43)
 template <class R> __host__ __device__ __forceinline__ R ms_m1(R s, R M) { return R(0.5) * (M + s * fabs(M)); }
 template <class R> __host__ __device__ __forceinline__ R ms_m2(R s, R M) { return s * R(0.25) * (M + s) * (M + s); }
 template <class R> __host__ __device__ __forceinline__ R ms_m4(R s, R M, R beta) {
   return ms_m2(s, M) * (R(1) - s * R(16) * beta * ms_m2(-s, M));
 }
-// (M1 + eps)/(|M| + eps) with eps the largest finite value
-template <class R> __host__ __device__ __forceinline__ R ms_p1(R s, R M) {
-  const R eps = Lim<R>::huge();
-  return (ms_m1(s, M) + eps) / (fabs(M) + eps);
+// (M1 + eps)/(|M| + eps) with eps the largest finite value, as the reference computes it
+// (1 for both signs); with FIX_MACH_SPLIT_P1 (s M1 + eps)/(|M| + eps), eps the smallest
+// normal value: M1/M, 1 on the side the flow comes from and 0 on the other
+template <class R> __host__ __device__ __forceinline__ R ms_p1(R s, R M, unsigned fixes) {
+  const bool fix = (fixes & FIX_MACH_SPLIT_P1) != 0u;
+  const R eps = fix ? Lim<R>::tiny() : Lim<R>::huge();
+  const R m1 = ms_m1(s, M);
+  return ((fix ? s * m1 : m1) + eps) / (fabs(M) + eps);
 }
 template <class R> __host__ __device__ __forceinline__ R ms_p3(R s, R M) { return ms_m2(s, M) * (s * R(2) - M); }
 template <class R> __host__ __device__ __forceinline__ R ms_p5(R s, R M, R alpha) {
@@ -374,7 +407,8 @@ template <class R> __host__ __device__ __forceinline__ R ms_p5(R s, R M, R alpha
 // by_mdot=false: literal reference upwinding by the sign of ua (slau.ipp:124-125);
 // by_mdot=true: upwinding by the sign of the interface mass flux.
 template <class R, bool by_mdot>
-__host__ __device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r) {
+__host__ __device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St<R>& l, const St<R>& r,
+                                                       unsigned fixes = 0u) {
   const R ua = sqrt(R(0.5) * (l.u2 + r.u2));
   R al, ar;
   sqrt_fast(l.a2, al);
@@ -391,8 +425,8 @@ __host__ __device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St
   const R dr = r.r - l.r, dp = r.p - l.p;
   const R mdot_c = l.r * unl + r.r * unr;
   const R mdot = R(0.5) * ((mdot_c - una * dr) * (R(1) - gs) - chi * dp * aa1) * A;
-  const R betal = (fabs(ml) > R(1)) ? ms_p1(R(1), ml) : ms_p3(R(1), ml);
-  const R betar = (fabs(mr) > R(1)) ? ms_p1(R(-1), mr) : ms_p3(R(-1), mr);
+  const R betal = (fabs(ml) > R(1)) ? ms_p1(R(1), ml, fixes) : ms_p3(R(1), ml);
+  const R betar = (fabs(mr) > R(1)) ? ms_p1(R(-1), mr, fixes) : ms_p3(R(-1), mr);
   const R p_c = l.p + r.p;
   const R p_dp = (betal - betar) * dp;
   const R p_du = -ma * (betal + betar - R(1)) * (p_c);
@@ -448,8 +482,8 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> ausmpup_flux(con
   const R mp = Kp * fmax(R(1) - sigma * m0 * m0, R(0)) * delp / (fa * ra * as * as);
   const R uaf = as * (mlp + mrm - mp) * A;
   const R alpha = alpha0 * (R(5) * fu * fu - R(4));
-  const R plp = lsup ? ms_p1(R(1), ml) : ms_p5(R(1), ml, alpha);
-  const R prm = rsup ? ms_p1(R(-1), mr) : ms_p5(R(-1), mr, alpha);
+  const R plp = lsup ? ms_p1(R(1), ml, g.fixes) : ms_p5(R(1), ml, alpha);
+  const R prm = rsup ? ms_p1(R(-1), mr, g.fixes) : ms_p5(R(-1), mr, alpha);
   const R pu = Ku * plp * prm * ra * (fu * as) * (unr - unl);
   const R pa = (plp * l.p + prm * r.p - pu) * A;
   const St<R>& w = (uaf > R(0)) ? l : r;
@@ -474,7 +508,7 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_ws_flux(cons
   sqrt_fast(l.a2, al);
   sqrt_fast(r.a2, ar);
   const Flux5<R> c = central_flux_u(nx, ny, A, l, r, al, ar);
-  // roe average (conservationLaws/euler/fluxes/roe.ipp:150-196)
+  // roe average (conservationLaws/euler/fluxes/roe.ipp:2-48)
   const R cr = sqrt(r.r * l.ir);
   const R wl = R(1) / (R(1) + cr);
   const R wr = R(1) - wl;
@@ -513,8 +547,9 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_ws_flux(cons
 template <class R, int FK>
 __host__ __device__ __forceinline__ Flux5<R> face_flux(const Gas<R>& g, R nx, R ny, R A, const St<R>& l, const St<R>& r) {
   if constexpr (FK == FLUX_ROE) return roe_flux(g, nx, ny, A, l, r);
-  else if constexpr (FK == FLUX_SLAU) return slau_flux<R, true>(nx, ny, A, l, r);
-  else if constexpr (FK == FLUX_SLAU_REF) return slau_flux<R, false>(nx, ny, A, l, r);
+  else if constexpr (FK == FLUX_ROE_FACE) return roe_flux<R, true>(g, nx, ny, A, l, r);
+  else if constexpr (FK == FLUX_SLAU) return slau_flux<R, true>(nx, ny, A, l, r, g.fixes);
+  else if constexpr (FK == FLUX_SLAU_REF) return slau_flux<R, false>(nx, ny, A, l, r, g.fixes);
   else if constexpr (FK == FLUX_AUSMPUP) return ausmpup_flux(g, nx, ny, A, l, r);
   else if constexpr (FK == FLUX_RUSANOV) return rusanov_flux(nx, ny, A, l, r);
   else if constexpr (FK == FLUX_ROE_WS) return roe_ws_flux(g, nx, ny, A, l, r);
@@ -583,9 +618,9 @@ __host__ __device__ __forceinline__ void limit4x2(int kind, const double* a, con
   }
 }
 
-// Slope limiters (limiters/limiter.ipp:141-297), called as limit(central, biased).
+// Slope limiters (limiters/limiter.ipp:8-161), called as limit(central, biased).
 // LIM_VANLEER is the harmonic-mean slope (a|b|+|a|b)/(|a|+|b|+eps);
-// LIM_VANLEER_REF the literal reference expression (limiter.ipp:216-224).
+// LIM_VANLEER_REF the literal reference expression (limiter.ipp:81-89).
 template <class R> __host__ __device__ __forceinline__ R limit(int kind, R a, R b) {
   const R tiny = Lim<R>::tiny();
   switch (kind) {
@@ -665,7 +700,7 @@ template <class R> __host__ __device__ __forceinline__ unsigned limit_piece(int 
 template <class R, int FK>
 __host__ __device__ __forceinline__ unsigned flux_bits(const Gas<R>& g, R nx, R ny, const St<R>& l, const St<R>& r) {
   const R unl = proj(nx, ny, l), unr = proj(nx, ny, r);
-  if constexpr (FK == FLUX_ROE) {
+  if constexpr (FK == FLUX_ROE || FK == FLUX_ROE_FACE) {
     R al, ar;
     sqrt_fast(l.a2, al);
     sqrt_fast(r.a2, ar);
@@ -722,7 +757,7 @@ __host__ __device__ __forceinline__ unsigned flux_bits(const Gas<R>& g, R nx, R 
 }
 
 // Roe average of two primitive states in the face frame, used by the far-field
-// boundary updates (conservationLaws/euler/fluxes/roe.ipp:150-196).
+// boundary updates (conservationLaws/euler/fluxes/roe.ipp:2-48).
 template <class R> __host__ __device__ __forceinline__ void roe_avg_vel(const St<R>& l, const St<R>& r, R* uav, R* u2,
                                                               R* a2, const Gas<R>& g) {
   const R cr = sqrt(r.r / l.r);
@@ -754,7 +789,8 @@ __host__ __device__ __forceinline__ void farfield_update(const Gas<R>& g, R nx, 
   R uav[2], u2a, a2a;
   roe_avg_vel(sI, sF, uav, &u2a, &a2a, g);
   const R thr = (BK == BC_RIEMANN) ? R(0.001) : R(0.0001);
-  if ((uav[0] / sqrt(u2a)) < thr) {
+  const R cosn = uav[0] / sqrt(u2a);
+  if (((g.fixes & FIX_FARFIELD_TRANSVERSE) ? fabs(cosn) : cosn) < thr) {
 #pragma unroll
     for (int k = 0; k < 4; ++k) qb[k] = qi[k];
     if (path) *path = 1u;

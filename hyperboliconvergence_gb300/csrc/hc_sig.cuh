@@ -26,6 +26,7 @@ template <class R, class C> cudaError_t launch_sig_flux(const StageArgs<R>& a, i
     case FLUX_AUSMPUP: return launch_sig_one<R, FLUX_AUSMPUP, C>(a, s);
     case FLUX_RUSANOV: return launch_sig_one<R, FLUX_RUSANOV, C>(a, s);
     case FLUX_ROE_WS: return launch_sig_one<R, FLUX_ROE_WS, C>(a, s);
+    case FLUX_ROE_FACE: return launch_sig_one<R, FLUX_ROE_FACE, C>(a, s);
     default: return launch_sig_one<R, FLUX_CENTRAL, C>(a, s);
   }
 }

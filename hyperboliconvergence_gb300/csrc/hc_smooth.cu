@@ -1,7 +1,7 @@
 // hc_smooth.cu -- residual smoothing of the reference's legacy 1D path on the device:
-// centralImplicitSmoothing (OLD.fieldOperations/centralImplicitSmoothing.ipp:3-52: four
+// centralImplicitSmoothing (OLD.fieldOperations/centralImplicitSmoothing.ipp:2-60: four
 // weighted-Jacobi sweeps, omega 2/3, of (1 - beta delta^2) r1 = r0, beta = (alpha^2-1)/4,
-// the result times alpha) and centralExplicitSmoothing (centralExplicitSmoothing.ipp:4-37).
+// the result times alpha) and centralExplicitSmoothing (centralExplicitSmoothing.ipp:5-39).
 // Ends: 'p' periodic, 'a' one-neighbour normalisation, otherwise unscaled (the
 // reference's GridControls1D::boundaryCondition).  Products and sums are rounded one by
 // one in the reference's order (no contraction), so FP64 results equal the oracle's.

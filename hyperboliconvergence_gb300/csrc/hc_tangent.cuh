@@ -92,7 +92,7 @@ template <class R> __host__ __device__ __forceinline__ Gas<Tan<R>> tan_gas(const
   Gas<T> gt;
   gt.gamma = T(g.gamma, R(0)); gt.gm1 = T(g.gm1, R(0)); gt.gamma1 = T(g.gamma1, R(0));
   gt.Rgas = T(g.Rgas, R(0)); gt.minf = T(g.minf, R(0)); gt.inv_gamma = T(g.inv_gamma, R(0));
-  gt.lref_dt = T(g.lref_dt, R(0)); gt.vscale = g.vscale; gt.pscale = g.pscale;
+  gt.lref_dt = T(g.lref_dt, R(0)); gt.vscale = g.vscale; gt.pscale = g.pscale; gt.fixes = g.fixes;
   return gt;
 }
 

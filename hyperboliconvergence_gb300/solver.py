@@ -37,14 +37,14 @@ class Mesh:
 
     @classmethod
     def cylinder(cls, nr: int, nth: int, rc: float, rb: float, stretch: float = 1.0) -> "Mesh":
-        """O-grid around a cylinder (make_cylinder_mesh, mesh/generate/twoD.h:223-263)."""
+        """O-grid around a cylinder (make_cylinder_mesh, mesh/generate/twoD.h:139-179)."""
         out = np.empty((nr + 1, nth + 1, 2))
         check(_capi.load().hc_mesh_cylinder_nodes(nr, nth, rc, rb, stretch, _dptr(out)))
         return cls(out)
 
     @classmethod
     def linspace(cls, nx: int, ny: int, lox: float, hix: float, loy: float, hiy: float) -> "Mesh":
-        """Uniform Cartesian mesh (make_linspace_mesh, mesh/generate/twoD.h:99-124)."""
+        """Uniform Cartesian mesh (make_linspace_mesh, mesh/generate/twoD.h:15-40)."""
         out = np.empty((nx + 1, ny + 1, 2))
         check(_capi.load().hc_mesh_linspace_nodes(nx, ny, lox, hix, loy, hiy, _dptr(out)))
         return cls(out)
@@ -60,7 +60,7 @@ class Mesh:
 
 
 class Mesh1D:
-    """One-dimensional mesh (Mesh<1,Real>, mesh/generate/oneD.h:12-35): nc cells between
+    """One-dimensional mesh (Mesh<1,Real>, mesh/generate/oneD.h:11-36): nc cells between
     increasing nodes x[0..nc].  A Solver on it runs the 1D Euler path with states of
     shape (3, nc), {u, rho, p}."""
 
@@ -75,7 +75,7 @@ class Mesh1D:
 
     @classmethod
     def linspace(cls, nc: int, lo: float, hi: float) -> "Mesh1D":
-        """Uniform 1D mesh (make_linspace_mesh, mesh/generate/oneD.h:12-35)."""
+        """Uniform 1D mesh (make_linspace_mesh, mesh/generate/oneD.h:11-36)."""
         return cls(lo + (hi - lo) / nc * np.arange(nc + 1))
 
     def centres(self) -> np.ndarray:
@@ -90,7 +90,7 @@ class Solver:
 
     def __init__(self, mesh: Mesh, bc, ref=None, flux="roe", limiter="vanleer", rk="ssp34",
                  precision="fp64", dt="global", cfl=0.5, species=(1.4, 287.058, 1e-4), stream=None, law="euler",
-                 low_mach=None, basis="primitive", tile=None):
+                 low_mach=None, basis="primitive", tile=None, corrections=None):
         self.lib = _capi.load()
         self.mesh = mesh
         self.precision = precision
@@ -118,6 +118,9 @@ class Solver:
         check(self.lib.hc_set_species(self.h, *[float(s) for s in species]))
         if tile is not None:
             self.set_tile(tile)
+        self.corrections = _capi.fix_mask(corrections)
+        if self.corrections:
+            check(self.lib.hc_set_corrections(self.h, self.corrections))
         self.low_mach = None
         if low_mach is not None:
             self.set_low_mach(*low_mach)
@@ -128,6 +131,12 @@ class Solver:
         """Cells per CTA tile of the 2D FP64/FP32 stage kernels: "8x32", "4x32" or "16x16"
         (the results do not depend on it)."""
         check(self.lib.hc_set_tile(self.h, _capi.TILE[tile]))
+
+    def set_corrections(self, corrections) -> None:
+        """Corrections of the reference's defects (hc_set_corrections): None, "all", or names
+        among "mach_split_p1" and "farfield_transverse"."""
+        self.corrections = _capi.fix_mask(corrections)
+        check(self.lib.hc_set_corrections(self.h, self.corrections))
 
     def set_low_mach(self, velocity="convective", pressure="convective", lref=1.0,
                      dt=np.finfo(np.float64).max) -> None:

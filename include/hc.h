@@ -36,17 +36,22 @@ typedef enum {
 
 /* Interface flux (FluxFunctor, conservationLaws/base/concepts.h:97-107) */
 typedef enum {
-  HC_FLUX_ROE = 0,      /* RoeFlux<Euler>, conservationLaws/base/fluxes/roeFlux.ipp:39-95 */
+  HC_FLUX_ROE = 0,      /* RoeFlux<Euler>, conservationLaws/base/fluxes/roeFlux.ipp:2-58 */
   HC_FLUX_SLAU = 1,     /* SLAU2 upwinded by the sign of the mass flux */
   HC_FLUX_SLAU_REF = 2, /* Slau<Convective,Acoustic> as written, conservationLaws/euler/fluxes/slau.ipp:4-161 */
   HC_FLUX_AUSMPUP = 3,  /* AusmPlusUP<V,P>, conservationLaws/euler/fluxes/ausmPlusUP.ipp:6-171;
                            (Convective,Convective) unless hc_set_low_mach chooses V and P */
-  HC_FLUX_RUSANOV = 4,  /* RusanovFlux<Euler>, conservationLaws/base/fluxes/rusanovFlux.ipp:99-147 */
-  HC_FLUX_CENTRAL = 5,  /* CentralFlux<Euler>, conservationLaws/base/fluxes/centralFlux.ipp:25-37 */
-  HC_FLUX_ROE_WS = 6    /* RoeUnprecWS, conservationLaws/euler/fluxes/roeUnprecWS.ipp:2-109 */
+  HC_FLUX_RUSANOV = 4,  /* RusanovFlux<Euler>, conservationLaws/base/fluxes/rusanovFlux.ipp:2-50 */
+  HC_FLUX_CENTRAL = 5,  /* CentralFlux<Euler>, conservationLaws/base/fluxes/centralFlux.ipp:2-14 */
+  HC_FLUX_ROE_WS = 6,   /* RoeUnprecWS, conservationLaws/euler/fluxes/roeUnprecWS.ipp:2-109 */
+  HC_FLUX_ROE_FACE = 7  /* RoeFlux with the Roe-averaged velocity taken into the face frame of the
+                           jump: RoeDissipation (roeFlux.ipp:40-54) rotates the jump but not the
+                           averaged state, so HC_FLUX_ROE is the Roe matrix's dissipation only for
+                           the face normal (1, 0); this variant is rotation-invariant and equal to
+                           HC_FLUX_ROE bit for bit for that normal.  Not in the reference. */
 } hc_flux;
 
-/* LowMachScaling (conservationLaws/euler/euler.h:334-339): AUSM+up's velocity (V) and
+/* LowMachScaling (conservationLaws/euler/euler.h:331-339): AUSM+up's velocity (V) and
  * pressure (P) diffusion scalings */
 typedef enum { HC_SCALING_CONVECTIVE = 0, HC_SCALING_ACOUSTIC = 1, HC_SCALING_ADAPTIVE = 2 } hc_scaling;
 
@@ -55,14 +60,14 @@ typedef enum {
   HC_LIM_NOLIMIT1 = 0, HC_LIM_NOLIMIT2 = 1, HC_LIM_NOLIMIT3 = 2, HC_LIM_VANALBADA = 3,
   HC_LIM_MINMOD = 4, HC_LIM_SUPERBEE = 5, HC_LIM_MC = 6,
   HC_LIM_VANLEER = 7,     /* harmonic-mean van Leer slope */
-  HC_LIM_VANLEER_REF = 8, /* Limiters::VanLeer2 as written, limiters/limiter.ipp:216-224 */
+  HC_LIM_VANLEER_REF = 8, /* Limiters::VanLeer2 as written, limiters/limiter.ipp:81-89 */
   HC_LIM_CADA3 = 9
 } hc_limiter;
 
 /* Basis of the solution field: the SolVarT of SolutionField<SolVarT,2>
  * (solutionField/solutionField.h:56-91).  Gradients, reconstruction and limiting act on
  * the basis variables; fluxes reach the State through set2State of the basis
- * (conservationLaws/euler/transforms/primitive.ipp:101-137, conserved.ipp:31-76); the RK
+ * (conservationLaws/euler/transforms/primitive.ipp:24-60, conservationLaws/euler/transforms/conserved.ipp:31-76); the RK
  * update goes through the conserved set (spatial/eulerForwardUpdate.h:38-92).  State
  * uploads/downloads and ghost reference layers are in the basis.  Euler law only. */
 typedef enum {
@@ -83,7 +88,7 @@ typedef enum { HC_FP64 = 0, HC_FP32 = 1, HC_FP64_DF = 2 } hc_precision;
  * local: per-cell cfl/lambda (spatial/eulerForwardUpdate.h:117-168) */
 typedef enum { HC_DT_GLOBAL = 0, HC_DT_LOCAL = 1 } hc_dtmode;
 
-/* Boundary condition of a mesh side (EulerBCs, conservationLaws/euler/euler.h:34-41).
+/* Boundary condition of a mesh side (EulerBCs, conservationLaws/euler/euler.h:31-41).
  * Sides: 0 = i low, 1 = i high, 2 = j low, 3 = j high; periodic pairs (0,1), (2,3). */
 typedef enum { HC_BC_PERIODIC = 0, HC_BC_FIXED = 1, HC_BC_RIEMANN = 2, HC_BC_ENTROPY = 3, HC_BC_WALL = 4 } hc_bc;
 
@@ -117,7 +122,7 @@ typedef struct {
   long long kernel_launches; /* kernels this context has launched so far */
 } hc_step_stats;
 
-/* Context lifetime.  Replaces the integrate() set-up of timestepping/rungeKutta.h:44-79. */
+/* Context lifetime.  Replaces the integrate() set-up of timestepping/rungeKutta.h:37-95. */
 int hc_context_create(const hc_config* cfg, hc_ctx** out);
 int hc_context_destroy(hc_ctx* ctx);
 /* Run the context's kernels on this CUDA stream (a cudaStream_t; NULL = the legacy
@@ -126,12 +131,12 @@ int hc_context_destroy(hc_ctx* ctx);
 int hc_set_stream(hc_ctx* ctx, void* stream);
 int hc_get_stream(hc_ctx* ctx, void** stream);
 
-/* Mesh<2,Real> nodes (mesh/mesh.h:283-321); cells and face metrics are derived on the
- * device: geom::volume/surface, dual, xmetrics (geometry/volume.ipp:55-96,
- * geometry/surface.ipp:12-29, mesh/dual.ipp:42-83, spatial/lsqMetrics.h:119-251). */
+/* Mesh<2,Real> nodes (mesh/mesh.h:19-57); cells and face metrics are derived on the
+ * device: geom::volume/surface, dual, xmetrics (geometry/volume.ipp:25-66,
+ * geometry/surface.ipp:12-29, mesh/dual.ipp:42-83, spatial/lsqMetrics.h:31-163). */
 int hc_mesh_upload(hc_ctx* ctx, int ni, int nj, const double* nodes_xy);
 
-/* Mesh<1,Real> nodes (mesh/generate/oneD.h:12-35): the one-dimensional Euler path
+/* Mesh<1,Real> nodes (mesh/generate/oneD.h:11-36): the one-dimensional Euler path
  * (interiorResidual, spatial/residualCalc.h:74-127, with the 1D boundary loops and LSQ
  * metrics).  nc cells between increasing nodes x[0..nc]; the state is 3 planes {u, rho, p}
  * (the nDim = 1 primitive set), the residual 3 flux planes {rho u, rho, rho E} and the
@@ -163,7 +168,7 @@ int hc_state_download(hc_ctx* ctx, double* prim_soa);
 int hc_state_upload_device(hc_ctx* ctx, const void* prim_soa_device);
 int hc_state_download_device(hc_ctx* ctx, void* prim_soa_device);
 
-/* One residual evaluation of the current state: residualCalc (spatial/residualCalc.h:45-69)
+/* One residual evaluation of the current state: residualCalc (spatial/residualCalc.h:27-69)
  * including the boundary update (spatial/boundary/boundaryUpdate.h:137-266).
  * out: 5 planes -- 4 conserved flux sums and the spectral-radius sum. */
 int hc_residual(hc_ctx* ctx, double* out5);
@@ -203,7 +208,7 @@ int hc_steady_run(hc_ctx* ctx, const hc_steady_controls* controls, double* histo
                   hc_steady_stats* stats);
 
 /* Residual smoothing of the reference's legacy 1D path (OLD.fieldOperations/
- * centralImplicitSmoothing.ipp:3-52, centralExplicitSmoothing.ipp:4-37) on device
+ * centralImplicitSmoothing.ipp:2-60, centralExplicitSmoothing.ipp:5-39) on device
  * memory: nplanes planes of n >= 2 values (plane stride n).  r1 may equal or overlap r0:
  * the explicit kind then smooths a copy of r0 taken from the stream-ordered allocator.
  * HC_SMOOTH_IMPLICIT: four weighted-Jacobi sweeps (omega 2/3) of
@@ -239,13 +244,13 @@ int hc_spectral_radius(const double* lambda_sum_device, const double* vol_device
 int hc_spectral_radius_noalloc(const double* lambda_sum_device, const double* vol_device, long long ncell,
                                double* out_device, void* stream);
 
-/* Dual-time stepping: ODE::Implicit::MultiStep in physical time (ode.h:10-83) with explicit
+/* Dual-time stepping: ODE::Implicit::MultiStep in physical time (ode.h:12-82) with explicit
  * pseudo-time iterations, the scheme of the reference's legacy 1D driver
- * (timestepping/dualTime.ipp:5-99, OLD.fieldOperations/dualTimeResidual.ipp:3-42) on this
+ * (timestepping/dualTime.ipp:4-105, OLD.fieldOperations/dualTimeResidual.ipp:2-41) on this
  * path.  Each physical step solves b_0 Q(u)/dt - g_0 R(u) = -(b_1 Q_n + b_2 Q_{n-1})/dt +
  * g_1 R(u_n) (Q the conserved set, R the flux residual, times the cell volume) by RK steps of
  * the context's table in pseudo time, the context's cfl and dt mode, each pseudo step
- * dtau / (1 + b_0 dtau / dt) (dualTime.ipp:61-62; local pseudo steps take the physical term
+ * dtau / (1 + b_0 dtau / dt) (dualTime.ipp:65-66; local pseudo steps take the physical term
  * into the spectral radius); the inner loop stops after inner_max steps or once the density
  * dual-time residual fell by inner_drop (checked every check_every steps; 0 = never).  The
  * first step of BDF2 takes u_{n-1} = u_n, as the reference's initialisation does. */
@@ -254,7 +259,7 @@ typedef struct {
   int outer_steps;   /* physical steps */
   double dt;         /* physical timestep; <= 0: cfl_outer / max(lambda/V) of the initial state */
   double cfl_outer;
-  int scheme;        /* hc_multistep: backwardDifference1/2, trapeziumRule2 (ode.h:30-83) */
+  int scheme;        /* hc_multistep: backwardDifference1/2, trapeziumRule2 (ode.h:34-82) */
   int inner_max;     /* pseudo-time steps per physical step at most */
   double inner_drop; /* stop once ||R*_rho|| <= inner_drop * its first value (0: run inner_max) */
   int check_every;   /* pseudo-time steps between convergence checks */
@@ -286,9 +291,9 @@ int hc_dual_time_run(hc_ctx* ctx, const hc_dual_time_controls* ctl, hc_dual_time
 int hc_face_signatures(hc_ctx* ctx, unsigned long long* sig_i, unsigned long long* sig_j, double* arg_i,
                        double* arg_j);
 
-/* Mesh generators: make_cylinder_mesh (mesh/generate/twoD.h:223-263), radial
+/* Mesh generators: make_cylinder_mesh (mesh/generate/twoD.h:139-179), radial
  * spacing stretched geometrically when stretch != 1; make_linspace_mesh
- * (mesh/generate/twoD.h:99-124). */
+ * (mesh/generate/twoD.h:15-40). */
 int hc_mesh_cylinder_nodes(int nr, int nth, double rc, double rb, double stretch, double* nodes_xy);
 int hc_mesh_linspace_nodes(int nx, int ny, double lox, double hix, double loy, double hiy, double* nodes_xy);
 
@@ -372,6 +377,23 @@ typedef struct {
  * gives the same results. */
 int hc_set_tile(hc_ctx* ctx, int tile);
 
+/* Corrections of two defects of the reference, off by default so that the reference's
+ * results are reproduced as it computes them.  Not in the reference.
+ * HC_FIX_MACH_SPLIT_P1: MachSplit_P1 (conservationLaws/euler/fluxes/machSplittings.ipp:26-31)
+ *   is (M1 + eps)/(|M| + eps) with eps = numeric_limits<Real>::max(), which rounds to 1 for
+ *   both signs: on supersonic faces SLAU and AUSM+up add the pressure of both sides, so
+ *   F(q, q) differs from the exact flux by p n.  Corrected, P1 is M1/M, 1 upwind and 0
+ *   downwind: (s M1 + eps)/(|M| + eps) with eps the smallest normal value.
+ * HC_FIX_FARFIELD_TRANSVERSE: the Riemann and entropy far fields
+ *   (conservationLaws/euler/boundary/riemann.ipp:48-50, entropy.ipp:47-49) copy the interior
+ *   state when u_n/|u| is below a threshold, without the absolute value, so every outflow
+ *   face copies the interior and a subsonic outflow receives nothing from the far field.
+ *   Corrected, the test is |u_n|/|u| and outflow faces get the characteristic update.
+ * The face-frame Roe dissipation is a flux of its own, HC_FLUX_ROE_FACE.  Applies from the
+ * next step; batches take the same mask through hc_batch_set_corrections. */
+typedef enum { HC_FIX_MACH_SPLIT_P1 = 1, HC_FIX_FARFIELD_TRANSVERSE = 2, HC_FIX_ALL = 3 } hc_fix;
+int hc_set_corrections(hc_ctx* ctx, unsigned mask);
+
 /* ninst meshes; nodes[k] as for hc_mesh_upload; bc[4k..4k+3] and ref[4k..4k+3]
  * as for hc_set_bcs (ref entries may be NULL where hc_set_bcs allows it).  cfg->law
  * HC_LAW_SCALAR: scalar advection instances (Rusanov or central flux; periodic, fixed
@@ -384,6 +406,7 @@ int hc_batch_set_stream(hc_batch* b, void* stream);
 int hc_batch_state_upload(hc_batch* b, int inst, const double* prim_soa);
 int hc_batch_state_download(hc_batch* b, int inst, double* prim_soa);
 int hc_batch_set_schedule(hc_batch* b, const hc_schedule* s);
+int hc_batch_set_corrections(hc_batch* b, unsigned mask);  /* hc_set_corrections for a batch */
 int hc_batch_get_schedule(hc_batch* b, hc_schedule* s);
 /* Enqueue nsteps RK steps of every instance (hc_batch_mode). */
 int hc_batch_step_async(hc_batch* b, int nsteps, int mode);

@@ -44,8 +44,8 @@ template <class R> R freeze(const R& x) { return x; }
 
 // ---------------------------------------------------------------- enums
 enum Flux { FLUX_ROE = 0, FLUX_SLAU = 1, FLUX_SLAU_REF = 2, FLUX_AUSMPUP = 3,
-            FLUX_RUSANOV = 4, FLUX_CENTRAL = 5, FLUX_ROE_WS = 6 };
-// LowMachScaling (conservationLaws/euler/euler.h:334-339)
+            FLUX_RUSANOV = 4, FLUX_CENTRAL = 5, FLUX_ROE_WS = 6, FLUX_ROE_FACE = 7 };
+// LowMachScaling (conservationLaws/euler/euler.h:331-339)
 enum Scaling { SCALING_CONVECTIVE = 0, SCALING_ACOUSTIC = 1, SCALING_ADAPTIVE = 2 };
 enum Limiter { LIM_NOLIMIT1 = 0, LIM_NOLIMIT2 = 1, LIM_NOLIMIT3 = 2, LIM_VANALBADA = 3,
                LIM_MINMOD = 4, LIM_SUPERBEE = 5, LIM_MC = 6, LIM_VANLEER = 7,
@@ -58,7 +58,15 @@ enum DtMode { DT_GLOBAL = 0, DT_LOCAL = 1 };
 // Species<Euler> (conservationLaws/euler/euler.h:48-60)
 template <class R> struct Species {
   R gamma, minf, lref, nu, pr, dt, Rgas, gamma1;
+  // corrections of two defects of the reference (FIX_*), 0 = as the reference computes
+  unsigned fixes;
 };
+// FIX_MACH_SPLIT_P1: MachSplit_P1 as M1/M, the 1/0 split it is meant to be, instead of the
+// (M1 + eps)/(|M| + eps) with the largest eps that it is (machSplittings.ipp:26-31);
+// FIX_FARFIELD_TRANSVERSE: the
+// far fields' transverse-flow test on |u_n|/|u| (conservationLaws/euler/boundary/riemann.ipp:48-50, entropy.ipp:47-49), so
+// outflow faces get the characteristic update instead of an interior copy
+enum : unsigned { FIX_MACH_SPLIT_P1 = 1u, FIX_FARFIELD_TRANSVERSE = 2u };
 
 // get_air_species (conservationLaws/euler/species.ipp:1-17)
 template <class R> Species<R> air_species() {
@@ -66,6 +74,7 @@ template <class R> Species<R> air_species() {
   s.gamma = 1.4; s.minf = 0.0001; s.lref = 1.; s.pr = 0.7; s.nu = 1.81e-5;
   s.dt = std::numeric_limits<R>::max(); s.Rgas = 287.058;
   s.gamma1 = 1. / (s.gamma - 1.);
+  s.fixes = 0u;
   return s;
 }
 
@@ -92,12 +101,12 @@ template <class R> Face<R> surface(const R* p0, const R* p1) {
   s.c[0] = p0[0] + 0.5 * t0x;
   s.c[1] = p0[1] + 0.5 * t0y;
   const R ux = l1 * t1x, uy = l1 * t1y;  // l1*tangent1
-  s.n[0] = -uy; s.n[1] = ux;               // orthog (geometry/operations.ipp:140-144)
+  s.n[0] = -uy; s.n[1] = ux;               // orthog (geometry/operations.ipp:43-47)
   s.t[0] = l1 * t0x; s.t[1] = l1 * t0y;
   return s;
 }
 
-// geom::volume(p0..p3) (geometry/volume.ipp:55-96): bilinear shape functions
+// geom::volume(p0..p3) (geometry/volume.ipp:25-66): bilinear shape functions
 // at the element centre (fem/fem.h:14-77).  The value is |J(0,0)|, which is a
 // quarter of the quad's area; it is kept as the reference defines it.
 template <class R> Cell<R> volume(const R* p0, const R* p1, const R* p2, const R* p3) {
@@ -120,7 +129,7 @@ template <class R> Cell<R> volume(const R* p0, const R* p1, const R* p2, const R
 }
 
 // ---------------------------------------------------------------- transforms
-// set2State(primitive) (conservationLaws/euler/transforms/primitive.ipp:101-137)
+// set2State(primitive) (conservationLaws/euler/transforms/primitive.ipp:24-60)
 template <class R> State<R> prim2state(const Species<R>& sp, const R* q) {
   State<R> s;
   s.u2 = 0;
@@ -209,7 +218,7 @@ template <class R> void rotate_from(const Face<R>& f, const R* q0, R* q1) {
   }
 }
 
-// delta2Delta conserved -> primitive (primitive.ipp:142-184)
+// delta2Delta conserved -> primitive (primitive.ipp:65-107)
 template <class R> void dcons2dprim(const Species<R>& sp, const State<R>& s, const R* dqc, R* dqp) {
   const R dr = dqc[2], dre = dqc[3];
   const R rho1 = 1. / s.r;
@@ -225,7 +234,7 @@ template <class R> void dcons2dprim(const Species<R>& sp, const State<R>& s, con
   dqp[2] = dr; dqp[3] = dp;
 }
 
-// delta2Delta primitive -> conserved (primitive.ipp:187-233)
+// delta2Delta primitive -> conserved (primitive.ipp:110-156)
 template <class R> void dprim2dcons(const Species<R>& sp, const State<R>& s, const R* dqp, R* dqc) {
   const R dr = dqp[2], dp = dqp[3];
   const R r = s.r;
@@ -241,7 +250,7 @@ template <class R> void dprim2dcons(const Species<R>& sp, const State<R>& s, con
   dqc[2] = dr; dqc[3] = dre;
 }
 
-// delta2Delta characteristic -> primitive (primitive.ipp:238-275)
+// delta2Delta characteristic -> primitive (characteristic.ipp:5-41)
 template <class R> void dchar2dprim(const Species<R>& sp, const State<R>& s, const R* dqw, R* dqp) {
   const R r = s.r;
   const R a = sqrt(s.a2);
@@ -252,7 +261,7 @@ template <class R> void dchar2dprim(const Species<R>& sp, const State<R>& s, con
   dqp[2] = dr; dqp[3] = dp;
 }
 
-// delta2Delta primitive -> characteristic (primitive.ipp:277-313)
+// delta2Delta primitive -> characteristic (characteristic.ipp:44-79)
 template <class R> void dprim2dchar(const Species<R>& sp, const State<R>& s, const R* dqp, R* dqw) {
   const R r1 = 1. / s.r;
   const R a1 = 1. / sqrt(s.a2);
@@ -264,7 +273,7 @@ template <class R> void dprim2dchar(const Species<R>& sp, const State<R>& s, con
 }
 
 // ---------------------------------------------------------------- fluxes
-// exactFlux (conservationLaws/euler/fluxes/exactFlux.ipp:231-263)
+// exactFlux (conservationLaws/euler/fluxes/exactFlux.ipp:4-36)
 template <class R> FluxRes<R> exact_flux(const R* n, const State<R>& s) {
   const R r = s.r, p = s.p, h = s.h;
   const R a = sqrt(s.a2);
@@ -277,7 +286,7 @@ template <class R> FluxRes<R> exact_flux(const R* n, const State<R>& s) {
   return fr;
 }
 
-// CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:25-37)
+// CentralFlux (conservationLaws/base/fluxes/centralFlux.ipp:2-14)
 template <class R> FluxRes<R> central_flux(const Face<R>& f, const State<R>& sl, const State<R>& sr) {
   const FluxRes<R> fl = exact_flux(f.n, sl), fr = exact_flux(f.n, sr);
   FluxRes<R> o;
@@ -286,7 +295,7 @@ template <class R> FluxRes<R> central_flux(const Face<R>& f, const State<R>& sl,
   return o;
 }
 
-// roeAverage (conservationLaws/euler/fluxes/roe.ipp:150-196)
+// roeAverage (conservationLaws/euler/fluxes/roe.ipp:2-48)
 template <class R> State<R> roe_average(const Species<R>& sp, const State<R>& sl, const State<R>& sr) {
   State<R> a;
   const R cr = sqrt(sr.r / sl.r);
@@ -308,7 +317,7 @@ template <class R> State<R> roe_average(const Species<R>& sp, const State<R>& sl
   return a;
 }
 
-// entropyfix, Harten eps=0.05 (conservationLaws/euler/fluxes/roe.ipp:198-226)
+// entropyfix, Harten eps=0.05 (conservationLaws/euler/fluxes/roe.ipp:50-78)
 template <class R> void entropy_fix(const R* la, const R* ll, const R* lr, R* sp) {
   const R ua = fabs(la[0]);
   sp[0] = ua; sp[3] = ua;
@@ -321,9 +330,15 @@ template <class R> void entropy_fix(const R* la, const R* ll, const R* lr, R* sp
   }
 }
 
-// RoeDissipation (conservationLaws/base/fluxes/roeFlux.ipp:59-95)
+// RoeDissipation (conservationLaws/base/fluxes/roeFlux.ipp:22-58)
+// face_frame = false is RoeDissipation as written: the jump is rotated to the face frame
+// while the Roe-averaged state keeps its global-frame velocity, which is the Roe matrix's
+// dissipation only for the face normal (1, 0).  face_frame = true (FLUX_ROE_FACE, not in
+// the reference) takes the averaged velocity into the face frame too, which makes the flux
+// invariant under rotation and equal to the literal one for the normal (1, 0).
 template <class R> FluxRes<R> roe_dissipation(const Species<R>& sp, const Face<R>& f,
-                                              const State<R>& sl, const State<R>& sr) {
+                                              const State<R>& sl, const State<R>& sr,
+                                              bool face_frame = false) {
   const State<R> ra = roe_average(sp, sl, sr);
   R wa[4], wl[4], wr[4], lam[4];
   wavespeeds(f.n, ra, wa); wavespeeds(f.n, sl, wl); wavespeeds(f.n, sr, wr);
@@ -333,12 +348,19 @@ template <class R> FluxRes<R> roe_dissipation(const Species<R>& sp, const Face<R
   for (int i = 0; i < 4; ++i) dq[i] = cr[i] - cl[i];
   rotate_to(f, dq, dqc);
   R dqp[4], dqw[4];
-  dcons2dprim(sp, ra, dqc, dqp);
-  dprim2dchar(sp, ra, dqp, dqw);
+  // face_frame: the averaged state's velocity in the frame of the jump, {n.u, t.u}
+  State<R> rf = ra;
+  if (face_frame) {
+    R u[4] = {ra.u[0], ra.u[1], 0, 0}, uf[4];
+    rotate_to(f, u, uf);
+    rf.u[0] = uf[0]; rf.u[1] = uf[1];
+  }
+  dcons2dprim(sp, rf, dqc, dqp);
+  dprim2dchar(sp, rf, dqp, dqw);
   for (int i = 0; i < 4; ++i) dqw[i] = lam[i] * dqw[i];
   R dp2[4], dc2[4], fd[4];
-  dchar2dprim(sp, ra, dqw, dp2);
-  dprim2dcons(sp, ra, dp2, dc2);
+  dchar2dprim(sp, rf, dqw, dp2);
+  dprim2dcons(sp, rf, dp2, dc2);
   rotate_from(f, dc2, fd);
   FluxRes<R> o;
   const R s = -0.5 * f.area;
@@ -347,18 +369,18 @@ template <class R> FluxRes<R> roe_dissipation(const Species<R>& sp, const Face<R
   return o;
 }
 
-// RoeFlux = Central + RoeDissipation (conservationLaws/base/fluxes/roeFlux.ipp:39-56)
+// RoeFlux = Central + RoeDissipation (conservationLaws/base/fluxes/roeFlux.ipp:2-19)
 template <class R> FluxRes<R> roe_flux(const Species<R>& sp, const Face<R>& f,
-                                       const State<R>& sl, const State<R>& sr) {
+                                       const State<R>& sl, const State<R>& sr, bool face_frame = false) {
   const FluxRes<R> c = central_flux(f, sl, sr);
-  const FluxRes<R> d = roe_dissipation(sp, f, sl, sr);
+  const FluxRes<R> d = roe_dissipation(sp, f, sl, sr, face_frame);
   FluxRes<R> o;
   for (int i = 0; i < 4; ++i) o.f[i] = c.f[i] + d.f[i];
   o.lam = fmax(c.lam, d.lam);
   return o;
 }
 
-// RusanovFlux (conservationLaws/base/fluxes/rusanovFlux.ipp:99-147)
+// RusanovFlux (conservationLaws/base/fluxes/rusanovFlux.ipp:2-50)
 template <class R> FluxRes<R> rusanov_flux(const Species<R>& sp, const Face<R>& f,
                                            const State<R>& sl, const State<R>& sr) {
   FluxRes<R> o = central_flux(f, sl, sr);
@@ -372,15 +394,19 @@ template <class R> FluxRes<R> rusanov_flux(const Species<R>& sp, const Face<R>& 
   return o;
 }
 
-// Mach-number splittings (conservationLaws/euler/fluxes/machSplittings.ipp:163-204)
+// Mach-number splittings (conservationLaws/euler/fluxes/machSplittings.ipp:8-43)
 template <class R> R msplit_m1(int s, R M) { return 0.5 * (M + s * fabs(M)); }
 template <class R> R msplit_m2(int s, R M) { return s * 0.25 * (M + s) * (M + s); }
 template <class R> R msplit_m4(int s, R M, R beta) {
   return msplit_m2(s, M) * (1. - s * 16. * beta * msplit_m2(-s, M));
 }
-template <class R> R msplit_p1(int s, R M) {
-  constexpr R eps = std::numeric_limits<R>::max();
-  return (msplit_m1(s, M) + eps) / (fabs(M) + eps);
+// as written: (M1 + eps)/(|M| + eps), eps the largest value (1 for both signs); with
+// FIX_MACH_SPLIT_P1: (s M1 + eps)/(|M| + eps), eps the smallest normal value, i.e. M1/M
+template <class R> R msplit_p1(int s, R M, unsigned fixes) {
+  const bool fix = (fixes & FIX_MACH_SPLIT_P1) != 0u;
+  const R eps = fix ? std::numeric_limits<R>::min() : std::numeric_limits<R>::max();
+  const R m1 = msplit_m1(s, M);
+  return ((fix ? R(s * m1) : m1) + eps) / (fabs(M) + eps);
 }
 template <class R> R msplit_p3(int s, R M) { return msplit_m2(s, M) * (s * 2. - M); }
 template <class R> R msplit_p5(int s, R M, R alpha) {
@@ -412,8 +438,8 @@ template <class R> FluxRes<R> slau_flux(const Species<R>& sp, const Face<R>& f,
   const R mdot = 0.5 * ((mdot_c - mdot_dr) * (1. - g) - mdot_dp) * f.area;
   const unsigned mlsup = fabs(ml) > 1 ? 1 : 0, mlsub = 1 - mlsup;
   const unsigned mrsup = fabs(mr) > 1 ? 1 : 0, mrsub = 1 - mrsup;
-  const R betal = mlsub * msplit_p3(1, ml) + mlsup * msplit_p1(1, ml);
-  const R betar = mrsub * msplit_p3(-1, mr) + mrsup * msplit_p1(-1, mr);
+  const R betal = mlsub * msplit_p3(1, ml) + mlsup * msplit_p1(1, ml, sp.fixes);
+  const R betar = mrsub * msplit_p3(-1, mr) + mrsup * msplit_p1(-1, mr, sp.fixes);
   const R p_c = sl.p + sr.p;
   const R p_dp = (betal - betar) * dp;
   const R p_du = -ma * (betal + betar - 1.) * (p_c);
@@ -463,8 +489,8 @@ template <class R> FluxRes<R> ausmpup_flux(const Species<R>& sp, const Face<R>& 
   const R mp = Kp * fmax(1. - sigma * m0 * m0, (R)0.) * delp / (fa_p * ra * as * as);
   const R uaf = as * (mlp + mrm - mp) * f.area;
   const R alpha = alpha0 * (5. * fa_u * fa_u - 4.);
-  const R plp = mlsub * msplit_p5(1, ml, alpha) + mlsup * msplit_p1(1, ml);
-  const R prm = mrsub * msplit_p5(-1, mr, alpha) + mrsup * msplit_p1(-1, mr);
+  const R plp = mlsub * msplit_p5(1, ml, alpha) + mlsup * msplit_p1(1, ml, sp.fixes);
+  const R prm = mrsub * msplit_p5(-1, mr, alpha) + mrsup * msplit_p1(-1, mr, sp.fixes);
   const R delu = unr - unl;
   const R pu = Ku * plp * prm * ra * (fa_u * as) * delu;
   const R pa = (plp * sl.p + prm * sr.p - pu) * f.area;
@@ -522,6 +548,7 @@ template <class R> FluxRes<R> face_flux(int kind, const Species<R>& sp, const Fa
                                         int vscale = SCALING_CONVECTIVE, int pscale = SCALING_CONVECTIVE) {
   switch (kind) {
     case FLUX_ROE: return roe_flux(sp, f, sl, sr);
+    case FLUX_ROE_FACE: return roe_flux(sp, f, sl, sr, true);
     case FLUX_SLAU: return slau_flux(sp, f, sl, sr, true);
     case FLUX_SLAU_REF: return slau_flux(sp, f, sl, sr, false);
     case FLUX_AUSMPUP: return ausmpup_flux(sp, f, sl, sr, vscale, pscale);
@@ -532,9 +559,9 @@ template <class R> FluxRes<R> face_flux(int kind, const Species<R>& sp, const Fa
 }
 
 // ---------------------------------------------------------------- limiters
-// limiters/limiter.ipp:141-297.  VANLEER is the textbook harmonic-mean slope
+// limiters/limiter.ipp:8-161.  VANLEER is the textbook harmonic-mean slope
 // (a|b|+|a|b)/(|a|+|b|+eps) with the reference's eps convention; VANLEER_REF
-// is the literal reference expression (b+|b|)/(a+|b|+eps) (limiter.ipp:216-224).
+// is the literal reference expression (b+|b|)/(a+|b|+eps) (limiter.ipp:81-89).
 template <class R> R limit(int kind, R a, R b) {
   switch (kind) {
     case LIM_NOLIMIT1: return 0;
@@ -584,8 +611,8 @@ template <class R> R limit(int kind, R a, R b) {
 }
 
 // ---------------------------------------------------------------- LSQ
-// lsq::xmetric (lsq/lsq.h:302-318), lsq::qmetric (lsq/lsq.h:367-389),
-// lsq::factor (lsq/lsq.h:403-412), lsq::solve (lsq/lsq.h:437-459).
+// lsq::xmetric (lsq/xmetric.ipp:53-69), lsq::qmetric (lsq/qmetric.ipp:48-70),
+// lsq::factor (lsq/factor_solve.ipp:13-22), lsq::solve (lsq/factor_solve.ipp:47-69).
 // QMetric index is q[2*var+dim] (the intent of lsq/lsq.h:72).
 template <class R> struct XM { R x[3]; };
 template <class R> struct QM { R q[8]; };
@@ -660,13 +687,13 @@ template <class R> unsigned limit_piece(int kind, R a, R b) {
 }
 
 // flux branches of two face states, with the reference's expressions: Roe -- Harten's
-// fix on waves 1 and 2 (roe.ipp:198-226); SLAU -- |M_L| > 1, |M_R| > 1, mean-speed Mach
+// fix on waves 1 and 2 (roe.ipp:50-78); SLAU -- |M_L| > 1, |M_R| > 1, mean-speed Mach
 // > 1 (slau.ipp:18-31); AUSM+up -- |M_L| > 1, |M_R| > 1, left critical speed below the
 // right (ausmPlusUP.ipp:30-55); others -- right spectral radius larger
 template <class R> unsigned flux_bits(int kind, const Species<R>& sp, const Face<R>& f, const State<R>& sl,
                                       const State<R>& sr) {
   const R unl = proj_vel(f.n, sl), unr = proj_vel(f.n, sr);
-  if (kind == FLUX_ROE) {
+  if (kind == FLUX_ROE || kind == FLUX_ROE_FACE) {
     const State<R> ra = roe_average(sp, sl, sr);
     R wa[4], wl[4], wr[4];
     wavespeeds(f.n, ra, wa); wavespeeds(f.n, sl, wl); wavespeeds(f.n, sr, wr);
@@ -728,7 +755,12 @@ void bc_riemann(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf
   R ri[4], rf[4];
   rotate_to(f, qi, ri); rotate_to(f, qf, rf);
   const State<R> sA = roe_average(sp, basis2state(sp, ri, basis), basis2state(sp, rf, basis));
-  if ((sA.u[0] / sqrt(sA.u2)) < 0.001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; if (path) *path = 1u; return; }
+  const R cosn = sA.u[0] / sqrt(sA.u2);
+  if (((sp.fixes & FIX_FARFIELD_TRANSVERSE) ? R(fabs(cosn)) : cosn) < 0.001) {
+    for (int k = 0; k < 4; ++k) qb[k] = qi[k];
+    if (path) *path = 1u;
+    return;
+  }
   const R ma = sA.u[0] / sqrt(sA.a2);
   const bool inflow = ma > 0;
   const R* quw = inflow ? qf : qi;
@@ -759,7 +791,12 @@ void bc_entropy(const Species<R>& sp, const Face<R>& f, const R* qi, const R* qf
   R ri[4], rf[4];
   rotate_to(f, qi, ri); rotate_to(f, qf, rf);
   const State<R> sA = roe_average(sp, basis2state(sp, ri, basis), basis2state(sp, rf, basis));
-  if ((sA.u[0] / sqrt(sA.u2)) < 0.0001) { for (int k = 0; k < 4; ++k) qb[k] = qi[k]; if (path) *path = 1u; return; }
+  const R cosn = sA.u[0] / sqrt(sA.u2);
+  if (((sp.fixes & FIX_FARFIELD_TRANSVERSE) ? R(fabs(cosn)) : cosn) < 0.0001) {
+    for (int k = 0; k < 4; ++k) qb[k] = qi[k];
+    if (path) *path = 1u;
+    return;
+  }
   const R ma = sA.u[0] / sqrt(sA.a2);
   const bool inflow = ma > 0;
   const R* quw = inflow ? qf : qi;

@@ -3,7 +3,7 @@
 // TEST INFRASTRUCTURE ONLY (see hc_oracle.hpp).  The reference's law
 // (conservationLaws/scalarAdvection/scalarAdvection.h:45-98) carries the
 // conserved set {u, v, q} in 2D: an advected scalar q and its advecting velocity,
-// constant in time.  Exact flux (fluxes/exactFlux.ipp:8-21): (0, 0, u_n q),
+// constant in time.  Exact flux (conservationLaws/scalarAdvection/fluxes/exactFlux.ipp:8-21): (0, 0, u_n q),
 // spectral radius |u_n|.  Rusanov and central fluxes are the reference's
 // law-generic ones (conservationLaws/base/fluxes/rusanovFlux.ipp:2-50,
 // centralFlux.ipp:2-14); the Riemann ghost update picks the boundary value on

@@ -1,9 +1,9 @@
 // hc_oracle_smooth.hpp -- residual smoothing of the reference's legacy 1D path.
 //
 // TEST INFRASTRUCTURE ONLY (see hc_oracle.hpp).  Restates, in the order the reference
-// writes it, OLD.fieldOperations/centralImplicitSmoothing.ipp:3-52 (centralImplicit-
+// writes it, OLD.fieldOperations/centralImplicitSmoothing.ipp:2-60 (centralImplicit-
 // Smoothing: four weighted-Jacobi sweeps, omega 2/3, of (1 - beta delta^2) r1 = r0 with
-// beta = (alpha^2 - 1)/4, the result times alpha) and centralExplicitSmoothing.ipp:4-37
+// beta = (alpha^2 - 1)/4, the result times alpha) and centralExplicitSmoothing.ipp:5-39
 // (centralExplicitSmoothing: r1 = r0 + gamma delta^2 r0 written as face differences,
 // gamma = ((1 + 4 beta)/alpha - 1)/4).  The line's end treatment is the reference's
 // GridControls1D::boundaryCondition character: 'p' periodic, 'a' one-neighbour

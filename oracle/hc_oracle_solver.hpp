@@ -7,7 +7,7 @@
 //   D2  LSQ stencil = the 4 face neighbours, periodic wrap neighbours included
 //       (their centres translated by the periodic shift); non-periodic sides
 //       add the mirrored-point xmetric with zero q contribution
-//       (spatial/lsqMetrics.h:155-251, qmetrics spatial/lsqMetrics.h:269-301).
+//       (spatial/lsqMetrics.h:104-163, qmetrics spatial/lsqMetrics.h:181-213).
 //   D3  QMetric index q[2*var+dim]; biased gradient projected on face.metric[0].
 //   D4  ghost faces: ghost side unreconstructed, interior side MUSCL with the
 //       mirror term removed; wall pressure from the interior state extrapolated
@@ -92,7 +92,7 @@ template <class R> struct Solver {
     for (int d = 0; d < 2; ++d)
       s[d] = 0.5 * ((node(i, nj)[d] - node(i, 0)[d]) + (node(i + 1, nj)[d] - node(i + 1, 0)[d]));
   }
-  // mirrored-point displacement of a boundary cell (spatial/lsqMetrics.h:204-212)
+  // mirrored-point displacement of a boundary cell (spatial/lsqMetrics.h:119-123)
   void mirror(int side, int k, R* m) const {
     int i0, j0, i1, j1;
     if (side == 0) { i0 = 0; j0 = k; i1 = 1; j1 = k; }
@@ -168,7 +168,7 @@ template <class R> struct Solver {
         const XM<R> v = xmetric<R>(b.c[0] - (a.c[0] - s[0]), b.c[1] - (a.c[1] - s[1]));
         addx(cid(i, nj - 1), v); addx(cid(i, 0), v);
       }
-    // boundary_xmetrics order (spatial/lsqMetrics.h:214-249): left/right per j, then bottom/top per i
+    // boundary_xmetrics order (spatial/lsqMetrics.h:126-162): left/right per j, then bottom/top per i
     for (int j = 0; j < nj; ++j)
       for (int side = 0; side < 2; ++side)
         if (bc[side] != BC_PERIODIC) { R m[2]; mirror(side, j, m); addx(side_cell(side, j), xmetric<R>(m[0], m[1])); }
@@ -203,7 +203,7 @@ template <class R> struct Solver {
     }
   }
 
-  // ---- qmetrics with periodic wrap (spatial/lsqMetrics.h:269-301, D2)
+  // ---- qmetrics with periodic wrap (spatial/lsqMetrics.h:181-213, D2)
   void qmetrics(const std::vector<R>& q) {
     for (auto& m : qm) m = QM<R>{};
     auto addq = [&](size_t a, const QM<R>& v) { for (int k = 0; k < 8; ++k) qm[a].q[k] += v.q[k]; };
@@ -237,7 +237,7 @@ template <class R> struct Solver {
       }
   }
 
-  // ---- make_muscl_flux (spatial/muscl.h:13-59) with bias_solves (lsq/lsq.h:461-490)
+  // ---- make_muscl_flux (spatial/muscl.h:13-59) with bias_solves (lsq/factor_solve.ipp:71-100)
   FluxRes<R> muscl(const Face<R>& f, const R* cl, const R* cr, const R* ql, const R* qr,
                    const XM<R>& xl, const XM<R>& xr, const QM<R>& ml, const QM<R>& mr, uint64_t* sg = nullptr) const {
     if (lim == LIM_NOLIMIT1) {  // first-order overload (spatial/muscl.h:62-87)
@@ -331,7 +331,7 @@ template <class R> struct Solver {
   static void acc_sub(FluxRes<R>& a, const FluxRes<R>& f) { for (int v = 0; v < 4; ++v) a.f[v] -= f.f[v]; a.lam += f.lam; }
   static void acc_add(FluxRes<R>& a, const FluxRes<R>& f) { for (int v = 0; v < 4; ++v) a.f[v] += f.f[v]; a.lam += f.lam; }
 
-  // ---- residualCalc (spatial/residualCalc.h:45-307)
+  // ---- residualCalc (spatial/residualCalc.h:27-307)
   void residual(const std::vector<R>& q, std::vector<FluxRes<R>>& r) {
     boundary_update(q);
     qmetrics(q);
@@ -360,7 +360,7 @@ template <class R> struct Solver {
     for (int side = 0; side < 4; ++side) {
       const int t = bc[side];
       if (t == BC_PERIODIC) {
-        // only the lower face of each periodic pair (periodicLoop.h:263-324)
+        // only the lower face of each periodic pair (periodicLoop.h:115-179)
         if (side == 0)
           for (int j = 0; j < nj; ++j) {
             R s[2]; shift_i(j, s);
@@ -404,8 +404,8 @@ template <class R> struct Solver {
     }
   }
 
-  // ---- dual time (ode.h:10-83, timestepping/dualTime.ipp:5-99,
-  // OLD.fieldOperations/dualTimeResidual.ipp:3-42): the flux residual of the iterate becomes
+  // ---- dual time (ode.h:12-82, timestepping/dualTime.ipp:4-105,
+  // OLD.fieldOperations/dualTimeResidual.ipp:2-41): the flux residual of the iterate becomes
   // g0 R(q) - V (b0/dt) Q(q) + src, src = g1 R(q_n) - V (b1 Q_n + b2 Q_{n-1}) / dt
   void cons_of(const R* q, R* qc) const {
     if (basis == BASIS_CONSERVED) for (int v = 0; v < 4; ++v) qc[v] = q[v];

@@ -42,6 +42,8 @@ void* hco_create(int ni, int nj, const double* nodes, const int* bc, int flux, i
   return s;
 }
 void hco_destroy(void* h) { delete static_cast<S*>(h); }
+// FIX_* corrections of the reference's defects (hc_set_corrections)
+void hco_set_corrections(void* h, unsigned mask) { static_cast<S*>(h)->sp.fixes = mask; }
 // solution basis (BASIS_*) of the state and ghost layers
 void hco_set_basis(void* h, int basis) { static_cast<S*>(h)->basis = basis; }
 // AUSM+up low-Mach scaling pair (SCALING_*) and the species' lref and dt
@@ -197,6 +199,20 @@ void hco_wall_flux_basis(int basis, const double* species, const double* face, c
                          double* out5) {
   put_flux(wall_flux(make_species(species), make_face(face), qi, dq, basis), out5);
 }
+// flux and far-field update with FIX_* corrections
+void hco_flux_fixed(int kind, unsigned fixes, const double* species, const double* face, const double* ql,
+                    const double* qr, double* out5) {
+  Species<double> sp = make_species(species);
+  sp.fixes = fixes;
+  put_flux(face_flux(kind, sp, make_face(face), prim2state(sp, ql), prim2state(sp, qr)), out5);
+}
+void hco_bc_update_fixed(int kind, unsigned fixes, const double* species, const double* face, const double* qi,
+                         const double* qf, double* qb) {
+  Species<double> sp = make_species(species);
+  sp.fixes = fixes;
+  if (kind == BC_RIEMANN) bc_riemann(sp, make_face(face), qi, qf, qb);
+  else bc_entropy(sp, make_face(face), qi, qf, qb);
+}
 // kind: 2 = Riemann, 3 = Entropy (face normal into the domain)
 void hco_bc_update(int kind, const double* species, const double* face, const double* qi,
                    const double* qf, double* qb) {
@@ -226,7 +242,7 @@ void hco_rk_table(int kind, double* out) {  // {nstages, maxcfl, alpha[16], beta
 }
 
 // ---------------------------------------------------------------- meshes
-// make_cylinder_mesh (mesh/generate/twoD.h:223-263): i radial, j around; with
+// make_cylinder_mesh (mesh/generate/twoD.h:139-179): i radial, j around; with
 // stretch s != 1 the radial spacing grows geometrically (D6).
 void hco_cylinder_nodes(int nr, int nth, double rc, double rb, double stretch, double* nodes) {
   const double dr = (rb - rc) / nr;
@@ -241,7 +257,7 @@ void hco_cylinder_nodes(int nr, int nth, double rc, double rb, double stretch, d
       nodes[(size_t(i) * (nth + 1) + j) * 2 + 1] = r * sin(th);
     }
 }
-// make_linspace_mesh (mesh/generate/twoD.h:99-124)
+// make_linspace_mesh (mesh/generate/twoD.h:15-40)
 void hco_linspace_nodes(int nx, int ny, double lox, double hix, double loy, double hiy, double* nodes) {
   const double dx = (hix - lox) / nx, dy = (hiy - loy) / ny;
   for (int i = 0; i <= nx; ++i)

@@ -20,7 +20,8 @@ _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 # enum values shared with oracle/hc_oracle.hpp and include/hc.h
-FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5, "roe_ws": 6}
+FLUX = {"roe": 0, "slau": 1, "slau_ref": 2, "ausmpup": 3, "rusanov": 4, "central": 5, "roe_ws": 6,
+        "roe_face": 7}
 SCALING = {"convective": 0, "acoustic": 1, "adaptive": 2}
 BASIS = {"primitive": 0, "conserved": 1}
 LIMITER = {"nolimit1": 0, "nolimit2": 1, "nolimit3": 2, "vanalbada": 3, "minmod": 4,
@@ -28,6 +29,18 @@ LIMITER = {"nolimit1": 0, "nolimit2": 1, "nolimit3": 2, "vanalbada": 3, "minmod"
 BC = {"periodic": 0, "fixed": 1, "riemann": 2, "entropy": 3, "wall": 4}
 RK = {"ssp11": 0, "ssp22": 1, "ssp33": 2, "ssp34": 3}
 DT = {"global": 0, "local": 1}
+# corrections of the reference's defects (FIX_* in hc_oracle.hpp, hc_fix in include/hc.h)
+FIX = {"mach_split_p1": 1, "farfield_transverse": 2}
+
+
+def fix_mask(corrections) -> int:
+    if corrections is None:
+        return 0
+    if isinstance(corrections, int):
+        return corrections
+    if isinstance(corrections, str):
+        return sum(FIX.values()) if corrections == "all" else FIX[corrections]
+    return sum(FIX[c] for c in set(corrections))
 
 
 def build(quiet: bool = True) -> None:
@@ -77,6 +90,21 @@ class Pointwise:
     def flux(self, kind, species, face, ql, qr):
         out = np.empty(5)
         self.fn("flux")(kind, species, face, ql, qr, out)
+        return out
+
+    def flux_fixed(self, kind, corrections, species, face, ql, qr):
+        """The flux with corrections of the reference's defects (oracle only)."""
+        f = self.lib.hco_flux_fixed
+        f.argtypes = [C.c_int, C.c_uint, _dp, _dp, _dp, _dp, _dp]
+        out = np.empty(5)
+        f(int(kind), fix_mask(corrections), species, face, ql, qr, out)
+        return out
+
+    def bc_update_fixed(self, kind, corrections, species, face, qi, qf):
+        f = self.lib.hco_bc_update_fixed
+        f.argtypes = [C.c_int, C.c_uint, _dp, _dp, _dp, _dp, _dp]
+        out = np.empty(4)
+        f(int(kind), fix_mask(corrections), species, face, qi, qf, out)
         return out
 
     def ausmpup_scaled(self, vscale, pscale, species5, face, ql, qr):
@@ -240,7 +268,7 @@ class OracleSolver:
 
     def __init__(self, ni, nj, nodes, bc, flux="roe", limiter="vanleer", rk="ssp34", dt="global",
                  cfl=0.5, species=(1.4, 287.058, 1e-4), ghost_ref=None, fast=False, low_mach=None,
-                 basis="primitive"):
+                 basis="primitive", corrections=None):
         self.lib = load(fast)
         self.ni, self.nj = ni, nj
         bcv = np.array([BC[b] if isinstance(b, str) else int(b) for b in bc], dtype=np.int32)
@@ -252,6 +280,9 @@ class OracleSolver:
                                      float(cfl), np.asarray(species, dtype=np.float64))
         self.lib.hco_set_basis.argtypes = [C.c_void_p, C.c_int]
         self.lib.hco_set_basis(self.h, BASIS[basis] if isinstance(basis, str) else int(basis))
+        if corrections:
+            self.lib.hco_set_corrections.argtypes = [C.c_void_p, C.c_uint]
+            self.lib.hco_set_corrections(self.h, fix_mask(corrections))
         if low_mach is not None:
             # (velocity scaling, pressure scaling, lref, species dt) of AUSM+up
             vs, ps, lref, sdt = low_mach

@@ -57,7 +57,7 @@ int main() {
   const double xs[NX] = {0.0, -0.0, 4.9e-324, 2.2250738585072014e-308, 1.0, 2.0, 1e300, INFINITY, NAN, -1.0};
   // zero-pressure pairs and ordinary ones: {u, v, rho, p} left, right
   const double qls[NF][4] = {{0, 0, 1, 0}, {0, 0, 1, 0}, {0.3, -0.2, 1, 0}, {0.1, 0.2, 1, 1}, {0, 0, 1, 1}, {0.5, 0, 1, 0}};
-  const double qrs[NF][4] = {{0, 0, 2, 0}, {0, 0, 1, 0}, {0.3, -0.2, 2, 0}, {0.2, 0.1, 2, 0.5}, {0, 0, 1, 0}, {-0.5, 0, 1, 0}};
+  const double qrs[NF][4] = {{0, 0, 2, 0}, {0, 0, 1, 0}, {0.3, -0.2, 1, 0}, {0.2, 0.1, 2, 0.5}, {0, 0, 1, 0}, {-0.5, 0, 1, 0}};
 
   double *dx, *ds, *dr, *dql, *dqr, *dout;
   CK(cudaMalloc(&dx, NX * sizeof(double)));

@@ -1,6 +1,6 @@
 """Dual-time stepping (hc_dual_time_run) of the CUDA path against the CPU oracle's
 restatement of the same scheme: outer physical steps of BDF1 / BDF2 / the trapezium
-rule (ode.h:10-83), inner pseudo-time RK steps of the dual-time residual
+rule (ode.h:12-82), inner pseudo-time RK steps of the dual-time residual
 g0 R(u) - V (b0 Q(u) + b1 Q_n + b2 Q_{n-1}) / dt + g1 R(u_n) with the pseudo step
 dtau / (1 + b0 dtau / dt).  With a fixed inner count the two runs do the same
 arithmetic: FP64 bar 1e-12 relative L-inf per conserved variable."""

