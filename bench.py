@@ -42,9 +42,25 @@ PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "stage_kernel_fp64_ogrid.md")
 
 
 def workload_config():
+    """The workload's description, identical on both arms of the benchmark."""
+    ncell = NR * NTH
+    ws = (3 * 4 + 3 * 5) * 8 * ncell / 2 ** 20 + 2 * 14 * 8 * ncell / 2 ** 20
     return {"workload": f"cylinder O-grid {NR}x{NTH}, r 0.5..20, stretch 1.01, M{MACH}",
-            "cells": NR * NTH, "flux": FLUX, "limiter": LIMITER, "gradients": "lsq", "rk": RKT,
-            "dt": DTMODE, "cfl": CFL, "precision": "fp64", "step": "one RK step (4 stages) over all cells"}
+            "cells": ncell, "flux": FLUX, "limiter": LIMITER, "gradients": "lsq", "rk": RKT,
+            "dt": DTMODE, "cfl": CFL, "precision": "fp64", "step": "one RK step (4 stages) over all cells",
+            "l2": f"no flush: per-step working set {ws:.0f} MiB > {L2_BYTES / 2 ** 20:.0f} MiB L2"}
+
+
+def oracle_cylinder(nr: int, nth: int, mach: float, rc: float = 0.5, rb: float = 20.0, stretch: float = 1.01):
+    """The O-grid workload built by the oracle alone (its own make_cylinder_mesh), so that
+    the CPU arm loads nothing of the product: nodes, boundary types, far-field reference,
+    uniform freestream state, species (rho 1, p 1/gamma, velocity (mach, 0))."""
+    from oracle import oracle_py
+    nodes = oracle_py.pointwise(fast=True).cylinder_nodes(nr, nth, rc, rb, stretch)
+    qinf = np.array([mach, 0.0, 1.0, 1.0 / 1.4])
+    q = np.broadcast_to(qinf[:, None, None], (4, nr, nth)).copy()
+    ref = [None, np.broadcast_to(qinf[:, None], (4, nth)).copy(), None, None]
+    return nodes, ["wall", "riemann", "periodic", "periodic"], ref, q, (1.4, 287.058, mach)
 
 
 def measured_peaks():
@@ -146,32 +162,36 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def cpu_baseline(steps_budget_s: float = 12.0, threads: int | None = None):
+def cpu_baseline(sample_s: float = 4.0, samples: int = 3, threads: int | None = None):
     """The reference algorithm on the host cores: OpenMP oracle port built with the
-    reference's flags (-O3 -ffast-math -fopenmp), on a bounded number of steps of
-    the same workload."""
-    from hyperboliconvergence_gb300 import cases
+    reference's flags (-O3 -ffast-math -fopenmp), `samples` timed samples of about
+    `sample_s` seconds each (at most 200 RK steps) of the same workload; the median."""
     from oracle import oracle_py
     threads = threads or os.cpu_count() or 1
     os.environ.setdefault("OMP_PROC_BIND", "close")
     lib = oracle_py.load(fast=True)
     lib.hco_set_threads(int(threads))
-    mesh, bc, ref, q, species = cases.cylinder(NR, NTH, mach=MACH)
-    o = oracle_py.OracleSolver(mesh.ni, mesh.nj, mesh.nodes.ravel(), bc, flux=FLUX, limiter=LIMITER, rk=RKT,
-                               dt=DTMODE, cfl=CFL, species=species, ghost_ref=ref, fast=True)
+    nodes, bc, ref, q, species = oracle_cylinder(NR, NTH, MACH)
+    o = oracle_py.OracleSolver(NR, NTH, nodes, bc, flux=FLUX, limiter=LIMITER, rk=RKT, dt=DTMODE, cfl=CFL,
+                               species=species, ghost_ref=ref, fast=True)
     o.set_state(q)
     o.step(1)  # warm-up (first touch of the arrays)
-    n, t0 = 0, time.perf_counter()
-    while True:
-        o.step(1)
-        n += 1
-        el = time.perf_counter() - t0
-        if el >= steps_budget_s or n >= 200:
-            break
-    v = NR * NTH * n / el
+    rates, steps = [], []
+    for _ in range(samples):
+        n, t0 = 0, time.perf_counter()
+        while True:
+            o.step(1)
+            n += 1
+            el = time.perf_counter() - t0
+            if el >= sample_s or n >= 200:
+                break
+        rates.append(NR * NTH * n / el)
+        steps.append(n)
+    v = statistics.median(rates)
     return {"value": v, "unit": UNIT, "cores": int(lib.hco_get_threads()), "kind": "port",
-            "sample": f"{n} RK steps of the {NR}x{NTH} O-grid workload ({el:.1f} s), OpenMP oracle port, "
-                      f"-O3 -ffast-math -fopenmp"}
+            "samples": rates,
+            "sample": f"median of {samples} samples of {min(steps)}-{max(steps)} RK steps of the {NR}x{NTH} "
+                      f"O-grid workload (~{sample_s:.0f} s each), OpenMP oracle port, -O3 -ffast-math -fopenmp"}
 
 
 def _events():
@@ -548,7 +568,7 @@ def run_reference(args):
     if rank != 0:
         return 0
     steps = max(1, args.steps)
-    cb = cpu_baseline(steps_budget_s=min(20.0, 4.0 + 2.0 * steps))
+    cb = cpu_baseline(sample_s=min(8.0, 2.0 + 0.5 * steps), samples=3)
     v = cb["value"]
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
             "warmup": args.warmup, "ms_per_step": NR * NTH / v * 1e3, "higher_is_better": True,
@@ -659,8 +679,6 @@ def run_gpu(args):
 
     if rank == 0:
         cfg = workload_config()
-        cfg["l2"] = (f"no flush: per-step working set {(3 * 4 + 3 * 5) * 8 * ncell / 2**20 + 2 * 14 * 8 * ncell / 2**20:.0f}"
-                     f" MiB > {L2_BYTES / 2**20:.0f} MiB L2")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",

@@ -434,6 +434,19 @@ int hc_batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_o
                               const double* const* targets, double* J, double* const* q0_bar,
                               hc_adjoint_stats* stats);
 
+/* One interface flux evaluated on the host with the pointwise functions the stage kernels
+ * compile: FluxInterface::flux(species, face, ql, qr) (conservationLaws/base/base.h:370-397)
+ * of the flux `flux` (hc_flux) as the reference writes it (no corrections), for the C++
+ * adapter's flux tags and for checks.  vscale, pscale: AUSM+up's LowMachScaling pair;
+ * species {gamma, R, minf, lref, dt}; face {area, centre x, centre y, normal x, normal y,
+ * tangent x, tangent y}; ql, qr primitive {u, v, rho, p}; out5 = {4 conserved flux
+ * components times the area, lambda times the area}. */
+int hc_flux_eval(int flux, int vscale, int pscale, const double species[5], const double face[7], const double ql[4],
+                 const double qr[4], double out5[5]);
+/* One slope limiter on the host, Limiter::limit(a, b) (limiters/limiter.h:14-28,
+ * limiters/limiter.ipp:8-161; HC_LIM_VANLEER the harmonic-mean slope). */
+int hc_limit_eval(int limiter, double a, double b, double* out);
+
 const char* hc_last_error_string(void);
 const char* hc_version(void);
 
