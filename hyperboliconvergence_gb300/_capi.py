@@ -77,6 +77,7 @@ def _declare(lib):
         "hc_set_low_mach": [p, i, i, d, d],
         "hc_set_tile": [p, i],
         "hc_set_corrections": [p, C.c_uint],
+        "hc_set_time": [p, d],
         "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],
         "hc_state_upload": [p, dp],
         "hc_state_download": [p, dp],

@@ -699,6 +699,15 @@ int hc_set_low_mach(hc_ctx* c, int velocity_scaling, int pressure_scaling, doubl
   return HC_OK;
 }
 
+int hc_set_time(hc_ctx* c, double t) {
+  if (int st = check_ctx(c)) return st;
+  if (!c->have_mesh || !c->info) return fail(HC_ERR_ARG, "upload the mesh before setting the time");
+  if (!std::isfinite(t)) return fail(HC_ERR_ARG, "the time must be finite");
+  HC_CUDA(cudaMemcpyAsync(&c->info->t, &t, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  HC_CUDA(cudaStreamSynchronize(c->stream));  // t is a host local
+  return HC_OK;
+}
+
 int hc_set_corrections(hc_ctx* c, unsigned mask) {
   if (int st = check_ctx(c)) return st;
   if (mask & ~unsigned(HC_FIX_ALL)) return fail(HC_ERR_ARG, "unknown correction bits");

@@ -13,15 +13,20 @@ binary checkpoint of a solver's state.
 * ``write_cartesian_result_dat``: per cell "x y" of the centroid then rho/rho0,
   u, v, p-p0, s/s0, a/a0, |u|/a, a blank line after each i-row
   (cpp/script/euler/gresho2D.cpp:36-69, 226-265).
-* ``save_checkpoint`` / ``load_checkpoint``: mesh nodes, boundary types and
-  reference layers, species, configuration and the primitive state in one
-  ``.npz`` file, enough to resume a run.
+* ``save_checkpoint`` / ``load_checkpoint``: a binary snapshot (HCCK format 2: a
+  JSON header with the run's configuration, step, time and dt, float64 SoA arrays
+  and a CRC-32) from which a run resumes bit for bit; a corrupted file is refused.
+  The reference has no checkpoint (its only output is the result.dat above).
 
 States are primitive {u, v, rho, p} arrays of shape (4, ni, nj).
 """
 from __future__ import annotations
 
+import json
 import math
+import os
+import struct
+import zlib
 
 import numpy as np
 
@@ -96,28 +101,126 @@ def read_dat(path):
     return blocks
 
 
+# ---------------------------------------------------------------- binary checkpoint
+#
+# Layout (little-endian), "HCCK" format 2:
+#   8 bytes   magic b"HCCKPT\x00\x02"
+#   u64       H, the byte length of the header
+#   u64       P, the byte length of the payload
+#   H bytes   header: UTF-8 JSON -- the run's configuration (law, basis, precision,
+#             flux, limiter, RK table, dt mode, CFL, species, AUSM+up low-Mach settings,
+#             corrections, tile), the mesh kind and shape, the boundary types, the step
+#             count, the accumulated time t and the last step's dt, and one entry per
+#             array {name, shape, offset} (offsets into the payload, 8-byte aligned)
+#   P bytes   payload: the arrays as float64 -- mesh nodes, the boundary reference
+#             layers that exist, the state in the solution basis (SoA planes)
+#   u32       CRC-32 of every byte before it
+# A file whose magic, lengths, CRC, header or array bounds do not check out is refused
+# with CheckpointError; nothing is built from it.
+
+MAGIC = b"HCCKPT\x00\x02"
+_PRE = struct.Struct("<8sQQ")
+
+
+class CheckpointError(ValueError):
+    """A checkpoint file that is not a complete, intact HCCK file."""
+
+
+def write_checkpoint(path, meta: dict, arrays: dict) -> None:
+    """Write meta (JSON-serialisable) and float64 arrays as one HCCK file, atomically (a
+    temporary file in the same directory, renamed over `path`)."""
+    entries, chunks, off = [], [], 0
+    for name, a in arrays.items():
+        a = np.ascontiguousarray(a, dtype="<f8")
+        entries.append({"name": name, "shape": list(a.shape), "offset": off})
+        chunks.append(a.tobytes())
+        off += a.nbytes
+    header = json.dumps(dict(meta, arrays=entries), sort_keys=True).encode()
+    body = _PRE.pack(MAGIC, len(header), off) + header + b"".join(chunks)
+    crc = zlib.crc32(body) & 0xFFFFFFFF
+    path = os.fspath(path)
+    tmp = f"{path}.tmp{os.getpid()}"
+    with open(tmp, "wb") as f:
+        f.write(body)
+        f.write(struct.pack("<I", crc))
+        f.flush()
+        os.fsync(f.fileno())
+    os.replace(tmp, path)
+
+
+def read_checkpoint(path):
+    """(meta, arrays) of an HCCK file, after checking its magic, lengths and CRC-32."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if len(data) < _PRE.size + 4:
+        raise CheckpointError("checkpoint truncated: shorter than its preamble")
+    magic, hlen, plen = _PRE.unpack_from(data, 0)
+    if magic != MAGIC:
+        raise CheckpointError("not an HCCK format-2 checkpoint (bad magic)")
+    if _PRE.size + hlen + plen + 4 != len(data):
+        raise CheckpointError(f"checkpoint truncated or padded: {len(data)} bytes, the preamble says "
+                              f"{_PRE.size + hlen + plen + 4}")
+    body, (crc,) = data[:-4], struct.unpack("<I", data[-4:])
+    if zlib.crc32(body) & 0xFFFFFFFF != crc:
+        raise CheckpointError("checkpoint corrupted: CRC-32 mismatch")
+    try:
+        meta = json.loads(body[_PRE.size:_PRE.size + hlen].decode())
+    except (UnicodeDecodeError, json.JSONDecodeError) as e:
+        raise CheckpointError(f"checkpoint header unreadable: {e}") from e
+    payload = body[_PRE.size + hlen:]
+    arrays = {}
+    for e in meta.pop("arrays", []):
+        n = int(np.prod(e["shape"], dtype=np.int64))
+        lo, hi = int(e["offset"]), int(e["offset"]) + 8 * n
+        if lo < 0 or hi > len(payload) or lo % 8:
+            raise CheckpointError(f"array {e['name']} lies outside the payload")
+        arrays[e["name"]] = np.frombuffer(payload[lo:hi], dtype="<f8").reshape(e["shape"]).astype(np.float64)
+    return meta, arrays
+
+
 def save_checkpoint(path, solver) -> None:
-    """Mesh, boundary set-up, species, configuration and current state of a Solver."""
+    """Everything needed to resume a Solver's run bit for bit: mesh, boundary types and
+    reference layers, species, configuration, the current state, the step count and the
+    accumulated time (HCCK format 2, above)."""
+    st = solver.sync()
     m = solver.mesh
-    refs = {f"ref{k}": (np.zeros((0,)) if r is None else np.asarray(r, dtype=np.float64))
-            for k, r in enumerate(solver.ref)}
-    np.savez(path, format=np.array([1]), nodes=m.nodes,
-             bc=np.array(solver.bc), species=np.array(solver.species, dtype=np.float64),
-             config=np.array([str(solver.flux), str(solver.limiter), str(solver.rk), solver.precision,
-                              solver.dt]),
-             cfl=solver.cfl, state=solver.get_state(), **refs)
+    meta = {"format": 2, "law": solver.law, "basis": solver.basis, "precision": solver.precision,
+            "flux": str(solver.flux), "limiter": str(solver.limiter), "rk": str(solver.rk), "dt_mode": solver.dt,
+            "cfl": solver.cfl, "species": list(solver.species), "low_mach": solver.low_mach,
+            "corrections": int(solver.corrections), "tile": solver.tile,
+            "mesh": {"dims": 1 if getattr(m, "one_d", False) else 2, "ni": m.ni, "nj": m.nj},
+            "nv": solver.nv, "bc": [str(b) for b in solver.bc], "step": int(solver.steps_done),
+            "t": float(st.t), "dt": float(st.dt)}
+    arrays = {"nodes": m.nodes, "state": solver.get_state()}
+    for k, r in enumerate(solver.ref):
+        if r is not None:
+            arrays[f"ref{k}"] = r
+    write_checkpoint(path, meta, arrays)
 
 
 def load_checkpoint(path, stream=None):
-    """A Solver rebuilt from a checkpoint, its state restored."""
-    from .solver import Mesh, Solver
-    d = np.load(path, allow_pickle=False)
-    if int(d["format"][0]) != 1:
-        raise ValueError("unknown checkpoint format")
-    mesh = Mesh(d["nodes"])
-    ref = [None if d[f"ref{k}"].size == 0 else d[f"ref{k}"] for k in range(4)]
-    flux, limiter, rk, precision, dt = (str(x) for x in d["config"])
-    s = Solver(mesh, [str(b) for b in d["bc"]], ref, flux=flux, limiter=limiter, rk=rk, precision=precision,
-               dt=dt, cfl=float(d["cfl"]), species=tuple(float(x) for x in d["species"]), stream=stream)
-    s.set_state(d["state"])
+    """A Solver rebuilt from an HCCK checkpoint: configuration, mesh, boundaries, state,
+    step count and time restored.  A corrupted or truncated file raises CheckpointError
+    before any device work."""
+    from .solver import Mesh, Mesh1D, Solver
+    meta, arrays = read_checkpoint(path)
+    if meta.get("format") != 2:
+        raise CheckpointError(f"unsupported checkpoint format {meta.get('format')!r}")
+    mk = meta["mesh"]
+    mesh = Mesh1D(arrays["nodes"]) if mk["dims"] == 1 else Mesh(arrays["nodes"])
+    if (mesh.ni, mesh.nj) != (mk["ni"], mk["nj"]):
+        raise CheckpointError("mesh nodes do not match the recorded shape")
+    state = arrays["state"]
+    want = (meta["nv"], mesh.ni) if mk["dims"] == 1 else (meta["nv"], mesh.ni, mesh.nj)
+    if tuple(state.shape) != want:
+        raise CheckpointError(f"state of shape {tuple(state.shape)}, expected {want}")
+    nsides = 2 if mk["dims"] == 1 else 4
+    ref = [arrays.get(f"ref{k}") for k in range(nsides)]
+    s = Solver(mesh, meta["bc"][:nsides], None if all(r is None for r in ref) else ref, flux=meta["flux"],
+               limiter=meta["limiter"], rk=meta["rk"], precision=meta["precision"], dt=meta["dt_mode"],
+               cfl=meta["cfl"], species=tuple(meta["species"]), stream=stream, law=meta["law"],
+               low_mach=None if meta["low_mach"] is None else tuple(meta["low_mach"]), basis=meta["basis"],
+               tile=meta["tile"], corrections=meta["corrections"])
+    s.set_state(state)
+    s.set_time(meta["t"], meta["step"])
     return s

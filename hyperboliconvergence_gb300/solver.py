@@ -121,6 +121,9 @@ class Solver:
         self.corrections = _capi.fix_mask(corrections)
         if self.corrections:
             check(self.lib.hc_set_corrections(self.h, self.corrections))
+        self.tile = tile
+        self.steps_done = 0
+        self.last = None
         self.low_mach = None
         if low_mach is not None:
             self.set_low_mach(*low_mach)
@@ -131,6 +134,7 @@ class Solver:
         """Cells per CTA tile of the 2D FP64/FP32 stage kernels: "8x32", "4x32" or "16x16"
         (the results do not depend on it)."""
         check(self.lib.hc_set_tile(self.h, _capi.TILE[tile]))
+        self.tile = tile
 
     def set_corrections(self, corrections) -> None:
         """Corrections of the reference's defects (hc_set_corrections): None, "all", or names
@@ -304,7 +308,16 @@ class Solver:
     def step(self, n: int = 1) -> StepStats:
         st = StepStats()
         check(self.lib.hc_step(self.h, int(n), C.byref(st)))
+        self.steps_done += int(n)
+        self.last = st
         return st
+
+    def set_time(self, t: float, steps_done: int | None = None) -> None:
+        """The accumulated time (and, optionally, the count of steps taken) a resumed run
+        continues from (hc_set_time)."""
+        check(self.lib.hc_set_time(self.h, float(t)))
+        if steps_done is not None:
+            self.steps_done = int(steps_done)
 
     def steady(self, max_steps: int, residual_drop: float = 1e-10, check_every: int = 100, smoothing=None):
         """Run to a steady state (SteadyTimeControls, controls.h:31-48): steps until the
@@ -318,6 +331,7 @@ class Solver:
         hist = np.empty(int(max_steps) // int(check_every) + 2)
         st = SteadyStats()
         check(self.lib.hc_steady_run(self.h, C.byref(ctl), _dptr(hist), hist.size, C.byref(st)))
+        self.steps_done += int(st.steps)
         return st, hist[:st.history_len].copy()
 
     def smooth_1d(self, r, alpha: float, kind: str = "implicit", ends: str = "a",
@@ -339,6 +353,7 @@ class Solver:
 
     def step_async(self, n: int = 1) -> None:
         check(self.lib.hc_step_async(self.h, int(n)))
+        self.steps_done += int(n)
 
     def sync(self) -> StepStats:
         st = StepStats()

@@ -175,6 +175,10 @@ int hc_residual(hc_ctx* ctx, double* out5);
 
 /* nsteps explicit RK steps: the time loop of integrate() (timestepping/rungeKutta.h:96-164). */
 int hc_step(hc_ctx* ctx, int nsteps, hc_step_stats* stats);
+/* The accumulated time t that hc_step_stats reports (the time integrate() accumulates,
+ * timestepping/rungeKutta.h:96-164); uploading a mesh sets it to 0.  A run restored from
+ * a checkpoint sets it to resume. */
+int hc_set_time(hc_ctx* ctx, double t);
 /* Enqueue nsteps without waiting; hc_sync waits and reports. */
 int hc_step_async(hc_ctx* ctx, int nsteps);
 int hc_sync(hc_ctx* ctx, hc_step_stats* stats);
