@@ -352,6 +352,126 @@ def _batch_accuracy(insts, steps: int = 200, nsub: int = 8):
                     "of its jump; the L1 difference measures the solution error"}
 
 
+def measure_vortex(stream):
+    """The isentropic-vortex configuration (periodic [0,10]^2, 128^2, Roe, MUSCL + van Leer,
+    LSQ, ssp34, CFL 0.5 global dt, FP64, 100 steps): cell-updates/s, and the L1 / L-inf
+    error of the conserved variables against the exact vortex translated by (t, t) at
+    t = 4 sum(dt); with the reference's Roe flux and with the face-frame one, and for the
+    face-frame flux the observed orders over 64^2 / 128^2 / 256^2 (50 / 100 / 200 steps).
+    Parity with the CPU oracle at steps 1, 50 and 100 is held by the tests."""
+    import torch
+    from hyperboliconvergence_gb300 import HCError, cases
+    from hyperboliconvergence_gb300.solver import Solver
+    g = 1.4
+
+    def cons(w):
+        u, v, r, p = w
+        return np.stack([r * u, r * v, r, p / (g - 1) + 0.5 * r * (u * u + v * v)])
+
+    def run(n, steps, flux, timed=False):
+        mesh, bc, ref, q, sp = cases.isentropic_vortex(n)
+        s = Solver(mesh, bc, ref, flux=flux, limiter="vanleer", rk="ssp34", dt="global", cfl=0.5, species=sp,
+                   stream=stream.cuda_stream)
+        s.set_state(q)
+        res = {}
+        try:
+            if timed:
+                s.step(3)
+                s.set_state(q)
+                s.set_time(0.0, 0)
+                e0, e1 = _events()
+                torch.cuda.synchronize()
+                e0.record(stream)
+                s.step_async(steps)
+                e1.record(stream)
+                st = s.sync()
+                ms = e0.elapsed_time(e1)
+                res.update(value=n * n * steps / (ms / 1e3), unit=UNIT, ms_per_step=ms / steps)
+            else:
+                st = s.step(steps)
+        except HCError as exc:
+            s.close()
+            return {"error": str(exc)}
+        c = mesh.centres()
+        e = np.abs(cons(s.get_state()) - cons(cases.vortex_state(c[0], c[1], 4.0 * st.t)))
+        res.update(t_physical=4.0 * st.t, l1=[float(x) for x in e.reshape(4, -1).mean(1)],
+                   linf=[float(x) for x in e.reshape(4, -1).max(1)])
+        s.close()
+        return res
+
+    out = {"grid": "128x128", "steps": 100, "flux_reference": run(128, 100, "roe", timed=True),
+           "flux_face_frame": run(128, 100, "roe_face", timed=True)}
+    conv = {n: run(n, k, "roe_face") for n, k in ((64, 50), (128, 100), (256, 200))}
+    ref256 = run(256, 200, "roe")
+    if all("l1" in v for v in conv.values()):
+        out["face_frame_orders"] = {
+            f"{a}->{b}": {"l1": [float(np.log2(x / y)) for x, y in zip(conv[a]["l1"], conv[b]["l1"])],
+                          "linf": [float(np.log2(x / y)) for x, y in zip(conv[a]["linf"], conv[b]["linf"])]}
+            for a, b in ((64, 128), (128, 256))}
+    out["reference_roe_256"] = ref256
+    return out
+
+
+def measure_steady(stream, steps: int = 2000, fluxes=("roe_face", "slau", "ausmpup"), machs=(0.3, 0.8)):
+    """The steady O-grid configuration: from the uniform freestream, local timestepping at
+    CFL 0.5 (ssp34, MUSCL + van Albada, LSQ) towards a density-residual drop of 1e-10, with
+    a cap of `steps` steps, for each flux at M 0.3 and 0.8 in FP64 and FP32.  The runs take
+    the corrections of the reference's defects (the face-frame Roe dissipation, the 1/0
+    MachSplit_P1, the far fields' outflow test); one run of the reference's own Roe flux and
+    far field, uncorrected, is reported beside them.  Per run: steps, residual drop, whether
+    1e-10 was reached, ms per step, the drag coefficient C_d = F_x / (rho U^2 / 2 * 2 r_c)
+    of the final state, and the FP32 state's relative L-inf / L1 difference from FP64."""
+    import torch
+    from hyperboliconvergence_gb300 import HCError, cases
+    from hyperboliconvergence_gb300.solver import Solver
+    g = 1.4
+
+    def cons(w):
+        u, v, r, p = w
+        return np.stack([r * u, r * v, r, p / (g - 1) + 0.5 * r * (u * u + v * v)])
+
+    def one(mach, flux, prec, corr):
+        mesh, bc, ref, q, species = cases.cylinder(NR, NTH, mach=mach)
+        s = Solver(mesh, bc, ref, flux=flux, limiter=LIMITER, rk=RKT, precision=prec, dt=DTMODE, cfl=CFL,
+                   species=species, stream=stream.cuda_stream, corrections=corr)
+        s.set_state(q)
+        e0, e1 = _events()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        try:
+            st, hist = s.steady(steps, residual_drop=1e-10, check_every=max(1, steps // 20))
+            ok = True
+        except HCError as exc:
+            ok = False
+            err = str(exc)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if not ok:
+            s.close()
+            return {"error": err, "steps_before_failure": s.steps_done}, None
+        res = {"steps": int(st.steps), "residual_drop": float(st.res / st.res0), "converged_1e-10": bool(st.converged),
+               "ms_per_step": e0.elapsed_time(e1) / max(1, st.steps),
+               "cd": s.wall_force((1.0, 0.0)) / (0.5 * mach * mach * 1.0)}
+        state = cons(s.get_state())
+        s.close()
+        return res, state
+
+    out = {"cap_steps": steps, "limiter": LIMITER, "cfl": CFL, "corrections": "all"}
+    for mach in machs:
+        for flux in fluxes:
+            r64, s64 = one(mach, flux, "fp64", "all")
+            r32, s32 = one(mach, flux, "fp32", "all")
+            entry = {"fp64": r64, "fp32": r32}
+            if s64 is not None and s32 is not None:
+                d = np.abs(s32 - s64).reshape(4, -1)
+                entry["fp32_vs_fp64_rel_linf"] = float((d.max(1) / np.abs(s64).reshape(4, -1).max(1)).max())
+                entry["fp32_vs_fp64_rel_l1"] = float((d.mean(1) / np.abs(s64).reshape(4, -1).mean(1)).max())
+            out[f"{flux}_M{mach}"] = entry
+    lit, _ = one(0.3, "roe", "fp64", None)
+    out["reference_roe_uncorrected_M0.3_fp64"] = lit
+    return out
+
+
 def measure_developed(stream, steps: int = 10):
     """The headline workload (FP64) started from a state that is non-uniform
     everywhere -- the freestream times 1 + 1% of a smooth field of r and theta --
@@ -706,6 +826,8 @@ def run_gpu(args):
                              ("batched", lambda: measure_batched(stream)),
                              ("variants", lambda: measure_variants(stream)),
                              ("developed", lambda: measure_developed(stream)),
+                             ("vortex", lambda: measure_vortex(stream)),
+                             ("steady", lambda: measure_steady(stream, args.steady_steps)),
                              ("adjoint", lambda: measure_adjoint(args.adjoint_steps, args.adjoint_snapshots)),
                              ("batched_adjoint", measure_batched_adjoint),
                              ("batched_adjoint_scalar", lambda: measure_batched_adjoint(law="scalar"))):
@@ -732,10 +854,14 @@ def main():
     ap.add_argument("--adjoint-snapshots", type=int, default=20, help="checkpoints of the adjoint measurement")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run only the FP64 adjoint measurement (no headline line), for profiling its kernels")
+    ap.add_argument("--steady-steps", type=int, default=2000,
+                    help="step cap of each run of the steady O-grid extra (residual drop target 1e-10)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP32, double-float, batched and adjoint measurements beside the headline")
-    ap.add_argument("--extras", default="fp32,fp64_df,batched,variants,developed,adjoint,batched_adjoint,batched_adjoint_scalar",
-                    help="comma-separated subset of fp32,fp64_df,batched,variants,developed,adjoint,"
+    ap.add_argument("--extras",
+                    default="fp32,fp64_df,batched,variants,developed,vortex,steady,adjoint,batched_adjoint,"
+                            "batched_adjoint_scalar",
+                    help="comma-separated subset of fp32,fp64_df,batched,variants,developed,vortex,steady,adjoint,"
                          "batched_adjoint,batched_adjoint_scalar to measure beside the headline")
     args = ap.parse_args()
     if args.impl == "reference":

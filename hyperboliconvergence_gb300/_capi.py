@@ -78,6 +78,7 @@ def _declare(lib):
         "hc_set_tile": [p, i],
         "hc_set_corrections": [p, C.c_uint],
         "hc_set_time": [p, d],
+        "hc_wall_force": [p, dp, dp],
         "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],
         "hc_state_upload": [p, dp],
         "hc_state_download": [p, dp],
@@ -153,6 +154,7 @@ def _declare_batch(lib):
         "hc_batch_destroy": [p],
         "hc_batch_set_stream": [p, p],
         "hc_batch_state_upload": [p, i, dp],
+        "hc_batch_state_upload_device": [p, i, C.c_void_p],
         "hc_batch_state_download": [p, i, dp],
         "hc_batch_set_schedule": [p, C.POINTER(Schedule)],
         "hc_batch_set_corrections": [p, C.c_uint],
@@ -173,7 +175,7 @@ def _declare_batch(lib):
 
 class Objective(C.Structure):
     _fields_ = [("kind", C.c_int), ("scale", C.c_double), ("dir", C.c_double * 2),
-                ("target", C.POINTER(C.c_double)), ("weight", C.c_double * 4)]
+                ("target", C.POINTER(C.c_double)), ("weight", C.c_double * 4), ("target_on_device", C.c_int)]
 
 
 class DualTimeControls(C.Structure):
@@ -218,5 +220,9 @@ def _declare_adjoint(lib):
     lib.hc_batch_adjoint_gradient.argtypes = [p, i, i, C.POINTER(Objective), C.POINTER(dp), dp, C.POINTER(dp),
                                               C.POINTER(AdjointStats)]
     lib.hc_batch_adjoint_gradient.restype = C.c_int
+    lib.hc_batch_adjoint_record.argtypes = [p, i, i, C.POINTER(Objective), C.POINTER(dp), dp]
+    lib.hc_batch_adjoint_reverse.argtypes = [p, C.POINTER(dp), i, C.POINTER(AdjointStats)]
+    lib.hc_adjoint_record.argtypes = [p, i, i, C.POINTER(Objective), dp, dp, dp]
+    lib.hc_adjoint_reverse.argtypes = [p, dp, dp, i, C.POINTER(AdjointStats)]
     lib.hc_dual_time_run.argtypes = [p, C.POINTER(DualTimeControls), C.POINTER(DualTimeStats)]
     lib.hc_dual_time_run.restype = C.c_int

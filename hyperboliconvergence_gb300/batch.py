@@ -148,6 +148,72 @@ class Batch:
         return J, grads, st
 
 
+    def upload_device(self, k: int, prim) -> None:
+        """Instance k's state from a float64 CUDA tensor of shape (nv, ni, nj), asynchronous
+        on the batch's stream (hc_batch_state_upload_device)."""
+        m = self.meshes[k]
+        if tuple(prim.shape) != (self.nv, m.ni, m.nj) or not prim.is_cuda or prim.dtype != _torch().float64:
+            raise ValueError(f"instance {k}: a float64 CUDA tensor of shape ({self.nv}, {m.ni}, {m.nj}) is needed")
+        check(self.lib.hc_batch_state_upload_device(self.h, k, C.c_void_p(prim.contiguous().data_ptr())))
+
+    def _l2(self, weight, on_device):
+        from ._capi import Objective
+        o = Objective()
+        o.kind = _capi.OBJECTIVE["l2"]
+        for v in range(4):
+            o.weight[v] = float(weight[v])
+        o.target_on_device = 1 if on_device else 0
+        return o
+
+    def record(self, nsteps, targets, snapshots=20, weight=(1.0, 1.0, 1.0, 1.0)) -> np.ndarray:
+        """The forward half of `gradient` (hc_batch_adjoint_record): every instance's J after
+        nsteps steps; the checkpoints stay in the batch for `reverse`.  targets: per instance
+        an array, or a float64 CUDA tensor (read on the device)."""
+        n = self.n
+        dev = all(hasattr(t, "is_cuda") and t.is_cuda for t in targets)
+        if dev:
+            self._tape_targets = [t.detach().contiguous() for t in targets]
+            ptrs = [C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double)) for t in self._tape_targets]
+        else:
+            self._tape_targets = [np.ascontiguousarray(t, dtype=np.float64) for t in targets]
+            ptrs = [_dptr(t) for t in self._tape_targets]
+        for k, t in enumerate(self._tape_targets):
+            m = self.meshes[k]
+            if tuple(t.shape) != (self.nv, m.ni, m.nj):
+                raise ValueError(f"target {k} must have shape ({self.nv}, {m.ni}, {m.nj})")
+        tptr = (C.POINTER(C.c_double) * n)(*ptrs)
+        o = self._l2(weight, dev)
+        J = np.empty(n)
+        check(self.lib.hc_batch_adjoint_record(self.h, int(nsteps), int(snapshots), C.byref(o), tptr, _dptr(J)))
+        return J
+
+    def reverse(self, out=None):
+        """The reverse half (hc_batch_adjoint_reverse): out[k] a float64 CUDA tensor of instance
+        k's state shape receiving dJ_k/dq0_k on the device (None entries skipped), or None for
+        host arrays returned as {k: q0_bar}.  Returns (grads or None, stats)."""
+        from ._capi import AdjointStats
+        n = self.n
+        gptr = (C.POINTER(C.c_double) * n)()
+        host = None
+        if out is None:
+            host = {k: np.empty((self.nv, m.ni, m.nj)) for k, m in enumerate(self.meshes)}
+            for k, g in host.items():
+                gptr[k] = _dptr(g)
+        else:
+            for k, g in enumerate(out):
+                if g is not None:
+                    gptr[k] = C.cast(C.c_void_p(g.data_ptr()), C.POINTER(C.c_double))
+        st = AdjointStats()
+        check(self.lib.hc_batch_adjoint_reverse(self.h, gptr, 0 if out is None else 1, C.byref(st)))
+        self._tape_targets = None
+        return host, st
+
+
+def _torch():
+    import torch
+    return torch
+
+
 def uneven_riemann_batch(n: int, seed: int, sizes=tuple(range(64, 1025, 32))):
     """n four-quadrant Riemann instances with Ni, Nj drawn uniformly from `sizes`."""
     from . import cases

@@ -24,6 +24,7 @@
 
 #include <cfloat>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -537,7 +538,8 @@ template <class R> int setup(Adj<R>& A, hc_ctx* c, int nsteps, int nsnap, const 
     if (int st = A.alloc(&A.target, n4)) return st;
     double* t64 = nullptr;
     if (int st = A.alloc(&t64, n4)) return st;
-    HC_CUDA(cudaMemcpyAsync(t64, obj->target, n4 * sizeof(double), cudaMemcpyHostToDevice, A.s()));
+    HC_CUDA(cudaMemcpyAsync(t64, obj->target, n4 * sizeof(double),
+                            obj->target_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, A.s()));
     convert_kernel<R><<<1024, 256, 0, A.s()>>>(t64, A.target, n4);
     HC_CUDA(cudaGetLastError());
   }
@@ -591,6 +593,43 @@ template <class R> int finish_stats(Adj<R>& A, double* J, double* rates_out, hc_
 }
 
 
+// the wall pressure force of the context's current state along dir: the momentum flux
+// through every inviscid-wall face, the interior state moved to the face with its LSQ
+// gradient as the stage kernels' wall flux does (inviscidWall.ipp:33-72)
+template <class R> int wall_force(hc_ctx* c, const double dir[2], double* out) {
+  if (!c || !dir || !out) return fail(HC_ERR_ARG, "null argument");
+  if (int st = ctx_ensure_ready(c)) return st;
+  if (c->oned || c->scalar) return fail(HC_ERR_UNSUPPORTED, "the wall force is defined on the 2D Euler path");
+  if (c->cfg.basis != HC_BASIS_PRIMITIVE) return fail(HC_ERR_UNSUPPORTED, "the wall force takes the primitive basis");
+  Adj<R> A;
+  A.c = c;
+  A.nv = 4;
+  A.n = c->ncell();
+  if (int st = A.alloc(&A.qm, 2 * A.state_values())) return st;
+  if (int st = A.alloc(&A.wall, size_t(std::max(c->ni, c->nj)))) return st;
+  if (int st = A.alloc(&A.jacc, 1)) return st;
+  HC_CUDA(cudaMemsetAsync(A.jacc, 0, sizeof(double), A.s()));
+  AdjArgs<R> a = adj_args(A);
+  a.q = (const R*)c->q[0];
+  a.obj_scale = R(1);
+  a.obj_dirx = R(dir[0]);
+  a.obj_diry = R(dir[1]);
+  adj_qm_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
+  int launches = 1;
+  for (int side = 0; side < 4; ++side) {
+    if (c->bc[side] != HC_BC_WALL) continue;
+    const int m = c->nface(side);
+    wall_force_kernel<R><<<blocks(m), 256, 0, A.s()>>>(a, A.qm, side, A.wall);
+    sum_into_kernel<R><<<1, 256, 0, A.s()>>>(A.wall, m, A.jacc);
+    launches += 2;
+  }
+  HC_CUDA(cudaGetLastError());
+  HC_CUDA(cudaMemcpyAsync(out, A.jacc, sizeof(double), cudaMemcpyDeviceToHost, A.s()));
+  HC_CUDA(cudaStreamSynchronize(A.s()));
+  c->launches += launches;
+  return HC_OK;
+}
+
 template <class R>
 int objective_forward(hc_ctx* c, int nsteps, const hc_objective* obj, const double* rates_in, double* rates_out,
                       double* J) {
@@ -600,23 +639,68 @@ int objective_forward(hc_ctx* c, int nsteps, const hc_objective* obj, const doub
   return finish_stats(A, J, rates_out, nullptr);
 }
 
-template <class R>
-int adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
-                     double* q0_bar, double* ref_bar, double* rates_out, hc_adjoint_stats* stats) {
+// A recorded forward sweep: the adjoint buffers with the checkpoints of the schedule's
+// first descent, the schedule and its free snapshot slots, kept in the context between
+// hc_adjoint_record and hc_adjoint_reverse.
+struct TapeBase {
+  virtual ~TapeBase() = default;
+};
+template <class R> struct Tape : TapeBase {
   Adj<R> A;
-  if (int st = setup(A, c, nsteps, snapshots, obj)) return st;
-  cudaEvent_t e0, e1, e2;
-  HC_CUDA(cudaEventCreate(&e0));
-  HC_CUDA(cudaEventCreate(&e1));
-  HC_CUDA(cudaEventCreate(&e2));
-  std::vector<int> stack;
-  for (int k = snapshots - 1; k >= 0; --k) stack.push_back(k);
   Schedule sched;
-  sched.build(nsteps, snapshots);
-  const std::vector<std::pair<int, int>> stores = first_descent(sched, nsteps, snapshots, stack);
-  cudaEventRecord(e0, A.s());
+  std::vector<int> stack;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ~Tape() override {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  }
+};
+inline void free_tape(void* p) { delete static_cast<TapeBase*>(p); }
+
+template <class R> __global__ void to_double_kernel(const R* __restrict__ a, double* __restrict__ b, size_t n) {
+  for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < n; k += size_t(gridDim.x) * blockDim.x)
+    b[k] = double(a[k]);
+}
+
+// forward half: J, the rates, and the tape kept in the context
+template <class R>
+int adjoint_record(hc_ctx* c, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
+                   double* rates_out, double* J) {
+  if (c) c->drop_adj_tape();
+  std::unique_ptr<Tape<R>> T(new Tape<R>());
+  Adj<R>& A = T->A;
+  if (int st = setup(A, c, nsteps, snapshots, obj)) return st;
+  HC_CUDA(cudaEventCreate(&T->e0));
+  HC_CUDA(cudaEventCreate(&T->e1));
+  for (int k = snapshots - 1; k >= 0; --k) T->stack.push_back(k);
+  T->sched.build(nsteps, snapshots);
+  const std::vector<std::pair<int, int>> stores = first_descent(T->sched, nsteps, snapshots, T->stack);
+  cudaEventRecord(T->e0, A.s());
   if (int st = forward_pass(A, rates_in, stores)) return st;
-  cudaEventRecord(e1, A.s());
+  cudaEventRecord(T->e1, A.s());
+  double j = 0;
+  HC_CUDA(cudaMemcpyAsync(&j, A.jacc, sizeof(double), cudaMemcpyDeviceToHost, A.s()));
+  HC_CUDA(cudaStreamSynchronize(A.s()));
+  if (J) *J = j;
+  if (rates_out) std::memcpy(rates_out, A.hrates.data(), A.nsteps * sizeof(double));
+  c->adj_tape = T.release();
+  c->adj_tape_free = free_tape;
+  return HC_OK;
+}
+
+// reverse half: consumes the tape; q0_bar / ref_bar to host memory or, with on_device, to
+// FP64 device memory
+template <class R>
+int adjoint_reverse(hc_ctx* c, double* q0_bar, double* ref_bar, bool on_device, hc_adjoint_stats* stats) {
+  if (!c) return fail(HC_ERR_ARG, "null context");
+  Tape<R>* T = c->adj_tape ? dynamic_cast<Tape<R>*>(static_cast<TapeBase*>(c->adj_tape)) : nullptr;
+  if (!T) return fail(HC_ERR_ARG, "no recorded forward sweep of this context's precision to reverse");
+  std::unique_ptr<Tape<R>> own(T);
+  c->adj_tape = nullptr;
+  Adj<R>& A = T->A;
+  const int nsteps = A.nsteps;
+  cudaEvent_t e2;
+  HC_CUDA(cudaEventCreate(&e2));
   HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], A.state_values() * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
   // adjoint of the final state
   if (A.obj.kind == HC_OBJ_DRAG) {
@@ -626,19 +710,20 @@ int adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective* o
                                                   A.obj.weight[2], A.obj.weight[3], nullptr, 1, A.lam, A.nv);
     A.launches += 1;
   }
-  if (int st = reverse(A, sched, 0, nsteps, -1, stack, true)) return st;
+  if (int st = reverse(A, T->sched, 0, nsteps, -1, T->stack, true)) return st;
   cudaEventRecord(e2, A.s());
-  HC_CUDA(cudaStreamSynchronize(A.s()));
-  float ms_f = 0, ms_t = 0;
-  cudaEventElapsedTime(&ms_f, e0, e1);
-  cudaEventElapsedTime(&ms_t, e0, e2);
-  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
   auto fetch = [&](double* dst, const R* src, size_t m) -> int {
     if constexpr (std::is_same<R, double>::value) {
-      HC_CUDA(cudaMemcpy(dst, src, m * sizeof(double), cudaMemcpyDeviceToHost));
+      HC_CUDA(cudaMemcpyAsync(dst, src, m * sizeof(double),
+                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, A.s()));
+    } else if (on_device) {
+      to_double_kernel<R><<<512, 256, 0, A.s()>>>(src, dst, m);
+      HC_CUDA(cudaGetLastError());
+      A.launches += 1;
     } else {
       std::vector<R> tmp(m);
-      HC_CUDA(cudaMemcpy(tmp.data(), src, m * sizeof(R), cudaMemcpyDeviceToHost));
+      HC_CUDA(cudaMemcpyAsync(tmp.data(), src, m * sizeof(R), cudaMemcpyDeviceToHost, A.s()));
+      HC_CUDA(cudaStreamSynchronize(A.s()));
       for (size_t k = 0; k < m; ++k) dst[k] = double(tmp[k]);
     }
     return HC_OK;
@@ -652,13 +737,26 @@ int adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective* o
       off += m;
     }
   }
-  if (int st = finish_stats(A, nullptr, rates_out, stats)) return st;
+  // the tape's buffers are freed when this returns: after the stream's work on them
+  HC_CUDA(cudaStreamSynchronize(A.s()));
+  float ms_f = 0, ms_t = 0;
+  cudaEventElapsedTime(&ms_f, T->e0, T->e1);
+  cudaEventElapsedTime(&ms_t, T->e0, e2);
+  cudaEventDestroy(e2);
+  if (int st = finish_stats(A, nullptr, nullptr, stats)) return st;
   if (stats) {
     stats->ms_forward = ms_f;
     stats->ms_total = ms_t;
     stats->ms_recompute = A.recompute_ms();
   }
   return HC_OK;
+}
+
+template <class R>
+int adjoint_gradient(hc_ctx* c, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
+                     double* q0_bar, double* ref_bar, double* rates_out, hc_adjoint_stats* stats) {
+  if (int st = adjoint_record<R>(c, nsteps, snapshots, obj, rates_in, rates_out, nullptr)) return st;
+  return adjoint_reverse<R>(c, q0_bar, ref_bar, false, stats);
 }
 
 

@@ -5,6 +5,9 @@
 namespace hc {
 namespace adj {
 template int objective_forward<float>(hc_ctx*, int, const hc_objective*, const double*, double*, double*);
+template int wall_force<float>(hc_ctx*, const double*, double*);
+template int adjoint_record<float>(hc_ctx*, int, int, const hc_objective*, const double*, double*, double*);
+template int adjoint_reverse<float>(hc_ctx*, double*, double*, bool, hc_adjoint_stats*);
 template int adjoint_gradient<float>(hc_ctx*, int, int, const hc_objective*, const double*, double*, double*,
                                      double*, hc_adjoint_stats*);
 }  // namespace adj

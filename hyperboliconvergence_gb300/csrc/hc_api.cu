@@ -576,6 +576,7 @@ int hc_context_create(const hc_config* cfg, hc_ctx** out) {
 int hc_context_destroy(hc_ctx* c) {
   if (!c) return HC_OK;
   cudaStreamSynchronize(c->stream);
+  c->drop_adj_tape();
   free_buffers(c);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -602,6 +603,7 @@ int hc_mesh_upload(hc_ctx* c, int ni, int nj, const double* nodes_xy) {
   if (ni < 3 || nj < 3) return fail(HC_ERR_ARG, "mesh needs at least 3 cells in each direction");
   if (size_t(ni + 1) * size_t(nj + 1) > (size_t(1) << 28)) return fail(HC_ERR_ARG, "mesh too large");
   HC_CUDA(cudaStreamSynchronize(c->stream));
+  c->drop_adj_tape();
   free_buffers(c);
   c->oned = false;
   c->nv = c->scalar ? 3 : 4;
@@ -654,6 +656,7 @@ int hc_mesh_upload_1d(hc_ctx* c, int nc, const double* nodes_x) {
   for (int i = 0; i < nc; ++i)
     if (!(nodes_x[i + 1] > nodes_x[i])) return fail(HC_ERR_ARG, "1D nodes must increase");
   HC_CUDA(cudaStreamSynchronize(c->stream));
+  c->drop_adj_tape();
   free_buffers(c);
   c->oned = true;
   c->nv = 3;

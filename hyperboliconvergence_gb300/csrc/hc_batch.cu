@@ -329,6 +329,7 @@ int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* n
 int hc_batch_destroy(hc_batch* b) {
   if (!b) return HC_OK;
   cudaStreamSynchronize(b->stream);
+  b->drop_adj_tape();
   free_all(b);
   if (b->own) cudaStreamDestroy(b->own);
   delete b;
@@ -355,6 +356,21 @@ int hc_batch_state_upload(hc_batch* b, int k, const double* prim) {
     HC_CUDA(cudaMemcpyAsync((double*)b->q[0] + 4 * b->cell_off[k], prim, m * 8, cudaMemcpyHostToDevice, b->stream));
   }
   HC_CUDA(cudaStreamSynchronize(b->stream));
+  return HC_OK;
+}
+
+int hc_batch_state_upload_device(hc_batch* b, int k, const double* prim_device) {
+  if (int st = check_b(b)) return st;
+  if (k < 0 || k >= b->ninst || !prim_device) return fail(HC_ERR_ARG, "bad instance or null state");
+  const size_t m = size_t(b->nv) * b->icells(k);
+  if (b->fp32) {
+    batch_d2r<float><<<512, 256, 0, b->stream>>>(prim_device, (float*)b->q[0] + 4 * b->cell_off[k], m);
+    HC_CUDA(cudaGetLastError());
+    b->launches += 1;
+  } else {
+    HC_CUDA(cudaMemcpyAsync((double*)b->q[0] + 4 * b->cell_off[k], prim_device, m * 8, cudaMemcpyDeviceToDevice,
+                            b->stream));
+  }
   return HC_OK;
 }
 

@@ -37,6 +37,14 @@ struct hc_batch {
   cudaGraphExec_t graph_exec = nullptr;
   int graph_steps = 0;
   long long launches = 0;
+  // the forward sweep recorded by hc_batch_adjoint_record for hc_batch_adjoint_reverse
+  // (owned here, released by the reverse sweep, the next record or destroy)
+  void* adj_tape = nullptr;
+  void (*adj_tape_free)(void*) = nullptr;
+  void drop_adj_tape() {
+    if (adj_tape && adj_tape_free) adj_tape_free(adj_tape);
+    adj_tape = nullptr;
+  }
 
   size_t icells(int k) const { return size_t(ni[k]) * nj[k]; }
 };

@@ -21,6 +21,8 @@
 #include "hc_adjoint_driver.cuh"
 #include "hc_batch.h"
 
+#include <memory>
+
 namespace hc {
 namespace adj {
 
@@ -318,7 +320,8 @@ int batch_setup(BAdj<R>& A, hc_batch* b, int nsteps, int nsnap, const hc_objecti
   if (b->scalar) HC_CUDA(cudaMemsetAsync(A.target, 0, n4 * sizeof(R), A.s()));
   for (int k = 0; k < A.ninst; ++k) {
     const size_t m = size_t(b->nv) * b->icells(k);
-    HC_CUDA(cudaMemcpyAsync(b->staging, targets[k], m * sizeof(double), cudaMemcpyHostToDevice, A.s()));
+    HC_CUDA(cudaMemcpyAsync(b->staging, targets[k], m * sizeof(double),
+                            obj->target_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, A.s()));
     convert_kernel<R><<<512, 256, 0, A.s()>>>(b->staging, A.target + 4 * b->cell_off[k], m);
     HC_CUDA(cudaGetLastError());
     HC_CUDA(cudaStreamSynchronize(A.s()));  // targets[k] and the staging buffer are reused
@@ -346,51 +349,99 @@ template <class R> int batch_forward_pass(BAdj<R>& A, const std::vector<std::pai
   return HC_OK;
 }
 
-template <class R>
-int batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj,
-                           const double* const* targets, double* J, double* const* q0_bar, hc_adjoint_stats* stats) {
+// A recorded forward sweep: the adjoint buffers with the checkpoints of the schedule's
+// first descent, the schedule and its free snapshot slots, kept between
+// hc_batch_adjoint_record and hc_batch_adjoint_reverse.
+struct BTapeBase {
+  virtual ~BTapeBase() = default;
+};
+template <class R> struct BTape : BTapeBase {
   BAdj<R> A;
-  if (int st = batch_setup(A, b, nsteps, snapshots, obj, targets)) return st;
-  cudaEvent_t e0, e1, e2;
-  HC_CUDA(cudaEventCreate(&e0));
-  HC_CUDA(cudaEventCreate(&e1));
-  HC_CUDA(cudaEventCreate(&e2));
-  std::vector<int> stack;
-  for (int k = snapshots - 1; k >= 0; --k) stack.push_back(k);
   Schedule sched;
-  sched.build(nsteps, snapshots);
-  const std::vector<std::pair<int, int>> stores = first_descent(sched, nsteps, snapshots, stack);
-  cudaEventRecord(e0, A.s());
+  std::vector<int> stack;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ~BTape() override {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  }
+};
+inline void free_btape(void* p) { delete static_cast<BTapeBase*>(p); }
+
+__global__ void to_double_kernel(const float* __restrict__ a, double* __restrict__ b, size_t n) {
+  for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < n; k += size_t(gridDim.x) * blockDim.x)
+    b[k] = double(a[k]);
+}
+
+// forward half: J per instance (host), the tape kept in the batch
+template <class R>
+int batch_record(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj, const double* const* targets,
+                 double* J) {
+  b->drop_adj_tape();
+  std::unique_ptr<BTape<R>> T(new BTape<R>());
+  BAdj<R>& A = T->A;
+  if (int st = batch_setup(A, b, nsteps, snapshots, obj, targets)) return st;
+  HC_CUDA(cudaEventCreate(&T->e0));
+  HC_CUDA(cudaEventCreate(&T->e1));
+  for (int k = snapshots - 1; k >= 0; --k) T->stack.push_back(k);
+  T->sched.build(nsteps, snapshots);
+  const std::vector<std::pair<int, int>> stores = first_descent(T->sched, nsteps, snapshots, T->stack);
+  cudaEventRecord(T->e0, A.s());
   if (int st = batch_forward_pass(A, stores)) return st;
-  cudaEventRecord(e1, A.s());
+  cudaEventRecord(T->e1, A.s());
+  if (J) {
+    HC_CUDA(cudaMemcpyAsync(J, A.jacc, A.ninst * sizeof(double), cudaMemcpyDeviceToHost, A.s()));
+    HC_CUDA(cudaStreamSynchronize(A.s()));
+  }
+  b->adj_tape = T.release();
+  b->adj_tape_free = free_btape;
+  return HC_OK;
+}
+
+// reverse half: consumes the tape; q0_bar[k] (NULL entries skipped) in host memory or, with
+// on_device, FP64 device memory written asynchronously on the batch's stream
+template <class R> int batch_reverse(hc_batch* b, double* const* q0_bar, bool on_device, hc_adjoint_stats* stats) {
+  BTape<R>* T = b->adj_tape ? dynamic_cast<BTape<R>*>(static_cast<BTapeBase*>(b->adj_tape)) : nullptr;
+  if (!T) return fail(HC_ERR_ARG, "no recorded forward sweep of this batch's precision to reverse");
+  std::unique_ptr<BTape<R>> own(T);
+  b->adj_tape = nullptr;
+  BAdj<R>& A = T->A;
+  const int nsteps = A.nsteps;
+  cudaEvent_t e2;
+  HC_CUDA(cudaEventCreate(&e2));
   HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], A.state_values() * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
   if (int st = l2_objective(A, true)) return st;  // adjoint of the final states
-  if (int st = reverse(A, sched, 0, nsteps, -1, stack, true)) return st;
+  if (int st = reverse(A, T->sched, 0, nsteps, -1, T->stack, true)) return st;
   cudaEventRecord(e2, A.s());
-  HC_CUDA(cudaStreamSynchronize(A.s()));
-  float ms_f = 0, ms_t = 0;
-  cudaEventElapsedTime(&ms_f, e0, e1);
-  cudaEventElapsedTime(&ms_t, e0, e2);
-  cudaEventDestroy(e0); cudaEventDestroy(e1); cudaEventDestroy(e2);
-  std::vector<double> jh(A.ninst);
-  HC_CUDA(cudaMemcpy(jh.data(), A.jacc, A.ninst * sizeof(double), cudaMemcpyDeviceToHost));
-  if (J) std::memcpy(J, jh.data(), A.ninst * sizeof(double));
   if (q0_bar) {
     for (int k = 0; k < A.ninst; ++k) {
       if (!q0_bar[k]) continue;
       const size_t m = size_t(b->nv) * b->icells(k);
       const R* src = A.lam + 4 * b->cell_off[k];
       if constexpr (std::is_same<R, double>::value) {
-        HC_CUDA(cudaMemcpy(q0_bar[k], src, m * sizeof(double), cudaMemcpyDeviceToHost));
+        HC_CUDA(cudaMemcpyAsync(q0_bar[k], src, m * sizeof(double),
+                                on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, A.s()));
+      } else if (on_device) {
+        to_double_kernel<<<512, 256, 0, A.s()>>>(src, q0_bar[k], m);
+        HC_CUDA(cudaGetLastError());
+        A.launches += 1;
       } else {
         std::vector<R> tmp(m);
-        HC_CUDA(cudaMemcpy(tmp.data(), src, m * sizeof(R), cudaMemcpyDeviceToHost));
+        HC_CUDA(cudaMemcpyAsync(tmp.data(), src, m * sizeof(R), cudaMemcpyDeviceToHost, A.s()));
+        HC_CUDA(cudaStreamSynchronize(A.s()));
         for (size_t v = 0; v < m; ++v) q0_bar[k][v] = double(tmp[v]);
       }
     }
   }
+  // the device's work and the tape's buffers end together: free them after the stream
+  HC_CUDA(cudaStreamSynchronize(A.s()));
+  float ms_f = 0, ms_t = 0;
+  cudaEventElapsedTime(&ms_f, T->e0, T->e1);
+  cudaEventElapsedTime(&ms_t, T->e0, e2);
+  cudaEventDestroy(e2);
   b->launches += A.launches;
   if (stats) {
+    std::vector<double> jh(A.ninst);
+    HC_CUDA(cudaMemcpy(jh.data(), A.jacc, A.ninst * sizeof(double), cudaMemcpyDeviceToHost));
     double jsum = 0;
     for (double v : jh) jsum += v;
     stats->J = jsum;
@@ -404,6 +455,13 @@ int batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_obje
   return HC_OK;
 }
 
+template <class R>
+int batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj,
+                           const double* const* targets, double* J, double* const* q0_bar, hc_adjoint_stats* stats) {
+  if (int st = batch_record<R>(b, nsteps, snapshots, obj, targets, J)) return st;
+  return batch_reverse<R>(b, q0_bar, false, stats);
+}
+
 }  // namespace adj
 }  // namespace hc
 
@@ -413,4 +471,17 @@ extern "C" int hc_batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots,
   if (!b) return hc::fail(HC_ERR_ARG, "null batch");
   if (b->fp32) return hc::adj::batch_adjoint_gradient<float>(b, nsteps, snapshots, obj, targets, J, q0_bar, stats);
   return hc::adj::batch_adjoint_gradient<double>(b, nsteps, snapshots, obj, targets, J, q0_bar, stats);
+}
+
+extern "C" int hc_batch_adjoint_record(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj,
+                                       const double* const* targets, double* J) {
+  if (!b) return hc::fail(HC_ERR_ARG, "null batch");
+  if (b->fp32) return hc::adj::batch_record<float>(b, nsteps, snapshots, obj, targets, J);
+  return hc::adj::batch_record<double>(b, nsteps, snapshots, obj, targets, J);
+}
+
+extern "C" int hc_batch_adjoint_reverse(hc_batch* b, double* const* q0_bar, int on_device, hc_adjoint_stats* stats) {
+  if (!b) return hc::fail(HC_ERR_ARG, "null batch");
+  if (b->fp32) return hc::adj::batch_reverse<float>(b, q0_bar, on_device != 0, stats);
+  return hc::adj::batch_reverse<double>(b, q0_bar, on_device != 0, stats);
 }

@@ -22,6 +22,14 @@ struct hc_ctx {
   double lref = 1., sdt = 1.7976931348623157e308;  // species lref and dt (AUSM+up scaling)
   int vscale = 0, pscale = 0;                       // AUSM+up LowMachScaling pair
   unsigned fixes = 0;                               // HC_FIX_* corrections (hc_set_corrections)
+  // the forward sweep recorded by hc_adjoint_record for hc_adjoint_reverse (owned here,
+  // released by the reverse sweep, the next record, a mesh upload or destroy)
+  void* adj_tape = nullptr;
+  void (*adj_tape_free)(void*) = nullptr;
+  void drop_adj_tape() {
+    if (adj_tape && adj_tape_free) adj_tape_free(adj_tape);
+    adj_tape = nullptr;
+  }
   void* dual_src = nullptr;                         // dual time: earlier levels' terms (4 planes, R)
   double dual_g0 = 1.0, dual_b0dt = 0.0;            // dual time: gamma_0 and beta_0 / dt
   double smooth_alpha = 0.0;                        // 1D residual smoothing factor (0: off)

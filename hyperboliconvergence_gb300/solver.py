@@ -225,6 +225,34 @@ class Solver:
             off += nv * nf
         return st.J, q0b, refb, rout, st
 
+    def record(self, nsteps, snapshots=20, kind="drag", rates=None, **kw):
+        """The forward half of `gradient` (hc_adjoint_record): (J, rates) of nsteps steps from
+        the current state; the checkpoints stay in the context for `reverse`."""
+        o = self._objective(kind, **kw)
+        self._tape_objective = o
+        J = C.c_double()
+        rout = np.empty(int(nsteps))
+        rin = None if rates is None else np.ascontiguousarray(rates, dtype=np.float64)
+        check(self.lib.hc_adjoint_record(self.h, int(nsteps), int(snapshots), C.byref(o),
+                                         _dptr(rin) if rin is not None else None, _dptr(rout), C.byref(J)))
+        return J.value, rout
+
+    def reverse(self, q0_bar=None, ref_bar=None):
+        """The reverse half (hc_adjoint_reverse) into float64 CUDA tensors: q0_bar of the state's
+        shape, ref_bar of sum over sides of nv * nface values (either may be None)."""
+        from ._capi import AdjointStats
+        st = AdjointStats()
+
+        def ptr(t):
+            return None if t is None else C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+        check(self.lib.hc_adjoint_reverse(self.h, ptr(q0_bar), ptr(ref_bar), 1, C.byref(st)))
+        self._tape_objective = None
+        return st
+
+    def upload_device(self, prim) -> None:
+        """The state from a CUDA tensor of the context's precision (hc_state_upload_device)."""
+        check(self.lib.hc_state_upload_device(self.h, C.c_void_p(prim.contiguous().data_ptr())))
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.hc_context_destroy(self.h)
@@ -311,6 +339,13 @@ class Solver:
         self.steps_done += int(n)
         self.last = st
         return st
+
+    def wall_force(self, direction=(1.0, 0.0)) -> float:
+        """Pressure force on the wall sides along `direction` (hc_wall_force)."""
+        d = np.ascontiguousarray(direction, dtype=np.float64)
+        out = np.zeros(1)
+        check(self.lib.hc_wall_force(self.h, _dptr(d), _dptr(out)))
+        return float(out[0])
 
     def set_time(self, t: float, steps_done: int | None = None) -> None:
         """The accumulated time (and, optionally, the count of steps taken) a resumed run

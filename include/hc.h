@@ -329,6 +329,7 @@ typedef struct {
   const double* target;  /* L2: J = sum_cells sum_v weight[v] (q_N - target)^2, target 4 planes (host;
                             3 for the scalar law) */
   double weight[4];
+  int target_on_device;  /* L2: target (and a batch's targets[k]) is FP64 device memory, not host */
 } hc_objective;
 
 typedef struct {
@@ -341,6 +342,12 @@ typedef struct {
   double ms_recompute;       /* part of the reverse sweep spent re-advancing from checkpoints */
 } hc_adjoint_stats;
 
+/* The pressure force on the inviscid-wall sides of the current state along dir (the
+ * momentum flux the wall faces' boundary flux carries, inviscidWall.ipp:33-72, summed over
+ * every wall face); the drag coefficient is that along the freestream divided by
+ * (rho U^2 / 2) times the body's length scale.  2D Euler contexts, primitive basis. */
+int hc_wall_force(hc_ctx* ctx, const double dir[2], double* force);
+
 /* J only; rates_in NULL = compute the timesteps (rates_out receives them, nsteps values). */
 int hc_objective_forward(hc_ctx* ctx, int nsteps, const hc_objective* obj, const double* rates_in,
                          double* rates_out, double* J);
@@ -350,6 +357,15 @@ int hc_objective_forward(hc_ctx* ctx, int nsteps, const hc_objective* obj, const
  * {u, v, q} with weight[0..2]; periodic, fixed or Riemann sides): 3 planes each. */
 int hc_adjoint_gradient(hc_ctx* ctx, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
                         double* q0_bar, double* ref_bar, double* rates_out, hc_adjoint_stats* stats);
+/* hc_adjoint_gradient in two calls: record runs the forward sweep (J, rates_out) and keeps
+ * its checkpoints in the context; reverse runs the reverse sweep from them without repeating
+ * the forward sweep, writes q0_bar and ref_bar (layouts as above; NULL to skip) to host
+ * memory or, with on_device, to FP64 device memory (asynchronous on the context's stream),
+ * and releases the recording.  A new record, a mesh upload or destroy drops an unreversed
+ * recording. */
+int hc_adjoint_record(hc_ctx* ctx, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
+                      double* rates_out, double* J);
+int hc_adjoint_reverse(hc_ctx* ctx, double* q0_bar, double* ref_bar, int on_device, hc_adjoint_stats* stats);
 
 /* ---------------------------------------------------------------------------
  * Batched path: many independent meshes of uneven sizes in one set of buffers.
@@ -437,6 +453,17 @@ long long hc_batch_kernel_launches(hc_batch* b);
 int hc_batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj,
                               const double* const* targets, double* J, double* const* q0_bar,
                               hc_adjoint_stats* stats);
+/* hc_batch_adjoint_gradient in two calls, for a differentiable forward whose backward comes
+ * later (torch.autograd.Function): record runs the forward sweep (J[k] to the host) and keeps
+ * its checkpoints in the batch; reverse runs the reverse sweep from them, writing q0_bar[k]
+ * to host memory or, with on_device, to FP64 device memory (asynchronous on the batch's
+ * stream), and releases them.  The forward sweep is not repeated.  A new record, or destroy,
+ * drops an unreversed recording. */
+int hc_batch_adjoint_record(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj,
+                            const double* const* targets, double* J);
+int hc_batch_adjoint_reverse(hc_batch* b, double* const* q0_bar, int on_device, hc_adjoint_stats* stats);
+/* instance k's state from FP64 device memory (asynchronous on the batch's stream) */
+int hc_batch_state_upload_device(hc_batch* b, int inst, const double* prim_soa_device);
 
 /* One interface flux evaluated on the host with the pointwise functions the stage kernels
  * compile: FluxInterface::flux(species, face, ql, qr) (conservationLaws/base/base.h:370-397)
