@@ -170,7 +170,10 @@ template <class C, class R> __device__ __forceinline__ Gas<C> gas_as(const Gas<R
 // REC: the recording instantiation also writes each face's branch signature to
 // a.sig_i / a.sig_j (the production instantiations compile without it).  DUAL: dual-time
 // terms are honoured (the batched instantiations, which have none, compile without them).
-template <int TI, int TJ, class R, int FK, class C = R, bool REC = false, bool DUAL = true, int NTH = TI * TJ>
+// LIM >= 0: the limiter is that compile-time constant (a.limiter must equal it), so its
+// selection folds away; -1: a.limiter chosen at run time.
+template <int TI, int TJ, class R, int FK, class C = R, bool REC = false, bool DUAL = true, int NTH = TI * TJ,
+          int LIM = -1>
 __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj, unsigned char* smem_raw) {
   constexpr bool same = std::is_same<C, R>::value;
   using SM = StageSmem<TI, TJ, C>;
@@ -257,12 +260,13 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   // ---- phase 3: face fluxes (i-faces then j-faces of the tile, each once)
   const Gas<C> g = gas_as<C>(a.gas);
   const bool cons = a.basis != 0;  // conserved solution basis
-  const int lim = a.limiter;
+  const int lim = LIM >= 0 ? LIM : a.limiter;
   constexpr int NFI = (TI + 1) * TJ, NFJ = TI * (TJ + 1);
-  for (int k = tid; k < NFI + NFJ; k += NT) {
-    const bool idir = k < NFI;
-    int la, lb;  // local coordinates of the face's right cell
-    if (idir) { la = k / TJ; lb = k % TJ; } else { const int kk = k - NFI; la = kk / (TJ + 1); lb = kk % (TJ + 1); }
+  // one face, its direction a compile-time constant (i-face kk or j-face kk of the tile)
+  auto face_body = [&](auto dirtag, const int kk) {
+    constexpr bool idir = decltype(dirtag)::value;
+    // local coordinates of the face's right cell
+    const int la = idir ? kk / TJ : kk / (TJ + 1), lb = idir ? kk % TJ : kk % (TJ + 1);
     const int gi = i0 + la, gj = j0 + lb;
     bool valid = idir ? (gi <= ni && gj < nj) : (gi < ni && gj <= nj);
     Flux5<C> F;
@@ -436,10 +440,16 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     }
     C* dst = idir ? sfi : sfj;
     const int slot = idir ? (la * TJ + lb) : (la * (TJ + 1) + lb);
-    const int pl = idir ? NFI : NFJ;
+    constexpr int pl = idir ? NFI : NFJ;
 #pragma unroll
     for (int v = 0; v < 4; ++v) dst[v * pl + slot] = F.f[v];
     dst[4 * pl + slot] = F.lam;
+  };
+  // the i-faces then the j-faces, dealt round-robin to the threads as one list (the branch
+  // is uniform in every warp wholly inside one direction's range)
+  for (int k = tid; k < NFI + NFJ; k += NT) {
+    if (k < NFI) face_body(std::true_type{}, k);
+    else face_body(std::false_type{}, k - NFI);
   }
   __syncthreads();
 
@@ -515,13 +525,13 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   R fac;
   if (a.mode == MODE_FUSED_GLOBAL) {
     const R dts = a.beta * R(a.info->dt);
-    fac = dts / a.vol[c];
+    fac = qdiv(dts, a.vol[c]);
   } else {
     // local timestep from the stage-0 spectral radius sum (eulerForwardUpdate.h:155-161)
     const R l0 = (a.stage == 0) ? lam : a.res_prev[0][4 * ncell + c];
     const R cs = a.beta * a.cfl;
     // dual time: dtau / (1 + b0 dtau / dt), the physical-time term's share of the spectral radius
-    fac = (DUAL && a.dual_src) ? cs / (l0 + a.cfl * a.vol[c] * a.dual_b0dt) : cs / l0;
+    fac = (DUAL && a.dual_src) ? cs / (l0 + a.cfl * a.vol[c] * a.dual_b0dt) : qdiv(cs, l0);
   }
   R q0[4], qn[4];
 #pragma unroll
@@ -544,11 +554,11 @@ template <class R, class C, int NT> struct StageResidency {
                                : (std::is_same<C, R>::value ? 512 / NT : 768 / NT);
 };
 
-template <int TI, int TJ, class R, int FK, class C = R, int NT = TI * TJ>
+template <int TI, int TJ, class R, int FK, class C = R, int NT = TI * TJ, int LIM = -1>
 __global__ void __launch_bounds__(NT, (StageResidency<R, C, NT>::value))
     stage_kernel(const StageArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_tile<TI, TJ, R, FK, C, false, true, NT>(a, blockIdx.y, blockIdx.x, smem_raw);
+  stage_tile<TI, TJ, R, FK, C, false, true, NT, LIM>(a, blockIdx.y, blockIdx.x, smem_raw);
 }
 
 // the recording variant (a diagnostic, not on the stepping path): the same tile with
@@ -680,7 +690,7 @@ template <class R, int NT> struct BatchResidency {
   static constexpr int value = (sizeof(R) == 4 ? 1024 : 512) / NT;
 };
 
-template <int TI, int TJ, class R, int FK>
+template <int TI, int TJ, class R, int FK, int LIM = -1>
 __global__ void __launch_bounds__(TI * TJ, (BatchResidency<R, TI * TJ>::value))
     batch_stage_kernel(const BatchArgs<R> b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -699,7 +709,7 @@ __global__ void __launch_bounds__(TI * TJ, (BatchResidency<R, TI * TJ>::value))
       tile_ij[1] = t % tj;
     }
     __syncthreads();
-    stage_tile<TI, TJ, R, FK, R, false, false>(sa, tile_ij[0], tile_ij[1], smem_raw);
+    stage_tile<TI, TJ, R, FK, R, false, false, TI * TJ, LIM>(sa, tile_ij[0], tile_ij[1], smem_raw);
   }
 }
 

@@ -74,18 +74,42 @@ inline void tile_dims(int tile, int* ti, int* tj) {
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,                             \
                                 int(StageSmem<TI, TJ, R>::bytes));                                       \
   }                                                                                                      \
-  template <class R, int TI, int TJ> static void gob(const BatchArgs<R>& b, int grid, cudaStream_t s) {  \
+  /* FP32 kernels with the limiter a compile-time constant (the FP32 stage is bound by */               \
+  /* instruction issue; the run-time selection costs ~9% of it): the 8x32 single-mesh  */               \
+  /* tile for the common limiters, and every batch tile for van Albada and NoLimit3     */               \
+  template <int LIM> static void go_lim(const StageArgs<float>& a, cudaStream_t s) {                     \
+    const dim3 grid((a.nj + 31) / 32, (a.ni + 7) / 8);                                                   \
+    stage_kernel<8, 32, float, FK, float, 256, LIM><<<grid, 256, StageSmem<8, 32, float>::bytes, s>>>(a); \
+  }                                                                                                      \
+  static bool go_fixed_lim(const StageArgs<float>& a, cudaStream_t s) {                                  \
+    switch (a.limiter) {                                                                                 \
+      case LIM_VANALBADA: go_lim<LIM_VANALBADA>(a, s); return true;                                      \
+      case LIM_VANLEER: go_lim<LIM_VANLEER>(a, s); return true;                                          \
+      case LIM_MINMOD: go_lim<LIM_MINMOD>(a, s); return true;                                            \
+      case LIM_NOLIMIT2: go_lim<LIM_NOLIMIT2>(a, s); return true;                                        \
+      case LIM_NOLIMIT3: go_lim<LIM_NOLIMIT3>(a, s); return true;                                        \
+      default: return false;                                                                             \
+    }                                                                                                    \
+  }                                                                                                      \
+  template <class R, int TI, int TJ, int LIM = -1>                                                        \
+  static void gob(const BatchArgs<R>& b, int grid, cudaStream_t s) {                                     \
     /* a persistent grid larger than what stays resident would run a second, partial wave */           \
     static int cap = 0;                                                                                  \
     if (cap == 0) {                                                                                      \
       int dev = 0, sms = 0, occ = 0;                                                                     \
       cudaGetDevice(&dev);                                                                               \
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);                                 \
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_stage_kernel<TI, TJ, R, FK>, TI * TJ,    \
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_stage_kernel<TI, TJ, R, FK, LIM>, TI * TJ, \
                                                     StageSmem<TI, TJ, R>::bytes);                        \
       cap = (sms > 0 && occ > 0) ? sms * occ : grid;                                                     \
     }                                                                                                    \
-    batch_stage_kernel<TI, TJ, R, FK><<<std::min(grid, cap), TI * TJ, StageSmem<TI, TJ, R>::bytes, s>>>(b); \
+    batch_stage_kernel<TI, TJ, R, FK, LIM><<<std::min(grid, cap), TI * TJ, StageSmem<TI, TJ, R>::bytes, s>>>( \
+        b);                                                                                              \
+  }                                                                                                      \
+  template <int LIM> static void gob_tile(const BatchArgs<float>& b, int tile, int grid, cudaStream_t s) { \
+    if (tile == TILE_4x32) gob<float, 4, 32, LIM>(b, grid, s);                                           \
+    else if (tile == TILE_16x16) gob<float, 16, 16, LIM>(b, grid, s);                                    \
+    else gob<float, 8, 32, LIM>(b, grid, s);                                                             \
   }                                                                                                      \
   template <> cudaError_t launch_batch_stage<double, FK>(const BatchArgs<double>& b, int tile, int grid, \
                                                          cudaStream_t s) {                               \
@@ -96,9 +120,9 @@ inline void tile_dims(int tile, int* ti, int* tj) {
   }                                                                                                      \
   template <> cudaError_t launch_batch_stage<float, FK>(const BatchArgs<float>& b, int tile, int grid,   \
                                                         cudaStream_t s) {                                \
-    if (tile == TILE_4x32) gob<float, 4, 32>(b, grid, s);                                                \
-    else if (tile == TILE_16x16) gob<float, 16, 16>(b, grid, s);                                         \
-    else gob<float, 8, 32>(b, grid, s);                                                                  \
+    if (b.limiter == LIM_VANALBADA) gob_tile<LIM_VANALBADA>(b, tile, grid, s);                           \
+    else if (b.limiter == LIM_NOLIMIT3) gob_tile<LIM_NOLIMIT3>(b, tile, grid, s);                        \
+    else gob_tile<-1>(b, tile, grid, s);                                                                 \
     return cudaGetLastError();                                                                           \
   }                                                                                                      \
   template <class R, int TI, int TJ> static void go(const StageArgs<R>& a, cudaStream_t s) {             \
@@ -131,6 +155,9 @@ inline void tile_dims(int tile, int* ti, int* tj) {
       stage_kernel<8, 32, double, FK, df64><<<grid, 256, StageSmem<8, 32, df64>::bytes, s>>>(           \
           *reinterpret_cast<const StageArgs<double>*>(&a));                                              \
       return cudaGetLastError();                                                                         \
+    }                                                                                                    \
+    if constexpr (std::is_same<R, float>::value) {                                                       \
+      if ((tile == TILE_8x32 || tile < 0 || tile >= TILE_COUNT) && go_fixed_lim(a, s)) return cudaGetLastError(); \
     }                                                                                                    \
     if (tile == TILE_4x32) go<R, 4, 32>(a, s);                                                           \
     else if (tile == TILE_16x16) go<R, 16, 16>(a, s);                                                    \

@@ -26,6 +26,22 @@ enum LimiterKind { LIM_NOLIMIT1 = 0, LIM_NOLIMIT2 = 1, LIM_NOLIMIT3 = 2, LIM_VAN
                    LIM_VANLEER_REF = 8, LIM_CADA3 = 9, LIM_COUNT = 10 };
 enum BcKind { BC_PERIODIC = 0, BC_FIXED = 1, BC_RIEMANN = 2, BC_ENTROPY = 3, BC_WALL = 4 };
 
+// a / b in the stage arithmetic.  FP32 on the device: the approximate quotient
+// (__fdividef: within 2 ulp for |b| in [2^-126, 2^126]); the FP32 stage kernels are
+// bound by instruction issue, and the correctly rounded division costs a sequence of
+// instructions with a slow path (measured: 19% of the FP32 stage).  Used where the
+// divisor is a density, a limiter denominator (at least the smallest normal value), an
+// averaged sound speed or a volume.  FP64 and double-float keep exact division, so the
+// FP64 results are unchanged.
+template <class R> __host__ __device__ __forceinline__ R qdiv(R a, R b) { return a / b; }
+template <> __host__ __device__ __forceinline__ float qdiv<float>(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+
 template <class R> struct Lim;
 template <> struct Lim<double> {
   __host__ __device__ static constexpr double tiny() { return DBL_MIN; }
@@ -136,7 +152,7 @@ template <class R> __host__ __device__ __forceinline__ St<R> cons_state_ir(const
 // set2State of the solution basis: primitive {u, v, rho, p} or conserved
 // {rho u, rho v, rho, rho E} (cons = true); the choice is uniform across a launch
 template <class R> __host__ __device__ __forceinline__ St<R> cons_state(const Gas<R>& g, const R* qc) {
-  return cons_state_ir(g, qc, R(1) / qc[2]);
+  return cons_state_ir(g, qc, qdiv(R(1), qc[2]));
 }
 
 template <class R> __host__ __device__ __forceinline__ St<R> basis_state(const Gas<R>& g, const R* q, bool cons) {
@@ -211,8 +227,8 @@ __host__ __device__ __forceinline__ void basis_state2(const Gas<R>& g, const R* 
       ir = 1.0 / qr[2];
     }
   } else {
-    il = R(1) / ql[2];
-    ir = R(1) / qr[2];
+    il = qdiv(R(1), ql[2]);
+    ir = qdiv(R(1), qr[2]);
   }
   if (cons) {
     sl = cons_state_ir(g, ql, il);
@@ -290,7 +306,7 @@ __host__ __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g, R nx, R n
   const Flux5<R> c = central_flux_u(nx, ny, A, l, r, al, ar);
   // roe average: cr = sqrt(rR/rL), ra = cr rL, 1/ra = cr/rR
   const R cr = sqrt(r.r * l.ir);
-  const R wl = R(1) / (R(1) + cr);
+  const R wl = qdiv(R(1), R(1) + cr);
   const R wr = R(1) - wl;
   const R ra = cr * l.r;
   const R ua = wl * l.u + wr * r.u;
@@ -343,7 +359,7 @@ __host__ __device__ __forceinline__ Flux5<R> roe_flux(const Gas<R>& g, R nx, R n
   cc -= ya * c1;
   const R dp = cc * g.gm1;
   // primitive -> characteristic, scaled by the wave speeds
-  if constexpr (!std::is_same<R, double>::value) a1 = R(1) / aa;
+  if constexpr (!std::is_same<R, double>::value) a1 = qdiv(R(1), aa);
   const R w0 = lam[0] * ((g.gamma * (dp * a1 * a1 - d2)) * rho1);
   const R w1 = lam[1] * (du0 - dp * rho1 * a1);
   const R w2 = lam[2] * (du0 + dp * rho1 * a1);
@@ -414,7 +430,7 @@ __host__ __device__ __forceinline__ Flux5<R> slau_flux(R nx, R ny, R A, const St
   sqrt_fast(l.a2, al);
   sqrt_fast(r.a2, ar);
   const R aa = R(0.5) * (al + ar);
-  const R aa1 = R(1) / aa;
+  const R aa1 = qdiv(R(1), aa);
   const R ma = ua * aa1;
   const R ma_hat = fmin(R(1), ma);
   const R unl = proj(nx, ny, l), unr = proj(nx, ny, r);
@@ -510,7 +526,7 @@ template <class R> __host__ __device__ __forceinline__ Flux5<R> roe_ws_flux(cons
   const Flux5<R> c = central_flux_u(nx, ny, A, l, r, al, ar);
   // roe average (conservationLaws/euler/fluxes/roe.ipp:2-48)
   const R cr = sqrt(r.r * l.ir);
-  const R wl = R(1) / (R(1) + cr);
+  const R wl = qdiv(R(1), R(1) + cr);
   const R wr = R(1) - wl;
   const R ra = cr * l.r;
   const R ua = wl * l.u + wr * r.u;
@@ -627,7 +643,7 @@ template <class R> __host__ __device__ __forceinline__ R limit(int kind, R a, R 
     case LIM_NOLIMIT1: return R(0);
     case LIM_NOLIMIT2: return R(0.5) * (a + b);
     case LIM_NOLIMIT3: return R(0.33333333333333333) * (R(2) * a + b);
-    case LIM_VANALBADA: return (a * b < R(0)) ? R(0) : (b * (a * a) + a * (b * b)) / (a * a + b * b + tiny);
+    case LIM_VANALBADA: return (a * b < R(0)) ? R(0) : qdiv(b * (a * a) + a * (b * b), a * a + b * b + tiny);
     case LIM_MINMOD: return (a > R(0)) ? fmin(a, fmax(b, R(0))) : fmax(a, fmin(b, R(0)));
     case LIM_SUPERBEE:
       return (a > R(0)) ? fmax(R(0), fmax(fmin(R(2) * a, b), fmin(R(2) * b, a)))
@@ -635,7 +651,7 @@ template <class R> __host__ __device__ __forceinline__ R limit(int kind, R a, R 
     case LIM_MC:
       return (a > R(0)) ? fmax(R(0), fmin(R(0.5) * (a + b), fmin(R(2) * b, R(2) * a)))
                         : fmin(R(0), fmax(R(0.5) * (a + b), fmax(R(2) * b, R(2) * a)));
-    case LIM_VANLEER: return (a * fabs(b) + fabs(a) * b) / (fabs(a) + fabs(b) + tiny);
+    case LIM_VANLEER: return qdiv(a * fabs(b) + fabs(a) * b, fabs(a) + fabs(b) + tiny);
     case LIM_VANLEER_REF: return (b + fabs(b)) / (a + fabs(b) + tiny);
     case LIM_CADA3: {
       const R gam = R(1.5), c1 = R(-2. / 7.), c2 = R(0.4), c3 = R(3) * gam - R(2);
@@ -736,7 +752,7 @@ __host__ __device__ __forceinline__ unsigned flux_bits(const Gas<R>& g, R nx, R 
     sqrt_fast(l.a2, al);
     sqrt_fast(r.a2, ar);
     const R aa = R(0.5) * (al + ar);
-    const R aa1 = R(1) / aa;
+    const R aa1 = qdiv(R(1), aa);
     const R ml = unl * aa1, mr = unr * aa1;
     return (fabs(ml) > R(1) ? 1u : 0u) | (fabs(mr) > R(1) ? 2u : 0u) | (ua * aa1 > R(1) ? 4u : 0u);
   } else if constexpr (FK == FLUX_AUSMPUP) {
