@@ -262,9 +262,10 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   const bool cons = a.basis != 0;  // conserved solution basis
   const int lim = LIM >= 0 ? LIM : a.limiter;
   constexpr int NFI = (TI + 1) * TJ, NFJ = TI * (TJ + 1);
-  // one face, its direction a compile-time constant (i-face kk or j-face kk of the tile)
-  auto face_body = [&](auto dirtag, const int kk) {
-    constexpr bool idir = decltype(dirtag)::value;
+  // one face: i-face kk (dir true) or j-face kk of the tile; dir is a bool, or a
+  // std::integral_constant that makes the direction a compile-time constant
+  auto face_body = [&](auto dir, const int kk) {
+    const bool idir = static_cast<bool>(dir);
     // local coordinates of the face's right cell
     const int la = idir ? kk / TJ : kk / (TJ + 1), lb = idir ? kk % TJ : kk % (TJ + 1);
     const int gi = i0 + la, gj = j0 + lb;
@@ -440,16 +441,24 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
     }
     C* dst = idir ? sfi : sfj;
     const int slot = idir ? (la * TJ + lb) : (la * (TJ + 1) + lb);
-    constexpr int pl = idir ? NFI : NFJ;
+    const int pl = idir ? NFI : NFJ;
 #pragma unroll
     for (int v = 0; v < 4; ++v) dst[v * pl + slot] = F.f[v];
     dst[4 * pl + slot] = F.lam;
   };
-  // the i-faces then the j-faces, dealt round-robin to the threads as one list (the branch
-  // is uniform in every warp wholly inside one direction's range)
+  // the i-faces then the j-faces, dealt round-robin to the threads as one list.  FP32: a
+  // body per direction (the branch is uniform in every warp wholly inside one direction's
+  // range; the issue-bound FP32 kernel saves the direction's selects); FP64 and
+  // double-float: one body with the direction a run-time value (two bodies measured 4%
+  // slower in the FP64-pipe-bound FP64 kernel)
   for (int k = tid; k < NFI + NFJ; k += NT) {
-    if (k < NFI) face_body(std::true_type{}, k);
-    else face_body(std::false_type{}, k - NFI);
+    if constexpr (std::is_same<C, float>::value) {
+      if (k < NFI) face_body(std::true_type{}, k);
+      else face_body(std::false_type{}, k - NFI);
+    } else {
+      const bool d = k < NFI;
+      face_body(d, d ? k : k - NFI);
+    }
   }
   __syncthreads();
 
