@@ -561,7 +561,9 @@ def measure_adjoint(nsteps: int = 400, snapshots: int = 20, precisions=("fp64", 
     angle of attack); binomial checkpointing with `snapshots` stored states.  Run with
     FP64 stages and with double-float forward stages (the reverse sweep is FP64 in
     both).  The adjoint-step metric is reverse-sweep time (checkpoint recomputation
-    included) per step over forward-sweep time per step."""
+    included) per step over forward-sweep time per step, with the default stage tapes
+    (snapshots + 1: each reversed step's stage states kept from the advance that computed
+    it last) and, for FP64, without them (every reversed step replayed)."""
     import math
     from hyperboliconvergence_gb300.solver import Mesh, Solver
     nr, nth, mach, alpha = 256, 512, 0.4, 0.0
@@ -572,11 +574,25 @@ def measure_adjoint(nsteps: int = 400, snapshots: int = 20, precisions=("fp64", 
     for prec in precisions:
         s = Solver(mesh, ["wall", "fixed", "periodic", "periodic"], ref, flux="roe", limiter="vanalbada",
                    rk="ssp34", precision=prec, dt="global", cfl=0.5, species=(1.4, 287.058, mach))
-        s.set_state(np.broadcast_to(qinf[:, None, None], (4, nr, nth)).copy())
+        q0 = np.broadcast_to(qinf[:, None, None], (4, nr, nth)).copy()
         scale = 1.0 / (0.5 * mach * mach * 2 * 0.5)
+        no_tapes = None
+        if prec == "fp64":
+            s.set_adjoint_tapes(0)
+            s.set_state(q0)
+            J0, g0, _, _, st0 = s.gradient(nsteps, snapshots=snapshots, kind="drag", scale=scale)
+            f0 = st0.ms_forward
+            no_tapes = {"adjoint_step_over_forward_step": (st0.ms_total - f0) / f0,
+                        "adjoint_step_over_forward_step_excl_recompute": (st0.ms_total - f0 - st0.ms_recompute) / f0,
+                        "replays": int(st0.replays), "forward_steps_total": int(st0.forward_steps)}
+            s.set_adjoint_tapes(-1)
+        s.set_state(q0)
         J, g, refb, rates, st = s.gradient(nsteps, snapshots=snapshots, kind="drag", scale=scale)
         s.close()
+        if no_tapes is not None:
+            no_tapes["gradient_bit_identical"] = bool(J0 == J and np.array_equal(g0, g))
         fwd, rev, rec = st.ms_forward, st.ms_total - st.ms_forward, st.ms_recompute
+        state_mib = 4 * nr * nth * 8 / 2 ** 20
         # freestream derivatives: q0 and the far-field layer both equal qinf(M, alpha);
         # Cd = scale(M) * D with scale ~ 1/M^2
         dq_dm = np.array([math.cos(alpha), math.sin(alpha), 0.0, 0.0])
@@ -590,7 +606,11 @@ def measure_adjoint(nsteps: int = 400, snapshots: int = 20, precisions=("fp64", 
             "forward_step_ms": fwd / nsteps,
             "adjoint_step_over_forward_step": rev / fwd,
             "adjoint_step_over_forward_step_excl_recompute": (rev - rec) / fwd,
-            "forward_steps_total": int(st.forward_steps), "adjoint_steps": int(st.adjoint_steps)}
+            "forward_steps_total": int(st.forward_steps), "adjoint_steps": int(st.adjoint_steps),
+            "replays": int(st.replays), "stage_tapes": int(st.stage_tapes),
+            "snapshot_mib": snapshots * state_mib, "stage_tape_mib": int(st.stage_tapes) * 4 * state_mib}
+        if no_tapes is not None:
+            out[prec]["without_stage_tapes"] = no_tapes
     if "fp64" in out and "fp64_df" in out:
         a, b = out["fp64"], out["fp64_df"]
         out["df_vs_fp64_grad_rel_diff"] = {k: abs(b[k] - a[k]) / max(abs(a[k]), 1e-300)

@@ -77,6 +77,7 @@ def _declare(lib):
         "hc_set_low_mach": [p, i, i, d, d],
         "hc_set_tile": [p, i],
         "hc_set_corrections": [p, C.c_uint],
+        "hc_set_adjoint_tapes": [p, C.c_int],
         "hc_set_time": [p, d],
         "hc_wall_force": [p, dp, dp],
         "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],
@@ -158,6 +159,7 @@ def _declare_batch(lib):
         "hc_batch_state_download": [p, i, dp],
         "hc_batch_set_schedule": [p, C.POINTER(Schedule)],
         "hc_batch_set_corrections": [p, C.c_uint],
+        "hc_batch_set_adjoint_tapes": [p, C.c_int],
         "hc_batch_get_schedule": [p, C.POINTER(Schedule)],
         "hc_batch_step_async": [p, i, i],
         "hc_batch_graph_capture": [p, i],
@@ -204,7 +206,7 @@ class SteadyStats(C.Structure):
 class AdjointStats(C.Structure):
     _fields_ = [("J", C.c_double), ("forward_steps", C.c_longlong), ("adjoint_steps", C.c_longlong),
                 ("kernel_launches", C.c_longlong), ("ms_forward", C.c_double), ("ms_total", C.c_double),
-                ("ms_recompute", C.c_double)]
+                ("ms_recompute", C.c_double), ("replays", C.c_longlong), ("stage_tapes", C.c_longlong)]
 
 
 OBJECTIVE = {"drag": 0, "l2": 1}

@@ -118,6 +118,11 @@ class Batch:
     def kernel_launches(self) -> int:
         return int(self.lib.hc_batch_kernel_launches(self.h))
 
+    def set_adjoint_tapes(self, ntapes: int = -1) -> None:
+        """Stage tapes of the batched adjoint's checkpointing (hc_batch_set_adjoint_tapes):
+        -1 one per snapshot and one more, 0 none, k at most k."""
+        check(self.lib.hc_batch_set_adjoint_tapes(self.h, int(ntapes)))
+
     def gradient(self, nsteps, targets, snapshots=20, weight=(1.0, 1.0, 1.0, 1.0), want=None):
         """Every instance's L2 objective J_k = sum w_v (q_k(N) - target_k)^2 after nsteps
         steps and its gradient with respect to the instance's current state, from one

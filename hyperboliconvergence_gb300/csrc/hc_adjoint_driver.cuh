@@ -22,6 +22,7 @@
 #include "hc_ctx.h"
 #include "hc_scalar.cuh"
 
+#include <algorithm>
 #include <cfloat>
 #include <cstring>
 #include <memory>
@@ -60,6 +61,15 @@ struct AdjCommon {
   }
 };
 
+// A stage tape: the start state and the stage states (sq[0..nst-1]) of one step, kept from
+// the advance (or the forward sweep) that computed the step last before its reversal, so
+// that the reversal needs no replay of the step.  Buffers move between sq and the tapes by
+// pointer exchange, never by copy.
+template <class R> struct StageTape {
+  R* q[4] = {nullptr, nullptr, nullptr, nullptr};
+  int step = -1;  // -1: free
+};
+
 template <class R> struct Adj : AdjCommon {
   hc_ctx* c = nullptr;
   int nst = 4;
@@ -80,6 +90,8 @@ template <class R> struct Adj : AdjCommon {
   R* snaps = nullptr;
   R* qnext = nullptr;  // the start state of the step reversed last (the output of the one reversed next)
   int nsnap = 0;
+  std::vector<StageTape<R>> tapes;
+  long long replays = 0;
   double* rates = nullptr;   // device, one max-rate per step
   R* wall = nullptr;    // per wall face partial forces
   double* jacc = nullptr;    // device accumulator of the objective
@@ -166,6 +178,40 @@ template <class R> int forward_step(Adj<R>& A, int step, bool rec, int nstages =
 
 // sq[nst] -> sq[0] (the step output becomes the next step's start)
 template <class AD> void swap_out(AD& A) { std::swap(A.sq[0], A.sq[A.nst]); }
+
+// ---- stage tapes (shared by the single-mesh and batched drivers)
+template <class AD> int tape_of(const AD& A, int step) {
+  for (size_t k = 0; k < A.tapes.size(); ++k)
+    if (A.tapes[k].step == step) return int(k);
+  return -1;
+}
+// after forward_step(A, step) and before swap_out: keep sq[0..nst-1] (q_step and its stage
+// states) in a free tape, if there is one
+template <class AD> void keep_stages(AD& A, int step) {
+  const int k = tape_of(A, -1);
+  if (k < 0) return;
+  for (int j = 0; j < A.nst; ++j) std::swap(A.sq[j], A.tapes[k].q[j]);
+  A.tapes[k].step = step;
+}
+// sq[0..nst-1] = q_step and its stage states: from the step's tape (released), or replayed
+// from q_step in sq[0]
+template <class AD> int stage_states(AD& A, int step) {
+  const int k = tape_of(A, step);
+  if (k < 0) {
+    A.replays += 1;
+    return forward_step(A, step, false, A.nst - 1);
+  }
+  for (int j = 0; j < A.nst; ++j) std::swap(A.sq[j], A.tapes[k].q[j]);
+  A.tapes[k].step = -1;
+  return HC_OK;
+}
+template <class AD> int alloc_tapes(AD& A, int ntapes) {
+  A.tapes.assign(size_t(std::max(ntapes, 0)), {});
+  for (auto& t : A.tapes)
+    for (int j = 0; j < A.nst; ++j)
+      if (int st = A.alloc(&t.q[j], A.state_values())) return st;
+  return HC_OK;
+}
 
 // acc[0] += sum of v[0..m) by one 256-thread block in a fixed order (deterministic)
 template <class R> __device__ __forceinline__ void block_sum_into(const R* __restrict__ v, int m, double* acc) {
@@ -292,9 +338,9 @@ template <class R> double step_dt(const Adj<R>& A, int step) {
 // lam holds the adjoint of q_{step+1}; sq[0] holds q_step.  On return lam holds
 // the adjoint of q_step (objective terms of q_step included).
 template <class R> int adjoint_step(Adj<R>& A, int step) {
-  // replay the step's stages but the last: its output q_{step+1} is the start state of
-  // the step reversed before this one, kept in qnext
-  if (int st = forward_step(A, step, false, A.nst - 1)) return st;
+  // the step's stage states from its tape, or a replay of its stages but the last (its
+  // output q_{step+1} is the start state of the step reversed before this one, kept in qnext)
+  if (int st = stage_states(A, step)) return st;
   const size_t bytes4 = A.state_values() * sizeof(R);
   HC_CUDA(cudaMemcpyAsync(A.sq[A.nst], A.qnext, bytes4, cudaMemcpyDeviceToDevice, A.s()));
   HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], bytes4, cudaMemcpyDeviceToDevice, A.s()));
@@ -417,6 +463,7 @@ template <class AD> int advance(AD& A, int from, int to) {
   HC_CUDA(cudaEventRecord(ev[0], A.s()));
   for (int k = from; k < to; ++k) {
     if (int st = forward_step(A, k, false)) return st;
+    if (k == to - 1) keep_stages(A, k);  // the step reversed next after the right part
     swap_out(A);
   }
   HC_CUDA(cudaEventRecord(ev[1], A.s()));
@@ -446,14 +493,24 @@ int reverse(AD& A, const Schedule& sc, int a, int b, int slot, std::vector<int>&
   const int sfree = int(stack.size());
   if (n <= 0) return HC_OK;
   if (n == 1) {
-    if (int st = restore(A, slot)) return st;
+    if (tape_of(A, a) < 0)
+      if (int st = restore(A, slot)) return st;
     return adjoint_step(A, a);
   }
   if (sfree == 0) {
+    // every step re-advanced from a; each advance keeps the stages of its last step, the
+    // next one reversed (a step with a tape first releases it, then advances for the next)
     for (int i = b - 1; i >= a; --i) {
-      if (int st = restore(A, slot)) return st;
-      if (int st = advance(A, a, i)) return st;
-      if (int st = adjoint_step(A, i)) return st;
+      if (tape_of(A, i) >= 0) {
+        if (int st = adjoint_step(A, i)) return st;
+        if (i == a) break;
+        if (int st = restore(A, slot)) return st;
+        if (int st = advance(A, a, i)) return st;
+      } else {
+        if (int st = restore(A, slot)) return st;
+        if (int st = advance(A, a, i)) return st;
+        if (int st = adjoint_step(A, i)) return st;
+      }
     }
     return HC_OK;
   }
@@ -547,15 +604,30 @@ template <class R> int setup(Adj<R>& A, hc_ctx* c, int nsteps, int nsnap, const 
   return HC_OK;
 }
 
+// The steps whose stages the forward sweep keeps: the last step and each one before a
+// stored position (the first steps reversed after the parts to their right), the latest
+// ones when there are fewer tapes than that.
+inline std::vector<char> sweep_keeps(int nsteps, const std::vector<std::pair<int, int>>& stores, int ntapes) {
+  std::vector<char> keep(size_t(nsteps), 0);
+  std::vector<int> cand;
+  for (const auto& p : stores) cand.push_back(p.first - 1);
+  cand.push_back(nsteps - 1);
+  std::sort(cand.begin(), cand.end());
+  for (int k = int(cand.size()) - 1, left = ntapes; k >= 0 && left > 0; --k, --left) keep[size_t(cand[k])] = 1;
+  return keep;
+}
+
 // forward pass from the base state: J and (rates == nullptr) the max-rate
 // history; the states at the positions of `stores` go to their snapshot slots
 template <class R>
 int forward_pass(Adj<R>& A, const double* rates_in, const std::vector<std::pair<int, int>>& stores = {}) {
   if (rates_in) HC_CUDA(cudaMemcpyAsync(A.rates, rates_in, A.nsteps * sizeof(double), cudaMemcpyHostToDevice, A.s()));
   if (int st = restore(A, -1)) return st;
+  const std::vector<char> keep = sweep_keeps(A.nsteps, stores, int(A.tapes.size()));
   size_t next = 0;
   for (int k = 0; k < A.nsteps; ++k) {
     if (int st = forward_step(A, k, rates_in == nullptr)) return st;
+    if (keep[size_t(k)]) keep_stages(A, k);
     swap_out(A);
     while (next < stores.size() && stores[next].first == k + 1) {
       if (int st = store(A, stores[next].second)) return st;
@@ -588,6 +660,8 @@ template <class R> int finish_stats(Adj<R>& A, double* J, double* rates_out, hc_
     stats->forward_steps = A.fwd_steps;
     stats->adjoint_steps = A.adj_steps;
     stats->kernel_launches = A.launches;
+    stats->replays = A.replays;
+    stats->stage_tapes = (long long)A.tapes.size();
   }
   return HC_OK;
 }
@@ -670,6 +744,8 @@ int adjoint_record(hc_ctx* c, int nsteps, int snapshots, const hc_objective* obj
   std::unique_ptr<Tape<R>> T(new Tape<R>());
   Adj<R>& A = T->A;
   if (int st = setup(A, c, nsteps, snapshots, obj)) return st;
+  // stage tapes: by default one per snapshot and one more, enough for every reversal
+  if (int st = alloc_tapes(A, std::min(c->adj_tapes < 0 ? snapshots + 1 : c->adj_tapes, nsteps))) return st;
   HC_CUDA(cudaEventCreate(&T->e0));
   HC_CUDA(cudaEventCreate(&T->e1));
   for (int k = snapshots - 1; k >= 0; --k) T->stack.push_back(k);

@@ -718,6 +718,13 @@ int hc_set_corrections(hc_ctx* c, unsigned mask) {
   return HC_OK;
 }
 
+int hc_set_adjoint_tapes(hc_ctx* c, int ntapes) {
+  if (int st = check_ctx(c)) return st;
+  if (ntapes < -1) return fail(HC_ERR_ARG, "stage tapes: -1 (one per snapshot and one more) or a count >= 0");
+  c->adj_tapes = ntapes;
+  return HC_OK;
+}
+
 int hc_set_tile(hc_ctx* c, int tile) {
   if (int st = check_ctx(c)) return st;
   if (tile < HC_TILE_8x32 || tile > HC_TILE_16x16_H) return fail(HC_ERR_ARG, "unknown tile shape");

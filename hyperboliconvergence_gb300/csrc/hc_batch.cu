@@ -400,6 +400,13 @@ int hc_batch_set_corrections(hc_batch* b, unsigned mask) {
   return HC_OK;
 }
 
+int hc_batch_set_adjoint_tapes(hc_batch* b, int ntapes) {
+  if (int st = check_b(b)) return st;
+  if (ntapes < -1) return fail(HC_ERR_ARG, "stage tapes: -1 (one per snapshot and one more) or a count >= 0");
+  b->adj_tapes = ntapes;
+  return HC_OK;
+}
+
 int hc_batch_set_schedule(hc_batch* b, const hc_schedule* s) {
   if (int st = check_b(b)) return st;
   if (!s || s->tile < HC_TILE_8x32 || s->tile > HC_TILE_16x16 || s->ctas_per_sm < 1 || s->ctas_per_sm > 64 ||

@@ -17,6 +17,7 @@ struct hc_batch {
   std::vector<std::vector<double>> href;  // 4 per instance
   double gamma = 1.4, Rgas = 287.058, minf = 1e-4;
   unsigned fixes = 0;  // HC_FIX_* corrections (hc_batch_set_corrections)
+  int adj_tapes = -1;  // adjoint stage tapes (hc_batch_set_adjoint_tapes); -1 auto
   cudaStream_t own = nullptr, stream = nullptr;
   int sms = 152;
   hc_schedule sched{HC_TILE_8x32, 2, HC_ORDER_LARGEST_FIRST, 0.f};

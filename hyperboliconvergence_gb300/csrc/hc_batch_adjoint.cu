@@ -45,6 +45,8 @@ template <class R> struct BAdj : AdjCommon {
   R* base = nullptr;
   R* snaps = nullptr;
   R* qnext = nullptr;  // the start states of the step reversed last
+  std::vector<StageTape<R>> tapes;
+  long long replays = 0;
   R* target = nullptr;
   R* part = nullptr;
   double* rates = nullptr;  // [step][instance]
@@ -175,8 +177,9 @@ template <class R> int res_adj(BAdj<R>& A, const R* q, const R* rbar, const R* a
 // lam holds the adjoint of every instance's q_{step+1}, sq[0] their q_step; on return
 // lam holds the adjoint of q_step
 template <class R> int adjoint_step(BAdj<R>& A, int step) {
-  // the last stage's output is the start state of the step reversed before (qnext)
-  if (int st = forward_step(A, step, false, A.nst - 1)) return st;
+  // stage states from the step's tape or a replay of its stages but the last (whose output
+  // is the start state of the step reversed before, qnext)
+  if (int st = stage_states(A, step)) return st;
   const size_t bytes4 = A.state_values() * sizeof(R);
   HC_CUDA(cudaMemcpyAsync(A.sq[A.nst], A.qnext, bytes4, cudaMemcpyDeviceToDevice, A.s()));
   HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], bytes4, cudaMemcpyDeviceToDevice, A.s()));
@@ -332,9 +335,11 @@ int batch_setup(BAdj<R>& A, hc_batch* b, int nsteps, int nsnap, const hc_objecti
 
 template <class R> int batch_forward_pass(BAdj<R>& A, const std::vector<std::pair<int, int>>& stores) {
   if (int st = restore(A, -1)) return st;
+  const std::vector<char> keep = sweep_keeps(A.nsteps, stores, int(A.tapes.size()));
   size_t next = 0;
   for (int k = 0; k < A.nsteps; ++k) {
     if (int st = forward_step(A, k, true)) return st;
+    if (keep[size_t(k)]) keep_stages(A, k);
     swap_out(A);
     while (next < stores.size() && stores[next].first == k + 1) {
       if (int st = store(A, stores[next].second)) return st;
@@ -380,6 +385,7 @@ int batch_record(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj
   std::unique_ptr<BTape<R>> T(new BTape<R>());
   BAdj<R>& A = T->A;
   if (int st = batch_setup(A, b, nsteps, snapshots, obj, targets)) return st;
+  if (int st = alloc_tapes(A, std::min(b->adj_tapes < 0 ? snapshots + 1 : b->adj_tapes, nsteps))) return st;
   HC_CUDA(cudaEventCreate(&T->e0));
   HC_CUDA(cudaEventCreate(&T->e1));
   for (int k = snapshots - 1; k >= 0; --k) T->stack.push_back(k);
@@ -451,6 +457,8 @@ template <class R> int batch_reverse(hc_batch* b, double* const* q0_bar, bool on
     stats->ms_forward = ms_f;
     stats->ms_total = ms_t;
     stats->ms_recompute = A.recompute_ms();
+    stats->replays = A.replays;
+    stats->stage_tapes = (long long)A.tapes.size();
   }
   return HC_OK;
 }

@@ -22,6 +22,7 @@ struct hc_ctx {
   double lref = 1., sdt = 1.7976931348623157e308;  // species lref and dt (AUSM+up scaling)
   int vscale = 0, pscale = 0;                       // AUSM+up LowMachScaling pair
   unsigned fixes = 0;                               // HC_FIX_* corrections (hc_set_corrections)
+  int adj_tapes = -1;                               // adjoint stage tapes (hc_set_adjoint_tapes); -1 auto
   // the forward sweep recorded by hc_adjoint_record for hc_adjoint_reverse (owned here,
   // released by the reverse sweep, the next record, a mesh upload or destroy)
   void* adj_tape = nullptr;

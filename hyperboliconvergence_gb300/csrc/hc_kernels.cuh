@@ -194,6 +194,19 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
 
   // ---- phase 1: state tile with a 2-cell halo (periodic sides wrap)
+  // A tile whose halo lies inside the mesh needs no wrap, bounds or pair-face tests in
+  // phases 1-2 (uniform per block).  FP32 only: the FP64 stage is bound by its FP64 pipe
+  // and gains nothing from fewer integer instructions.  Same sums in the same order.
+  const bool interior = std::is_same<C, float>::value && i0 >= 2 && i0 + TI + 2 <= ni && j0 >= 2 && j0 + TJ + 2 <= nj;
+  if (interior) {
+    const R* qb = a.q + (size_t(i0 - 2) * nj + (j0 - 2));
+    for (int k = tid; k < QI * QJ; k += NT) {
+      const int la = k / QJ, lb = k % QJ;
+      const size_t c = size_t(la) * nj + lb;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sq[(v * QI + la) * QJ + lb] = cvt<C>(qb[v * ncell + c]);
+    }
+  } else
   for (int k = tid; k < QI * QJ; k += NT) {
     const int la = k / QJ, lb = k % QJ;
     int gi = i0 - 2 + la, gj = j0 - 2 + lb;
@@ -211,6 +224,35 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
 
   // ---- phase 2: qmetric of the tile cells and of the 1-cell halo strips
   // (lsq/qmetric.ipp via spatial/lsqMetrics.h:181-213; D2 periodic wrap)
+  if (interior) {
+    for (int k = tid; k < MI * MJ; k += NT) {
+      const int la = k / MJ - 1, lb = k % MJ - 1;
+      const bool corner = (la < 0 || la >= TI) && (lb < 0 || lb >= TJ);
+      const int gi = i0 + la, gj = j0 + lb;
+      C m[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) m[q] = C(0);
+      if (!corner) {
+        const int fi0 = gi * nj + gj, fj0 = gi * (nj + 1) + gj;
+        const C dxi0 = cfi[size_t(F_DXX) * nfi + fi0], dyi0 = cfi[size_t(F_DXY) * nfi + fi0];
+        const C dxi1 = cfi[size_t(F_DXX) * nfi + fi0 + nj], dyi1 = cfi[size_t(F_DXY) * nfi + fi0 + nj];
+        const C dxj0 = cfj[size_t(F_DXX) * nfj + fj0], dyj0 = cfj[size_t(F_DXY) * nfj + fj0];
+        const C dxj1 = cfj[size_t(F_DXX) * nfj + fj0 + 1], dyj1 = cfj[size_t(F_DXY) * nfj + fj0 + 1];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const C q0 = Q(v, la, lb);
+          const C a0 = q0 - Q(v, la - 1, lb), a1 = Q(v, la + 1, lb) - q0;
+          const C b0 = q0 - Q(v, la, lb - 1), b1 = Q(v, la, lb + 1) - q0;
+          m[2 * v] += a0 * dxi0; m[2 * v + 1] += a0 * dyi0;
+          m[2 * v] += a1 * dxi1; m[2 * v + 1] += a1 * dyi1;
+          m[2 * v] += b0 * dxj0; m[2 * v + 1] += b0 * dyj0;
+          m[2 * v] += b1 * dxj1; m[2 * v + 1] += b1 * dyj1;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) M(q, la, lb) = m[q];
+    }
+  } else
   for (int k = tid; k < MI * MJ; k += NT) {
     const int la = k / MJ - 1, lb = k % MJ - 1;
     const bool corner = (la < 0 || la >= TI) && (lb < 0 || lb >= TJ);

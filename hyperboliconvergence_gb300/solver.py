@@ -142,6 +142,12 @@ class Solver:
         self.corrections = _capi.fix_mask(corrections)
         check(self.lib.hc_set_corrections(self.h, self.corrections))
 
+    def set_adjoint_tapes(self, ntapes: int = -1) -> None:
+        """Stage tapes of the adjoint's checkpointing (hc_set_adjoint_tapes): -1 one per
+        snapshot and one more (no step's stages recomputed), 0 none (every reversed step
+        replays its stages from its start state), k at most k."""
+        check(self.lib.hc_set_adjoint_tapes(self.h, int(ntapes)))
+
     def set_low_mach(self, velocity="convective", pressure="convective", lref=1.0,
                      dt=np.finfo(np.float64).max) -> None:
         """AUSM+up's low-Mach scalings, AusmPlusUP<velocity, pressure> with "convective",

@@ -340,6 +340,8 @@ typedef struct {
   double ms_forward;         /* first forward sweep */
   double ms_total;           /* forward sweep + reverse sweep */
   double ms_recompute;       /* part of the reverse sweep spent re-advancing from checkpoints */
+  long long replays;         /* reversed steps whose stage states were recomputed (no stage tape) */
+  long long stage_tapes;     /* stage tapes allocated (hc_set_adjoint_tapes) */
 } hc_adjoint_stats;
 
 /* The pressure force on the inviscid-wall sides of the current state along dir (the
@@ -365,6 +367,15 @@ int hc_adjoint_gradient(hc_ctx* ctx, int nsteps, int snapshots, const hc_objecti
  * recording. */
 int hc_adjoint_record(hc_ctx* ctx, int nsteps, int snapshots, const hc_objective* obj, const double* rates_in,
                       double* rates_out, double* J);
+/* Stage tapes of the adjoint's checkpointing.  Reversing a step needs its stage states;
+ * without a tape they are recomputed from the step's start state (a replay of all stages
+ * but the last).  A stage tape keeps them (the start state and nst-1 stage states) from the
+ * forward sweep or the re-advance that computed the step last before its reversal: the
+ * last step of every re-advance and of the sweep's part before each stored checkpoint.
+ * -1 (default): snapshots + 1 tapes, enough that no step is replayed; 0: none (every step
+ * replayed, `snapshots` states the only storage); k: at most k live at once.  Each tape holds
+ * nst states of the mesh, allocated at record time.  Not in the reference (no adjoint). */
+int hc_set_adjoint_tapes(hc_ctx* ctx, int ntapes);
 int hc_adjoint_reverse(hc_ctx* ctx, double* q0_bar, double* ref_bar, int on_device, hc_adjoint_stats* stats);
 
 /* ---------------------------------------------------------------------------
@@ -462,6 +473,7 @@ int hc_batch_adjoint_gradient(hc_batch* b, int nsteps, int snapshots, const hc_o
 int hc_batch_adjoint_record(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj,
                             const double* const* targets, double* J);
 int hc_batch_adjoint_reverse(hc_batch* b, double* const* q0_bar, int on_device, hc_adjoint_stats* stats);
+int hc_batch_set_adjoint_tapes(hc_batch* b, int ntapes);  /* hc_set_adjoint_tapes for a batch */
 /* instance k's state from FP64 device memory (asynchronous on the batch's stream) */
 int hc_batch_state_upload_device(hc_batch* b, int inst, const double* prim_soa_device);
 
