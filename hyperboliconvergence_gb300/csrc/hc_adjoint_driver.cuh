@@ -271,63 +271,62 @@ __global__ void l2_kernel(const R* q, const R* t, size_t n, double w0, double w1
   l2_cell(q, t, n, w0, w1, w2, w3, part, mode_grad, lam, blockIdx.x * size_t(blockDim.x) + threadIdx.x, nv);
 }
 
-// residual adjoint: qbar_out = (dRes/dq at q)^T rbar (+ qbar_add); objective mode
-// uses only the wall faces with the drag weights instead of rbar
+// scalar-law residual adjoint: qbar_out = (dRes/dq at q)^T rbar (+ qbar_add)
 template <class R, int FK>
-int residual_adjoint(Adj<R>& A, const R* q, const R* rbar, const R* qbar_add, R* qbar_out, bool objective,
-                     double obj_scale) {
+int residual_adjoint_scalar(Adj<R>& A, const R* q, const R* rbar, const R* qbar_add, R* qbar_out) {
   AdjArgs<R> a = adj_args(A);
   a.q = q;
   a.rbar = rbar;
   a.qbar = qbar_out;
   a.qbar_add = qbar_add;
-  a.objective = objective ? 1 : 0;
-  a.obj_scale = R(obj_scale);
-  a.obj_dirx = R(A.obj.dir[0]);
-  a.obj_diry = R(A.obj.dir[1]);
-  if (A.c->scalar) {
-    if constexpr (FK == FLUX_RUSANOV || FK == FLUX_CENTRAL) {
-      adj_qm_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
-      adj_face_scalar_kernel<R, FK><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
-      adj_face_scalar_kernel<R, FK><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
-      adj_qmbar_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(a);
-      adj_gather_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(a);
-      A.launches += 5;
-      HC_CUDA(cudaGetLastError());
-    }
-    return HC_OK;
-  }
-  if constexpr (FK == FLUX_CENTRAL) return fail(HC_ERR_UNSUPPORTED, "the Euler adjoint has no central flux");
-  adj_qm_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
-  if constexpr (FK == FLUX_CENTRAL) {
-  } else if constexpr (FK == FLUX_BY_TANGENT) {
-    HC_CUDA(launch_adj_face_tangent<R>(A.c->cfg.flux, a, 0, face_blocks(A.nfi), kFaceThreads, A.s()));
-    HC_CUDA(launch_adj_face_tangent<R>(A.c->cfg.flux, a, 1, face_blocks(A.nfj), kFaceThreads, A.s()));
-  } else if constexpr (std::is_same<R, double>::value) {
-    if (A.c->df) {  // double-float face arithmetic on HC_FP64_DF contexts
-      adj_face_kernel<double, FK, df64><<<face_blocks(A.nfi), kFaceThreads, 0, A.s()>>>(a, 0);
-      adj_face_kernel<double, FK, df64><<<face_blocks(A.nfj), kFaceThreads, 0, A.s()>>>(a, 1);
-    } else {
-      adj_face_kernel<double, FK><<<face_blocks(A.nfi), kFaceThreads, 0, A.s()>>>(a, 0);
-      adj_face_kernel<double, FK><<<face_blocks(A.nfj), kFaceThreads, 0, A.s()>>>(a, 1);
-    }
-  } else {
-    adj_face_kernel<R, FK><<<face_blocks(A.nfi), kFaceThreads, 0, A.s()>>>(a, 0);
-    adj_face_kernel<R, FK><<<face_blocks(A.nfj), kFaceThreads, 0, A.s()>>>(a, 1);
-  }
-  adj_qmbar_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a);
-  adj_gather_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a);
+  adj_qm_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(a, A.qm);
+  adj_face_scalar_kernel<R, FK><<<blocks(A.nfi), 256, 0, A.s()>>>(a, 0);
+  adj_face_scalar_kernel<R, FK><<<blocks(A.nfj), 256, 0, A.s()>>>(a, 1);
+  adj_qmbar_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(a);
+  adj_gather_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(a);
   A.launches += 5;
   HC_CUDA(cudaGetLastError());
   return HC_OK;
 }
 
-template <class R> int res_adj(Adj<R>& A, const R* q, const R* rbar, const R* add, R* out, bool obj, double sc) {
-  if (A.c->scalar && A.c->cfg.flux == HC_FLUX_CENTRAL)
-    return residual_adjoint<R, FLUX_CENTRAL>(A, q, rbar, add, out, obj, sc);
-  if (A.c->cfg.flux == HC_FLUX_ROE) return residual_adjoint<R, FLUX_ROE>(A, q, rbar, add, out, obj, sc);
-  if (flux_by_tangent(A.c->cfg.flux)) return residual_adjoint<R, FLUX_BY_TANGENT>(A, q, rbar, add, out, obj, sc);
-  return residual_adjoint<R, FLUX_RUSANOV>(A, q, rbar, add, out, obj, sc);
+template <class R> int res_adj_scalar(Adj<R>& A, const R* q, const R* rbar, const R* add, R* out) {
+  if (A.c->cfg.flux == HC_FLUX_CENTRAL) return residual_adjoint_scalar<R, FLUX_CENTRAL>(A, q, rbar, add, out);
+  return residual_adjoint_scalar<R, FLUX_RUSANOV>(A, q, rbar, add, out);
+}
+
+// Euler face pass (pass 1) of the stage state a.q with residual adjoint a.rbar: both
+// directions in one launch
+template <class R> int euler_faces(Adj<R>& A, const AdjArgs<R>& a) {
+  const int nbi = int(face_blocks(A.nfi));
+  const unsigned nb = face_blocks(A.nfi) + face_blocks(A.nfj);
+  const int flux = A.c->cfg.flux;
+  if (flux_by_tangent(flux)) {
+    HC_CUDA(launch_adj_face_tangent<R>(flux, a, nbi, nb, kFaceThreads, A.s()));
+  } else if (flux == HC_FLUX_ROE) {
+    if constexpr (std::is_same<R, double>::value) {
+      if (A.c->df) adj_face_kernel<double, FLUX_ROE, df64><<<nb, kFaceThreads, 0, A.s()>>>(a, nbi);
+      else adj_face_kernel<double, FLUX_ROE><<<nb, kFaceThreads, 0, A.s()>>>(a, nbi);
+    } else {
+      adj_face_kernel<R, FLUX_ROE><<<nb, kFaceThreads, 0, A.s()>>>(a, nbi);
+    }
+  } else {
+    if constexpr (std::is_same<R, double>::value) {
+      if (A.c->df) adj_face_kernel<double, FLUX_RUSANOV, df64><<<nb, kFaceThreads, 0, A.s()>>>(a, nbi);
+      else adj_face_kernel<double, FLUX_RUSANOV><<<nb, kFaceThreads, 0, A.s()>>>(a, nbi);
+    } else {
+      adj_face_kernel<R, FLUX_RUSANOV><<<nb, kFaceThreads, 0, A.s()>>>(a, nbi);
+    }
+  }
+  A.launches += 1;
+  HC_CUDA(cudaGetLastError());
+  return HC_OK;
+}
+
+// the arguments of the drag objective's adjoint (J scaled by scale)
+template <class R> void drag_args(Adj<R>& A, AdjArgs<R>& a, double scale) {
+  a.obj_scale = R(scale);
+  a.obj_dirx = R(A.obj.dir[0]);
+  a.obj_diry = R(A.obj.dir[1]);
 }
 
 template <class R> double step_dt(const Adj<R>& A, int step) {
@@ -337,6 +336,11 @@ template <class R> double step_dt(const Adj<R>& A, int step) {
 
 // lam holds the adjoint of q_{step+1}; sq[0] holds q_step.  On return lam holds
 // the adjoint of q_step (objective terms of q_step included).
+// Euler: per stage s (last first) three launches -- faces of stage s, its qmetric
+// adjoint, and the fused cell pass (gather of stage s, update reverse of stage s-1,
+// qmetric of stage s-1's state; at s = 0 the gather with the update adjoints of q_step
+// and the drag objective into lam) -- after one cell pass that reverses the last
+// stage's update.
 template <class R> int adjoint_step(Adj<R>& A, int step) {
   // the step's stage states from its tape, or a replay of its stages but the last (its
   // output q_{step+1} is the start state of the step reversed before this one, kept in qnext)
@@ -348,26 +352,66 @@ template <class R> int adjoint_step(Adj<R>& A, int step) {
   HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
   const double dt = step_dt(A, step);
   const Gas<R> g = with_fixes(make_gas<R>(A.c->gamma, A.c->Rgas, A.c->minf), A.c->fixes);
-  for (int s = A.nst - 1; s >= 0; --s) {
-    const R* qbar_out = (s == A.nst - 1) ? A.lam : A.qbs;
-    R al[4] = {R(0), R(0), R(0), R(0)};
-    for (int k = 0; k <= s; ++k) al[k] = R(A.tab.alpha[s][k]);
-    if (A.c->scalar)
+  if (A.c->scalar) {
+    for (int s = A.nst - 1; s >= 0; --s) {
+      const R* qbar_out = (s == A.nst - 1) ? A.lam : A.qbs;
+      R al[4] = {R(0), R(0), R(0), R(0)};
+      for (int k = 0; k <= s; ++k) al[k] = R(A.tab.alpha[s][k]);
       adj_update_lin_kernel<R, 3><<<blocks(A.n), 256, 0, A.s()>>>(
           int(A.n), (const R*)A.c->vol, qbar_out, A.q0bar, A.rbar[0], A.rbar[1], A.rbar[2], A.rbar[3], al[0],
           al[1], al[2], al[3], s, R(A.tab.beta[s] * dt));
-    else
-      adj_update_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(
-          int(A.n), g, A.sq[s + 1], A.sq[0], (const R*)A.c->vol, qbar_out, A.q0bar, A.rbar[0], A.rbar[1],
-          A.rbar[2], A.rbar[3], al[0], al[1], al[2], al[3], s, R(A.tab.beta[s] * dt));
-    A.launches += 1;
-    HC_CUDA(cudaGetLastError());
-    if (int st = res_adj<R>(A, A.sq[s], A.rbar[s], s == 0 ? A.q0bar : nullptr, A.qbs, false, 0.0)) return st;
-  }
-  if (A.obj.kind == HC_OBJ_DRAG && step >= 1) {
-    if (int st = res_adj<R>(A, A.sq[0], nullptr, A.qbs, A.lam, true, A.obj.scale / A.nsteps)) return st;
-  } else {
+      A.launches += 1;
+      HC_CUDA(cudaGetLastError());
+      if (int st = res_adj_scalar<R>(A, A.sq[s], A.rbar[s], s == 0 ? A.q0bar : nullptr, A.qbs)) return st;
+    }
     HC_CUDA(cudaMemcpyAsync(A.lam, A.qbs, bytes4, cudaMemcpyDeviceToDevice, A.s()));
+    A.adj_steps += 1;
+    return HC_OK;
+  }
+  AdjArgs<R> a = adj_args(A);
+  drag_args(A, a, A.obj.scale / A.nsteps);
+  const unsigned cb = blocks(A.n);
+  // update reverse of stage s with the state adjoint qb of its output
+  auto update = [&](AdjCellArgs<R>& u, int s) {
+    u.update = 1;
+    u.g = g;
+    u.q_out = A.sq[s + 1];
+    u.q0 = A.sq[0];
+    u.vol = (const R*)A.c->vol;
+    u.q0bar = A.q0bar;
+    for (int k = 0; k < 4; ++k) {
+      u.rbar[k] = A.rbar[k];
+      u.alpha[k] = k <= s ? R(A.tab.alpha[s][k]) : R(0);
+    }
+    u.stage = s;
+    u.dts = R(A.tab.beta[s] * dt);
+  };
+  {
+    AdjCellArgs<R> u{};
+    u.qbar_in = A.lam;
+    update(u, A.nst - 1);
+    u.qm_q = A.sq[A.nst - 1];
+    adj_cell_kernel<R><<<cb, 256, 0, A.s()>>>(a, u);
+    A.launches += 1;
+  }
+  for (int s = A.nst - 1; s >= 0; --s) {
+    a.q = A.sq[s];
+    a.rbar = A.rbar[s];
+    a.qbar_add = s == 0 ? A.q0bar : nullptr;
+    if (int st = euler_faces(A, a)) return st;
+    adj_qmbar_kernel<R><<<cb, 256, 0, A.s()>>>(a);
+    AdjCellArgs<R> u{};
+    u.gather = 1;
+    if (s > 0) {
+      update(u, s - 1);
+      u.qm_q = A.sq[s - 1];
+    } else {
+      u.qbar_out = A.lam;
+      u.drag = A.obj.kind == HC_OBJ_DRAG && step >= 1;
+    }
+    adj_cell_kernel<R><<<cb, 256, 0, A.s()>>>(a, u);
+    A.launches += 2;
+    HC_CUDA(cudaGetLastError());
   }
   A.adj_steps += 1;
   return HC_OK;
@@ -780,7 +824,14 @@ int adjoint_reverse(hc_ctx* c, double* q0_bar, double* ref_bar, bool on_device, 
   HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], A.state_values() * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
   // adjoint of the final state
   if (A.obj.kind == HC_OBJ_DRAG) {
-    if (int st = res_adj<R>(A, A.sq[0], nullptr, nullptr, A.lam, true, A.obj.scale / A.nsteps)) return st;
+    AdjArgs<R> a = adj_args(A);
+    drag_args(A, a, A.obj.scale / A.nsteps);
+    AdjCellArgs<R> u{};
+    u.drag = 1;
+    u.qbar_out = A.lam;
+    adj_cell_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(a, u);
+    HC_CUDA(cudaGetLastError());
+    A.launches += 1;
   } else {
     l2_kernel<R><<<blocks(A.n), 256, 0, A.s()>>>(A.sq[0], A.target, A.n, A.obj.weight[0], A.obj.weight[1],
                                                   A.obj.weight[2], A.obj.weight[3], nullptr, 1, A.lam, A.nv);

@@ -45,13 +45,13 @@ template <class R> struct AdjArgs {
   R* qmbar;          // 8 planes
   R* qbar;           // output 4 planes
   const R* qbar_add; // optional: added to qbar (4 planes) or null
-  int objective;     // 1: only wall faces, F_bar = -(+/-) scale * (dirx, diry, 0, 0)
-  R obj_scale, obj_dirx, obj_diry;
+  R obj_scale, obj_dirx, obj_diry;  // drag objective: J = obj_scale * wall force along (dirx, diry)
 };
 
 // qmetric of cell c (phase 2 of the stage kernel, without tiling); NV variables
 // (4 Euler, 3 scalar advection), 2 NV planes
-template <class R, int NV = 4> __device__ __forceinline__ void adj_qm_cell(const AdjArgs<R>& a, R* qm, int c) {
+template <class R, int NV = 4>
+__device__ __forceinline__ void adj_qm_cell(const AdjArgs<R>& a, const R* __restrict__ q, R* qm, int c) {
   const int ni = a.ni, nj = a.nj;
   if (c >= ni * nj) return;
   const int gi = c / nj, gj = c % nj;
@@ -84,7 +84,7 @@ template <class R, int NV = 4> __device__ __forceinline__ void adj_qm_cell(const
     const R dx = rec[size_t(F_DXX) * nf + fidx], dy = rec[size_t(F_DXY) * nf + fidx];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const R dq = hi ? (a.q[v * n + nb] - a.q[v * n + c]) : (a.q[v * n + c] - a.q[v * n + nb]);
+      const R dq = hi ? (q[v * n + nb] - q[v * n + c]) : (q[v * n + c] - q[v * n + nb]);
       m[2 * v] += dq * dx;
       m[2 * v + 1] += dq * dy;
     }
@@ -93,7 +93,7 @@ template <class R, int NV = 4> __device__ __forceinline__ void adj_qm_cell(const
   for (int k = 0; k < 2 * NV; ++k) qm[k * n + c] = m[k];
 }
 template <class R, int NV = 4> __global__ void adj_qm_kernel(const AdjArgs<R> a, R* qm) {
-  adj_qm_cell<R, NV>(a, qm, int(blockIdx.x * blockDim.x + threadIdx.x));
+  adj_qm_cell<R, NV>(a, a.q, qm, int(blockIdx.x * blockDim.x + threadIdx.x));
 }
 
 template <class R, int FK>
@@ -130,7 +130,7 @@ __device__ __forceinline__ void adj_face_one(const AdjArgs<R>& a, int dir, int f
   const Gas<C> g = gas_as<C>(a.gas);
   const int lim = a.limiter;
   if (!bnd) {
-    if (!a.objective) {
+    {
       // left/right cells (periodic wrap on the boundary lines)
       int cl, cr;
       if (idir) { cl = wrapi(i - 1, ni) * nj + j; cr = wrapi(i, ni) * nj + j; }
@@ -215,20 +215,14 @@ __device__ __forceinline__ void adj_face_one(const AdjArgs<R>& a, int dir, int f
     C* gI = int_right ? gR : gL;
     if (bct == BC_WALL) {
       C Fb[4];
-      if (a.objective) {
-        const C sgn_in = int_right ? C(1) : C(-1);
-        Fb[0] = -sgn_in * C(a.obj_scale) * C(a.obj_dirx);
-        Fb[1] = -sgn_in * C(a.obj_scale) * C(a.obj_diry);
-      } else {
 #pragma unroll
-        for (int v = 0; v < 2; ++v) Fb[v] = int_right ? a.rbar[v * n + ci] : -a.rbar[v * n + ci];
-      }
+      for (int v = 0; v < 2; ++v) Fb[v] = int_right ? a.rbar[v * n + ci] : -a.rbar[v * n + ci];
       const C wx = int_right ? rd(F_WLX) : rd(F_WRX), wy = int_right ? rd(F_WLY) : rd(F_WRY);
       (void)wx; (void)wy;
       const C pb = A * (nx * Fb[0] + ny * Fb[1]);
       dI[3] += pb;
       gI[3] = -pb;  // pass 2 pairs it with the wall extrapolation weights
-    } else if (!a.objective) {
+    } else {
       C Fb[4], qg[4];
       R qref[4];
 #pragma unroll
@@ -297,8 +291,11 @@ __device__ __forceinline__ void adj_face_one(const AdjArgs<R>& a, int dir, int f
 #pragma unroll
   for (int k = 0; k < ADJ_FIELDS; ++k) out[size_t(k) * nf + f] = cvt<R>(res[k]);
 }
-template <class R, int FK, class C = R> __global__ void adj_face_kernel(const AdjArgs<R> a, int dir) {
-  adj_face_one<R, FK, C>(a, dir, int(blockIdx.x * blockDim.x + threadIdx.x));
+// both face directions in one launch: i-faces in blocks [0, nbi), j-faces in the rest
+template <class R, int FK, class C = R> __global__ void adj_face_kernel(const AdjArgs<R> a, int nbi) {
+  const int b = int(blockIdx.x);
+  const int dir = b < nbi ? 0 : 1;
+  adj_face_one<R, FK, C>(a, dir, (dir ? b - nbi : b) * int(blockDim.x) + int(threadIdx.x));
 }
 
 // ---- scalar advection law (conserved set {u, v, q}; scalar_face_flux, hc_scalar.cuh)
@@ -548,15 +545,14 @@ template <class R, int NV = 4> __global__ void adj_qmbar_kernel(const AdjArgs<R>
   adj_qmbar_cell<R, NV>(a, int(blockIdx.x * blockDim.x + threadIdx.x));
 }
 
-// pass 3: gather the state adjoint of cell c (NV variables)
-template <class R, int NV = 4> __device__ __forceinline__ void adj_gather_cell(const AdjArgs<R>& a, int c) {
+// pass 3: gather the state adjoint of cell c (NV variables) into qb
+template <class R, int NV>
+__device__ __forceinline__ void adj_gather_vals(const AdjArgs<R>& a, int c, R* qb) {
   const int ni = a.ni, nj = a.nj;
-  if (c >= ni * nj) return;
   const int gi = c / nj, gj = c % nj;
   const size_t n = size_t(ni) * nj;
   const int nfi = (ni + 1) * nj, nfj = ni * (nj + 1);
   const bool per_i = a.bc[0] == BC_PERIODIC, per_j = a.bc[2] == BC_PERIODIC;
-  R qb[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) qb[v] = a.qbar_add ? a.qbar_add[v * n + c] : R(0);
 #pragma unroll
@@ -580,6 +576,12 @@ template <class R, int NV = 4> __device__ __forceinline__ void adj_gather_cell(c
       qb[v] += sg * ((a.qmbar[(2 * v) * n + c] + a.qmbar[(2 * v) * n + nb]) * dx +
                      (a.qmbar[(2 * v + 1) * n + c] + a.qmbar[(2 * v + 1) * n + nb]) * dy);
   }
+}
+template <class R, int NV = 4> __device__ __forceinline__ void adj_gather_cell(const AdjArgs<R>& a, int c) {
+  if (c >= a.ni * a.nj) return;
+  const size_t n = size_t(a.ni) * a.nj;
+  R qb[NV];
+  adj_gather_vals<R, NV>(a, c, qb);
 #pragma unroll
   for (int v = 0; v < NV; ++v) a.qbar[v * n + c] = qb[v];
 }
@@ -620,6 +622,135 @@ __global__ void adj_update_kernel(int ncell, Gas<R> g, const R* __restrict__ q_o
                                   int stage, R dts) {
   adj_update_cell(ncell, g, q_out, q0, vol, qbar_out, q0bar, rbar0, rbar1, rbar2, rbar3, alpha0, alpha1, alpha2,
                   alpha3, stage, dts, int(blockIdx.x * blockDim.x + threadIdx.x));
+}
+
+// ---- the drag objective's adjoint
+// J = obj_scale * sum over wall faces of -sgn_in A p_wall (n . dir), p_wall = p_c - QM_c(p) . w
+// (the wall pressure extrapolated with the cell's LSQ gradient, inviscidWall.ipp:33-72).
+// Per wall face: pb = A (n . Fb), Fb = -sgn_in obj_scale dir; p_c takes pb directly and
+// the cell's pressure qmetric adjoint -pb w, which the gather spreads over the cell and
+// its pair neighbours.  wall_pb: pb and w of wall face k of `side`.
+template <class R>
+__device__ __forceinline__ void wall_pb(const AdjArgs<R>& a, int side, int k, R& pb, R& wx, R& wy) {
+  const bool idir = side < 2, int_right = side == 0 || side == 2;
+  const int ni = a.ni, nj = a.nj;
+  const int nf = idir ? (ni + 1) * nj : ni * (nj + 1);
+  const int fidx = idir ? (side == 0 ? 0 : ni) * nj + k : k * (nj + 1) + (side == 2 ? 0 : nj);
+  const R* rec = idir ? a.fi : a.fj;
+  const R nx = rec[size_t(F_NX) * nf + fidx], ny = rec[size_t(F_NY) * nf + fidx], A = rec[size_t(F_A) * nf + fidx];
+  const R sgn_in = int_right ? R(1) : R(-1);
+  const R fb0 = -sgn_in * a.obj_scale * a.obj_dirx, fb1 = -sgn_in * a.obj_scale * a.obj_diry;
+  pb = A * (nx * fb0 + ny * fb1);
+  wx = rec[size_t(int_right ? F_WLX : F_WRX) * nf + fidx];
+  wy = rec[size_t(int_right ? F_WLY : F_WRY) * nf + fidx];
+}
+// the pressure qmetric adjoint (m6, m7) of cell (ci, cj) from its wall faces; false: none
+template <class R> __device__ __forceinline__ bool drag_qmbar(const AdjArgs<R>& a, int ci, int cj, R& m6, R& m7) {
+  bool any = false;
+  m6 = m7 = R(0);
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    const int side = f;  // face order of the qmetric: i-lo, i-hi, j-lo, j-hi = sides 0..3
+    const bool on = side == 0 ? ci == 0 : side == 1 ? ci == a.ni - 1 : side == 2 ? cj == 0 : cj == a.nj - 1;
+    if (!on || a.bc[side] != BC_WALL) continue;
+    R pb, wx, wy;
+    wall_pb(a, side, side < 2 ? cj : ci, pb, wx, wy);
+    m6 += -pb * wx;
+    m7 += -pb * wy;
+    any = true;
+  }
+  return any;
+}
+// the drag adjoint of cell c's pressure: its wall faces' pb and the pair-face spread of
+// the pressure qmetric adjoints of c and its neighbours (zero away from the walls)
+template <class R> __device__ __forceinline__ R drag_cell(const AdjArgs<R>& a, int c) {
+  const int ni = a.ni, nj = a.nj;
+  const int gi = c / nj, gj = c % nj;
+  const bool per_i = a.bc[0] == BC_PERIODIC, per_j = a.bc[2] == BC_PERIODIC;
+  R out = R(0);
+  R m6c, m7c;
+  const bool mc = drag_qmbar(a, gi, gj, m6c, m7c);
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    const bool idir = f < 2;
+    const int hi = f & 1;
+    const int lo = idir ? gi + hi : gj + hi;
+    const int nalong = idir ? ni : nj;
+    const int side = idir ? (lo == 0 ? 0 : 1) : (lo == 0 ? 2 : 3);
+    if ((lo == 0 || lo == nalong) && a.bc[side] == BC_WALL) {
+      R pb, wx, wy;
+      wall_pb(a, side, idir ? gj : gi, pb, wx, wy);
+      out += pb;
+    }
+    const bool pair = idir ? ((lo > 0 && lo < ni) || per_i) : ((lo > 0 && lo < nj) || per_j);
+    if (!pair) continue;
+    const int ni_ = idir ? wrapi(gi + (hi ? 1 : -1), ni) : gi, nj_ = idir ? gj : wrapi(gj + (hi ? 1 : -1), nj);
+    R m6n, m7n;
+    const bool mn = drag_qmbar(a, ni_, nj_, m6n, m7n);
+    if (!mc && !mn) continue;
+    const int nf = idir ? (ni + 1) * nj : ni * (nj + 1);
+    const int fidx = idir ? lo * nj + gj : gi * (nj + 1) + lo;
+    const R* rec = idir ? a.fi : a.fj;
+    const R dx = rec[size_t(F_DXX) * nf + fidx], dy = rec[size_t(F_DXY) * nf + fidx];
+    const R sg = hi ? R(-1) : R(1);
+    out += sg * ((m6c + m6n) * dx + (m7c + m7n) * dy);
+  }
+  return out;
+}
+
+// ---- the fused cell pass of the Euler reverse (single mesh): per cell,
+//   qb = gather of the face adjoints (pass 3, qbar_add included) | qbar_in | 0
+//   qb.p += the drag objective's adjoint (drag)
+//   update: the RK update of the stage before reversed with qbar_out = qb; else qb -> qbar_out
+//   qm_q: the qmetric of that stage's state for the next face pass
+// so that a stage's reverse is three launches: faces, qmetric adjoint, this pass.
+template <class R> struct AdjCellArgs {
+  int gather, drag, update;
+  const R* qbar_in;
+  R* qbar_out;
+  Gas<R> g;
+  const R* q_out;
+  const R* q0;
+  const R* vol;
+  R* q0bar;
+  R* rbar[4];
+  R alpha[4];
+  int stage;
+  R dts;
+  const R* qm_q;
+};
+template <class R> __global__ void adj_cell_kernel(const AdjArgs<R> a, const AdjCellArgs<R> u) {
+  const int c = int(blockIdx.x * blockDim.x + threadIdx.x);
+  const int ncell = a.ni * a.nj;
+  if (c >= ncell) return;
+  const size_t n = size_t(ncell);
+  R qb[4];
+  if (u.gather) {
+    adj_gather_vals<R, 4>(a, c, qb);
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) qb[v] = u.qbar_in ? u.qbar_in[v * n + c] : R(0);
+  }
+  if (u.drag) qb[3] += drag_cell(a, c);
+  if (u.update) {
+    R q[4], qz[4], cb[4], z[4] = {R(0), R(0), R(0), R(0)};
+#pragma unroll
+    for (int v = 0; v < 4; ++v) { q[v] = u.q_out[v * n + c]; qz[v] = u.q0[v * n + c]; }
+    cons2prim_adj(u.g, q, qb, cb);
+    prim2cons_adj(u.g, qz, cb, z);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) u.q0bar[v * n + c] += z[v];
+    const R fac = u.dts / u.vol[c];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k <= u.stage)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) u.rbar[k][v * n + c] += u.alpha[k] * cb[v] * fac;
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) u.qbar_out[v * n + c] = qb[v];
+  }
+  if (u.qm_q) adj_qm_cell<R, 4>(a, u.qm_q, const_cast<R*>(a.qm), c);
 }
 
 // Drag of the wall faces of the state q (force on the body along (dirx, diry)
@@ -704,7 +835,6 @@ template <class R> __device__ __forceinline__ void batch_adj_args(const AdjBatch
   a.qmbar = b.qmbar + c8;
   a.qbar = b.qbar ? b.qbar + c4 : nullptr;
   a.qbar_add = b.qbar_add ? b.qbar_add + c4 : nullptr;
-  a.objective = 0;
   a.obj_scale = a.obj_dirx = a.obj_diry = R(0);
 }
 
@@ -730,7 +860,7 @@ template <class R> __device__ __forceinline__ void adj_block_setup(const AdjBatc
 template <class R, int NV = 4> __global__ void adj_qm_batch_kernel(const AdjBatchArgs<R> b) {
   __shared__ AdjBlock<R> sb;
   adj_block_setup(b, 1, sb);
-  adj_qm_cell<R, NV>(sb.a, const_cast<R*>(sb.a.qm), sb.local * int(blockDim.x) + int(threadIdx.x));
+  adj_qm_cell<R, NV>(sb.a, sb.a.q, const_cast<R*>(sb.a.qm), sb.local * int(blockDim.x) + int(threadIdx.x));
 }
 template <class R, int FK, class C = R> __global__ void adj_face_batch_kernel(const AdjBatchArgs<R> b) {
   __shared__ AdjBlock<R> sb;
@@ -782,9 +912,10 @@ template <class R> __global__ void adj_update_batch_kernel(const AdjUpdateBatch<
                   u.alpha[3], u.stage, R(u.beta * dt), c);
 }
 // Face passes of the Euler fluxes reversed by tangents (flux SLAU, SLAU as written,
-// AUSM+up or RoeUnprecWS), compiled in their own unit (hc_adjoint_tangent.cu)
+// AUSM+up, RoeUnprecWS or the face-frame Roe), compiled in their own unit
+// (hc_adjoint_tangent.cu); both directions in one launch, i-faces in blocks [0, nbi)
 template <class R>
-cudaError_t launch_adj_face_tangent(int flux, const AdjArgs<R>& a, int dir, unsigned blocks, int threads,
+cudaError_t launch_adj_face_tangent(int flux, const AdjArgs<R>& a, int nbi, unsigned blocks, int threads,
                                     cudaStream_t s);
 template <class R>
 cudaError_t launch_adj_face_tangent_batch(int flux, const AdjBatchArgs<R>& b, unsigned blocks, int threads,

@@ -8,8 +8,8 @@ namespace hc {
 
 namespace {
 template <class R, int FK>
-void face_one(const AdjArgs<R>& a, int dir, unsigned blocks, int threads, cudaStream_t s) {
-  adj_face_kernel<R, FK><<<blocks, threads, 0, s>>>(a, dir);
+void face_one(const AdjArgs<R>& a, int nbi, unsigned blocks, int threads, cudaStream_t s) {
+  adj_face_kernel<R, FK><<<blocks, threads, 0, s>>>(a, nbi);
 }
 template <class R, int FK>
 void face_batch(const AdjBatchArgs<R>& b, unsigned blocks, int threads, cudaStream_t s) {
@@ -18,14 +18,14 @@ void face_batch(const AdjBatchArgs<R>& b, unsigned blocks, int threads, cudaStre
 }  // namespace
 
 template <class R>
-cudaError_t launch_adj_face_tangent(int flux, const AdjArgs<R>& a, int dir, unsigned blocks, int threads,
+cudaError_t launch_adj_face_tangent(int flux, const AdjArgs<R>& a, int nbi, unsigned blocks, int threads,
                                     cudaStream_t s) {
   switch (flux) {
-    case FLUX_SLAU: face_one<R, FLUX_SLAU>(a, dir, blocks, threads, s); break;
-    case FLUX_SLAU_REF: face_one<R, FLUX_SLAU_REF>(a, dir, blocks, threads, s); break;
-    case FLUX_AUSMPUP: face_one<R, FLUX_AUSMPUP>(a, dir, blocks, threads, s); break;
-    case FLUX_ROE_WS: face_one<R, FLUX_ROE_WS>(a, dir, blocks, threads, s); break;
-    case FLUX_ROE_FACE: face_one<R, FLUX_ROE_FACE>(a, dir, blocks, threads, s); break;
+    case FLUX_SLAU: face_one<R, FLUX_SLAU>(a, nbi, blocks, threads, s); break;
+    case FLUX_SLAU_REF: face_one<R, FLUX_SLAU_REF>(a, nbi, blocks, threads, s); break;
+    case FLUX_AUSMPUP: face_one<R, FLUX_AUSMPUP>(a, nbi, blocks, threads, s); break;
+    case FLUX_ROE_WS: face_one<R, FLUX_ROE_WS>(a, nbi, blocks, threads, s); break;
+    case FLUX_ROE_FACE: face_one<R, FLUX_ROE_FACE>(a, nbi, blocks, threads, s); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
