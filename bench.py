@@ -658,6 +658,36 @@ def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int =
     bt = Batch(insts, precision="fp32", **kw)
     J, grads, st = bt.gradient(nsteps, targets, snapshots=snapshots, want=[kmin])
     wall = time.perf_counter() - t0
+    # the same batch through the torch.autograd.Function: per-instance J from CUDA tensors,
+    # loss.backward() one batched reverse sweep from the forward's checkpoints
+    import torch
+    from hyperboliconvergence_gb300.autograd import batch_l2_objective
+    q0s = [torch.tensor(q, dtype=torch.float64, device="cuda", requires_grad=True) for (_, _, _, q) in insts]
+    tgs = [torch.tensor(t, dtype=torch.float64, device="cuda") for t in targets]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    first_ms = None
+    for rep in range(2):  # the first call carries torch's one-time costs; the second is timed
+        for q in q0s:
+            q.grad = None
+        torch.cuda.synchronize()
+        ev[0].record()
+        Jt = batch_l2_objective(bt, q0s, tgs, nsteps, snapshots=snapshots)
+        ev[1].record()
+        Jt.sum().backward()
+        ev[2].record()
+        torch.cuda.synchronize()
+        if rep == 0:
+            first_ms = ev[0].elapsed_time(ev[2])
+    fst = bt.last_stats
+    fn = {"forward_ms": ev[0].elapsed_time(ev[1]), "backward_ms": ev[1].elapsed_time(ev[2]),
+          "library_reverse_ms": fst.ms_total - fst.ms_forward, "library_forward_ms": fst.ms_forward,
+          "library_reverse_sweep_ms": fst.ms_reverse, "one_call_reverse_sweep_ms": st.ms_reverse,
+          "replays": int(fst.replays), "stage_tapes": int(fst.stage_tapes),
+          "first_call_total_ms": first_ms,
+          "J_equal_one_call": bool(np.array_equal(Jt.detach().cpu().numpy(), J)),
+          "grad_equal_one_call": bool(np.array_equal(q0s[kmin].grad.cpu().numpy(), grads[kmin]))}
+    fn["backward_over_forward"] = fn["backward_ms"] / fn["forward_ms"]
+    del q0s, tgs, Jt
     bt.close()
     if not np.all(np.isfinite(J)) or not np.all(np.isfinite(grads[kmin])):
         raise RuntimeError("non-finite objective or gradient")
@@ -688,6 +718,8 @@ def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int =
             "recompute_ms": st.ms_recompute, "kernel_launches": int(st.kernel_launches),
             "forward_cell_updates_per_s": cells * nsteps / (fwd_ms / 1e3),
             "adjoint_step_over_forward_step": rev_ms / fwd_ms,
+            "replays": int(st.replays), "stage_tapes": int(st.stage_tapes),
+            "through_autograd_function": fn,
             "fp64_check": {"instance": kmin, "cells": sizes[kmin] ** 2,
                            "J_rel_diff": abs(float(J[kmin]) - j64) / abs(j64),
                            "grad_max_rel_diff": float(np.abs(g32 - g64).max() / np.abs(g64).max())},

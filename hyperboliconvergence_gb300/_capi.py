@@ -206,7 +206,8 @@ class SteadyStats(C.Structure):
 class AdjointStats(C.Structure):
     _fields_ = [("J", C.c_double), ("forward_steps", C.c_longlong), ("adjoint_steps", C.c_longlong),
                 ("kernel_launches", C.c_longlong), ("ms_forward", C.c_double), ("ms_total", C.c_double),
-                ("ms_recompute", C.c_double), ("replays", C.c_longlong), ("stage_tapes", C.c_longlong)]
+                ("ms_recompute", C.c_double), ("replays", C.c_longlong), ("stage_tapes", C.c_longlong),
+                ("ms_reverse", C.c_double)]
 
 
 OBJECTIVE = {"drag": 0, "l2": 1}

@@ -36,12 +36,13 @@ def _wait_for_torch(t: torch.Tensor) -> None:
 class _RunObjective(torch.autograd.Function):
     @staticmethod
     def forward(ctx, q0, solver: Solver, nsteps: int, snapshots: int, kind: str, kw: dict, *refs):
-        _wait_for_torch(q0)
         refn = [None if r is None else r.detach().to("cpu", torch.float64).numpy() for r in refs]
         solver.set_bcs(solver.bc, refn)
         if q0.is_cuda:
             dtype = torch.float32 if solver.precision == "fp32" else torch.float64
-            solver.upload_device(q0.detach().to(dtype).contiguous())
+            q = q0.detach().to(dtype).contiguous()
+            _wait_for_torch(q)  # the conversion runs on torch's stream, the upload on the library's
+            solver.upload_device(q)
         else:
             solver.set_state(q0.detach().to(torch.float64).numpy())
         J, rates = solver.record(nsteps, snapshots, kind=kind, **kw)
@@ -58,6 +59,7 @@ class _RunObjective(torch.autograd.Function):
         q0b = torch.empty((nv, m.ni, m.nj), dtype=torch.float64, device="cuda")
         nref = sum(nv * m.nface(side) for side in range(4))
         refb = torch.empty(max(nref, 1), dtype=torch.float64, device="cuda")
+        _wait_for_torch(refb)  # torch's earlier work on these blocks, before the library writes them
         s.reverse(q0b, refb)
         g = gJ.detach().to(device="cuda", dtype=torch.float64)
         dev, dt = ctx.q0_meta
@@ -83,12 +85,13 @@ def run_objective(solver: Solver, q0: torch.Tensor, refs, nsteps: int, snapshots
 class _BatchL2(torch.autograd.Function):
     @staticmethod
     def forward(ctx, batch, nsteps: int, snapshots: int, weight, targets, *q0s):
-        for q in q0s:
-            _wait_for_torch(q)
-        for k, q in enumerate(q0s):
-            batch.upload_device(k, q.detach().to(device="cuda", dtype=torch.float64).contiguous())
+        qs = [q.detach().to(device="cuda", dtype=torch.float64).contiguous() for q in q0s]
         tg = [t.detach().to(device="cuda", dtype=torch.float64).contiguous() if torch.is_tensor(t)
               else torch.from_numpy(np.ascontiguousarray(t, dtype=np.float64)).cuda() for t in targets]
+        # the conversions run on torch's stream, the uploads and the sweep on the library's
+        torch.cuda.current_stream().synchronize()
+        for k, q in enumerate(qs):
+            batch.upload_device(k, q)
         J = batch.record(nsteps, tg, snapshots, weight)
         ctx.batch = batch
         ctx.meta = [(tuple(q.shape), q.device, q.dtype) for q in q0s]
@@ -97,6 +100,7 @@ class _BatchL2(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gJ):
         outs = [torch.empty(shape, dtype=torch.float64, device="cuda") for shape, _, _ in ctx.meta]
+        torch.cuda.current_stream().synchronize()
         ctx.batch.reverse(outs)
         g = gJ.detach().to(device="cuda", dtype=torch.float64)
         grads = [(o * g[k]).to(device=dev, dtype=dt) for k, (o, (_, dev, dt)) in enumerate(zip(outs, ctx.meta))]

@@ -211,6 +211,7 @@ class Batch:
         st = AdjointStats()
         check(self.lib.hc_batch_adjoint_reverse(self.h, gptr, 0 if out is None else 1, C.byref(st)))
         self._tape_targets = None
+        self.last_stats = st
         return host, st
 
 

@@ -205,7 +205,16 @@ template <class AD> int stage_states(AD& A, int step) {
   A.tapes[k].step = -1;
   return HC_OK;
 }
-template <class AD> int alloc_tapes(AD& A, int ntapes) {
+// ntapes < 0: snapshots + 1 tapes (none replayed), as many of them as fit in half the
+// free device memory
+template <class AD> int alloc_tapes(AD& A, int ntapes, int snapshots) {
+  if (ntapes < 0) {
+    size_t free_b = 0, total_b = 0;
+    HC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t per = size_t(A.nst) * A.state_values() * sizeof(*A.sq[0]);
+    ntapes = int(std::min<size_t>(size_t(snapshots) + 1, free_b / 2 / std::max<size_t>(per, 1)));
+  }
+  ntapes = std::min(ntapes, A.nsteps);
   A.tapes.assign(size_t(std::max(ntapes, 0)), {});
   for (auto& t : A.tapes)
     for (int j = 0; j < A.nst; ++j)
@@ -788,8 +797,7 @@ int adjoint_record(hc_ctx* c, int nsteps, int snapshots, const hc_objective* obj
   std::unique_ptr<Tape<R>> T(new Tape<R>());
   Adj<R>& A = T->A;
   if (int st = setup(A, c, nsteps, snapshots, obj)) return st;
-  // stage tapes: by default one per snapshot and one more, enough for every reversal
-  if (int st = alloc_tapes(A, std::min(c->adj_tapes < 0 ? snapshots + 1 : c->adj_tapes, nsteps))) return st;
+  if (int st = alloc_tapes(A, c->adj_tapes, snapshots)) return st;
   HC_CUDA(cudaEventCreate(&T->e0));
   HC_CUDA(cudaEventCreate(&T->e1));
   for (int k = snapshots - 1; k >= 0; --k) T->stack.push_back(k);
@@ -819,8 +827,10 @@ int adjoint_reverse(hc_ctx* c, double* q0_bar, double* ref_bar, bool on_device, 
   c->adj_tape = nullptr;
   Adj<R>& A = T->A;
   const int nsteps = A.nsteps;
-  cudaEvent_t e2;
+  cudaEvent_t e2, er;
   HC_CUDA(cudaEventCreate(&e2));
+  HC_CUDA(cudaEventCreate(&er));
+  HC_CUDA(cudaEventRecord(er, A.s()));
   HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], A.state_values() * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
   // adjoint of the final state
   if (A.obj.kind == HC_OBJ_DRAG) {
@@ -866,15 +876,18 @@ int adjoint_reverse(hc_ctx* c, double* q0_bar, double* ref_bar, bool on_device, 
   }
   // the tape's buffers are freed when this returns: after the stream's work on them
   HC_CUDA(cudaStreamSynchronize(A.s()));
-  float ms_f = 0, ms_t = 0;
+  float ms_f = 0, ms_t = 0, ms_r = 0;
   cudaEventElapsedTime(&ms_f, T->e0, T->e1);
   cudaEventElapsedTime(&ms_t, T->e0, e2);
+  cudaEventElapsedTime(&ms_r, er, e2);
   cudaEventDestroy(e2);
+  cudaEventDestroy(er);
   if (int st = finish_stats(A, nullptr, nullptr, stats)) return st;
   if (stats) {
     stats->ms_forward = ms_f;
     stats->ms_total = ms_t;
     stats->ms_recompute = A.recompute_ms();
+    stats->ms_reverse = ms_r;
   }
   return HC_OK;
 }

@@ -385,7 +385,7 @@ int batch_record(hc_batch* b, int nsteps, int snapshots, const hc_objective* obj
   std::unique_ptr<BTape<R>> T(new BTape<R>());
   BAdj<R>& A = T->A;
   if (int st = batch_setup(A, b, nsteps, snapshots, obj, targets)) return st;
-  if (int st = alloc_tapes(A, std::min(b->adj_tapes < 0 ? snapshots + 1 : b->adj_tapes, nsteps))) return st;
+  if (int st = alloc_tapes(A, b->adj_tapes, snapshots)) return st;
   HC_CUDA(cudaEventCreate(&T->e0));
   HC_CUDA(cudaEventCreate(&T->e1));
   for (int k = snapshots - 1; k >= 0; --k) T->stack.push_back(k);
@@ -412,8 +412,10 @@ template <class R> int batch_reverse(hc_batch* b, double* const* q0_bar, bool on
   b->adj_tape = nullptr;
   BAdj<R>& A = T->A;
   const int nsteps = A.nsteps;
-  cudaEvent_t e2;
+  cudaEvent_t e2, er;
   HC_CUDA(cudaEventCreate(&e2));
+  HC_CUDA(cudaEventCreate(&er));
+  HC_CUDA(cudaEventRecord(er, A.s()));
   HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], A.state_values() * sizeof(R), cudaMemcpyDeviceToDevice, A.s()));
   if (int st = l2_objective(A, true)) return st;  // adjoint of the final states
   if (int st = reverse(A, T->sched, 0, nsteps, -1, T->stack, true)) return st;
@@ -440,10 +442,12 @@ template <class R> int batch_reverse(hc_batch* b, double* const* q0_bar, bool on
   }
   // the device's work and the tape's buffers end together: free them after the stream
   HC_CUDA(cudaStreamSynchronize(A.s()));
-  float ms_f = 0, ms_t = 0;
+  float ms_f = 0, ms_t = 0, ms_r = 0;
   cudaEventElapsedTime(&ms_f, T->e0, T->e1);
   cudaEventElapsedTime(&ms_t, T->e0, e2);
+  cudaEventElapsedTime(&ms_r, er, e2);
   cudaEventDestroy(e2);
+  cudaEventDestroy(er);
   b->launches += A.launches;
   if (stats) {
     std::vector<double> jh(A.ninst);
@@ -459,6 +463,7 @@ template <class R> int batch_reverse(hc_batch* b, double* const* q0_bar, bool on
     stats->ms_recompute = A.recompute_ms();
     stats->replays = A.replays;
     stats->stage_tapes = (long long)A.tapes.size();
+    stats->ms_reverse = ms_r;
   }
   return HC_OK;
 }

@@ -342,6 +342,7 @@ typedef struct {
   double ms_recompute;       /* part of the reverse sweep spent re-advancing from checkpoints */
   long long replays;         /* reversed steps whose stage states were recomputed (no stage tape) */
   long long stage_tapes;     /* stage tapes allocated (hc_set_adjoint_tapes) */
+  double ms_reverse;         /* the reverse sweep alone, from the reverse call's first work */
 } hc_adjoint_stats;
 
 /* The pressure force on the inviscid-wall sides of the current state along dir (the
@@ -372,9 +373,10 @@ int hc_adjoint_record(hc_ctx* ctx, int nsteps, int snapshots, const hc_objective
  * but the last).  A stage tape keeps them (the start state and nst-1 stage states) from the
  * forward sweep or the re-advance that computed the step last before its reversal: the
  * last step of every re-advance and of the sweep's part before each stored checkpoint.
- * -1 (default): snapshots + 1 tapes, enough that no step is replayed; 0: none (every step
- * replayed, `snapshots` states the only storage); k: at most k live at once.  Each tape holds
- * nst states of the mesh, allocated at record time.  Not in the reference (no adjoint). */
+ * -1 (default): snapshots + 1 tapes, enough that no step is replayed, as many of them as fit
+ * in half the free device memory at record time; 0: none (every step replayed, `snapshots`
+ * states the only storage); k: at most k live at once.  Each tape holds nst states of the
+ * mesh, allocated at record time.  Not in the reference (no adjoint). */
 int hc_set_adjoint_tapes(hc_ctx* ctx, int ntapes);
 int hc_adjoint_reverse(hc_ctx* ctx, double* q0_bar, double* ref_bar, int on_device, hc_adjoint_stats* stats);
 
