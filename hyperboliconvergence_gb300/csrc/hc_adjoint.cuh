@@ -358,11 +358,13 @@ template <class R> __host__ __device__ __forceinline__ void limit_grad(int kind,
 // Jacobian transposes of the primitive <-> conserved maps (the RK update
 // cons(q0) + R*f -> prim): prim adjoint at state q -> conserved adjoint, and
 // conserved adjoint at state q0 -> prim adjoint.
+// (one reciprocal of the density and the gas's 1/(gamma-1) instead of four divisions: the
+// reverse passes are bound by the FP64 pipe)
 template <class R> __host__ __device__ __forceinline__ void cons2prim_adj(const Gas<R>& g, const R* q, const R* pb, R* cb) {
-  const R u = q[0], v = q[1], r = q[2];
-  cb[0] = pb[0] / r - g.gm1 * u * pb[3];
-  cb[1] = pb[1] / r - g.gm1 * v * pb[3];
-  cb[2] = pb[2] - (u * pb[0] + v * pb[1]) / r + R(0.5) * g.gm1 * (u * u + v * v) * pb[3];
+  const R u = q[0], v = q[1], ir = R(1) / q[2];
+  cb[0] = pb[0] * ir - g.gm1 * u * pb[3];
+  cb[1] = pb[1] * ir - g.gm1 * v * pb[3];
+  cb[2] = pb[2] - (u * pb[0] + v * pb[1]) * ir + R(0.5) * g.gm1 * (u * u + v * v) * pb[3];
   cb[3] = g.gm1 * pb[3];
 }
 template <class R> __host__ __device__ __forceinline__ void prim2cons_adj(const Gas<R>& g, const R* q, const R* cb, R* pb) {
@@ -370,7 +372,7 @@ template <class R> __host__ __device__ __forceinline__ void prim2cons_adj(const 
   pb[0] += r * cb[0] + r * u * cb[3];
   pb[1] += r * cb[1] + r * v * cb[3];
   pb[2] += u * cb[0] + v * cb[1] + cb[2] + R(0.5) * (u * u + v * v) * cb[3];
-  pb[3] += cb[3] / g.gm1;
+  pb[3] += cb[3] * g.gamma1;
 }
 
 }  // namespace hc

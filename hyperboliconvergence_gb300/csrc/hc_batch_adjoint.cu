@@ -133,9 +133,9 @@ template <class R> int forward_step(BAdj<R>& A, int step, bool rec, int nstages 
   return HC_OK;
 }
 
-// qbar_out = (dRes/dq at q)^T rbar (+ qbar_add) for every instance: four launches
+// scalar law: qbar_out = (dRes/dq at q)^T rbar (+ qbar_add) for every instance, four launches
 template <class R, int FK>
-int residual_adjoint(BAdj<R>& A, const R* q, const R* rbar, const R* qbar_add, R* qbar_out) {
+int residual_adjoint_scalar(BAdj<R>& A, const R* q, const R* rbar, const R* qbar_add, R* qbar_out) {
   AdjBatchArgs<R> a = A.args();
   a.q = q;
   a.rbar = rbar;
@@ -146,36 +146,23 @@ int residual_adjoint(BAdj<R>& A, const R* q, const R* rbar, const R* qbar_add, R
   AdjBatchArgs<R> af = a;
   af.seg = A.seg_f;
   af.nseg = 2 * A.ninst;
-  if (A.b->scalar) {
-    if constexpr (FK == FLUX_RUSANOV || FK == FLUX_CENTRAL) {
-      adj_qm_batch_kernel<R, 3><<<A.blocks_c, 256, 0, A.s()>>>(a);
-      adj_face_scalar_batch_kernel<R, FK><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
-      adj_qmbar_batch_kernel<R, 3><<<A.blocks_c, 256, 0, A.s()>>>(a);
-      adj_gather_batch_kernel<R, 3><<<A.blocks_c, 256, 0, A.s()>>>(a);
-    }
-  } else if constexpr (FK != FLUX_CENTRAL) {
-    adj_qm_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
-    if constexpr (FK == FLUX_BY_TANGENT)
-      HC_CUDA(launch_adj_face_tangent_batch<R>(A.b->cfg.flux, af, A.blocks_f, kFaceThreads, A.s()));
-    else
-      adj_face_batch_kernel<R, FK><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
-    adj_qmbar_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
-    adj_gather_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
-  }
+  adj_qm_batch_kernel<R, 3><<<A.blocks_c, 256, 0, A.s()>>>(a);
+  adj_face_scalar_batch_kernel<R, FK><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
+  adj_qmbar_batch_kernel<R, 3><<<A.blocks_c, 256, 0, A.s()>>>(a);
+  adj_gather_batch_kernel<R, 3><<<A.blocks_c, 256, 0, A.s()>>>(a);
   A.launches += 4;
   HC_CUDA(cudaGetLastError());
   return HC_OK;
 }
 
 template <class R> int res_adj(BAdj<R>& A, const R* q, const R* rbar, const R* add, R* out) {
-  if (A.b->scalar && A.b->cfg.flux == HC_FLUX_CENTRAL) return residual_adjoint<R, FLUX_CENTRAL>(A, q, rbar, add, out);
-  if (A.b->cfg.flux == HC_FLUX_ROE) return residual_adjoint<R, FLUX_ROE>(A, q, rbar, add, out);
-  if (!A.b->scalar && flux_by_tangent(A.b->cfg.flux)) return residual_adjoint<R, FLUX_BY_TANGENT>(A, q, rbar, add, out);
-  return residual_adjoint<R, FLUX_RUSANOV>(A, q, rbar, add, out);
+  if (A.b->cfg.flux == HC_FLUX_CENTRAL) return residual_adjoint_scalar<R, FLUX_CENTRAL>(A, q, rbar, add, out);
+  return residual_adjoint_scalar<R, FLUX_RUSANOV>(A, q, rbar, add, out);
 }
 
 // lam holds the adjoint of every instance's q_{step+1}, sq[0] their q_step; on return
 // lam holds the adjoint of q_step
+template <class R> int adjoint_step_euler(BAdj<R>& A, int step);
 template <class R> int adjoint_step(BAdj<R>& A, int step) {
   // stage states from the step's tape or a replay of its stages but the last (whose output
   // is the start state of the step reversed before, qnext)
@@ -185,6 +172,7 @@ template <class R> int adjoint_step(BAdj<R>& A, int step) {
   HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], bytes4, cudaMemcpyDeviceToDevice, A.s()));
   for (int k = 0; k < A.nst; ++k) HC_CUDA(cudaMemsetAsync(A.rbar[k], 0, bytes4, A.s()));
   HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
+  if (!A.b->scalar) return adjoint_step_euler(A, step);
   for (int s = A.nst - 1; s >= 0; --s) {
     AdjUpdateBatch<R> u{};
     u.inst = A.b->inst_d;
@@ -204,13 +192,74 @@ template <class R> int adjoint_step(BAdj<R>& A, int step) {
     u.beta = A.tab.beta[s];
     u.cfl = A.b->cfg.cfl;
     u.rates = A.rates + size_t(step) * A.ninst;
-    if (A.b->scalar) adj_update_lin_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(u);
-    else adj_update_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(u);
+    adj_update_lin_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(u);
     A.launches += 1;
     HC_CUDA(cudaGetLastError());
     if (int st = res_adj<R>(A, A.sq[s], A.rbar[s], s == 0 ? A.q0bar : nullptr, A.qbs)) return st;
   }
   HC_CUDA(cudaMemcpyAsync(A.lam, A.qbs, bytes4, cudaMemcpyDeviceToDevice, A.s()));
+  A.adj_steps += 1;
+  return HC_OK;
+}
+
+// The Euler reverse of one step for every instance, as the single-mesh driver does it:
+// per stage the face pass, the qmetric adjoint and the fused cell pass (gather of the
+// stage, update reverse and qmetric of the stage before; at the first stage the gather
+// with the update adjoints of q_step into lam), after one cell pass that reverses the
+// last stage's update.
+template <class R> int adjoint_step_euler(BAdj<R>& A, int step) {
+  AdjCellBatch<R> ub{};
+  ub.u.g = with_fixes(make_gas<R>(A.b->gamma, A.b->Rgas, A.b->minf), A.b->fixes);
+  ub.u.q0 = A.sq[0];
+  ub.u.vol = (const R*)A.b->vol;
+  ub.u.q0bar = A.q0bar;
+  for (int k = 0; k < 4; ++k) ub.u.rbar[k] = A.rbar[k];
+  ub.cfl = A.b->cfg.cfl;
+  ub.rates = A.rates + size_t(step) * A.ninst;
+  auto update = [&](AdjCellBatch<R>& w, int s) {
+    w.u.update = 1;
+    w.u.q_out = A.sq[s + 1];
+    for (int k = 0; k < 4; ++k) w.u.alpha[k] = k <= s ? R(A.tab.alpha[s][k]) : R(0);
+    w.u.stage = s;
+    w.beta = A.tab.beta[s];
+  };
+  AdjBatchArgs<R> a = A.args();
+  a.seg = A.seg_c;
+  a.nseg = A.ninst;
+  {
+    AdjCellBatch<R> w = ub;
+    w.u.qbar_in = A.lam;
+    update(w, A.nst - 1);
+    w.u.qm_q = A.sq[A.nst - 1];
+    adj_cell_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a, w);
+    A.launches += 1;
+  }
+  for (int s = A.nst - 1; s >= 0; --s) {
+    a.q = A.sq[s];
+    a.rbar = A.rbar[s];
+    a.qbar_add = s == 0 ? A.q0bar : nullptr;
+    AdjBatchArgs<R> af = a;
+    af.seg = A.seg_f;
+    af.nseg = 2 * A.ninst;
+    if (flux_by_tangent(A.b->cfg.flux))
+      HC_CUDA(launch_adj_face_tangent_batch<R>(A.b->cfg.flux, af, A.blocks_f, kFaceThreads, A.s()));
+    else if (A.b->cfg.flux == HC_FLUX_ROE)
+      adj_face_batch_kernel<R, FLUX_ROE><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
+    else
+      adj_face_batch_kernel<R, FLUX_RUSANOV><<<A.blocks_f, kFaceThreads, 0, A.s()>>>(af);
+    adj_qmbar_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a);
+    AdjCellBatch<R> w = ub;
+    w.u.gather = 1;
+    if (s > 0) {
+      update(w, s - 1);
+      w.u.qm_q = A.sq[s - 1];
+    } else {
+      w.u.qbar_out = A.lam;
+    }
+    adj_cell_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a, w);
+    A.launches += 3;
+    HC_CUDA(cudaGetLastError());
+  }
   A.adj_steps += 1;
   return HC_OK;
 }
@@ -249,6 +298,8 @@ template <class R> int l2_objective(BAdj<R>& A, bool grad) {
 inline int check_batch_support(hc_batch* b) {
   if (b->cfg.basis != HC_BASIS_PRIMITIVE) return fail(HC_ERR_UNSUPPORTED, "the adjoint uses the primitive basis");
   if (b->scalar) {
+    if (b->cfg.flux != HC_FLUX_RUSANOV && b->cfg.flux != HC_FLUX_CENTRAL)
+      return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports the Rusanov and central fluxes");
     for (int t : b->bc)
       if (t != HC_BC_PERIODIC && t != HC_BC_FIXED && t != HC_BC_RIEMANN)
         return fail(HC_ERR_UNSUPPORTED, "the scalar-law adjoint supports periodic, fixed and Riemann boundaries");
