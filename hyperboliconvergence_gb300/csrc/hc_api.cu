@@ -336,10 +336,11 @@ int read_stats(hc_ctx* c, hc_step_stats* st) {
     }
     st->t = info.t;
     st->resnorm = std::sqrt(info.resnorm2);
-    st->status = info.status == ST_OK ? HC_OK : HC_ERR_NONPHYSICAL;
+    st->status = info.status == ST_OK ? HC_OK : info.status == ST_TIMEOUT ? HC_ERR_TIMEOUT : HC_ERR_NONPHYSICAL;
     st->bad_cell = info.bad_cell;
     st->kernel_launches = c->launches;
   }
+  if (info.status == ST_TIMEOUT) return fail(HC_ERR_TIMEOUT, "a staged tile load did not complete in its bounded wait");
   if (info.status != ST_OK)
     return fail(HC_ERR_NONPHYSICAL, "non-physical state at cell " + std::to_string(info.bad_cell));
   return HC_OK;

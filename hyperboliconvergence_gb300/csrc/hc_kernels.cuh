@@ -17,6 +17,8 @@
 
 #include "hc_physics.cuh"
 
+#include <cuda.h>  // CUtensorMap (the tensor-map type of the TMA-staged FP32 stage kernel)
+
 #include <cstdint>
 #include <type_traits>
 
@@ -37,7 +39,7 @@ struct StepInfo {
 };
 
 // Status codes of the device-side checks
-enum { ST_OK = 0, ST_NONPHYSICAL = 1 };
+enum { ST_OK = 0, ST_NONPHYSICAL = 1, ST_TIMEOUT = 2 };
 
 template <class R> struct StageArgs {
   int ni, nj;
@@ -86,6 +88,43 @@ template <class R> __global__ void convert_kernel(const double* __restrict__ a, 
 }
 
 // ---------------------------------------------------------------- stage kernel
+// ---- TMA and mbarrier primitives (inline PTX) of the TMA-staged FP32 stage kernel
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return static_cast<unsigned>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// a 3D box of the tensor map at (x, y, z) into shared memory, completing on bar
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];\n" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+// wait for phase 0 of bar with an iteration bound: a copy that never lands marks the step
+// ST_TIMEOUT (the host returns HC_ERR_TIMEOUT) instead of hanging the GPU
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, StepInfo* info) {
+  for (unsigned it = 0; !mbar_try_wait(bar, 0); ++it) {
+    if (it >= (1u << 22)) {
+      atomicCAS(&info->status, ST_OK, ST_TIMEOUT);
+      return;
+    }
+  }
+}
+
 template <int TI, int TJ, class R> struct StageSmem {
   static constexpr int QI = TI + 4, QJ = TJ + 4;   // state tile with a 2-cell halo
   static constexpr int MI = TI + 2, MJ = TJ + 2;   // qmetric tile with a 1-cell halo
@@ -94,6 +133,22 @@ template <int TI, int TJ, class R> struct StageSmem {
   static constexpr size_t fi_elems = size_t(5) * (TI + 1) * TJ;
   static constexpr size_t fj_elems = size_t(5) * TI * (TJ + 1);
   static constexpr size_t bytes = (q_elems + m_elems + fi_elems + fj_elems) * sizeof(R);
+};
+
+// Shared memory of the TMA-staged FP32 tile: the state tile as the tensor copy lands it (rows
+// of TJ + 8 values from column j0 - 4, so that each copy starts on a 16-byte boundary), the
+// qmetric tile, the i-face records' first TMA_FIELDS fields (each face's fluxes later overwrite
+// the first five fields of its own record), the j-face fluxes.
+constexpr int TMA_FIELDS = 12;  // F_NX..F_SR: the fields the face phase reads
+template <int TI, int TJ> struct StageSmemTma {
+  static constexpr int QI = TI + 4, QJ = TJ + 8;
+  static constexpr size_t q_elems = size_t(4) * QI * QJ;
+  static constexpr size_t m_elems = size_t(8) * (TI + 2) * (TJ + 2);
+  static constexpr size_t ri_elems = size_t(TMA_FIELDS) * (TI + 1) * TJ;
+  static constexpr size_t fj_elems = size_t(5) * TI * (TJ + 1);
+  static constexpr size_t ri_offset = (q_elems + m_elems) * sizeof(float);
+  static constexpr size_t bytes = (q_elems + m_elems + ri_elems + fj_elems) * sizeof(float);
+  static_assert(ri_offset % 128 == 0, "the i-face records' tensor copy lands on a 128-byte boundary");
 };
 
 __device__ __forceinline__ int wrapi(int a, int n) {
@@ -172,15 +227,22 @@ template <class C, class R> __device__ __forceinline__ Gas<C> gas_as(const Gas<R
 // terms are honoured (the batched instantiations, which have none, compile without them).
 // LIM >= 0: the limiter is that compile-time constant (a.limiter must equal it), so its
 // selection folds away; -1: a.limiter chosen at run time.
+// TMA: the FP32 tile whose state tile (interior tiles) and i-face records arrive by tensor
+// copies (tq, tfi; bars two mbarriers in shared memory), see stage_kernel_tma.
 template <int TI, int TJ, class R, int FK, class C = R, bool REC = false, bool DUAL = true, int NTH = TI * TJ,
-          int LIM = -1>
-__device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj, unsigned char* smem_raw) {
+          int LIM = -1, bool TMA = false>
+__device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj, unsigned char* smem_raw,
+                                           const CUtensorMap* tq = nullptr, const CUtensorMap* tfi = nullptr,
+                                           uint64_t* bars = nullptr) {
   constexpr bool same = std::is_same<C, R>::value;
   using SM = StageSmem<TI, TJ, C>;
+  static_assert(!TMA || std::is_same<C, float>::value, "the TMA-staged tile is the FP32 one");
+  constexpr int QJT = TMA ? TJ + 8 : SM::QJ;  // row length of the state tile in shared memory
+  constexpr int QSH = TMA ? 2 : 0;            // its column shift (the halo's column 0 at QSH)
   C* sq = reinterpret_cast<C*>(smem_raw);
-  C* sm = sq + SM::q_elems;
+  C* sm = sq + size_t(4) * SM::QI * QJT;
   C* sfi = sm + SM::m_elems;
-  C* sfj = sfi + SM::fi_elems;
+  C* sfj = sfi + (TMA ? size_t(TMA_FIELDS) * (TI + 1) * TJ : SM::fi_elems);
   const C* cfi = same ? reinterpret_cast<const C*>(a.fi) : reinterpret_cast<const C*>(a.fic);
   const C* cfj = same ? reinterpret_cast<const C*>(a.fj) : reinterpret_cast<const C*>(a.fjc);
   constexpr int QI = SM::QI, QJ = SM::QJ, MI = SM::MI, MJ = SM::MJ;
@@ -198,28 +260,56 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   // phases 1-2 (uniform per block).  FP32 only: the FP64 stage is bound by its FP64 pipe
   // and gains nothing from fewer integer instructions.  Same sums in the same order.
   const bool interior = std::is_same<C, float>::value && i0 >= 2 && i0 + TI + 2 <= ni && j0 >= 2 && j0 + TJ + 2 <= nj;
-  if (interior) {
+  // TMA: one thread arms the two barriers and issues the tensor copies -- the interior tile's
+  // state (4 planes x (TI + 4) rows x (TJ + 8) columns from (i0 - 2, j0 - 4); columns past the
+  // mesh read zeros and are never used) and the i-face records (TMA_FIELDS fields x (TI + 1)
+  // rows x TJ columns from (i0, j0); rows or columns past the mesh belong to no valid face);
+  // they land while the threads run the halo and qmetric phases
+  bool tma = false;
+  if constexpr (TMA) {
+    tma = (smem_u32(sq) % 128u) == 0 && (smem_u32(sfi) % 128u) == 0;
+    if (tma) {
+      if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_fence_init();
+      }
+      __syncthreads();
+      if (tid == 0) {
+        if (interior) {
+          mbar_expect_tx(&bars[0], unsigned(4 * QI * QJT * sizeof(C)));
+          tma_load_3d(sq, tq, j0 - 4, i0 - 2, 0, &bars[0]);
+        }
+        mbar_expect_tx(&bars[1], unsigned(TMA_FIELDS * (TI + 1) * TJ * sizeof(C)));
+        tma_load_3d(sfi, tfi, j0, i0, 0, &bars[1]);
+      }
+    }
+  }
+  if (tma && interior) {
+    mbar_wait_bounded(&bars[0], a.info);
+  } else if (interior) {
     const R* qb = a.q + (size_t(i0 - 2) * nj + (j0 - 2));
     for (int k = tid; k < QI * QJ; k += NT) {
       const int la = k / QJ, lb = k % QJ;
       const size_t c = size_t(la) * nj + lb;
 #pragma unroll
-      for (int v = 0; v < 4; ++v) sq[(v * QI + la) * QJ + lb] = cvt<C>(qb[v * ncell + c]);
+      for (int v = 0; v < 4; ++v) sq[(v * QI + la) * QJT + lb + QSH] = cvt<C>(qb[v * ncell + c]);
     }
-  } else
-  for (int k = tid; k < QI * QJ; k += NT) {
-    const int la = k / QJ, lb = k % QJ;
-    int gi = i0 - 2 + la, gj = j0 - 2 + lb;
-    bool ok = true;
-    if (gi < 0 || gi >= ni) { if (per_i) gi = wrapi(gi, ni); else ok = false; }
-    if (gj < 0 || gj >= nj) { if (per_j) gj = wrapi(gj, nj); else ok = false; }
-    const size_t c = size_t(gi) * nj + gj;
+  } else {
+    for (int k = tid; k < QI * QJ; k += NT) {
+      const int la = k / QJ, lb = k % QJ;
+      int gi = i0 - 2 + la, gj = j0 - 2 + lb;
+      bool ok = true;
+      if (gi < 0 || gi >= ni) { if (per_i) gi = wrapi(gi, ni); else ok = false; }
+      if (gj < 0 || gj >= nj) { if (per_j) gj = wrapi(gj, nj); else ok = false; }
+      const size_t c = size_t(gi) * nj + gj;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) sq[(v * QI + la) * QJ + lb] = ok ? cvt<C>(a.q[v * ncell + c]) : C(0);
+      for (int v = 0; v < 4; ++v) sq[(v * QI + la) * QJT + lb + QSH] = ok ? cvt<C>(a.q[v * ncell + c]) : C(0);
+    }
   }
   __syncthreads();
 
-  auto Q = [&](int v, int la, int lb) -> C { return sq[(v * QI + la + 2) * QJ + lb + 2]; };  // tile coords
+  auto Q = [&](int v, int la, int lb) -> C { return sq[(v * QI + la + 2) * QJT + lb + 2 + QSH]; };  // tile coords
   auto M = [&](int k, int la, int lb) -> C& { return sm[(k * MI + la + 1) * MJ + lb + 1]; };
 
   // ---- phase 2: qmetric of the tile cells and of the 1-cell halo strips
@@ -297,6 +387,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
 #pragma unroll
     for (int q = 0; q < 8; ++q) M(q, la, lb) = m[q];
   }
+  if (tma) mbar_wait_bounded(&bars[1], a.info);
   __syncthreads();
 
   // ---- phase 3: face fluxes (i-faces then j-faces of the tile, each once)
@@ -319,7 +410,12 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
       const C* rec = idir ? cfi : cfj;
       const int nf = idir ? nfi : nfj;
       const int fidx = idir ? gi * nj + gj : gi * (nj + 1) + gj;
-      auto rd = [&](int fld) -> C { return rec[size_t(fld) * nf + fidx]; };
+      auto rd = [&](int fld) -> C {
+        if constexpr (TMA) {
+          if (idir && tma) return sfi[fld * NFI + la * TJ + lb];  // the tensor-copied i-face records
+        }
+        return rec[size_t(fld) * nf + fidx];
+      };
       const C nx = rd(F_NX), ny = rd(F_NY), A = rd(F_A);
       const int lo = idir ? gi : gj, nalong = idir ? ni : nj;
       const int side = idir ? (lo == 0 ? 0 : 1) : (lo == 0 ? 2 : 3);
@@ -610,6 +706,22 @@ __global__ void __launch_bounds__(NT, (StageResidency<R, C, NT>::value))
     stage_kernel(const StageArgs<R> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   stage_tile<TI, TJ, R, FK, C, false, true, NT, LIM>(a, blockIdx.y, blockIdx.x, smem_raw);
+}
+
+// The FP32 8x32 tile with its loads staged by the Tensor Memory Accelerator: the interior
+// tile's state and every tile's i-face records arrive by cp.async.bulk.tensor copies on
+// mbarriers, issued by one thread at the start, while the threads load the halo of edge
+// tiles and form the qmetric; the j-face records and the earlier stages' residuals stay
+// plain loads (the j-face planes' row pitch, (nj + 1) values, is not a multiple of 16 bytes).
+// The tensor maps are kernel parameters (encoded per launch by the launcher, hc_tma.h).
+template <int TI, int TJ, int FK, int LIM>
+__global__ void __launch_bounds__(TI * TJ, (StageResidency<float, float, TI * TJ>::value))
+    stage_kernel_tma(const StageArgs<float> a, const __grid_constant__ CUtensorMap tq,
+                     const __grid_constant__ CUtensorMap tfi) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + StageSmemTma<TI, TJ>::bytes);
+  stage_tile<TI, TJ, float, FK, float, false, true, TI * TJ, LIM, true>(a, blockIdx.y, blockIdx.x, smem_raw, &tq,
+                                                                          &tfi, bars);
 }
 
 // the recording variant (a diagnostic, not on the stepping path): the same tile with

@@ -4,6 +4,7 @@
 #pragma once
 
 #include "hc_kernels.cuh"
+#include "hc_tma.h"
 
 #include <algorithm>
 #include <type_traits>
@@ -77,8 +78,15 @@ inline void tile_dims(int tile, int* ti, int* tj) {
   /* FP32 kernels with the limiter a compile-time constant (the FP32 stage is bound by */               \
   /* instruction issue; the run-time selection costs ~9% of it): the 8x32 single-mesh  */               \
   /* tile for the common limiters, and every batch tile for van Albada and NoLimit3     */               \
+  /* with the state and i-face record loads staged by TMA where the mesh rows allow it */              \
   template <int LIM> static void go_lim(const StageArgs<float>& a, cudaStream_t s) {                     \
     const dim3 grid((a.nj + 31) / 32, (a.ni + 7) / 8);                                                   \
+    CUtensorMap tq, tfi;                                                                                 \
+    if (stage_tma_maps(a, &tq, &tfi)) {                                                                  \
+      stage_kernel_tma<8, 32, FK, LIM>                                                                   \
+          <<<grid, 256, StageSmemTma<8, 32>::bytes + 2 * sizeof(uint64_t), s>>>(a, tq, tfi);             \
+      return;                                                                                            \
+    }                                                                                                    \
     stage_kernel<8, 32, float, FK, float, 256, LIM><<<grid, 256, StageSmem<8, 32, float>::bytes, s>>>(a); \
   }                                                                                                      \
   static bool go_fixed_lim(const StageArgs<float>& a, cudaStream_t s) {                                  \
