@@ -78,6 +78,7 @@ def _declare(lib):
         "hc_set_tile": [p, i],
         "hc_set_corrections": [p, C.c_uint],
         "hc_set_adjoint_tapes": [p, C.c_int],
+        "hc_inject_stalled_copy": [p, C.c_int],
         "hc_set_time": [p, d],
         "hc_wall_force": [p, dp, dp],
         "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],

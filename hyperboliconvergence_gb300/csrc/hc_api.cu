@@ -719,6 +719,12 @@ int hc_set_corrections(hc_ctx* c, unsigned mask) {
   return HC_OK;
 }
 
+int hc_inject_stalled_copy(hc_ctx* c, int on) {
+  if (int st = check_ctx(c)) return st;
+  c->stall_copy = on ? 1 : 0;
+  return HC_OK;
+}
+
 int hc_set_adjoint_tapes(hc_ctx* c, int ntapes) {
   if (int st = check_ctx(c)) return st;
   if (ntapes < -1) return fail(HC_ERR_ARG, "stage tapes: -1 (one per snapshot and one more) or a count >= 0");

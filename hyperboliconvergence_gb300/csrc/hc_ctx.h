@@ -23,6 +23,7 @@ struct hc_ctx {
   int vscale = 0, pscale = 0;                       // AUSM+up LowMachScaling pair
   unsigned fixes = 0;                               // HC_FIX_* corrections (hc_set_corrections)
   int adj_tapes = -1;                               // adjoint stage tapes (hc_set_adjoint_tapes); -1 auto
+  int stall_copy = 0;                               // test hook (hc_inject_stalled_copy)
   // the forward sweep recorded by hc_adjoint_record for hc_adjoint_reverse (owned here,
   // released by the reverse sweep, the next record, a mesh upload or destroy)
   void* adj_tape = nullptr;
@@ -84,6 +85,7 @@ template <class R> StageArgs<R> base_args(hc_ctx* c) {
   a.q0 = (const R*)c->q[0];
   a.info = c->info;
   a.cfl = R(c->cfg.cfl);
+  a.stall_copy = c->stall_copy;
   return a;
 }
 

@@ -72,6 +72,8 @@ template <class R> struct StageArgs {
   // dual_src, Q the conserved set, dual_src (4 planes) the earlier time levels' terms
   const R* dual_src;
   R dual_g0, dual_b0dt;
+  int stall_copy;  // test hook (hc_inject_stalled_copy): the TMA-staged tile's records barrier
+                   // expects 16 bytes its copy never delivers, so the bounded wait runs out
 };
 
 // Branch signature of one face (recording kernels): bits 0-15 the limiter pieces of
@@ -114,11 +116,19 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
 }
-// wait for phase 0 of bar with an iteration bound: a copy that never lands marks the step
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// wait for phase 0 of bar for at most one second: a copy that never lands marks the step
 // ST_TIMEOUT (the host returns HC_ERR_TIMEOUT) instead of hanging the GPU
+constexpr unsigned long long kCopyWaitNs = 1000000000ull;
 __device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, StepInfo* info) {
-  for (unsigned it = 0; !mbar_try_wait(bar, 0); ++it) {
-    if (it >= (1u << 22)) {
+  if (mbar_try_wait(bar, 0)) return;
+  const unsigned long long t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, 0)) {
+    if (globaltimer_ns() - t0 > kCopyWaitNs) {
       atomicCAS(&info->status, ST_OK, ST_TIMEOUT);
       return;
     }
@@ -280,7 +290,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
           mbar_expect_tx(&bars[0], unsigned(4 * QI * QJT * sizeof(C)));
           tma_load_3d(sq, tq, j0 - 4, i0 - 2, 0, &bars[0]);
         }
-        mbar_expect_tx(&bars[1], unsigned(TMA_FIELDS * (TI + 1) * TJ * sizeof(C)));
+        mbar_expect_tx(&bars[1], unsigned(TMA_FIELDS * (TI + 1) * TJ * sizeof(C)) + (a.stall_copy ? 16u : 0u));
         tma_load_3d(sfi, tfi, j0, i0, 0, &bars[1]);
       }
     }

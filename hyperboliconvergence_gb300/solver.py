@@ -142,6 +142,12 @@ class Solver:
         self.corrections = _capi.fix_mask(corrections)
         check(self.lib.hc_set_corrections(self.h, self.corrections))
 
+    def inject_stalled_copy(self, on: bool = True) -> None:
+        """Test hook of the failure detection (hc_inject_stalled_copy): the TMA-staged FP32
+        stage kernel's copy barrier waits for bytes that never come, its bounded wait runs out
+        and the step raises HC_ERR_TIMEOUT with the context still usable."""
+        check(self.lib.hc_inject_stalled_copy(self.h, 1 if on else 0))
+
     def set_adjoint_tapes(self, ntapes: int = -1) -> None:
         """Stage tapes of the adjoint's checkpointing (hc_set_adjoint_tapes): -1 one per
         snapshot and one more (no step's stages recomputed), 0 none (every reversed step

@@ -378,6 +378,14 @@ int hc_adjoint_record(hc_ctx* ctx, int nsteps, int snapshots, const hc_objective
  * states the only storage); k: at most k live at once.  Each tape holds nst states of the
  * mesh, allocated at record time.  Not in the reference (no adjoint). */
 int hc_set_adjoint_tapes(hc_ctx* ctx, int ntapes);
+
+/* Test hook of the failure detection (no counterpart in the reference): with on != 0 the
+ * FP32 stage kernel whose loads are staged by TMA tensor copies (8x32 tiles, the common
+ * limiters, nj a multiple of 4) arms its face-record barrier for 16 bytes more than the copy
+ * delivers.  Every CTA's bounded wait (one second) then runs out, the step's status becomes
+ * HC_ERR_TIMEOUT and hc_step returns it; no copy is left in flight and the context stays
+ * usable.  0 (the default) clears it. */
+int hc_inject_stalled_copy(hc_ctx* ctx, int on);
 int hc_adjoint_reverse(hc_ctx* ctx, double* q0_bar, double* ref_bar, int on_device, hc_adjoint_stats* stats);
 
 /* ---------------------------------------------------------------------------
