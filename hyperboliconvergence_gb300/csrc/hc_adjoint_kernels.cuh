@@ -590,38 +590,26 @@ template <class R, int NV = 4> __global__ void adj_gather_kernel(const AdjArgs<R
 }
 
 // Reverse of one stage update q_out = prim(cons(q0) + (sum_k alpha_k R_k) * fac),
-// fac = beta*dt/V frozen: qbar_out -> q0bar (accumulated) and rbar_k (accumulated).
+// fac = beta*dt/V frozen, at cell c: qb (the adjoint of q_out) -> q0bar and rbar_k (both
+// accumulated, k <= stage)
 template <class R>
-__device__ __forceinline__ void adj_update_cell(int ncell, const Gas<R>& g, const R* __restrict__ q_out,
-                                                const R* __restrict__ q0, const R* __restrict__ vol,
-                                                const R* __restrict__ qbar_out, R* __restrict__ q0bar, R* rbar0,
-                                                R* rbar1, R* rbar2, R* rbar3, R alpha0, R alpha1, R alpha2,
-                                                R alpha3, int stage, R dts, int c) {
-  if (c >= ncell) return;
-  const size_t n = size_t(ncell);
-  R q[4], qz[4], pb[4], cb[4], z[4] = {R(0), R(0), R(0), R(0)};
+__device__ __forceinline__ void adj_update_apply(const Gas<R>& g, const R* __restrict__ q_out,
+                                                 const R* __restrict__ q0, const R* __restrict__ vol, const R* qb,
+                                                 R* __restrict__ q0bar, R* const* rbar, const R* alpha, int stage,
+                                                 R dts, size_t n, int c) {
+  R q[4], qz[4], cb[4], z[4] = {R(0), R(0), R(0), R(0)};
 #pragma unroll
-  for (int v = 0; v < 4; ++v) { q[v] = q_out[v * n + c]; qz[v] = q0[v * n + c]; pb[v] = qbar_out[v * n + c]; }
-  cons2prim_adj(g, q, pb, cb);
+  for (int v = 0; v < 4; ++v) { q[v] = q_out[v * n + c]; qz[v] = q0[v * n + c]; }
+  cons2prim_adj(g, q, qb, cb);
   prim2cons_adj(g, qz, cb, z);
 #pragma unroll
   for (int v = 0; v < 4; ++v) q0bar[v * n + c] += z[v];
   const R fac = dts / vol[c];
-  R* rb[4] = {rbar0, rbar1, rbar2, rbar3};
-  const R al[4] = {alpha0, alpha1, alpha2, alpha3};
 #pragma unroll
   for (int k = 0; k < 4; ++k)
     if (k <= stage)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) rb[k][v * n + c] += al[k] * cb[v] * fac;
-}
-template <class R>
-__global__ void adj_update_kernel(int ncell, Gas<R> g, const R* __restrict__ q_out, const R* __restrict__ q0,
-                                  const R* __restrict__ vol, const R* __restrict__ qbar_out, R* __restrict__ q0bar,
-                                  R* rbar0, R* rbar1, R* rbar2, R* rbar3, R alpha0, R alpha1, R alpha2, R alpha3,
-                                  int stage, R dts) {
-  adj_update_cell(ncell, g, q_out, q0, vol, qbar_out, q0bar, rbar0, rbar1, rbar2, rbar3, alpha0, alpha1, alpha2,
-                  alpha3, stage, dts, int(blockIdx.x * blockDim.x + threadIdx.x));
+      for (int v = 0; v < 4; ++v) rbar[k][v * n + c] += alpha[k] * cb[v] * fac;
 }
 
 // ---- the drag objective's adjoint
@@ -732,19 +720,7 @@ template <class R> __device__ __forceinline__ void adj_cell_body(const AdjArgs<R
   }
   if (u.drag) qb[3] += drag_cell(a, c);
   if (u.update) {
-    R q[4], qz[4], cb[4], z[4] = {R(0), R(0), R(0), R(0)};
-#pragma unroll
-    for (int v = 0; v < 4; ++v) { q[v] = u.q_out[v * n + c]; qz[v] = u.q0[v * n + c]; }
-    cons2prim_adj(u.g, q, qb, cb);
-    prim2cons_adj(u.g, qz, cb, z);
-#pragma unroll
-    for (int v = 0; v < 4; ++v) u.q0bar[v * n + c] += z[v];
-    const R fac = u.dts / u.vol[c];
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      if (k <= u.stage)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) u.rbar[k][v * n + c] += u.alpha[k] * cb[v] * fac;
+    adj_update_apply(u.g, u.q_out, u.q0, u.vol, qb, u.q0bar, u.rbar, u.alpha, u.stage, u.dts, n, c);
   } else {
 #pragma unroll
     for (int v = 0; v < 4; ++v) u.qbar_out[v * n + c] = qb[v];
@@ -892,8 +868,9 @@ template <class R, int NV = 4> __global__ void adj_gather_batch_kernel(const Adj
   adj_gather_cell<R, NV>(sb.a, sb.local * int(blockDim.x) + int(threadIdx.x));
 }
 
-// Reverse of one stage update for every instance; the frozen timestep of each
-// instance is cfl / max rate of the step, as the forward run took it.
+// Reverse of one stage update of a scalar-law batch for every instance (the Euler batch
+// reverses its updates in the fused cell pass); the frozen timestep of each instance is
+// cfl / max rate of the step, as the forward run took it.
 template <class R> struct AdjUpdateBatch {
   const BatchInst* inst;
   const int* seg;  // the cell-pass segments
@@ -937,16 +914,6 @@ __global__ void __launch_bounds__(256, CellResidency<sizeof(R)>::value)
   adj_cell_body(sb.a, u, sb.local * int(blockDim.x) + int(threadIdx.x));
 }
 
-template <class R> __global__ void adj_update_batch_kernel(const AdjUpdateBatch<R> u) {
-  const int s = find_segment(u.seg, u.nseg, int(blockIdx.x));
-  const BatchInst& in = u.inst[s];
-  const long long c4 = 4 * in.cell;
-  const double dt = u.cfl / fmax(DBL_MIN, u.rates[s]);
-  const int c = (int(blockIdx.x) - u.seg[s]) * int(blockDim.x) + int(threadIdx.x);
-  adj_update_cell(in.ni * in.nj, u.g, u.q_out + c4, u.q0 + c4, u.vol + in.cell, u.qbar_out + c4, u.q0bar + c4,
-                  u.rbar[0] + c4, u.rbar[1] + c4, u.rbar[2] + c4, u.rbar[3] + c4, u.alpha[0], u.alpha[1], u.alpha[2],
-                  u.alpha[3], u.stage, R(u.beta * dt), c);
-}
 // Face passes of the Euler fluxes reversed by tangents (flux SLAU, SLAU as written,
 // AUSM+up, RoeUnprecWS or the face-frame Roe), compiled in their own unit
 // (hc_adjoint_tangent.cu); both directions in one launch, i-faces in blocks [0, nbi)

@@ -28,9 +28,9 @@ pytestmark = pytest.mark.gpu
 
 N, STEPS = 128, 100
 TOL64 = 1e-12
-# free-running: 100 steps of round-off-level differences, amplified where the limiter
-# switches branch; bound measured with margin
-TOL_FREE = 1e-10
+# free-running: 100 steps of round-off-level differences (measured 1.6e-14 with the
+# reference's Roe flux, 6.9e-15 with the face-frame one), held to the per-step bar
+TOL_FREE = 1e-12
 
 
 def cons(q, g=1.4):
