@@ -2,6 +2,7 @@
 // one persistent launch per RK stage over a shared work list of tiles, with
 // CUDA-graph capture and a schedule autotuner.
 #include "hc_batch.h"
+#include "hc_tma.h"
 
 #include <algorithm>
 #include <cstring>
@@ -28,7 +29,7 @@ void free_all(hc_batch* b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   b->graph_exec = nullptr; b->graph = nullptr;
   void* ptrs[] = {b->nodes, b->cx, b->cy, b->xm, b->vol64, b->fi64, b->fj64, b->gref, b->q[0], b->q[1], b->q[2],
-                  b->res[0], b->res[1], b->res[2], b->staging, b->info, b->inst_d, b->order_d};
+                  b->res[0], b->res[1], b->res[2], b->staging, b->info, b->inst_d, b->order_d, b->tma_maps};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->fp32) {
@@ -78,6 +79,43 @@ int build_worklist(hc_batch* b) {
 
 
 
+// Tensor maps of an FP32 Euler batch (hc_tma.h): per instance, the three state pools' slices
+// (4 planes of ni x nj) and its i-face records; none when any instance's rows are not a
+// multiple of 16 bytes or a slice is not 16-byte aligned (the batch then keeps plain loads).
+int build_tma_maps(hc_batch* b) {
+  if (!b->fp32 || b->scalar) return HC_OK;
+  const int n = b->ninst;
+  std::vector<CUtensorMap> maps(size_t(4) * n);
+  for (int k = 0; k < n; ++k) {
+    StageArgs<float> a{};
+    a.ni = b->ni[k];
+    a.nj = b->nj[k];
+    a.fi = (const float*)b->fi + (long long)FREC * b->fi_off[k];
+    for (int buf = 0; buf < 3; ++buf) {
+      a.q = (const float*)b->q[buf] + 4 * b->cell_off[k];
+      CUtensorMap tfi;
+      if (!stage_tma_maps(a, &maps[size_t(buf) * n + k], &tfi)) return HC_OK;
+      if (buf == 0) maps[size_t(3) * n + k] = tfi;
+    }
+  }
+  HC_CUDA(cudaMalloc((void**)&b->tma_maps, maps.size() * sizeof(CUtensorMap)));
+  HC_CUDA(cudaMemcpy(b->tma_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+  return HC_OK;
+}
+
+// the maps of stage input pool q (one of b->q[0..2]) and of the records, or nulls
+template <class R> void tma_args(hc_batch* b, BatchArgs<R>& a) {
+  a.tmaps_q = a.tmaps_fi = nullptr;
+  if constexpr (std::is_same<R, float>::value) {
+    if (!b->tma_maps || b->sched.tile != HC_TILE_8x32) return;
+    for (int buf = 0; buf < 3; ++buf)
+      if (a.q == (const R*)b->q[buf]) {
+        a.tmaps_q = b->tma_maps + size_t(buf) * b->ninst;
+        a.tmaps_fi = b->tma_maps + size_t(3) * b->ninst;
+      }
+  }
+}
+
 template <class R> int persistent_step(hc_batch* b) {
   const RKTab tab = rk_table(b->cfg.rk);
   const int nst = tab.nst;
@@ -92,6 +130,7 @@ template <class R> int persistent_step(hc_batch* b) {
   for (int s = 0; s < nst; ++s) {
     BatchArgs<R> a = batch_args<R>(b);
     a.q = (s == 0) ? (const R*)b->q[0] : out_of(s - 1);
+    tma_args(b, a);
     a.stage = s;
     a.beta = R(tab.beta[s]);
     for (int k = 0; k <= s; ++k) a.alpha[k] = R(tab.alpha[s][k]);
@@ -322,6 +361,7 @@ int hc_batch_create(const hc_config* cfg, int ninst, const int* ni, const int* n
   }
   if (e != cudaSuccess) return bail(fail(HC_ERR_CUDA, std::string("batch set-up: ") + cudaGetErrorString(e)));
   if (int st = build_worklist(b)) return bail(st);
+  if (int st = build_tma_maps(b)) return bail(st);
   *out = b;
   return HC_OK;
 }

@@ -31,6 +31,10 @@ struct hc_batch {
   double* staging = nullptr;
   hc::StepInfo* info = nullptr;
   hc::BatchInst* inst_d = nullptr;
+  // FP32 Euler batches: per-instance tensor maps of the three state pools and of the i-face
+  // records ([4][ninst], device memory) for the TMA-staged 8x32 tile; null where a mesh's rows
+  // are not a multiple of 16 bytes
+  CUtensorMap* tma_maps = nullptr;
   int* order_d = nullptr;
   int nwork = 0, nwork_cap = 0;
   std::vector<hc::BatchInst> inst_h;

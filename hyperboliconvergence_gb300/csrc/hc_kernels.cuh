@@ -277,7 +277,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   // they land while the threads run the halo and qmetric phases
   bool tma = false;
   if constexpr (TMA) {
-    tma = (smem_u32(sq) % 128u) == 0 && (smem_u32(sfi) % 128u) == 0;
+    tma = tq != nullptr && tfi != nullptr && (smem_u32(sq) % 128u) == 0 && (smem_u32(sfi) % 128u) == 0;
     if (tma) {
       if (tid == 0) {
         mbar_init(&bars[0], 1);
@@ -286,6 +286,9 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
       }
       __syncthreads();
       if (tid == 0) {
+        // the block's earlier accesses to this shared memory (a persistent CTA's previous
+        // work item) before the tensor copies overwrite it
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         if (interior) {
           mbar_expect_tx(&bars[0], unsigned(4 * QI * QJT * sizeof(C)));
           tma_load_3d(sq, tq, j0 - 4, i0 - 2, 0, &bars[0]);
@@ -818,6 +821,10 @@ template <class R> struct BatchArgs {
   R beta, cfl;
   StepInfo* info;          // one per instance
   int basis;               // solution basis: 0 primitive, 1 conserved
+  // FP32 8x32 batches: per-instance tensor maps of the stage input buffer and of the i-face
+  // records (device memory), or null (plain loads)
+  const CUtensorMap* tmaps_q;
+  const CUtensorMap* tmaps_fi;
 };
 
 template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const BatchArgs<R>& b, int k) {
@@ -833,6 +840,7 @@ template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const B
   a.dual_src = nullptr;  // batches have no dual time
   a.dual_g0 = R(1);
   a.dual_b0dt = R(0);
+  a.stall_copy = 0;
   const long long n = (long long)in.ni * in.nj;
   const long long off4 = 4 * in.cell, off5 = 5 * in.cell;
   a.q = b.q + off4;
@@ -883,6 +891,34 @@ __global__ void __launch_bounds__(TI * TJ, (BatchResidency<R, TI * TJ>::value))
     }
     __syncthreads();
     stage_tile<TI, TJ, R, FK, R, false, false, TI * TJ, LIM>(sa, tile_ij[0], tile_ij[1], smem_raw);
+  }
+}
+
+// The persistent batch kernel with the TMA-staged FP32 8x32 tile (stage_kernel_tma): each
+// work item's copies use its instance's tensor maps (b.tmaps_q, b.tmaps_fi); the tile
+// re-arms its two mbarriers per item.
+template <int FK, int LIM>
+__global__ void __launch_bounds__(256, (BatchResidency<float, 256>::value))
+    batch_stage_kernel_tma(const BatchArgs<float> b) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + StageSmemTma<8, 32>::bytes);
+  __shared__ StageArgs<float> sa;
+  __shared__ int item[3];  // instance, tile row, tile column
+  for (int w = blockIdx.x; w < b.nwork; w += gridDim.x) {
+    __syncthreads();  // the previous work item may still read shared memory
+    if (threadIdx.x == 0) {
+      const int packed = b.order[w];
+      const int k = packed >> 16, t = packed & 0xffff;
+      const int tj = b.inst[k].tiles_j;
+      sa = instance_args(b, k);
+      item[0] = k;
+      item[1] = t / tj;
+      item[2] = t % tj;
+    }
+    __syncthreads();
+    const int k = item[0];
+    stage_tile<8, 32, float, FK, float, false, false, 256, LIM, true>(sa, item[1], item[2], smem_raw,
+                                                                      b.tmaps_q + k, b.tmaps_fi + k, bars);
   }
 }
 

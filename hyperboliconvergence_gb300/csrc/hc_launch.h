@@ -99,8 +99,24 @@ inline void tile_dims(int tile, int* ti, int* tj) {
       default: return false;                                                                             \
     }                                                                                                    \
   }                                                                                                      \
+  template <int LIM> static void gob_tma(const BatchArgs<float>& b, int grid, cudaStream_t s) {          \
+    constexpr size_t smem = StageSmemTma<8, 32>::bytes + 2 * sizeof(uint64_t);                           \
+    static int cap = 0;                                                                                  \
+    if (cap == 0) {                                                                                      \
+      int dev = 0, sms = 0, occ = 0;                                                                     \
+      cudaGetDevice(&dev);                                                                               \
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);                                 \
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_stage_kernel_tma<FK, LIM>, 256, smem);   \
+      cap = (sms > 0 && occ > 0) ? sms * occ : grid;                                                     \
+    }                                                                                                    \
+    batch_stage_kernel_tma<FK, LIM><<<std::min(grid, cap), 256, smem, s>>>(b);                           \
+  }                                                                                                      \
   template <class R, int TI, int TJ, int LIM = -1>                                                        \
   static void gob(const BatchArgs<R>& b, int grid, cudaStream_t s) {                                     \
+    /* the TMA-staged tile where the batch has tensor maps for this stage's input */                    \
+    if constexpr (std::is_same<R, float>::value && TI == 8 && TJ == 32) {                                \
+      if (b.tmaps_q && b.tmaps_fi) { gob_tma<LIM>(b, grid, s); return; }                                  \
+    }                                                                                                    \
     /* a persistent grid larger than what stays resident would run a second, partial wave */           \
     static int cap = 0;                                                                                  \
     if (cap == 0) {                                                                                      \

@@ -35,6 +35,23 @@ def test_persistent_equals_per_instance(precision, tile):
         assert np.array_equal(x, y)
 
 
+def test_persistent_tma_tile_equals_per_instance():
+    """Every instance's nj a multiple of 4: the FP32 8x32 batch stages its tile loads by TMA
+    with per-instance tensor maps (batch_stage_kernel_tma), the per-instance launches by the
+    single-mesh TMA kernel; both equal, over several steps and with edge, interior and partial
+    tiles (the single-mesh TMA kernel equals the plain-load kernel bit for bit)."""
+    insts = uneven_riemann_batch(6, 17, sizes=(12, 20, 36, 44, 68, 100))
+    a = Batch(insts, flux="slau", limiter="vanalbada", precision="fp32")
+    b = Batch(insts, flux="slau", limiter="vanalbada", precision="fp32")
+    a.set_schedule(tile="8x32", ctas_per_sm=2, order="largest_first")
+    b.set_schedule(tile="8x32")
+    a.step_async(4, "persistent")
+    b.step_async(4, "per_instance")
+    a.sync(), b.sync()
+    for x, y in zip(states(a), states(b)):
+        assert np.array_equal(x, y)
+
+
 def test_batch_equals_single_contexts():
     insts = small_batch(seed=11, n=4)
     bt = Batch(insts, flux="roe", limiter="vanleer", precision="fp64", dt="global")
