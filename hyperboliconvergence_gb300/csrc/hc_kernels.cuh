@@ -145,19 +145,19 @@ template <int TI, int TJ, class R> struct StageSmem {
   static constexpr size_t bytes = (q_elems + m_elems + fi_elems + fj_elems) * sizeof(R);
 };
 
-// Shared memory of the TMA-staged FP32 tile: the state tile as the tensor copy lands it (rows
-// of TJ + 8 values from column j0 - 4, so that each copy starts on a 16-byte boundary), the
-// qmetric tile, the i-face records' first TMA_FIELDS fields (each face's fluxes later overwrite
-// the first five fields of its own record), the j-face fluxes.
+// Shared memory of the TMA-staged tile (FP32 or FP64): the state tile as the tensor copy lands
+// it (rows of TJ + 8 values from column j0 - 4, so that each copy starts on a 16-byte
+// boundary), the qmetric tile, the i-face records' first TMA_FIELDS fields (each face's fluxes
+// later overwrite the first five fields of its own record), the j-face fluxes.
 constexpr int TMA_FIELDS = 12;  // F_NX..F_SR: the fields the face phase reads
-template <int TI, int TJ> struct StageSmemTma {
+template <int TI, int TJ, class C = float> struct StageSmemTma {
   static constexpr int QI = TI + 4, QJ = TJ + 8;
   static constexpr size_t q_elems = size_t(4) * QI * QJ;
   static constexpr size_t m_elems = size_t(8) * (TI + 2) * (TJ + 2);
   static constexpr size_t ri_elems = size_t(TMA_FIELDS) * (TI + 1) * TJ;
   static constexpr size_t fj_elems = size_t(5) * TI * (TJ + 1);
-  static constexpr size_t ri_offset = (q_elems + m_elems) * sizeof(float);
-  static constexpr size_t bytes = (q_elems + m_elems + ri_elems + fj_elems) * sizeof(float);
+  static constexpr size_t ri_offset = (q_elems + m_elems) * sizeof(C);
+  static constexpr size_t bytes = (q_elems + m_elems + ri_elems + fj_elems) * sizeof(C);
   static_assert(ri_offset % 128 == 0, "the i-face records' tensor copy lands on a 128-byte boundary");
 };
 
@@ -246,7 +246,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
                                            uint64_t* bars = nullptr) {
   constexpr bool same = std::is_same<C, R>::value;
   using SM = StageSmem<TI, TJ, C>;
-  static_assert(!TMA || std::is_same<C, float>::value, "the TMA-staged tile is the FP32 one");
+  static_assert(!TMA || std::is_same<C, R>::value, "the TMA-staged tile computes in its storage type");
   constexpr int QJT = TMA ? TJ + 8 : SM::QJ;  // row length of the state tile in shared memory
   constexpr int QSH = TMA ? 2 : 0;            // its column shift (the halo's column 0 at QSH)
   C* sq = reinterpret_cast<C*>(smem_raw);
@@ -269,7 +269,8 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   // A tile whose halo lies inside the mesh needs no wrap, bounds or pair-face tests in
   // phases 1-2 (uniform per block).  FP32 only: the FP64 stage is bound by its FP64 pipe
   // and gains nothing from fewer integer instructions.  Same sums in the same order.
-  const bool interior = std::is_same<C, float>::value && i0 >= 2 && i0 + TI + 2 <= ni && j0 >= 2 && j0 + TJ + 2 <= nj;
+  const bool interior =
+      (std::is_same<C, float>::value || TMA) && i0 >= 2 && i0 + TI + 2 <= ni && j0 >= 2 && j0 + TJ + 2 <= nj;
   // TMA: one thread arms the two barriers and issues the tensor copies -- the interior tile's
   // state (4 planes x (TI + 4) rows x (TJ + 8) columns from (i0 - 2, j0 - 4); columns past the
   // mesh read zeros and are never used) and the i-face records (TMA_FIELDS fields x (TI + 1)
@@ -727,14 +728,13 @@ __global__ void __launch_bounds__(NT, (StageResidency<R, C, NT>::value))
 // tiles and form the qmetric; the j-face records and the earlier stages' residuals stay
 // plain loads (the j-face planes' row pitch, (nj + 1) values, is not a multiple of 16 bytes).
 // The tensor maps are kernel parameters (encoded per launch by the launcher, hc_tma.h).
-template <int TI, int TJ, int FK, int LIM>
-__global__ void __launch_bounds__(TI * TJ, (StageResidency<float, float, TI * TJ>::value))
-    stage_kernel_tma(const StageArgs<float> a, const __grid_constant__ CUtensorMap tq,
+template <int TI, int TJ, class R, int FK, int LIM, int NT = TI * TJ>
+__global__ void __launch_bounds__(NT, (StageResidency<R, R, NT>::value))
+    stage_kernel_tma(const StageArgs<R> a, const __grid_constant__ CUtensorMap tq,
                      const __grid_constant__ CUtensorMap tfi) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + StageSmemTma<TI, TJ>::bytes);
-  stage_tile<TI, TJ, float, FK, float, false, true, TI * TJ, LIM, true>(a, blockIdx.y, blockIdx.x, smem_raw, &tq,
-                                                                          &tfi, bars);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + StageSmemTma<TI, TJ, R>::bytes);
+  stage_tile<TI, TJ, R, FK, R, false, true, NT, LIM, true>(a, blockIdx.y, blockIdx.x, smem_raw, &tq, &tfi, bars);
 }
 
 // the recording variant (a diagnostic, not on the stepping path): the same tile with

@@ -83,8 +83,8 @@ inline void tile_dims(int tile, int* ti, int* tj) {
     const dim3 grid((a.nj + 31) / 32, (a.ni + 7) / 8);                                                   \
     CUtensorMap tq, tfi;                                                                                 \
     if (stage_tma_maps(a, &tq, &tfi)) {                                                                  \
-      stage_kernel_tma<8, 32, FK, LIM>                                                                   \
-          <<<grid, 256, StageSmemTma<8, 32>::bytes + 2 * sizeof(uint64_t), s>>>(a, tq, tfi);             \
+      stage_kernel_tma<8, 32, float, FK, LIM, 256>                                                       \
+          <<<grid, 256, StageSmemTma<8, 32, float>::bytes + 2 * sizeof(uint64_t), s>>>(a, tq, tfi);      \
       return;                                                                                            \
     }                                                                                                    \
     stage_kernel<8, 32, float, FK, float, 256, LIM><<<grid, 256, StageSmem<8, 32, float>::bytes, s>>>(a); \
