@@ -211,8 +211,9 @@ __device__ __forceinline__ void adj_face_one(const AdjArgs<R>& a, int dir, int f
     C qi[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) qi[v] = a.q[v * n + ci];
-    C* dI = int_right ? dR : dL;
-    C* gI = int_right ? gR : gL;
+    // the interior side's adjoints, moved to its slots of res at the end (a pointer chosen
+    // at run time into res would put the whole array in local memory)
+    C dI[4] = {C(0), C(0), C(0), C(0)}, gI[4] = {C(0), C(0), C(0), C(0)};
     if (bct == BC_WALL) {
       C Fb[4];
 #pragma unroll
@@ -286,6 +287,13 @@ __device__ __forceinline__ void adj_face_one(const AdjArgs<R>& a, int dir, int f
 #pragma unroll
         for (int v = 0; v < 4; ++v) a.refbar[side][size_t(v) * nfs + kf] += rb[v];
       }
+    }
+    if (int_right) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) { dR[v] = dI[v]; gR[v] = gI[v]; }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) { dL[v] = dI[v]; gL[v] = gI[v]; }
     }
   }
 #pragma unroll
@@ -408,8 +416,7 @@ template <class R, int FK> __device__ __forceinline__ void adj_face_scalar_one(c
     const int ci = idir ? (int_right ? 0 : ni - 1) * nj + j : i * nj + (int_right ? 0 : nj - 1);
     const int kf = idir ? j : i;
     const int nfs = idir ? nj : ni;
-    R* dI = int_right ? dR : dL;
-    R* gI = int_right ? gR : gL;
+    R dI[3] = {R(0), R(0), R(0)}, gI[3] = {R(0), R(0), R(0)};  // moved to res at the end
     R Fb[3], qi[3], qg[3], qref[3];
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
@@ -464,6 +471,13 @@ template <class R, int FK> __device__ __forceinline__ void adj_face_scalar_one(c
     for (int v = 0; v < 3; ++v) {
       if (ghost_is_ref) a.refbar[side][size_t(v) * nfs + kf] += gb_ref[v];
       else dI[v] += gb_ref[v];
+    }
+    if (int_right) {
+#pragma unroll
+      for (int v = 0; v < 3; ++v) { dR[v] = dI[v]; gR[v] = gI[v]; }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 3; ++v) { dL[v] = dI[v]; gL[v] = gI[v]; }
     }
   }
 #pragma unroll
