@@ -824,22 +824,18 @@ def run_gpu(args):
             "kernel": "stage_kernel<16,16,double,ROE,128 threads>", "alg_bytes_per_launch": alg_bytes,
             "avg_launch_ms": stage_ms}
 
-    # end to end through the C ABI with host buffers: upload the state from
-    # pinned host memory, one RK step, download the state, every step
+    # end to end through the C ABI with host buffers (hc_step_host): every step uploads the
+    # state from pinned host memory, runs one RK step and downloads the result
     host_in = torch.from_numpy(np.ascontiguousarray(s.get_state())).pin_memory()
     host_out = torch.empty_like(host_in).pin_memory()
     in_np, out_np = host_in.numpy(), host_out.numpy()
     ke = max(3, min(args.steps, 20))
     for _ in range(2):
-        s.set_state(in_np)
-        s.step(1)
-        s.get_state(out=out_np)
+        s.step_host(in_np, out_np)
     barrier()
     t0 = time.perf_counter()
     for _ in range(ke):
-        s.set_state(in_np)
-        s.step(1)
-        s.get_state(out=out_np)
+        s.step_host(in_np, out_np)
     barrier()
     el = time.perf_counter() - t0
     tt = torch.tensor([el], dtype=torch.float64, device="cuda")

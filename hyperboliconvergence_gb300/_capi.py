@@ -79,6 +79,7 @@ def _declare(lib):
         "hc_set_corrections": [p, C.c_uint],
         "hc_set_adjoint_tapes": [p, C.c_int],
         "hc_inject_stalled_copy": [p, C.c_int],
+        "hc_set_staged_loads": [p, C.c_int],
         "hc_set_time": [p, d],
         "hc_wall_force": [p, dp, dp],
         "hc_set_bcs": [p, C.POINTER(C.c_int), C.POINTER(dp)],
@@ -90,6 +91,7 @@ def _declare(lib):
         "hc_face_signatures": [p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), p, p],
         "hc_step": [p, i, C.POINTER(StepStats)],
         "hc_step_async": [p, i],
+        "hc_step_host": [p, i, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(StepStats)],
         "hc_sync": [p, C.POINTER(StepStats)],
         "hc_steady_run": [p, C.POINTER(SteadyControls), dp, C.c_longlong, C.POINTER(SteadyStats)],
         "hc_smooth_1d": [p, i, v, v, C.c_longlong, i, d, i],

@@ -719,6 +719,12 @@ int hc_set_corrections(hc_ctx* c, unsigned mask) {
   return HC_OK;
 }
 
+int hc_set_staged_loads(hc_ctx* c, int on) {
+  if (int st = check_ctx(c)) return st;
+  c->staged_loads = on ? 1 : 0;
+  return HC_OK;
+}
+
 int hc_inject_stalled_copy(hc_ctx* c, int on) {
   if (int st = check_ctx(c)) return st;
   c->stall_copy = on ? 1 : 0;
@@ -883,6 +889,33 @@ int hc_step_async(hc_ctx* c, int nsteps) {
     if (st != HC_OK) return st;
   }
   return HC_OK;
+}
+
+int hc_step_host(hc_ctx* c, int nsteps, const double* state_in, double* state_out, hc_step_stats* stats) {
+  if (int st = check_ctx(c)) return st;
+  if (!c->have_mesh) return fail(HC_ERR_ARG, "upload the mesh first");
+  if (!state_in || !state_out) return fail(HC_ERR_ARG, "null state");
+  const size_t m = size_t(c->nv) * c->ncell();
+  // upload, steps and download in stream order; read_stats waits once for all of them
+  if (c->fp32) {
+    HC_CUDA(cudaMemcpyAsync(c->staging, state_in, m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    d2r_kernel<float><<<1024, 256, 0, c->stream>>>(c->staging, (float*)c->q[0], m);
+    HC_CUDA(cudaGetLastError());
+    c->launches += 1;
+  } else {
+    HC_CUDA(cudaMemcpyAsync(c->q[0], state_in, m * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  }
+  c->have_state = true;
+  if (int st = hc_step_async(c, nsteps)) return st;
+  if (c->fp32) {
+    r2d_kernel<float><<<1024, 256, 0, c->stream>>>((const float*)c->q[0], c->staging, m);
+    HC_CUDA(cudaGetLastError());
+    c->launches += 1;
+    HC_CUDA(cudaMemcpyAsync(state_out, c->staging, m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    HC_CUDA(cudaMemcpyAsync(state_out, c->q[0], m * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  }
+  return read_stats(c, stats);
 }
 
 int hc_sync(hc_ctx* c, hc_step_stats* stats) {

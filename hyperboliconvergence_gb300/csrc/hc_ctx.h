@@ -24,6 +24,7 @@ struct hc_ctx {
   unsigned fixes = 0;                               // HC_FIX_* corrections (hc_set_corrections)
   int adj_tapes = -1;                               // adjoint stage tapes (hc_set_adjoint_tapes); -1 auto
   int stall_copy = 0;                               // test hook (hc_inject_stalled_copy)
+  int staged_loads = 1;                             // TMA-staged FP32 tile loads (hc_set_staged_loads)
   // the forward sweep recorded by hc_adjoint_record for hc_adjoint_reverse (owned here,
   // released by the reverse sweep, the next record, a mesh upload or destroy)
   void* adj_tape = nullptr;
@@ -86,6 +87,7 @@ template <class R> StageArgs<R> base_args(hc_ctx* c) {
   a.info = c->info;
   a.cfl = R(c->cfg.cfl);
   a.stall_copy = c->stall_copy;
+  a.plain_loads = c->staged_loads ? 0 : 1;
   return a;
 }
 

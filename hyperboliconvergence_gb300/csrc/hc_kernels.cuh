@@ -74,6 +74,7 @@ template <class R> struct StageArgs {
   R dual_g0, dual_b0dt;
   int stall_copy;  // test hook (hc_inject_stalled_copy): the TMA-staged tile's records barrier
                    // expects 16 bytes its copy never delivers, so the bounded wait runs out
+  int plain_loads; // host side: 1 keeps the FP32 launch on the plain-load kernel (hc_set_staged_loads)
 };
 
 // Branch signature of one face (recording kernels): bits 0-15 the limiter pieces of
@@ -841,6 +842,7 @@ template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const B
   a.dual_g0 = R(1);
   a.dual_b0dt = R(0);
   a.stall_copy = 0;
+  a.plain_loads = 0;
   const long long n = (long long)in.ni * in.nj;
   const long long off4 = 4 * in.cell, off5 = 5 * in.cell;
   a.q = b.q + off4;

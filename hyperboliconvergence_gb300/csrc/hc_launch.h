@@ -82,7 +82,7 @@ inline void tile_dims(int tile, int* ti, int* tj) {
   template <int LIM> static void go_lim(const StageArgs<float>& a, cudaStream_t s) {                     \
     const dim3 grid((a.nj + 31) / 32, (a.ni + 7) / 8);                                                   \
     CUtensorMap tq, tfi;                                                                                 \
-    if (stage_tma_maps(a, &tq, &tfi)) {                                                                  \
+    if (!a.plain_loads && stage_tma_maps(a, &tq, &tfi)) {                                                \
       stage_kernel_tma<8, 32, float, FK, LIM, 256>                                                       \
           <<<grid, 256, StageSmemTma<8, 32, float>::bytes + 2 * sizeof(uint64_t), s>>>(a, tq, tfi);      \
       return;                                                                                            \

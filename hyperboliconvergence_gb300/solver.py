@@ -142,6 +142,11 @@ class Solver:
         self.corrections = _capi.fix_mask(corrections)
         check(self.lib.hc_set_corrections(self.h, self.corrections))
 
+    def set_staged_loads(self, on: bool = True) -> None:
+        """The FP32 stage's tile loads staged by TMA tensor copies (the default) or plain
+        per-thread loads (hc_set_staged_loads); bit-identical results."""
+        check(self.lib.hc_set_staged_loads(self.h, 1 if on else 0))
+
     def inject_stalled_copy(self, on: bool = True) -> None:
         """Test hook of the failure detection (hc_inject_stalled_copy): the TMA-staged FP32
         stage kernel's copy barrier waits for bytes that never come, its bounded wait runs out
@@ -348,6 +353,19 @@ class Solver:
     def step(self, n: int = 1) -> StepStats:
         st = StepStats()
         check(self.lib.hc_step(self.h, int(n), C.byref(st)))
+        self.steps_done += int(n)
+        self.last = st
+        return st
+
+    def step_host(self, state_in: np.ndarray, state_out: np.ndarray, n: int = 1) -> StepStats:
+        """n steps of a host state (hc_step_host): state_in uploaded, stepped, the result
+        written to state_out (C-contiguous float64 arrays of the state's shape; page-locked
+        memory lets the copies run asynchronously), one synchronisation."""
+        for a in (state_in, state_out):
+            if a.shape != self._shape or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"states must be C-contiguous float64 arrays of shape {self._shape}")
+        st = StepStats()
+        check(self.lib.hc_step_host(self.h, int(n), _dptr(state_in), _dptr(state_out), C.byref(st)))
         self.steps_done += int(n)
         self.last = st
         return st

@@ -181,6 +181,12 @@ int hc_step(hc_ctx* ctx, int nsteps, hc_step_stats* stats);
 int hc_set_time(hc_ctx* ctx, double t);
 /* Enqueue nsteps without waiting; hc_sync waits and reports. */
 int hc_step_async(hc_ctx* ctx, int nsteps);
+/* nsteps RK steps of a host-resident field, the way integrate() advances the caller's
+ * SolutionField in place (timestepping/rungeKutta.h:37-51): state_in (the solution basis's
+ * planes, as hc_state_upload takes them) is copied to the device, stepped, and the result
+ * copied to state_out (which may be state_in), with one synchronisation at the end; page-
+ * locked host buffers let both copies run asynchronously.  stats as hc_step reports them. */
+int hc_step_host(hc_ctx* ctx, int nsteps, const double* state_in, double* state_out, hc_step_stats* stats);
 int hc_sync(hc_ctx* ctx, hc_step_stats* stats);
 
 /* SteadyTimeControls (controls.h:31-48), which the reference declares but no driver
@@ -378,6 +384,11 @@ int hc_adjoint_record(hc_ctx* ctx, int nsteps, int snapshots, const hc_objective
  * states the only storage); k: at most k live at once.  Each tape holds nst states of the
  * mesh, allocated at record time.  Not in the reference (no adjoint). */
 int hc_set_adjoint_tapes(hc_ctx* ctx, int ntapes);
+
+/* The FP32 stage's tile loads staged by TMA tensor copies (on, the default, where the mesh's
+ * rows are a multiple of 16 bytes) or plain per-thread loads (0): the same results bit for
+ * bit, for comparison.  No counterpart in the reference. */
+int hc_set_staged_loads(hc_ctx* ctx, int on);
 
 /* Test hook of the failure detection (no counterpart in the reference): with on != 0 the
  * FP32 stage kernel whose loads are staged by TMA tensor copies (8x32 tiles, the common
