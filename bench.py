@@ -472,6 +472,52 @@ def measure_steady(stream, steps: int = 2000, fluxes=("roe_face", "slau", "ausmp
     return out
 
 
+def measure_steady_full(stream, max_steps: int = 300000, mach: float = 0.3):
+    """Configuration 2 run to convergence on its full 512 x 1024 O-grid (opt-in:
+    `--steady-full`, minutes of FP64 time): face-frame Roe, unlimited reconstruction
+    (NoLimit2; van Albada stalls near a 1e-4 drop), ssp34 with local timestepping at CFL 1.5,
+    the corrections, M 0.3, from the uniform freestream until the density residual fell by
+    1e-10 (cap `max_steps`); then FP32 with the same settings for as many steps, and its
+    difference from the FP64 converged state (per variable, relative to its largest
+    magnitude).  Reported: steps, drop, the residual history, C_d and C_l, times."""
+    import torch
+    from hyperboliconvergence_gb300 import cases
+    from hyperboliconvergence_gb300.solver import Solver
+    g = 1.4
+
+    def cons(w):
+        u, v, r, p = w
+        return np.stack([r * u, r * v, r, p / (g - 1) + 0.5 * r * (u * u + v * v)])
+
+    kw = dict(flux="roe_face", limiter="nolimit2", rk="ssp34", dt="local", cfl=1.5, corrections="all")
+    out = {"workload": f"cylinder O-grid {NR}x{NTH}, M{mach}, " + ", ".join(f"{k} {v}" for k, v in kw.items())}
+    states = {}
+    nsteps = max_steps
+    for prec in ("fp64", "fp32"):
+        mesh, bc, ref, q, species = cases.cylinder(NR, NTH, mach=mach)
+        s = Solver(mesh, bc, ref, precision=prec, species=species, stream=stream.cuda_stream, **kw)
+        s.set_state(q)
+        e0, e1 = _events()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        st, hist = s.steady(nsteps, residual_drop=1e-10, check_every=5000)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        qd = 0.5 * mach * mach
+        out[prec] = {"steps": int(st.steps), "residual_drop": float(st.res / st.res0),
+                     "converged_1e-10": bool(st.converged), "seconds": e0.elapsed_time(e1) / 1e3,
+                     "history_every_5000_steps": [float(h) for h in np.asarray(hist).ravel()[:80]],
+                     "cd": s.wall_force((1.0, 0.0)) / qd, "cl": s.wall_force((0.0, 1.0)) / qd}
+        states[prec] = cons(s.get_state())
+        s.close()
+        nsteps = int(st.steps)  # FP32: as many steps as FP64 took
+    d = np.abs(states["fp32"] - states["fp64"]).reshape(4, -1)
+    scale = np.abs(states["fp64"]).reshape(4, -1).max(1)
+    out["fp32_vs_fp64_converged"] = {"rel_linf": float((d.max(1) / scale).max()),
+                                     "rel_mean": float((d.mean(1) / scale).max())}
+    return out
+
+
 def measure_developed(stream, steps: int = 10):
     """The headline workload (FP64) started from a state that is non-uniform
     everywhere -- the freestream times 1 + 1% of a smooth field of r and theta --
@@ -762,6 +808,18 @@ def run_adjoint_only(args):
     return 0
 
 
+def run_steady_full(args):
+    """`--steady-full`: configuration 2 converged on its full grid (measure_steady_full);
+    prints one JSON line with that measurement and no headline."""
+    import torch
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        out = measure_steady_full(stream, max_steps=args.steady_full_cap)
+    print(json.dumps({"steady_full": True, "steady": out}), flush=True)
+    return 0
+
+
 def run_gpu(args):
     import torch
 
@@ -770,6 +828,8 @@ def run_gpu(args):
 
     if args.adjoint_only:
         return run_adjoint_only(args)
+    if args.steady_full:
+        return run_steady_full(args)
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
     pg = None
@@ -902,6 +962,9 @@ def main():
     ap.add_argument("--adjoint-snapshots", type=int, default=20, help="checkpoints of the adjoint measurement")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run only the FP64 adjoint measurement (no headline line), for profiling its kernels")
+    ap.add_argument("--steady-full", action="store_true",
+                    help="run only configuration 2 to a 1e-10 residual drop on its full grid (minutes; no headline)")
+    ap.add_argument("--steady-full-cap", type=int, default=300000, help="step cap of --steady-full")
     ap.add_argument("--steady-steps", type=int, default=2000,
                     help="step cap of each run of the steady O-grid extra (residual drop target 1e-10)")
     ap.add_argument("--no-extras", action="store_true",
