@@ -375,10 +375,9 @@ hc_step_stats integrate(const execution::gpu_policy policy, const UnsteadyTimeCo
     refs[s] = q.boundary[s].data();
   }
   check(hc_set_bcs(ctx.get(), bct, refs));
-  check(hc_state_upload(ctx.get(), q.interior.data()));
+  // the caller's field advanced in place: upload, steps, download, one wait
   hc_step_stats st{};
-  check(hc_step(ctx.get(), int(timeControls.nTimesteps), &st));
-  check(hc_state_download(ctx.get(), q.interior.data()));
+  check(hc_step_host(ctx.get(), int(timeControls.nTimesteps), q.interior.data(), q.interior.data(), &st));
   return st;
 }
 

@@ -355,13 +355,14 @@ template <class R> int adjoint_step(Adj<R>& A, int step) {
   // output q_{step+1} is the start state of the step reversed before this one, kept in qnext)
   if (int st = stage_states(A, step)) return st;
   const size_t bytes4 = A.state_values() * sizeof(R);
-  HC_CUDA(cudaMemcpyAsync(A.sq[A.nst], A.qnext, bytes4, cudaMemcpyDeviceToDevice, A.s()));
-  HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], bytes4, cudaMemcpyDeviceToDevice, A.s()));
-  for (int k = 0; k < A.nst; ++k) HC_CUDA(cudaMemsetAsync(A.rbar[k], 0, bytes4, A.s()));
-  HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
+  // q_{step+1} into sq[nst] by exchange with qnext; qnext takes q_step (sq[0]) the same way
+  // when the step is done
+  std::swap(A.sq[A.nst], A.qnext);
   const double dt = step_dt(A, step);
   const Gas<R> g = with_fixes(make_gas<R>(A.c->gamma, A.c->Rgas, A.c->minf), A.c->fixes);
   if (A.c->scalar) {
+    for (int k = 0; k < A.nst; ++k) HC_CUDA(cudaMemsetAsync(A.rbar[k], 0, bytes4, A.s()));
+    HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
     for (int s = A.nst - 1; s >= 0; --s) {
       const R* qbar_out = (s == A.nst - 1) ? A.lam : A.qbs;
       R al[4] = {R(0), R(0), R(0), R(0)};
@@ -374,6 +375,7 @@ template <class R> int adjoint_step(Adj<R>& A, int step) {
       if (int st = res_adj_scalar<R>(A, A.sq[s], A.rbar[s], s == 0 ? A.q0bar : nullptr, A.qbs)) return st;
     }
     HC_CUDA(cudaMemcpyAsync(A.lam, A.qbs, bytes4, cudaMemcpyDeviceToDevice, A.s()));
+    std::swap(A.qnext, A.sq[0]);
     A.adj_steps += 1;
     return HC_OK;
   }
@@ -399,6 +401,7 @@ template <class R> int adjoint_step(Adj<R>& A, int step) {
     AdjCellArgs<R> u{};
     u.qbar_in = A.lam;
     update(u, A.nst - 1);
+    u.first = 1;  // q0bar and every rbar_k written, not accumulated: no zeroing
     u.qm_q = A.sq[A.nst - 1];
     adj_cell_kernel<R><<<cb, 256, 0, A.s()>>>(a, u);
     A.launches += 1;
@@ -422,6 +425,7 @@ template <class R> int adjoint_step(Adj<R>& A, int step) {
     A.launches += 2;
     HC_CUDA(cudaGetLastError());
   }
+  std::swap(A.qnext, A.sq[0]);
   A.adj_steps += 1;
   return HC_OK;
 }

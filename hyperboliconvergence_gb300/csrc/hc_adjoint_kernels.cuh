@@ -604,26 +604,37 @@ template <class R, int NV = 4> __global__ void adj_gather_kernel(const AdjArgs<R
 }
 
 // Reverse of one stage update q_out = prim(cons(q0) + (sum_k alpha_k R_k) * fac),
-// fac = beta*dt/V frozen, at cell c: qb (the adjoint of q_out) -> q0bar and rbar_k (both
-// accumulated, k <= stage)
+// fac = beta*dt/V frozen, at cell c: qb (the adjoint of q_out) -> q0bar and rbar_k (k <=
+// stage), accumulated, or (first: the step's last stage, the first update reversed)
+// written, which spares zeroing them
 template <class R>
 __device__ __forceinline__ void adj_update_apply(const Gas<R>& g, const R* __restrict__ q_out,
                                                  const R* __restrict__ q0, const R* __restrict__ vol, const R* qb,
                                                  R* __restrict__ q0bar, R* const* rbar, const R* alpha, int stage,
-                                                 R dts, size_t n, int c) {
+                                                 R dts, size_t n, int c, bool first) {
   R q[4], qz[4], cb[4], z[4] = {R(0), R(0), R(0), R(0)};
 #pragma unroll
   for (int v = 0; v < 4; ++v) { q[v] = q_out[v * n + c]; qz[v] = q0[v * n + c]; }
   cons2prim_adj(g, q, qb, cb);
   prim2cons_adj(g, qz, cb, z);
-#pragma unroll
-  for (int v = 0; v < 4; ++v) q0bar[v * n + c] += z[v];
   const R fac = dts / vol[c];
+  if (first) {
 #pragma unroll
-  for (int k = 0; k < 4; ++k)
-    if (k <= stage)
+    for (int v = 0; v < 4; ++v) q0bar[v * n + c] = z[v];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) rbar[k][v * n + c] += alpha[k] * cb[v] * fac;
+    for (int k = 0; k < 4; ++k)
+      if (k <= stage)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) rbar[k][v * n + c] = alpha[k] * cb[v] * fac;
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) q0bar[v * n + c] += z[v];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (k <= stage)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) rbar[k][v * n + c] += alpha[k] * cb[v] * fac;
+  }
 }
 
 // ---- the drag objective's adjoint
@@ -708,6 +719,7 @@ template <class R> __device__ __forceinline__ R drag_cell(const AdjArgs<R>& a, i
 // so that a stage's reverse is three launches: faces, qmetric adjoint, this pass.
 template <class R> struct AdjCellArgs {
   int gather, drag, update;
+  int first;  // the step's first update reversed: writes q0bar and the rbar_k instead of adding
   const R* qbar_in;
   R* qbar_out;
   Gas<R> g;
@@ -734,7 +746,7 @@ template <class R> __device__ __forceinline__ void adj_cell_body(const AdjArgs<R
   }
   if (u.drag) qb[3] += drag_cell(a, c);
   if (u.update) {
-    adj_update_apply(u.g, u.q_out, u.q0, u.vol, qb, u.q0bar, u.rbar, u.alpha, u.stage, u.dts, n, c);
+    adj_update_apply(u.g, u.q_out, u.q0, u.vol, qb, u.q0bar, u.rbar, u.alpha, u.stage, u.dts, n, c, u.first != 0);
   } else {
 #pragma unroll
     for (int v = 0; v < 4; ++v) u.qbar_out[v * n + c] = qb[v];

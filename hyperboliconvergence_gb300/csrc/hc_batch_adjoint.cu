@@ -168,11 +168,12 @@ template <class R> int adjoint_step(BAdj<R>& A, int step) {
   // is the start state of the step reversed before, qnext)
   if (int st = stage_states(A, step)) return st;
   const size_t bytes4 = A.state_values() * sizeof(R);
-  HC_CUDA(cudaMemcpyAsync(A.sq[A.nst], A.qnext, bytes4, cudaMemcpyDeviceToDevice, A.s()));
-  HC_CUDA(cudaMemcpyAsync(A.qnext, A.sq[0], bytes4, cudaMemcpyDeviceToDevice, A.s()));
+  // q_{step+1} into sq[nst] by exchange with qnext; qnext takes q_step (sq[0]) the same way
+  // when the step is done
+  std::swap(A.sq[A.nst], A.qnext);
+  if (!A.b->scalar) return adjoint_step_euler(A, step);
   for (int k = 0; k < A.nst; ++k) HC_CUDA(cudaMemsetAsync(A.rbar[k], 0, bytes4, A.s()));
   HC_CUDA(cudaMemsetAsync(A.q0bar, 0, bytes4, A.s()));
-  if (!A.b->scalar) return adjoint_step_euler(A, step);
   for (int s = A.nst - 1; s >= 0; --s) {
     AdjUpdateBatch<R> u{};
     u.inst = A.b->inst_d;
@@ -198,6 +199,7 @@ template <class R> int adjoint_step(BAdj<R>& A, int step) {
     if (int st = res_adj<R>(A, A.sq[s], A.rbar[s], s == 0 ? A.q0bar : nullptr, A.qbs)) return st;
   }
   HC_CUDA(cudaMemcpyAsync(A.lam, A.qbs, bytes4, cudaMemcpyDeviceToDevice, A.s()));
+  std::swap(A.qnext, A.sq[0]);
   A.adj_steps += 1;
   return HC_OK;
 }
@@ -230,6 +232,7 @@ template <class R> int adjoint_step_euler(BAdj<R>& A, int step) {
     AdjCellBatch<R> w = ub;
     w.u.qbar_in = A.lam;
     update(w, A.nst - 1);
+    w.u.first = 1;  // q0bar and every rbar_k written, not accumulated: no zeroing
     w.u.qm_q = A.sq[A.nst - 1];
     adj_cell_batch_kernel<R><<<A.blocks_c, 256, 0, A.s()>>>(a, w);
     A.launches += 1;
@@ -260,6 +263,7 @@ template <class R> int adjoint_step_euler(BAdj<R>& A, int step) {
     A.launches += 3;
     HC_CUDA(cudaGetLastError());
   }
+  std::swap(A.qnext, A.sq[0]);
   A.adj_steps += 1;
   return HC_OK;
 }
