@@ -774,6 +774,18 @@ def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int =
                                        "speedup": single_ms / sub_ms}}
 
 
+def job_rate(pg, ms: float, world: int, units_per_rank: float, device: str = "cuda"):
+    """Whole-job throughput of a replicas-only run: every rank processed units_per_rank in
+    its own ms; the job took the slowest rank's time (the max over ranks), in which all
+    world x units_per_rank were processed.  Returns (units per second, max ms)."""
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    if pg is not None:
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    ms = float(t.item())
+    return world * units_per_rank / (ms / 1e3), ms
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -864,13 +876,8 @@ def run_gpu(args):
         barrier()
     st = s.sync()
     launches = st.kernel_launches - launches0
-    ms = ev0.elapsed_time(ev1)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if pg is not None:
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-    ms = float(t.item())
+    value, ms = job_rate(pg, ev0.elapsed_time(ev1), world, ncell * args.steps)
     ms_per_step = ms / args.steps
-    value = world * ncell * args.steps / (ms / 1e3)
 
     # roofline of the dominant kernel (the fused stage kernel; the timed region
     # holds only stage kernels and two 8-byte memsets per step)
@@ -897,11 +904,8 @@ def run_gpu(args):
     for _ in range(ke):
         s.step_host(in_np, out_np)
     barrier()
-    el = time.perf_counter() - t0
-    tt = torch.tensor([el], dtype=torch.float64, device="cuda")
-    if pg is not None:
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-    e2e = {"value": world * ncell * ke / float(tt.item()), "unit": UNIT,
+    e2e_value, _ = job_rate(pg, (time.perf_counter() - t0) * 1e3, world, ncell * ke)
+    e2e = {"value": e2e_value, "unit": UNIT,
            "h2d_bytes_per_step": int(host_in.numel() * 8), "d2h_bytes_per_step": int(host_out.numel() * 8),
            "steps": ke}
 
