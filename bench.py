@@ -368,10 +368,12 @@ def measure_vortex(stream):
         u, v, r, p = w
         return np.stack([r * u, r * v, r, p / (g - 1) + 0.5 * r * (u * u + v * v)])
 
-    def run(n, steps, flux, timed=False):
+    states = {}
+
+    def run(n, steps, flux, timed=False, precision="fp64"):
         mesh, bc, ref, q, sp = cases.isentropic_vortex(n)
         s = Solver(mesh, bc, ref, flux=flux, limiter="vanleer", rk="ssp34", dt="global", cfl=0.5, species=sp,
-                   stream=stream.cuda_stream)
+                   stream=stream.cuda_stream, precision=precision)
         s.set_state(q)
         res = {}
         try:
@@ -393,6 +395,7 @@ def measure_vortex(stream):
             s.close()
             return {"error": str(exc)}
         c = mesh.centres()
+        states[(n, flux, precision)] = cons(s.get_state())
         e = np.abs(cons(s.get_state()) - cons(cases.vortex_state(c[0], c[1], 4.0 * st.t)))
         res.update(t_physical=4.0 * st.t, l1=[float(x) for x in e.reshape(4, -1).mean(1)],
                    linf=[float(x) for x in e.reshape(4, -1).max(1)])
@@ -409,6 +412,14 @@ def measure_vortex(stream):
                           "linf": [float(np.log2(x / y)) for x, y in zip(conv[a]["linf"], conv[b]["linf"])]}
             for a, b in ((64, 128), (128, 256))}
     out["reference_roe_256"] = ref256
+    # FP32: the same 100 steps, against the FP64 run (per variable, relative to its largest magnitude)
+    out["fp32_face_frame"] = run(128, 100, "roe_face", timed=True, precision="fp32")
+    a, b = states.get((128, "roe_face", "fp32")), states.get((128, "roe_face", "fp64"))
+    if a is not None and b is not None:
+        d = np.abs(a - b).reshape(4, -1)
+        scale = np.abs(b).reshape(4, -1).max(1)
+        out["fp32_vs_fp64_after_100_steps"] = {"rel_linf": float((d.max(1) / scale).max()),
+                                               "rel_mean": float((d.mean(1) / scale).max())}
     return out
 
 
