@@ -233,6 +233,27 @@ def measure_precision(stream, steps: int, prec: str):
             out = {"value": cells / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
                    "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                                 "frac": ach / peak, "alg_bytes_per_cell_stage": 14 * esz}}
+            # the step's buffers (3 states, 4 stage residuals, the face records, volumes): in
+            # FP32 about the size of L2, so the back-to-back steps above reuse what L2 holds;
+            # the same steps again, each after a write of twice L2's size, time them cold
+            ws = (3 * 4 + 4 * 5 + 2 * 14 + 1) * esz * cells / 2 ** 20
+            flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+            cold = 0.0
+            for _ in range(steps):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                e0, e1 = _events()
+                e0.record(stream)
+                s.step_async(1)
+                e1.record(stream)
+                s.sync()
+                torch.cuda.synchronize()
+                cold += e0.elapsed_time(e1)
+            del flush
+            out["l2"] = (f"back-to-back steps, no flush: the step's buffers take {ws:.0f} MiB against "
+                         f"{L2_BYTES / 2 ** 20:.0f} MiB of L2")
+            out["l2_flushed"] = {"value": cells / (cold / steps / 1e3), "unit": UNIT, "ms_per_step": cold / steps,
+                                 "how": "L2 flushed (a write of twice its size) before each timed step"}
         s.set_state(q)
         s.step(1)
         one = s.get_state()

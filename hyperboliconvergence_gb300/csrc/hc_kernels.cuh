@@ -325,7 +325,35 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
   __syncthreads();
 
   auto Q = [&](int v, int la, int lb) -> C { return sq[(v * QI + la + 2) * QJT + lb + 2 + QSH]; };  // tile coords
-  auto M = [&](int k, int la, int lb) -> C& { return sm[(k * MI + la + 1) * MJ + lb + 1]; };
+  // the qmetric tile: FP32 keeps a cell's eight values as two float4 (the gradients of
+  // variables 0-1, then 2-3), so that a face reads a cell's eight in two vector loads;
+  // the other types keep one plane per value
+  constexpr bool MV = std::is_same<C, float>::value;
+  auto M = [&](int k, int la, int lb) -> C& {
+    const int c = (la + 1) * MJ + lb + 1;
+    return MV ? sm[((k >> 2) * MI * MJ + c) * 4 + (k & 3)] : sm[k * MI * MJ + c];
+  };
+  auto mload = [&](int la, int lb, C* m) {
+    if constexpr (MV) {
+      const float4* p = reinterpret_cast<const float4*>(sm) + (la + 1) * MJ + lb + 1;
+      const float4 x = p[0], y = p[MI * MJ];
+      m[0] = x.x; m[1] = x.y; m[2] = x.z; m[3] = x.w;
+      m[4] = y.x; m[5] = y.y; m[6] = y.z; m[7] = y.w;
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) m[k] = M(k, la, lb);
+    }
+  };
+  auto mstore = [&](int la, int lb, const C* m) {
+    if constexpr (MV) {
+      float4* p = reinterpret_cast<float4*>(sm) + (la + 1) * MJ + lb + 1;
+      p[0] = make_float4(m[0], m[1], m[2], m[3]);
+      p[MI * MJ] = make_float4(m[4], m[5], m[6], m[7]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) M(k, la, lb) = m[k];
+    }
+  };
 
   // ---- phase 2: qmetric of the tile cells and of the 1-cell halo strips
   // (lsq/qmetric.ipp via spatial/lsqMetrics.h:181-213; D2 periodic wrap)
@@ -354,8 +382,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
           m[2 * v] += b1 * dxj1; m[2 * v + 1] += b1 * dyj1;
         }
       }
-#pragma unroll
-      for (int q = 0; q < 8; ++q) M(q, la, lb) = m[q];
+      mstore(la, lb, m);
     }
   } else
   for (int k = tid; k < MI * MJ; k += NT) {
@@ -399,8 +426,7 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
         }
       }
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) M(q, la, lb) = m[q];
+    mstore(la, lb, m);
   }
   if (tma) mbar_wait_bounded(&bars[1], a.info);
   __syncthreads();
@@ -474,12 +500,15 @@ __device__ __forceinline__ void stage_tile(const StageArgs<R>& a, int bi, int bj
               qR[v] = qr[v] - dr * sR[v];
             }
           } else {
+            C ml[8], mr[8];
+            mload(la_l, lb_l, ml);
+            mload(la, lb, mr);
 #pragma unroll
             for (int v = 0; v < 4; ++v) {
               const C dq = qr[v] - ql[v];
               const C gc = dq * idlr;
-              const C gl = (M(2 * v, la_l, lb_l) * wlx + M(2 * v + 1, la_l, lb_l) * wly) - dq * sl;
-              const C gr = (M(2 * v, la, lb) * wrx + M(2 * v + 1, la, lb) * wry) - dq * sr;
+              const C gl = (ml[2 * v] * wlx + ml[2 * v + 1] * wly) - dq * sl;
+              const C gr = (mr[2 * v] * wrx + mr[2 * v + 1] * wry) - dq * sr;
               qL[v] = ql[v] + dl * limit<C>(lim, gc, gl);
               qR[v] = qr[v] - dr * limit<C>(lim, gc, gr);
               if constexpr (REC) {
@@ -843,6 +872,7 @@ template <class R> __device__ __forceinline__ StageArgs<R> instance_args(const B
   a.dual_b0dt = R(0);
   a.stall_copy = 0;
   a.plain_loads = 0;
+  a.fic = a.fjc = nullptr;  // batches compute in their storage type
   const long long n = (long long)in.ni * in.nj;
   const long long off4 = 4 * in.cell, off5 = 5 * in.cell;
   a.q = b.q + off4;
