@@ -109,7 +109,8 @@ def fp64_peak_tflops(n: int = 4096, reps: int = 5):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 20 ms while the context is
+    open (the bench opens it before the warm-up and closes it after the timed region)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -124,11 +125,20 @@ class ClockSampler:
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
+
+    def wait_first(self, timeout_s: float = 3.0):
+        """Block until the sampler has written its first sample (nvidia-smi takes a moment
+        to start), at most timeout_s, so that the samples cover what follows."""
+        t0 = time.perf_counter()
+        while self.proc is not None and time.perf_counter() - t0 < timeout_s:
+            if os.path.exists(self.path) and os.path.getsize(self.path) > 0:
+                return
+            time.sleep(0.01)
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -159,7 +169,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
-                "reasons": sorted(reasons)}
+                "reasons": sorted(reasons), "window": "the warm-up and the timed region, 20 ms samples"}
 
 
 def cpu_baseline(sample_s: float = 4.0, samples: int = 3, threads: int | None = None):
@@ -894,13 +904,16 @@ def run_gpu(args):
             pg.barrier()
         torch.cuda.synchronize()
 
-    # warm-up
-    s.step_async(max(3, args.warmup))
-    s.sync()
-    barrier()
-    launches0 = s.sync().kernel_launches
+    # the clock sampler runs from before the warm-up to the end of the timed region (20 ms
+    # samples; its first sample is waited for, so that the samples cover both)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        clk.wait_first()
+        # warm-up
+        s.step_async(max(3, args.warmup))
+        s.sync()
+        barrier()
+        launches0 = s.sync().kernel_launches
         barrier()
         ev0.record(stream)
         s.step_async(args.steps)
