@@ -707,7 +707,7 @@ def measure_adjoint(nsteps: int = 400, snapshots: int = 20, precisions=("fp64", 
 
 
 def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int = 20, seed: int = 2027,
-                            compare: int = 8, law: str = "euler"):
+                            compare: int = 8, law: str = "euler", budget: int = 50):
     """Batched and differentiated case: `ninst` periodic instances on [0,1]^2, n x n
     cells with n drawn from {128, 192, ..., 1024}.  Euler: density = 5 plus 8 seeded
     Gaussians (widths 0.02..0.2, amplitudes -0.5..0.5) on u = 0.5, v = 0.25, p = 1;
@@ -718,7 +718,8 @@ def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int =
     `nsteps` steps against its own seeded target; gradient with respect to every
     instance's initial state in FP32 from one batched adjoint (hc_batch_adjoint_gradient:
     one persistent launch per forward stage and one launch per reverse pass over all
-    instances, `snapshots` checkpoints of the whole batch).  Checks: the smallest
+    instances, `snapshots` checkpoints of the whole batch; timed again with `budget`
+    checkpoints).  Checks: the smallest
     instance's FP32 gradient from the batch against its FP64 single-mesh gradient, and
     the first `compare` instances timed as single-mesh adjoints against the batched
     adjoint of the same instances."""
@@ -776,6 +777,17 @@ def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int =
           "grad_equal_one_call": bool(np.array_equal(q0s[kmin].grad.cpu().numpy(), grads[kmin]))}
     fn["backward_over_forward"] = fn["backward_ms"] / fn["forward_ms"]
     del q0s, tgs, Jt
+    # the same gradient with a larger checkpoint budget (the configuration names none; the
+    # single-mesh differentiated one names 20): fewer recomputed steps for more memory
+    state_gib = sum(n * n for n in sizes) * 4 * 4 / 2 ** 30
+    try:
+        _, _, stb = bt.gradient(nsteps, targets, snapshots=budget, want=[])
+        larger = {"snapshots": budget, "snapshot_gib": budget * state_gib, "forward_ms": stb.ms_forward,
+                  "reverse_ms": stb.ms_total - stb.ms_forward, "recompute_ms": stb.ms_recompute,
+                  "stage_tapes": int(stb.stage_tapes),
+                  "adjoint_step_over_forward_step": (stb.ms_total - stb.ms_forward) / stb.ms_forward}
+    except Exception as exc:  # reported beside the 20-checkpoint figures, which stand alone
+        larger = {"snapshots": budget, "error": f"{type(exc).__name__}: {exc}"}
     bt.close()
     if not np.all(np.isfinite(J)) or not np.all(np.isfinite(grads[kmin])):
         raise RuntimeError("non-finite objective or gradient")
@@ -807,6 +819,7 @@ def measure_batched_adjoint(ninst: int = 64, nsteps: int = 100, snapshots: int =
             "forward_cell_updates_per_s": cells * nsteps / (fwd_ms / 1e3),
             "adjoint_step_over_forward_step": rev_ms / fwd_ms,
             "replays": int(st.replays), "stage_tapes": int(st.stage_tapes),
+            "larger_checkpoint_budget": larger,
             "through_autograd_function": fn,
             "fp64_check": {"instance": kmin, "cells": sizes[kmin] ** 2,
                            "J_rel_diff": abs(float(J[kmin]) - j64) / abs(j64),
